@@ -1,0 +1,172 @@
+/*
+ * mpet_gpu.h - C ABI of libmpetgpu, the GB300 (sm_103a) assemble + solve
+ * engine for the backward-Euler / theta-scheme MPET block system of
+ * waterscapes' mpet.MPETSolver.
+ *
+ * The reference is pure Python on top of DOLFIN/PETSc; there is no native
+ * FFI in it.  Each entry point below replaces one native call that
+ * MPETSolver makes through DOLFIN or PETSc (file:line in the reference's
+ * src/mpet/mpet/ tree), so that a Python MPETSolver can keep its API and
+ * call this library through ctypes instead.
+ *
+ * Conventions
+ *  - Every function returns an int status: MPET_OK (0) or a negative
+ *    MPET_ERR_* code.  Nothing aborts or traps; the text of the last error
+ *    is available from mpet_last_error().
+ *  - Arrays named *_host are host memory.  All other array arguments are
+ *    device pointers (CUDA global memory on the context's device), e.g.
+ *    torch.Tensor.data_ptr() of a CUDA tensor.
+ *  - Work is ordered on the context's stream (mpet_set_stream; default:
+ *    a stream the context creates).  One context per host thread.
+ *  - Global DOF order ("block natural"): P2 nodes are the vertices
+ *    followed by the edges sorted by (low, high) vertex id; displacement
+ *    DOF (node i, component k) = 3*i + k; pressure DOF of network a at
+ *    vertex v = Nu + a*nv + v with Nu = 3*(nv + ne).
+ */
+#ifndef MPET_GPU_H
+#define MPET_GPU_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define MPET_OK 0
+#define MPET_ERR_INVALID (-1)   /* bad argument or size */
+#define MPET_ERR_NOMEM (-2)     /* device or host allocation failed */
+#define MPET_ERR_CUDA (-3)      /* CUDA runtime error */
+#define MPET_ERR_MAXIT (-4)     /* Krylov iteration limit reached */
+#define MPET_ERR_BREAKDOWN (-5) /* Krylov breakdown (indefinite preconditioner, NaN) */
+#define MPET_ERR_TIMEOUT (-6)   /* a bounded device wait gave up */
+#define MPET_ERR_STATE (-7)     /* call order violated (e.g. solve before setup) */
+
+#define MPET_MAX_NETWORKS 8
+
+#define MPET_PRECISION_FP64 0  /* FP64 matrix, FP64 MINRES, FP64 AMG */
+#define MPET_PRECISION_MIXED 1 /* FP32 inner MINRES + AMG inside FP64 refinement */
+
+typedef struct mpet_ctx mpet_ctx;
+
+/* Problem and solver parameters.  Material keys follow MPETProblem.params
+ * (src/mpet/mpet/mpetproblem.py:169-180, J/alpha/K/S/c with E,nu converted
+ * to mu,lmbda by convert_to_mu_lmbda, mpetproblem.py:13-16); theta follows
+ * MPETSolver.default_params (mpetsolver.py:86-98). */
+typedef struct mpet_params {
+    int32_t num_networks;              /* J (A in the configs), 1..8 */
+    int32_t precision;                 /* MPET_PRECISION_* */
+    double mu, lmbda;                  /* Lame parameters */
+    double alpha[MPET_MAX_NETWORKS];   /* Biot-Willis coefficients */
+    double c[MPET_MAX_NETWORKS];       /* storage coefficients */
+    double K[MPET_MAX_NETWORKS];       /* permeabilities */
+    double S[MPET_MAX_NETWORKS * MPET_MAX_NETWORKS]; /* transfer, row-major J x J (stride 8) */
+    double theta;                      /* theta-scheme weight */
+    double rtol;                       /* relative preconditioned residual, e.g. 1e-10 */
+    double inner_rtol;                 /* mixed: reduction per inner FP32 MINRES solve */
+    int32_t maxit;                     /* Krylov iterations per solve (all inner solves) */
+    int32_t max_outer;                 /* refinement sweeps per solve */
+    double amg_theta;                  /* strength threshold, e.g. 0.1 */
+    int32_t amg_cheb_degree;           /* Chebyshev smoother degree, e.g. 3 */
+    int32_t amg_coarse_size;           /* dense solve below this size, e.g. 500 */
+    int32_t check_every;               /* host convergence check period (iterations) */
+} mpet_params;
+
+typedef struct mpet_stats {
+    int32_t iterations;     /* total Krylov iterations */
+    int32_t outer;          /* refinement sweeps (1 for FP64) */
+    int32_t status;         /* MPET_OK, MPET_ERR_MAXIT or MPET_ERR_BREAKDOWN */
+    int32_t pad;
+    double relres;          /* final preconditioned residual / initial */
+    double relres_true;     /* final ||D^-1 r||_2 / ||D^-1 b||_2 in FP64 */
+} mpet_stats;
+
+/* Context ---------------------------------------------------------------- */
+int mpet_ctx_create(int device, mpet_ctx** out);
+int mpet_ctx_destroy(mpet_ctx* ctx);
+const char* mpet_last_error(const mpet_ctx* ctx);
+int mpet_set_stream(mpet_ctx* ctx, void* cuda_stream);
+int mpet_synchronize(mpet_ctx* ctx);
+
+/* Mesh and markers (host arrays).  Replaces the DOLFIN Mesh / MeshFunction
+ * inputs of MPETProblem (mpetproblem.py:103-166).  tets: nc x 4 vertex ids;
+ * bfacets: nf x 3 boundary facets; markers: (1 + J) x nf, row 0 the
+ * momentum markers, row 1 + a those of network a (0 Dirichlet, 1 Neumann,
+ * 2 Robin, anything else unmarked). */
+int mpet_mesh_upload(mpet_ctx* ctx, int64_t nv, const double* xyz_host, int64_t nc,
+                     const int32_t* tets_host, int64_t nf, const int32_t* bfacets_host,
+                     const int32_t* markers_host, int32_t num_networks);
+
+/* Dofmap, CSR sparsity pattern and Dirichlet DOF lists, built on the GPU.
+ * Replaces create_function_spaces (mpetsolver.py:100-132), DOLFIN's
+ * SparsityPatternBuilder used by assemble(self.a) (mpetsolver.py:335) and
+ * the topological DOF search of DirichletBC (mpetsolver.py:63-84). */
+int mpet_setup(mpet_ctx* ctx, const mpet_params* params);
+int mpet_update_params(mpet_ctx* ctx, const mpet_params* params);
+int mpet_get_sizes(mpet_ctx* ctx, int64_t* N, int64_t* nnz, int64_t* nnodes, int64_t* nedges);
+/* Copies of the pattern (row_ptr N+1, col nnz) and the edge list (2 x ne). */
+int mpet_get_pattern(mpet_ctx* ctx, int64_t* row_ptr_host, int32_t* col_host);
+int mpet_get_edges(mpet_ctx* ctx, int64_t* edges_host);
+
+/* Matrix assembly: assemble(self.a) + Robin axpy + bc.apply(A)
+ * (mpetsolver.py:335-344 / 412-419).  apply_bc != 0 replaces Dirichlet
+ * rows by unit rows (DirichletBC.apply).  In mixed precision an FP32 copy
+ * of the values is written in the same pass. */
+int mpet_assemble(mpet_ctx* ctx, double dt, int32_t apply_bc);
+int mpet_get_values(mpet_ctx* ctx, double* values_host);
+
+/* Dirichlet data.  field 0 = displacement (DirichletBC(VP.sub(0)),
+ * mpetsolver.py:74), field 1 + a = network a (mpetsolver.py:81).
+ * mpet_get_bc copies the DOF ids and their coordinates (count x 3) into
+ * device arrays; mpet_set_bc_values takes the values at those DOFs
+ * (device array, same order; displacement values node-major). */
+int mpet_get_bc_count(mpet_ctx* ctx, int32_t field, int64_t* count);
+int mpet_get_bc(mpet_ctx* ctx, int32_t field, int32_t* dofs, double* coords);
+int mpet_set_bc_values(mpet_ctx* ctx, int32_t field, const double* values);
+
+/* Sources as Lagrange interpolants at the current step (device arrays or
+ * NULL for zero): f at P2 nodes (nnodes x 3, node-major), g of network a at
+ * vertices (J x nv).  They enter b exactly as the reference's L0 / L1 dx
+ * terms (mpetsolver.py:233, 249). */
+int mpet_set_sources(mpet_ctx* ctx, const double* f_nodes, const double* g_vertices);
+
+/* Right-hand side: assemble(L) + sum assemble(L1) + assemble(L0) and
+ * bc.apply(b) (mpetsolver.py:356-376).  up_prev and b are device arrays
+ * of length N. */
+int mpet_rhs(mpet_ctx* ctx, double dt, const double* up_prev, double* b);
+
+/* Block-diagonal preconditioner (mpetsolver.py:264-271): one smoothed-
+ * aggregation AMG hierarchy per diagonal block, built for this dt. */
+int mpet_setup_preconditioner(mpet_ctx* ctx, double dt);
+int mpet_get_amg_info(mpet_ctx* ctx, int32_t block, int32_t* levels, int64_t* sizes_host,
+                      int64_t* nnz_host);
+
+/* Solve A x = b with the assembled (BC-applied) matrix; x holds the
+ * initial guess on entry (its Dirichlet entries are replaced by the BC
+ * values).  Replaces LUSolver(A, "mumps").solve / PETScKrylovSolver
+ * ("minres", "hypre_amg").solve (mpetsolver.py:379, 456, 556). */
+int mpet_solve(mpet_ctx* ctx, const double* b, double* x, mpet_stats* stats);
+
+/* One time step from up_prev: rhs (with the BC values and sources last
+ * set) and solve into up (initial guess up_prev).  MPETSolver.step without
+ * the matrix assembly, i.e. one pass of the solve_direct time loop
+ * (mpetsolver.py:424-462). */
+int mpet_step(mpet_ctx* ctx, double dt, const double* up_prev, double* up, mpet_stats* stats);
+
+/* y = A x with the assembled values; precision selects FP64 (x, y double)
+ * or the FP32 copy (x, y float).  Used by tests and the bandwidth bench. */
+int mpet_spmv(mpet_ctx* ctx, int32_t precision, const void* x, void* y);
+
+/* apply_symmetric / MatZeroRowsColumns (src/mpet/mpet/bc_symmetric.py:11-22):
+ * zero the Dirichlet columns of the assembled matrix in place (rows were
+ * replaced by mpet_assemble).  b, if not NULL, is lifted with x_bc. */
+int mpet_apply_symmetric(mpet_ctx* ctx, double* b, const double* x_bc);
+
+/* Per-kernel timing of the last solve (CUDA events): total ms and launches. */
+int mpet_get_timing(mpet_ctx* ctx, double* spmv_ms, int64_t* spmv_launches,
+                    double* precond_ms, int64_t* kernel_launches);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* MPET_GPU_H */

@@ -1,0 +1,227 @@
+"""Preconditioned MINRES and smoothed-aggregation AMG on the CPU (oracle).
+
+Test infrastructure and CPU baseline.  The reference's iterative path is
+``PETScKrylovSolver("minres", "hypre_amg")`` on the block-diagonal
+preconditioner form (src/mpet/mpet/mpetsolver.py:264-271, 502-557; working
+twin src/mpet/mpet/mpettotalpressuresolver.py:414-505).  PETSc KSP MINRES
+(Paige-Saunders) and an AMG preconditioner are restated here: hypre's
+classical BoomerAMG is replaced by smoothed aggregation (one hierarchy per
+diagonal block), which is the method the GPU path implements.
+
+The AMG follows the standard SA recipe: symmetric strength of connection,
+greedy three-pass aggregation, piecewise-constant tentative prolongator
+(near-nullspace = constants per scalar block), Jacobi-smoothed prolongator
+P = (I - omega/rho D^-1 A) T with omega = 4/3, Galerkin coarse operators
+P^T A P, Chebyshev smoothing on D^-1 A over [rho/30, 1.1 rho], and a dense
+Cholesky solve on the coarsest level.
+"""
+from __future__ import annotations
+
+import math
+
+import numpy as np
+import scipy.linalg as sla
+import scipy.sparse as sp
+
+
+def strength(A, theta):
+    A = A.tocsr()
+    d = np.abs(A.diagonal())
+    rows = np.repeat(np.arange(A.shape[0]), np.diff(A.indptr))
+    cols = A.indices
+    v = np.abs(A.data)
+    keep = (rows != cols) & (v >= theta * np.sqrt(d[rows] * d[cols])) & (v > 0)
+    S = sp.csr_matrix((np.ones(keep.sum()), (rows[keep], cols[keep])), shape=A.shape)
+    S.sort_indices()
+    return S
+
+
+def aggregate(S):
+    """Standard greedy aggregation (three passes).  Returns agg id per node (-1 = isolated)."""
+    n = S.shape[0]
+    ptr, idx = S.indptr, S.indices
+    agg = np.full(n, -1, dtype=np.int64)
+    nagg = 0
+    # pass 1: node whose strong neighbourhood is entirely free starts an aggregate
+    for i in range(n):
+        if agg[i] != -1:
+            continue
+        nb = idx[ptr[i]:ptr[i + 1]]
+        if nb.size == 0:
+            continue
+        if np.all(agg[nb] == -1):
+            agg[i] = nagg
+            agg[nb] = nagg
+            nagg += 1
+    # pass 2: attach free nodes to a neighbouring aggregate (first one found)
+    agg2 = agg.copy()
+    for i in range(n):
+        if agg[i] != -1:
+            continue
+        nb = idx[ptr[i]:ptr[i + 1]]
+        for j in nb:
+            if agg[j] != -1:
+                agg2[i] = agg[j]
+                break
+    agg = agg2
+    # pass 3: remaining free nodes with neighbours form new aggregates
+    for i in range(n):
+        if agg[i] != -1:
+            continue
+        nb = idx[ptr[i]:ptr[i + 1]]
+        if nb.size == 0:
+            continue
+        agg[i] = nagg
+        free = nb[agg[nb] == -1]
+        agg[free] = nagg
+        nagg += 1
+    return agg, nagg
+
+
+def power_rho(DinvA, iters=15):
+    """Spectral radius of D^-1 A by power iteration from x_i = 0.5 + ((7919 i) mod 1009) / 1009."""
+    i = np.arange(DinvA.shape[0], dtype=np.int64)
+    x = 0.5 + ((7919 * i) % 1009) / 1009.0
+    lam = 0.0
+    for _ in range(iters):
+        y = DinvA @ x
+        nrm = np.linalg.norm(y)
+        if nrm == 0:
+            return 1.0
+        lam = nrm / np.linalg.norm(x)
+        x = y / nrm
+    return lam
+
+
+class SAHierarchy:
+    def __init__(self, A, theta=0.0, coarse_size=500, max_levels=12, cheb_degree=2):
+        self.levels = []
+        self.cheb_degree = cheb_degree
+        A = A.tocsr()
+        while True:
+            n = A.shape[0]
+            D = A.diagonal().copy()
+            Dinv = np.where(D != 0, 1.0 / np.where(D != 0, D, 1.0), 0.0)
+            DinvA = sp.diags(Dinv) @ A
+            rho = power_rho(DinvA)
+            lev = {"A": A, "Dinv": Dinv, "rho": rho}
+            self.levels.append(lev)
+            if n <= coarse_size or len(self.levels) >= max_levels:
+                break
+            S = strength(A, theta)
+            agg, nagg = aggregate(S)
+            if nagg == 0 or nagg >= n:
+                break
+            rows = np.nonzero(agg >= 0)[0]
+            sizes = np.bincount(agg[rows], minlength=nagg)
+            T = sp.csr_matrix((1.0 / np.sqrt(sizes[agg[rows]]), (rows, agg[rows])), shape=(n, nagg))
+            P = (T - (4.0 / 3.0 / rho) * (DinvA @ T)).tocsr()
+            R = P.T.tocsr()
+            lev["P"], lev["R"] = P, R
+            A = (R @ A @ P).tocsr()
+            A.sort_indices()
+        Ac = self.levels[-1]["A"].toarray()
+        self.coarse = sla.cho_factor(Ac)
+
+    def _cheb(self, lev, b, x):
+        A, Dinv, rho = lev["A"], lev["Dinv"], lev["rho"]
+        hi, lo = 1.1 * rho, 1.1 * rho / 30.0
+        theta = 0.5 * (hi + lo)
+        delta = 0.5 * (hi - lo)
+        sigma = theta / delta
+        rho_old = 1.0 / sigma
+        r = Dinv * (b - A @ x)
+        d = r / theta
+        x = x + d
+        for _ in range(1, self.cheb_degree):
+            r = Dinv * (b - A @ x)
+            rho_new = 1.0 / (2.0 * sigma - rho_old)
+            d = rho_new * rho_old * d + (2.0 * rho_new / delta) * r
+            x = x + d
+            rho_old = rho_new
+        return x
+
+    def vcycle(self, b, k=0):
+        lev = self.levels[k]
+        if k == len(self.levels) - 1:
+            return sla.cho_solve(self.coarse, b)
+        x = self._cheb(lev, b, np.zeros_like(b))
+        r = b - lev["A"] @ x
+        xc = self.vcycle(lev["R"] @ r, k + 1)
+        x = x + lev["P"] @ xc
+        x = self._cheb(lev, b, x)
+        return x
+
+    def operator_complexity(self):
+        return sum(l["A"].nnz for l in self.levels) / self.levels[0]["A"].nnz
+
+
+def block_preconditioner(hier_u, hier_p, d, Nu, nv):
+    """z = blockdiag(AMG(Lu) per displacement component, AMG(P_a) per network) r."""
+    J = len(hier_p)
+
+    def apply(r):
+        z = np.empty_like(r)
+        ru = r[:Nu].reshape(-1, d)
+        zu = np.stack([hier_u.vcycle(np.ascontiguousarray(ru[:, k])) for k in range(d)], 1)
+        z[:Nu] = zu.ravel()
+        for a in range(J):
+            s = slice(Nu + a * nv, Nu + (a + 1) * nv)
+            z[s] = hier_p[a].vcycle(r[s])
+        return z
+    return apply
+
+
+def minres(A, b, M=None, x0=None, rtol=1e-10, maxiter=1000):
+    """Preconditioned MINRES (Paige-Saunders recurrences).
+
+    Stops when the preconditioned residual estimate phibar <= rtol * beta1.
+    Returns (x, iterations, history of phibar / beta1).
+    """
+    n = b.shape[0]
+    x = np.zeros(n) if x0 is None else x0.copy()
+    Mf = (lambda v: v) if M is None else M
+    r1 = b - A @ x
+    y = Mf(r1)
+    beta1 = math.sqrt(max(float(r1 @ y), 0.0))
+    hist = [1.0]
+    if beta1 == 0.0:
+        return x, 0, hist
+    oldb, beta, dbar, epsln, phibar = 0.0, beta1, 0.0, 0.0, beta1
+    cs, sn = -1.0, 0.0
+    w = np.zeros(n)
+    w2 = np.zeros(n)
+    r2 = r1.copy()
+    it = 0
+    while it < maxiter:
+        it += 1
+        s = 1.0 / beta
+        v = s * y
+        y = A @ v
+        if it >= 2:
+            y = y - (beta / oldb) * r1
+        alfa = float(v @ y)
+        y = y - (alfa / beta) * r2
+        r1 = r2
+        r2 = y
+        y = Mf(r2)
+        oldb = beta
+        beta = math.sqrt(max(float(r2 @ y), 0.0))
+        oldeps = epsln
+        delta = cs * dbar + sn * alfa
+        gbar = sn * dbar - cs * alfa
+        epsln = sn * beta
+        dbar = -cs * beta
+        gamma = max(math.hypot(gbar, beta), 1e-300)
+        cs = gbar / gamma
+        sn = beta / gamma
+        phi = cs * phibar
+        phibar = sn * phibar
+        w1 = w2
+        w2 = w
+        w = (v - oldeps * w1 - delta * w2) / gamma
+        x = x + phi * w
+        hist.append(phibar / beta1)
+        if phibar <= rtol * beta1:
+            break
+    return x, it, hist

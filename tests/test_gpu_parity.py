@@ -1,0 +1,200 @@
+"""GPU parity of the assemble + solve path against the CPU oracle.
+
+All engine calls go through the C ABI (libmpetgpu via ctypes).  Bars:
+sparsity bit-exact; matrix / right-hand side within 1e-12 relative (FP64,
+different summation order); solutions within 1e-8 relative of the SuperLU
+solution for both precisions (the spec bar is 1e-8 against FP64).
+"""
+import ctypes
+import math
+
+import numpy as np
+import pytest
+
+from helpers import make_oracle, make_problem, oracle_data
+
+pytestmark = pytest.mark.gpu
+
+torch = pytest.importorskip("torch")
+
+
+def _lib():
+    from waterscapes_gb300 import _lib
+    return _lib
+
+
+def _solver(problem, dt, **kw):
+    from waterscapes_gb300 import MPETSolver
+    params = dict(dt=dt, T=10 * dt, theta=1.0)
+    params.update(kw)
+    return MPETSolver(problem, params)
+
+
+def _np(t):
+    return t.detach().cpu().numpy()
+
+
+@pytest.mark.parametrize("n,J", [(2, 1), (2, 2), (3, 4), (4, 2)])
+def test_pattern_bit_exact(n, J):
+    problem, dt = make_problem(n, J)
+    s = _solver(problem, dt)
+    om = make_oracle(problem)
+    A = om.assemble_matrix(dt)
+    rp, ci = s.pattern()
+    assert s.N == om.dm.N and s.nnz == A.nnz
+    assert np.array_equal(rp, A.indptr.astype(np.int64))
+    assert np.array_equal(ci, A.indices.astype(np.int32))
+    assert np.array_equal(s.edges(), om.dm.edges)
+
+
+@pytest.mark.parametrize("n,J,apply_bc", [(3, 2, 1), (3, 4, 1), (3, 2, 0), (2, 3, 1)])
+def test_matrix_values(n, J, apply_bc):
+    problem, dt = make_problem(n, J)
+    s = _solver(problem, dt)
+    om = make_oracle(problem)
+    A = om.assemble_matrix(dt)
+    if apply_bc:
+        dofs, _ = om.dirichlet_values(dt, oracle_data(J))
+        A = om.apply_bc_matrix(A, dofs)
+    s.ctx.call("mpet_assemble", dt, apply_bc)
+    v = s.matrix_values()
+    scale = np.abs(A.data).max()
+    assert np.allclose(v, A.data, rtol=1e-12, atol=1e-13 * scale)
+
+
+def _f_expr(x, t):
+    return (x * x) * (1.0 + t)
+
+
+def _g_expr(a):
+    return lambda x, t: x[:, 0] * x[:, 1] * (a + 1) + t
+
+
+@pytest.mark.parametrize("theta", [1.0, 0.5])
+def test_rhs_parity(theta):
+    from waterscapes_gb300 import Expression
+    J = 2
+    problem, dt = make_problem(3, J)
+    problem.f = Expression(_f_expr)
+    problem.g = [Expression(_g_expr(a)) for a in range(J)]
+    s = _solver(problem, dt, theta=theta)
+    om = make_oracle(problem, theta)
+    rng = np.random.default_rng(1)
+    up_prev = rng.standard_normal(om.dm.N)
+    t0 = 0.3
+    t_theta, t1 = t0 + theta * dt, t0 + dt
+    data = oracle_data(J)
+    data["f"] = _f_expr
+    data["g"] = [_g_expr(a) for a in range(J)]
+    b = om.rhs_L(up_prev, dt) + om.rhs_L1(up_prev, dt, t_theta, data) + om.rhs_L0(t1, data)
+    dofs, vals = om.dirichlet_values(t1, data)
+    b = om.apply_bc_vector(b, dofs, vals)
+    s._set_sources(t_theta, t1)
+    s._set_bc_values(t1)
+    up = torch.tensor(up_prev, dtype=torch.float64, device=s.device)
+    bg = torch.empty(s.N, dtype=torch.float64, device=s.device)
+    s.ctx.call("mpet_rhs", dt, _lib()._ptr(up), _lib()._ptr(bg))
+    torch.cuda.synchronize()
+    assert np.allclose(_np(bg), b, rtol=1e-12, atol=1e-13 * np.abs(b).max())
+
+
+@pytest.mark.parametrize("precision", ["fp64", "mixed"])
+@pytest.mark.parametrize("n,J", [(4, 2), (3, 4)])
+def test_step_matches_direct_solve(precision, n, J):
+    problem, dt = make_problem(n, J)
+    s = _solver(problem, dt, precision=precision, rtol=1e-11)
+    om = make_oracle(problem)
+    rng = np.random.default_rng(2)
+    up_prev = rng.standard_normal(om.dm.N) * 1e-2
+    x_ref = om.step(up_prev, 0.0, dt, oracle_data(J))
+    s.up_.assign(torch.tensor(up_prev))
+    problem.time.assign(0.0)
+    st = s.step(dt)
+    x = _np(s.up.vector())
+    err = np.linalg.norm(x - x_ref) / np.linalg.norm(x_ref)
+    assert st.status == 0
+    assert err <= 1e-8, (err, s.last_stats)
+    assert float(problem.time) == pytest.approx(dt)
+
+
+@pytest.mark.parametrize("precision", ["fp64", "mixed"])
+def test_solve_direct_sequence(precision):
+    J = 2
+    problem, dt = make_problem(4, J)
+    s = _solver(problem, dt, precision=precision, T=6 * dt)
+    om = make_oracle(problem)
+    ref = list(om.solve_direct(np.zeros(om.dm.N), 0.0, 6 * dt, dt, oracle_data(J)))
+    got = []
+    for up, t in s.solve():
+        got.append((_np(up.vector()).copy(), t))
+    assert len(got) == len(ref) == 6
+    for (xg, tg), (xr, tr) in zip(got, ref):
+        assert tg == pytest.approx(tr)
+        assert np.linalg.norm(xg - xr) <= 1e-8 * np.linalg.norm(xr)
+    assert len(s.solver_monitor["niter"]) == 6
+
+
+def test_apply_symmetric_matches_zero_rows_columns():
+    J = 2
+    problem, dt = make_problem(3, J)
+    s = _solver(problem, dt, precision="fp64")
+    om = make_oracle(problem)
+    data = oracle_data(J)
+    A = om.assemble_matrix(dt)
+    dofs, vals = om.dirichlet_values(dt, data)
+    Abc = om.apply_bc_matrix(A, dofs)
+    rng = np.random.default_rng(3)
+    b = rng.standard_normal(om.dm.N)
+    xbc = np.zeros(om.dm.N)
+    for d, v in zip(dofs, vals):
+        xbc[d] = v
+        b[d] = v
+    As, bs = om.zero_rows_columns(Abc, dofs, b, xbc)
+    s.ctx.call("mpet_assemble", dt, 1)
+    bg = torch.tensor(b, device=s.device)
+    xg = torch.tensor(xbc, device=s.device)
+    s.ctx.call("mpet_apply_symmetric", _lib()._ptr(bg), _lib()._ptr(xg))
+    v = s.matrix_values()
+    assert np.allclose(v, As.data, rtol=1e-12, atol=1e-13 * np.abs(As.data).max())
+    assert np.allclose(_np(bg), bs, rtol=1e-12, atol=1e-12 * np.abs(bs).max())
+
+
+@pytest.mark.parametrize("precision", ["fp64", "mixed"])
+def test_spmv_parity(precision):
+    J = 4
+    problem, dt = make_problem(3, J)
+    s = _solver(problem, dt, precision=precision)
+    om = make_oracle(problem)
+    A = om.apply_bc_matrix(om.assemble_matrix(dt), om.dirichlet_values(dt, oracle_data(J))[0])
+    s.ctx.call("mpet_assemble", dt, 1)
+    rng = np.random.default_rng(4)
+    x = rng.standard_normal(om.dm.N)
+    y_ref = A @ x
+    y64 = torch.empty(s.N, dtype=torch.float64, device=s.device)
+    s.ctx.call("mpet_spmv", 0, _lib()._ptr(torch.tensor(x, device=s.device)), _lib()._ptr(y64))
+    torch.cuda.synchronize()
+    assert np.allclose(_np(y64), y_ref, rtol=1e-12, atol=1e-12 * np.abs(y_ref).max())
+    if precision == "mixed":
+        y32 = torch.empty(s.N, dtype=torch.float32, device=s.device)
+        x32 = torch.tensor(x, dtype=torch.float32, device=s.device)
+        s.ctx.call("mpet_spmv", 1, _lib()._ptr(x32), _lib()._ptr(y32))
+        torch.cuda.synchronize()
+        assert np.linalg.norm(_np(y32) - y_ref) <= 1e-5 * np.linalg.norm(y_ref)
+
+
+def test_assembly_and_solve_are_deterministic():
+    J = 2
+    problem, dt = make_problem(4, J)
+    s = _solver(problem, dt, precision="mixed")
+    s.ctx.call("mpet_assemble", dt, 1)
+    v1 = s.matrix_values()
+    s.ctx.call("mpet_assemble", dt, 1)
+    v2 = s.matrix_values()
+    assert np.array_equal(v1, v2)
+    problem.time.assign(0.0)
+    s.step(dt)
+    x1 = _np(s.up.vector()).copy()
+    problem.time.assign(0.0)
+    s.step(dt)
+    x2 = _np(s.up.vector()).copy()
+    assert np.array_equal(x1, x2)

@@ -1,0 +1,351 @@
+// Host-side smoothed-aggregation AMG setup for one scalar SPD block.
+//
+// The reference's iterative path preconditions with hypre BoomerAMG
+// (PETScKrylovSolver("minres", "hypre_amg"), src/mpet/mpet/mpetsolver.py:507)
+// applied to the block-diagonal form of mpetsolver.py:264-271.  This file
+// builds instead one smoothed-aggregation hierarchy per diagonal block:
+//   strength   |a_ij| >= theta sqrt(|a_ii a_jj|), i != j
+//   aggregates three greedy passes (root + free neighbourhood, attach,
+//              leftovers), isolated rows (Dirichlet unit rows) unaggregated
+//   T          piecewise constant, columns scaled to unit 2-norm
+//   P          (I - 4/3 rho^-1 D^-1 A) T, rho = spectral radius of D^-1 A
+//              from 15 power iterations on a fixed start vector
+//   A_c        P^T A P (Gustavson sparse products, rows sorted)
+//   coarsest   explicit inverse via Cholesky (FP64)
+// The V-cycle itself runs on the GPU (solve.cu).
+#include <math.h>
+#include <string.h>
+
+#include <algorithm>
+#include <vector>
+
+#ifdef _OPENMP
+#include <omp.h>
+#endif
+
+#include "mpet_internal.cuh"
+
+namespace mpet {
+
+static void transpose(const HostCsr& A, HostCsr& T) {
+    T.n = A.m;
+    T.m = A.n;
+    const int64_t nnz = (int64_t)A.ci.size();
+    T.rp.assign(T.n + 1, 0);
+    T.ci.resize(nnz);
+    T.v.resize(nnz);
+    for (int64_t e = 0; e < nnz; ++e) T.rp[A.ci[e] + 1]++;
+    for (int64_t i = 0; i < T.n; ++i) T.rp[i + 1] += T.rp[i];
+    std::vector<int64_t> pos(T.rp.begin(), T.rp.end() - 1);
+    for (int64_t i = 0; i < A.n; ++i)
+        for (int64_t e = A.rp[i]; e < A.rp[i + 1]; ++e) {
+            int64_t p = pos[A.ci[e]]++;
+            T.ci[p] = (int32_t)i;
+            T.v[p] = A.v[e];
+        }
+}
+
+// C = A * B (Gustavson, dense accumulator per thread, columns sorted).
+static void spgemm(const HostCsr& A, const HostCsr& B, HostCsr& C) {
+    C.n = A.n;
+    C.m = B.m;
+    C.rp.assign(C.n + 1, 0);
+    const int64_t n = A.n;
+#pragma omp parallel
+    {
+        std::vector<int64_t> mark(B.m, -1);
+#pragma omp for schedule(dynamic, 1024)
+        for (int64_t i = 0; i < n; ++i) {
+            int64_t cnt = 0;
+            for (int64_t e = A.rp[i]; e < A.rp[i + 1]; ++e) {
+                const int32_t k = A.ci[e];
+                for (int64_t f = B.rp[k]; f < B.rp[k + 1]; ++f) {
+                    const int32_t j = B.ci[f];
+                    if (mark[j] != i) {
+                        mark[j] = i;
+                        ++cnt;
+                    }
+                }
+            }
+            C.rp[i + 1] = cnt;
+        }
+    }
+    for (int64_t i = 0; i < n; ++i) C.rp[i + 1] += C.rp[i];
+    const int64_t nnz = C.rp[n];
+    C.ci.resize(nnz);
+    C.v.resize(nnz);
+#pragma omp parallel
+    {
+        std::vector<int64_t> mark(B.m, -1);
+        std::vector<double> acc(B.m, 0.0);
+        std::vector<int32_t> cols;
+#pragma omp for schedule(dynamic, 1024)
+        for (int64_t i = 0; i < n; ++i) {
+            cols.clear();
+            for (int64_t e = A.rp[i]; e < A.rp[i + 1]; ++e) {
+                const int32_t k = A.ci[e];
+                const double a = A.v[e];
+                for (int64_t f = B.rp[k]; f < B.rp[k + 1]; ++f) {
+                    const int32_t j = B.ci[f];
+                    if (mark[j] != i) {
+                        mark[j] = i;
+                        acc[j] = 0.0;
+                        cols.push_back(j);
+                    }
+                    acc[j] += a * B.v[f];
+                }
+            }
+            std::sort(cols.begin(), cols.end());
+            int64_t p = C.rp[i];
+            for (int32_t j : cols) {
+                C.ci[p] = j;
+                C.v[p] = acc[j];
+                ++p;
+            }
+        }
+    }
+}
+
+static void csr_matvec(const HostCsr& A, const std::vector<double>& x, std::vector<double>& y) {
+    y.assign(A.n, 0.0);
+#pragma omp parallel for schedule(static)
+    for (int64_t i = 0; i < A.n; ++i) {
+        double s = 0.0;
+        for (int64_t e = A.rp[i]; e < A.rp[i + 1]; ++e) s += A.v[e] * x[A.ci[e]];
+        y[i] = s;
+    }
+}
+
+static double diag_of(const HostCsr& A, int64_t i) {
+    for (int64_t e = A.rp[i]; e < A.rp[i + 1]; ++e)
+        if (A.ci[e] == i) return A.v[e];
+    return 0.0;
+}
+
+// Spectral radius of D^-1 A by power iteration from x_i = 0.5 + ((7919 i) mod 1009)/1009.
+static double power_rho(const HostCsr& A, const std::vector<double>& dinv, int iters) {
+    const int64_t n = A.n;
+    std::vector<double> x(n), y;
+    for (int64_t i = 0; i < n; ++i) x[i] = 0.5 + (double)((7919LL * i) % 1009LL) / 1009.0;
+    double lam = 1.0;
+    for (int k = 0; k < iters; ++k) {
+        csr_matvec(A, x, y);
+        double ny = 0.0, nx = 0.0;
+        for (int64_t i = 0; i < n; ++i) {
+            y[i] *= dinv[i];
+            ny += y[i] * y[i];
+            nx += x[i] * x[i];
+        }
+        if (ny == 0.0) return 1.0;
+        lam = sqrt(ny) / sqrt(nx);
+        const double s = 1.0 / sqrt(ny);
+        for (int64_t i = 0; i < n; ++i) x[i] = y[i] * s;
+    }
+    return lam;
+}
+
+static void strength(const HostCsr& A, double theta, HostCsr& S) {
+    const int64_t n = A.n;
+    std::vector<double> d(n);
+    for (int64_t i = 0; i < n; ++i) d[i] = fabs(diag_of(A, i));
+    S.n = S.m = n;
+    S.rp.assign(n + 1, 0);
+    for (int64_t i = 0; i < n; ++i) {
+        int64_t cnt = 0;
+        for (int64_t e = A.rp[i]; e < A.rp[i + 1]; ++e) {
+            const int32_t j = A.ci[e];
+            const double v = fabs(A.v[e]);
+            if (j != i && v > 0.0 && v >= theta * sqrt(d[i] * d[j])) ++cnt;
+        }
+        S.rp[i + 1] = S.rp[i] + cnt;
+    }
+    S.ci.resize(S.rp[n]);
+    for (int64_t i = 0; i < n; ++i) {
+        int64_t p = S.rp[i];
+        for (int64_t e = A.rp[i]; e < A.rp[i + 1]; ++e) {
+            const int32_t j = A.ci[e];
+            const double v = fabs(A.v[e]);
+            if (j != i && v > 0.0 && v >= theta * sqrt(d[i] * d[j])) S.ci[p++] = j;
+        }
+    }
+}
+
+static int64_t aggregate(const HostCsr& S, std::vector<int64_t>& agg) {
+    const int64_t n = S.n;
+    agg.assign(n, -1);
+    int64_t nagg = 0;
+    for (int64_t i = 0; i < n; ++i) {
+        if (agg[i] != -1) continue;
+        const int64_t b = S.rp[i], e = S.rp[i + 1];
+        if (b == e) continue;
+        bool free = true;
+        for (int64_t q = b; q < e && free; ++q) free = agg[S.ci[q]] == -1;
+        if (!free) continue;
+        agg[i] = nagg;
+        for (int64_t q = b; q < e; ++q) agg[S.ci[q]] = nagg;
+        ++nagg;
+    }
+    std::vector<int64_t> agg2(agg);
+    for (int64_t i = 0; i < n; ++i) {
+        if (agg[i] != -1) continue;
+        for (int64_t q = S.rp[i]; q < S.rp[i + 1]; ++q)
+            if (agg[S.ci[q]] != -1) {
+                agg2[i] = agg[S.ci[q]];
+                break;
+            }
+    }
+    agg.swap(agg2);
+    for (int64_t i = 0; i < n; ++i) {
+        if (agg[i] != -1) continue;
+        const int64_t b = S.rp[i], e = S.rp[i + 1];
+        if (b == e) continue;
+        agg[i] = nagg;
+        for (int64_t q = b; q < e; ++q)
+            if (agg[S.ci[q]] == -1) agg[S.ci[q]] = nagg;
+        ++nagg;
+    }
+    return nagg;
+}
+
+static bool cholesky_inverse(std::vector<double>& a, int64_t n, std::vector<double>& inv) {
+    // in-place lower Cholesky of a (row-major n x n)
+    for (int64_t j = 0; j < n; ++j) {
+        double s = a[j * n + j];
+        for (int64_t k = 0; k < j; ++k) s -= a[j * n + k] * a[j * n + k];
+        if (!(s > 0.0)) return false;
+        const double l = sqrt(s);
+        a[j * n + j] = l;
+        for (int64_t i = j + 1; i < n; ++i) {
+            double t = a[i * n + j];
+            for (int64_t k = 0; k < j; ++k) t -= a[i * n + k] * a[j * n + k];
+            a[i * n + j] = t / l;
+        }
+    }
+    inv.assign(n * n, 0.0);
+    std::vector<double> y(n);
+    for (int64_t col = 0; col < n; ++col) {
+        for (int64_t i = 0; i < n; ++i) {
+            double t = (i == col) ? 1.0 : 0.0;
+            for (int64_t k = 0; k < i; ++k) t -= a[i * n + k] * y[k];
+            y[i] = t / a[i * n + i];
+        }
+        for (int64_t i = n - 1; i >= 0; --i) {
+            double t = y[i];
+            for (int64_t k = i + 1; k < n; ++k) t -= a[k * n + i] * inv[k * n + col];
+            inv[i * n + col] = t / a[i * n + i];
+        }
+    }
+    return true;
+}
+
+void amg_setup_host(const HostCsr& A0, double theta, int coarse_size, int max_levels, HostAmg& out) {
+    out.lev.clear();
+    HostCsr A = A0;
+    if (coarse_size < 1) coarse_size = 500;
+    if (max_levels < 1) max_levels = 12;
+    while (true) {
+        HostAmgLevel L;
+        const int64_t n = A.n;
+        L.dinv.resize(n);
+        for (int64_t i = 0; i < n; ++i) {
+            const double d = diag_of(A, i);
+            L.dinv[i] = d != 0.0 ? 1.0 / d : 0.0;
+        }
+        L.rho = power_rho(A, L.dinv, 15);
+        L.A = A;
+        out.lev.push_back(L);
+        HostAmgLevel& cur = out.lev.back();
+        if (n <= coarse_size || (int)out.lev.size() >= max_levels) break;
+        HostCsr S;
+        strength(A, theta, S);
+        std::vector<int64_t> agg;
+        const int64_t nagg = aggregate(S, agg);
+        if (nagg == 0 || nagg >= n) break;
+        std::vector<int64_t> size(nagg, 0);
+        for (int64_t i = 0; i < n; ++i)
+            if (agg[i] >= 0) size[agg[i]]++;
+        HostCsr T;
+        T.n = n;
+        T.m = nagg;
+        T.rp.assign(n + 1, 0);
+        for (int64_t i = 0; i < n; ++i) T.rp[i + 1] = T.rp[i] + (agg[i] >= 0 ? 1 : 0);
+        T.ci.resize(T.rp[n]);
+        T.v.resize(T.rp[n]);
+        for (int64_t i = 0; i < n; ++i)
+            if (agg[i] >= 0) {
+                T.ci[T.rp[i]] = (int32_t)agg[i];
+                T.v[T.rp[i]] = 1.0 / sqrt((double)size[agg[i]]);
+            }
+        // P = T - (4/3/rho) D^-1 A T
+        HostCsr AT;
+        spgemm(A, T, AT);
+        const double w = 4.0 / 3.0 / cur.rho;
+        HostCsr P;
+        P.n = n;
+        P.m = nagg;
+        P.rp.assign(n + 1, 0);
+        for (int64_t i = 0; i < n; ++i) {
+            // union of T row (<= 1 entry) and AT row, both sorted
+            int64_t cnt = AT.rp[i + 1] - AT.rp[i];
+            if (T.rp[i + 1] > T.rp[i]) {
+                const int32_t j = T.ci[T.rp[i]];
+                bool found = false;
+                for (int64_t e = AT.rp[i]; e < AT.rp[i + 1]; ++e)
+                    if (AT.ci[e] == j) found = true;
+                if (!found) ++cnt;
+            }
+            P.rp[i + 1] = P.rp[i] + cnt;
+        }
+        P.ci.resize(P.rp[n]);
+        P.v.resize(P.rp[n]);
+        for (int64_t i = 0; i < n; ++i) {
+            int64_t p = P.rp[i];
+            const bool hasT = T.rp[i + 1] > T.rp[i];
+            const int32_t tj = hasT ? T.ci[T.rp[i]] : -1;
+            const double tv = hasT ? T.v[T.rp[i]] : 0.0;
+            bool placed = !hasT;
+            for (int64_t e = AT.rp[i]; e < AT.rp[i + 1]; ++e) {
+                const int32_t j = AT.ci[e];
+                if (!placed && tj < j) {
+                    P.ci[p] = tj;
+                    P.v[p] = tv;
+                    ++p;
+                    placed = true;
+                }
+                double v = -w * cur.dinv[i] * AT.v[e];
+                if (j == tj) {
+                    v += tv;
+                    placed = true;
+                }
+                P.ci[p] = j;
+                P.v[p] = v;
+                ++p;
+            }
+            if (!placed) {
+                P.ci[p] = tj;
+                P.v[p] = tv;
+                ++p;
+            }
+        }
+        HostCsr R;
+        transpose(P, R);
+        HostCsr AP, Ac;
+        spgemm(A, P, AP);
+        spgemm(R, AP, Ac);
+        cur.P = std::move(P);
+        cur.R = std::move(R);
+        A = std::move(Ac);
+    }
+    // coarsest: dense inverse
+    HostAmgLevel& last = out.lev.back();
+    const int64_t nc = last.A.n;
+    if (nc > 6000) fail(MPET_ERR_INVALID, "AMG coarsest level too large for a dense solve");
+    std::vector<double> dense(nc * nc, 0.0);
+    for (int64_t i = 0; i < nc; ++i)
+        for (int64_t e = last.A.rp[i]; e < last.A.rp[i + 1]; ++e) dense[i * nc + last.A.ci[e]] = last.A.v[e];
+    out.ncoarse = nc;
+    if (!cholesky_inverse(dense, nc, out.cinv))
+        fail(MPET_ERR_INVALID, "AMG coarsest operator is not positive definite");
+}
+
+}  // namespace mpet

@@ -1,0 +1,409 @@
+// extern "C" entry points of libmpetgpu (declared in include/mpet_gpu.h).
+// Every entry point converts internal errors into status codes; nothing
+// aborts, traps or exits.
+#include <string.h>
+
+#include <algorithm>
+#include <chrono>
+
+#include "mpet_internal.cuh"
+
+namespace mpet {
+void convert_values_to_f32(mpet_ctx* c);
+}
+
+using namespace mpet;
+
+#define API_BEGIN(ctx)                  \
+    if (!(ctx)) return MPET_ERR_INVALID; \
+    try {                               \
+        MPET_CUDA(cudaSetDevice((ctx)->device));
+#define API_END(ctx)                                   \
+    }                                                  \
+    catch (const Error& e) {                           \
+        (ctx)->err = e.msg;                            \
+        return e.code;                                 \
+    }                                                  \
+    catch (const std::exception& e) {                  \
+        (ctx)->err = e.what();                         \
+        return MPET_ERR_NOMEM;                         \
+    }                                                  \
+    return MPET_OK;
+
+static void require(bool cond, int code, const char* msg) {
+    if (!cond) fail(code, msg);
+}
+
+extern "C" {
+
+int mpet_ctx_create(int device, mpet_ctx** out) {
+    if (!out) return MPET_ERR_INVALID;
+    *out = nullptr;
+    int ndev = 0;
+    if (cudaGetDeviceCount(&ndev) != cudaSuccess || device < 0 || device >= ndev) {
+        cudaGetLastError();
+        return MPET_ERR_CUDA;
+    }
+    mpet_ctx* c = new (std::nothrow) mpet_ctx();
+    if (!c) return MPET_ERR_NOMEM;
+    c->device = device;
+    if (cudaSetDevice(device) != cudaSuccess || cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking) != cudaSuccess) {
+        cudaGetLastError();
+        delete c;
+        return MPET_ERR_CUDA;
+    }
+    c->own_stream = true;
+    cudaEventCreate(&c->ev0);
+    cudaEventCreate(&c->ev1);
+    *out = c;
+    return MPET_OK;
+}
+
+int mpet_ctx_destroy(mpet_ctx* c) {
+    if (!c) return MPET_ERR_INVALID;
+    cudaSetDevice(c->device);
+    if (c->stream) cudaStreamSynchronize(c->stream);
+    c->pool.free_all();
+    if (c->sc_host) cudaFreeHost(c->sc_host);
+    if (c->ev0) cudaEventDestroy(c->ev0);
+    if (c->ev1) cudaEventDestroy(c->ev1);
+    if (c->own_stream && c->stream) cudaStreamDestroy(c->stream);
+    delete c;
+    return MPET_OK;
+}
+
+const char* mpet_last_error(const mpet_ctx* c) { return c ? c->err.c_str() : "null context"; }
+
+int mpet_set_stream(mpet_ctx* c, void* stream) {
+    API_BEGIN(c)
+    if (c->own_stream && c->stream) {
+        MPET_CUDA(cudaStreamSynchronize(c->stream));
+        MPET_CUDA(cudaStreamDestroy(c->stream));
+    }
+    c->stream = (cudaStream_t)stream;
+    c->own_stream = false;
+    API_END(c)
+}
+
+int mpet_synchronize(mpet_ctx* c) {
+    API_BEGIN(c)
+    MPET_CUDA(cudaStreamSynchronize(c->stream));
+    API_END(c)
+}
+
+int mpet_mesh_upload(mpet_ctx* c, int64_t nv, const double* xyz, int64_t nc, const int32_t* tets, int64_t nf,
+                     const int32_t* bfacets, const int32_t* markers, int32_t J) {
+    API_BEGIN(c)
+    require(!c->mesh_ready, MPET_ERR_STATE, "mesh already uploaded to this context");
+    require(nv > 0 && nc > 0 && nf >= 0 && xyz && tets, MPET_ERR_INVALID, "empty mesh");
+    require(J >= 1 && J <= MPET_MAX_NETWORKS, MPET_ERR_INVALID, "num_networks must be in 1..8");
+    require(nf == 0 || (bfacets && markers), MPET_ERR_INVALID, "facets without markers");
+    require(nv < 2147483647LL / 4, MPET_ERR_INVALID, "too many vertices");
+    for (int64_t i = 0; i < 4 * nc; ++i)
+        require(tets[i] >= 0 && tets[i] < nv, MPET_ERR_INVALID, "cell vertex index out of range");
+    for (int64_t i = 0; i < 3 * nf; ++i)
+        require(bfacets[i] >= 0 && bfacets[i] < nv, MPET_ERR_INVALID, "facet vertex index out of range");
+    // cells with ascending vertex ids (DOLFIN's ordered-mesh convention)
+    std::vector<int32_t> sorted(tets, tets + 4 * nc);
+    for (int64_t k = 0; k < nc; ++k) std::sort(sorted.begin() + 4 * k, sorted.begin() + 4 * k + 4);
+    c->nv = nv;
+    c->nc = nc;
+    c->nf = nf;
+    c->J = J;
+    c->x = c->pool.alloc<double>(3 * nv);
+    c->cells = c->pool.alloc<int32_t>(4 * nc);
+    c->bfacets = c->pool.alloc<int32_t>(3 * (nf > 0 ? nf : 1));
+    c->markers = c->pool.alloc<int32_t>((1 + J) * (nf > 0 ? nf : 1));
+    MPET_CUDA(cudaMemcpyAsync(c->x, xyz, sizeof(double) * 3 * nv, cudaMemcpyHostToDevice, c->stream));
+    MPET_CUDA(cudaMemcpyAsync(c->cells, sorted.data(), sizeof(int32_t) * 4 * nc, cudaMemcpyHostToDevice, c->stream));
+    if (nf > 0) {
+        MPET_CUDA(cudaMemcpyAsync(c->bfacets, bfacets, sizeof(int32_t) * 3 * nf, cudaMemcpyHostToDevice, c->stream));
+        MPET_CUDA(cudaMemcpyAsync(c->markers, markers, sizeof(int32_t) * (1 + J) * nf, cudaMemcpyHostToDevice,
+                                  c->stream));
+    }
+    MPET_CUDA(cudaStreamSynchronize(c->stream));
+    c->mesh_ready = true;
+    API_END(c)
+}
+
+static void check_params(const mpet_ctx* c, const mpet_params* p) {
+    require(p != nullptr, MPET_ERR_INVALID, "params is NULL");
+    require(p->num_networks == c->J, MPET_ERR_INVALID, "params.num_networks differs from the mesh upload");
+    require(p->precision == MPET_PRECISION_FP64 || p->precision == MPET_PRECISION_MIXED, MPET_ERR_INVALID,
+            "unknown precision");
+    require(p->theta > 0.0 && p->theta <= 1.0, MPET_ERR_INVALID, "theta must be in (0, 1]");
+    require(p->rtol > 0.0, MPET_ERR_INVALID, "rtol must be positive");
+}
+
+int mpet_setup(mpet_ctx* c, const mpet_params* p) {
+    API_BEGIN(c)
+    require(c->mesh_ready, MPET_ERR_STATE, "mpet_mesh_upload must come first");
+    require(!c->setup_done, MPET_ERR_STATE, "mpet_setup already done");
+    check_params(c, p);
+    c->prm = *p;
+    if (c->prm.inner_rtol <= 0) c->prm.inner_rtol = 1e-4;
+    if (c->prm.amg_theta < 0) c->prm.amg_theta = 0.1;
+    build_topology(c);
+    build_pattern(c);
+    build_bc(c);
+    c->A.v64 = c->pool.alloc<double>(c->nnz);
+    if (c->prm.precision == MPET_PRECISION_MIXED) c->A.v32 = c->pool.alloc<float>(c->nnz);
+    c->dinv = c->pool.alloc<double>(c->N);
+    c->Lu.v64 = c->pool.alloc<double>(c->Lu.nnz);
+    for (int a = 0; a < c->J; ++a) c->Pp[a].v64 = c->pool.alloc<double>(c->Pp[a].nnz);
+    alloc_krylov(c);
+    MPET_CUDA(cudaStreamSynchronize(c->stream));
+    c->setup_done = true;
+    API_END(c)
+}
+
+int mpet_update_params(mpet_ctx* c, const mpet_params* p) {
+    API_BEGIN(c)
+    require(c->setup_done, MPET_ERR_STATE, "mpet_setup must come first");
+    check_params(c, p);
+    require(p->precision == c->prm.precision, MPET_ERR_INVALID, "precision is fixed at setup");
+    c->prm = *p;
+    if (c->prm.inner_rtol <= 0) c->prm.inner_rtol = 1e-4;
+    c->assembled = false;
+    c->precond_ready = false;
+    API_END(c)
+}
+
+int mpet_get_sizes(mpet_ctx* c, int64_t* N, int64_t* nnz, int64_t* nnodes, int64_t* nedges) {
+    API_BEGIN(c)
+    require(c->setup_done, MPET_ERR_STATE, "mpet_setup must come first");
+    if (N) *N = c->N;
+    if (nnz) *nnz = c->nnz;
+    if (nnodes) *nnodes = c->nnodes;
+    if (nedges) *nedges = c->ne;
+    API_END(c)
+}
+
+int mpet_get_pattern(mpet_ctx* c, int64_t* rp, int32_t* ci) {
+    API_BEGIN(c)
+    require(c->setup_done, MPET_ERR_STATE, "mpet_setup must come first");
+    if (rp) MPET_CUDA(cudaMemcpyAsync(rp, c->A.rp, sizeof(int64_t) * (c->N + 1), cudaMemcpyDeviceToHost, c->stream));
+    if (ci) MPET_CUDA(cudaMemcpyAsync(ci, c->A.ci, sizeof(int32_t) * c->nnz, cudaMemcpyDeviceToHost, c->stream));
+    MPET_CUDA(cudaStreamSynchronize(c->stream));
+    API_END(c)
+}
+
+int mpet_get_edges(mpet_ctx* c, int64_t* edges) {
+    API_BEGIN(c)
+    require(c->setup_done, MPET_ERR_STATE, "mpet_setup must come first");
+    std::vector<int64_t> k(c->ne);
+    MPET_CUDA(cudaMemcpyAsync(k.data(), c->edge_key, sizeof(int64_t) * c->ne, cudaMemcpyDeviceToHost, c->stream));
+    MPET_CUDA(cudaStreamSynchronize(c->stream));
+    for (int64_t e = 0; e < c->ne; ++e) {
+        edges[2 * e] = k[e] / c->nv;
+        edges[2 * e + 1] = k[e] % c->nv;
+    }
+    API_END(c)
+}
+
+int mpet_assemble(mpet_ctx* c, double dt, int32_t apply_bc) {
+    API_BEGIN(c)
+    require(c->setup_done, MPET_ERR_STATE, "mpet_setup must come first");
+    require(dt > 0.0, MPET_ERR_INVALID, "dt must be positive");
+    launch_assemble_matrix(c, dt, apply_bc != 0, c->A.v32 != nullptr);
+    MPET_CUDA(cudaStreamSynchronize(c->stream));
+    c->assembled = true;
+    c->asm_dt = dt;
+    API_END(c)
+}
+
+int mpet_get_values(mpet_ctx* c, double* vals) {
+    API_BEGIN(c)
+    require(c->assembled, MPET_ERR_STATE, "mpet_assemble must come first");
+    MPET_CUDA(cudaMemcpyAsync(vals, c->A.v64, sizeof(double) * c->nnz, cudaMemcpyDeviceToHost, c->stream));
+    MPET_CUDA(cudaStreamSynchronize(c->stream));
+    API_END(c)
+}
+
+int mpet_get_bc_count(mpet_ctx* c, int32_t field, int64_t* count) {
+    API_BEGIN(c)
+    require(c->setup_done, MPET_ERR_STATE, "mpet_setup must come first");
+    require(field >= 0 && field <= c->J && count, MPET_ERR_INVALID, "bad field");
+    *count = c->bc_off[field + 1] - c->bc_off[field];
+    API_END(c)
+}
+
+__global__ void k_bc_coords(const int32_t* __restrict__ dofs, int64_t n, int64_t Nu, int64_t nv,
+                            const double* __restrict__ x, const int64_t* __restrict__ ekey, double* coords) {
+    int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    int64_t d = dofs[i];
+    int64_t node = d < Nu ? d / 3 : (d - Nu) % nv;
+    for (int k = 0; k < 3; ++k) {
+        double v;
+        if (node < nv) {
+            v = x[3 * node + k];
+        } else {
+            int64_t key = ekey[node - nv];
+            v = 0.5 * (x[3 * (key / nv) + k] + x[3 * (key % nv) + k]);
+        }
+        coords[3 * i + k] = v;
+    }
+}
+
+int mpet_get_bc(mpet_ctx* c, int32_t field, int32_t* dofs, double* coords) {
+    API_BEGIN(c)
+    require(c->setup_done, MPET_ERR_STATE, "mpet_setup must come first");
+    require(field >= 0 && field <= c->J, MPET_ERR_INVALID, "bad field");
+    const int64_t off = c->bc_off[field], n = c->bc_off[field + 1] - off;
+    if (n > 0) {
+        if (dofs)
+            MPET_CUDA(cudaMemcpyAsync(dofs, c->bc_dofs + off, sizeof(int32_t) * n, cudaMemcpyDeviceToDevice, c->stream));
+        if (coords) {
+            k_bc_coords<<<(int)((n + 255) / 256), 256, 0, c->stream>>>(c->bc_dofs + off, n, c->Nu, c->nv, c->x,
+                                                                        c->edge_key, coords);
+            MPET_CHECK_LAUNCH();
+        }
+    }
+    MPET_CUDA(cudaStreamSynchronize(c->stream));
+    API_END(c)
+}
+
+int mpet_set_bc_values(mpet_ctx* c, int32_t field, const double* vals) {
+    API_BEGIN(c)
+    require(c->setup_done, MPET_ERR_STATE, "mpet_setup must come first");
+    require(field >= 0 && field <= c->J, MPET_ERR_INVALID, "bad field");
+    const int64_t off = c->bc_off[field], n = c->bc_off[field + 1] - off;
+    if (n > 0) {
+        if (vals)
+            MPET_CUDA(cudaMemcpyAsync(c->bc_vals + off, vals, sizeof(double) * n, cudaMemcpyDefault, c->stream));
+        else
+            MPET_CUDA(cudaMemsetAsync(c->bc_vals + off, 0, sizeof(double) * n, c->stream));
+    }
+    API_END(c)
+}
+
+int mpet_set_sources(mpet_ctx* c, const double* f, const double* g) {
+    API_BEGIN(c)
+    require(c->setup_done, MPET_ERR_STATE, "mpet_setup must come first");
+    c->f_nodes = f;
+    c->g_vert = g;
+    API_END(c)
+}
+
+int mpet_rhs(mpet_ctx* c, double dt, const double* up_prev, double* b) {
+    API_BEGIN(c)
+    require(c->setup_done, MPET_ERR_STATE, "mpet_setup must come first");
+    require(up_prev && b, MPET_ERR_INVALID, "NULL vector");
+    launch_rhs(c, dt, up_prev, b);
+    API_END(c)
+}
+
+int mpet_setup_preconditioner(mpet_ctx* c, double dt) {
+    API_BEGIN(c)
+    require(c->setup_done, MPET_ERR_STATE, "mpet_setup must come first");
+    require(dt > 0.0, MPET_ERR_INVALID, "dt must be positive");
+    launch_assemble_prec_blocks(c, dt);
+    const bool fp32 = c->prm.precision == MPET_PRECISION_MIXED;
+    auto fetch = [&](const Csr& d, HostCsr& h) {
+        h.n = d.n;
+        h.m = d.m;
+        h.rp.resize(d.n + 1);
+        h.ci.resize(d.nnz);
+        h.v.resize(d.nnz);
+        MPET_CUDA(cudaMemcpyAsync(h.rp.data(), d.rp, sizeof(int64_t) * (d.n + 1), cudaMemcpyDeviceToHost, c->stream));
+        MPET_CUDA(cudaMemcpyAsync(h.ci.data(), d.ci, sizeof(int32_t) * d.nnz, cudaMemcpyDeviceToHost, c->stream));
+        MPET_CUDA(cudaMemcpyAsync(h.v.data(), d.v64, sizeof(double) * d.nnz, cudaMemcpyDeviceToHost, c->stream));
+        MPET_CUDA(cudaStreamSynchronize(c->stream));
+        // the pattern arrays of the P1 blocks cover all P2 nodes: keep the vertex rows
+        if (h.rp[0] != 0) fail(MPET_ERR_STATE, "unexpected row pointer base");
+    };
+    const int cs = c->prm.amg_coarse_size > 0 ? c->prm.amg_coarse_size : 500;
+    {
+        HostCsr h;
+        fetch(c->Lu, h);
+        HostAmg ha;
+        amg_setup_host(h, c->prm.amg_theta, cs, 12, ha);
+        upload_amg(c, c->amg_u, ha, 3, fp32);
+    }
+    for (int a = 0; a < c->J; ++a) {
+        HostCsr h;
+        fetch(c->Pp[a], h);
+        HostAmg ha;
+        amg_setup_host(h, c->prm.amg_theta, cs, 12, ha);
+        upload_amg(c, c->amg_p[a], ha, 1, fp32);
+    }
+    c->precond_ready = true;
+    c->prec_dt = dt;
+    API_END(c)
+}
+
+int mpet_get_amg_info(mpet_ctx* c, int32_t block, int32_t* levels, int64_t* sizes, int64_t* nnz) {
+    API_BEGIN(c)
+    require(c->precond_ready, MPET_ERR_STATE, "mpet_setup_preconditioner must come first");
+    require(block >= 0 && block <= c->J, MPET_ERR_INVALID, "bad block");
+    const AmgHier& h = block == 0 ? c->amg_u : c->amg_p[block - 1];
+    if (levels) *levels = (int32_t)h.lev.size();
+    for (size_t k = 0; k < h.lev.size(); ++k) {
+        if (sizes) sizes[k] = h.lev[k].A.n;
+        if (nnz) nnz[k] = h.lev[k].A.nnz;
+    }
+    API_END(c)
+}
+
+int mpet_solve(mpet_ctx* c, const double* b, double* x, mpet_stats* st) {
+    API_BEGIN(c)
+    require(c->assembled, MPET_ERR_STATE, "mpet_assemble must come first");
+    require(c->precond_ready, MPET_ERR_STATE, "mpet_setup_preconditioner must come first");
+    require(b && x, MPET_ERR_INVALID, "NULL vector");
+    int s = solve_system(c, b, x, st);
+    if (s != MPET_OK) {
+        c->err = s == MPET_ERR_MAXIT ? "Krylov iteration limit reached" : "Krylov breakdown";
+        return s;
+    }
+    API_END(c)
+}
+
+int mpet_step(mpet_ctx* c, double dt, const double* up_prev, double* up, mpet_stats* st) {
+    API_BEGIN(c)
+    require(c->assembled, MPET_ERR_STATE, "mpet_assemble must come first");
+    require(c->precond_ready, MPET_ERR_STATE, "mpet_setup_preconditioner must come first");
+    require(up_prev && up && up_prev != up, MPET_ERR_INVALID, "up_prev and up must be distinct device arrays");
+    double* b = c->ob ? c->ob : (c->ob = c->pool.alloc<double>(c->N));
+    launch_rhs(c, dt, up_prev, b);
+    if (up != up_prev)
+        MPET_CUDA(cudaMemcpyAsync(up, up_prev, sizeof(double) * c->N, cudaMemcpyDeviceToDevice, c->stream));
+    int s = solve_system(c, b, up, st);
+    if (s != MPET_OK) {
+        c->err = s == MPET_ERR_MAXIT ? "Krylov iteration limit reached" : "Krylov breakdown";
+        return s;
+    }
+    API_END(c)
+}
+
+int mpet_spmv(mpet_ctx* c, int32_t precision, const void* x, void* y) {
+    API_BEGIN(c)
+    require(c->assembled, MPET_ERR_STATE, "mpet_assemble must come first");
+    if (precision == MPET_PRECISION_MIXED) {
+        require(c->A.v32 != nullptr, MPET_ERR_STATE, "no FP32 values (setup precision is FP64)");
+        spmv<float>(c, c->A, 1, (const float*)x, (float*)y);
+    } else {
+        spmv<double>(c, c->A, 1, (const double*)x, (double*)y);
+    }
+    API_END(c)
+}
+
+int mpet_apply_symmetric(mpet_ctx* c, double* b, const double* xbc) {
+    API_BEGIN(c)
+    require(c->assembled, MPET_ERR_STATE, "mpet_assemble must come first");
+    launch_zero_bc_columns(c, b, xbc);
+    convert_values_to_f32(c);
+    MPET_CUDA(cudaStreamSynchronize(c->stream));
+    API_END(c)
+}
+
+int mpet_get_timing(mpet_ctx* c, double* spmv_ms, int64_t* spmv_launches, double* precond_ms, int64_t* launches) {
+    API_BEGIN(c)
+    if (spmv_ms) *spmv_ms = c->t_spmv_ms;
+    if (spmv_launches) *spmv_launches = c->n_spmv;
+    if (precond_ms) *precond_ms = c->t_prec_ms;
+    if (launches) *launches = c->n_launch;
+    API_END(c)
+}
+
+}  // extern "C"

@@ -1,0 +1,567 @@
+// Element kernels of the MPET operator and right-hand side.
+//
+// Local tensors restate the forms of src/mpet/mpet/mpetsolver.py:196-201
+// (a = lhs(F)) and :233, :249 (sources) for P2 vector displacement and P1
+// pressures on affine tetrahedra, integrated exactly: P2 gradients are
+// linear, so with g_{j,r} the value of grad(phi_j) at vertex r and
+// s_j = sum_r g_{j,r},
+//   int d_k phi_m d_l phi_j = |T|/20 (sum_r g_{m,r,k} g_{j,r,l} + s_{m,k} s_{j,l})
+//   int lambda_w d_k phi_j  = |T|/20 (g_{j,w,k} + s_{j,k})
+//   int lambda_v lambda_w   = |T|/20 (1 + delta_vw),   int grad lambda_v . grad lambda_w = |T| b_v . b_w.
+//
+// Assembly is a row-owner gather: one warp owns the displacement rows of a
+// P2 node (and, for a vertex, its J pressure rows), walks the node's cells
+// in ascending order and adds that node's row slice of each cell matrix at
+// the CSR positions given by the per-cell rank tables.  Every value is
+// written by exactly one warp in a fixed order, so the result is
+// deterministic and needs neither atomics nor a cell colouring.
+#include "mpet_internal.cuh"
+
+namespace mpet {
+
+__constant__ int c_edges[6][2] = {{2, 3}, {1, 3}, {1, 2}, {0, 3}, {0, 2}, {0, 1}};
+
+// int phi_i phi_j / |T| for P2 on a tetrahedron, times 420.
+__constant__ double c_m2[10][10] = {
+    {6, 1, 1, 1, -6, -6, -6, -4, -4, -4},     {1, 6, 1, 1, -6, -4, -4, -6, -6, -4},
+    {1, 1, 6, 1, -4, -6, -4, -6, -4, -6},     {1, 1, 1, 6, -4, -4, -6, -4, -6, -6},
+    {-6, -6, -4, -4, 32, 16, 16, 16, 16, 8},  {-6, -4, -6, -4, 16, 32, 16, 16, 8, 16},
+    {-6, -4, -4, -6, 16, 16, 32, 8, 16, 16},  {-4, -6, -6, -4, 16, 16, 8, 32, 16, 16},
+    {-4, -6, -4, -6, 16, 8, 16, 16, 32, 16},  {-4, -4, -6, -6, 8, 16, 16, 16, 16, 32}};
+
+struct MatCoef {
+    double mu, lmbda, dt_theta;
+    int J;
+    double alpha[MPET_MAX_NETWORKS], c[MPET_MAX_NETWORKS], K[MPET_MAX_NETWORKS];
+    double S[MPET_MAX_NETWORKS * MPET_MAX_NETWORKS];  // row-major, stride 8
+    double Ssum[MPET_MAX_NETWORKS];                   // sum_b S_ab
+};
+
+struct Geo {
+    double b[4][3];
+    double vol;
+};
+
+__device__ __forceinline__ void load_geo(const double* __restrict__ geo, int64_t c, Geo& G) {
+    const double* g = geo + 16 * c;
+#pragma unroll
+    for (int r = 0; r < 4; ++r)
+#pragma unroll
+        for (int k = 0; k < 3; ++k) G.b[r][k] = g[3 * r + k];
+    G.vol = g[12];
+}
+
+// g_{j,r} (value of grad phi_j at vertex r) for all r, and s_j.
+__device__ __forceinline__ void p2_grad_table(const Geo& G, int j, double g[4][3], double s[3]) {
+    if (j < 4) {
+#pragma unroll
+        for (int r = 0; r < 4; ++r) {
+            double f = (r == j) ? 3.0 : -1.0;
+#pragma unroll
+            for (int k = 0; k < 3; ++k) g[r][k] = f * G.b[j][k];
+        }
+#pragma unroll
+        for (int k = 0; k < 3; ++k) s[k] = 0.0;
+    } else {
+        int ea = c_edges[j - 4][0], eb = c_edges[j - 4][1];
+#pragma unroll
+        for (int r = 0; r < 4; ++r)
+#pragma unroll
+            for (int k = 0; k < 3; ++k)
+                g[r][k] = (r == ea ? 4.0 * G.b[eb][k] : 0.0) + (r == eb ? 4.0 * G.b[ea][k] : 0.0);
+#pragma unroll
+        for (int k = 0; k < 3; ++k) s[k] = 4.0 * (G.b[ea][k] + G.b[eb][k]);
+    }
+}
+
+// value of grad phi_j at vertex r, plus s_j
+__device__ __forceinline__ void p2_grad_at(const Geo& G, int j, int r, double g[3], double s[3]) {
+    if (j < 4) {
+        double f = (r == j) ? 3.0 : -1.0;
+#pragma unroll
+        for (int k = 0; k < 3; ++k) {
+            g[k] = f * G.b[j][k];
+            s[k] = 0.0;
+        }
+    } else {
+        int ea = c_edges[j - 4][0], eb = c_edges[j - 4][1];
+#pragma unroll
+        for (int k = 0; k < 3; ++k) {
+            g[k] = (r == ea ? 4.0 * G.b[eb][k] : 0.0) + (r == eb ? 4.0 * G.b[ea][k] : 0.0);
+            s[k] = 4.0 * (G.b[ea][k] + G.b[eb][k]);
+        }
+    }
+}
+
+__device__ __forceinline__ int lb_i32(const int32_t* a, int n, int32_t key) {
+    int lo = 0, hi = n;
+    while (lo < hi) {
+        int mid = (lo + hi) >> 1;
+        if (a[mid] < key) lo = mid + 1; else hi = mid;
+    }
+    return lo;
+}
+
+struct AsmArgs {
+    int64_t nnodes, nv, Nu;
+    const int64_t* row_ptr;
+    const int64_t* n2_ptr;
+    const int32_t* n2_col;
+    const int64_t* n1_ptr;
+    const int32_t* n1_col;
+    const int64_t* inc_ptr;
+    const int32_t* inc;
+    const uint16_t* rank2;
+    const uint16_t* rank1;
+    const double* geo;
+    const uint8_t* dof_bc;
+    double* v64;
+    float* v32;
+    double* dinv;
+    int apply_bc;
+};
+
+__global__ void __launch_bounds__(256) k_assemble_matrix(AsmArgs A, MatCoef P) {
+    const int lane = threadIdx.x & 31;
+    const int64_t warp = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) >> 5;
+    const int64_t nwarps = ((int64_t)gridDim.x * blockDim.x) >> 5;
+    const int J = P.J;
+    for (int64_t i = warp; i < A.nnodes; i += nwarps) {
+        const bool isv = i < A.nv;
+        const int64_t s2 = A.n2_ptr[i], s1 = A.n1_ptr[i];
+        const int d2 = (int)(A.n2_ptr[i + 1] - s2), d1 = (int)(A.n1_ptr[i + 1] - s1);
+        const int L = 3 * d2 + J * d1;
+        const int nrows = 3 + (isv ? J : 0);
+        int64_t rows[3 + MPET_MAX_NETWORKS];
+        for (int k = 0; k < 3; ++k) rows[k] = 3 * i + k;
+        for (int a = 0; a < J; ++a) rows[3 + a] = A.Nu + (int64_t)a * A.nv + i;
+        int64_t rp[3 + MPET_MAX_NETWORKS];
+        for (int q = 0; q < nrows; ++q) rp[q] = A.row_ptr[rows[q]];
+        for (int q = 0; q < nrows; ++q)
+            for (int e = lane; e < L; e += 32) A.v64[rp[q] + e] = 0.0;
+        __syncwarp();
+        for (int64_t it = A.inc_ptr[i]; it < A.inc_ptr[i + 1]; ++it) {
+            const int32_t packed = A.inc[it];
+            const int64_t cell = packed >> 4;
+            const int m = packed & 15;
+            Geo G;
+            load_geo(A.geo, cell, G);
+            double gm[4][3], sm[3];
+            p2_grad_table(G, m, gm, sm);
+            const double w20 = G.vol * (1.0 / 20.0);
+            const uint16_t* rk2 = A.rank2 + cell * 100 + m * 10;
+            const uint16_t* rk1 = A.rank1 + cell * 40 + m * 4;
+            const int ntask = isv ? 76 : 42;
+            for (int t = lane; t < ntask; t += 32) {
+                if (t < 30) {
+                    const int j = t / 3, k = t % 3;
+                    double gj[4][3], sj[3];
+                    p2_grad_table(G, j, gj, sj);
+                    double M[3][3];
+#pragma unroll
+                    for (int a = 0; a < 3; ++a)
+#pragma unroll
+                        for (int b = 0; b < 3; ++b) {
+                            double acc = sm[a] * sj[b];
+#pragma unroll
+                            for (int r = 0; r < 4; ++r) acc += gm[r][a] * gj[r][b];
+                            M[a][b] = w20 * acc;
+                        }
+                    const double tr = M[0][0] + M[1][1] + M[2][2];
+                    const int64_t base = rp[k] + 3 * (int64_t)rk2[j];
+#pragma unroll
+                    for (int l = 0; l < 3; ++l) {
+                        double v = P.mu * M[l][k] + P.lmbda * M[k][l];
+                        if (l == k) v += P.mu * tr;
+                        A.v64[base + l] += v;
+                    }
+                } else if (t < 42) {
+                    const int tt = t - 30, k = tt / 4, w = tt % 4;
+                    const double C = w20 * (gm[w][k] + sm[k]);
+                    const int64_t base = rp[k] + 3 * (int64_t)d2 + rk1[w];
+                    for (int a = 0; a < J; ++a) A.v64[base + (int64_t)a * d1] += -P.alpha[a] * C;
+                } else if (t < 72) {
+                    const int tt = t - 42, j = tt / 3, l = tt % 3;
+                    double g[3], s[3];
+                    p2_grad_at(G, j, m, g, s);
+                    const double C = w20 * (g[l] + s[l]);
+                    for (int a = 0; a < J; ++a) A.v64[rp[3 + a] + 3 * (int64_t)rk2[j] + l] += -P.alpha[a] * C;
+                } else {
+                    const int w = t - 72;
+                    const double M1 = w20 * (m == w ? 2.0 : 1.0);
+                    const double L1 = G.vol * (G.b[m][0] * G.b[w][0] + G.b[m][1] * G.b[w][1] + G.b[m][2] * G.b[w][2]);
+                    for (int a = 0; a < J; ++a) {
+                        const int64_t base = rp[3 + a] + 3 * (int64_t)d2 + rk1[w];
+                        for (int b = 0; b < J; ++b) {
+                            double v = -P.dt_theta * ((a == b ? P.Ssum[a] : 0.0) - P.S[a * MPET_MAX_NETWORKS + b]) * M1;
+                            if (a == b) v += -P.c[a] * M1 - P.dt_theta * P.K[a] * L1;
+                            A.v64[base + (int64_t)b * d1] += v;
+                        }
+                    }
+                }
+            }
+            __syncwarp();
+        }
+        // Dirichlet rows (DirichletBC.apply(A): zero row, unit diagonal)
+        int self2 = lb_i32(A.n2_col + s2, d2, (int32_t)i);
+        int self1 = isv ? lb_i32(A.n1_col + s1, d1, (int32_t)i) : 0;
+        for (int q = 0; q < nrows; ++q) {
+            const int64_t dpos = q < 3 ? rp[q] + 3 * self2 + q : rp[q] + 3 * (int64_t)d2 + (int64_t)(q - 3) * d1 + self1;
+            if (A.apply_bc && A.dof_bc[rows[q]]) {
+                for (int e = lane; e < L; e += 32) A.v64[rp[q] + e] = 0.0;
+                __syncwarp();
+                if (lane == 0) A.v64[dpos] = 1.0;
+                __syncwarp();
+            }
+            if (lane == 0) {
+                double dg = fabs(A.v64[dpos]);
+                A.dinv[rows[q]] = dg > 0.0 ? 1.0 / dg : 1.0;
+            }
+        }
+        __syncwarp();
+        if (A.v32) {
+            for (int q = 0; q < nrows; ++q)
+                for (int e = lane; e < L; e += 32) A.v32[rp[q] + e] = (float)A.v64[rp[q] + e];
+        }
+        __syncwarp();
+    }
+}
+
+// Preconditioner blocks (mpetsolver.py:264-271): mu (grad u, grad v) per
+// displacement component on P2 nodes and c_a M + dt theta K_a L +
+// dt theta sum_{b != a} S_ab M on P1 vertices; Dirichlet DOFs eliminated
+// symmetrically (zero row and column, unit diagonal).
+struct PrecArgs {
+    int64_t nnodes, nv;
+    const int64_t* n2_ptr;
+    const int32_t* n2_col;
+    const int64_t* n1_ptr;
+    const int32_t* n1_col;
+    const int64_t* inc_ptr;
+    const int32_t* inc;
+    const uint16_t* rank2;
+    const uint16_t* rank1;
+    const double* geo;
+    const int32_t* cell_nodes;
+    const int32_t* cells;
+    const uint8_t* node_bc;
+    const uint8_t* vert_bc;
+    double* lu;
+    double* pp[MPET_MAX_NETWORKS];
+};
+
+__global__ void __launch_bounds__(256) k_assemble_prec(PrecArgs A, MatCoef P) {
+    const int lane = threadIdx.x & 31;
+    const int64_t warp = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) >> 5;
+    const int64_t nwarps = ((int64_t)gridDim.x * blockDim.x) >> 5;
+    const int J = P.J;
+    for (int64_t i = warp; i < A.nnodes; i += nwarps) {
+        const bool isv = i < A.nv;
+        const int64_t s2 = A.n2_ptr[i], s1 = A.n1_ptr[i];
+        const int d2 = (int)(A.n2_ptr[i + 1] - s2), d1 = (int)(A.n1_ptr[i + 1] - s1);
+        for (int e = lane; e < d2; e += 32) A.lu[s2 + e] = 0.0;
+        if (isv)
+            for (int a = 0; a < J; ++a)
+                for (int e = lane; e < d1; e += 32) A.pp[a][s1 + e] = 0.0;
+        __syncwarp();
+        const bool rowbc = A.node_bc[i] != 0;
+        for (int64_t it = A.inc_ptr[i]; it < A.inc_ptr[i + 1]; ++it) {
+            const int32_t packed = A.inc[it];
+            const int64_t cell = packed >> 4;
+            const int m = packed & 15;
+            Geo G;
+            load_geo(A.geo, cell, G);
+            const double w20 = G.vol * (1.0 / 20.0);
+            const int ntask = isv ? 14 : 10;
+            for (int t = lane; t < ntask; t += 32) {
+                if (t < 10) {
+                    const int j = t;
+                    const int32_t nj = A.cell_nodes[10 * cell + j];
+                    if (rowbc || A.node_bc[nj]) continue;
+                    double gm[4][3], sm[3], gj[4][3], sj[3];
+                    p2_grad_table(G, m, gm, sm);
+                    p2_grad_table(G, j, gj, sj);
+                    double tr = 0.0;
+#pragma unroll
+                    for (int a = 0; a < 3; ++a) {
+                        double acc = sm[a] * sj[a];
+#pragma unroll
+                        for (int r = 0; r < 4; ++r) acc += gm[r][a] * gj[r][a];
+                        tr += acc;
+                    }
+                    A.lu[s2 + A.rank2[cell * 100 + m * 10 + j]] += P.mu * w20 * tr;
+                } else {
+                    const int w = t - 10;
+                    const int32_t vw = A.cells[4 * cell + w];
+                    const double M1 = w20 * (m == w ? 2.0 : 1.0);
+                    const double L1 = G.vol * (G.b[m][0] * G.b[w][0] + G.b[m][1] * G.b[w][1] + G.b[m][2] * G.b[w][2]);
+                    const int64_t pos = s1 + A.rank1[cell * 40 + m * 4 + w];
+                    for (int a = 0; a < J; ++a) {
+                        if (A.vert_bc[(int64_t)a * A.nv + i] || A.vert_bc[(int64_t)a * A.nv + vw]) continue;
+                        double sS = P.Ssum[a] - P.S[a * MPET_MAX_NETWORKS + a];
+                        A.pp[a][pos] += (P.c[a] + P.dt_theta * sS) * M1 + P.dt_theta * P.K[a] * L1;
+                    }
+                }
+            }
+            __syncwarp();
+        }
+        if (lane == 0) {
+            if (rowbc) A.lu[s2 + lb_i32(A.n2_col + s2, d2, (int32_t)i)] = 1.0;
+            if (isv) {
+                int self1 = lb_i32(A.n1_col + s1, d1, (int32_t)i);
+                for (int a = 0; a < J; ++a)
+                    if (A.vert_bc[(int64_t)a * A.nv + i]) A.pp[a][s1 + self1] = 1.0;
+            }
+        }
+        __syncwarp();
+    }
+}
+
+// --- right-hand side ----------------------------------------------------------
+
+struct RhsArgs {
+    int64_t nnodes, nv, Nu;
+    const int64_t* inc_ptr;
+    const int32_t* inc;
+    const double* geo;
+    const int32_t* cell_nodes;
+    const int32_t* cells;
+    const double* up;     // previous state
+    const double* f;      // nnodes x 3 or null
+    const double* g;      // J x nv or null
+    double* b;
+    double dt, theta;
+};
+
+// Pressure rows of L = rhs(F) (mpetsolver.py:196-201, 261) plus dt g_a q_a
+// (L1, :249):  -alpha_a (div u^n, q) - c_a (p_a^n, q)
+//   + dt (1-theta) [K_a (grad p_a^n, grad q) + sum_b S_ab (p_a^n - p_b^n, q)] + dt (g_a, q).
+__global__ void __launch_bounds__(128) k_rhs_p(RhsArgs A, MatCoef P) {
+    const int64_t v = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    if (v >= A.nv) return;
+    const int J = P.J;
+    double acc[MPET_MAX_NETWORKS];
+    for (int a = 0; a < J; ++a) acc[a] = 0.0;
+    const double omt = A.dt * (1.0 - A.theta);
+    for (int64_t it = A.inc_ptr[v]; it < A.inc_ptr[v + 1]; ++it) {
+        const int32_t packed = A.inc[it];
+        const int64_t cell = packed >> 4;
+        const int m = packed & 15;
+        Geo G;
+        load_geo(A.geo, cell, G);
+        const double w20 = G.vol * (1.0 / 20.0);
+        double cp = 0.0;
+        for (int j = 0; j < 10; ++j) {
+            double g[3], s[3];
+            p2_grad_at(G, j, m, g, s);
+            const int64_t nj = A.cell_nodes[10 * cell + j];
+            cp += (g[0] + s[0]) * A.up[3 * nj] + (g[1] + s[1]) * A.up[3 * nj + 1] + (g[2] + s[2]) * A.up[3 * nj + 2];
+        }
+        cp *= w20;
+        double M1[4], L1[4];
+        int32_t vw[4];
+        for (int w = 0; w < 4; ++w) {
+            vw[w] = A.cells[4 * cell + w];
+            M1[w] = w20 * (m == w ? 2.0 : 1.0);
+            L1[w] = G.vol * (G.b[m][0] * G.b[w][0] + G.b[m][1] * G.b[w][1] + G.b[m][2] * G.b[w][2]);
+        }
+        double mp[MPET_MAX_NETWORKS], lp[MPET_MAX_NETWORKS];
+        for (int a = 0; a < J; ++a) {
+            const double* pa = A.up + A.Nu + (int64_t)a * A.nv;
+            double sm = 0.0, sl = 0.0, sg = 0.0;
+            for (int w = 0; w < 4; ++w) {
+                sm += M1[w] * pa[vw[w]];
+                sl += L1[w] * pa[vw[w]];
+                if (A.g) sg += M1[w] * A.g[(int64_t)a * A.nv + vw[w]];
+            }
+            mp[a] = sm;
+            lp[a] = sl;
+            acc[a] += A.dt * sg;
+        }
+        for (int a = 0; a < J; ++a) {
+            double t = -P.alpha[a] * cp - P.c[a] * mp[a] + omt * P.K[a] * lp[a];
+            for (int b = 0; b < J; ++b) {
+                const double sab = P.S[a * MPET_MAX_NETWORKS + b];
+                if (sab != 0.0) t += omt * sab * (mp[a] - mp[b]);
+            }
+            acc[a] += t;
+        }
+    }
+    for (int a = 0; a < J; ++a) A.b[A.Nu + (int64_t)a * A.nv + v] = acc[a];
+}
+
+// Displacement rows: (f, v) with f the P2 interpolant (L0, mpetsolver.py:233).
+__global__ void __launch_bounds__(128) k_rhs_u(RhsArgs A) {
+    const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    if (i >= A.nnodes) return;
+    double acc[3] = {0.0, 0.0, 0.0};
+    if (A.f) {
+        for (int64_t it = A.inc_ptr[i]; it < A.inc_ptr[i + 1]; ++it) {
+            const int32_t packed = A.inc[it];
+            const int64_t cell = packed >> 4;
+            const int m = packed & 15;
+            const double vol = A.geo[16 * cell + 12] * (1.0 / 420.0);
+            for (int j = 0; j < 10; ++j) {
+                const int64_t nj = A.cell_nodes[10 * cell + j];
+                const double w = vol * c_m2[m][j];
+                acc[0] += w * A.f[3 * nj];
+                acc[1] += w * A.f[3 * nj + 1];
+                acc[2] += w * A.f[3 * nj + 2];
+            }
+        }
+    }
+    A.b[3 * i] = acc[0];
+    A.b[3 * i + 1] = acc[1];
+    A.b[3 * i + 2] = acc[2];
+}
+
+__global__ void k_scatter_bc(const int32_t* __restrict__ dofs, const double* __restrict__ vals, int64_t n,
+                             double* b) {
+    const int64_t k = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    if (k < n) b[dofs[k]] = vals[k];
+}
+
+// MatZeroRowsColumns on the row-replaced matrix: for rows that are not
+// Dirichlet rows, b -= sum over Dirichlet columns a_rc x_c, then zero them.
+__global__ void k_zero_bc_columns(int64_t N, const int64_t* __restrict__ rp, const int32_t* __restrict__ ci,
+                                  double* v, const uint8_t* __restrict__ dof_bc, double* b,
+                                  const double* __restrict__ xbc) {
+    const int lane = threadIdx.x & 31;
+    const int64_t warp = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) >> 5;
+    const int64_t nwarps = ((int64_t)gridDim.x * blockDim.x) >> 5;
+    for (int64_t r = warp; r < N; r += nwarps) {
+        if (dof_bc[r]) continue;
+        double s = 0.0;
+        for (int64_t e = rp[r] + lane; e < rp[r + 1]; e += 32) {
+            const int32_t col = ci[e];
+            if (dof_bc[col]) {
+                if (xbc) s += v[e] * xbc[col];
+                v[e] = 0.0;
+            }
+        }
+        if (b) {
+#pragma unroll
+            for (int o = 16; o > 0; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
+            if (lane == 0) b[r] -= s;
+        }
+    }
+}
+
+static MatCoef make_coef(const mpet_ctx* c, double dt) {
+    MatCoef P{};
+    P.mu = c->prm.mu;
+    P.lmbda = c->prm.lmbda;
+    P.dt_theta = dt * c->prm.theta;
+    P.J = c->J;
+    for (int a = 0; a < c->J; ++a) {
+        P.alpha[a] = c->prm.alpha[a];
+        P.c[a] = c->prm.c[a];
+        P.K[a] = c->prm.K[a];
+        double s = 0.0;
+        for (int b = 0; b < c->J; ++b) {
+            P.S[a * MPET_MAX_NETWORKS + b] = c->prm.S[a * MPET_MAX_NETWORKS + b];
+            s += c->prm.S[a * MPET_MAX_NETWORKS + b];
+        }
+        P.Ssum[a] = s;
+    }
+    return P;
+}
+
+static inline int grid_for(int64_t n, int threads) {
+    int64_t g = (n + threads - 1) / threads;
+    if (g > 2147483647LL) g = 2147483647LL;
+    return (int)(g < 1 ? 1 : g);
+}
+
+void launch_assemble_matrix(mpet_ctx* c, double dt, bool apply_bc, bool write32) {
+    AsmArgs A{};
+    A.nnodes = c->nnodes;
+    A.nv = c->nv;
+    A.Nu = c->Nu;
+    A.row_ptr = c->A.rp;
+    A.n2_ptr = c->n2_ptr;
+    A.n2_col = c->n2_col;
+    A.n1_ptr = c->n1_ptr;
+    A.n1_col = c->n1_col;
+    A.inc_ptr = c->inc_ptr;
+    A.inc = c->inc;
+    A.rank2 = c->rank2;
+    A.rank1 = c->rank1;
+    A.geo = c->geo;
+    A.dof_bc = c->dof_bc;
+    A.v64 = c->A.v64;
+    A.v32 = write32 ? c->A.v32 : nullptr;
+    A.dinv = c->dinv;
+    A.apply_bc = apply_bc ? 1 : 0;
+    MatCoef P = make_coef(c, dt);
+    int64_t warps_needed = c->nnodes;
+    int blocks = grid_for(warps_needed * 32, 256);
+    if (blocks > 152 * 64) blocks = 152 * 64;
+    k_assemble_matrix<<<blocks, 256, 0, c->stream>>>(A, P);
+    MPET_CHECK_LAUNCH();
+}
+
+void launch_assemble_prec_blocks(mpet_ctx* c, double dt) {
+    PrecArgs A{};
+    A.nnodes = c->nnodes;
+    A.nv = c->nv;
+    A.n2_ptr = c->n2_ptr;
+    A.n2_col = c->n2_col;
+    A.n1_ptr = c->n1_ptr;
+    A.n1_col = c->n1_col;
+    A.inc_ptr = c->inc_ptr;
+    A.inc = c->inc;
+    A.rank2 = c->rank2;
+    A.rank1 = c->rank1;
+    A.geo = c->geo;
+    A.cell_nodes = c->cell_nodes;
+    A.cells = c->cells;
+    A.node_bc = c->node_bc;
+    A.vert_bc = c->vert_bc;
+    A.lu = c->Lu.v64;
+    for (int a = 0; a < c->J; ++a) A.pp[a] = c->Pp[a].v64;
+    MatCoef P = make_coef(c, dt);
+    int blocks = grid_for(c->nnodes * 32, 256);
+    if (blocks > 152 * 64) blocks = 152 * 64;
+    k_assemble_prec<<<blocks, 256, 0, c->stream>>>(A, P);
+    MPET_CHECK_LAUNCH();
+}
+
+void launch_rhs(mpet_ctx* c, double dt, const double* up_prev, double* b) {
+    RhsArgs A{};
+    A.nnodes = c->nnodes;
+    A.nv = c->nv;
+    A.Nu = c->Nu;
+    A.inc_ptr = c->inc_ptr;
+    A.inc = c->inc;
+    A.geo = c->geo;
+    A.cell_nodes = c->cell_nodes;
+    A.cells = c->cells;
+    A.up = up_prev;
+    A.f = c->f_nodes;
+    A.g = c->g_vert;
+    A.b = b;
+    A.dt = dt;
+    A.theta = c->prm.theta;
+    MatCoef P = make_coef(c, dt);
+    k_rhs_u<<<grid_for(c->nnodes, 128), 128, 0, c->stream>>>(A);
+    k_rhs_p<<<grid_for(c->nv, 128), 128, 0, c->stream>>>(A, P);
+    MPET_CHECK_LAUNCH();
+    launch_bc_vector(c, b);
+}
+
+void launch_bc_vector(mpet_ctx* c, double* b) {
+    if (c->nbc_dofs > 0) {
+        k_scatter_bc<<<grid_for(c->nbc_dofs, 256), 256, 0, c->stream>>>(c->bc_dofs, c->bc_vals, c->nbc_dofs, b);
+        MPET_CHECK_LAUNCH();
+    }
+}
+
+void launch_set_bc_in_x(mpet_ctx* c, double* x) { launch_bc_vector(c, x); }
+
+void launch_zero_bc_columns(mpet_ctx* c, double* b, const double* xbc) {
+    k_zero_bc_columns<<<152 * 16, 256, 0, c->stream>>>(c->N, c->A.rp, c->A.ci, c->A.v64, c->dof_bc, b, xbc);
+    MPET_CHECK_LAUNCH();
+}
+
+}  // namespace mpet

@@ -1,0 +1,230 @@
+// Internal declarations of libmpetgpu (not part of the C ABI).
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include <string>
+#include <vector>
+
+#include "../../include/mpet_gpu.h"
+
+namespace mpet {
+
+struct Error {
+    int code;
+    std::string msg;
+};
+
+[[noreturn]] inline void fail(int code, const std::string& msg) { throw Error{code, msg}; }
+
+#define MPET_CUDA(call)                                                                  \
+    do {                                                                                 \
+        cudaError_t e_ = (call);                                                         \
+        if (e_ != cudaSuccess)                                                           \
+            ::mpet::fail(MPET_ERR_CUDA, std::string(#call) + ": " + cudaGetErrorString(e_)); \
+    } while (0)
+
+#define MPET_CHECK_LAUNCH() MPET_CUDA(cudaGetLastError())
+
+// Device allocation tracked by the context so destroy() frees everything.
+struct DevPool {
+    std::vector<void*> ptrs;
+    template <typename T>
+    T* alloc(int64_t n) {
+        if (n <= 0) n = 1;
+        void* p = nullptr;
+        cudaError_t e = cudaMalloc(&p, (size_t)n * sizeof(T));
+        if (e != cudaSuccess) {
+            cudaGetLastError();
+            fail(MPET_ERR_NOMEM, "cudaMalloc of " + std::to_string((size_t)n * sizeof(T)) + " bytes failed");
+        }
+        ptrs.push_back(p);
+        return (T*)p;
+    }
+    void release(void* p) {
+        if (!p) return;
+        for (auto& q : ptrs)
+            if (q == p) {
+                cudaFree(q);
+                q = nullptr;
+            }
+    }
+    void free_all() {
+        for (auto p : ptrs)
+            if (p) cudaFree(p);
+        ptrs.clear();
+    }
+};
+
+// CSR with int64 row pointers and int32 column ids; values in FP64 and
+// (optionally) an FP32 copy sharing the same pattern.
+struct Csr {
+    int64_t n = 0, m = 0, nnz = 0;
+    int64_t* rp = nullptr;
+    int32_t* ci = nullptr;
+    double* v64 = nullptr;
+    float* v32 = nullptr;
+    int lpr = 32;  // lanes per row used by the SpMV kernels
+};
+
+struct AmgLevel {
+    Csr A, P, R;       // P: n x nc (prolongation), R = P^T
+    double* dinv64 = nullptr;
+    float* dinv32 = nullptr;
+    double rho = 1.0;  // spectral radius estimate of D^-1 A
+    // work buffers, each n * nvec elements of double (reused for float)
+    void* x = nullptr;
+    void* b = nullptr;
+    void* r = nullptr;
+    void* d = nullptr;
+    void* t0 = nullptr;
+    void* t1 = nullptr;
+};
+
+struct AmgHier {
+    int nvec = 1;
+    int cheb_degree = 3;
+    std::vector<AmgLevel> lev;
+    int64_t ncoarse = 0;
+    double* cinv = nullptr;  // dense inverse of the coarsest operator, FP64
+};
+
+// Device-resident MINRES scalars (all FP64).
+struct MinresScalars {
+    double beta1, beta, oldb, alfa, dbar, epsln, oldeps, phibar, phi, cs, sn, gamma, delta, gbar;
+    double c_r1;     // beta/oldb (0 on the first iteration)
+    double c_r2;     // alfa/beta
+    double inv_beta; // 1/beta
+    double inv_gamma;
+    double rel;      // phibar / beta1
+    double flag;     // 1 = breakdown
+    double nr2, nb2; // outer residual sums
+};
+
+// Host-side setup of one SA hierarchy from an FP64 CSR (amg_setup.cpp).
+struct HostCsr {
+    int64_t n = 0, m = 0;
+    std::vector<int64_t> rp;
+    std::vector<int32_t> ci;
+    std::vector<double> v;
+};
+struct HostAmgLevel {
+    HostCsr A, P, R;
+    std::vector<double> dinv;
+    double rho = 1.0;
+};
+struct HostAmg {
+    std::vector<HostAmgLevel> lev;
+    int64_t ncoarse = 0;
+    std::vector<double> cinv;
+};
+void amg_setup_host(const HostCsr& A, double theta, int coarse_size, int max_levels, HostAmg& out);
+
+}  // namespace mpet
+
+struct mpet_ctx {
+    int device = 0;
+    cudaStream_t stream = nullptr;
+    bool own_stream = false;
+    std::string err;
+    mpet::DevPool pool;
+
+    // mesh
+    int64_t nv = 0, nc = 0, nf = 0, ne = 0, nnodes = 0;
+    int J = 0;
+    double* x = nullptr;          // nv * 3
+    int32_t* cells = nullptr;     // nc * 4 (ascending vertex ids)
+    int32_t* bfacets = nullptr;   // nf * 3
+    int32_t* markers = nullptr;   // (1 + J) * nf
+    int64_t* edge_key = nullptr;  // ne, lo * nv + hi, ascending
+    int32_t* cell_nodes = nullptr;// nc * 10
+    double* geo = nullptr;        // nc * 16: grad lambda_0..3 (12), |T|
+    int64_t* n2_ptr = nullptr;    // P2 node adjacency
+    int32_t* n2_col = nullptr;
+    int64_t n2_nnz = 0;
+    int64_t* n1_ptr = nullptr;    // vertices adjacent to each P2 node
+    int32_t* n1_col = nullptr;
+    int64_t n1_nnz = 0;
+    int64_t* inc_ptr = nullptr;   // node -> (cell * 16 + local) incidence
+    int32_t* inc = nullptr;
+    uint16_t* rank2 = nullptr;    // nc * 100
+    uint16_t* rank1 = nullptr;    // nc * 40
+
+    // global system
+    int64_t N = 0, Nu = 0, nnz = 0;
+    mpet::Csr A;                  // rp/ci/v64/v32
+    double* dinv = nullptr;       // |diag|^-1 (1 where 0), FP64
+
+    // Dirichlet data
+    int64_t nbc_nodes[1 + MPET_MAX_NETWORKS] = {0};
+    int32_t* bc_nodes[1 + MPET_MAX_NETWORKS] = {nullptr};
+    int64_t nbc_dofs = 0;
+    int64_t bc_off[2 + MPET_MAX_NETWORKS] = {0};  // dof offsets per field in bc_dofs
+    int32_t* bc_dofs = nullptr;
+    double* bc_vals = nullptr;
+    uint8_t* node_bc = nullptr;   // nnodes flags (displacement)
+    uint8_t* vert_bc = nullptr;   // J * nv flags
+    uint8_t* dof_bc = nullptr;    // N flags
+
+    // sources (borrowed device pointers)
+    const double* f_nodes = nullptr;
+    const double* g_vert = nullptr;
+
+    mpet_params prm{};
+    bool mesh_ready = false, setup_done = false, assembled = false, precond_ready = false;
+    bool values_mixed = false;
+    double asm_dt = 0.0, prec_dt = -1.0;
+
+    // preconditioner blocks
+    mpet::Csr Lu;                 // mu-Laplacian on P2 nodes (pattern n2)
+    mpet::Csr Pp[MPET_MAX_NETWORKS]; // P1 blocks (pattern n1 restricted to vertices)
+    mpet::AmgHier amg_u;
+    mpet::AmgHier amg_p[MPET_MAX_NETWORKS];
+
+    // Krylov work
+    void* kv = nullptr;           // v
+    void* kr[3] = {nullptr, nullptr, nullptr};
+    void* kw[3] = {nullptr, nullptr, nullptr};
+    void* kd = nullptr;           // correction
+    double* ox = nullptr;         // outer FP64 vectors
+    double* orr = nullptr;
+    double* ob = nullptr;
+    double* partials = nullptr;   // reduction partials
+    mpet::MinresScalars* sc = nullptr;
+    mpet::MinresScalars* sc_host = nullptr;  // pinned
+
+    // timing
+    cudaEvent_t ev0 = nullptr, ev1 = nullptr;
+    double t_spmv_ms = 0.0, t_prec_ms = 0.0;
+    int64_t n_spmv = 0, n_launch = 0;
+    bool timing = false;
+};
+
+namespace mpet {
+
+constexpr int NB_RED = 608;   // fixed block count of every reduction kernel (152 SMs x 4)
+constexpr int RED_THREADS = 256;
+
+// setup.cu
+void build_topology(mpet_ctx* c);
+void build_pattern(mpet_ctx* c);
+void build_bc(mpet_ctx* c);
+
+// assemble.cu
+void launch_assemble_matrix(mpet_ctx* c, double dt, bool apply_bc, bool write32);
+void launch_assemble_prec_blocks(mpet_ctx* c, double dt);
+void launch_rhs(mpet_ctx* c, double dt, const double* up_prev, double* b);
+void launch_bc_vector(mpet_ctx* c, double* b);
+void launch_set_bc_in_x(mpet_ctx* c, double* x);
+void launch_zero_bc_columns(mpet_ctx* c, double* b, const double* xbc);
+
+// solve.cu
+template <typename T>
+void spmv(mpet_ctx* c, const Csr& A, int nvec, const T* x, T* y);
+void upload_amg(mpet_ctx* c, AmgHier& h, const HostAmg& ha, int nvec, bool fp32);
+int solve_system(mpet_ctx* c, const double* b, double* x, mpet_stats* st);
+void alloc_krylov(mpet_ctx* c);
+int choose_lpr(int64_t n, int64_t nnz);
+
+}  // namespace mpet

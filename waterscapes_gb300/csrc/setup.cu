@@ -1,0 +1,507 @@
+// Dofmap, adjacency, CSR sparsity pattern and Dirichlet DOF lists, all
+// built on the GPU once per mesh.
+//
+// The pattern follows DOLFIN's SparsityPatternBuilder as used by
+// assemble(self.a) in src/mpet/mpet/mpetsolver.py:335: for every cell the
+// dense block over all (30 + 4J) mixed DOFs is inserted, so a row of a P2
+// node i holds every displacement DOF of every P2 node sharing a cell with
+// i, followed by every pressure DOF of every vertex sharing a cell with i
+// (network-major).  Columns are ascending because displacement DOFs come
+// first and each list is sorted.
+//
+// Everything is derived from sorted 64-bit keys (radix sort + unique), which
+// keeps the construction deterministic.
+#include <cub/cub.cuh>
+#include <thrust/iterator/counting_iterator.h>
+
+#include "mpet_internal.cuh"
+
+namespace mpet {
+
+typedef unsigned long long u64;
+
+__constant__ int c_tet_edges[6][2] = {{2, 3}, {1, 3}, {1, 2}, {0, 3}, {0, 2}, {0, 1}};
+
+struct TmpBuf {
+    void* p = nullptr;
+    explicit TmpBuf(size_t bytes) {
+        if (cudaMalloc(&p, bytes ? bytes : 1) != cudaSuccess) {
+            cudaGetLastError();
+            fail(MPET_ERR_NOMEM, "temporary cudaMalloc of " + std::to_string(bytes) + " bytes failed");
+        }
+    }
+    ~TmpBuf() {
+        if (p) cudaFree(p);
+    }
+    template <typename T>
+    T* as() { return (T*)p; }
+};
+
+static inline int grid_for(int64_t n, int threads) {
+    int64_t g = (n + threads - 1) / threads;
+    if (g > 2147483647LL) g = 2147483647LL;
+    return (int)(g < 1 ? 1 : g);
+}
+
+__device__ __forceinline__ int64_t lower_bound_u64(const u64* a, int64_t n, u64 key) {
+    int64_t lo = 0, hi = n;
+    while (lo < hi) {
+        int64_t mid = (lo + hi) >> 1;
+        if (a[mid] < key) lo = mid + 1; else hi = mid;
+    }
+    return lo;
+}
+
+__device__ __forceinline__ int lower_bound_i32(const int32_t* a, int n, int32_t key) {
+    int lo = 0, hi = n;
+    while (lo < hi) {
+        int mid = (lo + hi) >> 1;
+        if (a[mid] < key) lo = mid + 1; else hi = mid;
+    }
+    return lo;
+}
+
+// Sort keys in place (ping-pong through a temporary) and keep the unique
+// ones; returns a freshly allocated exact-size array from the pool.
+static int64_t sort_unique(mpet_ctx* c, u64* keys, int64_t n, int end_bit, u64** out_keys) {
+    if (n > 2147483647LL) fail(MPET_ERR_INVALID, "too many adjacency keys for one radix sort");
+    int ni = (int)n;
+    TmpBuf sorted(sizeof(u64) * (size_t)n);
+    size_t tb = 0;
+    MPET_CUDA(cub::DeviceRadixSort::SortKeys(nullptr, tb, keys, sorted.as<u64>(), ni, 0, end_bit, c->stream));
+    {
+        TmpBuf tmp(tb);
+        MPET_CUDA(cub::DeviceRadixSort::SortKeys(tmp.p, tb, keys, sorted.as<u64>(), ni, 0, end_bit, c->stream));
+    }
+    TmpBuf nsel(sizeof(int64_t));
+    tb = 0;
+    MPET_CUDA(cub::DeviceSelect::Unique(nullptr, tb, sorted.as<u64>(), keys, nsel.as<int64_t>(), ni, c->stream));
+    {
+        TmpBuf tmp(tb);
+        MPET_CUDA(cub::DeviceSelect::Unique(tmp.p, tb, sorted.as<u64>(), keys, nsel.as<int64_t>(), ni, c->stream));
+    }
+    int64_t cnt = 0;
+    MPET_CUDA(cudaMemcpyAsync(&cnt, nsel.p, sizeof(int64_t), cudaMemcpyDeviceToHost, c->stream));
+    MPET_CUDA(cudaStreamSynchronize(c->stream));
+    u64* o = c->pool.alloc<u64>(cnt);
+    MPET_CUDA(cudaMemcpyAsync(o, keys, sizeof(u64) * cnt, cudaMemcpyDeviceToDevice, c->stream));
+    *out_keys = o;
+    return cnt;
+}
+
+static int bits_for(u64 maxval) {
+    int b = 1;
+    while (b < 64 && (maxval >> b) != 0) ++b;
+    return b;
+}
+
+// --- kernels ------------------------------------------------------------------
+
+__global__ void k_edge_keys(const int32_t* __restrict__ cells, int64_t nc, int64_t nv, u64* keys) {
+    int64_t idx = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    if (idx >= nc * 6) return;
+    int64_t c = idx / 6;
+    int e = (int)(idx % 6);
+    int64_t a = cells[4 * c + c_tet_edges[e][0]];
+    int64_t b = cells[4 * c + c_tet_edges[e][1]];
+    int64_t lo = a < b ? a : b, hi = a < b ? b : a;
+    keys[idx] = (u64)(lo * nv + hi);
+}
+
+__global__ void k_cell_nodes(const int32_t* __restrict__ cells, int64_t nc, int64_t nv,
+                             const u64* __restrict__ ekey, int64_t ne, int32_t* cell_nodes) {
+    int64_t idx = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    if (idx >= nc * 10) return;
+    int64_t c = idx / 10;
+    int j = (int)(idx % 10);
+    if (j < 4) {
+        cell_nodes[idx] = cells[4 * c + j];
+        return;
+    }
+    int e = j - 4;
+    int64_t a = cells[4 * c + c_tet_edges[e][0]];
+    int64_t b = cells[4 * c + c_tet_edges[e][1]];
+    int64_t lo = a < b ? a : b, hi = a < b ? b : a;
+    int64_t pos = lower_bound_u64(ekey, ne, (u64)(lo * nv + hi));
+    cell_nodes[idx] = (int32_t)(nv + pos);
+}
+
+__global__ void k_geometry(const double* __restrict__ x, const int32_t* __restrict__ cells, int64_t nc,
+                           double* geo) {
+    int64_t c = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    if (c >= nc) return;
+    double p[4][3];
+    for (int i = 0; i < 4; ++i)
+        for (int k = 0; k < 3; ++k) p[i][k] = x[3 * (int64_t)cells[4 * c + i] + k];
+    double e1[3], e2[3], e3[3];
+    for (int k = 0; k < 3; ++k) {
+        e1[k] = p[1][k] - p[0][k];
+        e2[k] = p[2][k] - p[0][k];
+        e3[k] = p[3][k] - p[0][k];
+    }
+    double c23[3] = {e2[1] * e3[2] - e2[2] * e3[1], e2[2] * e3[0] - e2[0] * e3[2], e2[0] * e3[1] - e2[1] * e3[0]};
+    double c31[3] = {e3[1] * e1[2] - e3[2] * e1[1], e3[2] * e1[0] - e3[0] * e1[2], e3[0] * e1[1] - e3[1] * e1[0]};
+    double c12[3] = {e1[1] * e2[2] - e1[2] * e2[1], e1[2] * e2[0] - e1[0] * e2[2], e1[0] * e2[1] - e1[1] * e2[0]};
+    double det = e1[0] * c23[0] + e1[1] * c23[1] + e1[2] * c23[2];
+    double id = 1.0 / det;
+    double* g = geo + 16 * c;
+    for (int k = 0; k < 3; ++k) {
+        double b1 = c23[k] * id, b2 = c31[k] * id, b3 = c12[k] * id;
+        g[3 + k] = b1;
+        g[6 + k] = b2;
+        g[9 + k] = b3;
+        g[k] = -(b1 + b2 + b3);
+    }
+    g[12] = fabs(det) / 6.0;
+    g[13] = g[14] = g[15] = 0.0;
+}
+
+__global__ void k_pairs_n2(const int32_t* __restrict__ cn, int64_t nc, int64_t nnodes, u64* keys) {
+    int64_t idx = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    if (idx >= nc * 100) return;
+    int64_t c = idx / 100;
+    int r = (int)(idx % 100);
+    int m = r / 10, j = r % 10;
+    keys[idx] = (u64)cn[10 * c + m] * (u64)nnodes + (u64)cn[10 * c + j];
+}
+
+__global__ void k_pairs_n1(const int32_t* __restrict__ cn, const int32_t* __restrict__ cells, int64_t nc,
+                           int64_t nv, u64* keys) {
+    int64_t idx = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    if (idx >= nc * 40) return;
+    int64_t c = idx / 40;
+    int r = (int)(idx % 40);
+    int m = r / 4, w = r % 4;
+    keys[idx] = (u64)cn[10 * c + m] * (u64)nv + (u64)cells[4 * c + w];
+}
+
+__global__ void k_pairs_inc(const int32_t* __restrict__ cn, int64_t nc, u64* keys) {
+    int64_t idx = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    if (idx >= nc * 10) return;
+    int64_t c = idx / 10;
+    int m = (int)(idx % 10);
+    keys[idx] = ((u64)cn[idx] << 32) | (u64)(c * 16 + m);
+}
+
+__global__ void k_ptr_from_keys(const u64* __restrict__ keys, int64_t nkeys, int64_t nrows, u64 stride,
+                                int64_t* ptr) {
+    int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    if (i > nrows) return;
+    ptr[i] = lower_bound_u64(keys, nkeys, (u64)i * stride);
+}
+
+__global__ void k_low_from_keys(const u64* __restrict__ keys, int64_t nkeys, u64 stride, int32_t* out) {
+    int64_t p = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    if (p >= nkeys) return;
+    out[p] = (int32_t)(keys[p] % stride);
+}
+
+__global__ void k_low32_from_keys(const u64* __restrict__ keys, int64_t nkeys, int32_t* out) {
+    int64_t p = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    if (p >= nkeys) return;
+    out[p] = (int32_t)(keys[p] & 0xffffffffULL);
+}
+
+__global__ void k_max_degree(const int64_t* __restrict__ ptr, int64_t n, int* out) {
+    int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    atomicMax(out, (int)(ptr[i + 1] - ptr[i]));
+}
+
+__global__ void k_ranks(const int32_t* __restrict__ cn, const int32_t* __restrict__ cells, int64_t nc,
+                        const int64_t* __restrict__ n2_ptr, const int32_t* __restrict__ n2_col,
+                        const int64_t* __restrict__ n1_ptr, const int32_t* __restrict__ n1_col,
+                        uint16_t* rank2, uint16_t* rank1) {
+    int64_t idx = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    if (idx >= nc * 140) return;
+    int64_t c = idx / 140;
+    int r = (int)(idx % 140);
+    if (r < 100) {
+        int m = r / 10, j = r % 10;
+        int32_t i = cn[10 * c + m];
+        int64_t s = n2_ptr[i];
+        int d = (int)(n2_ptr[i + 1] - s);
+        rank2[100 * c + r] = (uint16_t)lower_bound_i32(n2_col + s, d, cn[10 * c + j]);
+    } else {
+        r -= 100;
+        int m = r / 4, w = r % 4;
+        int32_t i = cn[10 * c + m];
+        int64_t s = n1_ptr[i];
+        int d = (int)(n1_ptr[i + 1] - s);
+        rank1[40 * c + r] = (uint16_t)lower_bound_i32(n1_col + s, d, cells[4 * c + w]);
+    }
+}
+
+__global__ void k_row_len(int64_t N, int64_t Nu, int64_t nv, int J, const int64_t* __restrict__ n2_ptr,
+                          const int64_t* __restrict__ n1_ptr, int64_t* len) {
+    int64_t r = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    if (r > N) return;
+    if (r == N) {
+        len[r] = 0;
+        return;
+    }
+    int64_t node = r < Nu ? r / 3 : (r - Nu) % nv;
+    len[r] = 3 * (n2_ptr[node + 1] - n2_ptr[node]) + (int64_t)J * (n1_ptr[node + 1] - n1_ptr[node]);
+}
+
+__global__ void k_fill_cols(int64_t N, int64_t Nu, int64_t nv, int J, const int64_t* __restrict__ row_ptr,
+                            const int64_t* __restrict__ n2_ptr, const int32_t* __restrict__ n2_col,
+                            const int64_t* __restrict__ n1_ptr, const int32_t* __restrict__ n1_col,
+                            int32_t* col) {
+    int lane = threadIdx.x & 31;
+    int64_t warp = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) >> 5;
+    int64_t nwarps = ((int64_t)gridDim.x * blockDim.x) >> 5;
+    for (int64_t r = warp; r < N; r += nwarps) {
+        int64_t node = r < Nu ? r / 3 : (r - Nu) % nv;
+        int64_t s2 = n2_ptr[node], s1 = n1_ptr[node];
+        int d2 = (int)(n2_ptr[node + 1] - s2), d1 = (int)(n1_ptr[node + 1] - s1);
+        int L = 3 * d2 + J * d1;
+        int64_t base = row_ptr[r];
+        for (int e = lane; e < L; e += 32) {
+            int32_t cidx;
+            if (e < 3 * d2) {
+                cidx = 3 * n2_col[s2 + e / 3] + e % 3;
+            } else {
+                int e2 = e - 3 * d2;
+                int a = e2 / d1;
+                cidx = (int32_t)(Nu + (int64_t)a * nv + n1_col[s1 + e2 % d1]);
+            }
+            col[base + e] = cidx;
+        }
+    }
+}
+
+__global__ void k_bc_flags(const int32_t* __restrict__ bf, const int32_t* __restrict__ mk, int64_t nf, int J,
+                           int64_t nv, const u64* __restrict__ ekey, int64_t ne, uint8_t* node_bc,
+                           uint8_t* vert_bc) {
+    int64_t f = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    if (f >= nf) return;
+    int64_t v[3] = {bf[3 * f], bf[3 * f + 1], bf[3 * f + 2]};
+    if (mk[f] == 0) {
+        for (int k = 0; k < 3; ++k) node_bc[v[k]] = 1;
+        const int pr[3][2] = {{0, 1}, {0, 2}, {1, 2}};
+        for (int k = 0; k < 3; ++k) {
+            int64_t a = v[pr[k][0]], b = v[pr[k][1]];
+            int64_t lo = a < b ? a : b, hi = a < b ? b : a;
+            int64_t pos = lower_bound_u64(ekey, ne, (u64)(lo * nv + hi));
+            if (pos < ne && ekey[pos] == (u64)(lo * nv + hi)) node_bc[nv + pos] = 1;
+        }
+    }
+    for (int a = 0; a < J; ++a)
+        if (mk[(int64_t)(1 + a) * nf + f] == 0)
+            for (int k = 0; k < 3; ++k) vert_bc[(int64_t)a * nv + v[k]] = 1;
+}
+
+__global__ void k_bc_dofs_u(const int32_t* __restrict__ nodes, int64_t n, int32_t* dofs, uint8_t* dof_bc) {
+    int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    for (int k = 0; k < 3; ++k) {
+        int32_t d = 3 * nodes[i] + k;
+        dofs[3 * i + k] = d;
+        dof_bc[d] = 1;
+    }
+}
+
+__global__ void k_bc_dofs_p(const int32_t* __restrict__ verts, int64_t n, int64_t base, int32_t* dofs,
+                            uint8_t* dof_bc) {
+    int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    int32_t d = (int32_t)(base + verts[i]);
+    dofs[i] = d;
+    dof_bc[d] = 1;
+}
+
+// --- host drivers -------------------------------------------------------------------
+
+void build_topology(mpet_ctx* c) {
+    cudaStream_t s = c->stream;
+    const int T = 256;
+    int64_t nc = c->nc, nv = c->nv;
+    // edges
+    {
+        TmpBuf keys(sizeof(u64) * nc * 6);
+        k_edge_keys<<<grid_for(nc * 6, T), T, 0, s>>>(c->cells, nc, nv, keys.as<u64>());
+        MPET_CHECK_LAUNCH();
+        u64* ek = nullptr;
+        c->ne = sort_unique(c, keys.as<u64>(), nc * 6, bits_for((u64)nv * (u64)nv), &ek);
+        c->edge_key = (int64_t*)ek;
+    }
+    c->nnodes = nv + c->ne;
+    c->cell_nodes = c->pool.alloc<int32_t>(nc * 10);
+    k_cell_nodes<<<grid_for(nc * 10, T), T, 0, s>>>(c->cells, nc, nv, (const u64*)c->edge_key, c->ne,
+                                                     c->cell_nodes);
+    MPET_CHECK_LAUNCH();
+    c->geo = c->pool.alloc<double>(nc * 16);
+    k_geometry<<<grid_for(nc, T), T, 0, s>>>(c->x, c->cells, nc, c->geo);
+    MPET_CHECK_LAUNCH();
+    int64_t nn = c->nnodes;
+    // P2 node adjacency
+    {
+        TmpBuf keys(sizeof(u64) * nc * 100);
+        k_pairs_n2<<<grid_for(nc * 100, T), T, 0, s>>>(c->cell_nodes, nc, nn, keys.as<u64>());
+        MPET_CHECK_LAUNCH();
+        u64* uk = nullptr;
+        c->n2_nnz = sort_unique(c, keys.as<u64>(), nc * 100, bits_for((u64)nn * (u64)nn), &uk);
+        c->n2_ptr = c->pool.alloc<int64_t>(nn + 1);
+        c->n2_col = c->pool.alloc<int32_t>(c->n2_nnz);
+        k_ptr_from_keys<<<grid_for(nn + 1, T), T, 0, s>>>(uk, c->n2_nnz, nn, (u64)nn, c->n2_ptr);
+        k_low_from_keys<<<grid_for(c->n2_nnz, T), T, 0, s>>>(uk, c->n2_nnz, (u64)nn, c->n2_col);
+        MPET_CHECK_LAUNCH();
+        MPET_CUDA(cudaStreamSynchronize(s));
+        c->pool.release(uk);
+    }
+    // vertices adjacent to each node
+    {
+        TmpBuf keys(sizeof(u64) * nc * 40);
+        k_pairs_n1<<<grid_for(nc * 40, T), T, 0, s>>>(c->cell_nodes, c->cells, nc, nv, keys.as<u64>());
+        MPET_CHECK_LAUNCH();
+        u64* uk = nullptr;
+        c->n1_nnz = sort_unique(c, keys.as<u64>(), nc * 40, bits_for((u64)nn * (u64)nv), &uk);
+        c->n1_ptr = c->pool.alloc<int64_t>(nn + 1);
+        c->n1_col = c->pool.alloc<int32_t>(c->n1_nnz);
+        k_ptr_from_keys<<<grid_for(nn + 1, T), T, 0, s>>>(uk, c->n1_nnz, nn, (u64)nv, c->n1_ptr);
+        k_low_from_keys<<<grid_for(c->n1_nnz, T), T, 0, s>>>(uk, c->n1_nnz, (u64)nv, c->n1_col);
+        MPET_CHECK_LAUNCH();
+        MPET_CUDA(cudaStreamSynchronize(s));
+        c->pool.release(uk);
+    }
+    // node -> cell incidence (cells ascending within a node)
+    {
+        if (nc >= (1LL << 27)) fail(MPET_ERR_INVALID, "too many cells (limit 2^27: cell * 16 + local fits int32)");
+        TmpBuf keys(sizeof(u64) * nc * 10);
+        k_pairs_inc<<<grid_for(nc * 10, T), T, 0, s>>>(c->cell_nodes, nc, keys.as<u64>());
+        MPET_CHECK_LAUNCH();
+        u64* uk = nullptr;
+        int64_t n = sort_unique(c, keys.as<u64>(), nc * 10, 32 + bits_for((u64)nn), &uk);
+        if (n != nc * 10) fail(MPET_ERR_INVALID, "degenerate cell (repeated vertex)");
+        c->inc_ptr = c->pool.alloc<int64_t>(nn + 1);
+        c->inc = c->pool.alloc<int32_t>(n);
+        k_ptr_from_keys<<<grid_for(nn + 1, T), T, 0, s>>>(uk, n, nn, 1ULL << 32, c->inc_ptr);
+        k_low32_from_keys<<<grid_for(n, T), T, 0, s>>>(uk, n, c->inc);
+        MPET_CHECK_LAUNCH();
+        MPET_CUDA(cudaStreamSynchronize(s));
+        c->pool.release(uk);
+    }
+    // degree limits of the 16-bit rank tables
+    {
+        TmpBuf mx(sizeof(int) * 2);
+        MPET_CUDA(cudaMemsetAsync(mx.p, 0, sizeof(int) * 2, s));
+        k_max_degree<<<grid_for(nn, T), T, 0, s>>>(c->n2_ptr, nn, mx.as<int>());
+        k_max_degree<<<grid_for(nn, T), T, 0, s>>>(c->inc_ptr, nn, mx.as<int>() + 1);
+        MPET_CHECK_LAUNCH();
+        int h[2];
+        MPET_CUDA(cudaMemcpyAsync(h, mx.p, sizeof(h), cudaMemcpyDeviceToHost, s));
+        MPET_CUDA(cudaStreamSynchronize(s));
+        if (h[0] >= 65535) fail(MPET_ERR_INVALID, "node degree too large for 16-bit ranks");
+    }
+    c->rank2 = c->pool.alloc<uint16_t>(nc * 100);
+    c->rank1 = c->pool.alloc<uint16_t>(nc * 40);
+    k_ranks<<<grid_for(nc * 140, T), T, 0, s>>>(c->cell_nodes, c->cells, nc, c->n2_ptr, c->n2_col, c->n1_ptr,
+                                                 c->n1_col, c->rank2, c->rank1);
+    MPET_CHECK_LAUNCH();
+}
+
+void build_pattern(mpet_ctx* c) {
+    cudaStream_t s = c->stream;
+    const int T = 256;
+    int J = c->J;
+    c->Nu = 3 * c->nnodes;
+    c->N = c->Nu + (int64_t)J * c->nv;
+    if (c->N >= 2147483647LL) fail(MPET_ERR_INVALID, "too many DOFs for 32-bit column ids");
+    int64_t N = c->N;
+    c->A.n = c->A.m = N;
+    c->A.rp = c->pool.alloc<int64_t>(N + 1);
+    {
+        TmpBuf len(sizeof(int64_t) * (N + 1));
+        k_row_len<<<grid_for(N + 1, T), T, 0, s>>>(N, c->Nu, c->nv, J, c->n2_ptr, c->n1_ptr, len.as<int64_t>());
+        MPET_CHECK_LAUNCH();
+        size_t tb = 0;
+        MPET_CUDA(cub::DeviceScan::ExclusiveSum(nullptr, tb, len.as<int64_t>(), c->A.rp, (int)(N + 1), s));
+        TmpBuf tmp(tb);
+        MPET_CUDA(cub::DeviceScan::ExclusiveSum(tmp.p, tb, len.as<int64_t>(), c->A.rp, (int)(N + 1), s));
+    }
+    MPET_CUDA(cudaMemcpyAsync(&c->nnz, c->A.rp + N, sizeof(int64_t), cudaMemcpyDeviceToHost, s));
+    MPET_CUDA(cudaStreamSynchronize(s));
+    c->A.nnz = c->nnz;
+    c->A.ci = c->pool.alloc<int32_t>(c->nnz);
+    k_fill_cols<<<152 * 16, 256, 0, s>>>(N, c->Nu, c->nv, J, c->A.rp, c->n2_ptr, c->n2_col, c->n1_ptr, c->n1_col,
+                                         c->A.ci);
+    MPET_CHECK_LAUNCH();
+    c->A.lpr = choose_lpr(N, c->nnz);
+    // preconditioner block patterns: u-Laplacian on n2, P1 blocks on the vertex rows of n1
+    c->Lu.n = c->Lu.m = c->nnodes;
+    c->Lu.nnz = c->n2_nnz;
+    c->Lu.rp = c->n2_ptr;
+    c->Lu.ci = c->n2_col;
+    c->Lu.lpr = choose_lpr(c->nnodes, c->n2_nnz);
+    int64_t p1nnz = 0;
+    MPET_CUDA(cudaMemcpyAsync(&p1nnz, c->n1_ptr + c->nv, sizeof(int64_t), cudaMemcpyDeviceToHost, s));
+    MPET_CUDA(cudaStreamSynchronize(s));
+    for (int a = 0; a < J; ++a) {
+        c->Pp[a].n = c->Pp[a].m = c->nv;
+        c->Pp[a].nnz = p1nnz;
+        c->Pp[a].rp = c->n1_ptr;
+        c->Pp[a].ci = c->n1_col;
+        c->Pp[a].lpr = choose_lpr(c->nv, p1nnz);
+    }
+}
+
+static int64_t compact_flags(mpet_ctx* c, const uint8_t* flags, int64_t n, int32_t** out) {
+    TmpBuf buf(sizeof(int32_t) * (n > 0 ? n : 1));
+    TmpBuf nsel(sizeof(int));
+    size_t tb = 0;
+    thrust::counting_iterator<int32_t> it(0);
+    MPET_CUDA(cub::DeviceSelect::Flagged(nullptr, tb, it, flags, buf.as<int32_t>(), nsel.as<int>(), (int)n, c->stream));
+    {
+        TmpBuf tmp(tb);
+        MPET_CUDA(cub::DeviceSelect::Flagged(tmp.p, tb, it, flags, buf.as<int32_t>(), nsel.as<int>(), (int)n,
+                                             c->stream));
+    }
+    int cnt = 0;
+    MPET_CUDA(cudaMemcpyAsync(&cnt, nsel.p, sizeof(int), cudaMemcpyDeviceToHost, c->stream));
+    MPET_CUDA(cudaStreamSynchronize(c->stream));
+    int32_t* o = c->pool.alloc<int32_t>(cnt);
+    if (cnt) MPET_CUDA(cudaMemcpyAsync(o, buf.p, sizeof(int32_t) * cnt, cudaMemcpyDeviceToDevice, c->stream));
+    MPET_CUDA(cudaStreamSynchronize(c->stream));
+    *out = o;
+    return cnt;
+}
+
+void build_bc(mpet_ctx* c) {
+    cudaStream_t s = c->stream;
+    const int T = 256;
+    int J = c->J;
+    c->node_bc = c->pool.alloc<uint8_t>(c->nnodes);
+    c->vert_bc = c->pool.alloc<uint8_t>((int64_t)J * c->nv);
+    c->dof_bc = c->pool.alloc<uint8_t>(c->N);
+    MPET_CUDA(cudaMemsetAsync(c->node_bc, 0, c->nnodes, s));
+    MPET_CUDA(cudaMemsetAsync(c->vert_bc, 0, (size_t)J * c->nv, s));
+    MPET_CUDA(cudaMemsetAsync(c->dof_bc, 0, c->N, s));
+    if (c->nf > 0) {
+        k_bc_flags<<<grid_for(c->nf, T), T, 0, s>>>(c->bfacets, c->markers, c->nf, J, c->nv,
+                                                     (const u64*)c->edge_key, c->ne, c->node_bc, c->vert_bc);
+        MPET_CHECK_LAUNCH();
+    }
+    c->nbc_nodes[0] = compact_flags(c, c->node_bc, c->nnodes, &c->bc_nodes[0]);
+    for (int a = 0; a < J; ++a)
+        c->nbc_nodes[1 + a] = compact_flags(c, c->vert_bc + (int64_t)a * c->nv, c->nv, &c->bc_nodes[1 + a]);
+    c->bc_off[0] = 0;
+    c->bc_off[1] = 3 * c->nbc_nodes[0];
+    for (int a = 0; a < J; ++a) c->bc_off[2 + a] = c->bc_off[1 + a] + c->nbc_nodes[1 + a];
+    c->nbc_dofs = c->bc_off[1 + J];
+    c->bc_dofs = c->pool.alloc<int32_t>(c->nbc_dofs);
+    c->bc_vals = c->pool.alloc<double>(c->nbc_dofs);
+    MPET_CUDA(cudaMemsetAsync(c->bc_vals, 0, sizeof(double) * (c->nbc_dofs > 0 ? c->nbc_dofs : 1), s));
+    if (c->nbc_nodes[0])
+        k_bc_dofs_u<<<grid_for(c->nbc_nodes[0], T), T, 0, s>>>(c->bc_nodes[0], c->nbc_nodes[0], c->bc_dofs,
+                                                                c->dof_bc);
+    for (int a = 0; a < J; ++a)
+        if (c->nbc_nodes[1 + a])
+            k_bc_dofs_p<<<grid_for(c->nbc_nodes[1 + a], T), T, 0, s>>>(
+                c->bc_nodes[1 + a], c->nbc_nodes[1 + a], c->Nu + (int64_t)a * c->nv, c->bc_dofs + c->bc_off[1 + a],
+                c->dof_bc);
+    MPET_CHECK_LAUNCH();
+    MPET_CUDA(cudaStreamSynchronize(s));
+}
+
+}  // namespace mpet

@@ -1,0 +1,703 @@
+// Krylov solver of the MPET system: block-diagonally preconditioned MINRES
+// with one smoothed-aggregation AMG V-cycle per diagonal block, wrapped in
+// an FP64 iterative-refinement loop.
+//
+// Replaces the direct LUSolver(A, "mumps") of src/mpet/mpet/mpetsolver.py:347
+// and the PETScKrylovSolver("minres", "hypre_amg") of mpetsolver.py:507-557
+// (working twin mpettotalpressuresolver.py:448-493).
+//
+// Precision: MPET_PRECISION_FP64 runs everything in FP64.  MPET_PRECISION_MIXED
+// computes the outer residual r = b - A x with the FP64 matrix and solves
+// each correction with FP32 matrix values, FP32 Krylov vectors and an FP32
+// AMG (coarsest level solved in FP64), as many sweeps as needed for the
+// FP64 preconditioned residual to drop by rtol.
+//
+// Dirichlet rows: the stored matrix has DirichletBC rows replaced by unit
+// rows.  Every Krylov vector has zero Dirichlet entries (the right-hand side
+// of a correction has them, and the AMG maps them to zero), so on those
+// vectors the stored matrix acts as the symmetric elimination of
+// bc_symmetric.py:20-22 without touching the columns.
+//
+// All reductions are deterministic: a fixed grid of NB_RED blocks writes one
+// partial per block and a single block sums the partials in a fixed order.
+#include <math.h>
+
+#include "mpet_internal.cuh"
+
+namespace mpet {
+
+static inline int grid_for(int64_t n, int threads) {
+    int64_t g = (n + threads - 1) / threads;
+    if (g > 2147483647LL) g = 2147483647LL;
+    return (int)(g < 1 ? 1 : g);
+}
+
+int choose_lpr(int64_t n, int64_t nnz) {
+    double avg = n > 0 ? (double)nnz / (double)n : 0.0;
+    if (avg >= 48.0) return 32;
+    if (avg >= 20.0) return 16;
+    if (avg >= 8.0) return 8;
+    return 4;
+}
+
+// ---- reductions ------------------------------------------------------------------
+
+__device__ __forceinline__ double warp_sum(double v) {
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+    return v;
+}
+
+// Sum over a 256-thread block in a fixed order; result valid in thread 0.
+__device__ __forceinline__ double block_sum256(double v, double* sh) {
+    v = warp_sum(v);
+    const int w = threadIdx.x >> 5, l = threadIdx.x & 31;
+    if (l == 0) sh[w] = v;
+    __syncthreads();
+    double t = 0.0;
+    if (threadIdx.x < 32) {
+        t = threadIdx.x < (blockDim.x >> 5) ? sh[threadIdx.x] : 0.0;
+        t = warp_sum(t);
+    }
+    __syncthreads();
+    return t;
+}
+
+// Sum of NB_RED partials by one 256-thread block (fixed order).
+__device__ __forceinline__ double sum_partials(const double* p, double* sh) {
+    double v = 0.0;
+    for (int i = threadIdx.x; i < NB_RED; i += 256) v += p[i];
+    return block_sum256(v, sh);
+}
+
+// ---- SpMV with fused epilogues -------------------------------------------------------
+
+template <typename T, int NV>
+struct EpiStore {
+    T* y;
+    static constexpr int kRed = 0;
+    __device__ __forceinline__ void operator()(int64_t row, const T* acc, double&, double&) const {
+#pragma unroll
+        for (int k = 0; k < NV; ++k) y[NV * row + k] = acc[k];
+    }
+};
+
+// y = alpha * (A x) + beta * z   (z may alias y)
+template <typename T, int NV>
+struct EpiAxpby {
+    T* y;
+    const T* z;
+    T alpha, beta;
+    static constexpr int kRed = 0;
+    __device__ __forceinline__ void operator()(int64_t row, const T* acc, double&, double&) const {
+#pragma unroll
+        for (int k = 0; k < NV; ++k) {
+            T zz = z ? z[NV * row + k] : T(0);
+            y[NV * row + k] = alpha * acc[k] + beta * zz;
+        }
+    }
+};
+
+// One Chebyshev step on D^-1 A: d = c1 d + c2 D^-1 (b - A xin); xout = xin + d.
+template <typename T, int NV>
+struct EpiCheb {
+    const T* b;
+    const T* xin;
+    T* d;
+    T* xout;
+    const T* dinv;
+    T c1, c2;
+    static constexpr int kRed = 0;
+    __device__ __forceinline__ void operator()(int64_t row, const T* acc, double&, double&) const {
+        const T di = dinv[row];
+#pragma unroll
+        for (int k = 0; k < NV; ++k) {
+            const int64_t i = NV * row + k;
+            const T dn = c1 * d[i] + c2 * di * (b[i] - acc[k]);
+            d[i] = dn;
+            xout[i] = xin[i] + dn;
+        }
+    }
+};
+
+// MINRES Lanczos step: y = A v - (beta/oldb) r1; partial v.y
+template <typename T>
+struct EpiMinres {
+    T* y;
+    const T* r1;
+    const T* v;
+    const MinresScalars* sc;
+    static constexpr int kRed = 1;
+    __device__ __forceinline__ void operator()(int64_t row, const T* acc, double& r0, double&) const {
+        const T c = (T)sc->c_r1;
+        const T yy = acc[0] - c * r1[row];
+        y[row] = yy;
+        r0 += (double)v[row] * (double)yy;
+    }
+};
+
+// FP64 residual r = b - A x with partial sums of (r/d)^2 and (b/d)^2.
+struct EpiResid64 {
+    double* r;
+    const double* b;
+    const double* dinv;
+    static constexpr int kRed = 2;
+    __device__ __forceinline__ void operator()(int64_t row, const double* acc, double& r0, double& r1) const {
+        const double rr = b[row] - acc[0];
+        r[row] = rr;
+        const double di = dinv[row];
+        r0 += (rr * di) * (rr * di);
+        r1 += (b[row] * di) * (b[row] * di);
+    }
+};
+
+template <typename T, int NV, int LPR, class Epi>
+__global__ void __launch_bounds__(256) k_spmv(int64_t n, const int64_t* __restrict__ rp,
+                                              const int32_t* __restrict__ ci, const T* __restrict__ va,
+                                              const T* __restrict__ x, Epi epi, double* partials) {
+    constexpr int RPW = 32 / LPR;  // rows per warp per pass
+    const int lane = threadIdx.x & 31;
+    const int sub = lane & (LPR - 1);
+    const int grp = lane / LPR;
+    const int64_t warp = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) >> 5;
+    const int64_t nwarps = ((int64_t)gridDim.x * blockDim.x) >> 5;
+    double r0 = 0.0, r1 = 0.0;
+    for (int64_t base = warp * RPW; base < n; base += nwarps * RPW) {
+        const int64_t row = base + grp;
+        T acc[NV];
+#pragma unroll
+        for (int k = 0; k < NV; ++k) acc[k] = T(0);
+        if (row < n) {
+            const int64_t e1 = rp[row + 1];
+#pragma unroll 4
+            for (int64_t e = rp[row] + sub; e < e1; e += LPR) {
+                const int64_t c = ci[e];
+                const T a = va[e];
+#pragma unroll
+                for (int k = 0; k < NV; ++k) acc[k] += a * x[NV * c + k];
+            }
+        }
+#pragma unroll
+        for (int o = LPR / 2; o > 0; o >>= 1)
+#pragma unroll
+            for (int k = 0; k < NV; ++k) acc[k] += __shfl_xor_sync(0xffffffffu, acc[k], o);
+        if (row < n && sub == 0) epi(row, acc, r0, r1);
+    }
+    if constexpr (Epi::kRed > 0) {
+        __shared__ double sh[8];
+        double t0 = block_sum256(r0, sh);
+        if (threadIdx.x == 0) partials[blockIdx.x] = t0;
+        if constexpr (Epi::kRed > 1) {
+            double t1 = block_sum256(r1, sh);
+            if (threadIdx.x == 0) partials[NB_RED + blockIdx.x] = t1;
+        }
+    }
+}
+
+template <typename T, int NV, class Epi>
+static void launch_spmv(mpet_ctx* c, const Csr& A, const T* va, const T* x, const Epi& epi) {
+    int blocks;
+    if (Epi::kRed > 0) {
+        blocks = NB_RED;
+    } else {
+        int64_t rows_per_block = 256 / A.lpr;
+        blocks = grid_for(A.n, (int)rows_per_block);
+        if (blocks > 152 * 16) blocks = 152 * 16;
+    }
+    double* part = c->partials;
+    switch (A.lpr) {
+        case 32: k_spmv<T, NV, 32, Epi><<<blocks, 256, 0, c->stream>>>(A.n, A.rp, A.ci, va, x, epi, part); break;
+        case 16: k_spmv<T, NV, 16, Epi><<<blocks, 256, 0, c->stream>>>(A.n, A.rp, A.ci, va, x, epi, part); break;
+        case 8: k_spmv<T, NV, 8, Epi><<<blocks, 256, 0, c->stream>>>(A.n, A.rp, A.ci, va, x, epi, part); break;
+        default: k_spmv<T, NV, 4, Epi><<<blocks, 256, 0, c->stream>>>(A.n, A.rp, A.ci, va, x, epi, part); break;
+    }
+    MPET_CHECK_LAUNCH();
+    c->n_launch++;
+}
+
+template <typename T>
+static const T* vals(const Csr& A);
+template <>
+const double* vals<double>(const Csr& A) { return A.v64; }
+template <>
+const float* vals<float>(const Csr& A) { return A.v32; }
+
+template <typename T>
+static const T* dinv_of(const AmgLevel& L);
+template <>
+const double* dinv_of<double>(const AmgLevel& L) { return L.dinv64; }
+template <>
+const float* dinv_of<float>(const AmgLevel& L) { return L.dinv32; }
+
+template <typename T>
+void spmv(mpet_ctx* c, const Csr& A, int nvec, const T* x, T* y) {
+    if (nvec == 3) launch_spmv<T, 3>(c, A, vals<T>(A), x, EpiStore<T, 3>{y});
+    else launch_spmv<T, 1>(c, A, vals<T>(A), x, EpiStore<T, 1>{y});
+}
+template void spmv<double>(mpet_ctx*, const Csr&, int, const double*, double*);
+template void spmv<float>(mpet_ctx*, const Csr&, int, const float*, float*);
+
+// ---- vector kernels ----------------------------------------------------------------
+
+template <typename T>
+__global__ void k_cheb_first(int64_t n, int nvec, const T* __restrict__ b, const T* __restrict__ dinv, T* d, T* x,
+                             T inv_theta) {
+    int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    T v = dinv[i / nvec] * b[i] * inv_theta;
+    d[i] = v;
+    x[i] = v;
+}
+
+template <typename T>
+__global__ void k_dense_coarse(int64_t n, int nvec, const double* __restrict__ cinv, const T* __restrict__ b, T* x) {
+    const int lane = threadIdx.x & 31;
+    const int64_t warp = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) >> 5;
+    if (warp >= n * nvec) return;
+    const int64_t row = warp / nvec;
+    const int k = (int)(warp % nvec);
+    double s = 0.0;
+    for (int64_t j = lane; j < n; j += 32) s += cinv[row * n + j] * (double)b[nvec * j + k];
+    s = warp_sum(s);
+    if (lane == 0) x[nvec * row + k] = (T)s;
+}
+
+template <typename T>
+__global__ void k_dot(int64_t n, const T* __restrict__ a, const T* __restrict__ b, double* partials) {
+    __shared__ double sh[8];
+    double s = 0.0;
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
+        s += (double)a[i] * (double)b[i];
+    s = block_sum256(s, sh);
+    if (threadIdx.x == 0) partials[blockIdx.x] = s;
+}
+
+template <typename T>
+__global__ void k_copy2(int64_t n, const T* __restrict__ a, T* b, T* c) {
+    int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    T v = a[i];
+    b[i] = v;
+    c[i] = v;
+}
+
+template <typename T>
+__global__ void k_mr_v(int64_t n, const T* __restrict__ y, T* v, const MinresScalars* sc) {
+    int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    v[i] = y[i] * (T)sc->inv_beta;
+}
+
+template <typename T>
+__global__ void k_mr_axpy(int64_t n, T* y, const T* __restrict__ r2, const MinresScalars* sc) {
+    int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    y[i] -= (T)sc->c_r2 * r2[i];
+}
+
+// w = (v - oldeps w1 - delta w2) / gamma ; d += phi w  (w1, w2 already rotated)
+template <typename T>
+__global__ void k_mr_update(int64_t n, const T* __restrict__ v, const T* __restrict__ w1, const T* __restrict__ w2,
+                            T* w, T* d, const MinresScalars* sc) {
+    int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const T oe = (T)sc->oldeps, de = (T)sc->delta, ig = (T)sc->inv_gamma, ph = (T)sc->phi;
+    const T wn = (v[i] - oe * w1[i] - de * w2[i]) * ig;
+    w[i] = wn;
+    d[i] += ph * wn;
+}
+
+__global__ void k_mr_init(MinresScalars* s, const double* partials) {
+    __shared__ double sh[8];
+    double t = sum_partials(partials, sh);
+    if (threadIdx.x == 0) {
+        bool bad = !(t >= 0.0) || isnan(t);
+        double b1 = bad ? 0.0 : sqrt(t);
+        s->beta1 = b1;
+        s->beta = b1;
+        s->oldb = 0.0;
+        s->dbar = 0.0;
+        s->epsln = 0.0;
+        s->phibar = b1;
+        s->cs = -1.0;
+        s->sn = 0.0;
+        s->c_r1 = 0.0;
+        s->c_r2 = 0.0;
+        s->inv_beta = b1 > 0.0 ? 1.0 / b1 : 0.0;
+        s->rel = 1.0;
+        s->flag = bad ? 1.0 : 0.0;
+    }
+}
+
+__global__ void k_mr_alfa(MinresScalars* s, const double* partials) {
+    __shared__ double sh[8];
+    double t = sum_partials(partials, sh);
+    if (threadIdx.x == 0) {
+        s->alfa = t;
+        s->c_r2 = t * s->inv_beta;
+    }
+}
+
+__global__ void k_mr_beta(MinresScalars* s, const double* partials) {
+    __shared__ double sh[8];
+    double t = sum_partials(partials, sh);
+    if (threadIdx.x == 0) {
+        if (!(t >= 0.0) || isnan(t)) {
+            s->flag = 1.0;
+            t = 0.0;
+        }
+        const double oldb = s->beta;
+        const double beta = sqrt(t);
+        const double oldeps = s->epsln;
+        const double delta = s->cs * s->dbar + s->sn * s->alfa;
+        const double gbar = s->sn * s->dbar - s->cs * s->alfa;
+        const double epsln = s->sn * beta;
+        const double dbar = -s->cs * beta;
+        double gamma = hypot(gbar, beta);
+        if (gamma < 1e-300) gamma = 1e-300;
+        const double cs = gbar / gamma, sn = beta / gamma;
+        const double phi = cs * s->phibar;
+        const double phibar = sn * s->phibar;
+        s->oldb = oldb;
+        s->beta = beta;
+        s->oldeps = oldeps;
+        s->delta = delta;
+        s->gbar = gbar;
+        s->epsln = epsln;
+        s->dbar = dbar;
+        s->gamma = gamma;
+        s->cs = cs;
+        s->sn = sn;
+        s->phi = phi;
+        s->phibar = phibar;
+        s->inv_gamma = 1.0 / gamma;
+        s->inv_beta = beta > 0.0 ? 1.0 / beta : 0.0;
+        s->c_r1 = oldb > 0.0 ? beta / oldb : 0.0;
+        s->rel = s->beta1 > 0.0 ? phibar / s->beta1 : 0.0;
+        if (beta == 0.0 && phibar > 0.0) s->flag = 1.0;
+    }
+}
+
+__global__ void k_outer_norms(MinresScalars* s, const double* partials) {
+    __shared__ double sh[8];
+    double a = sum_partials(partials, sh);
+    double b = sum_partials(partials + NB_RED, sh);
+    if (threadIdx.x == 0) {
+        s->nr2 = a;
+        s->nb2 = b;
+    }
+}
+
+// rhs_T = r / ||D^-1 r||  (scale read on the device)
+template <typename T>
+__global__ void k_scale_to(int64_t n, const double* __restrict__ r, T* out, const MinresScalars* s) {
+    int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const double nr = sqrt(s->nr2);
+    const double sc = nr > 0.0 ? 1.0 / nr : 0.0;
+    out[i] = (T)(r[i] * sc);
+}
+
+template <typename T>
+__global__ void k_add_scaled(int64_t n, double* x, const T* __restrict__ d, const MinresScalars* s) {
+    int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    x[i] += sqrt(s->nr2) * (double)d[i];
+}
+
+__global__ void k_f64_to_f32(int64_t n, const double* __restrict__ a, float* b) {
+    int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    if (i < n) b[i] = (float)a[i];
+}
+
+// ---- AMG V-cycle -------------------------------------------------------------------------
+
+template <typename T>
+static void cheb(mpet_ctx* c, AmgHier& h, AmgLevel& L, const T* b, const T* xin, T* xout) {
+    const int nv = h.nvec;
+    const int64_t n = L.A.n * nv;
+    const double hi = 1.1 * L.rho, lo = hi / 30.0;
+    const double theta = 0.5 * (hi + lo), delta = 0.5 * (hi - lo);
+    const double sigma = theta / delta;
+    double rho_old = 1.0 / sigma;
+    const int s = h.cheb_degree;
+    T* d = (T*)L.d;
+    T* t0 = (T*)L.t0;
+    T* t1 = (T*)L.t1;
+    const T* dinv = dinv_of<T>(L);
+    T* cur = (s == 1) ? xout : t0;
+    if (!xin) {
+        k_cheb_first<T><<<grid_for(n, 256), 256, 0, c->stream>>>(n, nv, b, dinv, d, cur, (T)(1.0 / theta));
+        MPET_CHECK_LAUNCH();
+        c->n_launch++;
+    } else {
+        if (nv == 3)
+            launch_spmv<T, 3>(c, L.A, vals<T>(L.A), xin, EpiCheb<T, 3>{b, xin, d, cur, dinv, T(0), (T)(1.0 / theta)});
+        else
+            launch_spmv<T, 1>(c, L.A, vals<T>(L.A), xin, EpiCheb<T, 1>{b, xin, d, cur, dinv, T(0), (T)(1.0 / theta)});
+    }
+    for (int j = 1; j < s; ++j) {
+        const double rho_new = 1.0 / (2.0 * sigma - rho_old);
+        const T c1 = (T)(rho_new * rho_old), c2 = (T)(2.0 * rho_new / delta);
+        T* nxt = (j == s - 1) ? xout : (cur == t0 ? t1 : t0);
+        if (nv == 3)
+            launch_spmv<T, 3>(c, L.A, vals<T>(L.A), cur, EpiCheb<T, 3>{b, cur, d, nxt, dinv, c1, c2});
+        else
+            launch_spmv<T, 1>(c, L.A, vals<T>(L.A), cur, EpiCheb<T, 1>{b, cur, d, nxt, dinv, c1, c2});
+        cur = nxt;
+        rho_old = rho_new;
+    }
+}
+
+template <typename T>
+static void vcycle(mpet_ctx* c, AmgHier& h, size_t k, const T* b, T* x) {
+    const int nv = h.nvec;
+    if (k + 1 == h.lev.size()) {
+        const int64_t rows = h.ncoarse * nv;
+        k_dense_coarse<T><<<grid_for(rows * 32, 256), 256, 0, c->stream>>>(h.ncoarse, nv, h.cinv, b, x);
+        MPET_CHECK_LAUNCH();
+        c->n_launch++;
+        return;
+    }
+    AmgLevel& L = h.lev[k];
+    AmgLevel& C = h.lev[k + 1];
+    T* xs = (T*)L.x;
+    T* r = (T*)L.r;
+    cheb<T>(c, h, L, b, nullptr, xs);
+    if (nv == 3) {
+        launch_spmv<T, 3>(c, L.A, vals<T>(L.A), xs, EpiAxpby<T, 3>{r, b, T(-1), T(1)});
+        launch_spmv<T, 3>(c, L.R, vals<T>(L.R), r, EpiStore<T, 3>{(T*)C.b});
+    } else {
+        launch_spmv<T, 1>(c, L.A, vals<T>(L.A), xs, EpiAxpby<T, 1>{r, b, T(-1), T(1)});
+        launch_spmv<T, 1>(c, L.R, vals<T>(L.R), r, EpiStore<T, 1>{(T*)C.b});
+    }
+    vcycle<T>(c, h, k + 1, (const T*)C.b, (T*)C.x);
+    if (nv == 3)
+        launch_spmv<T, 3>(c, L.P, vals<T>(L.P), (const T*)C.x, EpiAxpby<T, 3>{xs, xs, T(1), T(1)});
+    else
+        launch_spmv<T, 1>(c, L.P, vals<T>(L.P), (const T*)C.x, EpiAxpby<T, 1>{xs, xs, T(1), T(1)});
+    cheb<T>(c, h, L, b, xs, x);
+}
+
+template <typename T>
+static void precond(mpet_ctx* c, const T* r, T* z) {
+    vcycle<T>(c, c->amg_u, 0, r, z);
+    for (int a = 0; a < c->J; ++a) {
+        const int64_t off = c->Nu + (int64_t)a * c->nv;
+        vcycle<T>(c, c->amg_p[a], 0, r + off, z + off);
+    }
+}
+
+// ---- MINRES ----------------------------------------------------------------------------
+
+template <typename T>
+static int minres_run(mpet_ctx* c, double target, int max_iters, int* iters_done) {
+    const int64_t n = c->N;
+    const int G = grid_for(n, 256);
+    T* v = (T*)c->kv;
+    T* d = (T*)c->kd;
+    int ir1 = 0, ir2 = 1, iy = 2;   // indices into kr
+    int iw = 0, iw1 = 1, iw2 = 2;   // indices into kw (all zero at start)
+    const int every = c->prm.check_every > 0 ? c->prm.check_every : 4;
+    int it = 0;
+    int status = MPET_OK;
+    while (it < max_iters) {
+        for (int q = 0; q < every && it < max_iters; ++q, ++it) {
+            T* r1 = (T*)c->kr[ir1];
+            T* r2 = (T*)c->kr[ir2];
+            T* y = (T*)c->kr[iy];
+            k_mr_v<T><<<G, 256, 0, c->stream>>>(n, y, v, c->sc);
+            launch_spmv<T, 1>(c, c->A, vals<T>(c->A), v, EpiMinres<T>{y, r1, v, c->sc});
+            c->n_spmv++;
+            k_mr_alfa<<<1, 256, 0, c->stream>>>(c->sc, c->partials);
+            k_mr_axpy<T><<<G, 256, 0, c->stream>>>(n, y, r2, c->sc);
+            MPET_CHECK_LAUNCH();
+            c->n_launch += 3;
+            // rotate: r1 <- r2, r2 <- y, y <- old r1
+            int old1 = ir1;
+            ir1 = ir2;
+            ir2 = iy;
+            iy = old1;
+            precond<T>(c, (const T*)c->kr[ir2], (T*)c->kr[iy]);
+            k_dot<T><<<NB_RED, 256, 0, c->stream>>>(n, (const T*)c->kr[ir2], (const T*)c->kr[iy], c->partials);
+            k_mr_beta<<<1, 256, 0, c->stream>>>(c->sc, c->partials);
+            // w rotation: w1 <- w2, w2 <- w, w <- old w1 buffer
+            int oldw1 = iw1;
+            iw1 = iw2;
+            iw2 = iw;
+            iw = oldw1;
+            // w1 <- old w2 (kw[iw1]), w2 <- old w (kw[iw2]); the new w goes into old w1's buffer
+            k_mr_update<T><<<G, 256, 0, c->stream>>>(n, v, (const T*)c->kw[iw1], (const T*)c->kw[iw2],
+                                                     (T*)c->kw[iw], d, c->sc);
+            MPET_CHECK_LAUNCH();
+            c->n_launch += 3;
+        }
+        MPET_CUDA(cudaMemcpyAsync(c->sc_host, c->sc, sizeof(MinresScalars), cudaMemcpyDeviceToHost, c->stream));
+        MPET_CUDA(cudaStreamSynchronize(c->stream));
+        if (c->sc_host->flag != 0.0) {
+            status = MPET_ERR_BREAKDOWN;
+            break;
+        }
+        if (c->sc_host->rel <= target) break;
+    }
+    *iters_done = it;
+    return status;
+}
+
+template <typename T>
+static int solve_impl(mpet_ctx* c, const double* b, double* x, mpet_stats* st) {
+    const int64_t n = c->N;
+    const int G = grid_for(n, 256);
+    launch_set_bc_in_x(c, x);
+    double eta0 = -1.0;
+    int iters = 0, outer = 0;
+    int status = MPET_OK;
+    double relres = 1.0, relres_true = 0.0;
+    const bool fp64 = sizeof(T) == 8;
+    const int max_outer = c->prm.max_outer > 0 ? c->prm.max_outer : 20;
+    const int maxit = c->prm.maxit > 0 ? c->prm.maxit : 5000;
+    for (outer = 0; outer < max_outer; ++outer) {
+        launch_spmv<double, 1>(c, c->A, c->A.v64, x, EpiResid64{c->orr, b, c->dinv});
+        c->n_spmv++;
+        k_outer_norms<<<1, 256, 0, c->stream>>>(c->sc, c->partials);
+        T* rhs = (T*)c->kr[0];
+        k_scale_to<T><<<G, 256, 0, c->stream>>>(n, c->orr, rhs, c->sc);
+        k_copy2<T><<<G, 256, 0, c->stream>>>(n, rhs, (T*)c->kr[1], (T*)c->kr[1]);
+        MPET_CHECK_LAUNCH();
+        // y = M^-1 r1 into kr[2]
+        precond<T>(c, (const T*)c->kr[0], (T*)c->kr[2]);
+        k_dot<T><<<NB_RED, 256, 0, c->stream>>>(n, (const T*)c->kr[0], (const T*)c->kr[2], c->partials);
+        k_mr_init<<<1, 256, 0, c->stream>>>(c->sc, c->partials);
+        MPET_CHECK_LAUNCH();
+        MPET_CUDA(cudaMemcpyAsync(c->sc_host, c->sc, sizeof(MinresScalars), cudaMemcpyDeviceToHost, c->stream));
+        MPET_CUDA(cudaStreamSynchronize(c->stream));
+        const MinresScalars h = *c->sc_host;
+        const double nr = sqrt(h.nr2 > 0 ? h.nr2 : 0.0);
+        relres_true = h.nb2 > 0 ? sqrt(h.nr2 / h.nb2) : 0.0;
+        if (h.flag != 0.0) {
+            status = MPET_ERR_BREAKDOWN;
+            break;
+        }
+        const double eta = h.beta1 * nr;
+        if (eta0 < 0) eta0 = eta;
+        relres = eta0 > 0 ? eta / eta0 : 0.0;
+        if (eta == 0.0 || eta <= c->prm.rtol * eta0) break;
+        if (iters >= maxit) {
+            status = MPET_ERR_MAXIT;
+            break;
+        }
+        double target = c->prm.rtol * eta0 / eta;
+        if (fp64) {
+            if (target < 1e-15) target = 1e-15;
+        } else {
+            if (target < c->prm.inner_rtol) target = c->prm.inner_rtol;
+        }
+        MPET_CUDA(cudaMemsetAsync(c->kd, 0, sizeof(T) * n, c->stream));
+        for (int q = 0; q < 3; ++q) MPET_CUDA(cudaMemsetAsync(c->kw[q], 0, sizeof(T) * n, c->stream));
+        int done = 0;
+        int s2 = minres_run<T>(c, target, maxit - iters, &done);
+        iters += done;
+        k_add_scaled<T><<<G, 256, 0, c->stream>>>(n, x, (const T*)c->kd, c->sc);
+        MPET_CHECK_LAUNCH();
+        if (s2 != MPET_OK) {
+            status = s2;
+            break;
+        }
+    }
+    if (outer >= max_outer && status == MPET_OK) status = MPET_ERR_MAXIT;
+    if (st) {
+        st->iterations = iters;
+        st->outer = outer + 1;
+        st->status = status;
+        st->relres = relres;
+        st->relres_true = relres_true;
+    }
+    return status;
+}
+
+int solve_system(mpet_ctx* c, const double* b, double* x, mpet_stats* st) {
+    if (c->prm.precision == MPET_PRECISION_MIXED) return solve_impl<float>(c, b, x, st);
+    return solve_impl<double>(c, b, x, st);
+}
+
+void alloc_krylov(mpet_ctx* c) {
+    const int64_t n = c->N;
+    c->kv = c->pool.alloc<double>(n);
+    c->kd = c->pool.alloc<double>(n);
+    for (int q = 0; q < 3; ++q) {
+        c->kr[q] = c->pool.alloc<double>(n);
+        c->kw[q] = c->pool.alloc<double>(n);
+    }
+    c->orr = c->pool.alloc<double>(n);
+    c->partials = c->pool.alloc<double>(2 * NB_RED);
+    c->sc = c->pool.alloc<MinresScalars>(1);
+    if (!c->sc_host) MPET_CUDA(cudaMallocHost(&c->sc_host, sizeof(MinresScalars)));
+}
+
+// ---- AMG upload ---------------------------------------------------------------------------
+
+static void upload_csr(mpet_ctx* c, const HostCsr& h, Csr& d, bool fp32) {
+    d.n = h.n;
+    d.m = h.m;
+    d.nnz = (int64_t)h.ci.size();
+    d.rp = c->pool.alloc<int64_t>(d.n + 1);
+    d.ci = c->pool.alloc<int32_t>(d.nnz);
+    d.v64 = c->pool.alloc<double>(d.nnz);
+    MPET_CUDA(cudaMemcpyAsync(d.rp, h.rp.data(), sizeof(int64_t) * (d.n + 1), cudaMemcpyHostToDevice, c->stream));
+    if (d.nnz) {
+        MPET_CUDA(cudaMemcpyAsync(d.ci, h.ci.data(), sizeof(int32_t) * d.nnz, cudaMemcpyHostToDevice, c->stream));
+        MPET_CUDA(cudaMemcpyAsync(d.v64, h.v.data(), sizeof(double) * d.nnz, cudaMemcpyHostToDevice, c->stream));
+    }
+    if (fp32) {
+        d.v32 = c->pool.alloc<float>(d.nnz);
+        if (d.nnz) k_f64_to_f32<<<grid_for(d.nnz, 256), 256, 0, c->stream>>>(d.nnz, d.v64, d.v32);
+        MPET_CHECK_LAUNCH();
+    }
+    d.lpr = choose_lpr(d.n, d.nnz);
+}
+
+void upload_amg(mpet_ctx* c, AmgHier& h, const HostAmg& ha, int nvec, bool fp32) {
+    h.nvec = nvec;
+    h.cheb_degree = c->prm.amg_cheb_degree > 0 ? c->prm.amg_cheb_degree : 3;
+    h.lev.clear();
+    h.lev.resize(ha.lev.size());
+    for (size_t k = 0; k < ha.lev.size(); ++k) {
+        const HostAmgLevel& hl = ha.lev[k];
+        AmgLevel& L = h.lev[k];
+        upload_csr(c, hl.A, L.A, fp32);
+        L.rho = hl.rho;
+        const int64_t n = hl.A.n;
+        L.dinv64 = c->pool.alloc<double>(n);
+        MPET_CUDA(cudaMemcpyAsync(L.dinv64, hl.dinv.data(), sizeof(double) * n, cudaMemcpyHostToDevice, c->stream));
+        if (fp32) {
+            L.dinv32 = c->pool.alloc<float>(n);
+            k_f64_to_f32<<<grid_for(n, 256), 256, 0, c->stream>>>(n, L.dinv64, L.dinv32);
+        }
+        if (k + 1 < ha.lev.size()) {
+            upload_csr(c, hl.P, L.P, fp32);
+            upload_csr(c, hl.R, L.R, fp32);
+        }
+        const int64_t nn = n * nvec;
+        L.x = c->pool.alloc<double>(nn);
+        L.b = c->pool.alloc<double>(nn);
+        L.r = c->pool.alloc<double>(nn);
+        L.d = c->pool.alloc<double>(nn);
+        L.t0 = c->pool.alloc<double>(nn);
+        L.t1 = c->pool.alloc<double>(nn);
+    }
+    h.ncoarse = ha.ncoarse;
+    h.cinv = c->pool.alloc<double>(ha.ncoarse * ha.ncoarse);
+    MPET_CUDA(cudaMemcpyAsync(h.cinv, ha.cinv.data(), sizeof(double) * ha.ncoarse * ha.ncoarse,
+                              cudaMemcpyHostToDevice, c->stream));
+    MPET_CUDA(cudaStreamSynchronize(c->stream));
+}
+
+// ---- public helpers used by the API ------------------------------------------------------
+
+void convert_values_to_f32(mpet_ctx* c) {
+    if (!c->A.v32) return;
+    k_f64_to_f32<<<grid_for(c->nnz, 256), 256, 0, c->stream>>>(c->nnz, c->A.v64, c->A.v32);
+    MPET_CHECK_LAUNCH();
+}
+
+}  // namespace mpet

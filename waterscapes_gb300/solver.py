@@ -1,0 +1,329 @@
+"""MPETSolver drop-in: the reference's API over the GB300 engine.
+
+Mirrors src/mpet/mpet/mpetsolver.py: constructor ``MPETSolver(problem,
+params)``, ``default_params`` (:86-98, plus engine keys the reference does
+not read), ``step(dt)`` (:317-379), ``solve()`` (:300-309) and
+``solve_direct()`` (:382-462) generators yielding ``(up, t)``, the fields
+``up`` / ``up_`` with ``vector()``, ``split()`` and ``assign()``, ``dt`` as a
+mutable Constant and ``solver_monitor`` with the Krylov iteration counts.
+
+Every numerical operation runs in libmpetgpu on the GPU (element kernels,
+CSR assembly, Dirichlet rows, right-hand side, MINRES + AMG); this module
+only moves parameters, evaluates the user's boundary/source expressions at
+DOF coordinates, and orders the calls as the reference does.
+"""
+from __future__ import annotations
+
+import ctypes
+import math
+import warnings
+
+import numpy as np
+
+from . import _lib
+from .problem import Constant, Expression, is_zero
+
+DIRICHLET_MARKER = 0
+NEUMANN_MARKER = 1
+ROBIN_MARKER = 2
+
+
+def _torch():
+    import torch
+    return torch
+
+
+class Function:
+    """State vector in the global block-natural DOF order (float64, on the GPU)."""
+
+    def __init__(self, solver, data):
+        self._solver = solver
+        self._v = data
+
+    def vector(self):
+        return self._v
+
+    def function_space(self):
+        return self._solver
+
+    def split(self, deepcopy=False):
+        s = self._solver
+        v = self._v.clone() if deepcopy else self._v
+        u = v[:s.Nu].view(s.nnodes, 3)
+        ps = [v[s.Nu + a * s.nv: s.Nu + (a + 1) * s.nv] for a in range(s.J)]
+        return tuple([u] + ps)
+
+    def assign(self, other):
+        src = other.vector() if isinstance(other, Function) else other
+        if not hasattr(src, "data_ptr"):
+            src = _torch().as_tensor(np.asarray(src, dtype=np.float64))
+        self._v.copy_(src.to(self._v.device, dtype=self._v.dtype))
+
+    def __len__(self):
+        return self._v.shape[0]
+
+
+class MPETSolver:
+    """Backward-Euler / theta-scheme MPET solver on one GB300."""
+
+    def __init__(self, problem, params=None):
+        torch = _torch()
+        self.problem = problem
+        self.params = self.default_params()
+        if params is not None:
+            self.params.update(params)
+        self.solver_monitor = {"niter": [], "relres": []}
+        mesh = problem.mesh
+        if mesh.gdim != 3:
+            raise NotImplementedError("the GPU engine assembles tetrahedral (3D) meshes only")
+        if problem.u_has_nullspace or any(problem.p_has_nullspace):
+            raise NotImplementedError("rigid-motion / constant nullspace multipliers are not built on the GPU")
+        pp = problem.params
+        self.J = int(pp["J"])
+        S = np.asarray([[float(v) for v in row] for row in pp["S"]], dtype=np.float64).reshape(self.J, self.J)
+        if not np.allclose(S, S.T, rtol=0, atol=0):
+            raise NotImplementedError("non-symmetric transfer matrix S needs GMRES (not built); MINRES needs S = S^T")
+        self._check_facet_data()
+        dev = int(self.params["device"])
+        self.device = torch.device("cuda", dev)
+        torch.cuda.set_device(self.device)
+        self._ctx = _lib.Context(dev)
+        self._stream = torch.cuda.current_stream(self.device)
+        self._ctx.call("mpet_set_stream", ctypes.c_void_p(self._stream.cuda_stream))
+        # mesh and markers
+        x = np.ascontiguousarray(mesh.coordinates(), dtype=np.float64)
+        cells = np.ascontiguousarray(mesh.cells(), dtype=np.int32)
+        bf = np.ascontiguousarray(mesh.boundary_facets(), dtype=np.int32)
+        markers = np.ascontiguousarray(np.stack(
+            [problem.momentum_boundary_markers.as_int32()]
+            + [problem.continuity_boundary_markers[a].as_int32() for a in range(self.J)], 0), dtype=np.int32)
+        self._ctx.call("mpet_mesh_upload", x.shape[0], _lib._ptr(x), cells.shape[0], _lib._ptr(cells),
+                       bf.shape[0], _lib._ptr(bf), _lib._ptr(markers), self.J)
+        self._prm = self._make_params()
+        self._ctx.call("mpet_setup", ctypes.byref(self._prm))
+        N, nnz, nn, ne = (ctypes.c_int64(), ctypes.c_int64(), ctypes.c_int64(), ctypes.c_int64())
+        self._ctx.call("mpet_get_sizes", ctypes.byref(N), ctypes.byref(nnz), ctypes.byref(nn), ctypes.byref(ne))
+        self.N, self.nnz, self.nnodes, self.ne = N.value, nnz.value, nn.value, ne.value
+        self.nv = mesh.num_vertices()
+        self.Nu = 3 * self.nnodes
+        f64 = dict(dtype=torch.float64, device=self.device)
+        self.up_ = Function(self, torch.zeros(self.N, **f64))
+        self.up = Function(self, torch.zeros(self.N, **f64))
+        self.dt = Constant(float(self.params["dt"]))
+        self._bcs = self.create_dirichlet_bcs()
+        self._node_x = None
+        self._assembled_dt = None
+        self._prec_dt = None
+        self._f = None
+        self._g = None
+
+    # --- parameters --------------------------------------------------------------
+    @staticmethod
+    def default_params():
+        """mpetsolver.py:86-98 plus engine keys (ignored by the reference)."""
+        return {"dt": 0.1, "t": 0.0, "T": 1.0, "theta": 1.0, "u_degree": 2, "p_degree": 1,
+                "direct_solver": True,
+                "precision": "mixed", "rtol": 1e-10, "inner_rtol": 1e-4, "maxit": 20000,
+                "max_outer": 40, "amg_theta": 0.1, "amg_cheb_degree": 3, "amg_coarse_size": 500,
+                "check_every": 4, "device": 0}
+
+    def _make_params(self):
+        pp = self.problem.params
+        mu, lmbda = self.problem.lame()
+        prm = _lib.MpetParams()
+        prm.num_networks = self.J
+        prm.precision = _lib.PRECISION[self.params["precision"]]
+        prm.mu, prm.lmbda = mu, lmbda
+        for a in range(self.J):
+            prm.alpha[a] = float(pp["alpha"][a])
+            prm.c[a] = float(pp["c"][a])
+            prm.K[a] = float(pp["K"][a])
+            for b in range(self.J):
+                prm.S[a * _lib.MAX_NETWORKS + b] = float(pp["S"][a][b])
+        prm.theta = float(self.params["theta"])
+        if int(self.params["u_degree"]) != 2 or int(self.params["p_degree"]) != 1:
+            raise NotImplementedError("the GPU engine implements the P2 x P1 pair (u_degree=2, p_degree=1)")
+        prm.rtol = float(self.params["rtol"])
+        prm.inner_rtol = float(self.params["inner_rtol"])
+        prm.maxit = int(self.params["maxit"])
+        prm.max_outer = int(self.params["max_outer"])
+        prm.amg_theta = float(self.params["amg_theta"])
+        prm.amg_cheb_degree = int(self.params["amg_cheb_degree"])
+        prm.amg_coarse_size = int(self.params["amg_coarse_size"])
+        prm.check_every = int(self.params["check_every"])
+        return prm
+
+    def _check_facet_data(self):
+        p = self.problem
+        mm = p.momentum_boundary_markers.array()
+        if (mm == NEUMANN_MARKER).any() and not is_zero(p.s):
+            raise NotImplementedError("traction boundary terms are not built on the GPU")
+        for a in range(int(p.params["J"])):
+            cm = p.continuity_boundary_markers[a].array()
+            if (cm == NEUMANN_MARKER).any() and not is_zero(p.I[a]):
+                raise NotImplementedError("flux boundary terms are not built on the GPU")
+            if (cm == ROBIN_MARKER).any():
+                raise NotImplementedError("Robin boundary terms are not built on the GPU")
+
+    # --- boundary conditions -------------------------------------------------------
+    def create_dirichlet_bcs(self):
+        """DOFs and coordinates of the topological Dirichlet conditions (mpetsolver.py:63-84)."""
+        torch = _torch()
+        bcs = []
+        for field in range(1 + self.J):
+            cnt = ctypes.c_int64()
+            self._ctx.call("mpet_get_bc_count", field, ctypes.byref(cnt))
+            n = cnt.value
+            dofs = torch.empty(max(n, 1), dtype=torch.int32, device=self.device)
+            coords = torch.empty(max(n, 1), 3, dtype=torch.float64, device=self.device)
+            self._ctx.call("mpet_get_bc", field, _lib._ptr(dofs), _lib._ptr(coords))
+            bcs.append({"field": field, "n": n, "dofs": dofs[:n], "coords": coords[:n]})
+        self.bcs = [[bcs[0]], bcs[1:]]
+        return bcs
+
+    def _eval(self, expr, x, t, vector):
+        torch = _torch()
+        n = x.shape[0]
+        if expr is None:
+            v = torch.zeros((n, 3) if vector else (n,), dtype=torch.float64, device=self.device)
+            return v
+        if isinstance(expr, Constant) or isinstance(expr, (int, float, tuple, list)):
+            val = expr.values() if isinstance(expr, Constant) else expr
+            if vector:
+                val = tuple(float(a) for a in (val if isinstance(val, (tuple, list)) else (val,) * 3))
+                return torch.tensor(val, dtype=torch.float64, device=self.device).expand(n, 3).contiguous()
+            return torch.full((n,), float(val), dtype=torch.float64, device=self.device)
+        v = expr(x, t)
+        v = torch.as_tensor(v, dtype=torch.float64, device=self.device)
+        if vector:
+            v = v.reshape(n, 3) if v.numel() == 3 * n else v.expand(n, 3)
+        else:
+            v = v.reshape(n) if v.numel() == n else v.expand(n)
+        return v.contiguous()
+
+    def _set_bc_values(self, t):
+        p = self.problem
+        b0 = self._bcs[0]
+        if b0["n"]:
+            xn = b0["coords"][0::3]
+            vals = self._eval(p.u_bar, xn, t, True).reshape(-1).contiguous()
+            self._bcv0 = vals
+            self._ctx.call("mpet_set_bc_values", 0, _lib._ptr(vals))
+        self._bcvp = []
+        for a in range(self.J):
+            ba = self._bcs[1 + a]
+            if ba["n"]:
+                vals = self._eval(p.p_bar[a], ba["coords"], t, False)
+                self._bcvp.append(vals)
+                self._ctx.call("mpet_set_bc_values", 1 + a, _lib._ptr(vals))
+
+    def _node_coordinates(self):
+        torch = _torch()
+        if self._node_x is None:
+            edges = np.empty((self.ne, 2), dtype=np.int64)
+            self._ctx.call("mpet_get_edges", _lib._ptr(edges))
+            x = self.problem.mesh.coordinates()
+            nx = np.concatenate([x, 0.5 * (x[edges[:, 0]] + x[edges[:, 1]])], 0)
+            self._node_x = torch.as_tensor(nx, dtype=torch.float64, device=self.device)
+        return self._node_x
+
+    def _set_sources(self, t_theta, t1):
+        p = self.problem
+        f = None
+        if not is_zero(p.f):
+            f = self._eval(p.f, self._node_coordinates(), t1, True).reshape(-1).contiguous()
+        g = None
+        if any(not is_zero(gi) for gi in p.g):
+            xv = self._node_coordinates()[:self.nv]
+            g = _torch().stack([self._eval(gi, xv, t_theta, False) for gi in p.g], 0).contiguous()
+        self._f, self._g = f, g
+        self._ctx.call("mpet_set_sources", _lib._ptr(f), _lib._ptr(g))
+
+    # --- assembly / solve -------------------------------------------------------------
+    def _assemble(self, dt):
+        self._ctx.call("mpet_assemble", float(dt), 1)
+        self._assembled_dt = float(dt)
+        if self._prec_dt != float(dt):
+            self._ctx.call("mpet_setup_preconditioner", float(dt))
+            self._prec_dt = float(dt)
+
+    def _advance(self, dt, t0):
+        theta = float(self.params["theta"])
+        time = self.problem.time
+        t_theta = t0 + theta * dt
+        t1 = t0 + dt
+        time.assign(t_theta)
+        g_t = t_theta
+        time.assign(t1)
+        self._set_sources(g_t, t1)
+        self._set_bc_values(t1)
+        st = _lib.MpetStats()
+        self._ctx.call("mpet_step", float(dt), _lib._ptr(self.up_.vector()), _lib._ptr(self.up.vector()),
+                       ctypes.byref(st))
+        self.solver_monitor["niter"].append(st.iterations)
+        self.solver_monitor["relres"].append(st.relres)
+        self.last_stats = st.as_dict()
+        return st
+
+    def step(self, dt=None, up_=None):
+        """One time step t -> t + dt (mpetsolver.py:317-379): assemble, BCs, solve.
+
+        Like the reference, updates ``up`` and ``time`` but not ``up_``.
+        """
+        self.params["dt"] = float(dt)
+        self.dt.assign(dt)
+        if up_ is not None:
+            self.up_.assign(up_)
+        t0 = float(self.problem.time)
+        self._assemble(float(dt))
+        return self._advance(float(dt), t0)
+
+    def solve(self):
+        """mpetsolver.py:300-309: always the direct-solve time loop."""
+        warnings.warn("Solving using direct solver, ignoring solver type.")
+        return self.solve_direct()
+
+    def solve_direct(self):
+        """Generator of (up, t) over [t, T) (mpetsolver.py:382-462).
+
+        The matrix is assembled once before the loop; each step assembles the
+        right-hand side and solves.
+        """
+        dt = float(self.params["dt"])
+        T = float(self.params["T"])
+        time = self.problem.time
+        self._bcs = self.create_dirichlet_bcs()
+        self._assemble(dt)
+        while float(time) < (T - 1.0e-9):
+            t0 = float(time)
+            self._advance(dt, t0)
+            yield self.up, float(time)
+            self.up_.assign(self.up)
+
+    # --- engine access used by tests and the bench --------------------------------------
+    @property
+    def ctx(self):
+        return self._ctx
+
+    def pattern(self):
+        rp = np.empty(self.N + 1, dtype=np.int64)
+        ci = np.empty(self.nnz, dtype=np.int32)
+        self._ctx.call("mpet_get_pattern", _lib._ptr(rp), _lib._ptr(ci))
+        return rp, ci
+
+    def matrix_values(self):
+        v = np.empty(self.nnz, dtype=np.float64)
+        self._ctx.call("mpet_get_values", _lib._ptr(v))
+        return v
+
+    def edges(self):
+        e = np.empty((self.ne, 2), dtype=np.int64)
+        self._ctx.call("mpet_get_edges", _lib._ptr(e))
+        return e
+
+    def amg_info(self, block):
+        lv = ctypes.c_int32()
+        sizes = np.zeros(16, dtype=np.int64)
+        nnz = np.zeros(16, dtype=np.int64)
+        self._ctx.call("mpet_get_amg_info", block, ctypes.byref(lv), _lib._ptr(sizes), _lib._ptr(nnz))
+        return sizes[:lv.value].tolist(), nnz[:lv.value].tolist()
