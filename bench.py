@@ -1,0 +1,384 @@
+"""Benchmark: MPET time steps per second on one GB300 (64^3 Kuhn cube, A=4).
+
+Workload (default): unit cube, 64^3 hexahedra x 6 tetrahedra (1,572,864
+cells), P2 displacement + 4 P1 pressures (N = 7,538,567 DOFs, nnz =
+1,026,610,225), mu=1e3, lambda=1e4, alpha=0.25, c=1e-4, K=(1e-4..1e-1),
+S off-diagonals 1e-2, dt=0.01, u=0 and p_a = sin(2 pi t) x0 a on the
+boundary, zero initial state.  Synthetic by construction (generated mesh).
+
+A "step" is one pass of the solve_direct time loop (mpetsolver.py:424-462):
+right-hand side assembly + block-AMG-preconditioned MINRES solve to a 1e-10
+relative preconditioned residual, with the matrix and the AMG hierarchy built
+once before the loop (the reference assembles A and factorises once there).
+``value`` is the mixed-precision (FP32 inner / FP64 refinement) rate with
+the state resident in HBM; the FP64 path, the relative error between the
+two, the FP32/FP64 SpMV bandwidth, the step() rate with per-step matrix
+assembly and an end-to-end rate through the public API with host buffers
+are reported alongside.
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--n 64] [--impl reference]
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import math
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = "MPET steps/s at 64³ A=4, mixed vs FP64 GPU at 1e-8 rel err; SpMV HBM GB/s"
+
+
+def peaks():
+    p = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    if os.path.exists(p):
+        d = json.load(open(p))
+        return float(d["hbm_gbs"]), "measured"
+    return 6800.0, "fallback"
+
+
+def workload(n, J):
+    import sys as _s
+    _s.path.insert(0, os.path.join(ROOT, "tests"))
+    from waterscapes_gb300 import CompiledSubDomain, Constant, Expression, MPETProblem, UnitCubeMesh, convert_to_E_nu
+    mesh = UnitCubeMesh(n)
+    if J == 4:
+        S = np.full((4, 4), 1e-2)
+        np.fill_diagonal(S, 0.0)
+        mat = dict(alpha=(0.25,) * 4, c=(1e-4,) * 4, K=(1e-4, 1e-3, 1e-2, 1e-1), S=tuple(map(tuple, S)))
+        dt = 0.01
+    else:
+        mat = dict(alpha=(0.5, 0.5), c=(1e-4, 1e-4), K=(1e-3, 1e-2), S=((0.0, 0.1), (0.1, 0.0)))
+        dt = 0.0125
+    E, nu = convert_to_E_nu(1.0e3, 1.0e4)
+    time_c = Constant(0.0)
+    problem = MPETProblem(mesh, time_c, params=dict(J=J, E=E, nu=nu, **mat))
+    CompiledSubDomain.on_boundary().mark(problem.momentum_boundary_markers, 0)
+    for a in range(J):
+        CompiledSubDomain.on_boundary().mark(problem.continuity_boundary_markers[a], 0)
+    problem.p_bar = [Expression((lambda a: (lambda x, t: math.sin(2 * math.pi * t) * x[:, 0] * (a + 1)))(a))
+                     for a in range(J)]
+    return problem, dt
+
+
+class ClockSampler:
+    """nvidia-smi clocks/throttle reasons sampled every 200 ms during the timed region."""
+
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index=0):
+        self.index = index
+        self.proc = None
+        self.lines = []
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "-i", str(self.index), "--query-gpu=" + self.FIELDS, "--format=csv,noheader,nounits",
+                 "-lms", "200"], stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.t = threading.Thread(target=self._read, daemon=True)
+            self.t.start()
+        except Exception:
+            self.proc = None
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def stop(self):
+        if self.proc is None:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except Exception:
+            self.proc.kill()
+        sm, smax, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in self.lines:
+            parts = [p.strip() for p in ln.split(",")]
+            if len(parts) < 9:
+                continue
+            try:
+                sm.append(float(parts[1]))
+                smax.append(float(parts[2]))
+            except ValueError:
+                continue
+            for nm, v in zip(names, parts[5:9]):
+                if v.lower() == "active":
+                    reasons.add(nm)
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": max(smax) if smax else None,
+                "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def time_spmv(solver, torch, lib, reps=20):
+    """FP32 and FP64 SpMV with the assembled matrix, CUDA events on the engine's stream."""
+    N, nnz = solver.N, solver.nnz
+    out = {}
+    stream = solver._stream
+    for prec, dtype, sv in ((1, torch.float32, 4), (0, torch.float64, 8)):
+        if prec == 1 and solver.params["precision"] != "mixed":
+            continue
+        x = torch.randn(N, dtype=dtype, device=solver.device)
+        y = torch.empty(N, dtype=dtype, device=solver.device)
+        for _ in range(3):
+            solver.ctx.call("mpet_spmv", prec, lib._ptr(x), lib._ptr(y))
+        torch.cuda.synchronize()
+        e0 = torch.cuda.Event(enable_timing=True)
+        e1 = torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        for _ in range(reps):
+            solver.ctx.call("mpet_spmv", prec, lib._ptr(x), lib._ptr(y))
+        e1.record(stream)
+        torch.cuda.synchronize()
+        ms = e0.elapsed_time(e1) / reps
+        bytes_ = nnz * (sv + 4) + (N + 1) * 8 + 2 * N * sv
+        out["fp32" if prec == 1 else "fp64"] = {"ms": ms, "alg_bytes": bytes_, "gbs": bytes_ / ms / 1e6}
+    return out
+
+
+def run_steps(solver, torch, steps, warmup, dt):
+    """solve_direct steps with the state on the device; returns (ms total, iterations, states)."""
+    problem = solver.problem
+    problem.time.assign(0.0)
+    solver.up_.vector().zero_()
+    gen = solver.solve_direct()
+    for _ in range(warmup):
+        next(gen)
+    torch.cuda.synchronize()
+    stream = solver._stream
+    e0 = torch.cuda.Event(enable_timing=True)
+    e1 = torch.cuda.Event(enable_timing=True)
+    it0 = len(solver.solver_monitor["niter"])
+    e0.record(stream)
+    for _ in range(steps):
+        next(gen)
+    e1.record(stream)
+    torch.cuda.synchronize()
+    ms = e0.elapsed_time(e1)
+    its = solver.solver_monitor["niter"][it0:]
+    return ms, its, solver.up.vector().clone()
+
+
+def launches(solver):
+    import ctypes
+    n = ctypes.c_int64()
+    solver.ctx.call("mpet_get_timing", None, None, None, ctypes.byref(n))
+    return n.value
+
+
+def cpu_baseline_sample(n_sample=12, J=4, steps=1):
+    """Oracle (numpy/scipy FP64, 1 thread) solve_direct steps on a small cube, scaled by N."""
+    sys.path.insert(0, os.path.join(ROOT, "tests"))
+    from oracle import krylov
+    from oracle.mpet import OracleMPET
+    problem, dt = workload(n_sample, J)
+    m = problem.mesh
+    om = OracleMPET(m.coordinates(), m.cells(), m.boundary_facets(), m.boundary_facet_cells(), problem.params, 1.0,
+                    problem.momentum_boundary_markers.array(),
+                    [problem.continuity_boundary_markers[a].array() for a in range(J)])
+    data = {"p_bar": [(lambda a: (lambda x, t: math.sin(2 * math.pi * t) * x[:, 0] * (a + 1)))(a) for a in range(J)]}
+    A = om.assemble_matrix(dt)
+    dofs0, _ = om.dirichlet_values(0.0, data)
+    Abc = om.apply_bc_matrix(A, dofs0)
+    blocks = om.preconditioner_blocks(dt)
+    hu = krylov.SAHierarchy(blocks[0], theta=0.1, cheb_degree=3)
+    hp = [krylov.SAHierarchy(B, theta=0.1, cheb_degree=3) for B in blocks[1:]]
+    M = krylov.block_preconditioner(hu, hp, 3, om.dm.Nu, om.dm.nv)
+    up = np.zeros(om.dm.N)
+    t = 0.0
+    t0 = time.perf_counter()
+    for _ in range(steps):
+        b = om.rhs_L(up, dt) + om.rhs_L1(up, dt, t + dt, data) + om.rhs_L0(t + dt, data)
+        dofs, vals = om.dirichlet_values(t + dt, data)
+        b = om.apply_bc_vector(b, dofs, vals)
+        x0 = up.copy()
+        for d_, v_ in zip(dofs, vals):
+            x0[d_] = v_
+        d, it, _ = krylov.minres(Abc, b - Abc @ x0, M, rtol=1e-10, maxiter=5000)
+        up = x0 + d
+        t += dt
+    sec = (time.perf_counter() - t0) / steps
+    return sec, om.dm.N
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=10)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--n", type=int, default=64)
+    ap.add_argument("--networks", type=int, default=4)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--no-fp64", action="store_true")
+    ap.add_argument("--no-cpu", action="store_true")
+    args = ap.parse_args()
+    n, J = args.n, args.networks
+    N_full = 3 * (2 * n + 1) ** 3 + J * (n + 1) ** 3
+    workload_name = "Kuhn cube %d^3 x 6 tets, A=%d networks, P2/P1 (N=%d)" % (n, J, N_full)
+
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    local_rank = int(os.environ.get("LOCAL_RANK", "0"))
+
+    if args.impl == "reference":
+        if rank != 0:
+            return
+        steps = max(1, args.steps)
+        sec, Ns = cpu_baseline_sample(12, J, steps=min(steps, 3))
+        scaled = 1.0 / (sec * N_full / Ns)
+        line = {"impl": "reference", "metric": METRIC, "value": scaled, "unit": "steps/s", "n_gpus": 0,
+                "steps": min(steps, 3), "warmup": 0, "ms_per_step": 1e3 / scaled, "higher_is_better": True,
+                "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+                "config": {"workload": workload_name},
+                "cpu_baseline": {"value": scaled, "unit": "steps/s", "cores": 1, "kind": "port",
+                                 "sample": "oracle (numpy/scipy FP64 MINRES + SA-AMG, solve_direct step) on the 12^3 "
+                                           "A=4 cube (N=%d), per-step time scaled by N ratio %.1f; FEniCS/PETSc "
+                                           "(the reference's own path) is not installable here" % (Ns, N_full / Ns)},
+                "e2e": {"value": scaled, "unit": "steps/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+        print(json.dumps(line))
+        return
+
+    import torch
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("gloo")
+    torch.cuda.set_device(local_rank)
+    from waterscapes_gb300 import MPETSolver, _lib
+    lib = _lib
+    hbm, peak_kind = peaks()
+
+    problem, dt = workload(n, J)
+    base = dict(dt=dt, T=1e9, theta=1.0, rtol=1e-10, device=local_rank)
+    t0 = time.perf_counter()
+    sol = MPETSolver(problem, dict(base, precision="mixed"))
+    t_setup = time.perf_counter() - t0
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    sol._assemble(dt)
+    torch.cuda.synchronize()
+    t_asm_amg = time.perf_counter() - t0
+    # matrix assembly alone (step() semantics re-assemble every step)
+    e0 = torch.cuda.Event(enable_timing=True)
+    e1 = torch.cuda.Event(enable_timing=True)
+    e0.record(sol._stream)
+    sol.ctx.call("mpet_assemble", dt, 1)
+    e1.record(sol._stream)
+    torch.cuda.synchronize()
+    asm_ms = e0.elapsed_time(e1)
+    spmv = time_spmv(sol, torch, lib)
+
+    clk = ClockSampler(local_rank)
+    if world > 1:
+        torch.distributed.barrier()
+    L0 = launches(sol)
+    clk.start()
+    ms_mixed, its_mixed, x_mixed = run_steps(sol, torch, args.steps, args.warmup, dt)
+    clocks = clk.stop()
+    L1 = launches(sol)
+    ms_max = ms_mixed
+    if world > 1:
+        t = torch.tensor([ms_mixed], dtype=torch.float64)
+        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+        ms_max = float(t.item())
+    value = world * args.steps / (ms_max / 1e3)
+
+    # end to end through the public API with host buffers (pinned), copies timed
+    problem.time.assign(0.0)
+    host_prev = torch.zeros(sol.N, dtype=torch.float64).pin_memory()
+    host_out = torch.empty(sol.N, dtype=torch.float64).pin_memory()
+    for _ in range(2):
+        sol.up_.vector().copy_(host_prev, non_blocking=True)
+        sol.step(dt)
+        host_out.copy_(sol.up.vector(), non_blocking=True)
+    torch.cuda.synchronize()
+    problem.time.assign(0.0)
+    host_prev.zero_()
+    e0.record(sol._stream)
+    ke = max(2, min(args.steps, 5))
+    for _ in range(ke):
+        sol.up_.vector().copy_(host_prev, non_blocking=True)
+        sol.advance(dt)
+        host_out.copy_(sol.up.vector(), non_blocking=True)
+        torch.cuda.current_stream().synchronize()
+        host_prev.copy_(host_out)
+    e1.record(sol._stream)
+    torch.cuda.synchronize()
+    e2e_ms = e0.elapsed_time(e1) / ke
+
+    # step() semantics: assemble every step
+    step_ms = asm_ms + ms_mixed / args.steps
+
+    res = {"mixed": {"ms_per_step": ms_mixed / args.steps, "iterations": its_mixed}}
+    rel_err = None
+    if not args.no_fp64:
+        sol64 = MPETSolver(problem, dict(base, precision="fp64"))
+        sol64._assemble(dt)
+        spmv64 = time_spmv(sol64, torch, lib)
+        spmv["fp64_only_ctx"] = spmv64.get("fp64")
+        ms64, its64, x64 = run_steps(sol64, torch, args.steps, args.warmup, dt)
+        rel_err = float(torch.linalg.norm(x_mixed - x64) / torch.linalg.norm(x64))
+        res["fp64"] = {"ms_per_step": ms64 / args.steps, "iterations": its64}
+        del sol64
+
+    cpu = None
+    if rank == 0 and not args.no_cpu:
+        sec, Ns = cpu_baseline_sample(12, J, steps=1)
+        cpu_val = 1.0 / (sec * N_full / Ns)
+        cpu = {"value": cpu_val, "unit": "steps/s", "cores": 1, "kind": "port",
+               "sample": "oracle (numpy/scipy FP64 MINRES + SA-AMG) one solve_direct step on the 12^3 A=4 cube "
+                         "(N=%d, %.1f s), scaled by the DOF ratio %.1f" % (Ns, sec, N_full / Ns)}
+
+    if rank != 0:
+        return
+    sp32 = spmv.get("fp32") or spmv.get("fp64")
+    line = {
+        "metric": METRIC,
+        "value": value,
+        "unit": "steps/s",
+        "n_gpus": world,
+        "steps": args.steps,
+        "warmup": args.warmup,
+        "ms_per_step": ms_max / args.steps,
+        "higher_is_better": True,
+        "scaling": "weak",
+        "vs_baseline": None,
+        "dtype": "f32 inner + f64 refinement",
+        "data": "synthetic",
+        "config": {"workload": workload_name, "nnz": sol.nnz, "dt": dt, "rtol": 1e-10,
+                   "semantics": "solve_direct step: rhs + MINRES/block-SA-AMG solve (matrix and AMG built once)",
+                   "l2": "inputs larger than L2 (CSR %.1f GB)" % (sol.nnz * 16 / 1e9),
+                   "parallelism": "replicas" if world > 1 else "single GPU"},
+        "fp64_steps_per_s": (1e3 / res["fp64"]["ms_per_step"]) if "fp64" in res else None,
+        "mixed_over_fp64": (res["fp64"]["ms_per_step"] / res["mixed"]["ms_per_step"]) if "fp64" in res else None,
+        "rel_err_mixed_vs_fp64": rel_err,
+        "iterations_per_step": {"mixed": its_mixed, "fp64": res.get("fp64", {}).get("iterations")},
+        "step_semantics": {"ms_per_step": step_ms, "assemble_ms": asm_ms},
+        "setup_s": {"mesh_dofmap_pattern": t_setup, "assemble_plus_amg": t_asm_amg},
+        "spmv": spmv,
+        "roofline": {"kernel": "k_spmv<float,1,32,EpiMinres> (FP32 CSR SpMV)" if "fp32" in spmv else "k_spmv<double>",
+                     "bound": "hbm", "achieved": sp32["gbs"], "peak": hbm, "unit": "GB/s",
+                     "frac": sp32["gbs"] / hbm, "peak_kind": peak_kind,
+                     "alg_bytes_per_launch": sp32["alg_bytes"], "traffic": None},
+        "cpu_baseline": cpu,
+        "e2e": {"value": 1e3 / e2e_ms, "unit": "steps/s", "h2d_bytes_per_step": sol.N * 8,
+                "d2h_bytes_per_step": sol.N * 8},
+        "clocks": clocks,
+        "gpu_launches": (L1 - L0),
+    }
+    print(json.dumps(line))
+
+
+if __name__ == "__main__":
+    main()

@@ -8,7 +8,8 @@ twin src/mpet/mpet/mpettotalpressuresolver.py:414-505).  PETSc KSP MINRES
 classical BoomerAMG is replaced by smoothed aggregation (one hierarchy per
 diagonal block), which is the method the GPU path implements.
 
-The AMG follows the standard SA recipe: symmetric strength of connection,
+The AMG follows the standard SA recipe: symmetric strength of connection
+(threshold halved per level, 0 when a level has no strong connection),
 greedy three-pass aggregation, piecewise-constant tentative prolongator
 (near-nullspace = constants per scalar block), Jacobi-smoothed prolongator
 P = (I - omega/rho D^-1 A) T with omega = 4/3, Galerkin coarse operators
@@ -108,8 +109,11 @@ class SAHierarchy:
             self.levels.append(lev)
             if n <= coarse_size or len(self.levels) >= max_levels:
                 break
-            S = strength(A, theta)
+            th = theta * 0.5 ** (len(self.levels) - 1)
+            S = strength(A, th)
             agg, nagg = aggregate(S)
+            if nagg == 0 and th > 0.0:
+                agg, nagg = aggregate(strength(A, 0.0))
             if nagg == 0 or nagg >= n:
                 break
             rows = np.nonzero(agg >= 0)[0]

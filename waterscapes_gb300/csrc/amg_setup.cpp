@@ -4,7 +4,8 @@
 // (PETScKrylovSolver("minres", "hypre_amg"), src/mpet/mpet/mpetsolver.py:507)
 // applied to the block-diagonal form of mpetsolver.py:264-271.  This file
 // builds instead one smoothed-aggregation hierarchy per diagonal block:
-//   strength   |a_ij| >= theta sqrt(|a_ii a_jj|), i != j
+//   strength   |a_ij| >= theta_l sqrt(|a_ii a_jj|), i != j, theta_l = theta 2^-l
+//              (0 on a level that has no strong connection)
 //   aggregates three greedy passes (root + free neighbourhood, attach,
 //              leftovers), isolated rows (Dirichlet unit rows) unaggregated
 //   T          piecewise constant, columns scaled to unit 2-norm
@@ -238,11 +239,43 @@ static bool cholesky_inverse(std::vector<double>& a, int64_t n, std::vector<doub
     return true;
 }
 
+// Threads for the setup: the affinity set, capped by a cgroup CPU quota
+// (containers often expose every core but grant only a fraction).
+static int host_threads() {
+    int n = 1;
+#ifdef _OPENMP
+    n = omp_get_num_procs();
+#endif
+    long quota = -1, period = -1;
+    if (FILE* f = fopen("/sys/fs/cgroup/cpu.max", "r")) {
+        char q[64] = {0};
+        if (fscanf(f, "%63s %ld", q, &period) == 2 && strcmp(q, "max") != 0) quota = atol(q);
+        fclose(f);
+    } else if (FILE* f1 = fopen("/sys/fs/cgroup/cpu/cpu.cfs_quota_us", "r")) {
+        if (fscanf(f1, "%ld", &quota) != 1) quota = -1;
+        fclose(f1);
+        if (FILE* f2 = fopen("/sys/fs/cgroup/cpu/cpu.cfs_period_us", "r")) {
+            if (fscanf(f2, "%ld", &period) != 1) period = -1;
+            fclose(f2);
+        }
+    }
+    if (quota > 0 && period > 0) {
+        long q = quota / period;
+        if (q < 1) q = 1;
+        if (q < n) n = (int)q;
+    }
+    if (n > 32) n = 32;
+    return n < 1 ? 1 : n;
+}
+
 void amg_setup_host(const HostCsr& A0, double theta, int coarse_size, int max_levels, HostAmg& out) {
     out.lev.clear();
     HostCsr A = A0;
     if (coarse_size < 1) coarse_size = 500;
     if (max_levels < 1) max_levels = 12;
+#ifdef _OPENMP
+    omp_set_num_threads(host_threads());
+#endif
     while (true) {
         HostAmgLevel L;
         const int64_t n = A.n;
@@ -256,10 +289,17 @@ void amg_setup_host(const HostCsr& A0, double theta, int coarse_size, int max_le
         out.lev.push_back(L);
         HostAmgLevel& cur = out.lev.back();
         if (n <= coarse_size || (int)out.lev.size() >= max_levels) break;
+        // the threshold halves per level; a level without any strong
+        // connection is aggregated on its full graph (threshold 0)
+        const double th = theta * pow(0.5, (double)(out.lev.size() - 1));
         HostCsr S;
-        strength(A, theta, S);
+        strength(A, th, S);
         std::vector<int64_t> agg;
-        const int64_t nagg = aggregate(S, agg);
+        int64_t nagg = aggregate(S, agg);
+        if (nagg == 0 && th > 0.0) {
+            strength(A, 0.0, S);
+            nagg = aggregate(S, agg);
+        }
         if (nagg == 0 || nagg >= n) break;
         std::vector<int64_t> size(nagg, 0);
         for (int64_t i = 0; i < n; ++i)

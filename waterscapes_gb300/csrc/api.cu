@@ -8,10 +8,6 @@
 
 #include "mpet_internal.cuh"
 
-namespace mpet {
-void convert_values_to_f32(mpet_ctx* c);
-}
-
 using namespace mpet;
 
 #define API_BEGIN(ctx)                  \
@@ -63,6 +59,8 @@ int mpet_ctx_destroy(mpet_ctx* c) {
     if (!c) return MPET_ERR_INVALID;
     cudaSetDevice(c->device);
     if (c->stream) cudaStreamSynchronize(c->stream);
+    destroy_minres_graph(c);
+    if (c->cap_stream) cudaStreamDestroy(c->cap_stream);
     c->pool.free_all();
     if (c->sc_host) cudaFreeHost(c->sc_host);
     if (c->ev0) cudaEventDestroy(c->ev0);
@@ -298,6 +296,7 @@ int mpet_setup_preconditioner(mpet_ctx* c, double dt) {
     API_BEGIN(c)
     require(c->setup_done, MPET_ERR_STATE, "mpet_setup must come first");
     require(dt > 0.0, MPET_ERR_INVALID, "dt must be positive");
+    destroy_minres_graph(c);
     launch_assemble_prec_blocks(c, dt);
     const bool fp32 = c->prm.precision == MPET_PRECISION_MIXED;
     auto fetch = [&](const Csr& d, HostCsr& h) {

@@ -194,6 +194,11 @@ struct mpet_ctx {
     mpet::MinresScalars* sc = nullptr;
     mpet::MinresScalars* sc_host = nullptr;  // pinned
 
+    // MINRES iterations replayed from a CUDA graph (3 iterations per launch)
+    cudaStream_t cap_stream = nullptr;
+    cudaGraphExec_t mr_graph = nullptr;
+    int64_t mr_graph_launches = 0;  // kernels per graph launch
+
     // timing
     cudaEvent_t ev0 = nullptr, ev1 = nullptr;
     double t_spmv_ms = 0.0, t_prec_ms = 0.0;
@@ -203,7 +208,7 @@ struct mpet_ctx {
 
 namespace mpet {
 
-constexpr int NB_RED = 608;   // fixed block count of every reduction kernel (152 SMs x 4)
+constexpr int NB_RED = 1216;  // fixed block count of every reduction kernel (152 SMs x 8)
 constexpr int RED_THREADS = 256;
 
 // setup.cu
@@ -226,5 +231,7 @@ void upload_amg(mpet_ctx* c, AmgHier& h, const HostAmg& ha, int nvec, bool fp32)
 int solve_system(mpet_ctx* c, const double* b, double* x, mpet_stats* st);
 void alloc_krylov(mpet_ctx* c);
 int choose_lpr(int64_t n, int64_t nnz);
+void destroy_minres_graph(mpet_ctx* c);
+void convert_values_to_f32(mpet_ctx* c);
 
 }  // namespace mpet

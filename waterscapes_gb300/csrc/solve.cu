@@ -168,13 +168,25 @@ __global__ void __launch_bounds__(256) k_spmv(int64_t n, const int64_t* __restri
 #pragma unroll
         for (int k = 0; k < NV; ++k) acc[k] = T(0);
         if (row < n) {
-            const int64_t e1 = rp[row + 1];
-#pragma unroll 4
-            for (int64_t e = rp[row] + sub; e < e1; e += LPR) {
-                const int64_t c = ci[e];
-                const T a = va[e];
+            // U independent (column, value) loads per lane are issued before
+            // any dependent x gather; matrix streams use evict-first loads so
+            // the x vector stays resident in L2.
+            constexpr int U = 4;
+            const int64_t e0 = rp[row], e1 = rp[row + 1];
+            for (int64_t b = e0; b < e1; b += LPR * U) {
+                int32_t cc[U];
+                T aa[U];
 #pragma unroll
-                for (int k = 0; k < NV; ++k) acc[k] += a * x[NV * c + k];
+                for (int u = 0; u < U; ++u) {
+                    const int64_t e = b + sub + u * LPR;
+                    const bool ok = e < e1;
+                    cc[u] = ok ? __ldcs(ci + e) : 0;
+                    aa[u] = ok ? __ldcs(va + e) : T(0);
+                }
+#pragma unroll
+                for (int u = 0; u < U; ++u)
+#pragma unroll
+                    for (int k = 0; k < NV; ++k) acc[k] += aa[u] * x[(int64_t)NV * cc[u] + k];
             }
         }
 #pragma unroll
@@ -490,48 +502,94 @@ static void precond(mpet_ctx* c, const T* r, T* z) {
 
 // ---- MINRES ----------------------------------------------------------------------------
 
+// Three MINRES iterations.  The Lanczos vectors rotate through kr[0..2]
+// (r1, r2, y) and the direction vectors through kw[0..2] (w, w1, w2); both
+// rotations have period 3, so three iterations start and end in the same
+// buffer assignment and can be captured once and replayed as a CUDA graph.
 template <typename T>
-static int minres_run(mpet_ctx* c, double target, int max_iters, int* iters_done) {
+static void minres_three(mpet_ctx* c) {
     const int64_t n = c->N;
     const int G = grid_for(n, 256);
     T* v = (T*)c->kv;
     T* d = (T*)c->kd;
-    int ir1 = 0, ir2 = 1, iy = 2;   // indices into kr
-    int iw = 0, iw1 = 1, iw2 = 2;   // indices into kw (all zero at start)
-    const int every = c->prm.check_every > 0 ? c->prm.check_every : 4;
+    int ir1 = 0, ir2 = 1, iy = 2;
+    int iw = 0, iw1 = 1, iw2 = 2;
+    for (int q = 0; q < 3; ++q) {
+        T* r1 = (T*)c->kr[ir1];
+        T* r2 = (T*)c->kr[ir2];
+        T* y = (T*)c->kr[iy];
+        k_mr_v<T><<<G, 256, 0, c->stream>>>(n, y, v, c->sc);
+        launch_spmv<T, 1>(c, c->A, vals<T>(c->A), v, EpiMinres<T>{y, r1, v, c->sc});
+        c->n_spmv++;
+        k_mr_alfa<<<1, 256, 0, c->stream>>>(c->sc, c->partials);
+        k_mr_axpy<T><<<G, 256, 0, c->stream>>>(n, y, r2, c->sc);
+        MPET_CHECK_LAUNCH();
+        c->n_launch += 3;
+        const int old1 = ir1;
+        ir1 = ir2;
+        ir2 = iy;
+        iy = old1;
+        precond<T>(c, (const T*)c->kr[ir2], (T*)c->kr[iy]);
+        k_dot<T><<<NB_RED, 256, 0, c->stream>>>(n, (const T*)c->kr[ir2], (const T*)c->kr[iy], c->partials);
+        k_mr_beta<<<1, 256, 0, c->stream>>>(c->sc, c->partials);
+        const int oldw1 = iw1;
+        iw1 = iw2;
+        iw2 = iw;
+        iw = oldw1;
+        k_mr_update<T><<<G, 256, 0, c->stream>>>(n, v, (const T*)c->kw[iw1], (const T*)c->kw[iw2],
+                                                 (T*)c->kw[iw], d, c->sc);
+        MPET_CHECK_LAUNCH();
+        c->n_launch += 3;
+    }
+}
+
+template <typename T>
+static void capture_minres_graph(mpet_ctx* c) {
+    if (!c->cap_stream) MPET_CUDA(cudaStreamCreateWithFlags(&c->cap_stream, cudaStreamNonBlocking));
+    cudaStream_t saved = c->stream;
+    const int64_t l0 = c->n_launch, s0 = c->n_spmv;
+    c->stream = c->cap_stream;
+    cudaGraph_t g = nullptr;
+    cudaError_t e = cudaStreamBeginCapture(c->cap_stream, cudaStreamCaptureModeThreadLocal);
+    if (e == cudaSuccess) {
+        try {
+            minres_three<T>(c);
+        } catch (...) {
+            cudaStreamEndCapture(c->cap_stream, &g);
+            if (g) cudaGraphDestroy(g);
+            c->stream = saved;
+            throw;
+        }
+        e = cudaStreamEndCapture(c->cap_stream, &g);
+    }
+    c->stream = saved;
+    c->mr_graph_launches = c->n_launch - l0;
+    c->n_launch = l0;
+    c->n_spmv = s0;
+    if (e != cudaSuccess) fail(MPET_ERR_CUDA, std::string("MINRES graph capture: ") + cudaGetErrorString(e));
+    e = cudaGraphInstantiate(&c->mr_graph, g, 0);
+    cudaGraphDestroy(g);
+    if (e != cudaSuccess) {
+        c->mr_graph = nullptr;
+        fail(MPET_ERR_CUDA, std::string("MINRES graph instantiate: ") + cudaGetErrorString(e));
+    }
+}
+
+void destroy_minres_graph(mpet_ctx* c) {
+    if (c->mr_graph) cudaGraphExecDestroy(c->mr_graph);
+    c->mr_graph = nullptr;
+}
+
+template <typename T>
+static int minres_run(mpet_ctx* c, double target, int max_iters, int* iters_done) {
+    if (!c->mr_graph) capture_minres_graph<T>(c);
     int it = 0;
     int status = MPET_OK;
     while (it < max_iters) {
-        for (int q = 0; q < every && it < max_iters; ++q, ++it) {
-            T* r1 = (T*)c->kr[ir1];
-            T* r2 = (T*)c->kr[ir2];
-            T* y = (T*)c->kr[iy];
-            k_mr_v<T><<<G, 256, 0, c->stream>>>(n, y, v, c->sc);
-            launch_spmv<T, 1>(c, c->A, vals<T>(c->A), v, EpiMinres<T>{y, r1, v, c->sc});
-            c->n_spmv++;
-            k_mr_alfa<<<1, 256, 0, c->stream>>>(c->sc, c->partials);
-            k_mr_axpy<T><<<G, 256, 0, c->stream>>>(n, y, r2, c->sc);
-            MPET_CHECK_LAUNCH();
-            c->n_launch += 3;
-            // rotate: r1 <- r2, r2 <- y, y <- old r1
-            int old1 = ir1;
-            ir1 = ir2;
-            ir2 = iy;
-            iy = old1;
-            precond<T>(c, (const T*)c->kr[ir2], (T*)c->kr[iy]);
-            k_dot<T><<<NB_RED, 256, 0, c->stream>>>(n, (const T*)c->kr[ir2], (const T*)c->kr[iy], c->partials);
-            k_mr_beta<<<1, 256, 0, c->stream>>>(c->sc, c->partials);
-            // w rotation: w1 <- w2, w2 <- w, w <- old w1 buffer
-            int oldw1 = iw1;
-            iw1 = iw2;
-            iw2 = iw;
-            iw = oldw1;
-            // w1 <- old w2 (kw[iw1]), w2 <- old w (kw[iw2]); the new w goes into old w1's buffer
-            k_mr_update<T><<<G, 256, 0, c->stream>>>(n, v, (const T*)c->kw[iw1], (const T*)c->kw[iw2],
-                                                     (T*)c->kw[iw], d, c->sc);
-            MPET_CHECK_LAUNCH();
-            c->n_launch += 3;
-        }
+        MPET_CUDA(cudaGraphLaunch(c->mr_graph, c->stream));
+        it += 3;
+        c->n_launch += c->mr_graph_launches;
+        c->n_spmv += 3;
         MPET_CUDA(cudaMemcpyAsync(c->sc_host, c->sc, sizeof(MinresScalars), cudaMemcpyDeviceToHost, c->stream));
         MPET_CUDA(cudaStreamSynchronize(c->stream));
         if (c->sc_host->flag != 0.0) {

@@ -247,6 +247,16 @@ class MPETSolver:
             self._ctx.call("mpet_setup_preconditioner", float(dt))
             self._prec_dt = float(dt)
 
+    def advance(self, dt=None):
+        """One pass of the solve_direct loop body from ``up_`` at the current time
+        with the matrix already assembled: time-dependent data at t0 + theta dt
+        and t1, right-hand side, solve into ``up``; updates ``time`` but not ``up_``.
+        Assembles first if no matrix for this dt exists."""
+        dt = float(self.params["dt"] if dt is None else dt)
+        if self._assembled_dt != dt:
+            self._assemble(dt)
+        return self._advance(dt, float(self.problem.time))
+
     def _advance(self, dt, t0):
         theta = float(self.params["theta"])
         time = self.problem.time
