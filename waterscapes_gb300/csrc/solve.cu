@@ -178,10 +178,14 @@ __global__ void __launch_bounds__(256) k_spmv(int64_t n, const int64_t* __restri
                 T aa[U];
 #pragma unroll
                 for (int u = 0; u < U; ++u) {
+                    // the address is clamped into the row (non-empty here), so
+                    // a load issued regardless of the predicate stays in bounds
                     const int64_t e = b + sub + u * LPR;
                     const bool ok = e < e1;
-                    cc[u] = ok ? __ldcs(ci + e) : 0;
-                    aa[u] = ok ? __ldcs(va + e) : T(0);
+                    const int64_t es = ok ? e : e1 - 1;
+                    cc[u] = __ldcs(ci + es);
+                    const T a = __ldcs(va + es);
+                    aa[u] = ok ? a : T(0);
                 }
 #pragma unroll
                 for (int u = 0; u < U; ++u)
