@@ -193,8 +193,9 @@ def cpu_baseline_sample(n_sample=12, J=4, steps=1):
     dofs0, _ = om.dirichlet_values(0.0, data)
     Abc = om.apply_bc_matrix(A, dofs0)
     blocks = om.preconditioner_blocks(dt)
-    hu = krylov.SAHierarchy(blocks[0], theta=0.1, cheb_degree=3)
-    hp = [krylov.SAHierarchy(B, theta=0.1, cheb_degree=3) for B in blocks[1:]]
+    P0 = krylov.p1_in_p2_embedding(om.dm, om.dirichlet_dofs()[0][0])
+    hu = krylov.SAHierarchy(blocks[0], theta=0.1, cheb_degree=4, P0=P0)
+    hp = [krylov.SAHierarchy(B, theta=0.1, cheb_degree=4) for B in blocks[1:]]
     M = krylov.block_preconditioner(hu, hp, 3, om.dm.Nu, om.dm.nv)
     up = np.zeros(om.dm.N)
     t = 0.0
@@ -213,6 +214,25 @@ def cpu_baseline_sample(n_sample=12, J=4, steps=1):
     return sec, om.dm.N
 
 
+def profile_case(args):
+    """Set-up, assembly and one time step capped at --maxit Krylov iterations."""
+    import torch
+    from waterscapes_gb300 import MPETSolver, _lib
+    problem, dt = workload(args.n, args.networks)
+    sol = MPETSolver(problem, dict(dt=dt, T=1e9, precision="mixed", maxit=args.maxit, rtol=1e-10))
+    sol._assemble(dt)
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    try:
+        sol.advance(dt)
+    except _lib.MpetError as e:
+        if e.code != -4:
+            raise
+    torch.cuda.synchronize()
+    print(json.dumps({"profile_case": args.n, "networks": args.networks, "maxit": args.maxit, "N": sol.N,
+                      "nnz": sol.nnz, "step_s": time.perf_counter() - t0}))
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -223,7 +243,12 @@ def main():
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--no-fp64", action="store_true")
     ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--profile", action="store_true",
+                    help="one step with at most --maxit MINRES iterations (small launch count for ncu)")
+    ap.add_argument("--maxit", type=int, default=12)
     args = ap.parse_args()
+    if args.profile:
+        return profile_case(args)
     n, J = args.n, args.networks
     N_full = 3 * (2 * n + 1) ** 3 + J * (n + 1) ** 3
     workload_name = "Kuhn cube %d^3 x 6 tets, A=%d networks, P2/P1 (N=%d)" % (n, J, N_full)

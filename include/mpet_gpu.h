@@ -66,9 +66,11 @@ typedef struct mpet_params {
     int32_t maxit;                     /* Krylov iterations per solve (all inner solves) */
     int32_t max_outer;                 /* refinement sweeps per solve */
     double amg_theta;                  /* strength threshold, e.g. 0.1 */
-    int32_t amg_cheb_degree;           /* Chebyshev smoother degree, e.g. 3 */
+    int32_t amg_cheb_degree;           /* Chebyshev smoother degree, e.g. 4 */
     int32_t amg_coarse_size;           /* dense solve below this size, e.g. 500 */
     int32_t check_every;               /* host convergence check period (iterations) */
+    int32_t amg_p2_to_p1;              /* 1: displacement hierarchy starts with the P1-in-P2
+                                          embedding (p-multigrid), then aggregation */
 } mpet_params;
 
 typedef struct mpet_stats {

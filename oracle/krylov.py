@@ -79,23 +79,54 @@ def aggregate(S):
     return agg, nagg
 
 
-def power_rho(DinvA, iters=15):
-    """Spectral radius of D^-1 A by power iteration from x_i = 0.5 + ((7919 i) mod 1009) / 1009."""
-    i = np.arange(DinvA.shape[0], dtype=np.int64)
-    x = 0.5 + ((7919 * i) % 1009) / 1009.0
-    lam = 0.0
-    for _ in range(iters):
-        y = DinvA @ x
-        nrm = np.linalg.norm(y)
-        if nrm == 0:
-            return 1.0
-        lam = nrm / np.linalg.norm(x)
-        x = y / nrm
-    return lam
+def lanczos_rho(A, Dinv, steps=30):
+    """Spectral radius of D^-1 A: ``steps`` Lanczos steps (no reorthogonalisation) on
+    D^-1/2 A D^-1/2 from x_i = 0.5 + ((7919 i) mod 1009) / 1009, largest Ritz value."""
+    n = A.shape[0]
+    s = np.sqrt(np.where(Dinv > 0, Dinv, 0.0))
+    i = np.arange(n, dtype=np.int64)
+    v = 0.5 + ((7919 * i) % 1009) / 1009.0
+    v = v / np.linalg.norm(v)
+    vprev = np.zeros(n)
+    al, be = [], []
+    beta = 0.0
+    for k in range(min(steps, n)):
+        w = s * (A @ (s * v)) - beta * vprev
+        alpha = float(w @ v)
+        al.append(alpha)
+        w = w - alpha * v
+        beta = float(np.linalg.norm(w))
+        if beta <= 1e-14 * abs(alpha) or k + 1 == steps or k + 1 == n:
+            break
+        be.append(beta)
+        vprev, v = v, w / beta
+    if not be:
+        return max(al)
+    return float(sla.eigh_tridiagonal(np.array(al), np.array(be), eigvals_only=True)[-1])
+
+
+def p1_in_p2_embedding(dm, bc_nodes):
+    """Prolongator from the P1 functions vanishing at the displacement Dirichlet
+    nodes to P2: vertex values copied, edge-midpoint values averaged; Dirichlet
+    rows are zero and coarse DOFs are the non-Dirichlet vertices in order."""
+    nv, ne = dm.nv, dm.ne
+    isbc = np.zeros(dm.nnodes, dtype=bool)
+    isbc[np.asarray(bc_nodes, dtype=np.int64)] = True
+    cidx = np.full(nv, -1, dtype=np.int64)
+    free = ~isbc[:nv]
+    cidx[free] = np.arange(free.sum())
+    rows = np.concatenate([np.arange(nv), nv + np.arange(ne), nv + np.arange(ne)])
+    cols = np.concatenate([np.arange(nv), dm.edges[:, 0], dm.edges[:, 1]])
+    vals = np.concatenate([np.ones(nv), 0.5 * np.ones(ne), 0.5 * np.ones(ne)])
+    keep = (~isbc[rows]) & (cidx[cols] >= 0)
+    return sp.csr_matrix((vals[keep], (rows[keep], cidx[cols[keep]])), shape=(dm.nnodes, int(free.sum())))
 
 
 class SAHierarchy:
-    def __init__(self, A, theta=0.0, coarse_size=500, max_levels=12, cheb_degree=2):
+    """Smoothed-aggregation hierarchy; ``P0`` (optional) replaces aggregation on
+    the first level (the strength threshold then counts aggregation levels)."""
+
+    def __init__(self, A, theta=0.0, coarse_size=500, max_levels=12, cheb_degree=2, P0=None):
         self.levels = []
         self.cheb_degree = cheb_degree
         A = A.tocsr()
@@ -104,22 +135,26 @@ class SAHierarchy:
             D = A.diagonal().copy()
             Dinv = np.where(D != 0, 1.0 / np.where(D != 0, D, 1.0), 0.0)
             DinvA = sp.diags(Dinv) @ A
-            rho = power_rho(DinvA)
+            rho = lanczos_rho(A, Dinv)
             lev = {"A": A, "Dinv": Dinv, "rho": rho}
             self.levels.append(lev)
-            if n <= coarse_size or len(self.levels) >= max_levels:
+            given = P0 is not None and len(self.levels) == 1
+            if not given and (n <= coarse_size or len(self.levels) >= max_levels):
                 break
-            th = theta * 0.5 ** (len(self.levels) - 1)
-            S = strength(A, th)
-            agg, nagg = aggregate(S)
-            if nagg == 0 and th > 0.0:
-                agg, nagg = aggregate(strength(A, 0.0))
-            if nagg == 0 or nagg >= n:
-                break
-            rows = np.nonzero(agg >= 0)[0]
-            sizes = np.bincount(agg[rows], minlength=nagg)
-            T = sp.csr_matrix((1.0 / np.sqrt(sizes[agg[rows]]), (rows, agg[rows])), shape=(n, nagg))
-            P = (T - (4.0 / 3.0 / rho) * (DinvA @ T)).tocsr()
+            if given:
+                P = P0.tocsr()
+            else:
+                th = theta * 0.5 ** (len(self.levels) - 1 - (1 if P0 is not None else 0))
+                S = strength(A, th)
+                agg, nagg = aggregate(S)
+                if nagg == 0 and th > 0.0:
+                    agg, nagg = aggregate(strength(A, 0.0))
+                if nagg == 0 or nagg >= n:
+                    break
+                rows = np.nonzero(agg >= 0)[0]
+                sizes = np.bincount(agg[rows], minlength=nagg)
+                T = sp.csr_matrix((1.0 / np.sqrt(sizes[agg[rows]]), (rows, agg[rows])), shape=(n, nagg))
+                P = (T - (4.0 / 3.0 / rho) * (DinvA @ T)).tocsr()
             R = P.T.tocsr()
             lev["P"], lev["R"] = P, R
             A = (R @ A @ P).tocsr()

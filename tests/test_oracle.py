@@ -107,8 +107,9 @@ def test_minres_amg_reaches_lu_solution():
         x0[d] = v
     r0 = bbc - Abc @ x0
     blocks = om.preconditioner_blocks(dt)
-    hu = krylov.SAHierarchy(blocks[0], theta=0.1, cheb_degree=3)
-    hp = [krylov.SAHierarchy(B, theta=0.1, cheb_degree=3) for B in blocks[1:]]
+    P0 = krylov.p1_in_p2_embedding(om.dm, om.dirichlet_dofs()[0][0])
+    hu = krylov.SAHierarchy(blocks[0], theta=0.1, cheb_degree=4, P0=P0)
+    hp = [krylov.SAHierarchy(B, theta=0.1, cheb_degree=4) for B in blocks[1:]]
     M = krylov.block_preconditioner(hu, hp, 3, om.dm.Nu, om.dm.nv)
     d, it, hist = krylov.minres(Abc, r0, M, rtol=1e-11, maxiter=3000)
     assert hist[-1] <= 1e-11

@@ -45,6 +45,7 @@ class MpetParams(ctypes.Structure):
         ("amg_cheb_degree", ctypes.c_int32),
         ("amg_coarse_size", ctypes.c_int32),
         ("check_every", ctypes.c_int32),
+        ("amg_p2_to_p1", ctypes.c_int32),
     ]
 
 

@@ -10,7 +10,7 @@
 //              leftovers), isolated rows (Dirichlet unit rows) unaggregated
 //   T          piecewise constant, columns scaled to unit 2-norm
 //   P          (I - 4/3 rho^-1 D^-1 A) T, rho = spectral radius of D^-1 A
-//              from 15 power iterations on a fixed start vector
+//              from 30 Lanczos steps on D^-1/2 A D^-1/2 (fixed start vector)
 //   A_c        P^T A P (Gustavson sparse products, rows sorted)
 //   coarsest   explicit inverse via Cholesky (FP64)
 // The V-cycle itself runs on the GPU (solve.cu).
@@ -123,26 +123,77 @@ static double diag_of(const HostCsr& A, int64_t i) {
     return 0.0;
 }
 
-// Spectral radius of D^-1 A by power iteration from x_i = 0.5 + ((7919 i) mod 1009)/1009.
-static double power_rho(const HostCsr& A, const std::vector<double>& dinv, int iters) {
-    const int64_t n = A.n;
-    std::vector<double> x(n), y;
-    for (int64_t i = 0; i < n; ++i) x[i] = 0.5 + (double)((7919LL * i) % 1009LL) / 1009.0;
-    double lam = 1.0;
-    for (int k = 0; k < iters; ++k) {
-        csr_matvec(A, x, y);
-        double ny = 0.0, nx = 0.0;
-        for (int64_t i = 0; i < n; ++i) {
-            y[i] *= dinv[i];
-            ny += y[i] * y[i];
-            nx += x[i] * x[i];
-        }
-        if (ny == 0.0) return 1.0;
-        lam = sqrt(ny) / sqrt(nx);
-        const double s = 1.0 / sqrt(ny);
-        for (int64_t i = 0; i < n; ++i) x[i] = y[i] * s;
+// Largest eigenvalue of a symmetric tridiagonal matrix (diagonal a, off-
+// diagonal b[1..m-1]) by Sturm-sequence bisection.
+static double tridiag_max_eig(const std::vector<double>& a, const std::vector<double>& b) {
+    const int m = (int)a.size();
+    double lo = 1e300, hi = -1e300;
+    for (int i = 0; i < m; ++i) {
+        const double r = (i > 0 ? fabs(b[i]) : 0.0) + (i + 1 < m ? fabs(b[i + 1]) : 0.0);
+        lo = fmin(lo, a[i] - r);
+        hi = fmax(hi, a[i] + r);
     }
-    return lam;
+    auto below = [&](double x) {  // eigenvalues < x
+        int cnt = 0;
+        double d = 1.0;
+        for (int i = 0; i < m; ++i) {
+            d = a[i] - x - (i > 0 ? b[i] * b[i] / d : 0.0);
+            if (d == 0.0) d = -1e-300;
+            if (d < 0.0) ++cnt;
+        }
+        return cnt;
+    };
+    for (int it = 0; it < 200 && hi - lo > 1e-12 * fmax(1.0, fabs(hi)); ++it) {
+        const double mid = 0.5 * (lo + hi);
+        if (below(mid) >= m) hi = mid; else lo = mid;
+    }
+    return hi;
+}
+
+// Spectral radius of D^-1 A: 30 Lanczos steps on D^-1/2 A D^-1/2 (same
+// spectrum, symmetric) from x_i = 0.5 + ((7919 i) mod 1009)/1009, then the
+// largest Ritz value.
+static double lanczos_rho(const HostCsr& A, const std::vector<double>& dinv, int steps) {
+    const int64_t n = A.n;
+    std::vector<double> s(n), v(n), vprev(n, 0.0), w(n), t;
+    for (int64_t i = 0; i < n; ++i) s[i] = dinv[i] > 0.0 ? sqrt(dinv[i]) : 0.0;
+    double nrm = 0.0;
+    for (int64_t i = 0; i < n; ++i) {
+        v[i] = 0.5 + (double)((7919LL * i) % 1009LL) / 1009.0;
+        nrm += v[i] * v[i];
+    }
+    nrm = sqrt(nrm);
+    for (int64_t i = 0; i < n; ++i) v[i] /= nrm;
+    std::vector<double> al, be(1, 0.0);
+    double beta = 0.0;
+    for (int k = 0; k < steps && k < n; ++k) {
+#pragma omp parallel for schedule(static)
+        for (int64_t i = 0; i < n; ++i) w[i] = s[i] * v[i];
+        csr_matvec(A, w, t);
+        double alpha = 0.0;
+#pragma omp parallel for schedule(static) reduction(+ : alpha)
+        for (int64_t i = 0; i < n; ++i) {
+            w[i] = s[i] * t[i] - beta * vprev[i];
+            alpha += w[i] * v[i];
+        }
+        al.push_back(alpha);
+        double nb = 0.0;
+#pragma omp parallel for schedule(static) reduction(+ : nb)
+        for (int64_t i = 0; i < n; ++i) {
+            w[i] -= alpha * v[i];
+            nb += w[i] * w[i];
+        }
+        beta = sqrt(nb);
+        if (beta <= 1e-14 * fabs(alpha) || k + 1 == steps || k + 1 == n) break;
+        be.push_back(beta);
+        const double ib = 1.0 / beta;
+#pragma omp parallel for schedule(static)
+        for (int64_t i = 0; i < n; ++i) {
+            vprev[i] = v[i];
+            v[i] = w[i] * ib;
+        }
+    }
+    return tridiag_max_eig(al, be);
 }
 
 static void strength(const HostCsr& A, double theta, HostCsr& S) {
@@ -268,7 +319,90 @@ static int host_threads() {
     return n < 1 ? 1 : n;
 }
 
-void amg_setup_host(const HostCsr& A0, double theta, int coarse_size, int max_levels, HostAmg& out) {
+// Smoothed-aggregation prolongator of level A (threshold th); false when the
+// level cannot be coarsened.
+static bool sa_prolongator(const HostCsr& A, const std::vector<double>& dinv, double rho, double th, HostCsr& P) {
+    const int64_t n = A.n;
+    HostCsr S;
+    strength(A, th, S);
+    std::vector<int64_t> agg;
+    int64_t nagg = aggregate(S, agg);
+    if (nagg == 0 && th > 0.0) {
+        strength(A, 0.0, S);
+        nagg = aggregate(S, agg);
+    }
+    if (nagg == 0 || nagg >= n) return false;
+    std::vector<int64_t> size(nagg, 0);
+    for (int64_t i = 0; i < n; ++i)
+        if (agg[i] >= 0) size[agg[i]]++;
+    HostCsr T;
+    T.n = n;
+    T.m = nagg;
+    T.rp.assign(n + 1, 0);
+    for (int64_t i = 0; i < n; ++i) T.rp[i + 1] = T.rp[i] + (agg[i] >= 0 ? 1 : 0);
+    T.ci.resize(T.rp[n]);
+    T.v.resize(T.rp[n]);
+    for (int64_t i = 0; i < n; ++i)
+        if (agg[i] >= 0) {
+            T.ci[T.rp[i]] = (int32_t)agg[i];
+            T.v[T.rp[i]] = 1.0 / sqrt((double)size[agg[i]]);
+        }
+    // P = T - (4/3/rho) D^-1 A T
+    HostCsr AT;
+    spgemm(A, T, AT);
+    const double w = 4.0 / 3.0 / rho;
+    P = HostCsr();
+    P.n = n;
+    P.m = nagg;
+    P.rp.assign(n + 1, 0);
+    for (int64_t i = 0; i < n; ++i) {
+        // union of T row (<= 1 entry) and AT row, both sorted
+        int64_t cnt = AT.rp[i + 1] - AT.rp[i];
+        if (T.rp[i + 1] > T.rp[i]) {
+            const int32_t j = T.ci[T.rp[i]];
+            bool found = false;
+            for (int64_t e = AT.rp[i]; e < AT.rp[i + 1]; ++e)
+                if (AT.ci[e] == j) found = true;
+            if (!found) ++cnt;
+        }
+        P.rp[i + 1] = P.rp[i] + cnt;
+    }
+    P.ci.resize(P.rp[n]);
+    P.v.resize(P.rp[n]);
+    for (int64_t i = 0; i < n; ++i) {
+        int64_t p = P.rp[i];
+        const bool hasT = T.rp[i + 1] > T.rp[i];
+        const int32_t tj = hasT ? T.ci[T.rp[i]] : -1;
+        const double tv = hasT ? T.v[T.rp[i]] : 0.0;
+        bool placed = !hasT;
+        for (int64_t e = AT.rp[i]; e < AT.rp[i + 1]; ++e) {
+            const int32_t j = AT.ci[e];
+            if (!placed && tj < j) {
+                P.ci[p] = tj;
+                P.v[p] = tv;
+                ++p;
+                placed = true;
+            }
+            double v = -w * dinv[i] * AT.v[e];
+            if (j == tj) {
+                v += tv;
+                placed = true;
+            }
+            P.ci[p] = j;
+            P.v[p] = v;
+            ++p;
+        }
+        if (!placed) {
+            P.ci[p] = tj;
+            P.v[p] = tv;
+            ++p;
+        }
+    }
+    return true;
+}
+
+void amg_setup_host(const HostCsr& A0, const HostCsr* P0, double theta, int coarse_size, int max_levels,
+                    HostAmg& out) {
     out.lev.clear();
     HostCsr A = A0;
     if (coarse_size < 1) coarse_size = 500;
@@ -284,88 +418,22 @@ void amg_setup_host(const HostCsr& A0, double theta, int coarse_size, int max_le
             const double d = diag_of(A, i);
             L.dinv[i] = d != 0.0 ? 1.0 / d : 0.0;
         }
-        L.rho = power_rho(A, L.dinv, 15);
+        L.rho = lanczos_rho(A, L.dinv, 30);
         L.A = A;
         out.lev.push_back(L);
         HostAmgLevel& cur = out.lev.back();
-        if (n <= coarse_size || (int)out.lev.size() >= max_levels) break;
-        // the threshold halves per level; a level without any strong
-        // connection is aggregated on its full graph (threshold 0)
-        const double th = theta * pow(0.5, (double)(out.lev.size() - 1));
-        HostCsr S;
-        strength(A, th, S);
-        std::vector<int64_t> agg;
-        int64_t nagg = aggregate(S, agg);
-        if (nagg == 0 && th > 0.0) {
-            strength(A, 0.0, S);
-            nagg = aggregate(S, agg);
-        }
-        if (nagg == 0 || nagg >= n) break;
-        std::vector<int64_t> size(nagg, 0);
-        for (int64_t i = 0; i < n; ++i)
-            if (agg[i] >= 0) size[agg[i]]++;
-        HostCsr T;
-        T.n = n;
-        T.m = nagg;
-        T.rp.assign(n + 1, 0);
-        for (int64_t i = 0; i < n; ++i) T.rp[i + 1] = T.rp[i] + (agg[i] >= 0 ? 1 : 0);
-        T.ci.resize(T.rp[n]);
-        T.v.resize(T.rp[n]);
-        for (int64_t i = 0; i < n; ++i)
-            if (agg[i] >= 0) {
-                T.ci[T.rp[i]] = (int32_t)agg[i];
-                T.v[T.rp[i]] = 1.0 / sqrt((double)size[agg[i]]);
-            }
-        // P = T - (4/3/rho) D^-1 A T
-        HostCsr AT;
-        spgemm(A, T, AT);
-        const double w = 4.0 / 3.0 / cur.rho;
+        const bool given = P0 != nullptr && out.lev.size() == 1;
+        if (!given && (n <= coarse_size || (int)out.lev.size() >= max_levels)) break;
         HostCsr P;
-        P.n = n;
-        P.m = nagg;
-        P.rp.assign(n + 1, 0);
-        for (int64_t i = 0; i < n; ++i) {
-            // union of T row (<= 1 entry) and AT row, both sorted
-            int64_t cnt = AT.rp[i + 1] - AT.rp[i];
-            if (T.rp[i + 1] > T.rp[i]) {
-                const int32_t j = T.ci[T.rp[i]];
-                bool found = false;
-                for (int64_t e = AT.rp[i]; e < AT.rp[i + 1]; ++e)
-                    if (AT.ci[e] == j) found = true;
-                if (!found) ++cnt;
-            }
-            P.rp[i + 1] = P.rp[i] + cnt;
-        }
-        P.ci.resize(P.rp[n]);
-        P.v.resize(P.rp[n]);
-        for (int64_t i = 0; i < n; ++i) {
-            int64_t p = P.rp[i];
-            const bool hasT = T.rp[i + 1] > T.rp[i];
-            const int32_t tj = hasT ? T.ci[T.rp[i]] : -1;
-            const double tv = hasT ? T.v[T.rp[i]] : 0.0;
-            bool placed = !hasT;
-            for (int64_t e = AT.rp[i]; e < AT.rp[i + 1]; ++e) {
-                const int32_t j = AT.ci[e];
-                if (!placed && tj < j) {
-                    P.ci[p] = tj;
-                    P.v[p] = tv;
-                    ++p;
-                    placed = true;
-                }
-                double v = -w * cur.dinv[i] * AT.v[e];
-                if (j == tj) {
-                    v += tv;
-                    placed = true;
-                }
-                P.ci[p] = j;
-                P.v[p] = v;
-                ++p;
-            }
-            if (!placed) {
-                P.ci[p] = tj;
-                P.v[p] = tv;
-                ++p;
-            }
+        if (given) {
+            if (P0->n != n) fail(MPET_ERR_INVALID, "first-level prolongator has the wrong row count");
+            P = *P0;
+        } else {
+            // the threshold halves per aggregation level; a level without any
+            // strong connection is aggregated on its full graph (threshold 0)
+            const int sa_level = (int)out.lev.size() - 1 - (P0 != nullptr ? 1 : 0);
+            const double th = theta * pow(0.5, (double)sa_level);
+            if (!sa_prolongator(A, cur.dinv, cur.rho, th, P)) break;
         }
         HostCsr R;
         transpose(P, R);

@@ -317,14 +317,61 @@ int mpet_setup_preconditioner(mpet_ctx* c, double dt) {
         HostCsr h;
         fetch(c->Lu, h);
         HostAmg ha;
-        amg_setup_host(h, c->prm.amg_theta, cs, 12, ha);
+        if (c->prm.amg_p2_to_p1) {
+            // First level of the displacement hierarchy: the P1 functions that
+            // vanish on the displacement Dirichlet boundary, embedded in P2
+            // (vertex values copied, edge-midpoint values averaged).
+            std::vector<int64_t> ek(c->ne);
+            std::vector<uint8_t> bc(c->nnodes);
+            MPET_CUDA(cudaMemcpyAsync(ek.data(), c->edge_key, sizeof(int64_t) * c->ne, cudaMemcpyDeviceToHost,
+                                      c->stream));
+            MPET_CUDA(cudaMemcpyAsync(bc.data(), c->node_bc, c->nnodes, cudaMemcpyDeviceToHost, c->stream));
+            MPET_CUDA(cudaStreamSynchronize(c->stream));
+            std::vector<int64_t> cidx(c->nv, -1);
+            int64_t m = 0;
+            for (int64_t v = 0; v < c->nv; ++v)
+                if (!bc[v]) cidx[v] = m++;
+            HostCsr P0;
+            P0.n = c->nnodes;
+            P0.m = m;
+            P0.rp.assign(c->nnodes + 1, 0);
+            for (int64_t i = 0; i < c->nnodes; ++i) {
+                int64_t cnt = 0;
+                if (!bc[i]) {
+                    if (i < c->nv) cnt = 1;
+                    else cnt = (cidx[ek[i - c->nv] / c->nv] >= 0) + (cidx[ek[i - c->nv] % c->nv] >= 0);
+                }
+                P0.rp[i + 1] = P0.rp[i] + cnt;
+            }
+            P0.ci.resize(P0.rp[c->nnodes]);
+            P0.v.resize(P0.rp[c->nnodes]);
+            for (int64_t i = 0; i < c->nnodes; ++i) {
+                int64_t p = P0.rp[i];
+                if (bc[i]) continue;
+                if (i < c->nv) {
+                    P0.ci[p] = (int32_t)cidx[i];
+                    P0.v[p] = 1.0;
+                } else {
+                    const int64_t lo = ek[i - c->nv] / c->nv, hi = ek[i - c->nv] % c->nv;
+                    for (int64_t w : {lo, hi})
+                        if (cidx[w] >= 0) {
+                            P0.ci[p] = (int32_t)cidx[w];
+                            P0.v[p] = 0.5;
+                            ++p;
+                        }
+                }
+            }
+            amg_setup_host(h, &P0, c->prm.amg_theta, cs, 12, ha);
+        } else {
+            amg_setup_host(h, nullptr, c->prm.amg_theta, cs, 12, ha);
+        }
         upload_amg(c, c->amg_u, ha, 3, fp32);
     }
     for (int a = 0; a < c->J; ++a) {
         HostCsr h;
         fetch(c->Pp[a], h);
         HostAmg ha;
-        amg_setup_host(h, c->prm.amg_theta, cs, 12, ha);
+        amg_setup_host(h, nullptr, c->prm.amg_theta, cs, 12, ha);
         upload_amg(c, c->amg_p[a], ha, 1, fp32);
     }
     c->precond_ready = true;

@@ -119,7 +119,9 @@ struct HostAmg {
     int64_t ncoarse = 0;
     std::vector<double> cinv;
 };
-void amg_setup_host(const HostCsr& A, double theta, int coarse_size, int max_levels, HostAmg& out);
+// P0, if given, is the prolongator of the first level (otherwise smoothed aggregation).
+void amg_setup_host(const HostCsr& A, const HostCsr* P0, double theta, int coarse_size, int max_levels,
+                    HostAmg& out);
 
 }  // namespace mpet
 

@@ -720,7 +720,7 @@ static void upload_csr(mpet_ctx* c, const HostCsr& h, Csr& d, bool fp32) {
 
 void upload_amg(mpet_ctx* c, AmgHier& h, const HostAmg& ha, int nvec, bool fp32) {
     h.nvec = nvec;
-    h.cheb_degree = c->prm.amg_cheb_degree > 0 ? c->prm.amg_cheb_degree : 3;
+    h.cheb_degree = c->prm.amg_cheb_degree > 0 ? c->prm.amg_cheb_degree : 4;
     h.lev.clear();
     h.lev.resize(ha.lev.size());
     for (size_t k = 0; k < ha.lev.size(); ++k) {

@@ -124,8 +124,8 @@ class MPETSolver:
         return {"dt": 0.1, "t": 0.0, "T": 1.0, "theta": 1.0, "u_degree": 2, "p_degree": 1,
                 "direct_solver": True,
                 "precision": "mixed", "rtol": 1e-10, "inner_rtol": 1e-4, "maxit": 20000,
-                "max_outer": 40, "amg_theta": 0.1, "amg_cheb_degree": 3, "amg_coarse_size": 500,
-                "check_every": 4, "device": 0}
+                "max_outer": 40, "amg_theta": 0.1, "amg_cheb_degree": 4, "amg_coarse_size": 500,
+                "amg_p2_to_p1": True, "check_every": 4, "device": 0}
 
     def _make_params(self):
         pp = self.problem.params
@@ -151,6 +151,7 @@ class MPETSolver:
         prm.amg_cheb_degree = int(self.params["amg_cheb_degree"])
         prm.amg_coarse_size = int(self.params["amg_coarse_size"])
         prm.check_every = int(self.params["check_every"])
+        prm.amg_p2_to_p1 = 1 if self.params["amg_p2_to_p1"] else 0
         return prm
 
     def _check_facet_data(self):
