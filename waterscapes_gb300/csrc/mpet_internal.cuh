@@ -28,13 +28,16 @@ struct Error {
 #define MPET_CHECK_LAUNCH() MPET_CUDA(cudaGetLastError())
 
 // Device allocation tracked by the context so destroy() frees everything.
+// Every allocation carries kTail spare bytes, so bulk copies whose size is
+// rounded up to 16 bytes may read past the last element without leaving it.
 struct DevPool {
+    static constexpr size_t kTail = 64;
     std::vector<void*> ptrs;
     template <typename T>
     T* alloc(int64_t n) {
         if (n <= 0) n = 1;
         void* p = nullptr;
-        cudaError_t e = cudaMalloc(&p, (size_t)n * sizeof(T));
+        cudaError_t e = cudaMalloc(&p, (size_t)n * sizeof(T) + kTail);
         if (e != cudaSuccess) {
             cudaGetLastError();
             fail(MPET_ERR_NOMEM, "cudaMalloc of " + std::to_string((size_t)n * sizeof(T)) + " bytes failed");
@@ -66,6 +69,10 @@ struct Csr {
     double* v64 = nullptr;
     float* v32 = nullptr;
     int lpr = 32;  // lanes per row used by the SpMV kernels
+    // Row tiles for the shared-memory staged SpMV: tiles[t]..tiles[t+1] are
+    // whole rows holding at most SPMV_TILE entries (ntiles = 0: not staged).
+    int32_t* tiles = nullptr;
+    int ntiles = 0;
 };
 
 struct AmgLevel {
@@ -201,6 +208,9 @@ struct mpet_ctx {
     cudaGraphExec_t mr_graph = nullptr;
     int64_t mr_graph_launches = 0;  // kernels per graph launch
 
+    // set by a kernel whose bounded wait gave up (read after each solve)
+    int* dev_err = nullptr;
+
     // timing
     cudaEvent_t ev0 = nullptr, ev1 = nullptr;
     double t_spmv_ms = 0.0, t_prec_ms = 0.0;
@@ -233,6 +243,8 @@ void upload_amg(mpet_ctx* c, AmgHier& h, const HostAmg& ha, int nvec, bool fp32)
 int solve_system(mpet_ctx* c, const double* b, double* x, mpet_stats* st);
 void alloc_krylov(mpet_ctx* c);
 int choose_lpr(int64_t n, int64_t nnz);
+void build_tiles(mpet_ctx* c, Csr& A, const int64_t* rp_host);
+constexpr int SPMV_TILE = 2048;  // entries per staged tile
 void destroy_minres_graph(mpet_ctx* c);
 void convert_values_to_f32(mpet_ctx* c);
 

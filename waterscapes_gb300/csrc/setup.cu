@@ -428,6 +428,12 @@ void build_pattern(mpet_ctx* c) {
                                          c->A.ci);
     MPET_CHECK_LAUNCH();
     c->A.lpr = choose_lpr(N, c->nnz);
+    {
+        std::vector<int64_t> rp(N + 1);
+        MPET_CUDA(cudaMemcpyAsync(rp.data(), c->A.rp, sizeof(int64_t) * (N + 1), cudaMemcpyDeviceToHost, s));
+        MPET_CUDA(cudaStreamSynchronize(s));
+        build_tiles(c, c->A, rp.data());
+    }
     // preconditioner block patterns: u-Laplacian on n2, P1 blocks on the vertex rows of n1
     c->Lu.n = c->Lu.m = c->nnodes;
     c->Lu.nnz = c->n2_nnz;

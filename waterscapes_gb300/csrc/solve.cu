@@ -168,18 +168,19 @@ __global__ void __launch_bounds__(256) k_spmv(int64_t n, const int64_t* __restri
 #pragma unroll
         for (int k = 0; k < NV; ++k) acc[k] = T(0);
         if (row < n) {
-            // U independent (column, value) loads per lane are issued before
-            // any dependent x gather; matrix streams use evict-first loads so
-            // the x vector stays resident in L2.
+            // Chunks of U (column, value) pairs per lane; the loads of the next
+            // chunk are issued before the dependent x gathers of the current
+            // one, so each warp keeps two chunks of matrix stream in flight.
+            // Matrix loads are evict-first so x stays resident in L2.  Every
+            // address is clamped into the (non-empty) row, so a load issued
+            // regardless of its predicate stays in bounds.
             constexpr int U = 4;
             const int64_t e0 = rp[row], e1 = rp[row + 1];
-            for (int64_t b = e0; b < e1; b += LPR * U) {
-                int32_t cc[U];
-                T aa[U];
+            int32_t cc[U];
+            T aa[U];
+            auto load_chunk = [&](int64_t b) {
 #pragma unroll
                 for (int u = 0; u < U; ++u) {
-                    // the address is clamped into the row (non-empty here), so
-                    // a load issued regardless of the predicate stays in bounds
                     const int64_t e = b + sub + u * LPR;
                     const bool ok = e < e1;
                     const int64_t es = ok ? e : e1 - 1;
@@ -187,10 +188,21 @@ __global__ void __launch_bounds__(256) k_spmv(int64_t n, const int64_t* __restri
                     const T a = __ldcs(va + es);
                     aa[u] = ok ? a : T(0);
                 }
+            };
+            if (e0 < e1) load_chunk(e0);
+            for (int64_t b = e0; b < e1; b += LPR * U) {
+                int32_t c0[U];
+                T a0[U];
+#pragma unroll
+                for (int u = 0; u < U; ++u) {
+                    c0[u] = cc[u];
+                    a0[u] = aa[u];
+                }
+                if (b + LPR * U < e1) load_chunk(b + LPR * U);
 #pragma unroll
                 for (int u = 0; u < U; ++u)
 #pragma unroll
-                    for (int k = 0; k < NV; ++k) acc[k] += aa[u] * x[(int64_t)NV * cc[u] + k];
+                    for (int k = 0; k < NV; ++k) acc[k] += a0[u] * x[(int64_t)NV * c0[u] + k];
             }
         }
 #pragma unroll
@@ -210,8 +222,207 @@ __global__ void __launch_bounds__(256) k_spmv(int64_t n, const int64_t* __restri
     }
 }
 
+// ---- shared-memory staged SpMV (bulk async copies) ----------------------------------
+//
+// A CTA walks a list of row tiles; each tile's column ids and values are a
+// contiguous range of the CSR arrays, copied to shared memory by one
+// cp.async.bulk per array (completion counted on an mbarrier).  Two buffers
+// alternate: while the warps reduce tile t from one buffer, the copy of the
+// CTA's next tile streams into the other, so HBM is fed by the copy engine
+// and the warps only wait on the x gathers (L2) and shared-memory reads.
+// The copy start is rounded down and its end up to 4 entries (16 bytes); the
+// 64-byte tail of every pool allocation covers the read past the last entry.
+
+constexpr int SPMV_CAP = SPMV_TILE + 8;  // buffer entries (alignment slack)
+constexpr int MBAR_SPIN_LIMIT = 1 << 22;
+
+__device__ __forceinline__ uint32_t smem_u32(const void* p) { return (uint32_t)__cvta_generic_to_shared(p); }
+
+__device__ __forceinline__ void mbar_init(uint64_t* bar, uint32_t count) {
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_u32(bar)), "r"(count) : "memory");
+}
+
+__device__ __forceinline__ void mbar_fence_init() { asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory"); }
+
+__device__ __forceinline__ void mbar_expect_tx(uint64_t* bar, uint32_t bytes) {
+    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_u32(bar)), "r"(bytes) : "memory");
+}
+
+__device__ __forceinline__ void bulk_copy_g2s(void* dst, const void* src, uint32_t bytes, uint64_t* bar) {
+    asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(
+                     smem_u32(dst)),
+                 "l"(src), "r"(bytes), "r"(smem_u32(bar))
+                 : "memory");
+}
+
+// Bounded wait for the phase with the given parity; false if it never completed.
+__device__ __forceinline__ bool mbar_wait(uint64_t* bar, uint32_t parity) {
+    for (int it = 0; it < MBAR_SPIN_LIMIT; ++it) {
+        uint32_t ok;
+        asm volatile(
+            "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n selp.u32 %0, 1, 0, p;\n}\n"
+            : "=r"(ok)
+            : "r"(smem_u32(bar)), "r"(parity)
+            : "memory");
+        if (ok) return true;
+    }
+    return false;
+}
+
+template <typename T>
+constexpr size_t staged_smem_bytes() {
+    return 128 + 2 * (size_t)SPMV_CAP * (4 + sizeof(T));
+}
+
+template <typename T, int NV, int LPR, class Epi>
+__global__ void __launch_bounds__(256) k_spmv_staged(const int64_t* __restrict__ rp, const int32_t* __restrict__ ci,
+                                                     const T* __restrict__ va, const T* __restrict__ x, Epi epi,
+                                                     double* partials, const int32_t* __restrict__ tiles, int ntiles,
+                                                     int* err) {
+    extern __shared__ __align__(128) unsigned char smem[];
+    uint64_t* bar = reinterpret_cast<uint64_t*>(smem);
+    unsigned char* base = smem + 128;
+    constexpr size_t bufb = (size_t)SPMV_CAP * (4 + sizeof(T));
+    auto scol = [&](int bb) { return (int32_t*)(base + bb * bufb); };
+    auto sval = [&](int bb) { return (T*)(base + bb * bufb + (size_t)SPMV_CAP * 4); };
+    if (threadIdx.x == 0) {
+        mbar_init(&bar[0], 1);
+        mbar_init(&bar[1], 1);
+        mbar_fence_init();
+    }
+    __syncthreads();
+    auto issue = [&](int t, int b) {
+        const int64_t a0 = rp[tiles[t]] & ~3LL;
+        const int64_t a1 = (rp[tiles[t + 1]] + 3) & ~3LL;
+        const uint32_t cnt = (uint32_t)(a1 - a0);
+        mbar_expect_tx(&bar[b], cnt * (uint32_t)(4 + sizeof(T)));
+        bulk_copy_g2s(scol(b), ci + a0, cnt * 4u, &bar[b]);
+        bulk_copy_g2s(sval(b), va + a0, cnt * (uint32_t)sizeof(T), &bar[b]);
+    };
+    const int sub = threadIdx.x & (LPR - 1);
+    const int gid = threadIdx.x / LPR;
+    constexpr int NGR = 256 / LPR;
+    double r0 = 0.0, r1 = 0.0;
+    uint32_t ph0 = 0, ph1 = 0;
+    bool pending0 = false, pending1 = false;
+    int b = 0;
+    if (threadIdx.x == 0 && (int)blockIdx.x < ntiles) {
+        issue(blockIdx.x, 0);
+        pending0 = true;
+    }
+    bool bad = false;
+    for (int t = blockIdx.x; t < ntiles; t += gridDim.x) {
+        const int tn = t + gridDim.x;
+        if (threadIdx.x == 0 && tn < ntiles) {
+            issue(tn, b ^ 1);
+            if (b) pending0 = true; else pending1 = true;
+        }
+        const bool ok = mbar_wait(&bar[b], b ? ph1 : ph0);
+        if (b) { ph1 ^= 1u; pending1 = false; } else { ph0 ^= 1u; pending0 = false; }
+        if (__syncthreads_or(!ok)) {
+            bad = true;
+            break;
+        }
+        const int64_t rs = tiles[t], re = tiles[t + 1];
+        const int64_t a0 = rp[rs] & ~3LL;
+        const int32_t* sc = scol(b);
+        const T* sv = sval(b);
+        for (int64_t rb = rs; rb < re; rb += NGR) {
+            const int64_t row = rb + gid;
+            T acc[NV];
+#pragma unroll
+            for (int k = 0; k < NV; ++k) acc[k] = T(0);
+            if (row < re) {
+                const int s = (int)(rp[row] - a0), e = (int)(rp[row + 1] - a0);
+                for (int q = s + sub; q < e; q += LPR) {
+                    const int64_t cidx = sc[q];
+                    const T a = sv[q];
+#pragma unroll
+                    for (int k = 0; k < NV; ++k) acc[k] += a * x[NV * cidx + k];
+                }
+            }
+#pragma unroll
+            for (int o = LPR / 2; o > 0; o >>= 1)
+#pragma unroll
+                for (int k = 0; k < NV; ++k) acc[k] += __shfl_xor_sync(0xffffffffu, acc[k], o);
+            if (row < re && sub == 0) epi(row, acc, r0, r1);
+        }
+        __syncthreads();  // buffer b consumed before it is refilled
+        b ^= 1;
+    }
+    if (bad) {
+        // record the failure and let any copy still in flight land (bounded)
+        if (threadIdx.x == 0) {
+            atomicExch(err, 1);
+            if (pending0) mbar_wait(&bar[0], ph0);
+            if (pending1) mbar_wait(&bar[1], ph1);
+        }
+        __syncthreads();
+    }
+    if constexpr (Epi::kRed > 0) {
+        __shared__ double sh[8];
+        double t0 = block_sum256(r0, sh);
+        double t1 = (Epi::kRed > 1) ? block_sum256(r1, sh) : 0.0;
+        if (threadIdx.x == 0) {
+            for (int p = blockIdx.x; p < NB_RED; p += gridDim.x) {
+                partials[p] = p == (int)blockIdx.x ? t0 : 0.0;
+                if (Epi::kRed > 1) partials[NB_RED + p] = p == (int)blockIdx.x ? t1 : 0.0;
+            }
+        }
+    }
+}
+
+template <typename T, int NV, int LPR, class Epi>
+static void launch_staged(mpet_ctx* c, const Csr& A, const T* va, const T* x, const Epi& epi) {
+    static int grid = 0;  // resident CTAs on this device (one per instantiation)
+    auto kern = k_spmv_staged<T, NV, LPR, Epi>;
+    const size_t sm = staged_smem_bytes<T>();
+    if (grid == 0) {
+        MPET_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm));
+        int per_sm = 0, nsm = 0, dev = 0;
+        MPET_CUDA(cudaGetDevice(&dev));
+        MPET_CUDA(cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev));
+        MPET_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, 256, sm));
+        grid = nsm * (per_sm > 0 ? per_sm : 1);
+        if (grid > NB_RED) grid = NB_RED;
+    }
+    kern<<<grid, 256, sm, c->stream>>>(A.rp, A.ci, va, x, epi, c->partials, A.tiles, A.ntiles, c->dev_err);
+    MPET_CHECK_LAUNCH();
+    c->n_launch++;
+}
+
+void build_tiles(mpet_ctx* c, Csr& A, const int64_t* rp) {
+    A.ntiles = 0;
+    A.tiles = nullptr;
+    if (A.nnz < (int64_t)SPMV_TILE * 64) return;  // small matrices: register kernel
+    std::vector<int32_t> t;
+    t.push_back(0);
+    int64_t start = rp[0];
+    for (int64_t r = 0; r < A.n; ++r) {
+        const int64_t len = rp[r + 1] - rp[r];
+        if (len > SPMV_TILE / 2) return;  // long rows: register kernel
+        if (rp[r + 1] - start > SPMV_TILE) {
+            t.push_back((int32_t)r);
+            start = rp[r];
+        }
+    }
+    t.push_back((int32_t)A.n);
+    A.tiles = c->pool.alloc<int32_t>((int64_t)t.size());
+    MPET_CUDA(cudaMemcpyAsync(A.tiles, t.data(), sizeof(int32_t) * t.size(), cudaMemcpyHostToDevice, c->stream));
+    MPET_CUDA(cudaStreamSynchronize(c->stream));
+    A.ntiles = (int)t.size() - 1;
+}
+
 template <typename T, int NV, class Epi>
 static void launch_spmv(mpet_ctx* c, const Csr& A, const T* va, const T* x, const Epi& epi) {
+    if (A.ntiles > 0) {
+        switch (A.lpr) {
+            case 32: launch_staged<T, NV, 32, Epi>(c, A, va, x, epi); return;
+            case 16: launch_staged<T, NV, 16, Epi>(c, A, va, x, epi); return;
+            case 8: launch_staged<T, NV, 8, Epi>(c, A, va, x, epi); return;
+            default: launch_staged<T, NV, 4, Epi>(c, A, va, x, epi); return;
+        }
+    }
     int blocks;
     if (Epi::kRed > 0) {
         blocks = NB_RED;
@@ -667,6 +878,13 @@ static int solve_impl(mpet_ctx* c, const double* b, double* x, mpet_stats* st) {
         }
     }
     if (outer >= max_outer && status == MPET_OK) status = MPET_ERR_MAXIT;
+    int derr = 0;
+    MPET_CUDA(cudaMemcpyAsync(&derr, c->dev_err, sizeof(int), cudaMemcpyDeviceToHost, c->stream));
+    MPET_CUDA(cudaStreamSynchronize(c->stream));
+    if (derr) {
+        MPET_CUDA(cudaMemsetAsync(c->dev_err, 0, sizeof(int), c->stream));
+        status = MPET_ERR_TIMEOUT;
+    }
     if (st) {
         st->iterations = iters;
         st->outer = outer + 1;
@@ -692,6 +910,8 @@ void alloc_krylov(mpet_ctx* c) {
     }
     c->orr = c->pool.alloc<double>(n);
     c->partials = c->pool.alloc<double>(2 * NB_RED);
+    c->dev_err = c->pool.alloc<int>(1);
+    MPET_CUDA(cudaMemsetAsync(c->dev_err, 0, sizeof(int), c->stream));
     c->sc = c->pool.alloc<MinresScalars>(1);
     if (!c->sc_host) MPET_CUDA(cudaMallocHost(&c->sc_host, sizeof(MinresScalars)));
 }
@@ -716,6 +936,7 @@ static void upload_csr(mpet_ctx* c, const HostCsr& h, Csr& d, bool fp32) {
         MPET_CHECK_LAUNCH();
     }
     d.lpr = choose_lpr(d.n, d.nnz);
+    build_tiles(c, d, h.rp.data());
 }
 
 void upload_amg(mpet_ctx* c, AmgHier& h, const HostAmg& ha, int nvec, bool fp32) {
