@@ -150,6 +150,7 @@ int mpet_setup(mpet_ctx* c, const mpet_params* p) {
     c->Lu.v64 = c->pool.alloc<double>(c->Lu.nnz);
     for (int a = 0; a < c->J; ++a) c->Pp[a].v64 = c->pool.alloc<double>(c->Pp[a].nnz);
     alloc_krylov(c);
+    autotune_system(c);
     MPET_CUDA(cudaStreamSynchronize(c->stream));
     c->setup_done = true;
     API_END(c)
@@ -365,7 +366,7 @@ int mpet_setup_preconditioner(mpet_ctx* c, double dt) {
         } else {
             amg_setup_host(h, nullptr, c->prm.amg_theta, cs, 12, ha);
         }
-        upload_amg(c, c->amg_u, ha, 3, fp32);
+        upload_amg(c, c->amg_u, ha, 4, fp32);
     }
     for (int a = 0; a < c->J; ++a) {
         HostCsr h;

@@ -95,6 +95,8 @@ struct AmgHier {
     std::vector<AmgLevel> lev;
     int64_t ncoarse = 0;
     double* cinv = nullptr;  // dense inverse of the coarsest operator, FP64
+    void* pack_in = nullptr;  // padded (nvec = 4) input/output of the first level
+    void* pack_out = nullptr;
 };
 
 // Device-resident MINRES scalars (all FP64).
@@ -242,6 +244,7 @@ void spmv(mpet_ctx* c, const Csr& A, int nvec, const T* x, T* y);
 void upload_amg(mpet_ctx* c, AmgHier& h, const HostAmg& ha, int nvec, bool fp32);
 int solve_system(mpet_ctx* c, const double* b, double* x, mpet_stats* st);
 void alloc_krylov(mpet_ctx* c);
+void autotune_system(mpet_ctx* c);
 int choose_lpr(int64_t n, int64_t nnz);
 void build_tiles(mpet_ctx* c, Csr& A, const int64_t* rp_host);
 constexpr int SPMV_TILE = 2048;  // entries per staged tile

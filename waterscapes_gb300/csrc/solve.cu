@@ -70,6 +70,45 @@ __device__ __forceinline__ double sum_partials(const double* p, double* sh) {
     return block_sum256(v, sh);
 }
 
+// ---- vector access -------------------------------------------------------------
+// Multi-vector data is node-interleaved (NV values per row).  With NV = 4
+// every row's values are one 16-byte-aligned group, accessed by vector
+// loads/stores (float4, or two double2 for FP64).
+
+template <typename T, int NV>
+struct VecIO {
+    static __device__ __forceinline__ void load(const T* p, int64_t row, T* v) {
+#pragma unroll
+        for (int k = 0; k < NV; ++k) v[k] = p[NV * row + k];
+    }
+    static __device__ __forceinline__ void store(T* p, int64_t row, const T* v) {
+#pragma unroll
+        for (int k = 0; k < NV; ++k) p[NV * row + k] = v[k];
+    }
+};
+template <>
+struct VecIO<float, 4> {
+    static __device__ __forceinline__ void load(const float* p, int64_t row, float* v) {
+        const float4 q = reinterpret_cast<const float4*>(p)[row];
+        v[0] = q.x; v[1] = q.y; v[2] = q.z; v[3] = q.w;
+    }
+    static __device__ __forceinline__ void store(float* p, int64_t row, const float* v) {
+        reinterpret_cast<float4*>(p)[row] = make_float4(v[0], v[1], v[2], v[3]);
+    }
+};
+template <>
+struct VecIO<double, 4> {
+    static __device__ __forceinline__ void load(const double* p, int64_t row, double* v) {
+        const double2 a = reinterpret_cast<const double2*>(p)[2 * row];
+        const double2 b = reinterpret_cast<const double2*>(p)[2 * row + 1];
+        v[0] = a.x; v[1] = a.y; v[2] = b.x; v[3] = b.y;
+    }
+    static __device__ __forceinline__ void store(double* p, int64_t row, const double* v) {
+        reinterpret_cast<double2*>(p)[2 * row] = make_double2(v[0], v[1]);
+        reinterpret_cast<double2*>(p)[2 * row + 1] = make_double2(v[2], v[3]);
+    }
+};
+
 // ---- SpMV with fused epilogues -------------------------------------------------------
 
 template <typename T, int NV>
@@ -77,8 +116,7 @@ struct EpiStore {
     T* y;
     static constexpr int kRed = 0;
     __device__ __forceinline__ void operator()(int64_t row, const T* acc, double&, double&) const {
-#pragma unroll
-        for (int k = 0; k < NV; ++k) y[NV * row + k] = acc[k];
+        VecIO<T, NV>::store(y, row, acc);
     }
 };
 
@@ -90,11 +128,11 @@ struct EpiAxpby {
     T alpha, beta;
     static constexpr int kRed = 0;
     __device__ __forceinline__ void operator()(int64_t row, const T* acc, double&, double&) const {
+        T zz[NV], out[NV];
+        if (z) VecIO<T, NV>::load(z, row, zz);
 #pragma unroll
-        for (int k = 0; k < NV; ++k) {
-            T zz = z ? z[NV * row + k] : T(0);
-            y[NV * row + k] = alpha * acc[k] + beta * zz;
-        }
+        for (int k = 0; k < NV; ++k) out[k] = alpha * acc[k] + beta * (z ? zz[k] : T(0));
+        VecIO<T, NV>::store(y, row, out);
     }
 };
 
@@ -110,13 +148,17 @@ struct EpiCheb {
     static constexpr int kRed = 0;
     __device__ __forceinline__ void operator()(int64_t row, const T* acc, double&, double&) const {
         const T di = dinv[row];
+        T bb[NV], dd[NV], xx[NV];
+        VecIO<T, NV>::load(b, row, bb);
+        VecIO<T, NV>::load(d, row, dd);
+        VecIO<T, NV>::load(xin, row, xx);
 #pragma unroll
         for (int k = 0; k < NV; ++k) {
-            const int64_t i = NV * row + k;
-            const T dn = c1 * d[i] + c2 * di * (b[i] - acc[k]);
-            d[i] = dn;
-            xout[i] = xin[i] + dn;
+            dd[k] = c1 * dd[k] + c2 * di * (bb[k] - acc[k]);
+            xx[k] += dd[k];
         }
+        VecIO<T, NV>::store(d, row, dd);
+        VecIO<T, NV>::store(xout, row, xx);
     }
 };
 
@@ -200,9 +242,12 @@ __global__ void __launch_bounds__(256) k_spmv(int64_t n, const int64_t* __restri
                 }
                 if (b + LPR * U < e1) load_chunk(b + LPR * U);
 #pragma unroll
-                for (int u = 0; u < U; ++u)
+                for (int u = 0; u < U; ++u) {
+                    T xv[NV];
+                    VecIO<T, NV>::load(x, c0[u], xv);
 #pragma unroll
-                    for (int k = 0; k < NV; ++k) acc[k] += a0[u] * x[(int64_t)NV * c0[u] + k];
+                    for (int k = 0; k < NV; ++k) acc[k] += a0[u] * xv[k];
+                }
             }
         }
 #pragma unroll
@@ -335,10 +380,11 @@ __global__ void __launch_bounds__(256) k_spmv_staged(const int64_t* __restrict__
             if (row < re) {
                 const int s = (int)(rp[row] - a0), e = (int)(rp[row + 1] - a0);
                 for (int q = s + sub; q < e; q += LPR) {
-                    const int64_t cidx = sc[q];
                     const T a = sv[q];
+                    T xv[NV];
+                    VecIO<T, NV>::load(x, sc[q], xv);
 #pragma unroll
-                    for (int k = 0; k < NV; ++k) acc[k] += a * x[NV * cidx + k];
+                    for (int k = 0; k < NV; ++k) acc[k] += a * xv[k];
                 }
             }
 #pragma unroll
@@ -456,9 +502,53 @@ const double* dinv_of<double>(const AmgLevel& L) { return L.dinv64; }
 template <>
 const float* dinv_of<float>(const AmgLevel& L) { return L.dinv32; }
 
+// Set-up autotuning: time the staged and the register SpMV on this matrix
+// (values, x and y in the given buffers) and keep the faster one.
+template <typename T, int NV>
+static void autotune_matrix(mpet_ctx* c, Csr& A, const T* x, T* y) {
+    if (A.ntiles == 0 || vals<T>(A) == nullptr) return;
+    const int saved = A.ntiles;
+    auto time_it = [&](bool staged) {
+        A.ntiles = staged ? saved : 0;
+        launch_spmv<T, NV>(c, A, vals<T>(A), x, EpiStore<T, NV>{y});
+        MPET_CUDA(cudaEventRecord(c->ev0, c->stream));
+        for (int q = 0; q < 3; ++q) launch_spmv<T, NV>(c, A, vals<T>(A), x, EpiStore<T, NV>{y});
+        MPET_CUDA(cudaEventRecord(c->ev1, c->stream));
+        MPET_CUDA(cudaEventSynchronize(c->ev1));
+        float ms = 0.f;
+        MPET_CUDA(cudaEventElapsedTime(&ms, c->ev0, c->ev1));
+        return ms;
+    };
+    const float ts = time_it(true), tr = time_it(false);
+    A.ntiles = ts < tr ? saved : 0;
+    c->n_launch -= 8;
+}
+
+void autotune_system(mpet_ctx* c) {
+    MPET_CUDA(cudaMemsetAsync(c->kv, 0, sizeof(double) * c->N, c->stream));
+    if (c->A.v32) autotune_matrix<float, 1>(c, c->A, (const float*)c->kv, (float*)c->kd);
+    else autotune_matrix<double, 1>(c, c->A, (const double*)c->kv, (double*)c->kd);
+}
+
+template <typename T, int NV>
+static void autotune_hier(mpet_ctx* c, AmgHier& h) {
+    for (size_t k = 0; k < h.lev.size(); ++k) {
+        AmgLevel& L = h.lev[k];
+        MPET_CUDA(cudaMemsetAsync(L.x, 0, sizeof(double) * L.A.n * NV, c->stream));
+        MPET_CUDA(cudaMemsetAsync(L.r, 0, sizeof(double) * L.A.n * NV, c->stream));
+        autotune_matrix<T, NV>(c, L.A, (const T*)L.x, (T*)L.t0);
+        if (k + 1 < h.lev.size()) {
+            AmgLevel& C = h.lev[k + 1];
+            MPET_CUDA(cudaMemsetAsync(C.x, 0, sizeof(double) * C.A.n * NV, c->stream));
+            autotune_matrix<T, NV>(c, L.P, (const T*)C.x, (T*)L.t0);
+            autotune_matrix<T, NV>(c, L.R, (const T*)L.r, (T*)C.b);
+        }
+    }
+}
+
 template <typename T>
 void spmv(mpet_ctx* c, const Csr& A, int nvec, const T* x, T* y) {
-    if (nvec == 3) launch_spmv<T, 3>(c, A, vals<T>(A), x, EpiStore<T, 3>{y});
+    if (nvec == 4) launch_spmv<T, 4>(c, A, vals<T>(A), x, EpiStore<T, 4>{y});
     else launch_spmv<T, 1>(c, A, vals<T>(A), x, EpiStore<T, 1>{y});
 }
 template void spmv<double>(mpet_ctx*, const Csr&, int, const double*, double*);
@@ -639,9 +729,9 @@ __global__ void k_f64_to_f32(int64_t n, const double* __restrict__ a, float* b) 
 
 // ---- AMG V-cycle -------------------------------------------------------------------------
 
-template <typename T>
+template <typename T, int NV>
 static void cheb(mpet_ctx* c, AmgHier& h, AmgLevel& L, const T* b, const T* xin, T* xout) {
-    const int nv = h.nvec;
+    const int nv = NV;
     const int64_t n = L.A.n * nv;
     const double hi = 1.1 * L.rho, lo = hi / 30.0;
     const double theta = 0.5 * (hi + lo), delta = 0.5 * (hi - lo);
@@ -658,30 +748,24 @@ static void cheb(mpet_ctx* c, AmgHier& h, AmgLevel& L, const T* b, const T* xin,
         MPET_CHECK_LAUNCH();
         c->n_launch++;
     } else {
-        if (nv == 3)
-            launch_spmv<T, 3>(c, L.A, vals<T>(L.A), xin, EpiCheb<T, 3>{b, xin, d, cur, dinv, T(0), (T)(1.0 / theta)});
-        else
-            launch_spmv<T, 1>(c, L.A, vals<T>(L.A), xin, EpiCheb<T, 1>{b, xin, d, cur, dinv, T(0), (T)(1.0 / theta)});
+        const EpiCheb<T, NV> e{b, xin, d, cur, dinv, T(0), (T)(1.0 / theta)};
+        launch_spmv<T, NV>(c, L.A, vals<T>(L.A), xin, e);
     }
     for (int j = 1; j < s; ++j) {
         const double rho_new = 1.0 / (2.0 * sigma - rho_old);
         const T c1 = (T)(rho_new * rho_old), c2 = (T)(2.0 * rho_new / delta);
         T* nxt = (j == s - 1) ? xout : (cur == t0 ? t1 : t0);
-        if (nv == 3)
-            launch_spmv<T, 3>(c, L.A, vals<T>(L.A), cur, EpiCheb<T, 3>{b, cur, d, nxt, dinv, c1, c2});
-        else
-            launch_spmv<T, 1>(c, L.A, vals<T>(L.A), cur, EpiCheb<T, 1>{b, cur, d, nxt, dinv, c1, c2});
+        launch_spmv<T, NV>(c, L.A, vals<T>(L.A), cur, EpiCheb<T, NV>{b, cur, d, nxt, dinv, c1, c2});
         cur = nxt;
         rho_old = rho_new;
     }
 }
 
-template <typename T>
+template <typename T, int NV>
 static void vcycle(mpet_ctx* c, AmgHier& h, size_t k, const T* b, T* x) {
-    const int nv = h.nvec;
     if (k + 1 == h.lev.size()) {
-        const int64_t rows = h.ncoarse * nv;
-        k_dense_coarse<T><<<grid_for(rows * 32, 256), 256, 0, c->stream>>>(h.ncoarse, nv, h.cinv, b, x);
+        const int64_t rows = h.ncoarse * NV;
+        k_dense_coarse<T><<<grid_for(rows * 32, 256), 256, 0, c->stream>>>(h.ncoarse, NV, h.cinv, b, x);
         MPET_CHECK_LAUNCH();
         c->n_launch++;
         return;
@@ -690,28 +774,49 @@ static void vcycle(mpet_ctx* c, AmgHier& h, size_t k, const T* b, T* x) {
     AmgLevel& C = h.lev[k + 1];
     T* xs = (T*)L.x;
     T* r = (T*)L.r;
-    cheb<T>(c, h, L, b, nullptr, xs);
-    if (nv == 3) {
-        launch_spmv<T, 3>(c, L.A, vals<T>(L.A), xs, EpiAxpby<T, 3>{r, b, T(-1), T(1)});
-        launch_spmv<T, 3>(c, L.R, vals<T>(L.R), r, EpiStore<T, 3>{(T*)C.b});
-    } else {
-        launch_spmv<T, 1>(c, L.A, vals<T>(L.A), xs, EpiAxpby<T, 1>{r, b, T(-1), T(1)});
-        launch_spmv<T, 1>(c, L.R, vals<T>(L.R), r, EpiStore<T, 1>{(T*)C.b});
-    }
-    vcycle<T>(c, h, k + 1, (const T*)C.b, (T*)C.x);
-    if (nv == 3)
-        launch_spmv<T, 3>(c, L.P, vals<T>(L.P), (const T*)C.x, EpiAxpby<T, 3>{xs, xs, T(1), T(1)});
-    else
-        launch_spmv<T, 1>(c, L.P, vals<T>(L.P), (const T*)C.x, EpiAxpby<T, 1>{xs, xs, T(1), T(1)});
-    cheb<T>(c, h, L, b, xs, x);
+    cheb<T, NV>(c, h, L, b, nullptr, xs);
+    launch_spmv<T, NV>(c, L.A, vals<T>(L.A), xs, EpiAxpby<T, NV>{r, b, T(-1), T(1)});
+    launch_spmv<T, NV>(c, L.R, vals<T>(L.R), r, EpiStore<T, NV>{(T*)C.b});
+    vcycle<T, NV>(c, h, k + 1, (const T*)C.b, (T*)C.x);
+    launch_spmv<T, NV>(c, L.P, vals<T>(L.P), (const T*)C.x, EpiAxpby<T, NV>{xs, xs, T(1), T(1)});
+    cheb<T, NV>(c, h, L, b, xs, x);
+}
+
+// displacement components (3 per node) <-> the padded 4-wide layout of the
+// displacement hierarchy
+template <typename T>
+__global__ void k_pack34(int64_t nodes, const T* __restrict__ a, T* b4) {
+    const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    if (i >= nodes) return;
+    const T v[4] = {a[3 * i], a[3 * i + 1], a[3 * i + 2], T(0)};
+    VecIO<T, 4>::store(b4, i, v);
+}
+
+template <typename T>
+__global__ void k_unpack43(int64_t nodes, const T* __restrict__ b4, T* a) {
+    const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    if (i >= nodes) return;
+    T v[4];
+    VecIO<T, 4>::load(b4, i, v);
+    a[3 * i] = v[0];
+    a[3 * i + 1] = v[1];
+    a[3 * i + 2] = v[2];
 }
 
 template <typename T>
 static void precond(mpet_ctx* c, const T* r, T* z) {
-    vcycle<T>(c, c->amg_u, 0, r, z);
+    AmgHier& hu = c->amg_u;
+    const int64_t nodes = c->nnodes;
+    T* bin = (T*)hu.pack_in;
+    T* xout = (T*)hu.pack_out;
+    k_pack34<T><<<grid_for(nodes, 256), 256, 0, c->stream>>>(nodes, r, bin);
+    vcycle<T, 4>(c, hu, 0, bin, xout);
+    k_unpack43<T><<<grid_for(nodes, 256), 256, 0, c->stream>>>(nodes, xout, z);
+    MPET_CHECK_LAUNCH();
+    c->n_launch += 2;
     for (int a = 0; a < c->J; ++a) {
         const int64_t off = c->Nu + (int64_t)a * c->nv;
-        vcycle<T>(c, c->amg_p[a], 0, r + off, z + off);
+        vcycle<T, 1>(c, c->amg_p[a], 0, r + off, z + off);
     }
 }
 
@@ -967,6 +1072,15 @@ void upload_amg(mpet_ctx* c, AmgHier& h, const HostAmg& ha, int nvec, bool fp32)
         L.d = c->pool.alloc<double>(nn);
         L.t0 = c->pool.alloc<double>(nn);
         L.t1 = c->pool.alloc<double>(nn);
+    }
+    if (nvec == 4) {
+        h.pack_in = c->pool.alloc<double>(ha.lev[0].A.n * 4);
+        h.pack_out = c->pool.alloc<double>(ha.lev[0].A.n * 4);
+    }
+    if (nvec == 4) {
+        if (fp32) autotune_hier<float, 4>(c, h); else autotune_hier<double, 4>(c, h);
+    } else {
+        if (fp32) autotune_hier<float, 1>(c, h); else autotune_hier<double, 1>(c, h);
     }
     h.ncoarse = ha.ncoarse;
     h.cinv = c->pool.alloc<double>(ha.ncoarse * ha.ncoarse);
