@@ -210,17 +210,15 @@ __global__ void __launch_bounds__(256) k_spmv(int64_t n, const int64_t* __restri
 #pragma unroll
         for (int k = 0; k < NV; ++k) acc[k] = T(0);
         if (row < n) {
-            // Chunks of U (column, value) pairs per lane; the loads of the next
-            // chunk are issued before the dependent x gathers of the current
-            // one, so each warp keeps two chunks of matrix stream in flight.
-            // Matrix loads are evict-first so x stays resident in L2.  Every
-            // address is clamped into the (non-empty) row, so a load issued
-            // regardless of its predicate stays in bounds.
+            // Chunks of U (column, value) pairs per lane, all issued before the
+            // dependent x gathers.  Matrix loads are evict-first so x stays
+            // resident in L2.  Every address is clamped into the (non-empty)
+            // row, so a load issued regardless of its predicate stays in bounds.
             constexpr int U = 4;
             const int64_t e0 = rp[row], e1 = rp[row + 1];
-            int32_t cc[U];
-            T aa[U];
-            auto load_chunk = [&](int64_t b) {
+            for (int64_t b = e0; b < e1; b += LPR * U) {
+                int32_t cc[U];
+                T aa[U];
 #pragma unroll
                 for (int u = 0; u < U; ++u) {
                     const int64_t e = b + sub + u * LPR;
@@ -230,23 +228,12 @@ __global__ void __launch_bounds__(256) k_spmv(int64_t n, const int64_t* __restri
                     const T a = __ldcs(va + es);
                     aa[u] = ok ? a : T(0);
                 }
-            };
-            if (e0 < e1) load_chunk(e0);
-            for (int64_t b = e0; b < e1; b += LPR * U) {
-                int32_t c0[U];
-                T a0[U];
-#pragma unroll
-                for (int u = 0; u < U; ++u) {
-                    c0[u] = cc[u];
-                    a0[u] = aa[u];
-                }
-                if (b + LPR * U < e1) load_chunk(b + LPR * U);
 #pragma unroll
                 for (int u = 0; u < U; ++u) {
                     T xv[NV];
-                    VecIO<T, NV>::load(x, c0[u], xv);
+                    VecIO<T, NV>::load(x, cc[u], xv);
 #pragma unroll
-                    for (int k = 0; k < NV; ++k) acc[k] += a0[u] * xv[k];
+                    for (int k = 0; k < NV; ++k) acc[k] += aa[u] * xv[k];
                 }
             }
         }
