@@ -154,6 +154,13 @@ int mpet_solve(mpet_ctx* ctx, const double* b, double* x, mpet_stats* stats);
  * (mpetsolver.py:424-462). */
 int mpet_step(mpet_ctx* ctx, double dt, const double* up_prev, double* up, mpet_stats* stats);
 
+/* FP64 residual r = b - A x of the assembled (Dirichlet-row) system and its
+ * Jacobi-scaled norms: norms_host[0] = ||D^-1 r||_2, norms_host[1] =
+ * ||D^-1 b||_2 (D = |diag A|).  The relative residual the reference's Krylov
+ * path monitors (PETScKrylovSolver.solve, mpetsolver.py:556) in the
+ * diagonally scaled norm; the reduction uses the context's scratch. */
+int mpet_residual(mpet_ctx* ctx, const double* b, const double* x, double* r, double* norms_host);
+
 /* y = A x with the assembled values; precision selects FP64 (x, y double)
  * or the FP32 copy (x, y float).  Used by tests and the bandwidth bench. */
 int mpet_spmv(mpet_ctx* ctx, int32_t precision, const void* x, void* y);

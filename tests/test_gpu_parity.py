@@ -182,6 +182,43 @@ def test_spmv_parity(precision):
         assert np.linalg.norm(_np(y32) - y_ref) <= 1e-5 * np.linalg.norm(y_ref)
 
 
+def test_residual_matches_oracle():
+    J = 2
+    problem, dt = make_problem(4, J)
+    s = _solver(problem, dt, precision="mixed")
+    om = make_oracle(problem)
+    A = om.apply_bc_matrix(om.assemble_matrix(dt), om.dirichlet_values(dt, oracle_data(J))[0])
+    s.ctx.call("mpet_assemble", dt, 1)
+    rng = np.random.default_rng(5)
+    x = rng.standard_normal(om.dm.N)
+    b = rng.standard_normal(om.dm.N)
+    r_ref = b - A @ x
+    dinv = 1.0 / np.abs(A.diagonal())
+    nr_ref, nb_ref = np.linalg.norm(r_ref * dinv), np.linalg.norm(b * dinv)
+    r = torch.empty(s.N, dtype=torch.float64, device=s.device)
+    norms = np.zeros(2)
+    s.ctx.call("mpet_residual", _lib()._ptr(torch.tensor(b, device=s.device)),
+               _lib()._ptr(torch.tensor(x, device=s.device)), _lib()._ptr(r), _lib()._ptr(norms))
+    assert np.allclose(_np(r), r_ref, rtol=1e-12, atol=1e-12 * np.abs(r_ref).max())
+    assert norms[0] == pytest.approx(nr_ref, rel=1e-12)
+    assert norms[1] == pytest.approx(nb_ref, rel=1e-12)
+
+
+def test_theta_half_step_matches_direct_solve():
+    J = 2
+    problem, dt = make_problem(4, J)
+    s = _solver(problem, dt, precision="mixed", theta=0.5, rtol=1e-11)
+    om = make_oracle(problem, theta=0.5)
+    rng = np.random.default_rng(6)
+    up_prev = rng.standard_normal(om.dm.N) * 1e-2
+    x_ref = om.step(up_prev, 0.0, dt, oracle_data(J))
+    s.up_.assign(torch.tensor(up_prev))
+    problem.time.assign(0.0)
+    s.step(dt)
+    x = _np(s.up.vector())
+    assert np.linalg.norm(x - x_ref) <= 1e-8 * np.linalg.norm(x_ref)
+
+
 def test_assembly_and_solve_are_deterministic():
     J = 2
     problem, dt = make_problem(4, J)

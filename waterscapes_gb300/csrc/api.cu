@@ -423,6 +423,14 @@ int mpet_step(mpet_ctx* c, double dt, const double* up_prev, double* up, mpet_st
     API_END(c)
 }
 
+int mpet_residual(mpet_ctx* c, const double* b, const double* x, double* r, double* norms) {
+    API_BEGIN(c)
+    require(c->assembled, MPET_ERR_STATE, "mpet_assemble must come first");
+    require(b && x && r && norms, MPET_ERR_INVALID, "NULL argument");
+    residual_norms(c, b, x, r, norms);
+    API_END(c)
+}
+
 int mpet_spmv(mpet_ctx* c, int32_t precision, const void* x, void* y) {
     API_BEGIN(c)
     require(c->assembled, MPET_ERR_STATE, "mpet_assemble must come first");

@@ -987,6 +987,16 @@ static int solve_impl(mpet_ctx* c, const double* b, double* x, mpet_stats* st) {
     return status;
 }
 
+void residual_norms(mpet_ctx* c, const double* b, const double* x, double* r, double* norms) {
+    launch_spmv<double, 1>(c, c->A, c->A.v64, x, EpiResid64{r, b, c->dinv});
+    k_outer_norms<<<1, 256, 0, c->stream>>>(c->sc, c->partials);
+    MPET_CHECK_LAUNCH();
+    MPET_CUDA(cudaMemcpyAsync(c->sc_host, c->sc, sizeof(MinresScalars), cudaMemcpyDeviceToHost, c->stream));
+    MPET_CUDA(cudaStreamSynchronize(c->stream));
+    norms[0] = sqrt(c->sc_host->nr2);
+    norms[1] = sqrt(c->sc_host->nb2);
+}
+
 int solve_system(mpet_ctx* c, const double* b, double* x, mpet_stats* st) {
     if (c->prm.precision == MPET_PRECISION_MIXED) return solve_impl<float>(c, b, x, st);
     return solve_impl<double>(c, b, x, st);
