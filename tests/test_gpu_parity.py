@@ -171,7 +171,8 @@ def test_spmv_parity(precision):
     x = rng.standard_normal(om.dm.N)
     y_ref = A @ x
     y64 = torch.empty(s.N, dtype=torch.float64, device=s.device)
-    s.ctx.call("mpet_spmv", 0, _lib()._ptr(torch.tensor(x, device=s.device)), _lib()._ptr(y64))
+    xg = torch.tensor(x, device=s.device)
+    s.ctx.call("mpet_spmv", 0, _lib()._ptr(xg), _lib()._ptr(y64))
     torch.cuda.synchronize()
     assert np.allclose(_np(y64), y_ref, rtol=1e-12, atol=1e-12 * np.abs(y_ref).max())
     if precision == "mixed":
@@ -197,8 +198,9 @@ def test_residual_matches_oracle():
     nr_ref, nb_ref = np.linalg.norm(r_ref * dinv), np.linalg.norm(b * dinv)
     r = torch.empty(s.N, dtype=torch.float64, device=s.device)
     norms = np.zeros(2)
-    s.ctx.call("mpet_residual", _lib()._ptr(torch.tensor(b, device=s.device)),
-               _lib()._ptr(torch.tensor(x, device=s.device)), _lib()._ptr(r), _lib()._ptr(norms))
+    bg = torch.tensor(b, device=s.device)
+    xg = torch.tensor(x, device=s.device)
+    s.ctx.call("mpet_residual", _lib()._ptr(bg), _lib()._ptr(xg), _lib()._ptr(r), _lib()._ptr(norms))
     assert np.allclose(_np(r), r_ref, rtol=1e-12, atol=1e-12 * np.abs(r_ref).max())
     assert norms[0] == pytest.approx(nr_ref, rel=1e-12)
     assert norms[1] == pytest.approx(nb_ref, rel=1e-12)

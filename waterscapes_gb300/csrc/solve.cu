@@ -992,7 +992,13 @@ void residual_norms(mpet_ctx* c, const double* b, const double* x, double* r, do
     k_outer_norms<<<1, 256, 0, c->stream>>>(c->sc, c->partials);
     MPET_CHECK_LAUNCH();
     MPET_CUDA(cudaMemcpyAsync(c->sc_host, c->sc, sizeof(MinresScalars), cudaMemcpyDeviceToHost, c->stream));
+    int derr = 0;
+    MPET_CUDA(cudaMemcpyAsync(&derr, c->dev_err, sizeof(int), cudaMemcpyDeviceToHost, c->stream));
     MPET_CUDA(cudaStreamSynchronize(c->stream));
+    if (derr) {
+        MPET_CUDA(cudaMemsetAsync(c->dev_err, 0, sizeof(int), c->stream));
+        fail(MPET_ERR_TIMEOUT, "a staged SpMV copy did not complete within its wait limit");
+    }
     norms[0] = sqrt(c->sc_host->nr2);
     norms[1] = sqrt(c->sc_host->nb2);
 }
