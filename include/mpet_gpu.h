@@ -161,6 +161,17 @@ int mpet_step(mpet_ctx* ctx, double dt, const double* up_prev, double* up, mpet_
  * diagonally scaled norm; the reduction uses the context's scratch. */
 int mpet_residual(mpet_ctx* ctx, const double* b, const double* x, double* r, double* norms_host);
 
+/* Same result as mpet_residual for callers that cannot allocate device
+ * memory (their allocator already holds the device, or they may not
+ * allocate or synchronise after start-up).  No counterpart in the
+ * reference: it exists only for such callers.  It allocates nothing: the
+ * reduction scratch is a 256 KiB static device array that every GPU loading
+ * the library keeps until exit, so the system may have at most 33,554,432
+ * rows (larger systems get MPET_ERR_INVALID).  The first call on a device
+ * looks up the array's device address and should come before any stream
+ * capture; calls that overlap on the GPU share the array and race. */
+int mpet_residual_noalloc(mpet_ctx* ctx, const double* b, const double* x, double* r, double* norms_host);
+
 /* y = A x with the assembled values; precision selects FP64 (x, y double)
  * or the FP32 copy (x, y float).  Used by tests and the bandwidth bench. */
 int mpet_spmv(mpet_ctx* ctx, int32_t precision, const void* x, void* y);

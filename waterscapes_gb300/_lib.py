@@ -100,6 +100,7 @@ SIGNATURES = {
     "mpet_solve": [_P, _P, _P, ctypes.POINTER(MpetStats)],
     "mpet_step": [_P, _D, _P, _P, ctypes.POINTER(MpetStats)],
     "mpet_residual": [_P, _P, _P, _P, _P],
+    "mpet_residual_noalloc": [_P, _P, _P, _P, _P],
     "mpet_spmv": [_P, _I32, _P, _P],
     "mpet_apply_symmetric": [_P, _P, _P],
     "mpet_get_timing": [_P, ctypes.POINTER(_D), ctypes.POINTER(_I64), ctypes.POINTER(_D), ctypes.POINTER(_I64)],
