@@ -37,7 +37,8 @@ int choose_lpr(int64_t n, int64_t nnz) {
     if (avg >= 48.0) return 32;
     if (avg >= 20.0) return 16;
     if (avg >= 8.0) return 8;
-    return 4;
+    if (avg >= 3.0) return 4;
+    return 1;
 }
 
 // ---- reductions ------------------------------------------------------------------
@@ -110,12 +111,18 @@ struct VecIO<double, 4> {
 };
 
 // ---- SpMV with fused epilogues -------------------------------------------------------
+//
+// An epilogue has pre(row), which loads the row's other operands and is
+// issued before the row's gather loop so that its latency overlaps the
+// gathers, and apply(row, acc, pre, ...), which combines them with A x.
 
 template <typename T, int NV>
 struct EpiStore {
     T* y;
     static constexpr int kRed = 0;
-    __device__ __forceinline__ void operator()(int64_t row, const T* acc, double&, double&) const {
+    struct Pre {};
+    __device__ __forceinline__ Pre pre(int64_t) const { return Pre{}; }
+    __device__ __forceinline__ void apply(int64_t row, const T* acc, const Pre&, double&, double&) const {
         VecIO<T, NV>::store(y, row, acc);
     }
 };
@@ -127,11 +134,21 @@ struct EpiAxpby {
     const T* z;
     T alpha, beta;
     static constexpr int kRed = 0;
-    __device__ __forceinline__ void operator()(int64_t row, const T* acc, double&, double&) const {
-        T zz[NV], out[NV];
-        if (z) VecIO<T, NV>::load(z, row, zz);
+    struct Pre {
+        T zz[NV];
+    };
+    __device__ __forceinline__ Pre pre(int64_t row) const {
+        Pre p;
+        if (z) VecIO<T, NV>::load(z, row, p.zz);
+        else
 #pragma unroll
-        for (int k = 0; k < NV; ++k) out[k] = alpha * acc[k] + beta * (z ? zz[k] : T(0));
+            for (int k = 0; k < NV; ++k) p.zz[k] = T(0);
+        return p;
+    }
+    __device__ __forceinline__ void apply(int64_t row, const T* acc, const Pre& p, double&, double&) const {
+        T out[NV];
+#pragma unroll
+        for (int k = 0; k < NV; ++k) out[k] = alpha * acc[k] + beta * p.zz[k];
         VecIO<T, NV>::store(y, row, out);
     }
 };
@@ -146,16 +163,23 @@ struct EpiCheb {
     const T* dinv;
     T c1, c2;
     static constexpr int kRed = 0;
-    __device__ __forceinline__ void operator()(int64_t row, const T* acc, double&, double&) const {
-        const T di = dinv[row];
-        T bb[NV], dd[NV], xx[NV];
-        VecIO<T, NV>::load(b, row, bb);
-        VecIO<T, NV>::load(d, row, dd);
-        VecIO<T, NV>::load(xin, row, xx);
+    struct Pre {
+        T bb[NV], dd[NV], xx[NV], di;
+    };
+    __device__ __forceinline__ Pre pre(int64_t row) const {
+        Pre p;
+        p.di = dinv[row];
+        VecIO<T, NV>::load(b, row, p.bb);
+        VecIO<T, NV>::load(d, row, p.dd);
+        VecIO<T, NV>::load(xin, row, p.xx);
+        return p;
+    }
+    __device__ __forceinline__ void apply(int64_t row, const T* acc, const Pre& p, double&, double&) const {
+        T dd[NV], xx[NV];
 #pragma unroll
         for (int k = 0; k < NV; ++k) {
-            dd[k] = c1 * dd[k] + c2 * di * (bb[k] - acc[k]);
-            xx[k] += dd[k];
+            dd[k] = c1 * p.dd[k] + c2 * p.di * (p.bb[k] - acc[k]);
+            xx[k] = p.xx[k] + dd[k];
         }
         VecIO<T, NV>::store(d, row, dd);
         VecIO<T, NV>::store(xout, row, xx);
@@ -170,11 +194,15 @@ struct EpiMinres {
     const T* v;
     const MinresScalars* sc;
     static constexpr int kRed = 1;
-    __device__ __forceinline__ void operator()(int64_t row, const T* acc, double& r0, double&) const {
+    struct Pre {
+        T r, v;
+    };
+    __device__ __forceinline__ Pre pre(int64_t row) const { return Pre{r1[row], v[row]}; }
+    __device__ __forceinline__ void apply(int64_t row, const T* acc, const Pre& p, double& r0, double&) const {
         const T c = (T)sc->c_r1;
-        const T yy = acc[0] - c * r1[row];
+        const T yy = acc[0] - c * p.r;
         y[row] = yy;
-        r0 += (double)v[row] * (double)yy;
+        r0 += (double)p.v * (double)yy;
     }
 };
 
@@ -184,12 +212,16 @@ struct EpiResid64 {
     const double* b;
     const double* dinv;
     static constexpr int kRed = 2;
-    __device__ __forceinline__ void operator()(int64_t row, const double* acc, double& r0, double& r1) const {
-        const double rr = b[row] - acc[0];
+    struct Pre {
+        double b, di;
+    };
+    __device__ __forceinline__ Pre pre(int64_t row) const { return Pre{b[row], dinv[row]}; }
+    __device__ __forceinline__ void apply(int64_t row, const double* acc, const Pre& p, double& r0,
+                                          double& r1) const {
+        const double rr = p.b - acc[0];
         r[row] = rr;
-        const double di = dinv[row];
-        r0 += (rr * di) * (rr * di);
-        r1 += (b[row] * di) * (b[row] * di);
+        r0 += (rr * p.di) * (rr * p.di);
+        r1 += (p.b * p.di) * (p.b * p.di);
     }
 };
 
@@ -209,6 +241,8 @@ __global__ void __launch_bounds__(256) k_spmv(int64_t n, const int64_t* __restri
         T acc[NV];
 #pragma unroll
         for (int k = 0; k < NV; ++k) acc[k] = T(0);
+        typename Epi::Pre pre{};
+        if (row < n && sub == 0) pre = epi.pre(row);
         if (row < n) {
             // Chunks of U (column, value) pairs per lane, all issued before the
             // dependent x gathers.  Matrix loads are evict-first so x stays
@@ -241,7 +275,7 @@ __global__ void __launch_bounds__(256) k_spmv(int64_t n, const int64_t* __restri
         for (int o = LPR / 2; o > 0; o >>= 1)
 #pragma unroll
             for (int k = 0; k < NV; ++k) acc[k] += __shfl_xor_sync(0xffffffffu, acc[k], o);
-        if (row < n && sub == 0) epi(row, acc, r0, r1);
+        if (row < n && sub == 0) epi.apply(row, acc, pre, r0, r1);
     }
     if constexpr (Epi::kRed > 0) {
         __shared__ double sh[8];
@@ -364,6 +398,8 @@ __global__ void __launch_bounds__(256) k_spmv_staged(const int64_t* __restrict__
             T acc[NV];
 #pragma unroll
             for (int k = 0; k < NV; ++k) acc[k] = T(0);
+            typename Epi::Pre pre{};
+            if (row < re && sub == 0) pre = epi.pre(row);
             if (row < re) {
                 const int s = (int)(rp[row] - a0), e = (int)(rp[row + 1] - a0);
                 for (int q = s + sub; q < e; q += LPR) {
@@ -378,7 +414,7 @@ __global__ void __launch_bounds__(256) k_spmv_staged(const int64_t* __restrict__
             for (int o = LPR / 2; o > 0; o >>= 1)
 #pragma unroll
                 for (int k = 0; k < NV; ++k) acc[k] += __shfl_xor_sync(0xffffffffu, acc[k], o);
-            if (row < re && sub == 0) epi(row, acc, r0, r1);
+            if (row < re && sub == 0) epi.apply(row, acc, pre, r0, r1);
         }
         __syncthreads();  // buffer b consumed before it is refilled
         b ^= 1;
@@ -453,7 +489,8 @@ static void launch_spmv(mpet_ctx* c, const Csr& A, const T* va, const T* x, cons
             case 32: launch_staged<T, NV, 32, Epi>(c, A, va, x, epi); return;
             case 16: launch_staged<T, NV, 16, Epi>(c, A, va, x, epi); return;
             case 8: launch_staged<T, NV, 8, Epi>(c, A, va, x, epi); return;
-            default: launch_staged<T, NV, 4, Epi>(c, A, va, x, epi); return;
+            case 4: launch_staged<T, NV, 4, Epi>(c, A, va, x, epi); return;
+            default: launch_staged<T, NV, 1, Epi>(c, A, va, x, epi); return;
         }
     }
     int blocks;
@@ -469,7 +506,8 @@ static void launch_spmv(mpet_ctx* c, const Csr& A, const T* va, const T* x, cons
         case 32: k_spmv<T, NV, 32, Epi><<<blocks, 256, 0, c->stream>>>(A.n, A.rp, A.ci, va, x, epi, part); break;
         case 16: k_spmv<T, NV, 16, Epi><<<blocks, 256, 0, c->stream>>>(A.n, A.rp, A.ci, va, x, epi, part); break;
         case 8: k_spmv<T, NV, 8, Epi><<<blocks, 256, 0, c->stream>>>(A.n, A.rp, A.ci, va, x, epi, part); break;
-        default: k_spmv<T, NV, 4, Epi><<<blocks, 256, 0, c->stream>>>(A.n, A.rp, A.ci, va, x, epi, part); break;
+        case 4: k_spmv<T, NV, 4, Epi><<<blocks, 256, 0, c->stream>>>(A.n, A.rp, A.ci, va, x, epi, part); break;
+        default: k_spmv<T, NV, 1, Epi><<<blocks, 256, 0, c->stream>>>(A.n, A.rp, A.ci, va, x, epi, part); break;
     }
     MPET_CHECK_LAUNCH();
     c->n_launch++;
