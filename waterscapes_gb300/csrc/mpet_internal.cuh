@@ -73,6 +73,7 @@ struct Csr {
     // whole rows holding at most SPMV_TILE entries (ntiles = 0: not staged).
     int32_t* tiles = nullptr;
     int ntiles = 0;
+    int max_row = 0;  // longest row (entries); selects the per-lane batch depth
 };
 
 struct AmgLevel {

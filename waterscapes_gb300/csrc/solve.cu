@@ -225,7 +225,7 @@ struct EpiResid64 {
     }
 };
 
-template <typename T, int NV, int LPR, class Epi>
+template <typename T, int NV, int LPR, int U, class Epi>
 __global__ void __launch_bounds__(256) k_spmv(int64_t n, const int64_t* __restrict__ rp,
                                               const int32_t* __restrict__ ci, const T* __restrict__ va,
                                               const T* __restrict__ x, Epi epi, double* partials) {
@@ -245,10 +245,11 @@ __global__ void __launch_bounds__(256) k_spmv(int64_t n, const int64_t* __restri
         if (row < n && sub == 0) pre = epi.pre(row);
         if (row < n) {
             // Chunks of U (column, value) pairs per lane, all issued before the
-            // dependent x gathers.  Matrix loads are evict-first so x stays
-            // resident in L2.  Every address is clamped into the (non-empty)
-            // row, so a load issued regardless of its predicate stays in bounds.
-            constexpr int U = 4;
+            // dependent x gathers (U is chosen so that LPR * U covers the
+            // longest row: one round trip per row).  Matrix loads are
+            // evict-first so x stays resident in L2.  Every address is clamped
+            // into the (non-empty) row, so a load issued regardless of its
+            // predicate stays in bounds.
             const int64_t e0 = rp[row], e1 = rp[row + 1];
             for (int64_t b = e0; b < e1; b += LPR * U) {
                 int32_t cc[U];
@@ -340,7 +341,7 @@ constexpr size_t staged_smem_bytes() {
     return 128 + 2 * (size_t)SPMV_CAP * (4 + sizeof(T));
 }
 
-template <typename T, int NV, int LPR, class Epi>
+template <typename T, int NV, int LPR, int U, class Epi>
 __global__ void __launch_bounds__(256) k_spmv_staged(const int64_t* __restrict__ rp, const int32_t* __restrict__ ci,
                                                      const T* __restrict__ va, const T* __restrict__ x, Epi epi,
                                                      double* partials, const int32_t* __restrict__ tiles, int ntiles,
@@ -401,13 +402,27 @@ __global__ void __launch_bounds__(256) k_spmv_staged(const int64_t* __restrict__
             typename Epi::Pre pre{};
             if (row < re && sub == 0) pre = epi.pre(row);
             if (row < re) {
+                // batches of U entries per lane: all shared-memory reads, then
+                // all x gathers, then the FMAs (indices clamped into the row)
                 const int s = (int)(rp[row] - a0), e = (int)(rp[row + 1] - a0);
-                for (int q = s + sub; q < e; q += LPR) {
-                    const T a = sv[q];
-                    T xv[NV];
-                    VecIO<T, NV>::load(x, sc[q], xv);
+                for (int q0 = s; q0 < e; q0 += LPR * U) {
+                    int32_t cc[U];
+                    T aa[U];
 #pragma unroll
-                    for (int k = 0; k < NV; ++k) acc[k] += a * xv[k];
+                    for (int u = 0; u < U; ++u) {
+                        const int q = q0 + sub + u * LPR;
+                        const bool ok = q < e;
+                        const int qs = ok ? q : e - 1;
+                        cc[u] = sc[qs];
+                        aa[u] = ok ? sv[qs] : T(0);
+                    }
+#pragma unroll
+                    for (int u = 0; u < U; ++u) {
+                        T xv[NV];
+                        VecIO<T, NV>::load(x, cc[u], xv);
+#pragma unroll
+                        for (int k = 0; k < NV; ++k) acc[k] += aa[u] * xv[k];
+                    }
                 }
             }
 #pragma unroll
@@ -441,10 +456,10 @@ __global__ void __launch_bounds__(256) k_spmv_staged(const int64_t* __restrict__
     }
 }
 
-template <typename T, int NV, int LPR, class Epi>
+template <typename T, int NV, int LPR, int U, class Epi>
 static void launch_staged(mpet_ctx* c, const Csr& A, const T* va, const T* x, const Epi& epi) {
     static int grid = 0;  // resident CTAs on this device (one per instantiation)
-    auto kern = k_spmv_staged<T, NV, LPR, Epi>;
+    auto kern = k_spmv_staged<T, NV, LPR, U, Epi>;
     const size_t sm = staged_smem_bytes<T>();
     if (grid == 0) {
         MPET_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm));
@@ -463,6 +478,8 @@ static void launch_staged(mpet_ctx* c, const Csr& A, const T* va, const T* x, co
 void build_tiles(mpet_ctx* c, Csr& A, const int64_t* rp) {
     A.ntiles = 0;
     A.tiles = nullptr;
+    A.max_row = 0;
+    for (int64_t r = 0; r < A.n; ++r) A.max_row = std::max<int64_t>(A.max_row, rp[r + 1] - rp[r]);
     if (A.nnz < (int64_t)SPMV_TILE * 64) return;  // small matrices: register kernel
     std::vector<int32_t> t;
     t.push_back(0);
@@ -484,13 +501,19 @@ void build_tiles(mpet_ctx* c, Csr& A, const int64_t* rp) {
 
 template <typename T, int NV, class Epi>
 static void launch_spmv(mpet_ctx* c, const Csr& A, const T* va, const T* x, const Epi& epi) {
+    // 32 lanes per row take 8 entries per lane and batch when rows exceed 128
+    // entries, so that every row is one round trip; narrower rows take 4
+    const bool deep = A.lpr == 32 && A.max_row > 128;
     if (A.ntiles > 0) {
         switch (A.lpr) {
-            case 32: launch_staged<T, NV, 32, Epi>(c, A, va, x, epi); return;
-            case 16: launch_staged<T, NV, 16, Epi>(c, A, va, x, epi); return;
-            case 8: launch_staged<T, NV, 8, Epi>(c, A, va, x, epi); return;
-            case 4: launch_staged<T, NV, 4, Epi>(c, A, va, x, epi); return;
-            default: launch_staged<T, NV, 1, Epi>(c, A, va, x, epi); return;
+            case 32:
+                if (deep) launch_staged<T, NV, 32, 8, Epi>(c, A, va, x, epi);
+                else launch_staged<T, NV, 32, 4, Epi>(c, A, va, x, epi);
+                return;
+            case 16: launch_staged<T, NV, 16, 4, Epi>(c, A, va, x, epi); return;
+            case 8: launch_staged<T, NV, 8, 4, Epi>(c, A, va, x, epi); return;
+            case 4: launch_staged<T, NV, 4, 4, Epi>(c, A, va, x, epi); return;
+            default: launch_staged<T, NV, 1, 4, Epi>(c, A, va, x, epi); return;
         }
     }
     int blocks;
@@ -502,12 +525,16 @@ static void launch_spmv(mpet_ctx* c, const Csr& A, const T* va, const T* x, cons
         if (blocks > 152 * 16) blocks = 152 * 16;
     }
     double* part = c->partials;
+    cudaStream_t s = c->stream;
     switch (A.lpr) {
-        case 32: k_spmv<T, NV, 32, Epi><<<blocks, 256, 0, c->stream>>>(A.n, A.rp, A.ci, va, x, epi, part); break;
-        case 16: k_spmv<T, NV, 16, Epi><<<blocks, 256, 0, c->stream>>>(A.n, A.rp, A.ci, va, x, epi, part); break;
-        case 8: k_spmv<T, NV, 8, Epi><<<blocks, 256, 0, c->stream>>>(A.n, A.rp, A.ci, va, x, epi, part); break;
-        case 4: k_spmv<T, NV, 4, Epi><<<blocks, 256, 0, c->stream>>>(A.n, A.rp, A.ci, va, x, epi, part); break;
-        default: k_spmv<T, NV, 1, Epi><<<blocks, 256, 0, c->stream>>>(A.n, A.rp, A.ci, va, x, epi, part); break;
+        case 32:
+            if (deep) k_spmv<T, NV, 32, 8, Epi><<<blocks, 256, 0, s>>>(A.n, A.rp, A.ci, va, x, epi, part);
+            else k_spmv<T, NV, 32, 4, Epi><<<blocks, 256, 0, s>>>(A.n, A.rp, A.ci, va, x, epi, part);
+            break;
+        case 16: k_spmv<T, NV, 16, 4, Epi><<<blocks, 256, 0, s>>>(A.n, A.rp, A.ci, va, x, epi, part); break;
+        case 8: k_spmv<T, NV, 8, 4, Epi><<<blocks, 256, 0, s>>>(A.n, A.rp, A.ci, va, x, epi, part); break;
+        case 4: k_spmv<T, NV, 4, 4, Epi><<<blocks, 256, 0, s>>>(A.n, A.rp, A.ci, va, x, epi, part); break;
+        default: k_spmv<T, NV, 1, 4, Epi><<<blocks, 256, 0, s>>>(A.n, A.rp, A.ci, va, x, epi, part); break;
     }
     MPET_CHECK_LAUNCH();
     c->n_launch++;
