@@ -171,6 +171,15 @@ def run_steps(solver, torch, steps, warmup, dt):
     return ms, its, solver.up.vector().clone()
 
 
+def spmv_tuning(solver):
+    import ctypes
+    ms = np.zeros(4)
+    ch = ctypes.c_int32()
+    solver.ctx.call("mpet_get_spmv_tuning", ms.ctypes.data_as(ctypes.c_void_p), ctypes.byref(ch))
+    names = ["register/4", "register/8", "staged/4", "staged/8"]
+    return {"ms": {names[v]: round(float(ms[v]), 4) for v in range(4) if ms[v] > 0}, "chosen": names[ch.value]}
+
+
 def launches(solver):
     import ctypes
     n = ctypes.c_int64()
@@ -392,6 +401,7 @@ def main():
         "step_semantics": {"ms_per_step": step_ms, "assemble_ms": asm_ms},
         "setup_s": {"mesh_dofmap_pattern": t_setup, "assemble_plus_amg": t_asm_amg},
         "spmv": spmv,
+        "spmv_tuning": spmv_tuning(sol),
         "roofline": {"kernel": "k_spmv<float,1,32,EpiMinres> (FP32 CSR SpMV)" if "fp32" in spmv else "k_spmv<double>",
                      "bound": "hbm", "achieved": sp32["gbs"], "peak": hbm, "unit": "GB/s",
                      "frac": sp32["gbs"] / hbm, "peak_kind": peak_kind,

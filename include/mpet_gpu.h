@@ -181,6 +181,12 @@ int mpet_spmv(mpet_ctx* ctx, int32_t precision, const void* x, void* y);
  * replaced by mpet_assemble).  b, if not NULL, is lifted with x_bc. */
 int mpet_apply_symmetric(mpet_ctx* ctx, double* b, const double* x_bc);
 
+/* Set-up autotuning of the system-matrix SpMV: ms per launch of the four
+ * variants (register / shared-memory staged x 4 / 8 entries per lane per
+ * batch; 0 where not applicable) and the chosen variant (0..3).  No
+ * reference counterpart (engine introspection for benchmarks). */
+int mpet_get_spmv_tuning(mpet_ctx* ctx, double* ms4_host, int32_t* chosen);
+
 /* Per-kernel timing of the last solve (CUDA events): total ms and launches. */
 int mpet_get_timing(mpet_ctx* ctx, double* spmv_ms, int64_t* spmv_launches,
                     double* precond_ms, int64_t* kernel_launches);

@@ -103,6 +103,7 @@ SIGNATURES = {
     "mpet_residual_noalloc": [_P, _P, _P, _P, _P],
     "mpet_spmv": [_P, _I32, _P, _P],
     "mpet_apply_symmetric": [_P, _P, _P],
+    "mpet_get_spmv_tuning": [_P, _P, ctypes.POINTER(_I32)],
     "mpet_get_timing": [_P, ctypes.POINTER(_D), ctypes.POINTER(_I64), ctypes.POINTER(_D), ctypes.POINTER(_I64)],
 }
 

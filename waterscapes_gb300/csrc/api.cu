@@ -452,6 +452,15 @@ int mpet_apply_symmetric(mpet_ctx* c, double* b, const double* xbc) {
     API_END(c)
 }
 
+int mpet_get_spmv_tuning(mpet_ctx* c, double* ms4, int32_t* chosen) {
+    API_BEGIN(c)
+    require(c->setup_done, MPET_ERR_STATE, "mpet_setup must come first");
+    if (ms4)
+        for (int v = 0; v < 4; ++v) ms4[v] = c->spmv_variant_ms[v];
+    if (chosen) *chosen = c->A.variant;
+    API_END(c)
+}
+
 int mpet_get_timing(mpet_ctx* c, double* spmv_ms, int64_t* spmv_launches, double* precond_ms, int64_t* launches) {
     API_BEGIN(c)
     if (spmv_ms) *spmv_ms = c->t_spmv_ms;

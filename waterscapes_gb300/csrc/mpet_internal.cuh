@@ -73,7 +73,10 @@ struct Csr {
     // whole rows holding at most SPMV_TILE entries (ntiles = 0: not staged).
     int32_t* tiles = nullptr;
     int ntiles = 0;
-    int max_row = 0;  // longest row (entries); selects the per-lane batch depth
+    int max_row = 0;  // longest row (entries)
+    // SpMV variant: bit 0 = 8 entries per lane per batch (else 4, only with
+    // 32 lanes per row), bit 1 = shared-memory staged (needs tiles)
+    int variant = 0;
 };
 
 struct AmgLevel {
@@ -213,6 +216,8 @@ struct mpet_ctx {
 
     // set by a kernel whose bounded wait gave up (read after each solve)
     int* dev_err = nullptr;
+    // set-up timings (ms) of the four SpMV variants on the system matrix
+    double spmv_variant_ms[4] = {0, 0, 0, 0};
 
     // timing
     cudaEvent_t ev0 = nullptr, ev1 = nullptr;

@@ -501,10 +501,8 @@ void build_tiles(mpet_ctx* c, Csr& A, const int64_t* rp) {
 
 template <typename T, int NV, class Epi>
 static void launch_spmv(mpet_ctx* c, const Csr& A, const T* va, const T* x, const Epi& epi) {
-    // 32 lanes per row take 8 entries per lane and batch when rows exceed 128
-    // entries, so that every row is one round trip; narrower rows take 4
-    const bool deep = A.lpr == 32 && A.max_row > 128;
-    if (A.ntiles > 0) {
+    const bool deep = A.lpr == 32 && (A.variant & 1);
+    if (A.ntiles > 0 && (A.variant & 2)) {
         switch (A.lpr) {
             case 32:
                 if (deep) launch_staged<T, NV, 32, 8, Epi>(c, A, va, x, epi);
@@ -554,32 +552,41 @@ const double* dinv_of<double>(const AmgLevel& L) { return L.dinv64; }
 template <>
 const float* dinv_of<float>(const AmgLevel& L) { return L.dinv32; }
 
-// Set-up autotuning: time the staged and the register SpMV on this matrix
-// (values, x and y in the given buffers) and keep the faster one.
+// Set-up autotuning: time every applicable SpMV variant on this matrix
+// (values, x and y in the given buffers; 2 warm-up + 5 timed launches each)
+// and keep the fastest.  Times (ms per launch) go to ms_out if given.
 template <typename T, int NV>
-static void autotune_matrix(mpet_ctx* c, Csr& A, const T* x, T* y) {
-    if (A.ntiles == 0 || vals<T>(A) == nullptr) return;
-    const int saved = A.ntiles;
-    auto time_it = [&](bool staged) {
-        A.ntiles = staged ? saved : 0;
-        launch_spmv<T, NV>(c, A, vals<T>(A), x, EpiStore<T, NV>{y});
+static void autotune_matrix(mpet_ctx* c, Csr& A, const T* x, T* y, double* ms_out = nullptr) {
+    if (vals<T>(A) == nullptr || A.nnz == 0) return;
+    const int64_t l0 = c->n_launch;
+    float best = 1e30f;
+    int best_v = 0;
+    for (int v = 0; v < 4; ++v) {
+        if ((v & 2) && A.ntiles == 0) continue;
+        if ((v & 1) && A.lpr != 32) continue;
+        A.variant = v;
+        for (int q = 0; q < 2; ++q) launch_spmv<T, NV>(c, A, vals<T>(A), x, EpiStore<T, NV>{y});
         MPET_CUDA(cudaEventRecord(c->ev0, c->stream));
-        for (int q = 0; q < 3; ++q) launch_spmv<T, NV>(c, A, vals<T>(A), x, EpiStore<T, NV>{y});
+        for (int q = 0; q < 5; ++q) launch_spmv<T, NV>(c, A, vals<T>(A), x, EpiStore<T, NV>{y});
         MPET_CUDA(cudaEventRecord(c->ev1, c->stream));
         MPET_CUDA(cudaEventSynchronize(c->ev1));
         float ms = 0.f;
         MPET_CUDA(cudaEventElapsedTime(&ms, c->ev0, c->ev1));
-        return ms;
-    };
-    const float ts = time_it(true), tr = time_it(false);
-    A.ntiles = ts < tr ? saved : 0;
-    c->n_launch -= 8;
+        ms /= 5.f;
+        if (ms_out) ms_out[v] = ms;
+        if (ms < best) {
+            best = ms;
+            best_v = v;
+        }
+    }
+    A.variant = best_v;
+    c->n_launch = l0;
 }
 
 void autotune_system(mpet_ctx* c) {
     MPET_CUDA(cudaMemsetAsync(c->kv, 0, sizeof(double) * c->N, c->stream));
-    if (c->A.v32) autotune_matrix<float, 1>(c, c->A, (const float*)c->kv, (float*)c->kd);
-    else autotune_matrix<double, 1>(c, c->A, (const double*)c->kv, (double*)c->kd);
+    if (c->A.v32) autotune_matrix<float, 1>(c, c->A, (const float*)c->kv, (float*)c->kd, c->spmv_variant_ms);
+    else autotune_matrix<double, 1>(c, c->A, (const double*)c->kv, (double*)c->kd, c->spmv_variant_ms);
 }
 
 template <typename T, int NV>
