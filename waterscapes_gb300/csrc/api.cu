@@ -61,6 +61,11 @@ int mpet_ctx_destroy(mpet_ctx* c) {
     if (c->stream) cudaStreamSynchronize(c->stream);
     destroy_minres_graph(c);
     if (c->cap_stream) cudaStreamDestroy(c->cap_stream);
+    for (int a = 0; a < MPET_MAX_NETWORKS; ++a) {
+        if (c->side[a]) cudaStreamDestroy(c->side[a]);
+        if (c->ev_join[a]) cudaEventDestroy(c->ev_join[a]);
+    }
+    if (c->ev_fork) cudaEventDestroy(c->ev_fork);
     c->pool.free_all();
     if (c->sc_host) cudaFreeHost(c->sc_host);
     if (c->ev0) cudaEventDestroy(c->ev0);

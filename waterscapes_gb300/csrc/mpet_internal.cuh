@@ -209,6 +209,12 @@ struct mpet_ctx {
     mpet::MinresScalars* sc = nullptr;
     mpet::MinresScalars* sc_host = nullptr;  // pinned
 
+    // side streams: the pressure-block V-cycles run concurrently with the
+    // displacement V-cycle (fork/join with events; parallel graph branches)
+    cudaStream_t side[MPET_MAX_NETWORKS] = {nullptr};
+    cudaEvent_t ev_fork = nullptr;
+    cudaEvent_t ev_join[MPET_MAX_NETWORKS] = {nullptr};
+
     // MINRES iterations replayed from a CUDA graph (3 iterations per launch)
     cudaStream_t cap_stream = nullptr;
     cudaGraphExec_t mr_graph = nullptr;

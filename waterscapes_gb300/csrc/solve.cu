@@ -552,55 +552,68 @@ const double* dinv_of<double>(const AmgLevel& L) { return L.dinv64; }
 template <>
 const float* dinv_of<float>(const AmgLevel& L) { return L.dinv32; }
 
-// Set-up autotuning: time every applicable SpMV variant on this matrix
-// (values, x and y in the given buffers; 2 warm-up + 5 timed launches each)
-// and keep the fastest.  Times (ms per launch) go to ms_out if given.
-template <typename T, int NV>
-static void autotune_matrix(mpet_ctx* c, Csr& A, const T* x, T* y, double* ms_out = nullptr) {
+// Set-up autotuning: time every applicable SpMV variant on this matrix with
+// the epilogue it runs in the solver (2 warm-up + 5 timed launches each) and
+// keep the fastest.  Times (ms per launch) go to ms_out if given.
+template <typename T, int NV, class Epi>
+static void autotune_matrix(mpet_ctx* c, Csr& A, const T* x, const Epi& epi, double* ms_out = nullptr) {
     if (vals<T>(A) == nullptr || A.nnz == 0) return;
     const int64_t l0 = c->n_launch;
     float best = 1e30f;
-    int best_v = 0;
-    for (int v = 0; v < 4; ++v) {
-        if ((v & 2) && A.ntiles == 0) continue;
-        if ((v & 1) && A.lpr != 32) continue;
-        A.variant = v;
-        for (int q = 0; q < 2; ++q) launch_spmv<T, NV>(c, A, vals<T>(A), x, EpiStore<T, NV>{y});
-        MPET_CUDA(cudaEventRecord(c->ev0, c->stream));
-        for (int q = 0; q < 5; ++q) launch_spmv<T, NV>(c, A, vals<T>(A), x, EpiStore<T, NV>{y});
-        MPET_CUDA(cudaEventRecord(c->ev1, c->stream));
-        MPET_CUDA(cudaEventSynchronize(c->ev1));
-        float ms = 0.f;
-        MPET_CUDA(cudaEventElapsedTime(&ms, c->ev0, c->ev1));
-        ms /= 5.f;
-        if (ms_out) ms_out[v] = ms;
-        if (ms < best) {
-            best = ms;
-            best_v = v;
+    int best_v = 0, best_lpr = A.lpr;
+    const int lpr0 = A.lpr;
+    for (int lpr : {lpr0, lpr0 / 2}) {
+        if (lpr < 4 && lpr != lpr0) continue;
+        A.lpr = lpr;
+        for (int v = 0; v < 4; ++v) {
+            if ((v & 2) && A.ntiles == 0) continue;
+            if ((v & 1) && lpr != 32) continue;
+            A.variant = v;
+            for (int q = 0; q < 2; ++q) launch_spmv<T, NV>(c, A, vals<T>(A), x, epi);
+            MPET_CUDA(cudaEventRecord(c->ev0, c->stream));
+            for (int q = 0; q < 5; ++q) launch_spmv<T, NV>(c, A, vals<T>(A), x, epi);
+            MPET_CUDA(cudaEventRecord(c->ev1, c->stream));
+            MPET_CUDA(cudaEventSynchronize(c->ev1));
+            float ms = 0.f;
+            MPET_CUDA(cudaEventElapsedTime(&ms, c->ev0, c->ev1));
+            ms /= 5.f;
+            if (ms_out && lpr == lpr0) ms_out[v] = ms;
+            if (ms < best) {
+                best = ms;
+                best_v = v;
+                best_lpr = lpr;
+            }
         }
     }
     A.variant = best_v;
+    A.lpr = best_lpr;
     c->n_launch = l0;
 }
 
 void autotune_system(mpet_ctx* c) {
     MPET_CUDA(cudaMemsetAsync(c->kv, 0, sizeof(double) * c->N, c->stream));
-    if (c->A.v32) autotune_matrix<float, 1>(c, c->A, (const float*)c->kv, (float*)c->kd, c->spmv_variant_ms);
-    else autotune_matrix<double, 1>(c, c->A, (const double*)c->kv, (double*)c->kd, c->spmv_variant_ms);
+    if (c->A.v32)
+        autotune_matrix<float, 1>(c, c->A, (const float*)c->kv, EpiStore<float, 1>{(float*)c->kd},
+                                  c->spmv_variant_ms);
+    else
+        autotune_matrix<double, 1>(c, c->A, (const double*)c->kv, EpiStore<double, 1>{(double*)c->kd},
+                                   c->spmv_variant_ms);
 }
 
 template <typename T, int NV>
 static void autotune_hier(mpet_ctx* c, AmgHier& h) {
     for (size_t k = 0; k < h.lev.size(); ++k) {
         AmgLevel& L = h.lev[k];
-        MPET_CUDA(cudaMemsetAsync(L.x, 0, sizeof(double) * L.A.n * NV, c->stream));
-        MPET_CUDA(cudaMemsetAsync(L.r, 0, sizeof(double) * L.A.n * NV, c->stream));
-        autotune_matrix<T, NV>(c, L.A, (const T*)L.x, (T*)L.t0);
+        const size_t bytes = sizeof(double) * L.A.n * NV;
+        for (void* p : {L.x, L.b, L.r, L.d, L.t0}) MPET_CUDA(cudaMemsetAsync(p, 0, bytes, c->stream));
+        const T* dinv = dinv_of<T>(L);
+        autotune_matrix<T, NV>(c, L.A, (const T*)L.x,
+                               EpiCheb<T, NV>{(const T*)L.b, (const T*)L.x, (T*)L.d, (T*)L.t0, dinv, T(0.5), T(0.5)});
         if (k + 1 < h.lev.size()) {
             AmgLevel& C = h.lev[k + 1];
             MPET_CUDA(cudaMemsetAsync(C.x, 0, sizeof(double) * C.A.n * NV, c->stream));
-            autotune_matrix<T, NV>(c, L.P, (const T*)C.x, (T*)L.t0);
-            autotune_matrix<T, NV>(c, L.R, (const T*)L.r, (T*)C.b);
+            autotune_matrix<T, NV>(c, L.P, (const T*)C.x, EpiAxpby<T, NV>{(T*)L.t0, (const T*)L.t0, T(1), T(1)});
+            autotune_matrix<T, NV>(c, L.R, (const T*)L.r, EpiStore<T, NV>{(T*)C.b});
         }
     }
 }
@@ -862,21 +875,32 @@ __global__ void k_unpack43(int64_t nodes, const T* __restrict__ b4, T* a) {
     a[3 * i + 2] = v[2];
 }
 
+// Block-diagonal preconditioner z = M^-1 r.  The J pressure V-cycles are
+// forked onto side streams and run concurrently with the displacement
+// V-cycle on the main stream (inside a CUDA graph capture they become
+// parallel branches); the main stream joins them at the end.
 template <typename T>
 static void precond(mpet_ctx* c, const T* r, T* z) {
+    cudaStream_t main = c->stream;
+    MPET_CUDA(cudaEventRecord(c->ev_fork, main));
+    for (int a = 0; a < c->J; ++a) {
+        MPET_CUDA(cudaStreamWaitEvent(c->side[a], c->ev_fork, 0));
+        c->stream = c->side[a];
+        const int64_t off = c->Nu + (int64_t)a * c->nv;
+        vcycle<T, 1>(c, c->amg_p[a], 0, r + off, z + off);
+        MPET_CUDA(cudaEventRecord(c->ev_join[a], c->side[a]));
+    }
+    c->stream = main;
     AmgHier& hu = c->amg_u;
     const int64_t nodes = c->nnodes;
     T* bin = (T*)hu.pack_in;
     T* xout = (T*)hu.pack_out;
-    k_pack34<T><<<grid_for(nodes, 256), 256, 0, c->stream>>>(nodes, r, bin);
+    k_pack34<T><<<grid_for(nodes, 256), 256, 0, main>>>(nodes, r, bin);
     vcycle<T, 4>(c, hu, 0, bin, xout);
-    k_unpack43<T><<<grid_for(nodes, 256), 256, 0, c->stream>>>(nodes, xout, z);
+    k_unpack43<T><<<grid_for(nodes, 256), 256, 0, main>>>(nodes, xout, z);
     MPET_CHECK_LAUNCH();
     c->n_launch += 2;
-    for (int a = 0; a < c->J; ++a) {
-        const int64_t off = c->Nu + (int64_t)a * c->nv;
-        vcycle<T, 1>(c, c->amg_p[a], 0, r + off, z + off);
-    }
+    for (int a = 0; a < c->J; ++a) MPET_CUDA(cudaStreamWaitEvent(main, c->ev_join[a], 0));
 }
 
 // ---- MINRES ----------------------------------------------------------------------------
@@ -1092,6 +1116,11 @@ void alloc_krylov(mpet_ctx* c) {
     c->partials = c->pool.alloc<double>(2 * NB_RED);
     c->dev_err = c->pool.alloc<int>(1);
     MPET_CUDA(cudaMemsetAsync(c->dev_err, 0, sizeof(int), c->stream));
+    if (!c->ev_fork) MPET_CUDA(cudaEventCreateWithFlags(&c->ev_fork, cudaEventDisableTiming));
+    for (int a = 0; a < c->J; ++a) {
+        if (!c->side[a]) MPET_CUDA(cudaStreamCreateWithFlags(&c->side[a], cudaStreamNonBlocking));
+        if (!c->ev_join[a]) MPET_CUDA(cudaEventCreateWithFlags(&c->ev_join[a], cudaEventDisableTiming));
+    }
     c->sc = c->pool.alloc<MinresScalars>(1);
     if (!c->sc_host) MPET_CUDA(cudaMallocHost(&c->sc_host, sizeof(MinresScalars)));
 }
