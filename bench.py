@@ -232,12 +232,14 @@ def profile_case(args):
     sol._assemble(dt)
     torch.cuda.synchronize()
     t0 = time.perf_counter()
+    torch.cuda.nvtx.range_push("step")
     try:
         sol.advance(dt)
     except _lib.MpetError as e:
         if e.code != -4:
             raise
     torch.cuda.synchronize()
+    torch.cuda.nvtx.range_pop()
     print(json.dumps({"profile_case": args.n, "networks": args.networks, "maxit": args.maxit, "N": sol.N,
                       "nnz": sol.nnz, "step_s": time.perf_counter() - t0}))
 
