@@ -257,18 +257,22 @@ __global__ void __launch_bounds__(256) k_spmv(int64_t n, const int64_t* __restri
 #pragma unroll
                 for (int u = 0; u < U; ++u) {
                     const int64_t e = b + sub + u * LPR;
-                    const bool ok = e < e1;
-                    const int64_t es = ok ? e : e1 - 1;
-                    cc[u] = __ldcs(ci + es);
-                    const T a = __ldcs(va + es);
-                    aa[u] = ok ? a : T(0);
+                    const int64_t es = e < e1 ? e : e1 - 1;
+                    cc[u] = 0;
+                    aa[u] = T(0);
+                    if (e < e1) {
+                        cc[u] = __ldcs(ci + es);
+                        aa[u] = __ldcs(va + es);
+                    }
                 }
 #pragma unroll
                 for (int u = 0; u < U; ++u) {
-                    T xv[NV];
-                    VecIO<T, NV>::load(x, cc[u], xv);
+                    if (b + sub + u * LPR < e1) {
+                        T xv[NV];
+                        VecIO<T, NV>::load(x, cc[u], xv);
 #pragma unroll
-                    for (int k = 0; k < NV; ++k) acc[k] += aa[u] * xv[k];
+                        for (int k = 0; k < NV; ++k) acc[k] += aa[u] * xv[k];
+                    }
                 }
             }
         }
@@ -411,17 +415,18 @@ __global__ void __launch_bounds__(256) k_spmv_staged(const int64_t* __restrict__
 #pragma unroll
                     for (int u = 0; u < U; ++u) {
                         const int q = q0 + sub + u * LPR;
-                        const bool ok = q < e;
-                        const int qs = ok ? q : e - 1;
+                        const int qs = q < e ? q : e - 1;
                         cc[u] = sc[qs];
-                        aa[u] = ok ? sv[qs] : T(0);
+                        aa[u] = q < e ? sv[qs] : T(0);
                     }
 #pragma unroll
                     for (int u = 0; u < U; ++u) {
-                        T xv[NV];
-                        VecIO<T, NV>::load(x, cc[u], xv);
+                        if (q0 + sub + u * LPR < e) {
+                            T xv[NV];
+                            VecIO<T, NV>::load(x, cc[u], xv);
 #pragma unroll
-                        for (int k = 0; k < NV; ++k) acc[k] += aa[u] * xv[k];
+                            for (int k = 0; k < NV; ++k) acc[k] += aa[u] * xv[k];
+                        }
                     }
                 }
             }
