@@ -131,6 +131,28 @@ int mpet_set_bc_values(mpet_ctx* ctx, int32_t field, const double* values);
  * terms (mpetsolver.py:233, 249). */
 int mpet_set_sources(mpet_ctx* ctx, const double* f_nodes, const double* g_vertices);
 
+/* Boundary facets (the nf facets of mpet_mesh_upload, same order): their P2
+ * nodes (nf x 6: the three vertices ascending, then the edges (1,2), (0,2),
+ * (0,1)) and area + outward unit normal (nf x 4), copied into device arrays
+ * so that facet data can be evaluated at those nodes. */
+int mpet_get_facet_data(mpet_ctx* ctx, int32_t* facet_nodes, double* area_normal);
+
+/* Facet data as Lagrange interpolants (device arrays, NULL = none):
+ *  MPET_FACET_TRACTION           s at the 6 facet P2 nodes, nf x 6 x 3 (used on
+ *                                momentum marker 1: (s, v) ds_m(1) in L0, mpetsolver.py:233)
+ *  MPET_FACET_FLUX               I_a at the 3 facet vertices, J x nf x 3 (marker 1:
+ *                                dt (I_a, q_a) ds(1) in L1, :249)
+ *  MPET_FACET_ROBIN_BETA         beta_a at t0 + theta dt, J x nf x 3 (marker 2, rhs(F2a), :252-254)
+ *  MPET_FACET_ROBIN_PRESSURE     p_robin_a at t0 + theta dt, J x nf x 3
+ *  MPET_FACET_ROBIN_BETA_MATRIX  beta_a for the Robin matrix lhs(F2a) added by
+ *                                mpet_assemble (A.axpy, :336-338), J x nf x 3 */
+#define MPET_FACET_TRACTION 0
+#define MPET_FACET_FLUX 1
+#define MPET_FACET_ROBIN_BETA 2
+#define MPET_FACET_ROBIN_PRESSURE 3
+#define MPET_FACET_ROBIN_BETA_MATRIX 4
+int mpet_set_facet_data(mpet_ctx* ctx, int32_t kind, const double* values);
+
 /* Right-hand side: assemble(L) + sum assemble(L1) + assemble(L0) and
  * bc.apply(b) (mpetsolver.py:356-376).  up_prev and b are device arrays
  * of length N. */

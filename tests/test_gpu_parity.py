@@ -221,6 +221,72 @@ def test_theta_half_step_matches_direct_solve():
     assert np.linalg.norm(x - x_ref) <= 1e-8 * np.linalg.norm(x_ref)
 
 
+def _facet_problem(theta):
+    """Neumann traction on x=1 (momentum), flux on x=0 (network 0), Robin on y=1 (network 1)."""
+    from waterscapes_gb300 import CompiledSubDomain, Constant, Expression
+    J = 2
+    problem, dt = make_problem(3, J)
+    near = lambda v, c: abs(v - c) < 1e-12
+    CompiledSubDomain(lambda x: near(x[:, 0], 1.0)).mark(problem.momentum_boundary_markers, 1)
+    CompiledSubDomain(lambda x: near(x[:, 0], 0.0)).mark(problem.continuity_boundary_markers[0], 1)
+    CompiledSubDomain(lambda x: near(x[:, 1], 1.0)).mark(problem.continuity_boundary_markers[1], 2)
+    s = lambda x, t, n: (1.0 + t) * n * x[:, :1]
+    I0 = lambda x, t: x[:, 1] + t
+    beta1 = lambda x, t: 2.0 + x[:, 2] + t
+    pr1 = lambda x, t: x[:, 0] * (1.0 + t)
+    problem.s = Expression(s)
+    problem.I = [Expression(I0), Constant(0.0)]
+    problem.beta = [Constant(0.0), Expression(beta1)]
+    problem.p_robin = [Constant(0.0), Expression(pr1)]
+    data = oracle_data(J)
+    data.update({"s": s, "I": [I0, None], "beta": [None, beta1], "p_robin": [None, pr1]})
+    return problem, dt, data
+
+
+def test_facet_terms_matrix_and_rhs():
+    theta = 0.5
+    problem, dt, data = _facet_problem(theta)
+    s = _solver(problem, dt, theta=theta, precision="fp64")
+    om = make_oracle(problem, theta)
+    t0 = 0.2
+    problem.time.assign(t0)
+    s._assemble(dt)
+    A = om.assemble_matrix(dt, t0, data)
+    dofs, _ = om.dirichlet_values(t0 + dt, data)
+    A = om.apply_bc_matrix(A, dofs)
+    v = s.matrix_values()
+    assert np.allclose(v, A.data, rtol=1e-12, atol=1e-13 * np.abs(A.data).max())
+    rng = np.random.default_rng(7)
+    up_prev = rng.standard_normal(om.dm.N)
+    t_theta, t1 = t0 + theta * dt, t0 + dt
+    b = om.rhs_L(up_prev, dt) + om.rhs_L1(up_prev, dt, t_theta, data) + om.rhs_L0(t1, data)
+    dofs, vals = om.dirichlet_values(t1, data)
+    b = om.apply_bc_vector(b, dofs, vals)
+    s._set_sources(t_theta, t1)
+    s._set_facet_sources(t_theta, t1)
+    s._set_bc_values(t1)
+    up = torch.tensor(up_prev, dtype=torch.float64, device=s.device)
+    bg = torch.empty(s.N, dtype=torch.float64, device=s.device)
+    s.ctx.call("mpet_rhs", dt, _lib()._ptr(up), _lib()._ptr(bg))
+    torch.cuda.synchronize()
+    assert np.allclose(_np(bg), b, rtol=1e-12, atol=1e-13 * np.abs(b).max())
+
+
+@pytest.mark.parametrize("precision", ["fp64", "mixed"])
+def test_facet_terms_step_matches_direct_solve(precision):
+    problem, dt, data = _facet_problem(1.0)
+    s = _solver(problem, dt, precision=precision, rtol=1e-11)
+    om = make_oracle(problem)
+    rng = np.random.default_rng(8)
+    up_prev = rng.standard_normal(om.dm.N) * 1e-2
+    x_ref = om.step(up_prev, 0.0, dt, data)
+    s.up_.assign(torch.tensor(up_prev))
+    problem.time.assign(0.0)
+    s.step(dt)
+    x = _np(s.up.vector())
+    assert np.linalg.norm(x - x_ref) <= 1e-8 * np.linalg.norm(x_ref)
+
+
 def test_assembly_and_solve_are_deterministic():
     J = 2
     problem, dt = make_problem(4, J)

@@ -149,6 +149,7 @@ int mpet_setup(mpet_ctx* c, const mpet_params* p) {
     build_topology(c);
     build_pattern(c);
     build_bc(c);
+    build_facets(c);
     c->A.v64 = c->pool.alloc<double>(c->nnz);
     if (c->prm.precision == MPET_PRECISION_MIXED) c->A.v32 = c->pool.alloc<float>(c->nnz);
     c->dinv = c->pool.alloc<double>(c->N);
@@ -210,6 +211,7 @@ int mpet_assemble(mpet_ctx* c, double dt, int32_t apply_bc) {
     require(c->setup_done, MPET_ERR_STATE, "mpet_setup must come first");
     require(dt > 0.0, MPET_ERR_INVALID, "dt must be positive");
     launch_assemble_matrix(c, dt, apply_bc != 0, c->A.v32 != nullptr);
+    launch_robin_matrix(c, dt);
     MPET_CUDA(cudaStreamSynchronize(c->stream));
     c->assembled = true;
     c->asm_dt = dt;
@@ -287,6 +289,35 @@ int mpet_set_sources(mpet_ctx* c, const double* f, const double* g) {
     require(c->setup_done, MPET_ERR_STATE, "mpet_setup must come first");
     c->f_nodes = f;
     c->g_vert = g;
+    API_END(c)
+}
+
+int mpet_get_facet_data(mpet_ctx* c, int32_t* fnodes, double* area_normal) {
+    API_BEGIN(c)
+    require(c->setup_done, MPET_ERR_STATE, "mpet_setup must come first");
+    if (c->nf > 0) {
+        if (fnodes)
+            MPET_CUDA(cudaMemcpyAsync(fnodes, c->fnodes, sizeof(int32_t) * 6 * c->nf, cudaMemcpyDeviceToDevice,
+                                      c->stream));
+        if (area_normal)
+            MPET_CUDA(cudaMemcpyAsync(area_normal, c->fgeo, sizeof(double) * 4 * c->nf, cudaMemcpyDeviceToDevice,
+                                      c->stream));
+        MPET_CUDA(cudaStreamSynchronize(c->stream));
+    }
+    API_END(c)
+}
+
+int mpet_set_facet_data(mpet_ctx* c, int32_t kind, const double* values) {
+    API_BEGIN(c)
+    require(c->setup_done, MPET_ERR_STATE, "mpet_setup must come first");
+    switch (kind) {
+        case MPET_FACET_TRACTION: c->f_traction = values; break;
+        case MPET_FACET_FLUX: c->f_flux = values; break;
+        case MPET_FACET_ROBIN_BETA: c->f_beta = values; break;
+        case MPET_FACET_ROBIN_PRESSURE: c->f_probin = values; break;
+        case MPET_FACET_ROBIN_BETA_MATRIX: c->f_beta_matrix = values; break;
+        default: fail(MPET_ERR_INVALID, "unknown facet data kind");
+    }
     API_END(c)
 }
 

@@ -547,6 +547,7 @@ void launch_rhs(mpet_ctx* c, double dt, const double* up_prev, double* b) {
     k_rhs_u<<<grid_for(c->nnodes, 128), 128, 0, c->stream>>>(A);
     k_rhs_p<<<grid_for(c->nv, 128), 128, 0, c->stream>>>(A, P);
     MPET_CHECK_LAUNCH();
+    launch_facet_rhs(c, dt, up_prev, b);
     launch_bc_vector(c, b);
 }
 

@@ -186,6 +186,19 @@ struct mpet_ctx {
     const double* f_nodes = nullptr;
     const double* g_vert = nullptr;
 
+    // boundary facets: P2 nodes (nf x 6), area + outward normal (nf x 4) and
+    // the boundary-node -> (facet * 8 + local) incidence
+    int32_t* fnodes = nullptr;
+    double* fgeo = nullptr;
+    int64_t* bn_ptr = nullptr;
+    int32_t* bn_list = nullptr;
+    // facet data (borrowed device pointers, MPET_FACET_*)
+    const double* f_traction = nullptr;
+    const double* f_flux = nullptr;
+    const double* f_beta = nullptr;
+    const double* f_probin = nullptr;
+    const double* f_beta_matrix = nullptr;
+
     mpet_params prm{};
     bool mesh_ready = false, setup_done = false, assembled = false, precond_ready = false;
     bool values_mixed = false;
@@ -241,6 +254,11 @@ constexpr int RED_THREADS = 256;
 void build_topology(mpet_ctx* c);
 void build_pattern(mpet_ctx* c);
 void build_bc(mpet_ctx* c);
+
+// facets.cu
+void build_facets(mpet_ctx* c);
+void launch_facet_rhs(mpet_ctx* c, double dt, const double* up_prev, double* b);
+void launch_robin_matrix(mpet_ctx* c, double dt);
 
 // assemble.cu
 void launch_assemble_matrix(mpet_ctx* c, double dt, bool apply_bc, bool write32);

@@ -155,16 +155,14 @@ class MPETSolver:
         return prm
 
     def _check_facet_data(self):
+        """Which boundary-facet terms are active (mpetsolver.py:231-254)."""
         p = self.problem
+        J = int(p.params["J"])
         mm = p.momentum_boundary_markers.array()
-        if (mm == NEUMANN_MARKER).any() and not is_zero(p.s):
-            raise NotImplementedError("traction boundary terms are not built on the GPU")
-        for a in range(int(p.params["J"])):
-            cm = p.continuity_boundary_markers[a].array()
-            if (cm == NEUMANN_MARKER).any() and not is_zero(p.I[a]):
-                raise NotImplementedError("flux boundary terms are not built on the GPU")
-            if (cm == ROBIN_MARKER).any():
-                raise NotImplementedError("Robin boundary terms are not built on the GPU")
+        self._traction_on = bool((mm == NEUMANN_MARKER).any() and not is_zero(p.s))
+        cm = [p.continuity_boundary_markers[a].array() for a in range(J)]
+        self._flux_on = any((cm[a] == NEUMANN_MARKER).any() and not is_zero(p.I[a]) for a in range(J))
+        self._robin_on = any((cm[a] == ROBIN_MARKER).any() for a in range(J))
 
     # --- boundary conditions -------------------------------------------------------
     def create_dirichlet_bcs(self):
@@ -240,8 +238,73 @@ class MPETSolver:
         self._f, self._g = f, g
         self._ctx.call("mpet_set_sources", _lib._ptr(f), _lib._ptr(g))
 
+    # --- boundary facets ------------------------------------------------------------
+    def _facet_geometry(self):
+        torch = _torch()
+        if getattr(self, "_fgeo", None) is None:
+            nf = self.problem.mesh.num_boundary_facets()
+            fn = torch.empty(max(nf, 1), 6, dtype=torch.int32, device=self.device)
+            geo = torch.empty(max(nf, 1), 4, dtype=torch.float64, device=self.device)
+            self._ctx.call("mpet_get_facet_data", _lib._ptr(fn), _lib._ptr(geo))
+            self._fnodes, self._fgeo = fn[:nf], geo[:nf]
+            self._fx = self._node_coordinates()[self._fnodes.long()]          # (nf, 6, 3)
+            p = self.problem
+            mk = lambda m: torch.as_tensor(m, device=self.device)
+            self._fmask_u = mk(p.momentum_boundary_markers.array() == NEUMANN_MARKER)
+            self._fmask_c = [(mk(p.continuity_boundary_markers[a].array() == NEUMANN_MARKER),
+                              mk(p.continuity_boundary_markers[a].array() == ROBIN_MARKER)) for a in range(self.J)]
+        return self._fx, self._fgeo
+
+    def _eval_traction(self, expr, x, t, n):
+        torch = _torch()
+        if isinstance(expr, Expression):
+            try:
+                v = expr.fn(x, t, n)
+            except TypeError:
+                v = expr.fn(x, t)
+            v = torch.as_tensor(v, dtype=torch.float64, device=self.device)
+            return v.expand(x.shape[0], 3) if v.numel() != 3 * x.shape[0] else v.reshape(x.shape[0], 3)
+        return self._eval(expr, x, t, True)
+
+    def _per_network_vertex_data(self, fields, t, mask_index):
+        torch = _torch()
+        fx, _ = self._facet_geometry()
+        xv = fx[:, :3, :].reshape(-1, 3)
+        nf = fx.shape[0]
+        out = torch.zeros(self.J, nf, 3, dtype=torch.float64, device=self.device)
+        for a in range(self.J):
+            mask = self._fmask_c[a][mask_index]
+            if fields[a] is None or not bool(mask.any()):
+                continue
+            v = self._eval(fields[a], xv, t, False).reshape(nf, 3)
+            out[a] = v * mask[:, None]
+        return out.contiguous()
+
+    def _set_facet_sources(self, t_theta, t1):
+        """Traction (at t1), flux and Robin data (at t0 + theta dt) at facet nodes."""
+        p = self.problem
+        if self._traction_on:
+            fx, geo = self._facet_geometry()
+            nf = fx.shape[0]
+            n = geo[:, 1:4].repeat_interleave(6, dim=0)
+            s = self._eval_traction(p.s, fx.reshape(-1, 3), t1, n).reshape(nf, 6, 3)
+            self._f_s = (s * self._fmask_u[:, None, None]).contiguous()
+            self._ctx.call("mpet_set_facet_data", 0, _lib._ptr(self._f_s))
+        if self._flux_on:
+            self._f_I = self._per_network_vertex_data(p.I, t_theta, 0)
+            self._ctx.call("mpet_set_facet_data", 1, _lib._ptr(self._f_I))
+        if self._robin_on:
+            self._f_b = self._per_network_vertex_data(p.beta, t_theta, 1)
+            self._f_pr = self._per_network_vertex_data(p.p_robin, t_theta, 1)
+            self._ctx.call("mpet_set_facet_data", 2, _lib._ptr(self._f_b))
+            self._ctx.call("mpet_set_facet_data", 3, _lib._ptr(self._f_pr))
+
     # --- assembly / solve -------------------------------------------------------------
     def _assemble(self, dt):
+        if self._robin_on:
+            # lhs(F2a) is assembled with the data at the current time (mpetsolver.py:336-338)
+            self._f_bm = self._per_network_vertex_data(self.problem.beta, float(self.problem.time), 1)
+            self._ctx.call("mpet_set_facet_data", 4, _lib._ptr(self._f_bm))
         self._ctx.call("mpet_assemble", float(dt), 1)
         self._assembled_dt = float(dt)
         if self._prec_dt != float(dt):
@@ -267,6 +330,7 @@ class MPETSolver:
         g_t = t_theta
         time.assign(t1)
         self._set_sources(g_t, t1)
+        self._set_facet_sources(g_t, t1)
         self._set_bc_values(t1)
         st = _lib.MpetStats()
         self._ctx.call("mpet_step", float(dt), _lib._ptr(self.up_.vector()), _lib._ptr(self.up.vector()),
