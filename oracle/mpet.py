@@ -170,7 +170,12 @@ class OracleMPET:
         if beta is not None:
             R = self._robin_matrix(dt, beta, t)
             if R is not None:
-                A = A + R  # PETSc MatAXPY with DIFFERENT_NONZERO_PATTERN
+                # PETSc MatAXPY(DIFFERENT_NONZERO_PATTERN): union pattern, stored
+                # zeros kept (a SciPy sum would drop them)
+                A, R = A.tocoo(), R.tocoo()
+                A = sp.coo_matrix((np.concatenate([A.data, R.data]),
+                                   (np.concatenate([A.row, R.row]), np.concatenate([A.col, R.col]))),
+                                  shape=A.shape).tocsr()
                 A.sort_indices()
         return A
 
