@@ -171,6 +171,20 @@ def run_steps(solver, torch, steps, warmup, dt):
     return ms, its, solver.up.vector().clone()
 
 
+def replica_rate(ms_local, steps):
+    """Whole-job steps/s of independent replicas: every rank ran ``steps`` steps in
+    ``ms_local`` ms; the job time is the slowest rank (max over ranks, gloo)."""
+    import torch
+    world = 1
+    ms = float(ms_local)
+    if torch.distributed.is_available() and torch.distributed.is_initialized():
+        world = torch.distributed.get_world_size()
+        t = torch.tensor([ms], dtype=torch.float64)
+        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+        ms = float(t.item())
+    return world * steps / (ms / 1e3), ms
+
+
 def spmv_tuning(solver):
     import ctypes
     ms = np.zeros(4)
@@ -323,12 +337,7 @@ def main():
     ms_mixed, its_mixed, x_mixed = run_steps(sol, torch, args.steps, args.warmup, dt)
     clocks = clk.stop()
     L1 = launches(sol)
-    ms_max = ms_mixed
-    if world > 1:
-        t = torch.tensor([ms_mixed], dtype=torch.float64)
-        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
-        ms_max = float(t.item())
-    value = world * args.steps / (ms_max / 1e3)
+    value, ms_max = replica_rate(ms_mixed, args.steps)
 
     # end to end through the public API with host buffers (pinned), copies timed
     problem.time.assign(0.0)
