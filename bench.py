@@ -46,15 +46,22 @@ def peaks():
     return 6800.0, "fallback"
 
 
-def workload(n, J):
-    import sys as _s
-    _s.path.insert(0, os.path.join(ROOT, "tests"))
-    from waterscapes_gb300 import CompiledSubDomain, Constant, Expression, MPETProblem, UnitCubeMesh, convert_to_E_nu
-    mesh = UnitCubeMesh(n)
+def workload(n, J, shape="cube"):
+    """Kuhn cube n^3 x 6 (the 16^3 A=2 and 64^3 A=4 cases), or the jittered
+    ellipsoidal shell (semi-axes 1, 0.8, 0.7, inner ratio 0.3, n radial layers,
+    144 n^3 cells) with log-normal per-cell K_a (log10 mean -3 + a, sigma 0.5,
+    seed 0)."""
+    from waterscapes_gb300 import (CompiledSubDomain, Constant, EllipsoidShellMesh, Expression, MPETProblem,
+                                   UnitCubeMesh, convert_to_E_nu)
+    mesh = UnitCubeMesh(n) if shape == "cube" else EllipsoidShellMesh(n, seed=0)
     if J == 4:
         S = np.full((4, 4), 1e-2)
         np.fill_diagonal(S, 0.0)
-        mat = dict(alpha=(0.25,) * 4, c=(1e-4,) * 4, K=(1e-4, 1e-3, 1e-2, 1e-1), S=tuple(map(tuple, S)))
+        K = (1e-4, 1e-3, 1e-2, 1e-1)
+        if shape != "cube":
+            rng = np.random.default_rng(0)
+            K = tuple(10.0 ** rng.normal(-3.0 + a, 0.5, size=mesh.num_cells()) for a in range(4))
+        mat = dict(alpha=(0.25,) * 4, c=(1e-4,) * 4, K=K, S=tuple(map(tuple, S)))
         dt = 0.01
     else:
         mat = dict(alpha=(0.5, 0.5), c=(1e-4, 1e-4), K=(1e-3, 1e-2), S=((0.0, 0.1), (0.1, 0.0)))
@@ -241,7 +248,7 @@ def profile_case(args):
     """Set-up, assembly and one time step capped at --maxit Krylov iterations."""
     import torch
     from waterscapes_gb300 import MPETSolver, _lib
-    problem, dt = workload(args.n, args.networks)
+    problem, dt = workload(args.n, args.networks, args.workload)
     sol = MPETSolver(problem, dict(dt=dt, T=1e9, precision="mixed", maxit=args.maxit, rtol=1e-10))
     sol._assemble(dt)
     torch.cuda.synchronize()
@@ -265,6 +272,8 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--n", type=int, default=64)
     ap.add_argument("--networks", type=int, default=4)
+    ap.add_argument("--workload", default="cube", choices=["cube", "ellipsoid"],
+                    help="cube: Kuhn n^3 cube; ellipsoid: jittered shell, n radial layers, per-cell K")
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--no-fp64", action="store_true")
     ap.add_argument("--no-cpu", action="store_true")
@@ -277,6 +286,9 @@ def main():
     n, J = args.n, args.networks
     N_full = 3 * (2 * n + 1) ** 3 + J * (n + 1) ** 3
     workload_name = "Kuhn cube %d^3 x 6 tets, A=%d networks, P2/P1 (N=%d)" % (n, J, N_full)
+    if args.workload == "ellipsoid":
+        workload_name = ("jittered ellipsoidal shell (1, 0.8, 0.7; inner 0.3), %d radial layers, %d tets, A=%d, "
+                         "log-normal per-cell K" % (n, 144 * n ** 3, J))
 
     rank = int(os.environ.get("RANK", "0"))
     world = int(os.environ.get("WORLD_SIZE", "1"))
@@ -309,7 +321,7 @@ def main():
     lib = _lib
     hbm, peak_kind = peaks()
 
-    problem, dt = workload(n, J)
+    problem, dt = workload(n, J, args.workload)
     base = dict(dt=dt, T=1e9, theta=1.0, rtol=1e-10, device=local_rank)
     t0 = time.perf_counter()
     sol = MPETSolver(problem, dict(base, precision="mixed"))

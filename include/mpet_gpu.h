@@ -131,6 +131,12 @@ int mpet_set_bc_values(mpet_ctx* ctx, int32_t field, const double* values);
  * terms (mpetsolver.py:233, 249). */
 int mpet_set_sources(mpet_ctx* ctx, const double* f_nodes, const double* g_vertices);
 
+/* Per-cell permeabilities (device array J x nc, cell order of the upload;
+ * NULL = the constants params.K).  K_a as a DG0 field in the form
+ * -dt (K_a grad pm_a, grad q_a) (mpetsolver.py:200) and in the preconditioner
+ * (:270); the matrix and preconditioner must be rebuilt afterwards. */
+int mpet_set_cell_permeability(mpet_ctx* ctx, const double* K_cells);
+
 /* Boundary facets (the nf facets of mpet_mesh_upload, same order): their P2
  * nodes (nf x 6: the three vertices ascending, then the edges (1,2), (0,2),
  * (0,1)) and area + outward unit normal (nf x 4), copied into device arrays

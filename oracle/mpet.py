@@ -92,7 +92,9 @@ class OracleMPET:
             self.mu, self.lmbda = convert_to_mu_lmbda(float(params["E"]), float(params["nu"]))
         self.alpha = np.asarray(params["alpha"], dtype=np.float64)
         self.c = np.asarray(params["c"], dtype=np.float64)
-        self.K = np.asarray(params["K"], dtype=np.float64)
+        # K_a: a constant or a per-cell (DG0) array; Kc[a] holds one value per cell
+        nc0 = np.asarray(cells).shape[0]
+        self.Kc = np.stack([np.broadcast_to(np.asarray(k, dtype=np.float64), (nc0,)) for k in params["K"]])
         self.S = np.asarray(params["S"], dtype=np.float64).reshape(self.J, self.J)
         self.bfacets = np.sort(np.asarray(bfacets, dtype=np.int64), axis=1)
         self.bfacet_cells = np.asarray(bfacet_cells, dtype=np.int64)
@@ -157,7 +159,7 @@ class OracleMPET:
                 ob = d * n2 + b_ * n1
                 blk = -dt * th * (Ssum[a] * (a == b_) - self.S[a, b_]) * self.M1
                 if a == b_:
-                    blk = blk - self.c[a] * self.M1 - dt * th * self.K[a] * self.L1
+                    blk = blk - self.c[a] * self.M1 - dt * th * self.Kc[a][:, None, None] * self.L1
                 Ae[:, o:o + n1, ob:ob + n1] += blk
         return Ae
 
@@ -220,7 +222,7 @@ class OracleMPET:
             o = d * n2 + a * n1
             val = -self.alpha[a] * np.einsum("ciw,ci->cw", Cf, u_loc)
             val -= self.c[a] * np.einsum("cvw,cw->cv", self.M1, p_loc[a])
-            val += dt * (1.0 - th) * self.K[a] * np.einsum("cvw,cw->cv", self.L1, p_loc[a])
+            val += dt * (1.0 - th) * self.Kc[a][:, None] * np.einsum("cvw,cw->cv", self.L1, p_loc[a])
             for b_ in range(J):
                 coef = self.S[a, b_]
                 if coef != 0.0:
@@ -385,7 +387,7 @@ class OracleMPET:
         blocks = [Lu]
         for a in range(self.J):
             sS = sum(self.S[a, b_] for b_ in range(self.J) if b_ != a)
-            loc = (self.c[a] + dt * self.theta * sS) * self.M1 + dt * self.theta * self.K[a] * self.L1
+            loc = (self.c[a] + dt * self.theta * sS) * self.M1 + dt * self.theta * self.Kc[a][:, None, None] * self.L1
             Pa = fem.assemble_csr(dm.cells, loc, dm.nv)
             Pa, _ = self.zero_rows_columns(Pa, [bcs[1 + a][0]])
             blocks.append(Pa)

@@ -287,6 +287,33 @@ def test_facet_terms_step_matches_direct_solve(precision):
     assert np.linalg.norm(x - x_ref) <= 1e-8 * np.linalg.norm(x_ref)
 
 
+@pytest.mark.parametrize("precision", ["fp64", "mixed"])
+def test_ellipsoid_per_cell_permeability_step(precision):
+    """Jittered ellipsoidal shell with log-normal per-cell K_a (the brain-like case)."""
+    from waterscapes_gb300 import CompiledSubDomain, Constant, EllipsoidShellMesh, Expression, MPETProblem
+    from helpers import p_bar_fn
+    mesh = EllipsoidShellMesh(3, seed=3)
+    J = 2
+    rng = np.random.default_rng(9)
+    K = [10.0 ** rng.normal(-3.0 + a, 0.5, size=mesh.num_cells()) for a in range(J)]
+    problem = MPETProblem(mesh, Constant(0.0), params=dict(J=J, E=2909.09, nu=0.4545, alpha=(0.25, 0.25),
+                                                           c=(1e-4, 1e-4), K=K, S=((0.0, 1e-2), (1e-2, 0.0))))
+    CompiledSubDomain.on_boundary().mark(problem.momentum_boundary_markers, 0)
+    for a in range(J):
+        CompiledSubDomain.on_boundary().mark(problem.continuity_boundary_markers[a], 0)
+    problem.p_bar = [Expression(p_bar_fn(a)) for a in range(J)]
+    dt = 0.01
+    s = _solver(problem, dt, precision=precision, rtol=1e-11)
+    om = make_oracle(problem)
+    up_prev = rng.standard_normal(om.dm.N) * 1e-2
+    x_ref = om.step(up_prev, 0.0, dt, oracle_data(J))
+    s.up_.assign(torch.tensor(up_prev))
+    problem.time.assign(0.0)
+    s.step(dt)
+    x = _np(s.up.vector())
+    assert np.linalg.norm(x - x_ref) <= 1e-8 * np.linalg.norm(x_ref)
+
+
 def test_assembly_and_solve_are_deterministic():
     J = 2
     problem, dt = make_problem(4, J)

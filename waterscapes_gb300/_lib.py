@@ -94,6 +94,7 @@ SIGNATURES = {
     "mpet_get_bc": [_P, _I32, _P, _P],
     "mpet_set_bc_values": [_P, _I32, _P],
     "mpet_set_sources": [_P, _P, _P],
+    "mpet_set_cell_permeability": [_P, _P],
     "mpet_get_facet_data": [_P, _P, _P],
     "mpet_set_facet_data": [_P, _I32, _P],
     "mpet_rhs": [_P, _D, _P, _P],

@@ -292,6 +292,15 @@ int mpet_set_sources(mpet_ctx* c, const double* f, const double* g) {
     API_END(c)
 }
 
+int mpet_set_cell_permeability(mpet_ctx* c, const double* K_cells) {
+    API_BEGIN(c)
+    require(c->setup_done, MPET_ERR_STATE, "mpet_setup must come first");
+    c->K_cells = K_cells;
+    c->assembled = false;
+    c->precond_ready = false;
+    API_END(c)
+}
+
 int mpet_get_facet_data(mpet_ctx* c, int32_t* fnodes, double* area_normal) {
     API_BEGIN(c)
     require(c->setup_done, MPET_ERR_STATE, "mpet_setup must come first");

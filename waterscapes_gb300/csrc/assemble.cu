@@ -35,6 +35,9 @@ struct MatCoef {
     double alpha[MPET_MAX_NETWORKS], c[MPET_MAX_NETWORKS], K[MPET_MAX_NETWORKS];
     double S[MPET_MAX_NETWORKS * MPET_MAX_NETWORKS];  // row-major, stride 8
     double Ssum[MPET_MAX_NETWORKS];                   // sum_b S_ab
+    const double* Kc;                                  // per-cell K (J x nc) or null
+    int64_t nc;
+    __device__ __forceinline__ double Kof(int a, int64_t cell) const { return Kc ? Kc[a * nc + cell] : K[a]; }
 };
 
 struct Geo {
@@ -194,7 +197,7 @@ __global__ void __launch_bounds__(256) k_assemble_matrix(AsmArgs A, MatCoef P) {
                         const int64_t base = rp[3 + a] + 3 * (int64_t)d2 + rk1[w];
                         for (int b = 0; b < J; ++b) {
                             double v = -P.dt_theta * ((a == b ? P.Ssum[a] : 0.0) - P.S[a * MPET_MAX_NETWORKS + b]) * M1;
-                            if (a == b) v += -P.c[a] * M1 - P.dt_theta * P.K[a] * L1;
+                            if (a == b) v += -P.c[a] * M1 - P.dt_theta * P.Kof(a, cell) * L1;
                             A.v64[base + (int64_t)b * d1] += v;
                         }
                     }
@@ -299,7 +302,7 @@ __global__ void __launch_bounds__(256) k_assemble_prec(PrecArgs A, MatCoef P) {
                     for (int a = 0; a < J; ++a) {
                         if (A.vert_bc[(int64_t)a * A.nv + i] || A.vert_bc[(int64_t)a * A.nv + vw]) continue;
                         double sS = P.Ssum[a] - P.S[a * MPET_MAX_NETWORKS + a];
-                        A.pp[a][pos] += (P.c[a] + P.dt_theta * sS) * M1 + P.dt_theta * P.K[a] * L1;
+                        A.pp[a][pos] += (P.c[a] + P.dt_theta * sS) * M1 + P.dt_theta * P.Kof(a, cell) * L1;
                     }
                 }
             }
@@ -379,7 +382,7 @@ __global__ void __launch_bounds__(128) k_rhs_p(RhsArgs A, MatCoef P) {
             acc[a] += A.dt * sg;
         }
         for (int a = 0; a < J; ++a) {
-            double t = -P.alpha[a] * cp - P.c[a] * mp[a] + omt * P.K[a] * lp[a];
+            double t = -P.alpha[a] * cp - P.c[a] * mp[a] + omt * P.Kof(a, cell) * lp[a];
             for (int b = 0; b < J; ++b) {
                 const double sab = P.S[a * MPET_MAX_NETWORKS + b];
                 if (sab != 0.0) t += omt * sab * (mp[a] - mp[b]);
@@ -464,6 +467,8 @@ static MatCoef make_coef(const mpet_ctx* c, double dt) {
         }
         P.Ssum[a] = s;
     }
+    P.Kc = c->K_cells;
+    P.nc = c->nc;
     return P;
 }
 

@@ -185,6 +185,7 @@ struct mpet_ctx {
     // sources (borrowed device pointers)
     const double* f_nodes = nullptr;
     const double* g_vert = nullptr;
+    const double* K_cells = nullptr;  // per-cell permeability (J x nc) or null
 
     // boundary facets: P2 nodes (nf x 6), area + outward normal (nf x 4) and
     // the boundary-node -> (facet * 8 + local) incidence

@@ -101,6 +101,14 @@ class MPETSolver:
                        bf.shape[0], _lib._ptr(bf), _lib._ptr(markers), self.J)
         self._prm = self._make_params()
         self._ctx.call("mpet_setup", ctypes.byref(self._prm))
+        # per-cell permeability fields (K_a given as an array with one value per cell)
+        Ks = [np.asarray(k, dtype=np.float64) for k in pp["K"]]
+        self._K_cells = None
+        if any(k.ndim > 0 for k in Ks):
+            nc = mesh.num_cells()
+            Kc = np.stack([np.broadcast_to(k, (nc,)) for k in Ks]).astype(np.float64)
+            self._K_cells = torch.as_tensor(np.ascontiguousarray(Kc), device=self.device)
+            self._ctx.call("mpet_set_cell_permeability", _lib._ptr(self._K_cells))
         N, nnz, nn, ne = (ctypes.c_int64(), ctypes.c_int64(), ctypes.c_int64(), ctypes.c_int64())
         self._ctx.call("mpet_get_sizes", ctypes.byref(N), ctypes.byref(nnz), ctypes.byref(nn), ctypes.byref(ne))
         self.N, self.nnz, self.nnodes, self.ne = N.value, nnz.value, nn.value, ne.value
@@ -137,7 +145,8 @@ class MPETSolver:
         for a in range(self.J):
             prm.alpha[a] = float(pp["alpha"][a])
             prm.c[a] = float(pp["c"][a])
-            prm.K[a] = float(pp["K"][a])
+            # a per-cell (DG0) permeability is uploaded separately; the scalar slot holds its mean
+            prm.K[a] = float(np.mean(np.asarray(pp["K"][a], dtype=np.float64)))
             for b in range(self.J):
                 prm.S[a * _lib.MAX_NETWORKS + b] = float(pp["S"][a][b])
         prm.theta = float(self.params["theta"])
