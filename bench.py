@@ -178,6 +178,26 @@ def run_steps(solver, torch, steps, warmup, dt):
     return ms, its, solver.up.vector().clone()
 
 
+def time_precond(solver, torch, lib, reps=10):
+    """One block-diagonal AMG preconditioner application (CUDA events)."""
+    mixed = solver.params["precision"] == "mixed"
+    dtype = torch.float32 if mixed else torch.float64
+    r = torch.randn(solver.N, dtype=dtype, device=solver.device)
+    z = torch.empty_like(r)
+    prec = 1 if mixed else 0
+    for _ in range(2):
+        solver.ctx.call("mpet_apply_preconditioner", prec, lib._ptr(r), lib._ptr(z))
+    torch.cuda.synchronize()
+    e0 = torch.cuda.Event(enable_timing=True)
+    e1 = torch.cuda.Event(enable_timing=True)
+    e0.record(solver._stream)
+    for _ in range(reps):
+        solver.ctx.call("mpet_apply_preconditioner", prec, lib._ptr(r), lib._ptr(z))
+    e1.record(solver._stream)
+    torch.cuda.synchronize()
+    return e0.elapsed_time(e1) / reps
+
+
 def replica_rate(ms_local, steps):
     """Whole-job steps/s of independent replicas: every rank ran ``steps`` steps in
     ``ms_local`` ms; the job time is the slowest rank (max over ranks, gloo)."""
@@ -340,6 +360,7 @@ def main():
     torch.cuda.synchronize()
     asm_ms = e0.elapsed_time(e1)
     spmv = time_spmv(sol, torch, lib)
+    precond_ms = time_precond(sol, torch, lib)
 
     clk = ClockSampler(local_rank)
     if world > 1:
@@ -425,6 +446,10 @@ def main():
         "setup_s": {"mesh_dofmap_pattern": t_setup, "assemble_plus_amg": t_asm_amg},
         "spmv": spmv,
         "spmv_tuning": spmv_tuning(sol),
+        "iteration_breakdown_ms": {
+            "per_iteration": ms_mixed / args.steps / max(1.0, float(np.mean(its_mixed))),
+            "spmv_fp32": (spmv.get("fp32") or spmv["fp64"])["ms"],
+            "preconditioner": precond_ms},
         "roofline": {"kernel": "k_spmv<float,1,32,EpiMinres> (FP32 CSR SpMV)" if "fp32" in spmv else "k_spmv<double>",
                      "bound": "hbm", "achieved": sp32["gbs"], "peak": hbm, "unit": "GB/s",
                      "frac": sp32["gbs"] / hbm, "peak_kind": peak_kind,

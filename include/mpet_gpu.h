@@ -182,6 +182,13 @@ int mpet_solve(mpet_ctx* ctx, const double* b, double* x, mpet_stats* stats);
  * (mpetsolver.py:424-462). */
 int mpet_step(mpet_ctx* ctx, double dt, const double* up_prev, double* up, mpet_stats* stats);
 
+/* z = M^-1 r with the block-diagonal AMG preconditioner (one V-cycle per
+ * block); r, z device arrays of length N in the hierarchy's precision (FP32
+ * for MPET_PRECISION_MIXED, FP64 otherwise).  The preconditioner the
+ * reference's iterative path hands to PETSc (solver.set_operators(A, P),
+ * mpetsolver.py:553). */
+int mpet_apply_preconditioner(mpet_ctx* ctx, int32_t precision, const void* r, void* z);
+
 /* FP64 residual r = b - A x of the assembled (Dirichlet-row) system and its
  * Jacobi-scaled norms: norms_host[0] = ||D^-1 r||_2, norms_host[1] =
  * ||D^-1 b||_2 (D = |diag A|).  The relative residual the reference's Krylov

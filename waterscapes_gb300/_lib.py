@@ -102,6 +102,7 @@ SIGNATURES = {
     "mpet_get_amg_info": [_P, _I32, ctypes.POINTER(_I32), _P, _P],
     "mpet_solve": [_P, _P, _P, ctypes.POINTER(MpetStats)],
     "mpet_step": [_P, _D, _P, _P, ctypes.POINTER(MpetStats)],
+    "mpet_apply_preconditioner": [_P, _I32, _P, _P],
     "mpet_residual": [_P, _P, _P, _P, _P],
     "mpet_residual_noalloc": [_P, _P, _P, _P, _P],
     "mpet_spmv": [_P, _I32, _P, _P],

@@ -468,6 +468,17 @@ int mpet_step(mpet_ctx* c, double dt, const double* up_prev, double* up, mpet_st
     API_END(c)
 }
 
+int mpet_apply_preconditioner(mpet_ctx* c, int32_t precision, const void* r, void* z) {
+    API_BEGIN(c)
+    require(c->precond_ready, MPET_ERR_STATE, "mpet_setup_preconditioner must come first");
+    require(r && z && r != z, MPET_ERR_INVALID, "r and z must be distinct device arrays");
+    const bool mixed = c->prm.precision == MPET_PRECISION_MIXED;
+    require(precision == (mixed ? MPET_PRECISION_MIXED : MPET_PRECISION_FP64), MPET_ERR_INVALID,
+            "the hierarchy holds FP32 values in mixed precision and FP64 values otherwise");
+    apply_preconditioner(c, precision, r, z);
+    API_END(c)
+}
+
 int mpet_residual(mpet_ctx* c, const double* b, const double* x, double* r, double* norms) {
     API_BEGIN(c)
     require(c->assembled, MPET_ERR_STATE, "mpet_assemble must come first");

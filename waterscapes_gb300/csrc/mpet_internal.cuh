@@ -277,6 +277,7 @@ int solve_system(mpet_ctx* c, const double* b, double* x, mpet_stats* st);
 void alloc_krylov(mpet_ctx* c);
 void autotune_system(mpet_ctx* c);
 void residual_norms(mpet_ctx* c, const double* b, const double* x, double* r, double* norms);
+void apply_preconditioner(mpet_ctx* c, int precision, const void* r, void* z);
 int choose_lpr(int64_t n, int64_t nnz);
 void build_tiles(mpet_ctx* c, Csr& A, const int64_t* rp_host);
 constexpr int SPMV_TILE = 2048;  // entries per staged tile

@@ -1088,6 +1088,11 @@ static int solve_impl(mpet_ctx* c, const double* b, double* x, mpet_stats* st) {
     return status;
 }
 
+void apply_preconditioner(mpet_ctx* c, int precision, const void* r, void* z) {
+    if (precision == MPET_PRECISION_MIXED) precond<float>(c, (const float*)r, (float*)z);
+    else precond<double>(c, (const double*)r, (double*)z);
+}
+
 void residual_norms(mpet_ctx* c, const double* b, const double* x, double* r, double* norms) {
     launch_spmv<double, 1>(c, c->A, c->A.v64, x, EpiResid64{r, b, c->dinv});
     k_outer_norms<<<1, 256, 0, c->stream>>>(c->sc, c->partials);
