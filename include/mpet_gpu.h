@@ -71,6 +71,11 @@ typedef struct mpet_params {
     int32_t check_every;               /* host convergence check period (iterations) */
     int32_t amg_p2_to_p1;              /* 1: displacement hierarchy starts with the P1-in-P2
                                           embedding (p-multigrid), then aggregation */
+    int32_t pad0;
+    double prec_u_weight;              /* w in the displacement block w (grad u, grad v) of the
+                                          preconditioner; the reference form uses mu
+                                          (mpetsolver.py:269), mu + lmbda balances the blocks;
+                                          <= 0 means mu */
 } mpet_params;
 
 typedef struct mpet_stats {

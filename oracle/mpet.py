@@ -373,15 +373,17 @@ class OracleMPET:
         return A, b
 
     # --- preconditioner blocks (mpetsolver.py:264-271) ---------------------------------
-    def preconditioner_blocks(self, dt):
-        """Scalar SPD blocks: mu (grad u, grad v) on P2 nodes and, per network,
+    def preconditioner_blocks(self, dt, u_weight=None):
+        """Scalar SPD blocks: w (grad u, grad v) on P2 nodes (w = mu in the
+        reference form, mpetsolver.py:269) and, per network,
         c_a M + dt theta K_a L + dt theta sum_{b != a} S_ab M on P1 vertices,
         with the Dirichlet DOFs eliminated symmetrically (unit diagonal)."""
         dm = self.dm
         nc = self.vol.shape[0]
         tr = np.einsum("cijkk->cij", self.Mg)
         cn = dm.cell_nodes
-        Lu = fem.assemble_csr(cn, self.mu * tr, dm.nnodes)
+        w = self.mu if u_weight is None else float(u_weight)
+        Lu = fem.assemble_csr(cn, w * tr, dm.nnodes)
         bcs = self.dirichlet_dofs()
         Lu, _ = self.zero_rows_columns(Lu, [bcs[0][0]])
         blocks = [Lu]

@@ -106,7 +106,7 @@ def test_minres_amg_reaches_lu_solution():
     for d, v in zip(dofs, vals):
         x0[d] = v
     r0 = bbc - Abc @ x0
-    blocks = om.preconditioner_blocks(dt)
+    blocks = om.preconditioner_blocks(dt, u_weight=om.mu + om.lmbda)
     P0 = krylov.p1_in_p2_embedding(om.dm, om.dirichlet_dofs()[0][0])
     hu = krylov.SAHierarchy(blocks[0], theta=0.1, cheb_degree=4, P0=P0)
     hp = [krylov.SAHierarchy(B, theta=0.1, cheb_degree=4) for B in blocks[1:]]

@@ -37,6 +37,7 @@ struct MatCoef {
     double Ssum[MPET_MAX_NETWORKS];                   // sum_b S_ab
     const double* Kc;                                  // per-cell K (J x nc) or null
     int64_t nc;
+    double prec_mu;                                    // weight of the displacement preconditioner block
     __device__ __forceinline__ double Kof(int a, int64_t cell) const { return Kc ? Kc[a * nc + cell] : K[a]; }
 };
 
@@ -292,7 +293,7 @@ __global__ void __launch_bounds__(256) k_assemble_prec(PrecArgs A, MatCoef P) {
                         for (int r = 0; r < 4; ++r) acc += gm[r][a] * gj[r][a];
                         tr += acc;
                     }
-                    A.lu[s2 + A.rank2[cell * 100 + m * 10 + j]] += P.mu * w20 * tr;
+                    A.lu[s2 + A.rank2[cell * 100 + m * 10 + j]] += P.prec_mu * w20 * tr;
                 } else {
                     const int w = t - 10;
                     const int32_t vw = A.cells[4 * cell + w];
@@ -469,6 +470,7 @@ static MatCoef make_coef(const mpet_ctx* c, double dt) {
     }
     P.Kc = c->K_cells;
     P.nc = c->nc;
+    P.prec_mu = c->prm.prec_u_weight > 0.0 ? c->prm.prec_u_weight : c->prm.mu;
     return P;
 }
 
