@@ -231,6 +231,35 @@ int mpet_get_spmv_tuning(mpet_ctx* ctx, double* ms4_host, int32_t* chosen);
 int mpet_get_timing(mpet_ctx* ctx, double* spmv_ms, int64_t* spmv_launches,
                     double* precond_ms, int64_t* kernel_launches);
 
+/* ---- discrete adjoint with respect to per-cell permeability ----------------
+ * The reference has no adjoint; these entry points differentiate the
+ * solve_direct time loop (mpetsolver.py:382-462) as this library discretises
+ * it, with respect to the per-cell K_a fields of mpet_set_cell_permeability.
+ * All vectors are device arrays of length N unless stated otherwise. */
+
+/* Final-pressure misfit 1/2 sum_a (p_a - p*_a)^T M (p_a - p*_a), M the P1
+ * mass matrix, of the state up against p_target (J x nv, network-major).
+ * Writes the value to *loss_host and, when dloss is not NULL, its gradient
+ * with respect to up (zero on the displacement rows). */
+int mpet_pressure_misfit(mpet_ctx* ctx, const double* up, const double* p_target, double* loss_host,
+                         double* dloss);
+
+/* out = B^T lam with its Dirichlet rows zeroed, B the old-state operator of
+ * the right-hand side (the rows -alpha_a (div u, q) - c_a (p_a, q)
+ * + dt (1-theta) [K_a (grad p_a, grad q) + sum_b S_ab (p_a - p_b, q)]): the
+ * seed of the adjoint step one step earlier.  MPET_ERR_INVALID for theta < 1
+ * with Robin terms set (their (1-theta) part is not differentiated). */
+int mpet_adjoint_rhs(mpet_ctx* ctx, double dt, const double* lam, double* out);
+
+/* One adjoint step: solve A^T lam = seed with lam zero on the Dirichlet DOFs
+ * (the seed's Dirichlet rows are ignored; A^T = A needs a symmetric S, else
+ * MPET_ERR_INVALID), then, when grad_K (J x nc) is not NULL, add
+ *   dt |e| grad lam_a . grad(theta p_a + (1 - theta) p_prev_a)
+ * per cell e, the step's contribution to dL/dK_a(e) (dA/dK_a(e) =
+ * -dt theta L_e and dB/dK_a(e) = dt (1-theta) L_e on the p_a block). */
+int mpet_adjoint_step(mpet_ctx* ctx, double dt, const double* seed, const double* up_prev, const double* up,
+                      double* lam, double* grad_K, mpet_stats* stats);
+
 #ifdef __cplusplus
 }
 #endif

@@ -111,6 +111,9 @@ SIGNATURES = {
     "mpet_apply_symmetric": [_P, _P, _P],
     "mpet_get_spmv_tuning": [_P, _P, ctypes.POINTER(_I32)],
     "mpet_get_timing": [_P, ctypes.POINTER(_D), ctypes.POINTER(_I64), ctypes.POINTER(_D), ctypes.POINTER(_I64)],
+    "mpet_pressure_misfit": [_P, _P, _P, ctypes.POINTER(_D), _P],
+    "mpet_adjoint_rhs": [_P, _D, _P, _P],
+    "mpet_adjoint_step": [_P, _D, _P, _P, _P, _P, _P, ctypes.POINTER(MpetStats)],
 }
 
 

@@ -526,4 +526,54 @@ int mpet_get_timing(mpet_ctx* c, double* spmv_ms, int64_t* spmv_launches, double
     API_END(c)
 }
 
+int mpet_pressure_misfit(mpet_ctx* c, const double* up, const double* p_target, double* loss, double* dloss) {
+    API_BEGIN(c)
+    require(c->setup_done, MPET_ERR_STATE, "mpet_setup must come first");
+    require(up && p_target && loss, MPET_ERR_INVALID, "NULL argument");
+    if (!c->adj_loss) c->adj_loss = c->pool.alloc<double>(1);
+    launch_misfit(c, up, p_target, dloss, c->adj_loss);
+    MPET_CUDA(cudaMemcpyAsync(loss, c->adj_loss, sizeof(double), cudaMemcpyDeviceToHost, c->stream));
+    MPET_CUDA(cudaStreamSynchronize(c->stream));
+    API_END(c)
+}
+
+static void require_adjoint_ok(mpet_ctx* c) {
+    require(!(c->prm.theta < 1.0 && (c->f_beta || c->f_beta_matrix)), MPET_ERR_INVALID,
+            "Robin terms are not differentiated for theta < 1");
+}
+
+int mpet_adjoint_rhs(mpet_ctx* c, double dt, const double* lam, double* out) {
+    API_BEGIN(c)
+    require(c->setup_done, MPET_ERR_STATE, "mpet_setup must come first");
+    require(lam && out && lam != out, MPET_ERR_INVALID, "lam and out must be distinct device arrays");
+    require_adjoint_ok(c);
+    launch_adjoint_rhs(c, dt, lam, out);
+    API_END(c)
+}
+
+int mpet_adjoint_step(mpet_ctx* c, double dt, const double* seed, const double* up_prev, const double* up,
+                      double* lam, double* grad_K, mpet_stats* st) {
+    API_BEGIN(c)
+    require(c->assembled, MPET_ERR_STATE, "mpet_assemble must come first");
+    require(c->precond_ready, MPET_ERR_STATE, "mpet_setup_preconditioner must come first");
+    require(seed && lam && lam != seed, MPET_ERR_INVALID, "seed and lam must be distinct device arrays");
+    require(!grad_K || (up_prev && up), MPET_ERR_INVALID, "the gradient needs up_prev and up");
+    require_adjoint_ok(c);
+    for (int a = 0; a < c->J; ++a)
+        for (int b = 0; b < a; ++b)
+            require(c->prm.S[a * MPET_MAX_NETWORKS + b] == c->prm.S[b * MPET_MAX_NETWORKS + a], MPET_ERR_INVALID,
+                    "A^T differs from A for a non-symmetric S");
+    if (!c->adj_b) c->adj_b = c->pool.alloc<double>(c->N);
+    MPET_CUDA(cudaMemcpyAsync(c->adj_b, seed, sizeof(double) * c->N, cudaMemcpyDeviceToDevice, c->stream));
+    launch_zero_bc_rows(c, c->adj_b);
+    MPET_CUDA(cudaMemsetAsync(lam, 0, sizeof(double) * c->N, c->stream));
+    int s = solve_system(c, c->adj_b, lam, st, true);
+    if (s != MPET_OK) {
+        c->err = s == MPET_ERR_MAXIT ? "Krylov iteration limit reached" : "Krylov breakdown";
+        return s;
+    }
+    if (grad_K) launch_adjoint_grad(c, dt, lam, up_prev, up, grad_K);
+    API_END(c)
+}
+
 }  // extern "C"

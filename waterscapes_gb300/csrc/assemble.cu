@@ -340,6 +340,9 @@ struct RhsArgs {
 // Pressure rows of L = rhs(F) (mpetsolver.py:196-201, 261) plus dt g_a q_a
 // (L1, :249):  -alpha_a (div u^n, q) - c_a (p_a^n, q)
 //   + dt (1-theta) [K_a (grad p_a^n, grad q) + sum_b S_ab (p_a^n - p_b^n, q)] + dt (g_a, q).
+// ADJ: the pressure rows of B^T lam for the old-state operator B of those
+// rows (no displacement or source term, S transposed).
+template <bool ADJ>
 __global__ void __launch_bounds__(128) k_rhs_p(RhsArgs A, MatCoef P) {
     const int64_t v = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
     if (v >= A.nv) return;
@@ -355,7 +358,7 @@ __global__ void __launch_bounds__(128) k_rhs_p(RhsArgs A, MatCoef P) {
         load_geo(A.geo, cell, G);
         const double w20 = G.vol * (1.0 / 20.0);
         double cp = 0.0;
-        for (int j = 0; j < 10; ++j) {
+        for (int j = 0; j < (ADJ ? 0 : 10); ++j) {
             double g[3], s[3];
             p2_grad_at(G, j, m, g, s);
             const int64_t nj = A.cell_nodes[10 * cell + j];
@@ -376,7 +379,7 @@ __global__ void __launch_bounds__(128) k_rhs_p(RhsArgs A, MatCoef P) {
             for (int w = 0; w < 4; ++w) {
                 sm += M1[w] * pa[vw[w]];
                 sl += L1[w] * pa[vw[w]];
-                if (A.g) sg += M1[w] * A.g[(int64_t)a * A.nv + vw[w]];
+                if (!ADJ && A.g) sg += M1[w] * A.g[(int64_t)a * A.nv + vw[w]];
             }
             mp[a] = sm;
             lp[a] = sl;
@@ -386,7 +389,8 @@ __global__ void __launch_bounds__(128) k_rhs_p(RhsArgs A, MatCoef P) {
             double t = -P.alpha[a] * cp - P.c[a] * mp[a] + omt * P.Kof(a, cell) * lp[a];
             for (int b = 0; b < J; ++b) {
                 const double sab = P.S[a * MPET_MAX_NETWORKS + b];
-                if (sab != 0.0) t += omt * sab * (mp[a] - mp[b]);
+                if (ADJ) t += omt * (sab * mp[a] - P.S[b * MPET_MAX_NETWORKS + a] * mp[b]);
+                else if (sab != 0.0) t += omt * sab * (mp[a] - mp[b]);
             }
             acc[a] += t;
         }
@@ -552,7 +556,7 @@ void launch_rhs(mpet_ctx* c, double dt, const double* up_prev, double* b) {
     A.theta = c->prm.theta;
     MatCoef P = make_coef(c, dt);
     k_rhs_u<<<grid_for(c->nnodes, 128), 128, 0, c->stream>>>(A);
-    k_rhs_p<<<grid_for(c->nv, 128), 128, 0, c->stream>>>(A, P);
+    k_rhs_p<false><<<grid_for(c->nv, 128), 128, 0, c->stream>>>(A, P);
     MPET_CHECK_LAUNCH();
     launch_facet_rhs(c, dt, up_prev, b);
     launch_bc_vector(c, b);
@@ -569,6 +573,165 @@ void launch_set_bc_in_x(mpet_ctx* c, double* x) { launch_bc_vector(c, x); }
 
 void launch_zero_bc_columns(mpet_ctx* c, double* b, const double* xbc) {
     k_zero_bc_columns<<<152 * 16, 256, 0, c->stream>>>(c->N, c->A.rp, c->A.ci, c->A.v64, c->dof_bc, b, xbc);
+    MPET_CHECK_LAUNCH();
+}
+
+// --- discrete adjoint -----------------------------------------------------------
+//
+// The time loop solves A_FF y_n = (B x_{n-1} + f_n)_F - A_FD g_n with B the
+// old-state operator of rhs(F).  Its adjoint needs B^T lam (below: the
+// displacement rows from the coupling block, the pressure rows from
+// k_rhs_p<true>), the sensitivity of A and B to a per-cell K_a (the element
+// stiffness on the p_a block, scaled by -dt theta and dt (1-theta)) and the
+// final-pressure misfit with its gradient.
+
+// Displacement rows of B^T lam: B holds -alpha_a (div u, q_a), so row (i, k)
+// is -sum_a alpha_a sum_{cells} int lam_a d_k phi_i.
+__global__ void __launch_bounds__(128) k_adj_rhs_u(RhsArgs A, MatCoef P) {
+    const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    if (i >= A.nnodes) return;
+    double acc[3] = {0.0, 0.0, 0.0};
+    for (int64_t it = A.inc_ptr[i]; it < A.inc_ptr[i + 1]; ++it) {
+        const int32_t packed = A.inc[it];
+        const int64_t cell = packed >> 4;
+        const int m = packed & 15;
+        Geo G;
+        load_geo(A.geo, cell, G);
+        const double w20 = G.vol * (1.0 / 20.0);
+        for (int w = 0; w < 4; ++w) {
+            const int64_t vw = A.cells[4 * cell + w];
+            double lam = 0.0;
+            for (int a = 0; a < P.J; ++a) lam += P.alpha[a] * A.up[A.Nu + (int64_t)a * A.nv + vw];
+            double g[3], sg[3];
+            p2_grad_at(G, m, w, g, sg);
+#pragma unroll
+            for (int k = 0; k < 3; ++k) acc[k] -= w20 * (g[k] + sg[k]) * lam;
+        }
+    }
+    A.b[3 * i] = acc[0];
+    A.b[3 * i + 1] = acc[1];
+    A.b[3 * i + 2] = acc[2];
+}
+
+__global__ void k_zero_rows(const int32_t* __restrict__ dofs, int64_t n, double* b) {
+    const int64_t k = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    if (k < n) b[dofs[k]] = 0.0;
+}
+
+// grad_K[a][cell] += dt |cell| grad lam_a . grad(theta p_a + (1 - theta) p_prev_a)
+__global__ void __launch_bounds__(128) k_adj_grad(int64_t nc, int64_t nv, int64_t Nu, int J,
+                                                  const double* __restrict__ geo, const int32_t* __restrict__ cells,
+                                                  const double* __restrict__ lam, const double* __restrict__ up_prev,
+                                                  const double* __restrict__ up, double dt, double theta,
+                                                  double* grad) {
+    const int64_t cell = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    if (cell >= nc) return;
+    Geo G;
+    load_geo(geo, cell, G);
+    int64_t v[4];
+#pragma unroll
+    for (int w = 0; w < 4; ++w) v[w] = cells[4 * cell + w];
+    for (int a = 0; a < J; ++a) {
+        const int64_t o = Nu + (int64_t)a * nv;
+        double gl[3] = {0.0, 0.0, 0.0}, gq[3] = {0.0, 0.0, 0.0};
+#pragma unroll
+        for (int w = 0; w < 4; ++w) {
+            const double l = lam[o + v[w]];
+            const double q = theta * up[o + v[w]] + (1.0 - theta) * up_prev[o + v[w]];
+#pragma unroll
+            for (int k = 0; k < 3; ++k) {
+                gl[k] += l * G.b[w][k];
+                gq[k] += q * G.b[w][k];
+            }
+        }
+        grad[(int64_t)a * nc + cell] += dt * G.vol * (gl[0] * gq[0] + gl[1] * gq[1] + gl[2] * gq[2]);
+    }
+}
+
+// Misfit 1/2 sum_a d_a^T M d_a, d_a = p_a - p*_a: per vertex (M d_a)_v by a
+// gather over the vertex's cells, written to dloss (when given) and folded
+// into fixed-grid block partials.
+__global__ void __launch_bounds__(256) k_misfit(int64_t nv, int64_t Nu, int J, const int64_t* __restrict__ inc_ptr,
+                                                const int32_t* __restrict__ inc, const double* __restrict__ geo,
+                                                const int32_t* __restrict__ cells, const double* __restrict__ up,
+                                                const double* __restrict__ target, double* dloss, double* partials) {
+    __shared__ double sh[8];
+    double part = 0.0;
+    for (int64_t v = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; v < nv; v += (int64_t)gridDim.x * blockDim.x) {
+        for (int a = 0; a < J; ++a) {
+            const double* p = up + Nu + (int64_t)a * nv;
+            const double* t = target + (int64_t)a * nv;
+            double md = 0.0;
+            for (int64_t it = inc_ptr[v]; it < inc_ptr[v + 1]; ++it) {
+                const int32_t packed = inc[it];
+                const int64_t cell = packed >> 4;
+                const int m = packed & 15;
+                const double w20 = geo[16 * cell + 12] * (1.0 / 20.0);
+#pragma unroll
+                for (int w = 0; w < 4; ++w) {
+                    const int64_t vw = cells[4 * cell + w];
+                    md += w20 * (m == w ? 2.0 : 1.0) * (p[vw] - t[vw]);
+                }
+            }
+            if (dloss) dloss[Nu + (int64_t)a * nv + v] = md;
+            part += 0.5 * (p[v] - t[v]) * md;
+        }
+    }
+    part = block_sum256(part, sh);
+    if (threadIdx.x == 0) partials[blockIdx.x] = part;
+}
+
+__global__ void k_finish_sum(const double* __restrict__ partials, double* out) {
+    __shared__ double sh[8];
+    const double s = sum_partials(partials, sh);
+    if (threadIdx.x == 0) *out = s;
+}
+
+static RhsArgs rhs_args(mpet_ctx* c, double dt, const double* state, double* b) {
+    RhsArgs A{};
+    A.nnodes = c->nnodes;
+    A.nv = c->nv;
+    A.Nu = c->Nu;
+    A.inc_ptr = c->inc_ptr;
+    A.inc = c->inc;
+    A.geo = c->geo;
+    A.cell_nodes = c->cell_nodes;
+    A.cells = c->cells;
+    A.up = state;
+    A.b = b;
+    A.dt = dt;
+    A.theta = c->prm.theta;
+    return A;
+}
+
+void launch_adjoint_rhs(mpet_ctx* c, double dt, const double* lam, double* out) {
+    RhsArgs A = rhs_args(c, dt, lam, out);
+    MatCoef P = make_coef(c, dt);
+    k_adj_rhs_u<<<grid_for(c->nnodes, 128), 128, 0, c->stream>>>(A, P);
+    k_rhs_p<true><<<grid_for(c->nv, 128), 128, 0, c->stream>>>(A, P);
+    MPET_CHECK_LAUNCH();
+    launch_zero_bc_rows(c, out);
+}
+
+void launch_zero_bc_rows(mpet_ctx* c, double* b) {
+    if (c->nbc_dofs > 0) {
+        k_zero_rows<<<grid_for(c->nbc_dofs, 256), 256, 0, c->stream>>>(c->bc_dofs, c->nbc_dofs, b);
+        MPET_CHECK_LAUNCH();
+    }
+}
+
+void launch_adjoint_grad(mpet_ctx* c, double dt, const double* lam, const double* up_prev, const double* up,
+                         double* grad) {
+    k_adj_grad<<<grid_for(c->nc, 128), 128, 0, c->stream>>>(c->nc, c->nv, c->Nu, c->J, c->geo, c->cells, lam,
+                                                             up_prev, up, dt, c->prm.theta, grad);
+    MPET_CHECK_LAUNCH();
+}
+
+void launch_misfit(mpet_ctx* c, const double* up, const double* target, double* dloss, double* loss_dev) {
+    if (dloss) MPET_CUDA(cudaMemsetAsync(dloss, 0, sizeof(double) * c->Nu, c->stream));
+    k_misfit<<<NB_RED, 256, 0, c->stream>>>(c->nv, c->Nu, c->J, c->inc_ptr, c->inc, c->geo, c->cells, up, target,
+                                             dloss, c->partials);
+    k_finish_sum<<<1, 256, 0, c->stream>>>(c->partials, loss_dev);
     MPET_CHECK_LAUNCH();
 }
 

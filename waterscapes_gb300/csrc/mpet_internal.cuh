@@ -219,6 +219,8 @@ struct mpet_ctx {
     double* ox = nullptr;         // outer FP64 vectors
     double* orr = nullptr;
     double* ob = nullptr;
+    double* adj_b = nullptr;      // adjoint right-hand side (Dirichlet rows zeroed)
+    double* adj_loss = nullptr;   // misfit value (1 double)
     double* partials = nullptr;   // reduction partials
     mpet::MinresScalars* sc = nullptr;
     mpet::MinresScalars* sc_host = nullptr;  // pinned
@@ -251,6 +253,36 @@ namespace mpet {
 constexpr int NB_RED = 1216;  // fixed block count of every reduction kernel (152 SMs x 8)
 constexpr int RED_THREADS = 256;
 
+#ifdef __CUDACC__
+__device__ __forceinline__ double warp_sum(double v) {
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+    return v;
+}
+
+// Sum over a 256-thread block in a fixed order; result valid in thread 0.
+__device__ __forceinline__ double block_sum256(double v, double* sh) {
+    v = warp_sum(v);
+    const int w = threadIdx.x >> 5, l = threadIdx.x & 31;
+    if (l == 0) sh[w] = v;
+    __syncthreads();
+    double t = 0.0;
+    if (threadIdx.x < 32) {
+        t = threadIdx.x < (blockDim.x >> 5) ? sh[threadIdx.x] : 0.0;
+        t = warp_sum(t);
+    }
+    __syncthreads();
+    return t;
+}
+
+// Sum of NB_RED partials by one 256-thread block (fixed order).
+__device__ __forceinline__ double sum_partials(const double* p, double* sh) {
+    double v = 0.0;
+    for (int i = threadIdx.x; i < NB_RED; i += 256) v += p[i];
+    return block_sum256(v, sh);
+}
+#endif
+
 // setup.cu
 void build_topology(mpet_ctx* c);
 void build_pattern(mpet_ctx* c);
@@ -268,12 +300,19 @@ void launch_rhs(mpet_ctx* c, double dt, const double* up_prev, double* b);
 void launch_bc_vector(mpet_ctx* c, double* b);
 void launch_set_bc_in_x(mpet_ctx* c, double* x);
 void launch_zero_bc_columns(mpet_ctx* c, double* b, const double* xbc);
+void launch_zero_bc_rows(mpet_ctx* c, double* b);
+void launch_adjoint_rhs(mpet_ctx* c, double dt, const double* lam, double* out);
+void launch_adjoint_grad(mpet_ctx* c, double dt, const double* lam, const double* up_prev, const double* up,
+                         double* grad);
+void launch_misfit(mpet_ctx* c, const double* up, const double* target, double* dloss, double* loss_dev);
 
 // solve.cu
 template <typename T>
 void spmv(mpet_ctx* c, const Csr& A, int nvec, const T* x, T* y);
 void upload_amg(mpet_ctx* c, AmgHier& h, const HostAmg& ha, int nvec, bool fp32);
-int solve_system(mpet_ctx* c, const double* b, double* x, mpet_stats* st);
+// homogeneous: the Dirichlet entries of x are zero (adjoint solves) instead
+// of the values set by mpet_set_bc_values
+int solve_system(mpet_ctx* c, const double* b, double* x, mpet_stats* st, bool homogeneous = false);
 void alloc_krylov(mpet_ctx* c);
 void autotune_system(mpet_ctx* c);
 void residual_norms(mpet_ctx* c, const double* b, const double* x, double* r, double* norms);

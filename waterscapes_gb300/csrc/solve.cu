@@ -41,36 +41,6 @@ int choose_lpr(int64_t n, int64_t nnz) {
     return 1;
 }
 
-// ---- reductions ------------------------------------------------------------------
-
-__device__ __forceinline__ double warp_sum(double v) {
-#pragma unroll
-    for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
-    return v;
-}
-
-// Sum over a 256-thread block in a fixed order; result valid in thread 0.
-__device__ __forceinline__ double block_sum256(double v, double* sh) {
-    v = warp_sum(v);
-    const int w = threadIdx.x >> 5, l = threadIdx.x & 31;
-    if (l == 0) sh[w] = v;
-    __syncthreads();
-    double t = 0.0;
-    if (threadIdx.x < 32) {
-        t = threadIdx.x < (blockDim.x >> 5) ? sh[threadIdx.x] : 0.0;
-        t = warp_sum(t);
-    }
-    __syncthreads();
-    return t;
-}
-
-// Sum of NB_RED partials by one 256-thread block (fixed order).
-__device__ __forceinline__ double sum_partials(const double* p, double* sh) {
-    double v = 0.0;
-    for (int i = threadIdx.x; i < NB_RED; i += 256) v += p[i];
-    return block_sum256(v, sh);
-}
-
 // ---- vector access -------------------------------------------------------------
 // Multi-vector data is node-interleaved (NV values per row).  With NV = 4
 // every row's values are one 16-byte-aligned group, accessed by vector
@@ -1011,10 +981,11 @@ static int minres_run(mpet_ctx* c, double target, int max_iters, int* iters_done
 }
 
 template <typename T>
-static int solve_impl(mpet_ctx* c, const double* b, double* x, mpet_stats* st) {
+static int solve_impl(mpet_ctx* c, const double* b, double* x, mpet_stats* st, bool homogeneous) {
     const int64_t n = c->N;
     const int G = grid_for(n, 256);
-    launch_set_bc_in_x(c, x);
+    if (homogeneous) launch_zero_bc_rows(c, x);
+    else launch_set_bc_in_x(c, x);
     double eta0 = -1.0;
     int iters = 0, outer = 0;
     int status = MPET_OK;
@@ -1109,9 +1080,9 @@ void residual_norms(mpet_ctx* c, const double* b, const double* x, double* r, do
     norms[1] = sqrt(c->sc_host->nb2);
 }
 
-int solve_system(mpet_ctx* c, const double* b, double* x, mpet_stats* st) {
-    if (c->prm.precision == MPET_PRECISION_MIXED) return solve_impl<float>(c, b, x, st);
-    return solve_impl<double>(c, b, x, st);
+int solve_system(mpet_ctx* c, const double* b, double* x, mpet_stats* st, bool homogeneous) {
+    if (c->prm.precision == MPET_PRECISION_MIXED) return solve_impl<float>(c, b, x, st, homogeneous);
+    return solve_impl<double>(c, b, x, st, homogeneous);
 }
 
 void alloc_krylov(mpet_ctx* c) {

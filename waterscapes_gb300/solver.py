@@ -386,6 +386,18 @@ class MPETSolver:
             yield self.up, float(time)
             self.up_.assign(self.up)
 
+    def set_cell_permeability(self, K):
+        """Replace the permeability by per-cell (DG0) fields K (J x num_cells);
+        the matrix and the preconditioner are rebuilt at the next step."""
+        torch = _torch()
+        K = torch.as_tensor(K, dtype=torch.float64, device=self.device).contiguous()
+        if K.shape != (self.J, self.problem.mesh.num_cells()):
+            raise ValueError("K must have shape (J, num_cells) = (%d, %d)" % (self.J, self.problem.mesh.num_cells()))
+        self._K_cells = K
+        self._ctx.call("mpet_set_cell_permeability", _lib._ptr(K))
+        self._assembled_dt = None
+        self._prec_dt = None
+
     # --- engine access used by tests and the bench --------------------------------------
     @property
     def ctx(self):
