@@ -214,11 +214,11 @@ def replica_rate(ms_local, steps):
 
 def spmv_tuning(solver):
     import ctypes
-    ms = np.zeros(4)
+    ms = np.zeros(6)
     ch = ctypes.c_int32()
     solver.ctx.call("mpet_get_spmv_tuning", ms.ctypes.data_as(ctypes.c_void_p), ctypes.byref(ch))
-    names = ["register/4", "register/8", "staged/4", "staged/8"]
-    return {"ms": {names[v]: round(float(ms[v]), 4) for v in range(4) if ms[v] > 0}, "chosen": names[ch.value]}
+    names = ["register/4", "register/8", "staged/4", "staged/8", "sell32/4", "sell32/8"]
+    return {"ms": {names[v]: round(float(ms[v]), 4) for v in range(6) if ms[v] > 0}, "chosen": names[ch.value]}
 
 
 def launches(solver):
@@ -285,6 +285,84 @@ def profile_case(args):
                       "nnz": sol.nnz, "step_s": time.perf_counter() - t0}))
 
 
+def adjoint_check(args):
+    """Gradient of the final-pressure misfit w.r.t. per-cell K by the discrete
+    adjoint: A=2 on the Kuhn n^3 cube (default 32^3), 20 steps of dt = 0.025,
+    a checkpoint every 5 steps; the target is the final pressure field of a
+    seeded log-normal "true" K (log10 K_a ~ N(log10 K_a0, 0.5)), the gradient is
+    taken at a second seeded field.  Checked against central differences
+    (h = 1e-6 along K-relative Gaussian directions) and against the FP64-path
+    adjoint.  Prints one JSON line."""
+    import torch
+    from waterscapes_gb300 import MPETSolver
+    from waterscapes_gb300.adjoint import MisfitAdjoint
+    n, J, nsteps, dt, every = args.n, 2, 20, 0.025, 5
+    problem, _ = workload(n, J, "cube")
+    nc = problem.mesh.num_cells()
+    K0 = np.asarray(problem.params["K"], dtype=np.float64)
+    rng = np.random.default_rng(0)
+    K_true = np.stack([K0[a] * 10.0 ** rng.normal(0.0, 0.5, nc) for a in range(J)])
+    K_eval = np.stack([K0[a] * 10.0 ** rng.normal(0.0, 0.5, nc) for a in range(J)])
+    dev = torch.device("cuda", 0)
+    f64 = dict(dtype=torch.float64, device=dev)
+    solvers = {p: MPETSolver(problem, dict(dt=dt, T=1e9, theta=1.0, rtol=1e-12, precision=p))
+               for p in ("mixed", "fp64")}
+    # central differences resolve a 1e-6 relative change of K only if the
+    # solves are much tighter than that times the solution's sensitivity
+    solvers["fd"] = MPETSolver(problem, dict(dt=dt, T=1e9, theta=1.0, rtol=1e-14, precision="mixed"))
+    zero = torch.zeros(solvers["mixed"].N, **f64)
+
+    def driver(p, target):
+        problem.time.assign(0.0)
+        return MisfitAdjoint(solvers[p], target, nsteps, checkpoint_every=every, t0=0.0, up0=zero)
+
+    # target: final pressures of the "true" field
+    d = driver("mixed", torch.zeros(J, solvers["mixed"].nv, **f64))
+    d.forward(torch.as_tensor(K_true, **f64))
+    s = solvers["mixed"]
+    target = d.x_final[s.Nu:].reshape(J, s.nv).clone()
+    out = {"metric": "discrete-adjoint gradient of the final-pressure misfit w.r.t. per-cell K",
+           "config": {"workload": "Kuhn cube %d^3 x 6 tets (%d cells), A=2, %d steps of dt=%g, checkpoint every %d"
+                      % (n, nc, nsteps, dt, every), "N": s.N, "rtol": 1e-12}}
+    for p in ("mixed", "fp64"):
+        d = driver(p, target)
+        Kt = torch.as_tensor(K_eval, **f64)
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        loss = d.forward(Kt)
+        torch.cuda.synchronize()
+        t1 = time.perf_counter()
+        g = d.backward()
+        torch.cuda.synchronize()
+        t2 = time.perf_counter()
+        out[p] = {"loss": loss, "forward_s": t1 - t0, "backward_s": t2 - t1,
+                  "forward_iterations": sum(d.stats["forward_iterations"][:nsteps]),
+                  "adjoint_iterations": sum(d.stats["adjoint_iterations"])}
+        if p == "mixed":
+            g_mixed, d_mixed = g.clone(), d
+        else:
+            g64 = g
+    out["rel_diff_mixed_vs_fp64_gradient"] = float(torch.linalg.norm(g_mixed - g64) / torch.linalg.norm(g64))
+    # central differences on the mixed path (FP64 refinement to rtol 1e-14)
+    rng = np.random.default_rng(2)
+    h = 1e-6
+    errs = []
+    d_fd = driver("fd", target)
+    t0 = time.perf_counter()
+    for _ in range(args.fd_dirs):
+        dK = torch.as_tensor(K_eval * rng.standard_normal(K_eval.shape), **f64)
+        Ke = torch.as_tensor(K_eval, **f64)
+        lp = d_fd.forward(Ke + h * dK)
+        lm = d_fd.forward(Ke - h * dK)
+        fd = (lp - lm) / (2.0 * h)
+        ad = float(torch.sum(g_mixed * dK))
+        errs.append(abs(fd - ad) / abs(ad))
+    out["central_differences"] = {"directions": args.fd_dirs, "h": h, "max_rel_err": max(errs),
+                                  "median_rel_err": statistics.median(errs), "seconds": time.perf_counter() - t0,
+                                  "path": "mixed precision, FP64 refinement to rtol 1e-14"}
+    print(json.dumps(out))
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -300,9 +378,14 @@ def main():
     ap.add_argument("--profile", action="store_true",
                     help="one step with at most --maxit MINRES iterations (small launch count for ncu)")
     ap.add_argument("--maxit", type=int, default=12)
+    ap.add_argument("--adjoint", action="store_true",
+                    help="discrete-adjoint gradient check (A=2 on the --n cube, 20 steps) instead of the bench")
+    ap.add_argument("--fd-dirs", type=int, default=64)
     args = ap.parse_args()
     if args.profile:
         return profile_case(args)
+    if args.adjoint:
+        return adjoint_check(args)
     n, J = args.n, args.networks
     N_full = 3 * (2 * n + 1) ** 3 + J * (n + 1) ** 3
     workload_name = "Kuhn cube %d^3 x 6 tets, A=%d networks, P2/P1 (N=%d)" % (n, J, N_full)

@@ -142,6 +142,15 @@ int mpet_set_sources(mpet_ctx* ctx, const double* f_nodes, const double* g_verti
  * (:270); the matrix and preconditioner must be rebuilt afterwards. */
 int mpet_set_cell_permeability(mpet_ctx* ctx, const double* K_cells);
 
+/* Per-cell storage coefficients c_a (device array J x nc) and transfer
+ * coefficients S_ab (J x J x nc, S_cells[(a J + b) nc + cell], symmetric in
+ * a, b per cell for MINRES); either may be NULL (= the constants of
+ * params).  The DG0 forms of c_a and S_ab in mpetsolver.py:200-201 and the
+ * preconditioner (:270); used for batches of independent instances with
+ * their own parameters in one mesh.  The matrix and preconditioner must be
+ * rebuilt afterwards. */
+int mpet_set_cell_coefficients(mpet_ctx* ctx, const double* c_cells, const double* S_cells);
+
 /* Boundary facets (the nf facets of mpet_mesh_upload, same order): their P2
  * nodes (nf x 6: the three vertices ascending, then the edges (1,2), (0,2),
  * (0,1)) and area + outward unit normal (nf x 4), copied into device arrays
@@ -221,11 +230,19 @@ int mpet_spmv(mpet_ctx* ctx, int32_t precision, const void* x, void* y);
  * replaced by mpet_assemble).  b, if not NULL, is lifted with x_bc. */
 int mpet_apply_symmetric(mpet_ctx* ctx, double* b, const double* x_bc);
 
-/* Set-up autotuning of the system-matrix SpMV: ms per launch of the four
- * variants (register / shared-memory staged x 4 / 8 entries per lane per
- * batch; 0 where not applicable) and the chosen variant (0..3).  No
- * reference counterpart (engine introspection for benchmarks). */
-int mpet_get_spmv_tuning(mpet_ctx* ctx, double* ms4_host, int32_t* chosen);
+/* Set-up autotuning of the system-matrix SpMV: ms per launch of the six
+ * variants, indexed by the variant bits (bit 0: 8 instead of 4 entries per
+ * lane per batch; bit 1: CSR rows staged in shared memory by bulk copies;
+ * bit 2: SELL-32 copy, one thread per row), 0 where not applicable, and the
+ * chosen variant (0..5).  No reference counterpart (engine introspection for
+ * benchmarks). */
+int mpet_get_spmv_tuning(mpet_ctx* ctx, double* ms6_host, int32_t* chosen);
+
+/* Override the autotuned system-matrix SpMV variant (bits as above);
+ * MPET_ERR_INVALID if the variant cannot run on this matrix.  Every variant
+ * computes the same product (summation order differs).  No reference
+ * counterpart (tuning and test hook). */
+int mpet_set_spmv_variant(mpet_ctx* ctx, int32_t variant);
 
 /* Per-kernel timing of the last solve (CUDA events): total ms and launches. */
 int mpet_get_timing(mpet_ctx* ctx, double* spmv_ms, int64_t* spmv_launches,

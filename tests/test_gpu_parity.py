@@ -172,15 +172,25 @@ def test_spmv_parity(precision):
     y_ref = A @ x
     y64 = torch.empty(s.N, dtype=torch.float64, device=s.device)
     xg = torch.tensor(x, device=s.device)
-    s.ctx.call("mpet_spmv", 0, _lib()._ptr(xg), _lib()._ptr(y64))
-    torch.cuda.synchronize()
-    assert np.allclose(_np(y64), y_ref, rtol=1e-12, atol=1e-12 * np.abs(y_ref).max())
-    if precision == "mixed":
-        y32 = torch.empty(s.N, dtype=torch.float32, device=s.device)
-        x32 = torch.tensor(x, dtype=torch.float32, device=s.device)
-        s.ctx.call("mpet_spmv", 1, _lib()._ptr(x32), _lib()._ptr(y32))
+    # every SpMV variant that can run on this matrix (CSR register / staged,
+    # SELL-32), not only the autotuned one
+    ran = []
+    for v in range(6):
+        try:
+            s.ctx.call("mpet_set_spmv_variant", v)
+        except _lib().MpetError:
+            continue
+        ran.append(v)
+        s.ctx.call("mpet_spmv", 0, _lib()._ptr(xg), _lib()._ptr(y64))
         torch.cuda.synchronize()
-        assert np.linalg.norm(_np(y32) - y_ref) <= 1e-5 * np.linalg.norm(y_ref)
+        assert np.allclose(_np(y64), y_ref, rtol=1e-12, atol=1e-12 * np.abs(y_ref).max())
+        if precision == "mixed":
+            y32 = torch.empty(s.N, dtype=torch.float32, device=s.device)
+            x32 = torch.tensor(x, dtype=torch.float32, device=s.device)
+            s.ctx.call("mpet_spmv", 1, _lib()._ptr(x32), _lib()._ptr(y32))
+            torch.cuda.synchronize()
+            assert np.linalg.norm(_np(y32) - y_ref) <= 1e-5 * np.linalg.norm(y_ref)
+    assert 4 in ran and 5 in ran
 
 
 def test_residual_matches_oracle():

@@ -156,6 +156,9 @@ int mpet_setup(mpet_ctx* c, const mpet_params* p) {
     c->Lu.v64 = c->pool.alloc<double>(c->Lu.nnz);
     for (int a = 0; a < c->J; ++a) c->Pp[a].v64 = c->pool.alloc<double>(c->Pp[a].nnz);
     alloc_krylov(c);
+    MPET_CUDA(cudaMemsetAsync(c->A.v64, 0, sizeof(double) * c->nnz, c->stream));
+    if (c->A.v32) MPET_CUDA(cudaMemsetAsync(c->A.v32, 0, sizeof(float) * c->nnz, c->stream));
+    build_sell(c, c->A, c->A.v32 != nullptr);
     autotune_system(c);
     MPET_CUDA(cudaStreamSynchronize(c->stream));
     c->setup_done = true;
@@ -212,6 +215,7 @@ int mpet_assemble(mpet_ctx* c, double dt, int32_t apply_bc) {
     require(dt > 0.0, MPET_ERR_INVALID, "dt must be positive");
     launch_assemble_matrix(c, dt, apply_bc != 0, c->A.v32 != nullptr);
     launch_robin_matrix(c, dt);
+    fill_sell(c, c->A);
     MPET_CUDA(cudaStreamSynchronize(c->stream));
     c->assembled = true;
     c->asm_dt = dt;
@@ -296,6 +300,16 @@ int mpet_set_cell_permeability(mpet_ctx* c, const double* K_cells) {
     API_BEGIN(c)
     require(c->setup_done, MPET_ERR_STATE, "mpet_setup must come first");
     c->K_cells = K_cells;
+    c->assembled = false;
+    c->precond_ready = false;
+    API_END(c)
+}
+
+int mpet_set_cell_coefficients(mpet_ctx* c, const double* c_cells, const double* S_cells) {
+    API_BEGIN(c)
+    require(c->setup_done, MPET_ERR_STATE, "mpet_setup must come first");
+    c->c_cells = c_cells;
+    c->S_cells = S_cells;
     c->assembled = false;
     c->precond_ready = false;
     API_END(c)
@@ -504,16 +518,26 @@ int mpet_apply_symmetric(mpet_ctx* c, double* b, const double* xbc) {
     require(c->assembled, MPET_ERR_STATE, "mpet_assemble must come first");
     launch_zero_bc_columns(c, b, xbc);
     convert_values_to_f32(c);
+    fill_sell(c, c->A);
     MPET_CUDA(cudaStreamSynchronize(c->stream));
     API_END(c)
 }
 
-int mpet_get_spmv_tuning(mpet_ctx* c, double* ms4, int32_t* chosen) {
+int mpet_get_spmv_tuning(mpet_ctx* c, double* ms6, int32_t* chosen) {
     API_BEGIN(c)
     require(c->setup_done, MPET_ERR_STATE, "mpet_setup must come first");
-    if (ms4)
-        for (int v = 0; v < 4; ++v) ms4[v] = c->spmv_variant_ms[v];
+    if (ms6)
+        for (int v = 0; v < 6; ++v) ms6[v] = c->spmv_variant_ms[v];
     if (chosen) *chosen = c->A.variant;
+    API_END(c)
+}
+
+int mpet_set_spmv_variant(mpet_ctx* c, int32_t variant) {
+    API_BEGIN(c)
+    require(c->setup_done, MPET_ERR_STATE, "mpet_setup must come first");
+    require(spmv_variant_available(c->A, variant), MPET_ERR_INVALID, "SpMV variant not available for this matrix");
+    destroy_minres_graph(c);
+    c->A.variant = variant;
     API_END(c)
 }
 

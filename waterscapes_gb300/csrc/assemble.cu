@@ -36,9 +36,21 @@ struct MatCoef {
     double S[MPET_MAX_NETWORKS * MPET_MAX_NETWORKS];  // row-major, stride 8
     double Ssum[MPET_MAX_NETWORKS];                   // sum_b S_ab
     const double* Kc;                                  // per-cell K (J x nc) or null
+    const double* cc;                                  // per-cell c (J x nc) or null
+    const double* Sc;                                  // per-cell S (J x J x nc) or null
     int64_t nc;
     double prec_mu;                                    // weight of the displacement preconditioner block
     __device__ __forceinline__ double Kof(int a, int64_t cell) const { return Kc ? Kc[a * nc + cell] : K[a]; }
+    __device__ __forceinline__ double cof(int a, int64_t cell) const { return cc ? cc[a * nc + cell] : c[a]; }
+    __device__ __forceinline__ double Sof(int a, int b, int64_t cell) const {
+        return Sc ? Sc[((int64_t)a * J + b) * nc + cell] : S[a * MPET_MAX_NETWORKS + b];
+    }
+    __device__ __forceinline__ double Ssumof(int a, int64_t cell) const {
+        if (!Sc) return Ssum[a];
+        double s = 0.0;
+        for (int b = 0; b < J; ++b) s += Sof(a, b, cell);
+        return s;
+    }
 };
 
 struct Geo {
@@ -197,8 +209,8 @@ __global__ void __launch_bounds__(256) k_assemble_matrix(AsmArgs A, MatCoef P) {
                     for (int a = 0; a < J; ++a) {
                         const int64_t base = rp[3 + a] + 3 * (int64_t)d2 + rk1[w];
                         for (int b = 0; b < J; ++b) {
-                            double v = -P.dt_theta * ((a == b ? P.Ssum[a] : 0.0) - P.S[a * MPET_MAX_NETWORKS + b]) * M1;
-                            if (a == b) v += -P.c[a] * M1 - P.dt_theta * P.Kof(a, cell) * L1;
+                            double v = -P.dt_theta * ((a == b ? P.Ssumof(a, cell) : 0.0) - P.Sof(a, b, cell)) * M1;
+                            if (a == b) v += -P.cof(a, cell) * M1 - P.dt_theta * P.Kof(a, cell) * L1;
                             A.v64[base + (int64_t)b * d1] += v;
                         }
                     }
@@ -302,8 +314,8 @@ __global__ void __launch_bounds__(256) k_assemble_prec(PrecArgs A, MatCoef P) {
                     const int64_t pos = s1 + A.rank1[cell * 40 + m * 4 + w];
                     for (int a = 0; a < J; ++a) {
                         if (A.vert_bc[(int64_t)a * A.nv + i] || A.vert_bc[(int64_t)a * A.nv + vw]) continue;
-                        double sS = P.Ssum[a] - P.S[a * MPET_MAX_NETWORKS + a];
-                        A.pp[a][pos] += (P.c[a] + P.dt_theta * sS) * M1 + P.dt_theta * P.Kof(a, cell) * L1;
+                        double sS = P.Ssumof(a, cell) - P.Sof(a, a, cell);
+                        A.pp[a][pos] += (P.cof(a, cell) + P.dt_theta * sS) * M1 + P.dt_theta * P.Kof(a, cell) * L1;
                     }
                 }
             }
@@ -386,10 +398,10 @@ __global__ void __launch_bounds__(128) k_rhs_p(RhsArgs A, MatCoef P) {
             acc[a] += A.dt * sg;
         }
         for (int a = 0; a < J; ++a) {
-            double t = -P.alpha[a] * cp - P.c[a] * mp[a] + omt * P.Kof(a, cell) * lp[a];
+            double t = -P.alpha[a] * cp - P.cof(a, cell) * mp[a] + omt * P.Kof(a, cell) * lp[a];
             for (int b = 0; b < J; ++b) {
-                const double sab = P.S[a * MPET_MAX_NETWORKS + b];
-                if (ADJ) t += omt * (sab * mp[a] - P.S[b * MPET_MAX_NETWORKS + a] * mp[b]);
+                const double sab = P.Sof(a, b, cell);
+                if (ADJ) t += omt * (sab * mp[a] - P.Sof(b, a, cell) * mp[b]);
                 else if (sab != 0.0) t += omt * sab * (mp[a] - mp[b]);
             }
             acc[a] += t;
@@ -473,6 +485,8 @@ static MatCoef make_coef(const mpet_ctx* c, double dt) {
         P.Ssum[a] = s;
     }
     P.Kc = c->K_cells;
+    P.cc = c->c_cells;
+    P.Sc = c->S_cells;
     P.nc = c->nc;
     P.prec_mu = c->prm.prec_u_weight > 0.0 ? c->prm.prec_u_weight : c->prm.mu;
     return P;

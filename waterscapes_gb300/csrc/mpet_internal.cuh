@@ -75,8 +75,17 @@ struct Csr {
     int ntiles = 0;
     int max_row = 0;  // longest row (entries)
     // SpMV variant: bit 0 = 8 entries per lane per batch (else 4, only with
-    // 32 lanes per row), bit 1 = shared-memory staged (needs tiles)
+    // 32 lanes per row, or with the SELL copy), bit 1 = shared-memory staged
+    // (needs tiles), bit 2 = SELL-32 copy (needs s_off)
     int variant = 0;
+    // SELL-32 copy: slices of 32 rows, column-major within a slice, padded
+    // to the slice's longest row with (row, 0) entries; s_off[s] is the first
+    // entry of slice s (nslices + 1 offsets)
+    int64_t nslices = 0;
+    int64_t* s_off = nullptr;
+    int32_t* s_ci = nullptr;
+    float* s_v32 = nullptr;
+    double* s_v64 = nullptr;
 };
 
 struct AmgLevel {
@@ -186,6 +195,8 @@ struct mpet_ctx {
     const double* f_nodes = nullptr;
     const double* g_vert = nullptr;
     const double* K_cells = nullptr;  // per-cell permeability (J x nc) or null
+    const double* c_cells = nullptr;  // per-cell storage coefficient (J x nc) or null
+    const double* S_cells = nullptr;  // per-cell transfer coefficients (J x J x nc) or null
 
     // boundary facets: P2 nodes (nf x 6), area + outward normal (nf x 4) and
     // the boundary-node -> (facet * 8 + local) incidence
@@ -238,8 +249,8 @@ struct mpet_ctx {
 
     // set by a kernel whose bounded wait gave up (read after each solve)
     int* dev_err = nullptr;
-    // set-up timings (ms) of the four SpMV variants on the system matrix
-    double spmv_variant_ms[4] = {0, 0, 0, 0};
+    // set-up timings (ms) of the six SpMV variants on the system matrix
+    double spmv_variant_ms[6] = {0, 0, 0, 0, 0, 0};
 
     // timing
     cudaEvent_t ev0 = nullptr, ev1 = nullptr;
@@ -319,6 +330,9 @@ void residual_norms(mpet_ctx* c, const double* b, const double* x, double* r, do
 void apply_preconditioner(mpet_ctx* c, int precision, const void* r, void* z);
 int choose_lpr(int64_t n, int64_t nnz);
 void build_tiles(mpet_ctx* c, Csr& A, const int64_t* rp_host);
+void build_sell(mpet_ctx* c, Csr& A, bool fp32);
+void fill_sell(mpet_ctx* c, Csr& A);
+bool spmv_variant_available(const Csr& A, int variant);
 constexpr int SPMV_TILE = 2048;  // entries per staged tile
 void destroy_minres_graph(mpet_ctx* c);
 void convert_values_to_f32(mpet_ctx* c);

@@ -263,6 +263,97 @@ __global__ void __launch_bounds__(256) k_spmv(int64_t n, const int64_t* __restri
     }
 }
 
+// ---- SELL-32 SpMV -------------------------------------------------------------------
+//
+// One thread owns one row of a 32-row slice; entry k of the slice's rows is
+// contiguous, so every column/value load of a warp is one coalesced 128-byte
+// line and a warp keeps 32 rows (U gathers each) in flight with no
+// cross-lane reduction.  Padding entries are (row, 0).  The loop bound is
+// the slice width, the same for every lane.
+template <typename T, int NV, int U, class Epi>
+__global__ void __launch_bounds__(256) k_spmv_sell(int64_t n, int64_t nslices, const int64_t* __restrict__ soff,
+                                                   const int32_t* __restrict__ sci, const T* __restrict__ sva,
+                                                   const T* __restrict__ x, Epi epi, double* partials) {
+    const int lane = threadIdx.x & 31;
+    const int64_t warp = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) >> 5;
+    const int64_t nwarps = ((int64_t)gridDim.x * blockDim.x) >> 5;
+    double r0 = 0.0, r1 = 0.0;
+    for (int64_t sl = warp; sl < nslices; sl += nwarps) {
+        const int64_t row = sl * 32 + lane;
+        const int64_t o1 = soff[sl + 1];
+        typename Epi::Pre pre{};
+        if (row < n) pre = epi.pre(row);
+        T acc[NV];
+#pragma unroll
+        for (int k = 0; k < NV; ++k) acc[k] = T(0);
+        for (int64_t e = soff[sl] + lane; e < o1; e += 32 * U) {
+            int32_t cc[U];
+            T aa[U];
+#pragma unroll
+            for (int u = 0; u < U; ++u) {
+                cc[u] = 0;
+                aa[u] = T(0);
+                if (e + u * 32 < o1) {
+                    cc[u] = __ldcs(sci + e + u * 32);
+                    aa[u] = __ldcs(sva + e + u * 32);
+                }
+            }
+#pragma unroll
+            for (int u = 0; u < U; ++u) {
+                if (e + u * 32 < o1) {
+                    T xv[NV];
+                    VecIO<T, NV>::load(x, cc[u], xv);
+#pragma unroll
+                    for (int k = 0; k < NV; ++k) acc[k] += aa[u] * xv[k];
+                }
+            }
+        }
+        if (row < n) epi.apply(row, acc, pre, r0, r1);
+    }
+    if constexpr (Epi::kRed > 0) {
+        __shared__ double sh[8];
+        double t0 = block_sum256(r0, sh);
+        if (threadIdx.x == 0) partials[blockIdx.x] = t0;
+        if constexpr (Epi::kRed > 1) {
+            double t1 = block_sum256(r1, sh);
+            if (threadIdx.x == 0) partials[NB_RED + blockIdx.x] = t1;
+        }
+    }
+}
+
+__global__ void k_sell_width(int64_t n, int64_t nslices, const int64_t* __restrict__ rp, int64_t* w32) {
+    const int64_t sl = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    if (sl >= nslices) return;
+    int64_t w = 0;
+    const int64_t r1 = (sl + 1) * 32 < n ? (sl + 1) * 32 : n;
+    for (int64_t r = sl * 32; r < r1; ++r) {
+        const int64_t len = rp[r + 1] - rp[r];
+        w = len > w ? len : w;
+    }
+    w32[sl] = 32 * w;
+}
+
+template <typename T>
+__global__ void k_sell_fill(int64_t n, int64_t nslices, const int64_t* __restrict__ rp,
+                            const int32_t* __restrict__ ci, const T* __restrict__ v,
+                            const int64_t* __restrict__ soff, int32_t* sci, T* sv) {
+    const int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    if (t >= nslices * 32) return;
+    const int64_t sl = t >> 5, lane = t & 31, row = t;
+    const int64_t w = (soff[sl + 1] - soff[sl]) >> 5;
+    const int64_t e0 = row < n ? rp[row] : 0, len = row < n ? rp[row + 1] - e0 : 0;
+    for (int64_t k = 0; k < w; ++k) {
+        const int64_t q = soff[sl] + k * 32 + lane;
+        if (k < len) {
+            sci[q] = ci[e0 + k];
+            sv[q] = v[e0 + k];
+        } else {
+            sci[q] = row < n ? (int32_t)row : 0;
+            sv[q] = T(0);
+        }
+    }
+}
+
 // ---- shared-memory staged SpMV (bulk async copies) ----------------------------------
 //
 // A CTA walks a list of row tiles; each tile's column ids and values are a
@@ -474,8 +565,76 @@ void build_tiles(mpet_ctx* c, Csr& A, const int64_t* rp) {
     A.ntiles = (int)t.size() - 1;
 }
 
+template <typename T>
+static const T* vals(const Csr& A);
+template <>
+const double* vals<double>(const Csr& A) { return A.v64; }
+template <>
+const float* vals<float>(const Csr& A) { return A.v32; }
+
+// SELL-32 layout of a matrix (slice offsets scanned on the host, column
+// ids and values allocated in the precision given); fill_sell copies the
+// current CSR values in (again after every change of the values).
+void build_sell(mpet_ctx* c, Csr& A, bool fp32) {
+    if (A.n == 0 || A.nnz == 0) return;
+    const int64_t ns = (A.n + 31) / 32;
+    int64_t* w = c->pool.alloc<int64_t>(ns + 1);
+    k_sell_width<<<grid_for(ns, 256), 256, 0, c->stream>>>(A.n, ns, A.rp, w);
+    MPET_CHECK_LAUNCH();
+    std::vector<int64_t> off(ns + 1);
+    MPET_CUDA(cudaMemcpyAsync(off.data(), w, sizeof(int64_t) * ns, cudaMemcpyDeviceToHost, c->stream));
+    MPET_CUDA(cudaStreamSynchronize(c->stream));
+    int64_t acc = 0;
+    for (int64_t s = 0; s < ns; ++s) {
+        const int64_t ws = off[s];
+        off[s] = acc;
+        acc += ws;
+    }
+    off[ns] = acc;
+    A.nslices = ns;
+    A.s_off = w;
+    MPET_CUDA(cudaMemcpyAsync(A.s_off, off.data(), sizeof(int64_t) * (ns + 1), cudaMemcpyHostToDevice, c->stream));
+    A.s_ci = c->pool.alloc<int32_t>(acc);
+    if (fp32) A.s_v32 = c->pool.alloc<float>(acc);
+    else A.s_v64 = c->pool.alloc<double>(acc);
+    MPET_CUDA(cudaStreamSynchronize(c->stream));
+    fill_sell(c, A);
+}
+
+void fill_sell(mpet_ctx* c, Csr& A) {
+    if (!A.s_off) return;
+    const int64_t ns = A.nslices;
+    if (A.s_v32)
+        k_sell_fill<float><<<grid_for(ns * 32, 256), 256, 0, c->stream>>>(A.n, ns, A.rp, A.ci, A.v32, A.s_off,
+                                                                          A.s_ci, A.s_v32);
+    else
+        k_sell_fill<double><<<grid_for(ns * 32, 256), 256, 0, c->stream>>>(A.n, ns, A.rp, A.ci, A.v64, A.s_off,
+                                                                           A.s_ci, A.s_v64);
+    MPET_CHECK_LAUNCH();
+}
+
+template <typename T>
+static const T* sell_vals(const Csr& A);
+template <>
+const double* sell_vals<double>(const Csr& A) { return A.s_v64; }
+template <>
+const float* sell_vals<float>(const Csr& A) { return A.s_v32; }
+
 template <typename T, int NV, class Epi>
 static void launch_spmv(mpet_ctx* c, const Csr& A, const T* va, const T* x, const Epi& epi) {
+    if ((A.variant & 4) && sell_vals<T>(A) && va == vals<T>(A)) {
+        int blocks = Epi::kRed > 0 ? NB_RED : grid_for(A.nslices * 32, 256);
+        if (Epi::kRed == 0 && blocks > 152 * 16) blocks = 152 * 16;
+        if (A.variant & 1)
+            k_spmv_sell<T, NV, 8, Epi><<<blocks, 256, 0, c->stream>>>(A.n, A.nslices, A.s_off, A.s_ci,
+                                                                      sell_vals<T>(A), x, epi, c->partials);
+        else
+            k_spmv_sell<T, NV, 4, Epi><<<blocks, 256, 0, c->stream>>>(A.n, A.nslices, A.s_off, A.s_ci,
+                                                                      sell_vals<T>(A), x, epi, c->partials);
+        MPET_CHECK_LAUNCH();
+        c->n_launch++;
+        return;
+    }
     const bool deep = A.lpr == 32 && (A.variant & 1);
     if (A.ntiles > 0 && (A.variant & 2)) {
         switch (A.lpr) {
@@ -514,18 +673,22 @@ static void launch_spmv(mpet_ctx* c, const Csr& A, const T* va, const T* x, cons
 }
 
 template <typename T>
-static const T* vals(const Csr& A);
-template <>
-const double* vals<double>(const Csr& A) { return A.v64; }
-template <>
-const float* vals<float>(const Csr& A) { return A.v32; }
-
-template <typename T>
 static const T* dinv_of(const AmgLevel& L);
 template <>
 const double* dinv_of<double>(const AmgLevel& L) { return L.dinv64; }
 template <>
 const float* dinv_of<float>(const AmgLevel& L) { return L.dinv32; }
+
+// Variant v (bits as in Csr::variant) can run on A with its current lanes
+// per row: staged needs row tiles, SELL its copy, 8 entries per lane (CSR)
+// 32 lanes per row.
+bool spmv_variant_available(const Csr& A, int v) {
+    if (v < 0 || v > 5) return false;
+    if (v & 4) return A.s_off != nullptr && !(v & 2);
+    if ((v & 2) && A.ntiles == 0) return false;
+    if ((v & 1) && A.lpr != 32) return false;
+    return true;
+}
 
 // Set-up autotuning: time every applicable SpMV variant on this matrix with
 // the epilogue it runs in the solver (2 warm-up + 5 timed launches each) and
@@ -540,9 +703,8 @@ static void autotune_matrix(mpet_ctx* c, Csr& A, const T* x, const Epi& epi, dou
     for (int lpr : {lpr0, lpr0 / 2}) {
         if (lpr < 4 && lpr != lpr0) continue;
         A.lpr = lpr;
-        for (int v = 0; v < 4; ++v) {
-            if ((v & 2) && A.ntiles == 0) continue;
-            if ((v & 1) && lpr != 32) continue;
+        for (int v = 0; v < 6; ++v) {
+            if (!spmv_variant_available(A, v) || (v >= 4 && (!sell_vals<T>(A) || lpr != lpr0))) continue;
             A.variant = v;
             for (int q = 0; q < 2; ++q) launch_spmv<T, NV>(c, A, vals<T>(A), x, epi);
             MPET_CUDA(cudaEventRecord(c->ev0, c->stream));
@@ -1127,6 +1289,7 @@ static void upload_csr(mpet_ctx* c, const HostCsr& h, Csr& d, bool fp32) {
     }
     d.lpr = choose_lpr(d.n, d.nnz);
     build_tiles(c, d, h.rp.data());
+    build_sell(c, d, fp32);
 }
 
 void upload_amg(mpet_ctx* c, AmgHier& h, const HostAmg& ha, int nvec, bool fp32) {
