@@ -151,6 +151,20 @@ int mpet_set_cell_permeability(mpet_ctx* ctx, const double* K_cells);
  * rebuilt afterwards. */
 int mpet_set_cell_coefficients(mpet_ctx* ctx, const double* c_cells, const double* S_cells);
 
+/* Declare the uploaded mesh a batch of ninst independent instances (disjoint
+ * instance meshes in one upload; vertex_instance: host array, the instance
+ * of every vertex).  The system and the preconditioner stay one block-
+ * diagonal operator run by the same kernels; the solves then converge every
+ * instance to params.rtol on its own (per-instance residual scaling and
+ * stopping; the stats report the worst instance).  No reference counterpart:
+ * the reference runs one problem per MPETSolver.  MPET_ERR_INVALID if an
+ * edge joins two instances. */
+int mpet_set_batch(mpet_ctx* ctx, int32_t ninst, const int32_t* vertex_instance);
+
+/* Per-instance relative preconditioned residual of the last batch solve
+ * (host array of ninst). */
+int mpet_get_batch_relres(mpet_ctx* ctx, double* relres_host);
+
 /* Boundary facets (the nf facets of mpet_mesh_upload, same order): their P2
  * nodes (nf x 6: the three vertices ascending, then the edges (1,2), (0,2),
  * (0,1)) and area + outward unit normal (nf x 4), copied into device arrays
@@ -243,6 +257,12 @@ int mpet_get_spmv_tuning(mpet_ctx* ctx, double* ms6_host, int32_t* chosen);
  * computes the same product (summation order differs).  No reference
  * counterpart (tuning and test hook). */
 int mpet_set_spmv_variant(mpet_ctx* ctx, int32_t variant);
+
+/* The same override for every matrix of the AMG hierarchies (operators,
+ * prolongations, restrictions): each takes the variant where it can run and
+ * the CSR register kernel (0) elsewhere, until the next
+ * mpet_setup_preconditioner.  No reference counterpart (test hook). */
+int mpet_set_hierarchy_spmv_variant(mpet_ctx* ctx, int32_t variant);
 
 /* Per-kernel timing of the last solve (CUDA events): total ms and launches. */
 int mpet_get_timing(mpet_ctx* ctx, double* spmv_ms, int64_t* spmv_launches,

@@ -340,3 +340,33 @@ def test_assembly_and_solve_are_deterministic():
     s.step(dt)
     x2 = _np(s.up.vector()).copy()
     assert np.array_equal(x1, x2)
+
+
+def test_preconditioner_spmv_variants_agree_and_symmetric():
+    """The block AMG preconditioner gives the same z = M^-1 r with every SpMV
+    variant of its matrices (CSR register, SELL-32 with 4 / 8 entries per
+    batch; rectangular prolongations and restrictions included), and M^-1 is
+    symmetric (MINRES needs it)."""
+    problem, dt = make_problem(5, 2)
+    s = _solver(problem, dt, precision="fp64")
+    s._assemble(dt)
+    rng = np.random.default_rng(11)
+    r = torch.tensor(rng.standard_normal(s.N), device=s.device)
+    q = torch.tensor(rng.standard_normal(s.N), device=s.device)
+    out = {}
+    for v in (0, 4, 5):
+        s.ctx.call("mpet_set_hierarchy_spmv_variant", v)
+        z = torch.empty_like(r)
+        s.ctx.call("mpet_apply_preconditioner", 0, _lib()._ptr(r), _lib()._ptr(z))
+        w = torch.empty_like(r)
+        s.ctx.call("mpet_apply_preconditioner", 0, _lib()._ptr(q), _lib()._ptr(w))
+        torch.cuda.synchronize()
+        out[v] = (_np(z), _np(w))
+    z0 = out[0][0]
+    assert np.all(np.isfinite(z0)) and np.linalg.norm(z0) > 0
+    for v in (4, 5):
+        assert np.linalg.norm(out[v][0] - z0) <= 1e-12 * np.linalg.norm(z0)
+    z, w = out[0]
+    rq = float(_np(q) @ z)
+    qr = float(_np(r) @ w)
+    assert abs(rq - qr) <= 1e-10 * (abs(rq) + abs(qr))

@@ -14,9 +14,12 @@ def __getattr__(name):
     if name in ("MPETSolver", "Function"):
         from . import solver
         return getattr(solver, name)
+    if name == "MPETBatchSolver":
+        from . import batch
+        return batch.MPETBatchSolver
     raise AttributeError(name)
 
 
 __all__ = ["Mesh", "MeshFunction", "CompiledSubDomain", "UnitCubeMesh", "UnitSquareMesh",
            "EllipsoidShellMesh", "near", "INVALID_MARKER", "Constant", "Expression", "MPETProblem",
-           "MPETSolver", "convert_to_E_nu", "convert_to_mu_lmbda"]
+           "MPETSolver", "MPETBatchSolver", "convert_to_E_nu", "convert_to_mu_lmbda"]

@@ -98,6 +98,8 @@ SIGNATURES = {
     "mpet_set_sources": [_P, _P, _P],
     "mpet_set_cell_permeability": [_P, _P],
     "mpet_set_cell_coefficients": [_P, _P, _P],
+    "mpet_set_batch": [_P, _I32, _P],
+    "mpet_get_batch_relres": [_P, _P],
     "mpet_get_facet_data": [_P, _P, _P],
     "mpet_set_facet_data": [_P, _I32, _P],
     "mpet_rhs": [_P, _D, _P, _P],
@@ -112,6 +114,7 @@ SIGNATURES = {
     "mpet_apply_symmetric": [_P, _P, _P],
     "mpet_get_spmv_tuning": [_P, _P, ctypes.POINTER(_I32)],
     "mpet_set_spmv_variant": [_P, _I32],
+    "mpet_set_hierarchy_spmv_variant": [_P, _I32],
     "mpet_get_timing": [_P, ctypes.POINTER(_D), ctypes.POINTER(_I64), ctypes.POINTER(_D), ctypes.POINTER(_I64)],
     "mpet_pressure_misfit": [_P, _P, _P, ctypes.POINTER(_D), _P],
     "mpet_adjoint_rhs": [_P, _D, _P, _P],

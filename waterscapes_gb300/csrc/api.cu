@@ -68,6 +68,7 @@ int mpet_ctx_destroy(mpet_ctx* c) {
     if (c->ev_fork) cudaEventDestroy(c->ev_fork);
     c->pool.free_all();
     if (c->sc_host) cudaFreeHost(c->sc_host);
+    if (c->inst_host) cudaFreeHost(c->inst_host);
     if (c->ev0) cudaEventDestroy(c->ev0);
     if (c->ev1) cudaEventDestroy(c->ev1);
     if (c->own_stream && c->stream) cudaStreamDestroy(c->stream);
@@ -315,6 +316,23 @@ int mpet_set_cell_coefficients(mpet_ctx* c, const double* c_cells, const double*
     API_END(c)
 }
 
+int mpet_set_batch(mpet_ctx* c, int32_t ninst, const int32_t* vertex_instance) {
+    API_BEGIN(c)
+    require(c->setup_done, MPET_ERR_STATE, "mpet_setup must come first");
+    require(c->ninst == 0, MPET_ERR_STATE, "the batch partition is already set");
+    require(ninst >= 1 && vertex_instance, MPET_ERR_INVALID, "need ninst >= 1 and an instance per vertex");
+    setup_batch(c, ninst, vertex_instance);
+    API_END(c)
+}
+
+int mpet_get_batch_relres(mpet_ctx* c, double* relres_host) {
+    API_BEGIN(c)
+    require(c->ninst > 0 && c->inst_host, MPET_ERR_STATE, "no batch solve yet");
+    require(relres_host, MPET_ERR_INVALID, "NULL argument");
+    batch_relres(c, relres_host);
+    API_END(c)
+}
+
 int mpet_get_facet_data(mpet_ctx* c, int32_t* fnodes, double* area_normal) {
     API_BEGIN(c)
     require(c->setup_done, MPET_ERR_STATE, "mpet_setup must come first");
@@ -529,6 +547,24 @@ int mpet_get_spmv_tuning(mpet_ctx* c, double* ms6, int32_t* chosen) {
     if (ms6)
         for (int v = 0; v < 6; ++v) ms6[v] = c->spmv_variant_ms[v];
     if (chosen) *chosen = c->A.variant;
+    API_END(c)
+}
+
+int mpet_set_hierarchy_spmv_variant(mpet_ctx* c, int32_t variant) {
+    API_BEGIN(c)
+    require(c->precond_ready, MPET_ERR_STATE, "mpet_setup_preconditioner must come first");
+    require(variant >= 0 && variant <= 5, MPET_ERR_INVALID, "variant out of range");
+    destroy_minres_graph(c);
+    auto set = [&](mpet::Csr& M) { M.variant = spmv_variant_available(M, variant) ? variant : 0; };
+    auto hier = [&](mpet::AmgHier& h) {
+        for (auto& L : h.lev) {
+            set(L.A);
+            set(L.P);
+            set(L.R);
+        }
+    };
+    hier(c->amg_u);
+    for (int a = 0; a < c->J; ++a) hier(c->amg_p[a]);
     API_END(c)
 }
 

@@ -79,8 +79,9 @@ struct Csr {
     // (needs tiles), bit 2 = SELL-32 copy (needs s_off)
     int variant = 0;
     // SELL-32 copy: slices of 32 rows, column-major within a slice, padded
-    // to the slice's longest row with (row, 0) entries; s_off[s] is the first
-    // entry of slice s (nslices + 1 offsets)
+    // to the slice's longest row with zero values at the row's last column
+    // (column 0 for empty rows); s_off[s] is the first entry of slice s
+    // (nslices + 1 offsets)
     int64_t nslices = 0;
     int64_t* s_off = nullptr;
     int32_t* s_ci = nullptr;
@@ -247,6 +248,20 @@ struct mpet_ctx {
     cudaGraphExec_t mr_graph = nullptr;
     int64_t mr_graph_launches = 0;  // kernels per graph launch
 
+    // batch of independent instances in one mesh (ninst = 0: one instance):
+    // DOF chunks of one instance each, the chunks of every instance in row
+    // order, per-chunk partial sums and per-instance scalars
+    int ninst = 0;
+    int64_t nchunks = 0;
+    int64_t* ch_lo = nullptr;
+    int32_t* ch_len = nullptr;
+    int32_t* ch_inst = nullptr;
+    int32_t* inst_cptr = nullptr;
+    int32_t* inst_chunks = nullptr;
+    double* ch_part = nullptr;
+    double* inst_v = nullptr;
+    double* inst_host = nullptr;  // pinned
+
     // set by a kernel whose bounded wait gave up (read after each solve)
     int* dev_err = nullptr;
     // set-up timings (ms) of the six SpMV variants on the system matrix
@@ -263,6 +278,7 @@ namespace mpet {
 
 constexpr int NB_RED = 1216;  // fixed block count of every reduction kernel (152 SMs x 8)
 constexpr int RED_THREADS = 256;
+constexpr int BATCH_CHUNK = 4096;  // rows per chunk of the per-instance reductions
 
 #ifdef __CUDACC__
 __device__ __forceinline__ double warp_sum(double v) {
@@ -328,6 +344,8 @@ void alloc_krylov(mpet_ctx* c);
 void autotune_system(mpet_ctx* c);
 void residual_norms(mpet_ctx* c, const double* b, const double* x, double* r, double* norms);
 void apply_preconditioner(mpet_ctx* c, int precision, const void* r, void* z);
+void setup_batch(mpet_ctx* c, int ninst, const int32_t* vertex_inst);
+void batch_relres(mpet_ctx* c, double* out);
 int choose_lpr(int64_t n, int64_t nnz);
 void build_tiles(mpet_ctx* c, Csr& A, const int64_t* rp_host);
 void build_sell(mpet_ctx* c, Csr& A, bool fp32);

@@ -268,8 +268,8 @@ __global__ void __launch_bounds__(256) k_spmv(int64_t n, const int64_t* __restri
 // One thread owns one row of a 32-row slice; entry k of the slice's rows is
 // contiguous, so every column/value load of a warp is one coalesced 128-byte
 // line and a warp keeps 32 rows (U gathers each) in flight with no
-// cross-lane reduction.  Padding entries are (row, 0).  The loop bound is
-// the slice width, the same for every lane.
+// cross-lane reduction.  Padding entries carry value 0 and a valid column
+// of the row.  The loop bound is the slice width, the same for every lane.
 template <typename T, int NV, int U, class Epi>
 __global__ void __launch_bounds__(256) k_spmv_sell(int64_t n, int64_t nslices, const int64_t* __restrict__ soff,
                                                    const int32_t* __restrict__ sci, const T* __restrict__ sva,
@@ -342,13 +342,16 @@ __global__ void k_sell_fill(int64_t n, int64_t nslices, const int64_t* __restric
     const int64_t sl = t >> 5, lane = t & 31, row = t;
     const int64_t w = (soff[sl + 1] - soff[sl]) >> 5;
     const int64_t e0 = row < n ? rp[row] : 0, len = row < n ? rp[row + 1] - e0 : 0;
+    // padding repeats the row's last column (a valid index of x, and a line
+    // the row has just read), or column 0 for an empty row
+    const int32_t pad = len > 0 ? ci[e0 + len - 1] : 0;
     for (int64_t k = 0; k < w; ++k) {
         const int64_t q = soff[sl] + k * 32 + lane;
         if (k < len) {
             sci[q] = ci[e0 + k];
             sv[q] = v[e0 + k];
         } else {
-            sci[q] = row < n ? (int32_t)row : 0;
+            sci[q] = pad;
             sv[q] = T(0);
         }
     }
@@ -1242,7 +1245,304 @@ void residual_norms(mpet_ctx* c, const double* b, const double* x, double* r, do
     norms[1] = sqrt(c->sc_host->nb2);
 }
 
+// ---- batches of independent instances -----------------------------------------------
+//
+// A batch is one mesh made of disjoint instance meshes, so the system and the
+// AMG hierarchies are block diagonal and every kernel above runs all
+// instances at once.  Only the refinement loop is per instance: the DOFs are
+// cut into chunks of at most BATCH_CHUNK rows of one instance; per-chunk
+// partial sums (one block each) are added per instance in chunk order, so
+// the per-instance norms are deterministic.  Each sweep scales every
+// unconverged instance's residual to a unit preconditioned norm (converged
+// instances to zero), runs one MINRES on the union, and adds each instance's
+// correction back with its own scale.
+
+template <typename T>
+__global__ void k_seg_dot(const int64_t* __restrict__ lo, const int32_t* __restrict__ len, int64_t nch,
+                          const T* __restrict__ a, const T* __restrict__ b, double* part) {
+    __shared__ double sh[8];
+    const int64_t ch = blockIdx.x;
+    double s = 0.0;
+    for (int i = threadIdx.x; i < len[ch]; i += 256) {
+        const int64_t r = lo[ch] + i;
+        s += (double)a[r] * (double)b[r];
+    }
+    s = block_sum256(s, sh);
+    if (threadIdx.x == 0) part[ch] = s;
+}
+
+// (r D^-1)^2 and (b D^-1)^2 per chunk
+__global__ void k_seg_norms(const int64_t* __restrict__ lo, const int32_t* __restrict__ len, int64_t nch,
+                            const double* __restrict__ r, const double* __restrict__ b,
+                            const double* __restrict__ dinv, double* part) {
+    __shared__ double sh[8];
+    const int64_t ch = blockIdx.x;
+    double s0 = 0.0, s1 = 0.0;
+    for (int i = threadIdx.x; i < len[ch]; i += 256) {
+        const int64_t q = lo[ch] + i;
+        const double di = dinv[q];
+        s0 += (r[q] * di) * (r[q] * di);
+        s1 += (b[q] * di) * (b[q] * di);
+    }
+    s0 = block_sum256(s0, sh);
+    s1 = block_sum256(s1, sh);
+    if (threadIdx.x == 0) {
+        part[ch] = s0;
+        part[nch + ch] = s1;
+    }
+}
+
+// out[v * ninst + i] = sum over instance i's chunks (in order) of part[v * nch + chunk]
+__global__ void k_seg_finish(int ninst, const int32_t* __restrict__ cptr, const int32_t* __restrict__ chunks,
+                             const double* __restrict__ part, int64_t nch, int nval, double* out) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= ninst) return;
+    for (int v = 0; v < nval; ++v) {
+        double s = 0.0;
+        for (int k = cptr[i]; k < cptr[i + 1]; ++k) s += part[v * nch + chunks[k]];
+        out[v * ninst + i] = s;
+    }
+}
+
+template <typename T>
+__global__ void k_seg_scale_from64(const int64_t* __restrict__ lo, const int32_t* __restrict__ len,
+                                   const int32_t* __restrict__ inst, const double* __restrict__ r,
+                                   const double* __restrict__ scale, T* out) {
+    const int64_t ch = blockIdx.x;
+    const double s = scale[inst[ch]];
+    for (int i = threadIdx.x; i < len[ch]; i += 256) out[lo[ch] + i] = (T)(r[lo[ch] + i] * s);
+}
+
+template <typename T>
+__global__ void k_seg_scale(const int64_t* __restrict__ lo, const int32_t* __restrict__ len,
+                            const int32_t* __restrict__ inst, const double* __restrict__ scale, T* v, T* w) {
+    const int64_t ch = blockIdx.x;
+    const T s = (T)scale[inst[ch]];
+    for (int i = threadIdx.x; i < len[ch]; i += 256) {
+        v[lo[ch] + i] *= s;
+        w[lo[ch] + i] *= s;
+    }
+}
+
+template <typename T>
+__global__ void k_seg_add(const int64_t* __restrict__ lo, const int32_t* __restrict__ len,
+                          const int32_t* __restrict__ inst, const double* __restrict__ scale, double* x,
+                          const T* __restrict__ d) {
+    const int64_t ch = blockIdx.x;
+    const double s = scale[inst[ch]];
+    for (int i = threadIdx.x; i < len[ch]; i += 256) x[lo[ch] + i] += s * (double)d[lo[ch] + i];
+}
+
+// Per-instance scalars (BatchVals rows of ninst doubles).
+enum BatchVals { BV_NR2, BV_NB2, BV_Q, BV_RSCALE, BV_SIN, BV_SOUT, BV_ETA, BV_ETA0, BV_DONE, BV_COUNT };
+
+__global__ void k_batch_rscale(int ninst, double* iv) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= ninst) return;
+    const double nr = sqrt(iv[BV_NR2 * ninst + i]);
+    iv[BV_RSCALE * ninst + i] = nr > 0.0 ? 1.0 / nr : 0.0;
+}
+
+// eta_i = sqrt(r_i^T M^-1 r_i) from q_i = rhs_i^T M^-1 rhs_i with rhs_i = r_i / ||D^-1 r_i||
+__global__ void k_batch_status(int ninst, double* iv, double rtol, int first) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= ninst) return;
+    const double nr = sqrt(iv[BV_NR2 * ninst + i]);
+    const double q = iv[BV_Q * ninst + i];
+    const double beta = q > 0.0 ? sqrt(q) : 0.0;
+    const double eta = beta * nr;
+    if (first) iv[BV_ETA0 * ninst + i] = eta;
+    const double eta0 = iv[BV_ETA0 * ninst + i];
+    const bool done = !(eta > 0.0) || eta <= rtol * eta0;
+    iv[BV_ETA * ninst + i] = eta;
+    iv[BV_DONE * ninst + i] = done ? 1.0 : 0.0;
+    iv[BV_SIN * ninst + i] = done ? 0.0 : 1.0 / beta;
+    iv[BV_SOUT * ninst + i] = done ? 0.0 : eta;
+}
+
+template <typename T>
+static int solve_batch(mpet_ctx* c, const double* b, double* x, mpet_stats* st, bool homogeneous) {
+    const int64_t n = c->N;
+    const int G = grid_for(n, 256);
+    const int ni = c->ninst;
+    const int64_t nch = c->nchunks;
+    const int gi = grid_for(ni, 128);
+    double* iv = c->inst_v;
+    if (homogeneous) launch_zero_bc_rows(c, x);
+    else launch_set_bc_in_x(c, x);
+    int iters = 0, outer = 0;
+    int status = MPET_OK;
+    double relres = 1.0, relres_true = 0.0;
+    const bool fp64 = sizeof(T) == 8;
+    const int max_outer = c->prm.max_outer > 0 ? c->prm.max_outer : 20;
+    const int maxit = c->prm.maxit > 0 ? c->prm.maxit : 5000;
+    T* rhs = (T*)c->kr[0];
+    T* y = (T*)c->kr[2];
+    for (outer = 0; outer < max_outer; ++outer) {
+        launch_spmv<double, 1>(c, c->A, c->A.v64, x, EpiResid64{c->orr, b, c->dinv});
+        c->n_spmv++;
+        k_seg_norms<<<(unsigned)nch, 256, 0, c->stream>>>(c->ch_lo, c->ch_len, nch, c->orr, b, c->dinv, c->ch_part);
+        k_seg_finish<<<gi, 128, 0, c->stream>>>(ni, c->inst_cptr, c->inst_chunks, c->ch_part, nch, 2,
+                                                iv + BV_NR2 * ni);
+        k_batch_rscale<<<gi, 128, 0, c->stream>>>(ni, iv);
+        k_seg_scale_from64<T><<<(unsigned)nch, 256, 0, c->stream>>>(c->ch_lo, c->ch_len, c->ch_inst, c->orr,
+                                                                    iv + BV_RSCALE * ni, rhs);
+        MPET_CHECK_LAUNCH();
+        precond<T>(c, rhs, y);
+        k_seg_dot<T><<<(unsigned)nch, 256, 0, c->stream>>>(c->ch_lo, c->ch_len, nch, rhs, y, c->ch_part);
+        k_seg_finish<<<gi, 128, 0, c->stream>>>(ni, c->inst_cptr, c->inst_chunks, c->ch_part, nch, 1,
+                                                iv + BV_Q * ni);
+        k_batch_status<<<gi, 128, 0, c->stream>>>(ni, iv, c->prm.rtol, outer == 0 ? 1 : 0);
+        MPET_CHECK_LAUNCH();
+        MPET_CUDA(cudaMemcpyAsync(c->inst_host, iv, sizeof(double) * BV_COUNT * ni, cudaMemcpyDeviceToHost,
+                                  c->stream));
+        MPET_CUDA(cudaStreamSynchronize(c->stream));
+        const double* h = c->inst_host;
+        int active = 0;
+        double worst = 0.0, worst_true = 0.0, need = 1.0;
+        for (int i = 0; i < ni; ++i) {
+            const double eta = h[BV_ETA * ni + i], eta0 = h[BV_ETA0 * ni + i];
+            const double rr = eta0 > 0.0 ? eta / eta0 : 0.0;
+            worst = rr > worst ? rr : worst;
+            const double nb2 = h[BV_NB2 * ni + i];
+            const double rt = nb2 > 0.0 ? sqrt(h[BV_NR2 * ni + i] / nb2) : 0.0;
+            worst_true = rt > worst_true ? rt : worst_true;
+            if (h[BV_DONE * ni + i] == 0.0) {
+                ++active;
+                const double want = c->prm.rtol * eta0 / eta;
+                need = want < need ? want : need;
+            }
+        }
+        relres = worst;
+        relres_true = worst_true;
+        if (active == 0) break;
+        if (iters >= maxit) {
+            status = MPET_ERR_MAXIT;
+            break;
+        }
+        // unit preconditioned norm per unconverged instance, zero otherwise
+        k_seg_scale<T><<<(unsigned)nch, 256, 0, c->stream>>>(c->ch_lo, c->ch_len, c->ch_inst, iv + BV_SIN * ni,
+                                                             rhs, y);
+        k_copy2<T><<<G, 256, 0, c->stream>>>(n, rhs, (T*)c->kr[1], (T*)c->kr[1]);
+        k_dot<T><<<NB_RED, 256, 0, c->stream>>>(n, rhs, y, c->partials);
+        k_mr_init<<<1, 256, 0, c->stream>>>(c->sc, c->partials);
+        MPET_CHECK_LAUNCH();
+        double target = need / sqrt((double)active);
+        if (fp64) {
+            if (target < 1e-15) target = 1e-15;
+        } else {
+            if (target < c->prm.inner_rtol) target = c->prm.inner_rtol;
+        }
+        MPET_CUDA(cudaMemsetAsync(c->kd, 0, sizeof(T) * n, c->stream));
+        for (int q = 0; q < 3; ++q) MPET_CUDA(cudaMemsetAsync(c->kw[q], 0, sizeof(T) * n, c->stream));
+        int done = 0;
+        int s2 = minres_run<T>(c, target, maxit - iters, &done);
+        iters += done;
+        k_seg_add<T><<<(unsigned)nch, 256, 0, c->stream>>>(c->ch_lo, c->ch_len, c->ch_inst, iv + BV_SOUT * ni, x,
+                                                           (const T*)c->kd);
+        MPET_CHECK_LAUNCH();
+        if (s2 != MPET_OK) {
+            status = s2;
+            break;
+        }
+    }
+    if (outer >= max_outer && status == MPET_OK) status = MPET_ERR_MAXIT;
+    int derr = 0;
+    MPET_CUDA(cudaMemcpyAsync(&derr, c->dev_err, sizeof(int), cudaMemcpyDeviceToHost, c->stream));
+    MPET_CUDA(cudaStreamSynchronize(c->stream));
+    if (derr) {
+        MPET_CUDA(cudaMemsetAsync(c->dev_err, 0, sizeof(int), c->stream));
+        status = MPET_ERR_TIMEOUT;
+    }
+    if (st) {
+        st->iterations = iters;
+        st->outer = outer + 1;
+        st->status = status;
+        st->relres = relres;
+        st->relres_true = relres_true;
+    }
+    return status;
+}
+
+// Chunks of the DOF range per instance (vertex_inst: instance of every mesh
+// vertex; an edge node belongs to the instance of its first vertex).
+void setup_batch(mpet_ctx* c, int ninst, const int32_t* vertex_inst) {
+    std::vector<int64_t> key(c->ne);
+    if (c->ne) {
+        MPET_CUDA(cudaMemcpyAsync(key.data(), c->edge_key, sizeof(int64_t) * c->ne, cudaMemcpyDeviceToHost,
+                                  c->stream));
+        MPET_CUDA(cudaStreamSynchronize(c->stream));
+    }
+    std::vector<int32_t> node_inst(c->nnodes);
+    for (int64_t v = 0; v < c->nv; ++v) {
+        const int32_t i = vertex_inst[v];
+        if (i < 0 || i >= ninst) fail(MPET_ERR_INVALID, "instance id out of range");
+        node_inst[v] = i;
+    }
+    for (int64_t e = 0; e < c->ne; ++e) {
+        const int32_t i0 = vertex_inst[key[e] / c->nv], i1 = vertex_inst[key[e] % c->nv];
+        if (i0 != i1) fail(MPET_ERR_INVALID, "an edge joins two instances: instance meshes must be disjoint");
+        node_inst[c->nv + e] = i0;
+    }
+    std::vector<int64_t> lo;
+    std::vector<int32_t> len, inst;
+    auto push = [&](int64_t row, int32_t i) {
+        if (!lo.empty() && inst.back() == i && lo.back() + len.back() == row && len.back() < BATCH_CHUNK) {
+            ++len.back();
+            return;
+        }
+        lo.push_back(row);
+        len.push_back(1);
+        inst.push_back(i);
+    };
+    for (int64_t k = 0; k < c->nnodes; ++k)
+        for (int d = 0; d < 3; ++d) push(3 * k + d, node_inst[k]);
+    for (int a = 0; a < c->J; ++a)
+        for (int64_t v = 0; v < c->nv; ++v) push(c->Nu + (int64_t)a * c->nv + v, node_inst[v]);
+    const int64_t nch = (int64_t)lo.size();
+    std::vector<int32_t> cptr(ninst + 1, 0), order(nch);
+    for (int64_t k = 0; k < nch; ++k) cptr[inst[k] + 1]++;
+    for (int i = 0; i < ninst; ++i) cptr[i + 1] += cptr[i];
+    {
+        std::vector<int32_t> fill(cptr.begin(), cptr.end() - 1);
+        for (int64_t k = 0; k < nch; ++k) order[fill[inst[k]]++] = (int32_t)k;
+    }
+    c->ninst = ninst;
+    c->nchunks = nch;
+    c->ch_lo = c->pool.alloc<int64_t>(nch);
+    c->ch_len = c->pool.alloc<int32_t>(nch);
+    c->ch_inst = c->pool.alloc<int32_t>(nch);
+    c->inst_cptr = c->pool.alloc<int32_t>(ninst + 1);
+    c->inst_chunks = c->pool.alloc<int32_t>(nch);
+    c->ch_part = c->pool.alloc<double>(2 * nch);
+    c->inst_v = c->pool.alloc<double>((int64_t)BV_COUNT * ninst);
+    MPET_CUDA(cudaMemcpyAsync(c->ch_lo, lo.data(), sizeof(int64_t) * nch, cudaMemcpyHostToDevice, c->stream));
+    MPET_CUDA(cudaMemcpyAsync(c->ch_len, len.data(), sizeof(int32_t) * nch, cudaMemcpyHostToDevice, c->stream));
+    MPET_CUDA(cudaMemcpyAsync(c->ch_inst, inst.data(), sizeof(int32_t) * nch, cudaMemcpyHostToDevice, c->stream));
+    MPET_CUDA(cudaMemcpyAsync(c->inst_cptr, cptr.data(), sizeof(int32_t) * (ninst + 1), cudaMemcpyHostToDevice,
+                              c->stream));
+    MPET_CUDA(cudaMemcpyAsync(c->inst_chunks, order.data(), sizeof(int32_t) * nch, cudaMemcpyHostToDevice,
+                              c->stream));
+    MPET_CUDA(cudaMemsetAsync(c->inst_v, 0, sizeof(double) * BV_COUNT * ninst, c->stream));
+    if (c->inst_host) MPET_CUDA(cudaFreeHost(c->inst_host));
+    MPET_CUDA(cudaMallocHost(&c->inst_host, sizeof(double) * BV_COUNT * ninst));
+    MPET_CUDA(cudaStreamSynchronize(c->stream));
+}
+
+void batch_relres(mpet_ctx* c, double* out) {
+    const int ni = c->ninst;
+    const double* h = c->inst_host;
+    for (int i = 0; i < ni; ++i) {
+        const double eta0 = h[BV_ETA0 * ni + i];
+        out[i] = eta0 > 0.0 ? h[BV_ETA * ni + i] / eta0 : 0.0;
+    }
+}
+
 int solve_system(mpet_ctx* c, const double* b, double* x, mpet_stats* st, bool homogeneous) {
+    if (c->ninst > 0) {
+        if (c->prm.precision == MPET_PRECISION_MIXED) return solve_batch<float>(c, b, x, st, homogeneous);
+        return solve_batch<double>(c, b, x, st, homogeneous);
+    }
     if (c->prm.precision == MPET_PRECISION_MIXED) return solve_impl<float>(c, b, x, st, homogeneous);
     return solve_impl<double>(c, b, x, st, homogeneous);
 }
