@@ -168,6 +168,7 @@ def run_steps(solver, torch, steps, warmup, dt):
     e0 = torch.cuda.Event(enable_timing=True)
     e1 = torch.cuda.Event(enable_timing=True)
     it0 = len(solver.solver_monitor["niter"])
+    before = solve_counters(solver)
     e0.record(stream)
     for _ in range(steps):
         next(gen)
@@ -175,7 +176,7 @@ def run_steps(solver, torch, steps, warmup, dt):
     torch.cuda.synchronize()
     ms = e0.elapsed_time(e1)
     its = solver.solver_monitor["niter"][it0:]
-    return ms, its, solver.up.vector().clone()
+    return ms, its, solver.up.vector().clone(), loop_split(solver, before, steps)
 
 
 def time_precond(solver, torch, lib, reps=10):
@@ -226,6 +227,24 @@ def launches(solver):
     n = ctypes.c_int64()
     solver.ctx.call("mpet_get_timing", None, None, None, ctypes.byref(n))
     return n.value
+
+
+def solve_counters(solver):
+    """(ms in MINRES graph replays, their iterations, ms in whole solves) so far."""
+    import ctypes
+    a, b, c = ctypes.c_double(), ctypes.c_int64(), ctypes.c_double()
+    solver.ctx.call("mpet_get_timing", ctypes.byref(a), ctypes.byref(b), ctypes.byref(c), None)
+    return a.value, b.value, c.value
+
+
+def loop_split(solver, before, steps):
+    """Where the timed steps went: inner MINRES (per iteration) vs the rest of
+    each solve (refinement residuals, preconditioner set-up per sweep)."""
+    a0, b0, c0 = before
+    a1, b1, c1 = solve_counters(solver)
+    its = max(1, b1 - b0)
+    return {"inner_ms_per_iteration": (a1 - a0) / its, "solve_ms_per_step": (c1 - c0) / steps,
+            "outside_inner_ms_per_step": ((c1 - c0) - (a1 - a0)) / steps}
 
 
 def cpu_baseline_sample(n_sample=12, J=4, steps=1):
@@ -450,7 +469,7 @@ def main():
         torch.distributed.barrier()
     L0 = launches(sol)
     clk.start()
-    ms_mixed, its_mixed, x_mixed = run_steps(sol, torch, args.steps, args.warmup, dt)
+    ms_mixed, its_mixed, x_mixed, split = run_steps(sol, torch, args.steps, args.warmup, dt)
     clocks = clk.stop()
     L1 = launches(sol)
     value, ms_max = replica_rate(ms_mixed, args.steps)
@@ -488,9 +507,12 @@ def main():
         sol64._assemble(dt)
         spmv64 = time_spmv(sol64, torch, lib)
         spmv["fp64_only_ctx"] = spmv64.get("fp64")
-        ms64, its64, x64 = run_steps(sol64, torch, args.steps, args.warmup, dt)
+        precond64_ms = time_precond(sol64, torch, lib)
+        ms64, its64, x64, split64 = run_steps(sol64, torch, args.steps, args.warmup, dt)
         rel_err = float(torch.linalg.norm(x_mixed - x64) / torch.linalg.norm(x64))
-        res["fp64"] = {"ms_per_step": ms64 / args.steps, "iterations": its64}
+        res["fp64"] = {"ms_per_step": ms64 / args.steps, "iterations": its64,
+                       "iteration_breakdown_ms": dict(split64, spmv_fp64=spmv64["fp64"]["ms"],
+                                                      preconditioner=precond64_ms)}
         del sol64
 
     cpu = None
@@ -529,10 +551,9 @@ def main():
         "setup_s": {"mesh_dofmap_pattern": t_setup, "assemble_plus_amg": t_asm_amg},
         "spmv": spmv,
         "spmv_tuning": spmv_tuning(sol),
-        "iteration_breakdown_ms": {
-            "per_iteration": ms_mixed / args.steps / max(1.0, float(np.mean(its_mixed))),
-            "spmv_fp32": (spmv.get("fp32") or spmv["fp64"])["ms"],
-            "preconditioner": precond_ms},
+        "iteration_breakdown_ms": dict(split, spmv_fp32=(spmv.get("fp32") or spmv["fp64"])["ms"],
+                                       preconditioner=precond_ms),
+        "fp64_iteration_breakdown_ms": res.get("fp64", {}).get("iteration_breakdown_ms"),
         "roofline": {"kernel": "k_spmv<float,1,32,EpiMinres> (FP32 CSR SpMV)" if "fp32" in spmv else "k_spmv<double>",
                      "bound": "hbm", "achieved": sp32["gbs"], "peak": hbm, "unit": "GB/s",
                      "frac": sp32["gbs"] / hbm, "peak_kind": peak_kind,

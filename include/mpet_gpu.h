@@ -264,9 +264,12 @@ int mpet_set_spmv_variant(mpet_ctx* ctx, int32_t variant);
  * mpet_setup_preconditioner.  No reference counterpart (test hook). */
 int mpet_set_hierarchy_spmv_variant(mpet_ctx* ctx, int32_t variant);
 
-/* Per-kernel timing of the last solve (CUDA events): total ms and launches. */
-int mpet_get_timing(mpet_ctx* ctx, double* spmv_ms, int64_t* spmv_launches,
-                    double* precond_ms, int64_t* kernel_launches);
+/* Timing counters (CUDA events on the context's stream), cumulative since
+ * the context was created: ms spent replaying the MINRES iteration graph
+ * and the iterations it ran, ms of whole solves (refinement sweeps
+ * included), and the kernels launched.  No reference counterpart. */
+int mpet_get_timing(mpet_ctx* ctx, double* inner_ms, int64_t* inner_iterations,
+                    double* solve_ms, int64_t* kernel_launches);
 
 /* ---- discrete adjoint with respect to per-cell permeability ----------------
  * The reference has no adjoint; these entry points differentiate the

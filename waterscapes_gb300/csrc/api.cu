@@ -51,6 +51,10 @@ int mpet_ctx_create(int device, mpet_ctx** out) {
     c->own_stream = true;
     cudaEventCreate(&c->ev0);
     cudaEventCreate(&c->ev1);
+    cudaEventCreate(&c->ev_in0);
+    cudaEventCreate(&c->ev_in1);
+    cudaEventCreate(&c->ev_sv0);
+    cudaEventCreate(&c->ev_sv1);
     *out = c;
     return MPET_OK;
 }
@@ -71,6 +75,8 @@ int mpet_ctx_destroy(mpet_ctx* c) {
     if (c->inst_host) cudaFreeHost(c->inst_host);
     if (c->ev0) cudaEventDestroy(c->ev0);
     if (c->ev1) cudaEventDestroy(c->ev1);
+    for (cudaEvent_t e : {c->ev_in0, c->ev_in1, c->ev_sv0, c->ev_sv1})
+        if (e) cudaEventDestroy(e);
     if (c->own_stream && c->stream) cudaStreamDestroy(c->stream);
     delete c;
     return MPET_OK;
@@ -159,7 +165,7 @@ int mpet_setup(mpet_ctx* c, const mpet_params* p) {
     alloc_krylov(c);
     MPET_CUDA(cudaMemsetAsync(c->A.v64, 0, sizeof(double) * c->nnz, c->stream));
     if (c->A.v32) MPET_CUDA(cudaMemsetAsync(c->A.v32, 0, sizeof(float) * c->nnz, c->stream));
-    build_sell(c, c->A, c->A.v32 != nullptr);
+    build_sell(c, c->A, c->A.v32 != nullptr, true);
     autotune_system(c);
     MPET_CUDA(cudaStreamSynchronize(c->stream));
     c->setup_done = true;
@@ -577,11 +583,11 @@ int mpet_set_spmv_variant(mpet_ctx* c, int32_t variant) {
     API_END(c)
 }
 
-int mpet_get_timing(mpet_ctx* c, double* spmv_ms, int64_t* spmv_launches, double* precond_ms, int64_t* launches) {
+int mpet_get_timing(mpet_ctx* c, double* inner_ms, int64_t* inner_iterations, double* solve_ms, int64_t* launches) {
     API_BEGIN(c)
-    if (spmv_ms) *spmv_ms = c->t_spmv_ms;
-    if (spmv_launches) *spmv_launches = c->n_spmv;
-    if (precond_ms) *precond_ms = c->t_prec_ms;
+    if (inner_ms) *inner_ms = c->t_inner_ms;
+    if (inner_iterations) *inner_iterations = c->n_inner_its;
+    if (solve_ms) *solve_ms = c->t_solve_ms;
     if (launches) *launches = c->n_launch;
     API_END(c)
 }

@@ -269,7 +269,9 @@ struct mpet_ctx {
 
     // timing
     cudaEvent_t ev0 = nullptr, ev1 = nullptr;
-    double t_spmv_ms = 0.0, t_prec_ms = 0.0;
+    double t_inner_ms = 0.0, t_solve_ms = 0.0;  // MINRES graph replays / whole solves
+    int64_t n_inner_its = 0;
+    cudaEvent_t ev_in0 = nullptr, ev_in1 = nullptr, ev_sv0 = nullptr, ev_sv1 = nullptr;
     int64_t n_spmv = 0, n_launch = 0;
     bool timing = false;
 };
@@ -348,7 +350,7 @@ void setup_batch(mpet_ctx* c, int ninst, const int32_t* vertex_inst);
 void batch_relres(mpet_ctx* c, double* out);
 int choose_lpr(int64_t n, int64_t nnz);
 void build_tiles(mpet_ctx* c, Csr& A, const int64_t* rp_host);
-void build_sell(mpet_ctx* c, Csr& A, bool fp32);
+void build_sell(mpet_ctx* c, Csr& A, bool fp32, bool with64);
 void fill_sell(mpet_ctx* c, Csr& A);
 bool spmv_variant_available(const Csr& A, int variant);
 constexpr int SPMV_TILE = 2048;  // entries per staged tile

@@ -576,9 +576,11 @@ template <>
 const float* vals<float>(const Csr& A) { return A.v32; }
 
 // SELL-32 layout of a matrix (slice offsets scanned on the host, column
-// ids and values allocated in the precision given); fill_sell copies the
-// current CSR values in (again after every change of the values).
-void build_sell(mpet_ctx* c, Csr& A, bool fp32) {
+// ids and values allocated in the precision given, plus FP64 values when
+// with64: the system matrix of the mixed path, whose refinement residual is
+// FP64); fill_sell copies the current CSR values in (again after every
+// change of the values).
+void build_sell(mpet_ctx* c, Csr& A, bool fp32, bool with64) {
     if (A.n == 0 || A.nnz == 0) return;
     const int64_t ns = (A.n + 31) / 32;
     int64_t* w = c->pool.alloc<int64_t>(ns + 1);
@@ -599,7 +601,7 @@ void build_sell(mpet_ctx* c, Csr& A, bool fp32) {
     MPET_CUDA(cudaMemcpyAsync(A.s_off, off.data(), sizeof(int64_t) * (ns + 1), cudaMemcpyHostToDevice, c->stream));
     A.s_ci = c->pool.alloc<int32_t>(acc);
     if (fp32) A.s_v32 = c->pool.alloc<float>(acc);
-    else A.s_v64 = c->pool.alloc<double>(acc);
+    if (!fp32 || with64) A.s_v64 = c->pool.alloc<double>(acc);
     MPET_CUDA(cudaStreamSynchronize(c->stream));
     fill_sell(c, A);
 }
@@ -610,7 +612,7 @@ void fill_sell(mpet_ctx* c, Csr& A) {
     if (A.s_v32)
         k_sell_fill<float><<<grid_for(ns * 32, 256), 256, 0, c->stream>>>(A.n, ns, A.rp, A.ci, A.v32, A.s_off,
                                                                           A.s_ci, A.s_v32);
-    else
+    if (A.s_v64)
         k_sell_fill<double><<<grid_for(ns * 32, 256), 256, 0, c->stream>>>(A.n, ns, A.rp, A.ci, A.v64, A.s_off,
                                                                            A.s_ci, A.s_v64);
     MPET_CHECK_LAUNCH();
@@ -1197,7 +1199,14 @@ static int solve_impl(mpet_ctx* c, const double* b, double* x, mpet_stats* st, b
         MPET_CUDA(cudaMemsetAsync(c->kd, 0, sizeof(T) * n, c->stream));
         for (int q = 0; q < 3; ++q) MPET_CUDA(cudaMemsetAsync(c->kw[q], 0, sizeof(T) * n, c->stream));
         int done = 0;
+        MPET_CUDA(cudaEventRecord(c->ev_in0, c->stream));
         int s2 = minres_run<T>(c, target, maxit - iters, &done);
+        MPET_CUDA(cudaEventRecord(c->ev_in1, c->stream));
+        MPET_CUDA(cudaEventSynchronize(c->ev_in1));
+        float ims = 0.f;
+        MPET_CUDA(cudaEventElapsedTime(&ims, c->ev_in0, c->ev_in1));
+        c->t_inner_ms += ims;
+        c->n_inner_its += done;
         iters += done;
         k_add_scaled<T><<<G, 256, 0, c->stream>>>(n, x, (const T*)c->kd, c->sc);
         MPET_CHECK_LAUNCH();
@@ -1436,7 +1445,14 @@ static int solve_batch(mpet_ctx* c, const double* b, double* x, mpet_stats* st, 
         MPET_CUDA(cudaMemsetAsync(c->kd, 0, sizeof(T) * n, c->stream));
         for (int q = 0; q < 3; ++q) MPET_CUDA(cudaMemsetAsync(c->kw[q], 0, sizeof(T) * n, c->stream));
         int done = 0;
+        MPET_CUDA(cudaEventRecord(c->ev_in0, c->stream));
         int s2 = minres_run<T>(c, target, maxit - iters, &done);
+        MPET_CUDA(cudaEventRecord(c->ev_in1, c->stream));
+        MPET_CUDA(cudaEventSynchronize(c->ev_in1));
+        float ims = 0.f;
+        MPET_CUDA(cudaEventElapsedTime(&ims, c->ev_in0, c->ev_in1));
+        c->t_inner_ms += ims;
+        c->n_inner_its += done;
         iters += done;
         k_seg_add<T><<<(unsigned)nch, 256, 0, c->stream>>>(c->ch_lo, c->ch_len, c->ch_inst, iv + BV_SOUT * ni, x,
                                                            (const T*)c->kd);
@@ -1539,12 +1555,19 @@ void batch_relres(mpet_ctx* c, double* out) {
 }
 
 int solve_system(mpet_ctx* c, const double* b, double* x, mpet_stats* st, bool homogeneous) {
-    if (c->ninst > 0) {
-        if (c->prm.precision == MPET_PRECISION_MIXED) return solve_batch<float>(c, b, x, st, homogeneous);
-        return solve_batch<double>(c, b, x, st, homogeneous);
-    }
-    if (c->prm.precision == MPET_PRECISION_MIXED) return solve_impl<float>(c, b, x, st, homogeneous);
-    return solve_impl<double>(c, b, x, st, homogeneous);
+    const bool mixed = c->prm.precision == MPET_PRECISION_MIXED;
+    MPET_CUDA(cudaEventRecord(c->ev_sv0, c->stream));
+    int s;
+    if (c->ninst > 0)
+        s = mixed ? solve_batch<float>(c, b, x, st, homogeneous) : solve_batch<double>(c, b, x, st, homogeneous);
+    else
+        s = mixed ? solve_impl<float>(c, b, x, st, homogeneous) : solve_impl<double>(c, b, x, st, homogeneous);
+    MPET_CUDA(cudaEventRecord(c->ev_sv1, c->stream));
+    MPET_CUDA(cudaEventSynchronize(c->ev_sv1));
+    float ms = 0.f;
+    MPET_CUDA(cudaEventElapsedTime(&ms, c->ev_sv0, c->ev_sv1));
+    c->t_solve_ms += ms;
+    return s;
 }
 
 void alloc_krylov(mpet_ctx* c) {
@@ -1589,7 +1612,7 @@ static void upload_csr(mpet_ctx* c, const HostCsr& h, Csr& d, bool fp32) {
     }
     d.lpr = choose_lpr(d.n, d.nnz);
     build_tiles(c, d, h.rp.data());
-    build_sell(c, d, fp32);
+    build_sell(c, d, fp32, false);
 }
 
 void upload_amg(mpet_ctx* c, AmgHier& h, const HostAmg& ha, int nvec, bool fp32) {
