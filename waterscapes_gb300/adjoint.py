@@ -57,11 +57,12 @@ class MisfitAdjoint:
         self.solver.set_cell_permeability(K)
         self.solver._assemble(self.dt)
 
-    def _step(self, x_prev, n):
-        """State n from state n - 1 (n = 1..nsteps)."""
+    def _step(self, x_prev, n, guess=None):
+        """State n from state n - 1 (n = 1..nsteps); the solve starts from
+        ``guess`` when given (else from x_prev)."""
         s = self.solver
         s.up_.assign(x_prev)
-        st = s._advance(self.dt, self.t0 + (n - 1) * self.dt)
+        st = s._advance(self.dt, self.t0 + (n - 1) * self.dt, guess)
         self.stats["forward_iterations"].append(st.iterations)
         return s.up.vector().clone()
 
@@ -74,16 +75,24 @@ class MisfitAdjoint:
         return loss.value, d
 
     # --- passes ------------------------------------------------------------------
-    def forward(self, K):
-        """Run the loop with permeability K; returns the loss (checkpoints kept)."""
+    def forward(self, K, guesses=None, keep_states=False):
+        """Run the loop with permeability K; returns the loss (checkpoints kept).
+
+        ``guesses[n]`` (optional) is the initial guess of step n's solve, e.g.
+        the states of a nearby K: the solves then resolve the difference to
+        the solver's relative tolerance (finite differences need that).
+        ``keep_states`` keeps every state in ``self.states``."""
         self._set_K(K)
         self.K = self.solver._K_cells
         x = self.up0.clone()
         self.checkpoints = {0: x.clone()}
+        self.states = [x.clone()] if keep_states else None
         for n in range(1, self.nsteps + 1):
-            x = self._step(x, n)
+            x = self._step(x, n, None if guesses is None else guesses[n])
             if n % self.every == 0 and n < self.nsteps:
                 self.checkpoints[n] = x.clone()
+            if keep_states:
+                self.states.append(x.clone())
         self.x_final = x
         return self.misfit(x, with_grad=False)[0]
 

@@ -231,6 +231,7 @@ struct mpet_ctx {
     double* ox = nullptr;         // outer FP64 vectors
     double* orr = nullptr;
     double* ob = nullptr;
+    unsigned char* l2_flush = nullptr;  // 256 MiB written between autotuner launches
     double* adj_b = nullptr;      // adjoint right-hand side (Dirichlet rows zeroed)
     double* adj_loss = nullptr;   // misfit value (1 double)
     double* partials = nullptr;   // reduction partials

@@ -332,7 +332,7 @@ class MPETSolver:
             self._assemble(dt)
         return self._advance(dt, float(self.problem.time))
 
-    def _advance(self, dt, t0):
+    def _advance(self, dt, t0, guess=None):
         theta = float(self.params["theta"])
         time = self.problem.time
         t_theta = t0 + theta * dt
@@ -344,8 +344,16 @@ class MPETSolver:
         self._set_facet_sources(g_t, t1)
         self._set_bc_values(t1)
         st = _lib.MpetStats()
-        self._ctx.call("mpet_step", float(dt), _lib._ptr(self.up_.vector()), _lib._ptr(self.up.vector()),
-                       ctypes.byref(st))
+        if guess is None:
+            self._ctx.call("mpet_step", float(dt), _lib._ptr(self.up_.vector()), _lib._ptr(self.up.vector()),
+                           ctypes.byref(st))
+        else:
+            # the same step with a caller-chosen initial guess (rhs, then solve from the guess)
+            if getattr(self, "_b", None) is None:
+                self._b = _torch().empty(self.N, dtype=_torch().float64, device=self.device)
+            self._ctx.call("mpet_rhs", float(dt), _lib._ptr(self.up_.vector()), _lib._ptr(self._b))
+            self.up.vector().copy_(guess)
+            self._ctx.call("mpet_solve", _lib._ptr(self._b), _lib._ptr(self.up.vector()), ctypes.byref(st))
         self.solver_monitor["niter"].append(st.iterations)
         self.solver_monitor["relres"].append(st.relres)
         self.last_stats = st.as_dict()
