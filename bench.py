@@ -37,6 +37,14 @@ sys.path.insert(0, ROOT)
 
 METRIC = "MPET steps/s at 64³ A=4, mixed vs FP64 GPU at 1e-8 rel err; SpMV HBM GB/s"
 
+# The system SpMV kernel the autotuner picked, and its DRAM bytes per launch
+# as a multiple of its algorithmic bytes (ncu dram__bytes_read.sum +
+# dram__bytes_write.sum of one launch on the 24^3 A=4 case, scaled by the
+# entries of a launch here; the summaries are under profiles/).
+ROOFLINE_KERNEL = {"csr": "k_spmv_sell<1,8,EpiMinres> (SELL-32)", "node-block": "k_spmv_nb<4,EpiMinres> (node blocks)"}
+TRAFFIC_RATIO = {}
+TRAFFIC_SOURCE = {}
+
 
 def peaks():
     p = os.path.join(ROOT, "MEASURED_PEAKS.json")
@@ -129,6 +137,21 @@ class ClockSampler:
                 "reasons": sorted(reasons), "samples": len(sm)}
 
 
+def spmv_alg_bytes(solver, sv):
+    """Algorithmic bytes of one system SpMV with the chosen variant: every
+    stored nonzero value once, one column id per nonzero (CSR / SELL) or per
+    block (node-block copy), row pointers (CSR), x and y once each."""
+    import ctypes
+    N, nnz = solver.N, solver.nnz
+    ch = ctypes.c_int32()
+    solver.ctx.call("mpet_get_spmv_tuning", None, ctypes.byref(ch))
+    if ch.value == 8:
+        nb = ctypes.c_int64()
+        solver.ctx.call("mpet_get_node_block_info", ctypes.byref(nb), None)
+        return nnz * sv + nb.value * 4 + 2 * N * sv, "node-block"
+    return nnz * (sv + 4) + (N + 1) * 8 + 2 * N * sv, "csr"
+
+
 def time_spmv(solver, torch, lib, reps=20):
     """FP32 and FP64 SpMV with the assembled matrix, CUDA events on the engine's stream."""
     N, nnz = solver.N, solver.nnz
@@ -150,8 +173,9 @@ def time_spmv(solver, torch, lib, reps=20):
         e1.record(stream)
         torch.cuda.synchronize()
         ms = e0.elapsed_time(e1) / reps
-        bytes_ = nnz * (sv + 4) + (N + 1) * 8 + 2 * N * sv
-        out["fp32" if prec == 1 else "fp64"] = {"ms": ms, "alg_bytes": bytes_, "gbs": bytes_ / ms / 1e6}
+        bytes_, layout = spmv_alg_bytes(solver, sv)
+        out["fp32" if prec == 1 else "fp64"] = {"ms": ms, "alg_bytes": bytes_, "gbs": bytes_ / ms / 1e6,
+                                                "layout": layout}
     return out
 
 
@@ -215,11 +239,12 @@ def replica_rate(ms_local, steps):
 
 def spmv_tuning(solver):
     import ctypes
-    ms = np.zeros(6)
+    ms = np.zeros(7)
     ch = ctypes.c_int32()
     solver.ctx.call("mpet_get_spmv_tuning", ms.ctypes.data_as(ctypes.c_void_p), ctypes.byref(ch))
-    names = ["register/4", "register/8", "staged/4", "staged/8", "sell32/4", "sell32/8"]
-    return {"ms": {names[v]: round(float(ms[v]), 4) for v in range(6) if ms[v] > 0}, "chosen": names[ch.value]}
+    names = ["register/4", "register/8", "staged/4", "staged/8", "sell32/4", "sell32/8", "node-block"]
+    return {"ms": {names[v]: round(float(ms[v]), 4) for v in range(7) if ms[v] > 0},
+            "chosen": names[6 if ch.value == 8 else ch.value]}
 
 
 def launches(solver):
@@ -326,6 +351,9 @@ def adjoint_check(args):
     f64 = dict(dtype=torch.float64, device=dev)
     solvers = {p: MPETSolver(problem, dict(dt=dt, T=1e9, theta=1.0, rtol=1e-12, precision=p))
                for p in ("mixed", "fp64")}
+    # finite-difference solves start from the unperturbed state of their step
+    # and reduce that O(h) residual by 1e-6 (far below h itself)
+    solvers["fd"] = MPETSolver(problem, dict(dt=dt, T=1e9, theta=1.0, rtol=1e-6, precision="mixed"))
     zero = torch.zeros(solvers["mixed"].N, **f64)
 
     def driver(p, target):
@@ -360,15 +388,16 @@ def adjoint_check(args):
             g64 = g
     out["rel_diff_mixed_vs_fp64_gradient"] = float(torch.linalg.norm(g_mixed - g64) / torch.linalg.norm(g64))
     # central differences on the mixed path.  Every perturbed solve starts
-    # from the unperturbed state of its step, so the relative tolerance
-    # applies to the O(h) difference and the differences resolve h = 1e-6.
+    # from the unperturbed state of its step (solved to 1e-12), so its
+    # relative tolerance applies to the O(h) difference only.
     rng = np.random.default_rng(2)
     h = 1e-6
     errs = []
-    d_fd = driver("mixed", target)
     Ke = torch.as_tensor(K_eval, **f64)
-    d_fd.forward(Ke, keep_states=True)
-    ref_states = d_fd.states
+    d_ref = driver("mixed", target)
+    d_ref.forward(Ke, keep_states=True)
+    ref_states = d_ref.states
+    d_fd = driver("fd", target)
     t0 = time.perf_counter()
     for _ in range(args.fd_dirs):
         dK = torch.as_tensor(K_eval * rng.standard_normal(K_eval.shape), **f64)
@@ -379,8 +408,9 @@ def adjoint_check(args):
         errs.append(abs(fd - ad) / abs(ad))
     out["central_differences"] = {"directions": args.fd_dirs, "h": h, "max_rel_err": max(errs),
                                   "median_rel_err": statistics.median(errs), "seconds": time.perf_counter() - t0,
-                                  "path": "mixed precision, FP64 refinement to rtol 1e-12, each perturbed "
-                                          "solve started from the unperturbed state"}
+                                  "path": "mixed precision with FP64 refinement; each perturbed solve starts "
+                                          "from the unperturbed state (solved to 1e-12) and reduces the residual "
+                                          "of the perturbation by 1e-6"}
     print(json.dumps(out))
 
 
@@ -556,15 +586,13 @@ def main():
         "iteration_breakdown_ms": dict(split, spmv_fp32=(spmv.get("fp32") or spmv["fp64"])["ms"],
                                        preconditioner=precond_ms),
         "fp64_iteration_breakdown_ms": res.get("fp64", {}).get("iteration_breakdown_ms"),
-        "roofline": {"kernel": "k_spmv<float,1,32,EpiMinres> (FP32 CSR SpMV)" if "fp32" in spmv else "k_spmv<double>",
+        "roofline": {"kernel": ROOFLINE_KERNEL[sp32["layout"]] + (" FP32" if "fp32" in spmv else " FP64"),
                      "bound": "hbm", "achieved": sp32["gbs"], "peak": hbm, "unit": "GB/s",
                      "frac": sp32["gbs"] / hbm, "peak_kind": peak_kind,
                      "alg_bytes_per_launch": sp32["alg_bytes"],
-                     # DRAM read+write bytes of one launch: ncu measured 1.008 x the
-                     # algorithmic bytes on the 24^3 case (55.2e6 entries); scaled by
-                     # the entries of this launch
-                     "traffic": sp32["alg_bytes"] * 1.008,
-                     "traffic_source": "ncu dram__bytes_read+write on the 24^3 case, scaled by nnz"},
+                     "traffic": (sp32["alg_bytes"] * TRAFFIC_RATIO[sp32["layout"]]
+                                 if sp32["layout"] in TRAFFIC_RATIO else None),
+                     "traffic_source": TRAFFIC_SOURCE.get(sp32["layout"])},
         "cpu_baseline": cpu,
         "e2e": {"value": 1e3 / e2e_ms, "unit": "steps/s", "h2d_bytes_per_step": sol.N * 8,
                 "d2h_bytes_per_step": sol.N * 8},

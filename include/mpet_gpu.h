@@ -244,13 +244,19 @@ int mpet_spmv(mpet_ctx* ctx, int32_t precision, const void* x, void* y);
  * replaced by mpet_assemble).  b, if not NULL, is lifted with x_bc. */
 int mpet_apply_symmetric(mpet_ctx* ctx, double* b, const double* x_bc);
 
-/* Set-up autotuning of the system-matrix SpMV: ms per launch of the six
- * variants, indexed by the variant bits (bit 0: 8 instead of 4 entries per
- * lane per batch; bit 1: CSR rows staged in shared memory by bulk copies;
- * bit 2: SELL-32 copy, one thread per row), 0 where not applicable, and the
- * chosen variant (0..5).  No reference counterpart (engine introspection for
+/* Set-up autotuning of the system-matrix SpMV: ms per launch (from a
+ * flushed L2) of the variants 0..5, indexed by the variant bits (bit 0: 8
+ * instead of 4 entries per lane per batch; bit 1: CSR rows staged in shared
+ * memory by bulk copies; bit 2: SELL-32 copy, one thread per row), and in
+ * ms7_host[6] of variant 8 (node-block copy: one column id per 3x3, 3xJ, Jx3
+ * or JxJ block of a P2 node's or vertex's rows), 0 where not applicable; and
+ * the chosen variant.  No reference counterpart (engine introspection for
  * benchmarks). */
-int mpet_get_spmv_tuning(mpet_ctx* ctx, double* ms6_host, int32_t* chosen);
+int mpet_get_spmv_tuning(mpet_ctx* ctx, double* ms7_host, int32_t* chosen);
+
+/* Size of the node-block copy: blocks of the matrix (one column id each) and
+ * stored values including padding.  No reference counterpart. */
+int mpet_get_node_block_info(mpet_ctx* ctx, int64_t* blocks, int64_t* stored_values);
 
 /* Override the autotuned system-matrix SpMV variant (bits as above);
  * MPET_ERR_INVALID if the variant cannot run on this matrix.  Every variant

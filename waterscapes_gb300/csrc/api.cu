@@ -166,6 +166,8 @@ int mpet_setup(mpet_ctx* c, const mpet_params* p) {
     MPET_CUDA(cudaMemsetAsync(c->A.v64, 0, sizeof(double) * c->nnz, c->stream));
     if (c->A.v32) MPET_CUDA(cudaMemsetAsync(c->A.v32, 0, sizeof(float) * c->nnz, c->stream));
     build_sell(c, c->A, c->A.v32 != nullptr, true);
+    build_node_blocks(c);
+    refresh_system_copies(c);
     autotune_system(c);
     MPET_CUDA(cudaStreamSynchronize(c->stream));
     c->setup_done = true;
@@ -222,7 +224,7 @@ int mpet_assemble(mpet_ctx* c, double dt, int32_t apply_bc) {
     require(dt > 0.0, MPET_ERR_INVALID, "dt must be positive");
     launch_assemble_matrix(c, dt, apply_bc != 0, c->A.v32 != nullptr);
     launch_robin_matrix(c, dt);
-    fill_sell(c, c->A);
+    refresh_system_copies(c);
     MPET_CUDA(cudaStreamSynchronize(c->stream));
     c->assembled = true;
     c->asm_dt = dt;
@@ -542,16 +544,16 @@ int mpet_apply_symmetric(mpet_ctx* c, double* b, const double* xbc) {
     require(c->assembled, MPET_ERR_STATE, "mpet_assemble must come first");
     launch_zero_bc_columns(c, b, xbc);
     convert_values_to_f32(c);
-    fill_sell(c, c->A);
+    refresh_system_copies(c);
     MPET_CUDA(cudaStreamSynchronize(c->stream));
     API_END(c)
 }
 
-int mpet_get_spmv_tuning(mpet_ctx* c, double* ms6, int32_t* chosen) {
+int mpet_get_spmv_tuning(mpet_ctx* c, double* ms7, int32_t* chosen) {
     API_BEGIN(c)
     require(c->setup_done, MPET_ERR_STATE, "mpet_setup must come first");
-    if (ms6)
-        for (int v = 0; v < 6; ++v) ms6[v] = c->spmv_variant_ms[v];
+    if (ms7)
+        for (int v = 0; v < 7; ++v) ms7[v] = c->spmv_variant_ms[v];
     if (chosen) *chosen = c->A.variant;
     API_END(c)
 }
@@ -559,7 +561,7 @@ int mpet_get_spmv_tuning(mpet_ctx* c, double* ms6, int32_t* chosen) {
 int mpet_set_hierarchy_spmv_variant(mpet_ctx* c, int32_t variant) {
     API_BEGIN(c)
     require(c->precond_ready, MPET_ERR_STATE, "mpet_setup_preconditioner must come first");
-    require(variant >= 0 && variant <= 5, MPET_ERR_INVALID, "variant out of range");
+    require((variant >= 0 && variant <= 5) || variant == 8, MPET_ERR_INVALID, "variant out of range");
     destroy_minres_graph(c);
     auto set = [&](mpet::Csr& M) { M.variant = spmv_variant_available(M, variant) ? variant : 0; };
     auto hier = [&](mpet::AmgHier& h) {
@@ -571,6 +573,14 @@ int mpet_set_hierarchy_spmv_variant(mpet_ctx* c, int32_t variant) {
     };
     hier(c->amg_u);
     for (int a = 0; a < c->J; ++a) hier(c->amg_p[a]);
+    API_END(c)
+}
+
+int mpet_get_node_block_info(mpet_ctx* c, int64_t* blocks, int64_t* stored_values) {
+    API_BEGIN(c)
+    require(c->setup_done, MPET_ERR_STATE, "mpet_setup must come first");
+    if (blocks) *blocks = c->A_nb.nblocks;
+    if (stored_values) *stored_values = c->A_nb.nvals;
     API_END(c)
 }
 

@@ -62,6 +62,29 @@ struct DevPool {
 
 // CSR with int64 row pointers and int32 column ids; values in FP64 and
 // (optionally) an FP32 copy sharing the same pattern.
+// Node-block copy of the system matrix.  The rows of a P2 node (3
+// displacement rows) and of a vertex (J pressure rows) share their columns,
+// which come in blocks: 3x3 (node-node), 3xJ (node-vertex), Jx3, JxJ.  One
+// column id per block; slices of 32 nodes / vertices store their blocks
+// lane-interleaved (value q of block k of lane l at voff + (k*B + q)*32 + l),
+// padded to the slice's widest row with zero blocks.  Within windows of 2048
+// consecutive nodes (vertices) the lanes take them in order of decreasing
+// row length, so the padding stays small.
+struct NbSlice {
+    int64_t coff, voff;  // first column id / value of the slice
+    int32_t w2, w1;      // blocks per lane with node columns / vertex columns
+};
+struct NodeBlocks {
+    int64_t nsu = 0, nsp = 0;  // node slices (displacement rows), vertex slices (pressure rows)
+    NbSlice* sl = nullptr;     // nsu + nsp
+    int32_t* perm = nullptr;   // (nsu + nsp) * 32: node / vertex of each slice lane, -1 past the end
+    int32_t* cols = nullptr;
+    float* v32 = nullptr;
+    double* v64 = nullptr;
+    int64_t ncols = 0, nvals = 0;  // stored (with padding)
+    int64_t nblocks = 0;           // blocks of the matrix (without padding)
+};
+
 struct Csr {
     int64_t n = 0, m = 0, nnz = 0;
     int64_t* rp = nullptr;
@@ -76,7 +99,7 @@ struct Csr {
     int max_row = 0;  // longest row (entries)
     // SpMV variant: bit 0 = 8 entries per lane per batch (else 4, only with
     // 32 lanes per row, or with the SELL copy), bit 1 = shared-memory staged
-    // (needs tiles), bit 2 = SELL-32 copy (needs s_off)
+    // (needs tiles), bit 2 = SELL-32 copy (needs s_off); 8 = node-block copy
     int variant = 0;
     // SELL-32 copy: slices of 32 rows, column-major within a slice, padded
     // to the slice's longest row with zero values at the row's last column
@@ -87,6 +110,8 @@ struct Csr {
     int32_t* s_ci = nullptr;
     float* s_v32 = nullptr;
     double* s_v64 = nullptr;
+    // node-block copy (system matrix only; variant 8)
+    NodeBlocks* nb = nullptr;
 };
 
 struct AmgLevel {
@@ -179,6 +204,7 @@ struct mpet_ctx {
     // global system
     int64_t N = 0, Nu = 0, nnz = 0;
     mpet::Csr A;                  // rp/ci/v64/v32
+    mpet::NodeBlocks A_nb;        // node-block copy of A
     double* dinv = nullptr;       // |diag|^-1 (1 where 0), FP64
 
     // Dirichlet data
@@ -265,8 +291,7 @@ struct mpet_ctx {
 
     // set by a kernel whose bounded wait gave up (read after each solve)
     int* dev_err = nullptr;
-    // set-up timings (ms) of the six SpMV variants on the system matrix
-    double spmv_variant_ms[6] = {0, 0, 0, 0, 0, 0};
+    double spmv_variant_ms[7] = {0, 0, 0, 0, 0, 0, 0};  // variants 0..5 and 8 (node blocks)
 
     // timing
     cudaEvent_t ev0 = nullptr, ev1 = nullptr;
@@ -353,6 +378,8 @@ int choose_lpr(int64_t n, int64_t nnz);
 void build_tiles(mpet_ctx* c, Csr& A, const int64_t* rp_host);
 void build_sell(mpet_ctx* c, Csr& A, bool fp32, bool with64);
 void fill_sell(mpet_ctx* c, Csr& A);
+void build_node_blocks(mpet_ctx* c);
+void refresh_system_copies(mpet_ctx* c);
 bool spmv_variant_available(const Csr& A, int variant);
 constexpr int SPMV_TILE = 2048;  // entries per staged tile
 void destroy_minres_graph(mpet_ctx* c);

@@ -22,6 +22,8 @@
 // partial per block and a single block sums the partials in a fixed order.
 #include <math.h>
 
+#include <algorithm>
+
 #include "mpet_internal.cuh"
 
 namespace mpet {
@@ -90,6 +92,7 @@ template <typename T, int NV>
 struct EpiStore {
     T* y;
     static constexpr int kRed = 0;
+    static constexpr bool kSystem = NV == 1;  // runs with the node-block system kernel
     struct Pre {};
     __device__ __forceinline__ Pre pre(int64_t) const { return Pre{}; }
     __device__ __forceinline__ void apply(int64_t row, const T* acc, const Pre&, double&, double&) const {
@@ -104,6 +107,7 @@ struct EpiAxpby {
     const T* z;
     T alpha, beta;
     static constexpr int kRed = 0;
+    static constexpr bool kSystem = false;
     struct Pre {
         T zz[NV];
     };
@@ -133,6 +137,7 @@ struct EpiCheb {
     const T* dinv;
     T c1, c2;
     static constexpr int kRed = 0;
+    static constexpr bool kSystem = false;
     struct Pre {
         T bb[NV], dd[NV], xx[NV], di;
     };
@@ -164,6 +169,7 @@ struct EpiMinres {
     const T* v;
     const MinresScalars* sc;
     static constexpr int kRed = 1;
+    static constexpr bool kSystem = true;
     struct Pre {
         T r, v;
     };
@@ -182,6 +188,7 @@ struct EpiResid64 {
     const double* b;
     const double* dinv;
     static constexpr int kRed = 2;
+    static constexpr bool kSystem = true;
     struct Pre {
         double b, di;
     };
@@ -353,6 +360,162 @@ __global__ void k_sell_fill(int64_t n, int64_t nslices, const int64_t* __restric
         } else {
             sci[q] = pad;
             sv[q] = T(0);
+        }
+    }
+}
+
+// ---- node-block SpMV of the system matrix --------------------------------------------
+//
+// One thread owns a P2 node (its 3 displacement rows) or a vertex (its J
+// pressure rows); a warp walks a 32-row-group slice.  Per block it loads one
+// column id and the block's values (each a coalesced 128-byte line across the
+// warp), gathers the 3 displacement or J pressure entries of x and updates
+// its 3 or J accumulators.  JM is a compile-time bound on J (loops unrolled).
+template <typename T, int JM, class Epi>
+__global__ void __launch_bounds__(256) k_spmv_nb(int64_t nnodes, int64_t nv, int64_t Nu, int J, int64_t nsu,
+                                                 int64_t ns, const NbSlice* __restrict__ sl,
+                                                 const int32_t* __restrict__ perm, const int32_t* __restrict__ cols,
+                                                 const T* __restrict__ vals, const T* __restrict__ x, Epi epi,
+                                                 double* partials) {
+    const int lane = threadIdx.x & 31;
+    const int64_t warp = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) >> 5;
+    const int64_t nwarps = ((int64_t)gridDim.x * blockDim.x) >> 5;
+    double r0 = 0.0, r1 = 0.0;
+    for (int64_t s = warp; s < ns; s += nwarps) {
+        const NbSlice S = sl[s];
+        const int32_t* c2 = cols + S.coff + lane;
+        const int32_t* c1 = c2 + (int64_t)S.w2 * 32;
+        const T* v2 = vals + S.voff + lane;
+        const int64_t g = perm[s * 32 + lane];  // node or vertex of this lane, -1 past the end
+        const bool ok = g >= 0;
+        if (s < nsu) {
+            const int64_t node = g;
+            typename Epi::Pre pre[3];
+            if (ok)
+#pragma unroll
+                for (int r = 0; r < 3; ++r) pre[r] = epi.pre(3 * node + r);
+            T acc[3] = {T(0), T(0), T(0)};
+#pragma unroll 2
+            for (int k = 0; k < S.w2; ++k) {
+                const int64_t j = __ldcs(c2 + (int64_t)k * 32);
+                T b[9];
+#pragma unroll
+                for (int q = 0; q < 9; ++q) b[q] = __ldcs(v2 + ((int64_t)k * 9 + q) * 32);
+                const T x0 = x[3 * j], x1 = x[3 * j + 1], x2 = x[3 * j + 2];
+#pragma unroll
+                for (int r = 0; r < 3; ++r) acc[r] += b[3 * r] * x0 + b[3 * r + 1] * x1 + b[3 * r + 2] * x2;
+            }
+            const T* v1 = v2 + (int64_t)S.w2 * 9 * 32;
+            const int B1 = 3 * J;
+            for (int m = 0; m < S.w1; ++m) {
+                const int64_t w = __ldcs(c1 + (int64_t)m * 32);
+#pragma unroll
+                for (int a = 0; a < JM; ++a) {
+                    if (a < J) {
+                        const T xp = x[Nu + (int64_t)a * nv + w];
+#pragma unroll
+                        for (int r = 0; r < 3; ++r) acc[r] += __ldcs(v1 + ((int64_t)m * B1 + r * J + a) * 32) * xp;
+                    }
+                }
+            }
+            if (ok)
+#pragma unroll
+                for (int r = 0; r < 3; ++r) epi.apply(3 * node + r, &acc[r], pre[r], r0, r1);
+        } else {
+            const int64_t v = g;
+            typename Epi::Pre pre[JM];
+#pragma unroll
+            for (int a = 0; a < JM; ++a)
+                if (ok && a < J) pre[a] = epi.pre(Nu + (int64_t)a * nv + v);
+            T acc[JM];
+#pragma unroll
+            for (int a = 0; a < JM; ++a) acc[a] = T(0);
+            const int B2 = 3 * J;
+#pragma unroll 2
+            for (int k = 0; k < S.w2; ++k) {
+                const int64_t j = __ldcs(c2 + (int64_t)k * 32);
+                const T x0 = x[3 * j], x1 = x[3 * j + 1], x2 = x[3 * j + 2];
+#pragma unroll
+                for (int a = 0; a < JM; ++a) {
+                    if (a < J) {
+                        const T* b = v2 + ((int64_t)k * B2 + 3 * a) * 32;
+                        acc[a] += __ldcs(b) * x0 + __ldcs(b + 32) * x1 + __ldcs(b + 64) * x2;
+                    }
+                }
+            }
+            const T* v1 = v2 + (int64_t)S.w2 * B2 * 32;
+            const int B1 = J * J;
+            for (int m = 0; m < S.w1; ++m) {
+                const int64_t w = __ldcs(c1 + (int64_t)m * 32);
+#pragma unroll
+                for (int b = 0; b < JM; ++b) {
+                    if (b < J) {
+                        const T xb = x[Nu + (int64_t)b * nv + w];
+#pragma unroll
+                        for (int a = 0; a < JM; ++a)
+                            if (a < J) acc[a] += __ldcs(v1 + ((int64_t)m * B1 + a * J + b) * 32) * xb;
+                    }
+                }
+            }
+            if (ok)
+#pragma unroll
+                for (int a = 0; a < JM; ++a)
+                    if (a < J) epi.apply(Nu + (int64_t)a * nv + v, &acc[a], pre[a], r0, r1);
+        }
+    }
+    if constexpr (Epi::kRed > 0) {
+        __shared__ double sh[8];
+        double t0 = block_sum256(r0, sh);
+        if (threadIdx.x == 0) partials[blockIdx.x] = t0;
+        if constexpr (Epi::kRed > 1) {
+            double t1 = block_sum256(r1, sh);
+            if (threadIdx.x == 0) partials[NB_RED + blockIdx.x] = t1;
+        }
+    }
+}
+
+// Copies the CSR values into the node-block layout (thread per slice lane).
+// A row group's CSR row holds its node columns (3 per node, n2 order) and
+// then, network-major, its vertex columns (n1 order).
+template <typename T>
+__global__ void k_nb_fill(int64_t nnodes, int64_t nv, int64_t Nu, int J, int64_t nsu, int64_t ns,
+                          const NbSlice* __restrict__ sl, const int32_t* __restrict__ perm,
+                          const int64_t* __restrict__ rp,
+                          const T* __restrict__ v, const int64_t* __restrict__ n2_ptr,
+                          const int32_t* __restrict__ n2_col, const int64_t* __restrict__ n1_ptr,
+                          const int32_t* __restrict__ n1_col, int32_t* cols, T* vals, int write_cols) {
+    const int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    if (t >= ns * 32) return;
+    const int64_t s = t >> 5;
+    const int lane = (int)(t & 31);
+    const NbSlice S = sl[s];
+    const bool urow = s < nsu;
+    const int64_t g = perm[t];  // node or vertex, -1 past the end
+    const bool ok = g >= 0;
+    const int64_t s2 = ok ? n2_ptr[g] : 0, s1 = ok ? n1_ptr[g] : 0;
+    const int d2 = ok ? (int)(n2_ptr[g + 1] - s2) : 0, d1 = ok ? (int)(n1_ptr[g + 1] - s1) : 0;
+    const int R = urow ? 3 : J;                       // rows of the group
+    const int B2 = urow ? 9 : 3 * J, B1 = urow ? 3 * J : J * J;
+    auto row_start = [&](int r) -> int64_t { return urow ? rp[3 * g + r] : rp[Nu + (int64_t)r * nv + g]; };
+    for (int k = 0; k < S.w2; ++k) {
+        const bool real = k < d2;
+        if (write_cols)
+            cols[S.coff + (int64_t)k * 32 + lane] = real ? n2_col[s2 + k] : (d2 > 0 ? n2_col[s2 + d2 - 1] : 0);
+        for (int r = 0; r < R; ++r) {
+            const int64_t e = real ? row_start(r) + 3 * k : 0;
+            for (int cc = 0; cc < 3; ++cc)
+                vals[S.voff + ((int64_t)k * B2 + r * 3 + cc) * 32 + lane] = real ? v[e + cc] : T(0);
+        }
+    }
+    const int64_t c1 = S.coff + (int64_t)S.w2 * 32, v1 = S.voff + (int64_t)S.w2 * B2 * 32;
+    for (int m = 0; m < S.w1; ++m) {
+        const bool real = m < d1;
+        if (write_cols)
+            cols[c1 + (int64_t)m * 32 + lane] = real ? n1_col[s1 + m] : (d1 > 0 ? n1_col[s1 + d1 - 1] : 0);
+        for (int r = 0; r < R; ++r) {
+            const int64_t base = real ? row_start(r) + 3 * d2 + m : 0;
+            for (int b = 0; b < J; ++b)
+                vals[v1 + ((int64_t)m * B1 + r * J + b) * 32 + lane] = real ? v[base + (int64_t)b * d1] : T(0);
         }
     }
 }
@@ -618,6 +781,118 @@ void fill_sell(mpet_ctx* c, Csr& A) {
     MPET_CHECK_LAUNCH();
 }
 
+// Node-block layout of the system matrix: slice widths from the node and
+// vertex adjacency counts (host), values filled on the device.
+void build_node_blocks(mpet_ctx* c) {
+    NodeBlocks& nb = c->A_nb;
+    const int J = c->J;
+    std::vector<int64_t> p2(c->nnodes + 1), p1(c->nnodes + 1);
+    MPET_CUDA(cudaMemcpyAsync(p2.data(), c->n2_ptr, sizeof(int64_t) * p2.size(), cudaMemcpyDeviceToHost, c->stream));
+    MPET_CUDA(cudaMemcpyAsync(p1.data(), c->n1_ptr, sizeof(int64_t) * p1.size(), cudaMemcpyDeviceToHost, c->stream));
+    MPET_CUDA(cudaStreamSynchronize(c->stream));
+    nb.nsu = (c->nnodes + 31) / 32;
+    nb.nsp = (c->nv + 31) / 32;
+    // lanes take the row groups of each window of NB_WINDOW groups in order of
+    // decreasing size (few padded blocks, locality kept within the window)
+    constexpr int64_t NB_WINDOW = 2048;
+    std::vector<int32_t> perm((nb.nsu + nb.nsp) * 32, -1);
+    auto order = [&](int64_t n, int64_t base, int B2, int B1) {
+        std::vector<int32_t> idx;
+        for (int64_t w0 = 0; w0 < n; w0 += NB_WINDOW) {
+            const int64_t w1 = std::min(w0 + NB_WINDOW, n);
+            idx.resize(w1 - w0);
+            for (int64_t g = w0; g < w1; ++g) idx[g - w0] = (int32_t)g;
+            std::stable_sort(idx.begin(), idx.end(), [&](int32_t a, int32_t b) {
+                return (p2[a + 1] - p2[a]) * B2 + (p1[a + 1] - p1[a]) * B1 >
+                       (p2[b + 1] - p2[b]) * B2 + (p1[b + 1] - p1[b]) * B1;
+            });
+            std::copy(idx.begin(), idx.end(), perm.begin() + base + w0);
+        }
+    };
+    order(c->nnodes, 0, 9, 3 * J);
+    order(c->nv, nb.nsu * 32, 3 * J, J * J);
+    std::vector<NbSlice> sl(nb.nsu + nb.nsp);
+    int64_t coff = 0, voff = 0;
+    for (int64_t s = 0; s < nb.nsu + nb.nsp; ++s) {
+        const bool urow = s < nb.nsu;
+        int32_t w2 = 0, w1 = 0;
+        for (int l = 0; l < 32; ++l) {
+            const int32_t g = perm[s * 32 + l];
+            if (g < 0) continue;
+            w2 = std::max<int32_t>(w2, (int32_t)(p2[g + 1] - p2[g]));
+            w1 = std::max<int32_t>(w1, (int32_t)(p1[g + 1] - p1[g]));
+        }
+        sl[s] = NbSlice{coff, voff, w2, w1};
+        coff += (int64_t)(w2 + w1) * 32;
+        voff += (urow ? (int64_t)w2 * 9 + (int64_t)w1 * 3 * J : (int64_t)w2 * 3 * J + (int64_t)w1 * J * J) * 32;
+    }
+    nb.ncols = coff;
+    nb.nvals = voff;
+    nb.nblocks = (p2[c->nnodes] - p2[0]) + (p1[c->nnodes] - p1[0]) + (p2[c->nv] - p2[0]) + (p1[c->nv] - p1[0]);
+    nb.sl = c->pool.alloc<NbSlice>((int64_t)sl.size());
+    nb.perm = c->pool.alloc<int32_t>((int64_t)perm.size());
+    MPET_CUDA(cudaMemcpyAsync(nb.perm, perm.data(), sizeof(int32_t) * perm.size(), cudaMemcpyHostToDevice,
+                              c->stream));
+    nb.cols = c->pool.alloc<int32_t>(coff);
+    if (c->A.v32) nb.v32 = c->pool.alloc<float>(voff);
+    nb.v64 = c->pool.alloc<double>(voff);
+    MPET_CUDA(cudaMemcpyAsync(nb.sl, sl.data(), sizeof(NbSlice) * sl.size(), cudaMemcpyHostToDevice, c->stream));
+    MPET_CUDA(cudaStreamSynchronize(c->stream));
+    c->A.nb = &nb;
+}
+
+static void fill_node_blocks(mpet_ctx* c) {
+    NodeBlocks& nb = c->A_nb;
+    if (!nb.sl) return;
+    const int64_t ns = nb.nsu + nb.nsp;
+    const int G = grid_for(ns * 32, 128);
+    int first = 1;
+    if (nb.v32) {
+        k_nb_fill<float><<<G, 128, 0, c->stream>>>(c->nnodes, c->nv, c->Nu, c->J, nb.nsu, ns, nb.sl, nb.perm,
+                                                   c->A.rp, c->A.v32, c->n2_ptr, c->n2_col, c->n1_ptr, c->n1_col,
+                                                   nb.cols, nb.v32, first);
+        first = 0;
+    }
+    k_nb_fill<double><<<G, 128, 0, c->stream>>>(c->nnodes, c->nv, c->Nu, c->J, nb.nsu, ns, nb.sl, nb.perm,
+                                                c->A.rp, c->A.v64, c->n2_ptr, c->n2_col, c->n1_ptr, c->n1_col,
+                                                nb.cols, nb.v64, first);
+    MPET_CHECK_LAUNCH();
+}
+
+// After every change of the system matrix values: its SELL and node-block copies.
+void refresh_system_copies(mpet_ctx* c) {
+    fill_sell(c, c->A);
+    fill_node_blocks(c);
+}
+
+template <typename T>
+static const T* nb_vals(const NodeBlocks& nb);
+template <>
+const double* nb_vals<double>(const NodeBlocks& nb) { return nb.v64; }
+template <>
+const float* nb_vals<float>(const NodeBlocks& nb) { return nb.v32; }
+
+template <typename T, class Epi>
+static void launch_nb(mpet_ctx* c, const NodeBlocks& nb, const T* x, const Epi& epi) {
+    const int64_t ns = nb.nsu + nb.nsp;
+    int blocks = Epi::kRed > 0 ? NB_RED : grid_for(ns * 32, 256);
+    if (Epi::kRed == 0 && blocks > 152 * 16) blocks = 152 * 16;
+    const int J = c->J;
+    cudaStream_t st = c->stream;
+    const T* v = nb_vals<T>(nb);
+    if (J <= 2)
+        k_spmv_nb<T, 2, Epi><<<blocks, 256, 0, st>>>(c->nnodes, c->nv, c->Nu, J, nb.nsu, ns, nb.sl, nb.perm,
+                                                     nb.cols, v, x, epi, c->partials);
+    else if (J <= 4)
+        k_spmv_nb<T, 4, Epi><<<blocks, 256, 0, st>>>(c->nnodes, c->nv, c->Nu, J, nb.nsu, ns, nb.sl, nb.perm,
+                                                     nb.cols, v, x, epi, c->partials);
+    else
+        k_spmv_nb<T, 8, Epi><<<blocks, 256, 0, st>>>(c->nnodes, c->nv, c->Nu, J, nb.nsu, ns, nb.sl, nb.perm,
+                                                     nb.cols, v, x, epi, c->partials);
+    MPET_CHECK_LAUNCH();
+    c->n_launch++;
+}
+
 template <typename T>
 static const T* sell_vals(const Csr& A);
 template <>
@@ -627,6 +902,12 @@ const float* sell_vals<float>(const Csr& A) { return A.s_v32; }
 
 template <typename T, int NV, class Epi>
 static void launch_spmv(mpet_ctx* c, const Csr& A, const T* va, const T* x, const Epi& epi) {
+    if constexpr (NV == 1 && Epi::kSystem) {
+        if (A.variant == 8 && A.nb && nb_vals<T>(*A.nb) && va == vals<T>(A)) {
+            launch_nb<T>(c, *A.nb, x, epi);
+            return;
+        }
+    }
     if ((A.variant & 4) && sell_vals<T>(A) && va == vals<T>(A)) {
         int blocks = Epi::kRed > 0 ? NB_RED : grid_for(A.nslices * 32, 256);
         if (Epi::kRed == 0 && blocks > 152 * 16) blocks = 152 * 16;
@@ -688,6 +969,7 @@ const float* dinv_of<float>(const AmgLevel& L) { return L.dinv32; }
 // per row: staged needs row tiles, SELL its copy, 8 entries per lane (CSR)
 // 32 lanes per row.
 bool spmv_variant_available(const Csr& A, int v) {
+    if (v == 8) return A.nb != nullptr;
     if (v < 0 || v > 5) return false;
     if (v & 4) return A.s_off != nullptr && !(v & 2);
     if ((v & 2) && A.ntiles == 0) return false;
@@ -713,8 +995,9 @@ static void autotune_matrix(mpet_ctx* c, Csr& A, const T* x, const Epi& epi, dou
     for (int lpr : {lpr0, lpr0 / 2, lpr0 * 2}) {
         if ((lpr < 4 || lpr > 32) && lpr != lpr0) continue;
         A.lpr = lpr;
-        for (int v = 0; v < 6; ++v) {
-            if (!spmv_variant_available(A, v) || (v >= 4 && (!sell_vals<T>(A) || lpr != lpr0))) continue;
+        for (int v : {0, 1, 2, 3, 4, 5, 8}) {
+            if (!spmv_variant_available(A, v) || (v >= 4 && v < 8 && (!sell_vals<T>(A) || lpr != lpr0))) continue;
+            if (v == 8 && (!Epi::kSystem || NV != 1 || !nb_vals<T>(*A.nb) || lpr != lpr0)) continue;
             A.variant = v;
             launch_spmv<T, NV>(c, A, vals<T>(A), x, epi);
             float ms = 0.f;
@@ -729,7 +1012,7 @@ static void autotune_matrix(mpet_ctx* c, Csr& A, const T* x, const Epi& epi, dou
                 ms += one;
             }
             ms /= 5.f;
-            if (ms_out && lpr == lpr0) ms_out[v] = ms;
+            if (ms_out && lpr == lpr0) ms_out[v == 8 ? 6 : v] = ms;
             if (ms < best) {
                 best = ms;
                 best_v = v;
