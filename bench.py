@@ -415,6 +415,100 @@ def adjoint_check(args):
     print(json.dumps(out))
 
 
+def batch_problems(count, n_lo, n_hi, seed=0):
+    """Independent A=2 instances: Kuhn cubes n^3 x 6 with n uniform in
+    [n_lo, n_hi], K_a in log-uniform[1e-5, 1e-1], c_a in log-uniform[1e-5, 1e-3],
+    S12 in log-uniform[1e-3, 1] (seeded); mu = 1e3, lambda = 1e4, alpha = 0.5;
+    u = 0 and p_a = sin(2 pi t) x0 (a + 1) on the boundary."""
+    from waterscapes_gb300 import (CompiledSubDomain, Constant, Expression, MPETProblem, UnitCubeMesh,
+                                   convert_to_E_nu)
+    rng = np.random.default_rng(seed)
+    E, nu = convert_to_E_nu(1.0e3, 1.0e4)
+    lu = lambda lo, hi: 10.0 ** rng.uniform(np.log10(lo), np.log10(hi))  # noqa: E731
+    out = []
+    for _ in range(count):
+        n = int(rng.integers(n_lo, n_hi + 1))
+        K = (lu(1e-5, 1e-1), lu(1e-5, 1e-1))
+        c = (lu(1e-5, 1e-3), lu(1e-5, 1e-3))
+        s12 = lu(1e-3, 1.0)
+        p = MPETProblem(UnitCubeMesh(n), Constant(0.0),
+                        params=dict(J=2, E=E, nu=nu, alpha=(0.5, 0.5), c=c, K=K, S=((0.0, s12), (s12, 0.0))))
+        CompiledSubDomain.on_boundary().mark(p.momentum_boundary_markers, 0)
+        for a in range(2):
+            CompiledSubDomain.on_boundary().mark(p.continuity_boundary_markers[a], 0)
+        p.p_bar = [Expression((lambda a: (lambda x, t: math.sin(2 * math.pi * t) * x[:, 0] * (a + 1)))(a))
+                   for a in range(2)]
+        out.append(p)
+    return out
+
+
+def batch_run(args):
+    """Many independent instances advanced together (one launch per kernel for
+    all of them): instance-steps/s of the mixed path over --steps steps of
+    dt = 0.02 after --warmup steps, each instance converged to 1e-10 on its
+    own; the final states of a few instances are checked against the same
+    instances solved alone on the FP64 path.  Prints one JSON line."""
+    import torch
+    from waterscapes_gb300 import MPETBatchSolver, MPETSolver
+    dt = 0.02
+    t0 = time.perf_counter()
+    problems = batch_problems(args.instances, args.n_min, args.n_max)
+    t_mesh = time.perf_counter() - t0
+    nsteps = args.warmup + args.steps
+    params = dict(dt=dt, T=nsteps * dt, theta=1.0, rtol=1e-10, precision="mixed")
+    t0 = time.perf_counter()
+    bs = MPETBatchSolver(problems, params)
+    torch.cuda.synchronize()
+    t_setup = time.perf_counter() - t0
+    t0 = time.perf_counter()
+    bs._assemble(dt)
+    torch.cuda.synchronize()
+    t_asm = time.perf_counter() - t0
+    gen = bs.solve_direct()
+    for _ in range(args.warmup):
+        next(gen)
+    torch.cuda.synchronize()
+    worst = 0.0
+    e0 = torch.cuda.Event(enable_timing=True)
+    e1 = torch.cuda.Event(enable_timing=True)
+    its0 = len(bs.solver_monitor["niter"])
+    e0.record(bs._stream)
+    for _ in range(args.steps):
+        next(gen)
+        worst = max(worst, float(bs.batch_relres().max()))
+    e1.record(bs._stream)
+    torch.cuda.synchronize()
+    ms = e0.elapsed_time(e1)
+    its = bs.solver_monitor["niter"][its0:]
+    # a few instances solved alone on the FP64 path
+    check = sorted(set(np.linspace(0, bs.ninst - 1, min(4, bs.ninst)).astype(int).tolist()))
+    errs = []
+    finals = {i: bs.instance_vector(i).clone() for i in check}
+    del gen
+    for i in check:
+        p = problems[i]
+        p.time.assign(0.0)
+        s = MPETSolver(p, dict(params, precision="fp64"))
+        for up, t in s.solve_direct():
+            pass
+        ref = up.vector()
+        errs.append(float(torch.linalg.norm(finals[i] - ref) / torch.linalg.norm(ref)))
+        del s
+    sizes = [p.mesh.num_cells() // 6 for p in problems]
+    out = {"metric": "batched MPET instance-steps/s (A=2 instances in one union mesh)",
+           "value": bs.ninst * args.steps / (ms / 1e3), "unit": "instance-steps/s",
+           "ms_per_step": ms / args.steps, "steps": args.steps, "warmup": args.warmup,
+           "config": {"workload": "%d Kuhn cubes n^3 x 6 tets, n in [%d, %d] (seeded), A=2, dt=0.02"
+                      % (bs.ninst, args.n_min, args.n_max), "N": bs.N, "nnz": bs.nnz,
+                      "cells": int(sum(p.mesh.num_cells() for p in problems)),
+                      "n_mean": float(np.mean(sizes) ** (1 / 3.0))},
+           "iterations_per_step": its, "worst_instance_relres": worst,
+           "fp64_single_instance_check": {"instances": check, "rel_err": errs},
+           "setup_s": {"meshes": t_mesh, "union_and_pattern": t_setup, "assemble_plus_amg": t_asm},
+           "spmv_tuning": spmv_tuning(bs)}
+    print(json.dumps(out))
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -433,7 +527,14 @@ def main():
     ap.add_argument("--adjoint", action="store_true",
                     help="discrete-adjoint gradient check (A=2 on the --n cube, 20 steps) instead of the bench")
     ap.add_argument("--fd-dirs", type=int, default=64)
+    ap.add_argument("--batch", action="store_true",
+                    help="batch of independent A=2 instances (--instances, n in [--n-min, --n-max]) instead of the bench")
+    ap.add_argument("--instances", type=int, default=256)
+    ap.add_argument("--n-min", type=int, default=8)
+    ap.add_argument("--n-max", type=int, default=32)
     args = ap.parse_args()
+    if args.batch:
+        return batch_run(args)
     if args.profile:
         return profile_case(args)
     if args.adjoint:
