@@ -73,6 +73,8 @@ int mpet_ctx_destroy(mpet_ctx* c) {
     c->pool.free_all();
     if (c->sc_host) cudaFreeHost(c->sc_host);
     if (c->inst_host) cudaFreeHost(c->inst_host);
+    if (c->bsc_host) cudaFreeHost(c->bsc_host);
+    if (c->bdone_host) cudaFreeHost(c->bdone_host);
     if (c->ev0) cudaEventDestroy(c->ev0);
     if (c->ev1) cudaEventDestroy(c->ev1);
     for (cudaEvent_t e : {c->ev_in0, c->ev_in1, c->ev_sv0, c->ev_sv1})

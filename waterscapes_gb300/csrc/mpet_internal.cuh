@@ -288,6 +288,15 @@ struct mpet_ctx {
     double* ch_part = nullptr;
     double* inst_v = nullptr;
     double* inst_host = nullptr;  // pinned
+    // batched MINRES: scalars, done flags and inner targets per instance
+    mpet::MinresScalars* bsc = nullptr;
+    mpet::MinresScalars* bsc_host = nullptr;  // pinned
+    double* bdone = nullptr;
+    double* bdone_host = nullptr;             // pinned
+    double* btarget = nullptr;
+    double* bval = nullptr;                   // per-instance reduced sums
+    cudaGraphExec_t bmr_graph = nullptr;
+    int64_t bmr_graph_launches = 0;
 
     // set by a kernel whose bounded wait gave up (read after each solve)
     int* dev_err = nullptr;

@@ -1131,76 +1131,83 @@ __global__ void k_mr_update(int64_t n, const T* __restrict__ v, const T* __restr
     d[i] += ph * wn;
 }
 
+// One MINRES scalar step (Paige-Saunders recurrences) on the reduced sums.
+__device__ void mr_init_one(MinresScalars* s, double t) {
+    bool bad = !(t >= 0.0) || isnan(t);
+    double b1 = bad ? 0.0 : sqrt(t);
+    s->beta1 = b1;
+    s->beta = b1;
+    s->oldb = 0.0;
+    s->dbar = 0.0;
+    s->epsln = 0.0;
+    s->phibar = b1;
+    s->cs = -1.0;
+    s->sn = 0.0;
+    s->c_r1 = 0.0;
+    s->c_r2 = 0.0;
+    s->inv_beta = b1 > 0.0 ? 1.0 / b1 : 0.0;
+    s->rel = 1.0;
+    s->flag = bad ? 1.0 : 0.0;
+}
+
+__device__ void mr_alfa_one(MinresScalars* s, double t) {
+    s->alfa = t;
+    s->c_r2 = t * s->inv_beta;
+}
+
+__device__ void mr_beta_one(MinresScalars* s, double t) {
+    if (!(t >= 0.0) || isnan(t)) {
+        s->flag = 1.0;
+        t = 0.0;
+    }
+    const double oldb = s->beta;
+    const double beta = sqrt(t);
+    const double oldeps = s->epsln;
+    const double delta = s->cs * s->dbar + s->sn * s->alfa;
+    const double gbar = s->sn * s->dbar - s->cs * s->alfa;
+    const double epsln = s->sn * beta;
+    const double dbar = -s->cs * beta;
+    double gamma = hypot(gbar, beta);
+    if (gamma < 1e-300) gamma = 1e-300;
+    const double cs = gbar / gamma, sn = beta / gamma;
+    const double phi = cs * s->phibar;
+    const double phibar = sn * s->phibar;
+    s->oldb = oldb;
+    s->beta = beta;
+    s->oldeps = oldeps;
+    s->delta = delta;
+    s->gbar = gbar;
+    s->epsln = epsln;
+    s->dbar = dbar;
+    s->gamma = gamma;
+    s->cs = cs;
+    s->sn = sn;
+    s->phi = phi;
+    s->phibar = phibar;
+    s->inv_gamma = 1.0 / gamma;
+    s->inv_beta = beta > 0.0 ? 1.0 / beta : 0.0;
+    s->c_r1 = oldb > 0.0 ? beta / oldb : 0.0;
+    s->rel = s->beta1 > 0.0 ? phibar / s->beta1 : 0.0;
+    if (beta == 0.0 && phibar > 0.0) s->flag = 1.0;
+}
+
 __global__ void k_mr_init(MinresScalars* s, const double* partials) {
     __shared__ double sh[8];
     double t = sum_partials(partials, sh);
-    if (threadIdx.x == 0) {
-        bool bad = !(t >= 0.0) || isnan(t);
-        double b1 = bad ? 0.0 : sqrt(t);
-        s->beta1 = b1;
-        s->beta = b1;
-        s->oldb = 0.0;
-        s->dbar = 0.0;
-        s->epsln = 0.0;
-        s->phibar = b1;
-        s->cs = -1.0;
-        s->sn = 0.0;
-        s->c_r1 = 0.0;
-        s->c_r2 = 0.0;
-        s->inv_beta = b1 > 0.0 ? 1.0 / b1 : 0.0;
-        s->rel = 1.0;
-        s->flag = bad ? 1.0 : 0.0;
-    }
+    if (threadIdx.x == 0) mr_init_one(s, t);
 }
-
 __global__ void k_mr_alfa(MinresScalars* s, const double* partials) {
     __shared__ double sh[8];
     double t = sum_partials(partials, sh);
-    if (threadIdx.x == 0) {
-        s->alfa = t;
-        s->c_r2 = t * s->inv_beta;
-    }
+    if (threadIdx.x == 0) mr_alfa_one(s, t);
 }
-
 __global__ void k_mr_beta(MinresScalars* s, const double* partials) {
     __shared__ double sh[8];
     double t = sum_partials(partials, sh);
-    if (threadIdx.x == 0) {
-        if (!(t >= 0.0) || isnan(t)) {
-            s->flag = 1.0;
-            t = 0.0;
-        }
-        const double oldb = s->beta;
-        const double beta = sqrt(t);
-        const double oldeps = s->epsln;
-        const double delta = s->cs * s->dbar + s->sn * s->alfa;
-        const double gbar = s->sn * s->dbar - s->cs * s->alfa;
-        const double epsln = s->sn * beta;
-        const double dbar = -s->cs * beta;
-        double gamma = hypot(gbar, beta);
-        if (gamma < 1e-300) gamma = 1e-300;
-        const double cs = gbar / gamma, sn = beta / gamma;
-        const double phi = cs * s->phibar;
-        const double phibar = sn * s->phibar;
-        s->oldb = oldb;
-        s->beta = beta;
-        s->oldeps = oldeps;
-        s->delta = delta;
-        s->gbar = gbar;
-        s->epsln = epsln;
-        s->dbar = dbar;
-        s->gamma = gamma;
-        s->cs = cs;
-        s->sn = sn;
-        s->phi = phi;
-        s->phibar = phibar;
-        s->inv_gamma = 1.0 / gamma;
-        s->inv_beta = beta > 0.0 ? 1.0 / beta : 0.0;
-        s->c_r1 = oldb > 0.0 ? beta / oldb : 0.0;
-        s->rel = s->beta1 > 0.0 ? phibar / s->beta1 : 0.0;
-        if (beta == 0.0 && phibar > 0.0) s->flag = 1.0;
-    }
+    if (threadIdx.x == 0) mr_beta_one(s, t);
 }
+
+
 
 __global__ void k_outer_norms(MinresScalars* s, const double* partials) {
     __shared__ double sh[8];
@@ -1381,8 +1388,9 @@ static void minres_three(mpet_ctx* c) {
     }
 }
 
-template <typename T>
-static void capture_minres_graph(mpet_ctx* c) {
+// Captures body(c) (issued on c->stream) into an executable graph.
+template <class F>
+static void capture_graph(mpet_ctx* c, F body, cudaGraphExec_t* out, int64_t* launches, const char* what) {
     if (!c->cap_stream) MPET_CUDA(cudaStreamCreateWithFlags(&c->cap_stream, cudaStreamNonBlocking));
     cudaStream_t saved = c->stream;
     const int64_t l0 = c->n_launch, s0 = c->n_spmv;
@@ -1391,7 +1399,7 @@ static void capture_minres_graph(mpet_ctx* c) {
     cudaError_t e = cudaStreamBeginCapture(c->cap_stream, cudaStreamCaptureModeThreadLocal);
     if (e == cudaSuccess) {
         try {
-            minres_three<T>(c);
+            body(c);
         } catch (...) {
             cudaStreamEndCapture(c->cap_stream, &g);
             if (g) cudaGraphDestroy(g);
@@ -1401,21 +1409,28 @@ static void capture_minres_graph(mpet_ctx* c) {
         e = cudaStreamEndCapture(c->cap_stream, &g);
     }
     c->stream = saved;
-    c->mr_graph_launches = c->n_launch - l0;
+    *launches = c->n_launch - l0;
     c->n_launch = l0;
     c->n_spmv = s0;
-    if (e != cudaSuccess) fail(MPET_ERR_CUDA, std::string("MINRES graph capture: ") + cudaGetErrorString(e));
-    e = cudaGraphInstantiate(&c->mr_graph, g, 0);
+    if (e != cudaSuccess) fail(MPET_ERR_CUDA, std::string(what) + " graph capture: " + cudaGetErrorString(e));
+    e = cudaGraphInstantiate(out, g, 0);
     cudaGraphDestroy(g);
     if (e != cudaSuccess) {
-        c->mr_graph = nullptr;
-        fail(MPET_ERR_CUDA, std::string("MINRES graph instantiate: ") + cudaGetErrorString(e));
+        *out = nullptr;
+        fail(MPET_ERR_CUDA, std::string(what) + " graph instantiate: " + cudaGetErrorString(e));
     }
+}
+
+template <typename T>
+static void capture_minres_graph(mpet_ctx* c) {
+    capture_graph(c, [](mpet_ctx* cc) { minres_three<T>(cc); }, &c->mr_graph, &c->mr_graph_launches, "MINRES");
 }
 
 void destroy_minres_graph(mpet_ctx* c) {
     if (c->mr_graph) cudaGraphExecDestroy(c->mr_graph);
     c->mr_graph = nullptr;
+    if (c->bmr_graph) cudaGraphExecDestroy(c->bmr_graph);
+    c->bmr_graph = nullptr;
 }
 
 template <typename T>
@@ -1551,13 +1566,10 @@ void residual_norms(mpet_ctx* c, const double* b, const double* x, double* r, do
 //
 // A batch is one mesh made of disjoint instance meshes, so the system and the
 // AMG hierarchies are block diagonal and every kernel above runs all
-// instances at once.  Only the refinement loop is per instance: the DOFs are
-// cut into chunks of at most BATCH_CHUNK rows of one instance; per-chunk
-// partial sums (one block each) are added per instance in chunk order, so
-// the per-instance norms are deterministic.  Each sweep scales every
-// unconverged instance's residual to a unit preconditioned norm (converged
-// instances to zero), runs one MINRES on the union, and adds each instance's
-// correction back with its own scale.
+// instances at once.  The Krylov scalars and the refinement loop are per
+// instance: the DOFs are cut into chunks of at most BATCH_CHUNK rows of one
+// instance; per-chunk partial sums (one block each) are added per instance
+// in chunk order, so every per-instance dot and norm is deterministic.
 
 template <typename T>
 __global__ void k_seg_dot(const int64_t* __restrict__ lo, const int32_t* __restrict__ len, int64_t nch,
@@ -1659,7 +1671,183 @@ __global__ void k_batch_status(int ninst, double* iv, double rtol, int first) {
     iv[BV_ETA * ninst + i] = eta;
     iv[BV_DONE * ninst + i] = done ? 1.0 : 0.0;
     iv[BV_SIN * ninst + i] = done ? 0.0 : 1.0 / beta;
-    iv[BV_SOUT * ninst + i] = done ? 0.0 : eta;
+    iv[BV_SOUT * ninst + i] = done ? 0.0 : nr;
+}
+
+// ---- batched MINRES: one Krylov recurrence per instance -------------------------------
+//
+// The vectors hold all instances; every scalar (alpha, beta, the Givens
+// rotation) is per instance, and the dots are per-instance chunk sums.  An
+// instance that reaches its target is frozen: its scalars are zeroed at the
+// start of the next iteration, so its Lanczos vectors and its correction
+// stop changing while the others continue.
+
+template <typename T>
+__global__ void k_bmr_v(const int64_t* __restrict__ lo, const int32_t* __restrict__ len,
+                        const int32_t* __restrict__ inst, const T* __restrict__ y, T* v,
+                        const MinresScalars* __restrict__ sc) {
+    const int64_t ch = blockIdx.x;
+    const T ib = (T)sc[inst[ch]].inv_beta;
+    for (int i = threadIdx.x; i < len[ch]; i += 256) v[lo[ch] + i] = y[lo[ch] + i] * ib;
+}
+
+// y -= c_r1 r1 and the chunk sums of v . y
+template <typename T>
+__global__ void k_bmr_axpy_dot(const int64_t* __restrict__ lo, const int32_t* __restrict__ len,
+                               const int32_t* __restrict__ inst, T* y, const T* __restrict__ r1,
+                               const T* __restrict__ v, const MinresScalars* __restrict__ sc, double* part) {
+    __shared__ double sh[8];
+    const int64_t ch = blockIdx.x;
+    const T c1 = (T)sc[inst[ch]].c_r1;
+    double s = 0.0;
+    for (int i = threadIdx.x; i < len[ch]; i += 256) {
+        const int64_t r = lo[ch] + i;
+        const T yy = y[r] - c1 * r1[r];
+        y[r] = yy;
+        s += (double)v[r] * (double)yy;
+    }
+    s = block_sum256(s, sh);
+    if (threadIdx.x == 0) part[ch] = s;
+}
+
+template <typename T>
+__global__ void k_bmr_axpy(const int64_t* __restrict__ lo, const int32_t* __restrict__ len,
+                           const int32_t* __restrict__ inst, T* y, const T* __restrict__ r2,
+                           const MinresScalars* __restrict__ sc) {
+    const int64_t ch = blockIdx.x;
+    const T c2 = (T)sc[inst[ch]].c_r2;
+    for (int i = threadIdx.x; i < len[ch]; i += 256) y[lo[ch] + i] -= c2 * r2[lo[ch] + i];
+}
+
+template <typename T>
+__global__ void k_bmr_update(const int64_t* __restrict__ lo, const int32_t* __restrict__ len,
+                             const int32_t* __restrict__ inst, const T* __restrict__ v, const T* __restrict__ w1,
+                             const T* __restrict__ w2, T* w, T* d, const MinresScalars* __restrict__ sc) {
+    const int64_t ch = blockIdx.x;
+    const MinresScalars& s = sc[inst[ch]];
+    const T oe = (T)s.oldeps, de = (T)s.delta, ig = (T)s.inv_gamma, ph = (T)s.phi;
+    for (int i = threadIdx.x; i < len[ch]; i += 256) {
+        const int64_t r = lo[ch] + i;
+        const T wn = (v[r] - oe * w1[r] - de * w2[r]) * ig;
+        w[r] = wn;
+        d[r] += ph * wn;
+    }
+}
+
+__device__ void mr_freeze(MinresScalars* s) {
+    s->inv_beta = 0.0;
+    s->c_r1 = 0.0;
+    s->c_r2 = 0.0;
+    s->phi = 0.0;
+    s->inv_gamma = 0.0;
+    s->oldeps = 0.0;
+    s->delta = 0.0;
+    s->alfa = 0.0;
+}
+
+// start: q_i = rhs_i . M^-1 rhs_i; instances with active_i == 0 start frozen
+__global__ void k_bmr_init(int ni, MinresScalars* sc, const double* q, const double* outer_done, double* done) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= ni) return;
+    const bool on = outer_done[i] == 0.0;
+    mr_init_one(&sc[i], on ? q[i] : 0.0);
+    if (!on) {
+        mr_freeze(&sc[i]);
+        sc[i].rel = 0.0;
+    }
+    done[i] = on ? 0.0 : 1.0;
+}
+
+__global__ void k_bmr_freeze(int ni, MinresScalars* sc, const double* done) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < ni && done[i] != 0.0) mr_freeze(&sc[i]);
+}
+
+__global__ void k_bmr_alfa(int ni, MinresScalars* sc, const double* t, const double* done) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < ni && done[i] == 0.0) mr_alfa_one(&sc[i], t[i]);
+}
+
+__global__ void k_bmr_beta(int ni, MinresScalars* sc, const double* t, const double* target, double* done) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= ni || done[i] != 0.0) return;
+    mr_beta_one(&sc[i], t[i]);
+    if (sc[i].rel <= target[i] || sc[i].flag != 0.0) done[i] = 1.0;
+}
+
+template <typename T>
+static void bminres_three(mpet_ctx* c) {
+    const int ni = c->ninst;
+    const int64_t nch = c->nchunks;
+    const int gi = grid_for(ni, 128);
+    T* v = (T*)c->kv;
+    T* d = (T*)c->kd;
+    int ir1 = 0, ir2 = 1, iy = 2;
+    int iw = 0, iw1 = 1, iw2 = 2;
+    for (int q = 0; q < 3; ++q) {
+        T* r1 = (T*)c->kr[ir1];
+        T* r2 = (T*)c->kr[ir2];
+        T* y = (T*)c->kr[iy];
+        k_bmr_freeze<<<gi, 128, 0, c->stream>>>(ni, c->bsc, c->bdone);
+        k_bmr_v<T><<<(unsigned)nch, 256, 0, c->stream>>>(c->ch_lo, c->ch_len, c->ch_inst, y, v, c->bsc);
+        MPET_CHECK_LAUNCH();
+        launch_spmv<T, 1>(c, c->A, vals<T>(c->A), v, EpiStore<T, 1>{y});
+        c->n_spmv++;
+        k_bmr_axpy_dot<T><<<(unsigned)nch, 256, 0, c->stream>>>(c->ch_lo, c->ch_len, c->ch_inst, y, r1, v, c->bsc,
+                                                                 c->ch_part);
+        k_seg_finish<<<gi, 128, 0, c->stream>>>(ni, c->inst_cptr, c->inst_chunks, c->ch_part, nch, 1, c->bval);
+        k_bmr_alfa<<<gi, 128, 0, c->stream>>>(ni, c->bsc, c->bval, c->bdone);
+        k_bmr_axpy<T><<<(unsigned)nch, 256, 0, c->stream>>>(c->ch_lo, c->ch_len, c->ch_inst, y, r2, c->bsc);
+        MPET_CHECK_LAUNCH();
+        c->n_launch += 6;
+        const int old1 = ir1;
+        ir1 = ir2;
+        ir2 = iy;
+        iy = old1;
+        precond<T>(c, (const T*)c->kr[ir2], (T*)c->kr[iy]);
+        k_seg_dot<T><<<(unsigned)nch, 256, 0, c->stream>>>(c->ch_lo, c->ch_len, nch, (const T*)c->kr[ir2],
+                                                           (const T*)c->kr[iy], c->ch_part);
+        k_seg_finish<<<gi, 128, 0, c->stream>>>(ni, c->inst_cptr, c->inst_chunks, c->ch_part, nch, 1, c->bval);
+        k_bmr_beta<<<gi, 128, 0, c->stream>>>(ni, c->bsc, c->bval, c->btarget, c->bdone);
+        const int oldw1 = iw1;
+        iw1 = iw2;
+        iw2 = iw;
+        iw = oldw1;
+        k_bmr_update<T><<<(unsigned)nch, 256, 0, c->stream>>>(c->ch_lo, c->ch_len, c->ch_inst, v,
+                                                              (const T*)c->kw[iw1], (const T*)c->kw[iw2],
+                                                              (T*)c->kw[iw], d, c->bsc);
+        MPET_CHECK_LAUNCH();
+        c->n_launch += 4;
+    }
+}
+
+// Replays the 3-iteration batched graph until every instance is done.
+template <typename T>
+static int bminres_run(mpet_ctx* c, int max_iters, int* iters_done) {
+    if (!c->bmr_graph)
+        capture_graph(c, [](mpet_ctx* cc) { bminres_three<T>(cc); }, &c->bmr_graph, &c->bmr_graph_launches,
+                      "batched MINRES");
+    const int ni = c->ninst;
+    int it = 0;
+    int status = MPET_OK;
+    while (it < max_iters) {
+        MPET_CUDA(cudaGraphLaunch(c->bmr_graph, c->stream));
+        it += 3;
+        c->n_launch += c->bmr_graph_launches;
+        c->n_spmv += 3;
+        MPET_CUDA(cudaMemcpyAsync(c->bdone_host, c->bdone, sizeof(double) * ni, cudaMemcpyDeviceToHost, c->stream));
+        MPET_CUDA(cudaMemcpyAsync(c->bsc_host, c->bsc, sizeof(MinresScalars) * ni, cudaMemcpyDeviceToHost,
+                                  c->stream));
+        MPET_CUDA(cudaStreamSynchronize(c->stream));
+        bool all = true;
+        for (int i = 0; i < ni; ++i) {
+            if (c->bsc_host[i].flag != 0.0) status = MPET_ERR_BREAKDOWN;
+            all = all && c->bdone_host[i] != 0.0;
+        }
+        if (status != MPET_OK || all) break;
+    }
+    *iters_done = it;
+    return status;
 }
 
 template <typename T>
@@ -1680,6 +1868,7 @@ static int solve_batch(mpet_ctx* c, const double* b, double* x, mpet_stats* st, 
     const int maxit = c->prm.maxit > 0 ? c->prm.maxit : 5000;
     T* rhs = (T*)c->kr[0];
     T* y = (T*)c->kr[2];
+    std::vector<double> target(ni);
     for (outer = 0; outer < max_outer; ++outer) {
         launch_spmv<double, 1>(c, c->A, c->A.v64, x, EpiResid64{c->orr, b, c->dinv});
         c->n_spmv++;
@@ -1701,7 +1890,7 @@ static int solve_batch(mpet_ctx* c, const double* b, double* x, mpet_stats* st, 
         MPET_CUDA(cudaStreamSynchronize(c->stream));
         const double* h = c->inst_host;
         int active = 0;
-        double worst = 0.0, worst_true = 0.0, need = 1.0;
+        double worst = 0.0, worst_true = 0.0;
         for (int i = 0; i < ni; ++i) {
             const double eta = h[BV_ETA * ni + i], eta0 = h[BV_ETA0 * ni + i];
             const double rr = eta0 > 0.0 ? eta / eta0 : 0.0;
@@ -1709,11 +1898,12 @@ static int solve_batch(mpet_ctx* c, const double* b, double* x, mpet_stats* st, 
             const double nb2 = h[BV_NB2 * ni + i];
             const double rt = nb2 > 0.0 ? sqrt(h[BV_NR2 * ni + i] / nb2) : 0.0;
             worst_true = rt > worst_true ? rt : worst_true;
+            double want = 1.0;
             if (h[BV_DONE * ni + i] == 0.0) {
                 ++active;
-                const double want = c->prm.rtol * eta0 / eta;
-                need = want < need ? want : need;
+                want = c->prm.rtol * eta0 / eta;
             }
+            target[i] = fp64 ? (want < 1e-15 ? 1e-15 : want) : (want < c->prm.inner_rtol ? c->prm.inner_rtol : want);
         }
         relres = worst;
         relres_true = worst_true;
@@ -1722,24 +1912,16 @@ static int solve_batch(mpet_ctx* c, const double* b, double* x, mpet_stats* st, 
             status = MPET_ERR_MAXIT;
             break;
         }
-        // unit preconditioned norm per unconverged instance, zero otherwise
-        k_seg_scale<T><<<(unsigned)nch, 256, 0, c->stream>>>(c->ch_lo, c->ch_len, c->ch_inst, iv + BV_SIN * ni,
-                                                             rhs, y);
+        MPET_CUDA(cudaMemcpyAsync(c->btarget, target.data(), sizeof(double) * ni, cudaMemcpyHostToDevice,
+                                  c->stream));
         k_copy2<T><<<G, 256, 0, c->stream>>>(n, rhs, (T*)c->kr[1], (T*)c->kr[1]);
-        k_dot<T><<<NB_RED, 256, 0, c->stream>>>(n, rhs, y, c->partials);
-        k_mr_init<<<1, 256, 0, c->stream>>>(c->sc, c->partials);
+        k_bmr_init<<<gi, 128, 0, c->stream>>>(ni, c->bsc, iv + BV_Q * ni, iv + BV_DONE * ni, c->bdone);
         MPET_CHECK_LAUNCH();
-        double target = need / sqrt((double)active);
-        if (fp64) {
-            if (target < 1e-15) target = 1e-15;
-        } else {
-            if (target < c->prm.inner_rtol) target = c->prm.inner_rtol;
-        }
         MPET_CUDA(cudaMemsetAsync(c->kd, 0, sizeof(T) * n, c->stream));
         for (int q = 0; q < 3; ++q) MPET_CUDA(cudaMemsetAsync(c->kw[q], 0, sizeof(T) * n, c->stream));
         int done = 0;
         MPET_CUDA(cudaEventRecord(c->ev_in0, c->stream));
-        int s2 = minres_run<T>(c, target, maxit - iters, &done);
+        int s2 = bminres_run<T>(c, maxit - iters, &done);
         MPET_CUDA(cudaEventRecord(c->ev_in1, c->stream));
         MPET_CUDA(cudaEventSynchronize(c->ev_in1));
         float ims = 0.f;
@@ -1747,6 +1929,7 @@ static int solve_batch(mpet_ctx* c, const double* b, double* x, mpet_stats* st, 
         c->t_inner_ms += ims;
         c->n_inner_its += done;
         iters += done;
+        // x_i += ||D^-1 r_i|| d_i for the instances that iterated
         k_seg_add<T><<<(unsigned)nch, 256, 0, c->stream>>>(c->ch_lo, c->ch_len, c->ch_inst, iv + BV_SOUT * ni, x,
                                                            (const T*)c->kd);
         MPET_CHECK_LAUNCH();
@@ -1835,6 +2018,13 @@ void setup_batch(mpet_ctx* c, int ninst, const int32_t* vertex_inst) {
     MPET_CUDA(cudaMemsetAsync(c->inst_v, 0, sizeof(double) * BV_COUNT * ninst, c->stream));
     if (c->inst_host) MPET_CUDA(cudaFreeHost(c->inst_host));
     MPET_CUDA(cudaMallocHost(&c->inst_host, sizeof(double) * BV_COUNT * ninst));
+    c->bsc = c->pool.alloc<MinresScalars>(ninst);
+    c->bdone = c->pool.alloc<double>(ninst);
+    c->btarget = c->pool.alloc<double>(ninst);
+    c->bval = c->pool.alloc<double>(ninst);
+    MPET_CUDA(cudaMallocHost(&c->bsc_host, sizeof(MinresScalars) * ninst));
+    MPET_CUDA(cudaMallocHost(&c->bdone_host, sizeof(double) * ninst));
+    destroy_minres_graph(c);
     MPET_CUDA(cudaStreamSynchronize(c->stream));
 }
 
