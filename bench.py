@@ -287,11 +287,12 @@ def cpu_baseline_sample(n_sample=12, J=4, steps=1):
     A = om.assemble_matrix(dt)
     dofs0, _ = om.dirichlet_values(0.0, data)
     Abc = om.apply_bc_matrix(A, dofs0)
-    blocks = om.preconditioner_blocks(dt, u_weight=om.mu + om.lmbda)
+    md = om.network_modes(dt)
+    blocks = om.preconditioner_blocks(dt, u_weight=om.mu + om.lmbda, modes=md)
     P0 = krylov.p1_in_p2_embedding(om.dm, om.dirichlet_dofs()[0][0])
     hu = krylov.SAHierarchy(blocks[0], theta=0.1, cheb_degree=4, P0=P0)
     hp = [krylov.SAHierarchy(B, theta=0.1, cheb_degree=4) for B in blocks[1:]]
-    M = krylov.block_preconditioner(hu, hp, 3, om.dm.Nu, om.dm.nv)
+    M = krylov.block_preconditioner(hu, hp, 3, om.dm.Nu, om.dm.nv, Q=md[0])
     up = np.zeros(om.dm.N)
     t = 0.0
     t0 = time.perf_counter()

@@ -71,7 +71,9 @@ typedef struct mpet_params {
     int32_t check_every;               /* host convergence check period (iterations) */
     int32_t amg_p2_to_p1;              /* 1: displacement hierarchy starts with the P1-in-P2
                                           embedding (p-multigrid), then aggregation */
-    int32_t pad0;
+    int32_t prec_network_modes;        /* 1: the pressure blocks of the preconditioner act on the
+                                          eigenmodes of the network coupling (see below), 0: on
+                                          the networks (the reference form, mpetsolver.py:270) */
     double prec_u_weight;              /* w in the displacement block w (grad u, grad v) of the
                                           preconditioner; the reference form uses mu
                                           (mpetsolver.py:269), mu + lmbda balances the blocks;

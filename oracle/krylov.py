@@ -195,8 +195,10 @@ class SAHierarchy:
         return sum(l["A"].nnz for l in self.levels) / self.levels[0]["A"].nnz
 
 
-def block_preconditioner(hier_u, hier_p, d, Nu, nv):
-    """z = blockdiag(AMG(Lu) per displacement component, AMG(P_a) per network) r."""
+def block_preconditioner(hier_u, hier_p, d, Nu, nv, Q=None):
+    """z = blockdiag(AMG(Lu) per displacement component, AMG(P_a) per network) r;
+    with Q (J x J orthogonal) the pressure hierarchies act on the network
+    eigenmodes: z_p = Q AMG_k((Q^T r_p)_k) vertex by vertex."""
     J = len(hier_p)
 
     def apply(r):
@@ -204,9 +206,13 @@ def block_preconditioner(hier_u, hier_p, d, Nu, nv):
         ru = r[:Nu].reshape(-1, d)
         zu = np.stack([hier_u.vcycle(np.ascontiguousarray(ru[:, k])) for k in range(d)], 1)
         z[:Nu] = zu.ravel()
-        for a in range(J):
-            s = slice(Nu + a * nv, Nu + (a + 1) * nv)
-            z[s] = hier_p[a].vcycle(r[s])
+        rp = r[Nu:].reshape(J, nv)
+        if Q is not None:
+            rp = Q.T @ rp
+        zp = np.stack([hier_p[a].vcycle(np.ascontiguousarray(rp[a])) for a in range(J)])
+        if Q is not None:
+            zp = Q @ zp
+        z[Nu:] = zp.ravel()
         return z
     return apply
 

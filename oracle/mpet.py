@@ -373,11 +373,46 @@ class OracleMPET:
         return A, b
 
     # --- preconditioner blocks (mpetsolver.py:264-271) ---------------------------------
-    def preconditioner_blocks(self, dt, u_weight=None):
+    def network_modes(self, dt, form="auto"):
+        """(Q, lambda) of the pressure blocks: per network (Q = I, lambda =
+        diag C) or per eigenmode of the network mass coupling C = Q diag(lambda)
+        Q^T, C = diag(c_a + dt theta sum_{b != a} S_ab) - dt theta S (off the
+        diagonal).  "auto" takes the form whose worst condition number of
+        P(t)^-1 (C + t dt theta diag(K)) over t in [1, 1e6] is smaller."""
+        J = self.J
+        dth = dt * self.theta
+        C = -dth * self.S.copy()
+        for a in range(J):
+            C[a, a] = self.c[a] + dth * sum(self.S[a, b_] for b_ in range(J) if b_ != a)
+        lam, Q = np.linalg.eigh(C)
+        per_net = (np.eye(J), np.diag(C).copy())
+        if form == "networks":
+            return per_net
+        if form == "modes":
+            return Q, lam
+        K = np.array([float(np.mean(self.Kc[a])) for a in range(J)])
+
+        def kappa(Qx, lx):
+            kt = (Qx ** 2).T @ K
+            worst = 1.0
+            for t in 10.0 ** (0.1 * np.arange(61)):
+                A = C + t * dth * np.diag(K)
+                P = Qx @ np.diag(lx + t * dth * kt) @ Qx.T
+                ev = np.linalg.eigvalsh(np.linalg.solve(np.linalg.cholesky(P), np.linalg.solve(
+                    np.linalg.cholesky(P), A).T).T)
+                worst = max(worst, ev.max() / ev.min())
+            return worst
+        if np.all(lam > 0) and kappa(Q, lam) < kappa(*per_net):
+            return Q, lam
+        return per_net
+
+    def preconditioner_blocks(self, dt, u_weight=None, modes=None):
         """Scalar SPD blocks: w (grad u, grad v) on P2 nodes (w = mu in the
         reference form, mpetsolver.py:269) and, per network,
         c_a M + dt theta K_a L + dt theta sum_{b != a} S_ab M on P1 vertices,
-        with the Dirichlet DOFs eliminated symmetrically (unit diagonal)."""
+        with the Dirichlet DOFs eliminated symmetrically (unit diagonal).
+        With modes = (Q, lambda) from network_modes, block k is instead
+        lambda_k M + dt theta (sum_a Q_ak^2 K_a) L."""
         dm = self.dm
         nc = self.vol.shape[0]
         tr = np.einsum("cijkk->cij", self.Mg)
@@ -388,8 +423,14 @@ class OracleMPET:
         Lu, _ = self.zero_rows_columns(Lu, [bcs[0][0]])
         blocks = [Lu]
         for a in range(self.J):
-            sS = sum(self.S[a, b_] for b_ in range(self.J) if b_ != a)
-            loc = (self.c[a] + dt * self.theta * sS) * self.M1 + dt * self.theta * self.Kc[a][:, None, None] * self.L1
+            if modes is not None:
+                Q, lam = modes
+                kk = sum(Q[b_, a] ** 2 * self.Kc[b_] for b_ in range(self.J))
+                loc = lam[a] * self.M1 + dt * self.theta * kk[:, None, None] * self.L1
+            else:
+                sS = sum(self.S[a, b_] for b_ in range(self.J) if b_ != a)
+                loc = ((self.c[a] + dt * self.theta * sS) * self.M1
+                       + dt * self.theta * self.Kc[a][:, None, None] * self.L1)
             Pa = fem.assemble_csr(dm.cells, loc, dm.nv)
             Pa, _ = self.zero_rows_columns(Pa, [bcs[1 + a][0]])
             blocks.append(Pa)

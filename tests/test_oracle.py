@@ -5,7 +5,8 @@
 * sparsity counts of the Kuhn cube (DOLFIN rule) at the workload sizes;
 * symmetric Dirichlet elimination (bc_symmetric.py) gives the same solution
   as row replacement;
-* preconditioned MINRES + SA-AMG reaches the SuperLU solution.
+* preconditioned MINRES + SA-AMG (pressure blocks per network or per network
+  eigenmode) reaches the SuperLU solution.
 """
 import math
 
@@ -96,7 +97,8 @@ def test_symmetric_elimination_matches_row_replacement():
     assert np.linalg.norm(xs - x) <= 1e-10 * np.linalg.norm(x)
 
 
-def test_minres_amg_reaches_lu_solution():
+@pytest.mark.parametrize("modes", ["networks", "modes", "auto"])
+def test_minres_amg_reaches_lu_solution(modes):
     problem, dt = make_problem(4, 4)
     om = make_oracle(problem)
     data = oracle_data(4)
@@ -106,11 +108,12 @@ def test_minres_amg_reaches_lu_solution():
     for d, v in zip(dofs, vals):
         x0[d] = v
     r0 = bbc - Abc @ x0
-    blocks = om.preconditioner_blocks(dt, u_weight=om.mu + om.lmbda)
+    md = om.network_modes(dt, form=modes)
+    blocks = om.preconditioner_blocks(dt, u_weight=om.mu + om.lmbda, modes=md)
     P0 = krylov.p1_in_p2_embedding(om.dm, om.dirichlet_dofs()[0][0])
     hu = krylov.SAHierarchy(blocks[0], theta=0.1, cheb_degree=4, P0=P0)
     hp = [krylov.SAHierarchy(B, theta=0.1, cheb_degree=4) for B in blocks[1:]]
-    M = krylov.block_preconditioner(hu, hp, 3, om.dm.Nu, om.dm.nv)
+    M = krylov.block_preconditioner(hu, hp, 3, om.dm.Nu, om.dm.nv, Q=md[0])
     d, it, hist = krylov.minres(Abc, r0, M, rtol=1e-11, maxiter=3000)
     assert hist[-1] <= 1e-11
     assert np.linalg.norm(x0 + d - x) <= 1e-8 * np.linalg.norm(x)

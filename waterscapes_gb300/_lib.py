@@ -46,7 +46,7 @@ class MpetParams(ctypes.Structure):
         ("amg_coarse_size", ctypes.c_int32),
         ("check_every", ctypes.c_int32),
         ("amg_p2_to_p1", ctypes.c_int32),
-        ("pad0", ctypes.c_int32),
+        ("prec_network_modes", ctypes.c_int32),
         ("prec_u_weight", ctypes.c_double),
     ]
 

@@ -18,6 +18,7 @@
 #include <string.h>
 
 #include <algorithm>
+#include <cmath>
 #include <vector>
 
 #ifdef _OPENMP
@@ -454,6 +455,105 @@ void amg_setup_host(const HostCsr& A0, const HostCsr* P0, double theta, int coar
     out.ncoarse = nc;
     if (!cholesky_inverse(dense, nc, out.cinv))
         fail(MPET_ERR_INVALID, "AMG coarsest operator is not positive definite");
+}
+
+// Symmetric eigendecomposition A = Q diag(lam) Q^T of a small n x n matrix
+// (row-major, n <= 8) by cyclic Jacobi rotations (Golub & Van Loan,
+// Matrix Computations, 4th ed., sec. 8.5.2); Q column i is eigenvector i.
+void sym_eig(int n, const double* A_in, double* Q, double* lam) {
+    std::vector<double> A(A_in, A_in + n * n);
+    for (int i = 0; i < n * n; ++i) Q[i] = 0.0;
+    for (int i = 0; i < n; ++i) Q[i * n + i] = 1.0;
+    for (int sweep = 0; sweep < 64; ++sweep) {
+        double off = 0.0, tot = 0.0;
+        for (int i = 0; i < n; ++i)
+            for (int j = 0; j < n; ++j) {
+                tot += A[i * n + j] * A[i * n + j];
+                if (i != j) off += A[i * n + j] * A[i * n + j];
+            }
+        if (off <= 1e-30 * tot) break;
+        for (int p = 0; p < n - 1; ++p)
+            for (int q = p + 1; q < n; ++q) {
+                const double apq = A[p * n + q];
+                if (apq == 0.0) continue;
+                const double tau = (A[q * n + q] - A[p * n + p]) / (2.0 * apq);
+                const double t = (tau >= 0.0 ? 1.0 : -1.0) / (std::fabs(tau) + std::sqrt(1.0 + tau * tau));
+                const double cs = 1.0 / std::sqrt(1.0 + t * t), sn = t * cs;
+                for (int k = 0; k < n; ++k) {  // A <- A J
+                    const double akp = A[k * n + p], akq = A[k * n + q];
+                    A[k * n + p] = cs * akp - sn * akq;
+                    A[k * n + q] = sn * akp + cs * akq;
+                }
+                for (int k = 0; k < n; ++k) {  // A <- J^T A
+                    const double apk = A[p * n + k], aqk = A[q * n + k];
+                    A[p * n + k] = cs * apk - sn * aqk;
+                    A[q * n + k] = sn * apk + cs * aqk;
+                }
+                for (int k = 0; k < n; ++k) {  // Q <- Q J
+                    const double qkp = Q[k * n + p], qkq = Q[k * n + q];
+                    Q[k * n + p] = cs * qkp - sn * qkq;
+                    Q[k * n + q] = sn * qkp + cs * qkq;
+                }
+            }
+    }
+    for (int i = 0; i < n; ++i) lam[i] = A[i * n + i];
+}
+
+// Worst condition number, over t in [1, 1e6] (the ratio of stiffness to
+// mass eigenvalues from the smoothest to the finest P1 mode), of the
+// preconditioned network operator P(t)^-1 (C + t g diag(K)) for
+// P(t) = Q (diag(lam) + t g diag(kt)) Q^T, kt_k = sum_a Q_ak^2 K_a.
+double network_kappa(int J, const double* C, const double* K, double g, const double* Q, const double* lam) {
+    double worst = 1.0;
+    std::vector<double> A(J * J), P(J * J), L(J * J), W(J * J), T(J * J), V(J * J), ev(J);
+    std::vector<double> kt(J);
+    for (int k = 0; k < J; ++k) {
+        kt[k] = 0.0;
+        for (int a = 0; a < J; ++a) kt[k] += Q[a * J + k] * Q[a * J + k] * K[a];
+    }
+    for (int step = 0; step <= 60; ++step) {
+        const double t = pow(10.0, 0.1 * step);
+        for (int a = 0; a < J; ++a)
+            for (int b = 0; b < J; ++b) {
+                A[a * J + b] = C[a * J + b] + (a == b ? t * g * K[a] : 0.0);
+                double p = 0.0;
+                for (int k = 0; k < J; ++k) p += Q[a * J + k] * (lam[k] + t * g * kt[k]) * Q[b * J + k];
+                P[a * J + b] = p;
+            }
+        // P = L L^T (Cholesky), W = L^-1 A L^-T, eigenvalues of W
+        for (int i = 0; i < J; ++i)
+            for (int j = 0; j <= i; ++j) {
+                double sum = P[i * J + j];
+                for (int k = 0; k < j; ++k) sum -= L[i * J + k] * L[j * J + k];
+                if (i == j) {
+                    if (!(sum > 0.0)) return 1e300;
+                    L[i * J + i] = sqrt(sum);
+                } else {
+                    L[i * J + j] = sum / L[j * J + j];
+                }
+            }
+        for (int col = 0; col < J; ++col)  // T = L^-1 A (forward substitution per column)
+            for (int i = 0; i < J; ++i) {
+                double sum = A[i * J + col];
+                for (int k = 0; k < i; ++k) sum -= L[i * J + k] * T[k * J + col];
+                T[i * J + col] = sum / L[i * J + i];
+            }
+        for (int row = 0; row < J; ++row)  // W = T L^-T
+            for (int i = 0; i < J; ++i) {
+                double sum = T[row * J + i];
+                for (int k = 0; k < i; ++k) sum -= W[row * J + k] * L[i * J + k];
+                W[row * J + i] = sum / L[i * J + i];
+            }
+        sym_eig(J, W.data(), V.data(), ev.data());
+        double lo = ev[0], hi = ev[0];
+        for (int k = 1; k < J; ++k) {
+            lo = std::min(lo, ev[k]);
+            hi = std::max(hi, ev[k]);
+        }
+        if (!(lo > 0.0)) return 1e300;
+        worst = std::max(worst, hi / lo);
+    }
+    return worst;
 }
 
 }  // namespace mpet

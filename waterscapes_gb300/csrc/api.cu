@@ -160,15 +160,21 @@ int mpet_setup(mpet_ctx* c, const mpet_params* p) {
     build_bc(c);
     build_facets(c);
     c->A.v64 = c->pool.alloc<double>(c->nnz);
-    if (c->prm.precision == MPET_PRECISION_MIXED) c->A.v32 = c->pool.alloc<float>(c->nnz);
     c->dinv = c->pool.alloc<double>(c->N);
     c->Lu.v64 = c->pool.alloc<double>(c->Lu.nnz);
     for (int a = 0; a < c->J; ++a) c->Pp[a].v64 = c->pool.alloc<double>(c->Pp[a].nnz);
     alloc_krylov(c);
     MPET_CUDA(cudaMemsetAsync(c->A.v64, 0, sizeof(double) * c->nnz, c->stream));
-    if (c->A.v32) MPET_CUDA(cudaMemsetAsync(c->A.v32, 0, sizeof(float) * c->nnz, c->stream));
-    build_sell(c, c->A, c->A.v32 != nullptr, true);
+    // optional copies of the system matrix for the SpMV variants, in order of
+    // use, each only while a fifth of HBM stays free: node blocks, the FP32
+    // CSR values, SELL-32
+    const bool mixed = c->prm.precision == MPET_PRECISION_MIXED;
     build_node_blocks(c);
+    if (mixed && device_fits(c, sizeof(float) * (size_t)c->nnz)) {
+        c->A.v32 = c->pool.alloc<float>(c->nnz);
+        MPET_CUDA(cudaMemsetAsync(c->A.v32, 0, sizeof(float) * c->nnz, c->stream));
+    }
+    if (!mixed || c->A.v32) build_sell(c, c->A, c->A.v32 != nullptr, true);
     refresh_system_copies(c);
     autotune_system(c);
     MPET_CUDA(cudaStreamSynchronize(c->stream));
@@ -332,6 +338,8 @@ int mpet_set_batch(mpet_ctx* c, int32_t ninst, const int32_t* vertex_instance) {
     require(c->ninst == 0, MPET_ERR_STATE, "the batch partition is already set");
     require(ninst >= 1 && vertex_instance, MPET_ERR_INVALID, "need ninst >= 1 and an instance per vertex");
     setup_batch(c, ninst, vertex_instance);
+    set_instances(c, ninst, vertex_instance);
+    c->precond_ready = false;
     API_END(c)
 }
 
@@ -385,6 +393,7 @@ int mpet_setup_preconditioner(mpet_ctx* c, double dt) {
     require(c->setup_done, MPET_ERR_STATE, "mpet_setup must come first");
     require(dt > 0.0, MPET_ERR_INVALID, "dt must be positive");
     destroy_minres_graph(c);
+    setup_network_modes(c, dt);
     launch_assemble_prec_blocks(c, dt);
     const bool fp32 = c->prm.precision == MPET_PRECISION_MIXED;
     auto fetch = [&](const Csr& d, HostCsr& h) {

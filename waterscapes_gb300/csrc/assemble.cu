@@ -15,6 +15,10 @@
 // the CSR positions given by the per-cell rank tables.  Every value is
 // written by exactly one warp in a fixed order, so the result is
 // deterministic and needs neither atomics nor a cell colouring.
+#include <string.h>
+
+#include <algorithm>
+
 #include "mpet_internal.cuh"
 
 namespace mpet {
@@ -264,6 +268,10 @@ struct PrecArgs {
     const uint8_t* vert_bc;
     double* lu;
     double* pp[MPET_MAX_NETWORKS];
+    // network eigenmodes (null: one block per network): per instance Q (J x J) and lambda (J)
+    const double* mQ;
+    const double* mlam;
+    const int32_t* cell_inst;
 };
 
 __global__ void __launch_bounds__(256) k_assemble_prec(PrecArgs A, MatCoef P) {
@@ -312,10 +320,22 @@ __global__ void __launch_bounds__(256) k_assemble_prec(PrecArgs A, MatCoef P) {
                     const double M1 = w20 * (m == w ? 2.0 : 1.0);
                     const double L1 = G.vol * (G.b[m][0] * G.b[w][0] + G.b[m][1] * G.b[w][1] + G.b[m][2] * G.b[w][2]);
                     const int64_t pos = s1 + A.rank1[cell * 40 + m * 4 + w];
-                    for (int a = 0; a < J; ++a) {
-                        if (A.vert_bc[(int64_t)a * A.nv + i] || A.vert_bc[(int64_t)a * A.nv + vw]) continue;
-                        double sS = P.Ssumof(a, cell) - P.Sof(a, a, cell);
-                        A.pp[a][pos] += (P.cof(a, cell) + P.dt_theta * sS) * M1 + P.dt_theta * P.Kof(a, cell) * L1;
+                    if (A.mQ) {
+                        // mode k: lambda_k M + dt theta (sum_a Q_ak^2 K_a) L  (Dirichlet sets equal for all networks)
+                        if (A.vert_bc[i] || A.vert_bc[vw]) continue;
+                        const int64_t inst = A.cell_inst ? A.cell_inst[cell] : 0;
+                        const double* Q = A.mQ + inst * J * J;
+                        for (int k = 0; k < J; ++k) {
+                            double kk = 0.0;
+                            for (int a = 0; a < J; ++a) kk += Q[a * J + k] * Q[a * J + k] * P.Kof(a, cell);
+                            A.pp[k][pos] += A.mlam[inst * J + k] * M1 + P.dt_theta * kk * L1;
+                        }
+                    } else {
+                        for (int a = 0; a < J; ++a) {
+                            if (A.vert_bc[(int64_t)a * A.nv + i] || A.vert_bc[(int64_t)a * A.nv + vw]) continue;
+                            double sS = P.Ssumof(a, cell) - P.Sof(a, a, cell);
+                            A.pp[a][pos] += (P.cof(a, cell) + P.dt_theta * sS) * M1 + P.dt_theta * P.Kof(a, cell) * L1;
+                        }
                     }
                 }
             }
@@ -545,6 +565,9 @@ void launch_assemble_prec_blocks(mpet_ctx* c, double dt) {
     A.vert_bc = c->vert_bc;
     A.lu = c->Lu.v64;
     for (int a = 0; a < c->J; ++a) A.pp[a] = c->Pp[a].v64;
+    A.mQ = c->net_modes ? c->mode_Q : nullptr;
+    A.mlam = c->net_modes ? c->mode_lam : nullptr;
+    A.cell_inst = c->cell_inst;
     MatCoef P = make_coef(c, dt);
     int blocks = grid_for(c->nnodes * 32, 256);
     if (blocks > 152 * 64) blocks = 152 * 64;
@@ -747,6 +770,135 @@ void launch_misfit(mpet_ctx* c, const double* up, const double* target, double* 
                                              dloss, c->partials);
     k_finish_sum<<<1, 256, 0, c->stream>>>(c->partials, loss_dev);
     MPET_CHECK_LAUNCH();
+}
+
+// --- network eigenmodes of the pressure preconditioner --------------------------
+//
+// The pressure blocks of the system couple the networks through the mass
+// terms C_ab M, C = diag(c_a + dt theta sum_{b != a} S_ab) - dt theta S (off
+// the diagonal).  With C = Q diag(lambda) Q^T per instance, the preconditioner
+// can run one AMG hierarchy per mode k on lambda_k M + dt theta kt_k L,
+// kt_k = sum_a Q_ak^2 K_a, between z = Q zt and rt = Q^T r at every vertex: an
+// SPD operator that keeps the exact mass coupling of the networks (the
+// reference's block-diagonal form, mpetsolver.py:270, drops it and loses
+// robustness when dt S >> c) but averages the K_a of the modes (poor when
+// the K_a differ by orders of magnitude).  Each instance takes the form with
+// the smaller worst-case condition number of its J x J network operator.
+
+__global__ void k_gather_coef(int ninst, const int64_t* __restrict__ rep, int J, int64_t nc,
+                              const double* __restrict__ cc, const double* __restrict__ Sc,
+                              const double* __restrict__ Kc, double* out) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= ninst) return;
+    const int64_t cell = rep[i];
+    double* o = out + (int64_t)i * (2 * J + J * J);
+    for (int a = 0; a < J; ++a) o[a] = cc ? cc[a * nc + cell] : 0.0;
+    for (int q = 0; q < J * J; ++q) o[J + q] = Sc ? Sc[q * nc + cell] : 0.0;
+    for (int a = 0; a < J; ++a) o[J + J * J + a] = Kc ? Kc[a * nc + cell] : 0.0;
+}
+
+__global__ void k_cell_inst(int64_t nc, const int32_t* __restrict__ cells, const int32_t* __restrict__ vinst,
+                            int32_t* cinst) {
+    const int64_t c = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    if (c < nc) cinst[c] = vinst[cells[4 * c]];
+}
+
+void set_instances(mpet_ctx* c, int ninst, const int32_t* vertex_inst_host) {
+    c->vert_inst = c->pool.alloc<int32_t>(c->nv);
+    MPET_CUDA(cudaMemcpyAsync(c->vert_inst, vertex_inst_host, sizeof(int32_t) * c->nv, cudaMemcpyHostToDevice,
+                              c->stream));
+    c->cell_inst = c->pool.alloc<int32_t>(c->nc);
+    k_cell_inst<<<grid_for(c->nc, 256), 256, 0, c->stream>>>(c->nc, c->cells, c->vert_inst, c->cell_inst);
+    MPET_CHECK_LAUNCH();
+    MPET_CUDA(cudaStreamSynchronize(c->stream));
+}
+
+void setup_network_modes(mpet_ctx* c, double dt) {
+    const int J = c->J;
+    c->net_modes = false;
+    if (!c->prm.prec_network_modes || J < 2) return;
+    // the transform mixes the networks at a vertex: all networks need the same Dirichlet vertices
+    std::vector<uint8_t> vb((size_t)J * c->nv);
+    MPET_CUDA(cudaMemcpyAsync(vb.data(), c->vert_bc, vb.size(), cudaMemcpyDeviceToHost, c->stream));
+    MPET_CUDA(cudaStreamSynchronize(c->stream));
+    for (int a = 1; a < J; ++a)
+        if (memcmp(vb.data(), vb.data() + (size_t)a * c->nv, c->nv) != 0) return;
+    const int ni = c->ninst > 0 ? c->ninst : 1;
+    // coefficients of one cell per instance (per-cell fields hold per-instance constants)
+    const int stride = 2 * J + J * J;
+    std::vector<double> coef((size_t)ni * stride);
+    const bool per_cell = c->c_cells || c->S_cells || (c->ninst > 0 && c->K_cells);
+    if (per_cell) {
+        std::vector<int64_t> rep(ni, 0);
+        if (c->ninst > 0) {
+            std::vector<int32_t> ci(c->nc);
+            MPET_CUDA(cudaMemcpyAsync(ci.data(), c->cell_inst, sizeof(int32_t) * c->nc, cudaMemcpyDeviceToHost,
+                                      c->stream));
+            MPET_CUDA(cudaStreamSynchronize(c->stream));
+            std::vector<char> seen(ni, 0);
+            for (int64_t e = 0; e < c->nc; ++e)
+                if (!seen[ci[e]]) {
+                    seen[ci[e]] = 1;
+                    rep[ci[e]] = e;
+                }
+        }
+        TmpBuf drep(sizeof(int64_t) * ni), dout(sizeof(double) * coef.size());
+        MPET_CUDA(cudaMemcpyAsync(drep.p, rep.data(), sizeof(int64_t) * ni, cudaMemcpyHostToDevice, c->stream));
+        k_gather_coef<<<grid_for(ni, 128), 128, 0, c->stream>>>(ni, (const int64_t*)drep.p, J, c->nc, c->c_cells,
+                                                                 c->S_cells, c->ninst > 0 ? c->K_cells : nullptr,
+                                                                 (double*)dout.p);
+        MPET_CHECK_LAUNCH();
+        MPET_CUDA(cudaMemcpyAsync(coef.data(), dout.p, sizeof(double) * coef.size(), cudaMemcpyDeviceToHost,
+                                  c->stream));
+        MPET_CUDA(cudaStreamSynchronize(c->stream));
+    }
+    const double dth = dt * c->prm.theta;
+    std::vector<double> Q((size_t)ni * J * J), lam((size_t)ni * J), C(J * J), K(J), Qm(J * J), lm(J), Qd(J * J),
+        ld(J);
+    int used = 0;
+    for (int i = 0; i < ni; ++i) {
+        const double* o = coef.data() + (size_t)i * stride;
+        for (int a = 0; a < J; ++a) {
+            double off = 0.0;
+            for (int b = 0; b < J; ++b) {
+                const double sab = c->S_cells ? o[J + a * J + b] : c->prm.S[a * MPET_MAX_NETWORKS + b];
+                if (b != a) {
+                    off += sab;
+                    C[a * J + b] = -dth * sab;
+                }
+            }
+            C[a * J + a] = (c->c_cells ? o[a] : c->prm.c[a]) + dth * off;
+            // the scalar slot holds the mean of a per-cell K of a single instance
+            K[a] = (c->ninst > 0 && c->K_cells) ? o[J + J * J + a] : c->prm.K[a];
+        }
+        // per network (Q = I, lambda = diag C) or per eigenmode of C, whichever
+        // keeps the network operator C + t dt theta diag(K) better conditioned
+        for (int a = 0; a < J; ++a) {
+            for (int b = 0; b < J; ++b) Qd[a * J + b] = a == b ? 1.0 : 0.0;
+            ld[a] = C[a * J + a];
+        }
+        sym_eig(J, C.data(), Qm.data(), lm.data());
+        bool modes_ok = true;
+        for (int k = 0; k < J; ++k) modes_ok = modes_ok && lm[k] > 0.0;
+        const double kd = network_kappa(J, C.data(), K.data(), dth, Qd.data(), ld.data());
+        const double km = modes_ok ? network_kappa(J, C.data(), K.data(), dth, Qm.data(), lm.data()) : 1e300;
+        const bool use = km < kd;
+        used += use ? 1 : 0;
+        std::copy((use ? Qm : Qd).begin(), (use ? Qm : Qd).end(), Q.begin() + (size_t)i * J * J);
+        std::copy((use ? lm : ld).begin(), (use ? lm : ld).end(), lam.begin() + (size_t)i * J);
+    }
+    if (used == 0) return;  // every instance keeps the per-network blocks
+    if (!c->mode_Q) {
+        c->mode_Q = c->pool.alloc<double>((int64_t)ni * J * J);
+        c->mode_lam = c->pool.alloc<double>((int64_t)ni * J);
+        c->mode_r = c->pool.alloc<double>((int64_t)J * c->nv);
+        c->mode_z = c->pool.alloc<double>((int64_t)J * c->nv);
+    }
+    MPET_CUDA(cudaMemcpyAsync(c->mode_Q, Q.data(), sizeof(double) * Q.size(), cudaMemcpyHostToDevice, c->stream));
+    MPET_CUDA(cudaMemcpyAsync(c->mode_lam, lam.data(), sizeof(double) * lam.size(), cudaMemcpyHostToDevice,
+                              c->stream));
+    MPET_CUDA(cudaStreamSynchronize(c->stream));
+    c->net_modes = true;
 }
 
 }  // namespace mpet

@@ -30,6 +30,22 @@ struct Error {
 // Device allocation tracked by the context so destroy() frees everything.
 // Every allocation carries kTail spare bytes, so bulk copies whose size is
 // rounded up to 16 bytes may read past the last element without leaving it.
+// Scoped temporary device buffer (freed on scope exit).
+struct TmpBuf {
+    void* p = nullptr;
+    explicit TmpBuf(size_t bytes) {
+        if (cudaMalloc(&p, bytes ? bytes : 1) != cudaSuccess) {
+            cudaGetLastError();
+            fail(MPET_ERR_NOMEM, "temporary cudaMalloc of " + std::to_string(bytes) + " bytes failed");
+        }
+    }
+    ~TmpBuf() {
+        if (p) cudaFree(p);
+    }
+    template <typename T>
+    T* as() { return (T*)p; }
+};
+
 struct DevPool {
     static constexpr size_t kTail = 64;
     std::vector<void*> ptrs;
@@ -170,6 +186,8 @@ struct HostAmg {
 // P0, if given, is the prolongator of the first level (otherwise smoothed aggregation).
 void amg_setup_host(const HostCsr& A, const HostCsr* P0, double theta, int coarse_size, int max_levels,
                     HostAmg& out);
+void sym_eig(int n, const double* A, double* Q, double* lam);
+double network_kappa(int J, const double* C, const double* K, double g, const double* Q, const double* lam);
 
 }  // namespace mpet
 
@@ -298,6 +316,17 @@ struct mpet_ctx {
     cudaGraphExec_t bmr_graph = nullptr;
     int64_t bmr_graph_launches = 0;
 
+    // network eigenmodes of the pressure preconditioner (prec_network_modes):
+    // per instance Q (J x J, column i = mode i) and lambda (J); vertex and
+    // cell instance ids (batches); transformed residual / correction (J x nv)
+    bool net_modes = false;
+    double* mode_Q = nullptr;
+    double* mode_lam = nullptr;
+    int32_t* vert_inst = nullptr;
+    int32_t* cell_inst = nullptr;
+    double* mode_r = nullptr;
+    double* mode_z = nullptr;
+
     // set by a kernel whose bounded wait gave up (read after each solve)
     int* dev_err = nullptr;
     double spmv_variant_ms[7] = {0, 0, 0, 0, 0, 0, 0};  // variants 0..5 and 8 (node blocks)
@@ -360,6 +389,8 @@ void launch_robin_matrix(mpet_ctx* c, double dt);
 // assemble.cu
 void launch_assemble_matrix(mpet_ctx* c, double dt, bool apply_bc, bool write32);
 void launch_assemble_prec_blocks(mpet_ctx* c, double dt);
+void setup_network_modes(mpet_ctx* c, double dt);
+void set_instances(mpet_ctx* c, int ninst, const int32_t* vertex_inst_host);
 void launch_rhs(mpet_ctx* c, double dt, const double* up_prev, double* b);
 void launch_bc_vector(mpet_ctx* c, double* b);
 void launch_set_bc_in_x(mpet_ctx* c, double* x);
@@ -388,6 +419,7 @@ void build_tiles(mpet_ctx* c, Csr& A, const int64_t* rp_host);
 void build_sell(mpet_ctx* c, Csr& A, bool fp32, bool with64);
 void fill_sell(mpet_ctx* c, Csr& A);
 void build_node_blocks(mpet_ctx* c);
+bool device_fits(mpet_ctx* c, size_t bytes);
 void refresh_system_copies(mpet_ctx* c);
 bool spmv_variant_available(const Csr& A, int variant);
 constexpr int SPMV_TILE = 2048;  // entries per staged tile

@@ -22,20 +22,6 @@ typedef unsigned long long u64;
 
 __constant__ int c_tet_edges[6][2] = {{2, 3}, {1, 3}, {1, 2}, {0, 3}, {0, 2}, {0, 1}};
 
-struct TmpBuf {
-    void* p = nullptr;
-    explicit TmpBuf(size_t bytes) {
-        if (cudaMalloc(&p, bytes ? bytes : 1) != cudaSuccess) {
-            cudaGetLastError();
-            fail(MPET_ERR_NOMEM, "temporary cudaMalloc of " + std::to_string(bytes) + " bytes failed");
-        }
-    }
-    ~TmpBuf() {
-        if (p) cudaFree(p);
-    }
-    template <typename T>
-    T* as() { return (T*)p; }
-};
 
 static inline int grid_for(int64_t n, int threads) {
     int64_t g = (n + threads - 1) / threads;

@@ -28,6 +28,14 @@
 
 namespace mpet {
 
+// True if `bytes` more can be allocated while a fifth of the device memory
+// stays free (room for the AMG hierarchies and work vectors allocated later).
+bool device_fits(mpet_ctx* c, size_t bytes) {
+    size_t free_b = 0, total_b = 0;
+    MPET_CUDA(cudaMemGetInfo(&free_b, &total_b));
+    return free_b > bytes && free_b - bytes >= total_b / 5;
+}
+
 static inline int grid_for(int64_t n, int threads) {
     int64_t g = (n + threads - 1) / threads;
     if (g > 2147483647LL) g = 2147483647LL;
@@ -477,11 +485,11 @@ __global__ void __launch_bounds__(256) k_spmv_nb(int64_t nnodes, int64_t nv, int
 // Copies the CSR values into the node-block layout (thread per slice lane).
 // A row group's CSR row holds its node columns (3 per node, n2 order) and
 // then, network-major, its vertex columns (n1 order).
-template <typename T>
+template <typename T, typename Tin>
 __global__ void k_nb_fill(int64_t nnodes, int64_t nv, int64_t Nu, int J, int64_t nsu, int64_t ns,
                           const NbSlice* __restrict__ sl, const int32_t* __restrict__ perm,
                           const int64_t* __restrict__ rp,
-                          const T* __restrict__ v, const int64_t* __restrict__ n2_ptr,
+                          const Tin* __restrict__ v, const int64_t* __restrict__ n2_ptr,
                           const int32_t* __restrict__ n2_col, const int64_t* __restrict__ n1_ptr,
                           const int32_t* __restrict__ n1_col, int32_t* cols, T* vals, int write_cols) {
     const int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
@@ -504,7 +512,7 @@ __global__ void k_nb_fill(int64_t nnodes, int64_t nv, int64_t Nu, int J, int64_t
         for (int r = 0; r < R; ++r) {
             const int64_t e = real ? row_start(r) + 3 * k : 0;
             for (int cc = 0; cc < 3; ++cc)
-                vals[S.voff + ((int64_t)k * B2 + r * 3 + cc) * 32 + lane] = real ? v[e + cc] : T(0);
+                vals[S.voff + ((int64_t)k * B2 + r * 3 + cc) * 32 + lane] = real ? (T)v[e + cc] : T(0);
         }
     }
     const int64_t c1 = S.coff + (int64_t)S.w2 * 32, v1 = S.voff + (int64_t)S.w2 * B2 * 32;
@@ -515,7 +523,7 @@ __global__ void k_nb_fill(int64_t nnodes, int64_t nv, int64_t Nu, int J, int64_t
         for (int r = 0; r < R; ++r) {
             const int64_t base = real ? row_start(r) + 3 * d2 + m : 0;
             for (int b = 0; b < J; ++b)
-                vals[v1 + ((int64_t)m * B1 + r * J + b) * 32 + lane] = real ? v[base + (int64_t)b * d1] : T(0);
+                vals[v1 + ((int64_t)m * B1 + r * J + b) * 32 + lane] = real ? (T)v[base + (int64_t)b * d1] : T(0);
         }
     }
 }
@@ -759,6 +767,7 @@ void build_sell(mpet_ctx* c, Csr& A, bool fp32, bool with64) {
         acc += ws;
     }
     off[ns] = acc;
+    if (!device_fits(c, (size_t)acc * (4 + (fp32 ? 4 : 0) + ((!fp32 || with64) ? 8 : 0)))) return;
     A.nslices = ns;
     A.s_off = w;
     MPET_CUDA(cudaMemcpyAsync(A.s_off, off.data(), sizeof(int64_t) * (ns + 1), cudaMemcpyHostToDevice, c->stream));
@@ -826,6 +835,9 @@ void build_node_blocks(mpet_ctx* c) {
         coff += (int64_t)(w2 + w1) * 32;
         voff += (urow ? (int64_t)w2 * 9 + (int64_t)w1 * 3 * J : (int64_t)w2 * 3 * J + (int64_t)w1 * J * J) * 32;
     }
+    const bool mixed = c->prm.precision == MPET_PRECISION_MIXED;
+    const size_t need = (size_t)coff * 4 + (size_t)voff * (mixed ? 4 : 8) + perm.size() * 4;
+    if (!device_fits(c, need)) return;  // optional copy: skipped when HBM is short
     nb.ncols = coff;
     nb.nvals = voff;
     nb.nblocks = (p2[c->nnodes] - p2[0]) + (p1[c->nnodes] - p1[0]) + (p2[c->nv] - p2[0]) + (p1[c->nv] - p1[0]);
@@ -834,8 +846,9 @@ void build_node_blocks(mpet_ctx* c) {
     MPET_CUDA(cudaMemcpyAsync(nb.perm, perm.data(), sizeof(int32_t) * perm.size(), cudaMemcpyHostToDevice,
                               c->stream));
     nb.cols = c->pool.alloc<int32_t>(coff);
-    if (c->A.v32) nb.v32 = c->pool.alloc<float>(voff);
-    nb.v64 = c->pool.alloc<double>(voff);
+    if (mixed) nb.v32 = c->pool.alloc<float>(voff);
+    // FP64 values: the Krylov matrix of the FP64 path, the refinement residual's of the mixed path
+    if (!mixed || device_fits(c, (size_t)voff * 8)) nb.v64 = c->pool.alloc<double>(voff);
     MPET_CUDA(cudaMemcpyAsync(nb.sl, sl.data(), sizeof(NbSlice) * sl.size(), cudaMemcpyHostToDevice, c->stream));
     MPET_CUDA(cudaStreamSynchronize(c->stream));
     c->A.nb = &nb;
@@ -848,14 +861,21 @@ static void fill_node_blocks(mpet_ctx* c) {
     const int G = grid_for(ns * 32, 128);
     int first = 1;
     if (nb.v32) {
-        k_nb_fill<float><<<G, 128, 0, c->stream>>>(c->nnodes, c->nv, c->Nu, c->J, nb.nsu, ns, nb.sl, nb.perm,
-                                                   c->A.rp, c->A.v32, c->n2_ptr, c->n2_col, c->n1_ptr, c->n1_col,
-                                                   nb.cols, nb.v32, first);
+        // from the FP32 CSR values when they exist (same rounding as the CSR kernels), else from FP64
+        if (c->A.v32)
+            k_nb_fill<float, float><<<G, 128, 0, c->stream>>>(c->nnodes, c->nv, c->Nu, c->J, nb.nsu, ns, nb.sl,
+                                                              nb.perm, c->A.rp, c->A.v32, c->n2_ptr, c->n2_col,
+                                                              c->n1_ptr, c->n1_col, nb.cols, nb.v32, first);
+        else
+            k_nb_fill<float, double><<<G, 128, 0, c->stream>>>(c->nnodes, c->nv, c->Nu, c->J, nb.nsu, ns, nb.sl,
+                                                               nb.perm, c->A.rp, c->A.v64, c->n2_ptr, c->n2_col,
+                                                               c->n1_ptr, c->n1_col, nb.cols, nb.v32, first);
         first = 0;
     }
-    k_nb_fill<double><<<G, 128, 0, c->stream>>>(c->nnodes, c->nv, c->Nu, c->J, nb.nsu, ns, nb.sl, nb.perm,
-                                                c->A.rp, c->A.v64, c->n2_ptr, c->n2_col, c->n1_ptr, c->n1_col,
-                                                nb.cols, nb.v64, first);
+    if (nb.v64)
+        k_nb_fill<double, double><<<G, 128, 0, c->stream>>>(c->nnodes, c->nv, c->Nu, c->J, nb.nsu, ns, nb.sl,
+                                                            nb.perm, c->A.rp, c->A.v64, c->n2_ptr, c->n2_col,
+                                                            c->n1_ptr, c->n1_col, nb.cols, nb.v64, first);
     MPET_CHECK_LAUNCH();
 }
 
@@ -1027,6 +1047,12 @@ static void autotune_matrix(mpet_ctx* c, Csr& A, const T* x, const Epi& epi, dou
 
 void autotune_system(mpet_ctx* c) {
     MPET_CUDA(cudaMemsetAsync(c->kv, 0, sizeof(double) * c->N, c->stream));
+    if (c->prm.precision == MPET_PRECISION_MIXED && !c->A.v32) {
+        // no FP32 CSR copy (HBM short): the node-block copy is the only FP32 matrix
+        if (!(c->A.nb && c->A.nb->v32)) fail(MPET_ERR_NOMEM, "no room for an FP32 copy of the system matrix");
+        c->A.variant = 8;
+        return;
+    }
     if (c->A.v32)
         autotune_matrix<float, 1>(c, c->A, (const float*)c->kv, EpiStore<float, 1>{(float*)c->kd},
                                   c->spmv_variant_ms);
@@ -1317,19 +1343,47 @@ __global__ void k_unpack43(int64_t nodes, const T* __restrict__ b4, T* a) {
     a[3 * i + 2] = v[2];
 }
 
-// Block-diagonal preconditioner z = M^-1 r.  The J pressure V-cycles are
-// forked onto side streams and run concurrently with the displacement
-// V-cycle on the main stream (inside a CUDA graph capture they become
-// parallel branches); the main stream joins them at the end.
+// rt_k = sum_a Q_ak r_a (fwd) or z_a = sum_k Q_ak zt_k (back) at every vertex,
+// with the Q of the vertex's instance
+template <typename T, bool FWD>
+__global__ void k_modes(int64_t nv, int J, const int32_t* __restrict__ vinst, const double* __restrict__ Q,
+                        const T* __restrict__ in, T* out) {
+    const int64_t v = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    if (v >= nv) return;
+    const double* q = Q + (vinst ? (int64_t)vinst[v] : 0) * J * J;
+    T a_in[MPET_MAX_NETWORKS];
+    for (int a = 0; a < J; ++a) a_in[a] = in[(int64_t)a * nv + v];
+    for (int k = 0; k < J; ++k) {
+        T s = T(0);
+        for (int a = 0; a < J; ++a) s += (T)(FWD ? q[a * J + k] : q[k * J + a]) * a_in[a];
+        out[(int64_t)k * nv + v] = s;
+    }
+}
+
+// Block-diagonal preconditioner z = M^-1 r.  The J pressure V-cycles (on the
+// networks, or on the network eigenmodes between two vertex-wise
+// transforms) are forked onto side streams and run concurrently with the
+// displacement V-cycle on the main stream (inside a CUDA graph capture they
+// become parallel branches); the main stream joins them at the end.
 template <typename T>
 static void precond(mpet_ctx* c, const T* r, T* z) {
     cudaStream_t main = c->stream;
+    const T* rp = r + c->Nu;
+    T* zp = z + c->Nu;
+    if (c->net_modes) {
+        k_modes<T, true><<<grid_for(c->nv, 256), 256, 0, main>>>(c->nv, c->J, c->vert_inst, c->mode_Q, rp,
+                                                                 (T*)c->mode_r);
+        MPET_CHECK_LAUNCH();
+        c->n_launch++;
+        rp = (const T*)c->mode_r;
+        zp = (T*)c->mode_z;
+    }
     MPET_CUDA(cudaEventRecord(c->ev_fork, main));
     for (int a = 0; a < c->J; ++a) {
         MPET_CUDA(cudaStreamWaitEvent(c->side[a], c->ev_fork, 0));
         c->stream = c->side[a];
-        const int64_t off = c->Nu + (int64_t)a * c->nv;
-        vcycle<T, 1>(c, c->amg_p[a], 0, r + off, z + off);
+        const int64_t off = (int64_t)a * c->nv;
+        vcycle<T, 1>(c, c->amg_p[a], 0, rp + off, zp + off);
         MPET_CUDA(cudaEventRecord(c->ev_join[a], c->side[a]));
     }
     c->stream = main;
@@ -1343,6 +1397,12 @@ static void precond(mpet_ctx* c, const T* r, T* z) {
     MPET_CHECK_LAUNCH();
     c->n_launch += 2;
     for (int a = 0; a < c->J; ++a) MPET_CUDA(cudaStreamWaitEvent(main, c->ev_join[a], 0));
+    if (c->net_modes) {
+        k_modes<T, false><<<grid_for(c->nv, 256), 256, 0, main>>>(c->nv, c->J, c->vert_inst, c->mode_Q,
+                                                                  (const T*)c->mode_z, z + c->Nu);
+        MPET_CHECK_LAUNCH();
+        c->n_launch++;
+    }
 }
 
 // ---- MINRES ----------------------------------------------------------------------------

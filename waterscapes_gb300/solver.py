@@ -133,7 +133,8 @@ class MPETSolver:
                 "direct_solver": True,
                 "precision": "mixed", "rtol": 1e-10, "inner_rtol": 1e-4, "maxit": 20000,
                 "max_outer": 40, "amg_theta": 0.1, "amg_cheb_degree": 4, "amg_coarse_size": 500,
-                "amg_p2_to_p1": True, "prec_u_weight": "mu+lmbda", "check_every": 4, "device": 0}
+                "amg_p2_to_p1": True, "prec_u_weight": "mu+lmbda", "prec_network_modes": True,
+                "check_every": 4, "device": 0}
 
     def _make_params(self):
         pp = self.problem.params
@@ -163,6 +164,7 @@ class MPETSolver:
         prm.amg_p2_to_p1 = 1 if self.params["amg_p2_to_p1"] else 0
         w = self.params["prec_u_weight"]
         prm.prec_u_weight = (mu + lmbda) if w == "mu+lmbda" else (mu if w == "mu" else float(w))
+        prm.prec_network_modes = 1 if self.params["prec_network_modes"] else 0
         return prm
 
     def _check_facet_data(self):
