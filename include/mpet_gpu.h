@@ -105,6 +105,16 @@ int mpet_mesh_upload(mpet_ctx* ctx, int64_t nv, const double* xyz_host, int64_t 
                      const int32_t* tets_host, int64_t nf, const int32_t* bfacets_host,
                      const int32_t* markers_host, int32_t num_networks);
 
+/* The same for dim = 2 (triangles: cells nc x 3, boundary facets nf x 2
+ * segments; coordinates still nv x 3 with z ignored) or dim = 3.  In 2D the
+ * displacement has 2 components per P2 node (DOF 2*i + k) and every
+ * assembly, boundary-term and solve entry point works as in 3D, as in the
+ * reference's 2D tests (test_convergence_mpetsolver.py); batches and the
+ * adjoint are built for tetrahedra only (MPET_ERR_INVALID in 2D). */
+int mpet_mesh_upload_dim(mpet_ctx* ctx, int32_t dim, int64_t nv, const double* xyz_host, int64_t nc,
+                         const int32_t* cells_host, int64_t nf, const int32_t* bfacets_host,
+                         const int32_t* markers_host, int32_t num_networks);
+
 /* Dofmap, CSR sparsity pattern and Dirichlet DOF lists, built on the GPU.
  * Replaces create_function_spaces (mpetsolver.py:100-132), DOLFIN's
  * SparsityPatternBuilder used by assemble(self.a) (mpetsolver.py:335) and

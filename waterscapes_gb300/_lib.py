@@ -85,6 +85,7 @@ SIGNATURES = {
     "mpet_set_stream": [_P, _P],
     "mpet_synchronize": [_P],
     "mpet_mesh_upload": [_P, _I64, _P, _I64, _P, _I64, _P, _P, _I32],
+    "mpet_mesh_upload_dim": [_P, _I32, _I64, _P, _I64, _P, _I64, _P, _P, _I32],
     "mpet_setup": [_P, ctypes.POINTER(MpetParams)],
     "mpet_update_params": [_P, ctypes.POINTER(MpetParams)],
     "mpet_get_sizes": [_P, ctypes.POINTER(_I64), ctypes.POINTER(_I64), ctypes.POINTER(_I64), ctypes.POINTER(_I64)],

@@ -103,39 +103,47 @@ int mpet_synchronize(mpet_ctx* c) {
     API_END(c)
 }
 
-int mpet_mesh_upload(mpet_ctx* c, int64_t nv, const double* xyz, int64_t nc, const int32_t* tets, int64_t nf,
-                     const int32_t* bfacets, const int32_t* markers, int32_t J) {
+int mpet_mesh_upload_dim(mpet_ctx* c, int32_t dim, int64_t nv, const double* xyz, int64_t nc, const int32_t* cells,
+                         int64_t nf, const int32_t* bfacets, const int32_t* markers, int32_t J) {
     API_BEGIN(c)
     require(!c->mesh_ready, MPET_ERR_STATE, "mesh already uploaded to this context");
-    require(nv > 0 && nc > 0 && nf >= 0 && xyz && tets, MPET_ERR_INVALID, "empty mesh");
+    require(dim == 2 || dim == 3, MPET_ERR_INVALID, "dim must be 2 (triangles) or 3 (tetrahedra)");
+    require(nv > 0 && nc > 0 && nf >= 0 && xyz && cells, MPET_ERR_INVALID, "empty mesh");
     require(J >= 1 && J <= MPET_MAX_NETWORKS, MPET_ERR_INVALID, "num_networks must be in 1..8");
     require(nf == 0 || (bfacets && markers), MPET_ERR_INVALID, "facets without markers");
     require(nv < 2147483647LL / 4, MPET_ERR_INVALID, "too many vertices");
-    for (int64_t i = 0; i < 4 * nc; ++i)
-        require(tets[i] >= 0 && tets[i] < nv, MPET_ERR_INVALID, "cell vertex index out of range");
-    for (int64_t i = 0; i < 3 * nf; ++i)
+    const int cv = dim + 1;
+    for (int64_t i = 0; i < cv * nc; ++i)
+        require(cells[i] >= 0 && cells[i] < nv, MPET_ERR_INVALID, "cell vertex index out of range");
+    for (int64_t i = 0; i < dim * nf; ++i)
         require(bfacets[i] >= 0 && bfacets[i] < nv, MPET_ERR_INVALID, "facet vertex index out of range");
     // cells with ascending vertex ids (DOLFIN's ordered-mesh convention)
-    std::vector<int32_t> sorted(tets, tets + 4 * nc);
-    for (int64_t k = 0; k < nc; ++k) std::sort(sorted.begin() + 4 * k, sorted.begin() + 4 * k + 4);
+    std::vector<int32_t> sorted(cells, cells + cv * nc);
+    for (int64_t k = 0; k < nc; ++k) std::sort(sorted.begin() + cv * k, sorted.begin() + cv * k + cv);
+    c->dim = dim;
     c->nv = nv;
     c->nc = nc;
     c->nf = nf;
     c->J = J;
     c->x = c->pool.alloc<double>(3 * nv);
-    c->cells = c->pool.alloc<int32_t>(4 * nc);
-    c->bfacets = c->pool.alloc<int32_t>(3 * (nf > 0 ? nf : 1));
+    c->cells = c->pool.alloc<int32_t>(cv * nc);
+    c->bfacets = c->pool.alloc<int32_t>(dim * (nf > 0 ? nf : 1));
     c->markers = c->pool.alloc<int32_t>((1 + J) * (nf > 0 ? nf : 1));
     MPET_CUDA(cudaMemcpyAsync(c->x, xyz, sizeof(double) * 3 * nv, cudaMemcpyHostToDevice, c->stream));
-    MPET_CUDA(cudaMemcpyAsync(c->cells, sorted.data(), sizeof(int32_t) * 4 * nc, cudaMemcpyHostToDevice, c->stream));
+    MPET_CUDA(cudaMemcpyAsync(c->cells, sorted.data(), sizeof(int32_t) * cv * nc, cudaMemcpyHostToDevice, c->stream));
     if (nf > 0) {
-        MPET_CUDA(cudaMemcpyAsync(c->bfacets, bfacets, sizeof(int32_t) * 3 * nf, cudaMemcpyHostToDevice, c->stream));
+        MPET_CUDA(cudaMemcpyAsync(c->bfacets, bfacets, sizeof(int32_t) * dim * nf, cudaMemcpyHostToDevice, c->stream));
         MPET_CUDA(cudaMemcpyAsync(c->markers, markers, sizeof(int32_t) * (1 + J) * nf, cudaMemcpyHostToDevice,
                                   c->stream));
     }
     MPET_CUDA(cudaStreamSynchronize(c->stream));
     c->mesh_ready = true;
     API_END(c)
+}
+
+int mpet_mesh_upload(mpet_ctx* c, int64_t nv, const double* xyz, int64_t nc, const int32_t* tets, int64_t nf,
+                     const int32_t* bfacets, const int32_t* markers, int32_t J) {
+    return mpet_mesh_upload_dim(c, 3, nv, xyz, nc, tets, nf, bfacets, markers, J);
 }
 
 static void check_params(const mpet_ctx* c, const mpet_params* p) {
@@ -255,12 +263,12 @@ int mpet_get_bc_count(mpet_ctx* c, int32_t field, int64_t* count) {
     API_END(c)
 }
 
-__global__ void k_bc_coords(const int32_t* __restrict__ dofs, int64_t n, int64_t Nu, int64_t nv,
+__global__ void k_bc_coords(const int32_t* __restrict__ dofs, int64_t n, int64_t Nu, int64_t nv, int dim,
                             const double* __restrict__ x, const int64_t* __restrict__ ekey, double* coords) {
     int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
     if (i >= n) return;
     int64_t d = dofs[i];
-    int64_t node = d < Nu ? d / 3 : (d - Nu) % nv;
+    int64_t node = d < Nu ? d / dim : (d - Nu) % nv;
     for (int k = 0; k < 3; ++k) {
         double v;
         if (node < nv) {
@@ -282,7 +290,7 @@ int mpet_get_bc(mpet_ctx* c, int32_t field, int32_t* dofs, double* coords) {
         if (dofs)
             MPET_CUDA(cudaMemcpyAsync(dofs, c->bc_dofs + off, sizeof(int32_t) * n, cudaMemcpyDeviceToDevice, c->stream));
         if (coords) {
-            k_bc_coords<<<(int)((n + 255) / 256), 256, 0, c->stream>>>(c->bc_dofs + off, n, c->Nu, c->nv, c->x,
+            k_bc_coords<<<(int)((n + 255) / 256), 256, 0, c->stream>>>(c->bc_dofs + off, n, c->Nu, c->nv, c->dim, c->x,
                                                                         c->edge_key, coords);
             MPET_CHECK_LAUNCH();
         }
@@ -335,6 +343,7 @@ int mpet_set_cell_coefficients(mpet_ctx* c, const double* c_cells, const double*
 int mpet_set_batch(mpet_ctx* c, int32_t ninst, const int32_t* vertex_instance) {
     API_BEGIN(c)
     require(c->setup_done, MPET_ERR_STATE, "mpet_setup must come first");
+    require(c->dim == 3, MPET_ERR_INVALID, "batches are built for tetrahedral meshes");
     require(c->ninst == 0, MPET_ERR_STATE, "the batch partition is already set");
     require(ninst >= 1 && vertex_instance, MPET_ERR_INVALID, "need ninst >= 1 and an instance per vertex");
     setup_batch(c, ninst, vertex_instance);
@@ -616,6 +625,7 @@ int mpet_get_timing(mpet_ctx* c, double* inner_ms, int64_t* inner_iterations, do
 int mpet_pressure_misfit(mpet_ctx* c, const double* up, const double* p_target, double* loss, double* dloss) {
     API_BEGIN(c)
     require(c->setup_done, MPET_ERR_STATE, "mpet_setup must come first");
+    require(c->dim == 3, MPET_ERR_INVALID, "the adjoint is built for tetrahedral meshes");
     require(up && p_target && loss, MPET_ERR_INVALID, "NULL argument");
     if (!c->adj_loss) c->adj_loss = c->pool.alloc<double>(1);
     launch_misfit(c, up, p_target, dloss, c->adj_loss);
@@ -625,6 +635,7 @@ int mpet_pressure_misfit(mpet_ctx* c, const double* up, const double* p_target, 
 }
 
 static void require_adjoint_ok(mpet_ctx* c) {
+    require(c->dim == 3, MPET_ERR_INVALID, "the adjoint is built for tetrahedral meshes");
     require(!(c->prm.theta < 1.0 && (c->f_beta || c->f_beta_matrix)), MPET_ERR_INVALID,
             "Robin terms are not differentiated for theta < 1");
 }

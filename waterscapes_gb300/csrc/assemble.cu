@@ -23,8 +23,6 @@
 
 namespace mpet {
 
-__constant__ int c_edges[6][2] = {{2, 3}, {1, 3}, {1, 2}, {0, 3}, {0, 2}, {0, 1}};
-
 // int phi_i phi_j / |T| for P2 on a tetrahedron, times 420.
 __constant__ double c_m2[10][10] = {
     {6, 1, 1, 1, -6, -6, -6, -4, -4, -4},     {1, 6, 1, 1, -6, -4, -4, -6, -6, -4},
@@ -32,6 +30,13 @@ __constant__ double c_m2[10][10] = {
     {-6, -6, -4, -4, 32, 16, 16, 16, 16, 8},  {-6, -4, -6, -4, 16, 32, 16, 16, 8, 16},
     {-6, -4, -4, -6, 16, 16, 32, 8, 16, 16},  {-4, -6, -6, -4, 16, 16, 8, 32, 16, 16},
     {-4, -6, -4, -6, 16, 8, 16, 16, 32, 16},  {-4, -4, -6, -6, 8, 16, 16, 16, 16, 32}};
+// int phi_i phi_j / |T| for P2 on a triangle, times 180 (vertices, then edges (1,2), (0,2), (0,1)).
+__constant__ double c_m2t[6][6] = {{6, -1, -1, -4, 0, 0},  {-1, 6, -1, 0, -4, 0},  {-1, -1, 6, 0, 0, -4},
+                                   {-4, 0, 0, 32, 16, 16}, {0, -4, 0, 16, 32, 16}, {0, 0, -4, 16, 16, 32}};
+
+// int lambda_r lambda_s / |T| = (1 + delta_rs) * KAPPA(D), KAPPA = d! / (d + 2)!
+template <int D>
+__host__ __device__ constexpr double kappa() { return D == 3 ? 1.0 / 20.0 : 1.0 / 12.0; }
 
 struct MatCoef {
     double mu, lmbda, dt_theta;
@@ -71,21 +76,24 @@ __device__ __forceinline__ void load_geo(const double* __restrict__ geo, int64_t
     G.vol = g[12];
 }
 
-// g_{j,r} (value of grad phi_j at vertex r) for all r, and s_j.
+// g_{j,r} (value of grad phi_j at vertex r) for all r, and s_j = sum_r g_{j,r}
+// (zero for a vertex of a tetrahedron, grad lambda_j for a vertex of a triangle).
+template <int D = 3>
 __device__ __forceinline__ void p2_grad_table(const Geo& G, int j, double g[4][3], double s[3]) {
-    if (j < 4) {
+    constexpr int NV = Simplex<D>::NV;
+    if (j < NV) {
 #pragma unroll
-        for (int r = 0; r < 4; ++r) {
+        for (int r = 0; r < NV; ++r) {
             double f = (r == j) ? 3.0 : -1.0;
 #pragma unroll
             for (int k = 0; k < 3; ++k) g[r][k] = f * G.b[j][k];
         }
 #pragma unroll
-        for (int k = 0; k < 3; ++k) s[k] = 0.0;
+        for (int k = 0; k < 3; ++k) s[k] = D == 3 ? 0.0 : G.b[j][k];
     } else {
-        int ea = c_edges[j - 4][0], eb = c_edges[j - 4][1];
+        int ea = edge_end<D>(j - NV, 0), eb = edge_end<D>(j - NV, 1);
 #pragma unroll
-        for (int r = 0; r < 4; ++r)
+        for (int r = 0; r < NV; ++r)
 #pragma unroll
             for (int k = 0; k < 3; ++k)
                 g[r][k] = (r == ea ? 4.0 * G.b[eb][k] : 0.0) + (r == eb ? 4.0 * G.b[ea][k] : 0.0);
@@ -95,16 +103,18 @@ __device__ __forceinline__ void p2_grad_table(const Geo& G, int j, double g[4][3
 }
 
 // value of grad phi_j at vertex r, plus s_j
+template <int D = 3>
 __device__ __forceinline__ void p2_grad_at(const Geo& G, int j, int r, double g[3], double s[3]) {
-    if (j < 4) {
+    constexpr int NV = Simplex<D>::NV;
+    if (j < NV) {
         double f = (r == j) ? 3.0 : -1.0;
 #pragma unroll
         for (int k = 0; k < 3; ++k) {
             g[k] = f * G.b[j][k];
-            s[k] = 0.0;
+            s[k] = D == 3 ? 0.0 : G.b[j][k];
         }
     } else {
-        int ea = c_edges[j - 4][0], eb = c_edges[j - 4][1];
+        int ea = edge_end<D>(j - NV, 0), eb = edge_end<D>(j - NV, 1);
 #pragma unroll
         for (int k = 0; k < 3; ++k) {
             g[k] = (r == ea ? 4.0 * G.b[eb][k] : 0.0) + (r == eb ? 4.0 * G.b[ea][k] : 0.0);
@@ -141,7 +151,15 @@ struct AsmArgs {
     int apply_bc;
 };
 
+// Task layout of one (node, cell) pair over the warp's lanes: NN*D
+// displacement-displacement entries (node j, component k), D*NV
+// displacement-pressure couplings (k, vertex w), and for a vertex node
+// NN*D pressure-displacement couplings (j, l) and NV pressure-pressure
+// entries (w): 30/42/72/76 on tetrahedra, 12/18/30/33 on triangles.
+template <int D>
 __global__ void __launch_bounds__(256) k_assemble_matrix(AsmArgs A, MatCoef P) {
+    constexpr int NV = Simplex<D>::NV, NN = Simplex<D>::NN;
+    constexpr int T1 = NN * D, T2 = T1 + D * NV, T3 = T2 + NN * D, T4 = T3 + NV;
     const int lane = threadIdx.x & 31;
     const int64_t warp = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) >> 5;
     const int64_t nwarps = ((int64_t)gridDim.x * blockDim.x) >> 5;
@@ -150,11 +168,11 @@ __global__ void __launch_bounds__(256) k_assemble_matrix(AsmArgs A, MatCoef P) {
         const bool isv = i < A.nv;
         const int64_t s2 = A.n2_ptr[i], s1 = A.n1_ptr[i];
         const int d2 = (int)(A.n2_ptr[i + 1] - s2), d1 = (int)(A.n1_ptr[i + 1] - s1);
-        const int L = 3 * d2 + J * d1;
-        const int nrows = 3 + (isv ? J : 0);
+        const int L = D * d2 + J * d1;
+        const int nrows = D + (isv ? J : 0);
         int64_t rows[3 + MPET_MAX_NETWORKS];
-        for (int k = 0; k < 3; ++k) rows[k] = 3 * i + k;
-        for (int a = 0; a < J; ++a) rows[3 + a] = A.Nu + (int64_t)a * A.nv + i;
+        for (int k = 0; k < D; ++k) rows[k] = D * i + k;
+        for (int a = 0; a < J; ++a) rows[D + a] = A.Nu + (int64_t)a * A.nv + i;
         int64_t rp[3 + MPET_MAX_NETWORKS];
         for (int q = 0; q < nrows; ++q) rp[q] = A.row_ptr[rows[q]];
         for (int q = 0; q < nrows; ++q)
@@ -167,51 +185,53 @@ __global__ void __launch_bounds__(256) k_assemble_matrix(AsmArgs A, MatCoef P) {
             Geo G;
             load_geo(A.geo, cell, G);
             double gm[4][3], sm[3];
-            p2_grad_table(G, m, gm, sm);
-            const double w20 = G.vol * (1.0 / 20.0);
-            const uint16_t* rk2 = A.rank2 + cell * 100 + m * 10;
-            const uint16_t* rk1 = A.rank1 + cell * 40 + m * 4;
-            const int ntask = isv ? 76 : 42;
+            p2_grad_table<D>(G, m, gm, sm);
+            const double w20 = G.vol * kappa<D>();
+            const uint16_t* rk2 = A.rank2 + cell * (NN * NN) + m * NN;
+            const uint16_t* rk1 = A.rank1 + cell * (NN * NV) + m * NV;
+            const int ntask = isv ? T4 : T2;
             for (int t = lane; t < ntask; t += 32) {
-                if (t < 30) {
-                    const int j = t / 3, k = t % 3;
+                if (t < T1) {
+                    const int j = t / D, k = t % D;
                     double gj[4][3], sj[3];
-                    p2_grad_table(G, j, gj, sj);
+                    p2_grad_table<D>(G, j, gj, sj);
                     double M[3][3];
 #pragma unroll
-                    for (int a = 0; a < 3; ++a)
+                    for (int a = 0; a < D; ++a)
 #pragma unroll
-                        for (int b = 0; b < 3; ++b) {
+                        for (int b = 0; b < D; ++b) {
                             double acc = sm[a] * sj[b];
 #pragma unroll
-                            for (int r = 0; r < 4; ++r) acc += gm[r][a] * gj[r][b];
+                            for (int r = 0; r < NV; ++r) acc += gm[r][a] * gj[r][b];
                             M[a][b] = w20 * acc;
                         }
-                    const double tr = M[0][0] + M[1][1] + M[2][2];
-                    const int64_t base = rp[k] + 3 * (int64_t)rk2[j];
+                    double tr = 0.0;
 #pragma unroll
-                    for (int l = 0; l < 3; ++l) {
+                    for (int a = 0; a < D; ++a) tr += M[a][a];
+                    const int64_t base = rp[k] + D * (int64_t)rk2[j];
+#pragma unroll
+                    for (int l = 0; l < D; ++l) {
                         double v = P.mu * M[l][k] + P.lmbda * M[k][l];
                         if (l == k) v += P.mu * tr;
                         A.v64[base + l] += v;
                     }
-                } else if (t < 42) {
-                    const int tt = t - 30, k = tt / 4, w = tt % 4;
+                } else if (t < T2) {
+                    const int tt = t - T1, k = tt / NV, w = tt % NV;
                     const double C = w20 * (gm[w][k] + sm[k]);
-                    const int64_t base = rp[k] + 3 * (int64_t)d2 + rk1[w];
+                    const int64_t base = rp[k] + D * (int64_t)d2 + rk1[w];
                     for (int a = 0; a < J; ++a) A.v64[base + (int64_t)a * d1] += -P.alpha[a] * C;
-                } else if (t < 72) {
-                    const int tt = t - 42, j = tt / 3, l = tt % 3;
+                } else if (t < T3) {
+                    const int tt = t - T2, j = tt / D, l = tt % D;
                     double g[3], s[3];
-                    p2_grad_at(G, j, m, g, s);
+                    p2_grad_at<D>(G, j, m, g, s);
                     const double C = w20 * (g[l] + s[l]);
-                    for (int a = 0; a < J; ++a) A.v64[rp[3 + a] + 3 * (int64_t)rk2[j] + l] += -P.alpha[a] * C;
+                    for (int a = 0; a < J; ++a) A.v64[rp[D + a] + D * (int64_t)rk2[j] + l] += -P.alpha[a] * C;
                 } else {
-                    const int w = t - 72;
+                    const int w = t - T3;
                     const double M1 = w20 * (m == w ? 2.0 : 1.0);
                     const double L1 = G.vol * (G.b[m][0] * G.b[w][0] + G.b[m][1] * G.b[w][1] + G.b[m][2] * G.b[w][2]);
                     for (int a = 0; a < J; ++a) {
-                        const int64_t base = rp[3 + a] + 3 * (int64_t)d2 + rk1[w];
+                        const int64_t base = rp[D + a] + D * (int64_t)d2 + rk1[w];
                         for (int b = 0; b < J; ++b) {
                             double v = -P.dt_theta * ((a == b ? P.Ssumof(a, cell) : 0.0) - P.Sof(a, b, cell)) * M1;
                             if (a == b) v += -P.cof(a, cell) * M1 - P.dt_theta * P.Kof(a, cell) * L1;
@@ -226,7 +246,7 @@ __global__ void __launch_bounds__(256) k_assemble_matrix(AsmArgs A, MatCoef P) {
         int self2 = lb_i32(A.n2_col + s2, d2, (int32_t)i);
         int self1 = isv ? lb_i32(A.n1_col + s1, d1, (int32_t)i) : 0;
         for (int q = 0; q < nrows; ++q) {
-            const int64_t dpos = q < 3 ? rp[q] + 3 * self2 + q : rp[q] + 3 * (int64_t)d2 + (int64_t)(q - 3) * d1 + self1;
+            const int64_t dpos = q < D ? rp[q] + D * self2 + q : rp[q] + D * (int64_t)d2 + (int64_t)(q - D) * d1 + self1;
             if (A.apply_bc && A.dof_bc[rows[q]]) {
                 for (int e = lane; e < L; e += 32) A.v64[rp[q] + e] = 0.0;
                 __syncwarp();
@@ -274,7 +294,9 @@ struct PrecArgs {
     const int32_t* cell_inst;
 };
 
+template <int D>
 __global__ void __launch_bounds__(256) k_assemble_prec(PrecArgs A, MatCoef P) {
+    constexpr int NV = Simplex<D>::NV, NN = Simplex<D>::NN;
     const int lane = threadIdx.x & 31;
     const int64_t warp = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) >> 5;
     const int64_t nwarps = ((int64_t)gridDim.x * blockDim.x) >> 5;
@@ -295,31 +317,31 @@ __global__ void __launch_bounds__(256) k_assemble_prec(PrecArgs A, MatCoef P) {
             const int m = packed & 15;
             Geo G;
             load_geo(A.geo, cell, G);
-            const double w20 = G.vol * (1.0 / 20.0);
-            const int ntask = isv ? 14 : 10;
+            const double w20 = G.vol * kappa<D>();
+            const int ntask = isv ? NN + NV : NN;
             for (int t = lane; t < ntask; t += 32) {
-                if (t < 10) {
+                if (t < NN) {
                     const int j = t;
-                    const int32_t nj = A.cell_nodes[10 * cell + j];
+                    const int32_t nj = A.cell_nodes[NN * cell + j];
                     if (rowbc || A.node_bc[nj]) continue;
                     double gm[4][3], sm[3], gj[4][3], sj[3];
-                    p2_grad_table(G, m, gm, sm);
-                    p2_grad_table(G, j, gj, sj);
+                    p2_grad_table<D>(G, m, gm, sm);
+                    p2_grad_table<D>(G, j, gj, sj);
                     double tr = 0.0;
 #pragma unroll
-                    for (int a = 0; a < 3; ++a) {
+                    for (int a = 0; a < D; ++a) {
                         double acc = sm[a] * sj[a];
 #pragma unroll
-                        for (int r = 0; r < 4; ++r) acc += gm[r][a] * gj[r][a];
+                        for (int r = 0; r < NV; ++r) acc += gm[r][a] * gj[r][a];
                         tr += acc;
                     }
-                    A.lu[s2 + A.rank2[cell * 100 + m * 10 + j]] += P.prec_mu * w20 * tr;
+                    A.lu[s2 + A.rank2[cell * (NN * NN) + m * NN + j]] += P.prec_mu * w20 * tr;
                 } else {
-                    const int w = t - 10;
-                    const int32_t vw = A.cells[4 * cell + w];
+                    const int w = t - NN;
+                    const int32_t vw = A.cells[NV * cell + w];
                     const double M1 = w20 * (m == w ? 2.0 : 1.0);
                     const double L1 = G.vol * (G.b[m][0] * G.b[w][0] + G.b[m][1] * G.b[w][1] + G.b[m][2] * G.b[w][2]);
-                    const int64_t pos = s1 + A.rank1[cell * 40 + m * 4 + w];
+                    const int64_t pos = s1 + A.rank1[cell * (NN * NV) + m * NV + w];
                     if (A.mQ) {
                         // mode k: lambda_k M + dt theta (sum_a Q_ak^2 K_a) L  (Dirichlet sets equal for all networks)
                         if (A.vert_bc[i] || A.vert_bc[vw]) continue;
@@ -374,8 +396,9 @@ struct RhsArgs {
 //   + dt (1-theta) [K_a (grad p_a^n, grad q) + sum_b S_ab (p_a^n - p_b^n, q)] + dt (g_a, q).
 // ADJ: the pressure rows of B^T lam for the old-state operator B of those
 // rows (no displacement or source term, S transposed).
-template <bool ADJ>
+template <int D, bool ADJ>
 __global__ void __launch_bounds__(128) k_rhs_p(RhsArgs A, MatCoef P) {
+    constexpr int NV = Simplex<D>::NV, NN = Simplex<D>::NN;
     const int64_t v = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
     if (v >= A.nv) return;
     const int J = P.J;
@@ -388,19 +411,23 @@ __global__ void __launch_bounds__(128) k_rhs_p(RhsArgs A, MatCoef P) {
         const int m = packed & 15;
         Geo G;
         load_geo(A.geo, cell, G);
-        const double w20 = G.vol * (1.0 / 20.0);
+        const double w20 = G.vol * kappa<D>();
         double cp = 0.0;
-        for (int j = 0; j < (ADJ ? 0 : 10); ++j) {
+        for (int j = 0; j < (ADJ ? 0 : NN); ++j) {
             double g[3], s[3];
-            p2_grad_at(G, j, m, g, s);
-            const int64_t nj = A.cell_nodes[10 * cell + j];
-            cp += (g[0] + s[0]) * A.up[3 * nj] + (g[1] + s[1]) * A.up[3 * nj + 1] + (g[2] + s[2]) * A.up[3 * nj + 2];
+            p2_grad_at<D>(G, j, m, g, s);
+            const int64_t nj = A.cell_nodes[NN * cell + j];
+            if (D == 3)
+                cp += (g[0] + s[0]) * A.up[3 * nj] + (g[1] + s[1]) * A.up[3 * nj + 1] +
+                      (g[2] + s[2]) * A.up[3 * nj + 2];
+            else
+                cp += (g[0] + s[0]) * A.up[2 * nj] + (g[1] + s[1]) * A.up[2 * nj + 1];
         }
         cp *= w20;
         double M1[4], L1[4];
         int32_t vw[4];
-        for (int w = 0; w < 4; ++w) {
-            vw[w] = A.cells[4 * cell + w];
+        for (int w = 0; w < NV; ++w) {
+            vw[w] = A.cells[NV * cell + w];
             M1[w] = w20 * (m == w ? 2.0 : 1.0);
             L1[w] = G.vol * (G.b[m][0] * G.b[w][0] + G.b[m][1] * G.b[w][1] + G.b[m][2] * G.b[w][2]);
         }
@@ -408,7 +435,7 @@ __global__ void __launch_bounds__(128) k_rhs_p(RhsArgs A, MatCoef P) {
         for (int a = 0; a < J; ++a) {
             const double* pa = A.up + A.Nu + (int64_t)a * A.nv;
             double sm = 0.0, sl = 0.0, sg = 0.0;
-            for (int w = 0; w < 4; ++w) {
+            for (int w = 0; w < NV; ++w) {
                 sm += M1[w] * pa[vw[w]];
                 sl += L1[w] * pa[vw[w]];
                 if (!ADJ && A.g) sg += M1[w] * A.g[(int64_t)a * A.nv + vw[w]];
@@ -431,7 +458,9 @@ __global__ void __launch_bounds__(128) k_rhs_p(RhsArgs A, MatCoef P) {
 }
 
 // Displacement rows: (f, v) with f the P2 interpolant (L0, mpetsolver.py:233).
+template <int D>
 __global__ void __launch_bounds__(128) k_rhs_u(RhsArgs A) {
+    constexpr int NN = Simplex<D>::NN;
     const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
     if (i >= A.nnodes) return;
     double acc[3] = {0.0, 0.0, 0.0};
@@ -440,19 +469,15 @@ __global__ void __launch_bounds__(128) k_rhs_u(RhsArgs A) {
             const int32_t packed = A.inc[it];
             const int64_t cell = packed >> 4;
             const int m = packed & 15;
-            const double vol = A.geo[16 * cell + 12] * (1.0 / 420.0);
-            for (int j = 0; j < 10; ++j) {
-                const int64_t nj = A.cell_nodes[10 * cell + j];
-                const double w = vol * c_m2[m][j];
-                acc[0] += w * A.f[3 * nj];
-                acc[1] += w * A.f[3 * nj + 1];
-                acc[2] += w * A.f[3 * nj + 2];
+            const double vol = A.geo[16 * cell + 12] * (D == 3 ? 1.0 / 420.0 : 1.0 / 180.0);
+            for (int j = 0; j < NN; ++j) {
+                const int64_t nj = A.cell_nodes[NN * cell + j];
+                const double w = vol * (D == 3 ? c_m2[m][j] : c_m2t[m][j]);
+                for (int k = 0; k < D; ++k) acc[k] += w * A.f[D * nj + k];
             }
         }
     }
-    A.b[3 * i] = acc[0];
-    A.b[3 * i + 1] = acc[1];
-    A.b[3 * i + 2] = acc[2];
+    for (int k = 0; k < D; ++k) A.b[D * i + k] = acc[k];
 }
 
 __global__ void k_scatter_bc(const int32_t* __restrict__ dofs, const double* __restrict__ vals, int64_t n,
@@ -542,7 +567,8 @@ void launch_assemble_matrix(mpet_ctx* c, double dt, bool apply_bc, bool write32)
     int64_t warps_needed = c->nnodes;
     int blocks = grid_for(warps_needed * 32, 256);
     if (blocks > 152 * 64) blocks = 152 * 64;
-    k_assemble_matrix<<<blocks, 256, 0, c->stream>>>(A, P);
+    if (c->dim == 2) k_assemble_matrix<2><<<blocks, 256, 0, c->stream>>>(A, P);
+    else k_assemble_matrix<3><<<blocks, 256, 0, c->stream>>>(A, P);
     MPET_CHECK_LAUNCH();
 }
 
@@ -571,7 +597,8 @@ void launch_assemble_prec_blocks(mpet_ctx* c, double dt) {
     MatCoef P = make_coef(c, dt);
     int blocks = grid_for(c->nnodes * 32, 256);
     if (blocks > 152 * 64) blocks = 152 * 64;
-    k_assemble_prec<<<blocks, 256, 0, c->stream>>>(A, P);
+    if (c->dim == 2) k_assemble_prec<2><<<blocks, 256, 0, c->stream>>>(A, P);
+    else k_assemble_prec<3><<<blocks, 256, 0, c->stream>>>(A, P);
     MPET_CHECK_LAUNCH();
 }
 
@@ -592,8 +619,13 @@ void launch_rhs(mpet_ctx* c, double dt, const double* up_prev, double* b) {
     A.dt = dt;
     A.theta = c->prm.theta;
     MatCoef P = make_coef(c, dt);
-    k_rhs_u<<<grid_for(c->nnodes, 128), 128, 0, c->stream>>>(A);
-    k_rhs_p<false><<<grid_for(c->nv, 128), 128, 0, c->stream>>>(A, P);
+    if (c->dim == 2) {
+        k_rhs_u<2><<<grid_for(c->nnodes, 128), 128, 0, c->stream>>>(A);
+        k_rhs_p<2, false><<<grid_for(c->nv, 128), 128, 0, c->stream>>>(A, P);
+    } else {
+        k_rhs_u<3><<<grid_for(c->nnodes, 128), 128, 0, c->stream>>>(A);
+        k_rhs_p<3, false><<<grid_for(c->nv, 128), 128, 0, c->stream>>>(A, P);
+    }
     MPET_CHECK_LAUNCH();
     launch_facet_rhs(c, dt, up_prev, b);
     launch_bc_vector(c, b);
@@ -745,7 +777,7 @@ void launch_adjoint_rhs(mpet_ctx* c, double dt, const double* lam, double* out) 
     RhsArgs A = rhs_args(c, dt, lam, out);
     MatCoef P = make_coef(c, dt);
     k_adj_rhs_u<<<grid_for(c->nnodes, 128), 128, 0, c->stream>>>(A, P);
-    k_rhs_p<true><<<grid_for(c->nv, 128), 128, 0, c->stream>>>(A, P);
+    k_rhs_p<3, true><<<grid_for(c->nv, 128), 128, 0, c->stream>>>(A, P);
     MPET_CHECK_LAUNCH();
     launch_zero_bc_rows(c, out);
 }

@@ -27,6 +27,21 @@ __constant__ double c_fm2[6][6] = {{6, -1, -1, -4, 0, 0},  {-1, 6, -1, 0, -4, 0}
 __constant__ double c_ft1[3][3][3] = {{{6, 2, 2}, {2, 2, 1}, {2, 1, 2}},
                                       {{2, 2, 1}, {2, 6, 2}, {1, 2, 2}},
                                       {{2, 1, 2}, {1, 2, 2}, {2, 2, 6}}};
+// 2D boundary facets are segments: int phi_i phi_j / |F| for P2 (vertices, midpoint), times 30,
+// and int lambda_v lambda_w lambda_m / |F|, times 12
+__constant__ double c_sm2[3][3] = {{4, -1, 2}, {-1, 4, 2}, {2, 2, 16}};
+__constant__ double c_st1[2][2][2] = {{{3, 1}, {1, 1}}, {{1, 1}, {1, 3}}};
+
+// Facet tables of the P2 / P1 pair: P2 mass, P1 mass (1 + delta) factor and P1 triple
+// products, each divided by |F|.
+template <int D>
+__device__ __forceinline__ double fm2(int i, int j) { return D == 3 ? c_fm2[i][j] / 180.0 : c_sm2[i][j] / 30.0; }
+template <int D>
+__device__ __forceinline__ double fm1(int v, int w) { return (v == w ? 2.0 : 1.0) / (D == 3 ? 12.0 : 6.0); }
+template <int D>
+__device__ __forceinline__ double ft1(int v, int w, int m) {
+    return D == 3 ? c_ft1[v][w][m] / 60.0 : c_st1[v][w][m] / 12.0;
+}
 
 static inline int grid_for(int64_t n, int threads) {
     int64_t g = (n + threads - 1) / threads;
@@ -107,12 +122,58 @@ __global__ void k_facet_geometry(int64_t nf, const int32_t* __restrict__ bf, con
     for (int d = 0; d < 3; ++d) geo[4 * f + 1 + d] = n[d];
 }
 
-__global__ void k_facet_keys(int64_t nf, const int32_t* __restrict__ fnodes, u64* keys) {
+// segments of a triangle mesh: vertices ascending, then the edge node; length
+// and outward unit normal (x, y; z slot 0)
+__global__ void k_facet_geometry2(int64_t nf, const int32_t* __restrict__ bf, const double* __restrict__ x,
+                                  const int32_t* __restrict__ cells, const int64_t* __restrict__ inc_ptr,
+                                  const int32_t* __restrict__ inc, const u64* __restrict__ ekey, int64_t ne,
+                                  int64_t nv, int32_t* fnodes, double* geo) {
+    const int64_t f = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    if (f >= nf) return;
+    int32_t v0 = bf[2 * f], v1 = bf[2 * f + 1];
+    if (v0 > v1) {
+        const int32_t t = v0;
+        v0 = v1;
+        v1 = t;
+    }
+    fnodes[6 * f] = v0;
+    fnodes[6 * f + 1] = v1;
+    fnodes[6 * f + 2] = (int32_t)(nv + lb_u64(ekey, ne, (u64)v0 * (u64)nv + (u64)v1));
+    fnodes[6 * f + 3] = fnodes[6 * f + 4] = fnodes[6 * f + 5] = -1;
+    int32_t opp = v0;
+    for (int64_t it = inc_ptr[v0]; it < inc_ptr[v0 + 1]; ++it) {
+        const int64_t c = inc[it] >> 4;
+        int hit = 0, other = -1;
+        for (int q = 0; q < 3; ++q) {
+            const int32_t w = cells[3 * c + q];
+            if (w == v0 || w == v1) ++hit; else other = w;
+        }
+        if (hit == 2) {
+            opp = other;
+            break;
+        }
+    }
+    const double px = x[3 * (int64_t)v1] - x[3 * (int64_t)v0], py = x[3 * (int64_t)v1 + 1] - x[3 * (int64_t)v0 + 1];
+    const double len = sqrt(px * px + py * py);
+    double n[2] = {py / len, -px / len};
+    const double mx = 0.5 * (x[3 * (int64_t)v0] + x[3 * (int64_t)v1]) - x[3 * (int64_t)opp];
+    const double my = 0.5 * (x[3 * (int64_t)v0 + 1] + x[3 * (int64_t)v1 + 1]) - x[3 * (int64_t)opp + 1];
+    if (n[0] * mx + n[1] * my < 0.0) {
+        n[0] = -n[0];
+        n[1] = -n[1];
+    }
+    geo[4 * f] = len;
+    geo[4 * f + 1] = n[0];
+    geo[4 * f + 2] = n[1];
+    geo[4 * f + 3] = 0.0;
+}
+
+__global__ void k_facet_keys(int64_t nf, int fn, const int32_t* __restrict__ fnodes, u64* keys) {
     const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
-    if (i >= nf * 6) return;
-    const int64_t f = i / 6;
-    const int m = (int)(i % 6);
-    keys[i] = ((u64)fnodes[i] << 32) | (u64)(f * 8 + m);
+    if (i >= nf * fn) return;
+    const int64_t f = i / fn;
+    const int m = (int)(i % fn);
+    keys[i] = ((u64)fnodes[6 * f + m] << 32) | (u64)(f * 8 + m);
 }
 
 __global__ void k_ptr_u64(const u64* __restrict__ keys, int64_t nkeys, int64_t nrows, int64_t* ptr) {
@@ -133,13 +194,20 @@ void build_facets(mpet_ctx* c) {
     if (nf >= (1LL << 28)) fail(MPET_ERR_INVALID, "too many boundary facets (limit 2^28)");
     c->fnodes = c->pool.alloc<int32_t>(nf * 6);
     c->fgeo = c->pool.alloc<double>(nf * 4);
-    k_facet_geometry<<<grid_for(nf, 128), 128, 0, s>>>(nf, c->bfacets, c->x, c->cells, c->inc_ptr, c->inc,
-                                                       (const u64*)c->edge_key, c->ne, c->nv, c->fnodes, c->fgeo);
+    if (c->dim == 2)
+        k_facet_geometry2<<<grid_for(nf, 128), 128, 0, s>>>(nf, c->bfacets, c->x, c->cells, c->inc_ptr, c->inc,
+                                                            (const u64*)c->edge_key, c->ne, c->nv, c->fnodes,
+                                                            c->fgeo);
+    else
+        k_facet_geometry<<<grid_for(nf, 128), 128, 0, s>>>(nf, c->bfacets, c->x, c->cells, c->inc_ptr, c->inc,
+                                                           (const u64*)c->edge_key, c->ne, c->nv, c->fnodes,
+                                                           c->fgeo);
     MPET_CHECK_LAUNCH();
-    const int64_t nk = nf * 6;
+    const int fn = c->dim == 2 ? 3 : 6;
+    const int64_t nk = nf * fn;
     u64* keys = c->pool.alloc<u64>(nk);
     u64* sorted = c->pool.alloc<u64>(nk);
-    k_facet_keys<<<grid_for(nk, 256), 256, 0, s>>>(nf, c->fnodes, keys);
+    k_facet_keys<<<grid_for(nk, 256), 256, 0, s>>>(nf, fn, c->fnodes, keys);
     MPET_CHECK_LAUNCH();
     size_t tb = 0;
     MPET_CUDA(cub::DeviceRadixSort::SortKeys(nullptr, tb, keys, sorted, (int)nk, 0, 64, s));
@@ -164,16 +232,18 @@ struct FacetRhsArgs {
     const int32_t* fnodes;
     const double* fgeo;
     const int32_t* markers;  // (1 + J) x nf
-    const double* traction;  // nf x 6 x 3
-    const double* flux;      // J x nf x 3
-    const double* beta;      // J x nf x 3 (at t_theta)
-    const double* probin;    // J x nf x 3
+    const double* traction;  // nf x FN x D (facet P2 nodes, components)
+    const double* flux;      // J x nf x FV (facet vertices)
+    const double* beta;      // J x nf x FV (at t_theta)
+    const double* probin;    // J x nf x FV
     const double* up;        // previous state
     double* b;
     double dt, theta;
 };
 
+template <int D>
 __global__ void k_facet_rhs(FacetRhsArgs A) {
+    constexpr int FV = Simplex<D>::FV, FN = Simplex<D>::FN;
     const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
     if (i >= A.nnodes) return;
     const int64_t q0 = A.bn_ptr[i], q1 = A.bn_ptr[i + 1];
@@ -186,26 +256,26 @@ __global__ void k_facet_rhs(FacetRhsArgs A) {
         const int m = A.bn_list[q] & 7;
         const double area = A.fgeo[4 * f];
         if (A.traction && A.markers[f] == 1) {
-            const double* sv = A.traction + 18 * f;
-            for (int j = 0; j < 6; ++j) {
-                const double w = area * c_fm2[m][j] * (1.0 / 180.0);
-                for (int k = 0; k < 3; ++k) bu[k] += w * sv[3 * j + k];
+            const double* sv = A.traction + FN * D * f;
+            for (int j = 0; j < FN; ++j) {
+                const double w = area * fm2<D>(m, j);
+                for (int k = 0; k < D; ++k) bu[k] += w * sv[D * j + k];
             }
         }
-        if (i < A.nv && m < 3) {
+        if (i < A.nv && m < FV) {
             const int32_t* fv = A.fnodes + 6 * f;
             for (int a = 0; a < A.J; ++a) {
                 const int mk = A.markers[(int64_t)(1 + a) * A.nf + f];
                 if (mk == 1 && A.flux) {
-                    const double* Iv = A.flux + ((int64_t)a * A.nf + f) * 3;
-                    for (int w = 0; w < 3; ++w) bp[a] += A.dt * area * (m == w ? 2.0 : 1.0) * (1.0 / 12.0) * Iv[w];
+                    const double* Iv = A.flux + ((int64_t)a * A.nf + f) * FV;
+                    for (int w = 0; w < FV; ++w) bp[a] += A.dt * area * fm1<D>(m, w) * Iv[w];
                 } else if (mk == 2 && A.beta) {
-                    const double* bv = A.beta + ((int64_t)a * A.nf + f) * 3;
-                    const double* pr = A.probin ? A.probin + ((int64_t)a * A.nf + f) * 3 : nullptr;
+                    const double* bv = A.beta + ((int64_t)a * A.nf + f) * FV;
+                    const double* pr = A.probin ? A.probin + ((int64_t)a * A.nf + f) * FV : nullptr;
                     const double* pa = A.up + A.Nu + (int64_t)a * A.nv;
-                    for (int v = 0; v < 3; ++v)
-                        for (int w = 0; w < 3; ++w) {
-                            const double t = area * c_ft1[v][w][m] * (1.0 / 60.0) * bv[v];
+                    for (int v = 0; v < FV; ++v)
+                        for (int w = 0; w < FV; ++w) {
+                            const double t = area * ft1<D>(v, w, m) * bv[v];
                             bp[a] += A.dt * (1.0 - A.theta) * t * pa[fv[w]];
                             if (pr) bp[a] -= A.dt * t * pr[w];
                         }
@@ -213,7 +283,7 @@ __global__ void k_facet_rhs(FacetRhsArgs A) {
             }
         }
     }
-    for (int k = 0; k < 3; ++k) A.b[3 * i + k] += bu[k];
+    for (int k = 0; k < D; ++k) A.b[D * i + k] += bu[k];
     if (i < A.nv)
         for (int a = 0; a < A.J; ++a) A.b[A.Nu + (int64_t)a * A.nv + i] += bp[a];
 }
@@ -240,12 +310,14 @@ void launch_facet_rhs(mpet_ctx* c, double dt, const double* up_prev, double* b) 
     A.b = b;
     A.dt = dt;
     A.theta = c->prm.theta;
-    k_facet_rhs<<<grid_for(c->nnodes, 128), 128, 0, c->stream>>>(A);
+    if (c->dim == 2) k_facet_rhs<2><<<grid_for(c->nnodes, 128), 128, 0, c->stream>>>(A);
+    else k_facet_rhs<3><<<grid_for(c->nnodes, 128), 128, 0, c->stream>>>(A);
     MPET_CHECK_LAUNCH();
 }
 
 // Robin matrix: row of p_a at boundary vertex i gains
-// -dt theta sum_f |F|/60 sum_v beta_v T[v][m][w] at column p_a(w).
+// -dt theta sum_f |F| sum_v beta_v T[v][m][w] at column p_a(w).
+template <int D>
 __global__ void k_robin_matrix(int64_t nv, int64_t Nu, int64_t nf, int J, const int64_t* __restrict__ bn_ptr,
                                const int32_t* __restrict__ bn_list, const int32_t* __restrict__ fnodes,
                                const double* __restrict__ fgeo, const int32_t* __restrict__ markers,
@@ -263,19 +335,20 @@ __global__ void k_robin_matrix(int64_t nv, int64_t Nu, int64_t nf, int J, const 
     for (int a = 0; a < J; ++a) {
         const int64_t row = Nu + (int64_t)a * nv + i;
         if (dof_bc[row]) continue;  // Dirichlet rows stay unit rows
-        const int64_t base = row_ptr[row] + 3 * (int64_t)d2 + (int64_t)a * d1;
+        constexpr int FV = Simplex<D>::FV;
+        const int64_t base = row_ptr[row] + D * (int64_t)d2 + (int64_t)a * d1;
         bool touched = false;
         for (int64_t q = q0; q < q1; ++q) {
             const int64_t f = bn_list[q] >> 3;
             const int m = bn_list[q] & 7;
-            if (m >= 3 || markers[(int64_t)(1 + a) * nf + f] != 2) continue;
+            if (m >= FV || markers[(int64_t)(1 + a) * nf + f] != 2) continue;
             const double area = fgeo[4 * f];
-            const double* bv = beta + ((int64_t)a * nf + f) * 3;
-            for (int w = 0; w < 3; ++w) {
+            const double* bv = beta + ((int64_t)a * nf + f) * FV;
+            for (int w = 0; w < FV; ++w) {
                 double t = 0.0;
-                for (int v = 0; v < 3; ++v) t += bv[v] * c_ft1[v][m][w];
+                for (int v = 0; v < FV; ++v) t += bv[v] * ft1<D>(v, m, w);
                 const int64_t pos = base + lb_i32f(n1_col + s1, d1, fnodes[6 * f + w]);
-                v64[pos] += -dt_theta * area * (1.0 / 60.0) * t;
+                v64[pos] += -dt_theta * area * t;
                 if (v32) v32[pos] = (float)v64[pos];
             }
             touched = true;
@@ -289,7 +362,8 @@ __global__ void k_robin_matrix(int64_t nv, int64_t Nu, int64_t nf, int J, const 
 
 void launch_robin_matrix(mpet_ctx* c, double dt) {
     if (c->nf == 0 || !c->bn_ptr || !c->f_beta_matrix) return;
-    k_robin_matrix<<<grid_for(c->nv, 128), 128, 0, c->stream>>>(
+    auto kern = c->dim == 2 ? k_robin_matrix<2> : k_robin_matrix<3>;
+    kern<<<grid_for(c->nv, 128), 128, 0, c->stream>>>(
         c->nv, c->Nu, c->nf, c->J, c->bn_ptr, c->bn_list, c->fnodes, c->fgeo, c->markers, c->f_beta_matrix,
         c->A.rp, c->n2_ptr, c->n1_ptr, c->n1_col, c->dof_bc, c->A.v64, c->A.v32, c->dinv, dt * c->prm.theta);
     MPET_CHECK_LAUNCH();

@@ -30,6 +30,27 @@ struct Error {
 // Device allocation tracked by the context so destroy() frees everything.
 // Every allocation carries kTail spare bytes, so bulk copies whose size is
 // rounded up to 16 bytes may read past the last element without leaving it.
+// Simplex constants of the P2/P1 pair on triangles (D = 2) and tetrahedra
+// (D = 3): vertices, edges, P2 nodes per cell; vertices and P2 nodes per
+// boundary facet.  Local P2 nodes: the vertices, then the edges in UFC
+// order (tet (2,3),(1,3),(1,2),(0,3),(0,2),(0,1); triangle (1,2),(0,2),(0,1)).
+template <int D>
+struct Simplex;
+template <>
+struct Simplex<3> {
+    static constexpr int NV = 4, NE = 6, NN = 10, FV = 3, FN = 6;
+    static constexpr int EA = 0x000112, EB = 0x123233;  // edge e = (EA >> 4e & 15, EB >> 4e & 15)
+};
+template <>
+struct Simplex<2> {
+    static constexpr int NV = 3, NE = 3, NN = 6, FV = 2, FN = 3;
+    static constexpr int EA = 0x001, EB = 0x122;
+};
+template <int D>
+__host__ __device__ __forceinline__ int edge_end(int e, int k) {
+    return ((k == 0 ? Simplex<D>::EA : Simplex<D>::EB) >> (4 * e)) & 15;
+}
+
 // Scoped temporary device buffer (freed on scope exit).
 struct TmpBuf {
     void* p = nullptr;
@@ -199,6 +220,7 @@ struct mpet_ctx {
     mpet::DevPool pool;
 
     // mesh
+    int dim = 3;                  // 2: triangles, 3: tetrahedra
     int64_t nv = 0, nc = 0, nf = 0, ne = 0, nnodes = 0;
     int J = 0;
     double* x = nullptr;          // nv * 3

@@ -20,8 +20,6 @@ namespace mpet {
 
 typedef unsigned long long u64;
 
-__constant__ int c_tet_edges[6][2] = {{2, 3}, {1, 3}, {1, 2}, {0, 3}, {0, 2}, {0, 1}};
-
 
 static inline int grid_for(int64_t n, int threads) {
     int64_t g = (n + threads - 1) / threads;
@@ -83,33 +81,62 @@ static int bits_for(u64 maxval) {
 
 // --- kernels ------------------------------------------------------------------
 
+template <int D>
 __global__ void k_edge_keys(const int32_t* __restrict__ cells, int64_t nc, int64_t nv, u64* keys) {
+    constexpr int NV = Simplex<D>::NV, NE = Simplex<D>::NE;
     int64_t idx = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
-    if (idx >= nc * 6) return;
-    int64_t c = idx / 6;
-    int e = (int)(idx % 6);
-    int64_t a = cells[4 * c + c_tet_edges[e][0]];
-    int64_t b = cells[4 * c + c_tet_edges[e][1]];
+    if (idx >= nc * NE) return;
+    int64_t c = idx / NE;
+    int e = (int)(idx % NE);
+    int64_t a = cells[NV * c + edge_end<D>(e, 0)];
+    int64_t b = cells[NV * c + edge_end<D>(e, 1)];
     int64_t lo = a < b ? a : b, hi = a < b ? b : a;
     keys[idx] = (u64)(lo * nv + hi);
 }
 
+template <int D>
 __global__ void k_cell_nodes(const int32_t* __restrict__ cells, int64_t nc, int64_t nv,
                              const u64* __restrict__ ekey, int64_t ne, int32_t* cell_nodes) {
+    constexpr int NV = Simplex<D>::NV, NN = Simplex<D>::NN;
     int64_t idx = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
-    if (idx >= nc * 10) return;
-    int64_t c = idx / 10;
-    int j = (int)(idx % 10);
-    if (j < 4) {
-        cell_nodes[idx] = cells[4 * c + j];
+    if (idx >= nc * NN) return;
+    int64_t c = idx / NN;
+    int j = (int)(idx % NN);
+    if (j < NV) {
+        cell_nodes[idx] = cells[NV * c + j];
         return;
     }
-    int e = j - 4;
-    int64_t a = cells[4 * c + c_tet_edges[e][0]];
-    int64_t b = cells[4 * c + c_tet_edges[e][1]];
+    int e = j - NV;
+    int64_t a = cells[NV * c + edge_end<D>(e, 0)];
+    int64_t b = cells[NV * c + edge_end<D>(e, 1)];
     int64_t lo = a < b ? a : b, hi = a < b ? b : a;
     int64_t pos = lower_bound_u64(ekey, ne, (u64)(lo * nv + hi));
     cell_nodes[idx] = (int32_t)(nv + pos);
+}
+
+// Triangles: gradients of the barycentric coordinates (x, y in slots 3r, 3r+1
+// of the 16-double record, z slot 0) and the area in slot 12.
+__global__ void k_geometry2(const double* __restrict__ x, const int32_t* __restrict__ cells, int64_t nc,
+                            double* geo) {
+    int64_t c = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    if (c >= nc) return;
+    double p[3][2];
+    for (int i = 0; i < 3; ++i)
+        for (int k = 0; k < 2; ++k) p[i][k] = x[3 * (int64_t)cells[3 * c + i] + k];
+    const double e1[2] = {p[1][0] - p[0][0], p[1][1] - p[0][1]};
+    const double e2[2] = {p[2][0] - p[0][0], p[2][1] - p[0][1]};
+    const double det = e1[0] * e2[1] - e1[1] * e2[0];
+    const double id = 1.0 / det;
+    // rows of the inverse Jacobian: grad lambda_1 = ( e2y, -e2x)/det, grad lambda_2 = (-e1y, e1x)/det
+    double* g = geo + 16 * c;
+    for (int q = 0; q < 16; ++q) g[q] = 0.0;
+    g[3] = e2[1] * id;
+    g[4] = -e2[0] * id;
+    g[6] = -e1[1] * id;
+    g[7] = e1[0] * id;
+    g[0] = -(g[3] + g[6]);
+    g[1] = -(g[4] + g[7]);
+    g[12] = fabs(det) / 2.0;
 }
 
 __global__ void k_geometry(const double* __restrict__ x, const int32_t* __restrict__ cells, int64_t nc,
@@ -142,30 +169,36 @@ __global__ void k_geometry(const double* __restrict__ x, const int32_t* __restri
     g[13] = g[14] = g[15] = 0.0;
 }
 
+template <int D>
 __global__ void k_pairs_n2(const int32_t* __restrict__ cn, int64_t nc, int64_t nnodes, u64* keys) {
+    constexpr int NN = Simplex<D>::NN;
     int64_t idx = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
-    if (idx >= nc * 100) return;
-    int64_t c = idx / 100;
-    int r = (int)(idx % 100);
-    int m = r / 10, j = r % 10;
-    keys[idx] = (u64)cn[10 * c + m] * (u64)nnodes + (u64)cn[10 * c + j];
+    if (idx >= nc * NN * NN) return;
+    int64_t c = idx / (NN * NN);
+    int r = (int)(idx % (NN * NN));
+    int m = r / NN, j = r % NN;
+    keys[idx] = (u64)cn[NN * c + m] * (u64)nnodes + (u64)cn[NN * c + j];
 }
 
+template <int D>
 __global__ void k_pairs_n1(const int32_t* __restrict__ cn, const int32_t* __restrict__ cells, int64_t nc,
                            int64_t nv, u64* keys) {
+    constexpr int NN = Simplex<D>::NN, NV = Simplex<D>::NV;
     int64_t idx = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
-    if (idx >= nc * 40) return;
-    int64_t c = idx / 40;
-    int r = (int)(idx % 40);
-    int m = r / 4, w = r % 4;
-    keys[idx] = (u64)cn[10 * c + m] * (u64)nv + (u64)cells[4 * c + w];
+    if (idx >= nc * NN * NV) return;
+    int64_t c = idx / (NN * NV);
+    int r = (int)(idx % (NN * NV));
+    int m = r / NV, w = r % NV;
+    keys[idx] = (u64)cn[NN * c + m] * (u64)nv + (u64)cells[NV * c + w];
 }
 
+template <int D>
 __global__ void k_pairs_inc(const int32_t* __restrict__ cn, int64_t nc, u64* keys) {
+    constexpr int NN = Simplex<D>::NN;
     int64_t idx = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
-    if (idx >= nc * 10) return;
-    int64_t c = idx / 10;
-    int m = (int)(idx % 10);
+    if (idx >= nc * NN) return;
+    int64_t c = idx / NN;
+    int m = (int)(idx % NN);
     keys[idx] = ((u64)cn[idx] << 32) | (u64)(c * 16 + m);
 }
 
@@ -194,31 +227,33 @@ __global__ void k_max_degree(const int64_t* __restrict__ ptr, int64_t n, int* ou
     atomicMax(out, (int)(ptr[i + 1] - ptr[i]));
 }
 
+template <int D>
 __global__ void k_ranks(const int32_t* __restrict__ cn, const int32_t* __restrict__ cells, int64_t nc,
                         const int64_t* __restrict__ n2_ptr, const int32_t* __restrict__ n2_col,
                         const int64_t* __restrict__ n1_ptr, const int32_t* __restrict__ n1_col,
                         uint16_t* rank2, uint16_t* rank1) {
+    constexpr int NN = Simplex<D>::NN, NV = Simplex<D>::NV, R2 = NN * NN, R1 = NN * NV;
     int64_t idx = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
-    if (idx >= nc * 140) return;
-    int64_t c = idx / 140;
-    int r = (int)(idx % 140);
-    if (r < 100) {
-        int m = r / 10, j = r % 10;
-        int32_t i = cn[10 * c + m];
+    if (idx >= nc * (R2 + R1)) return;
+    int64_t c = idx / (R2 + R1);
+    int r = (int)(idx % (R2 + R1));
+    if (r < R2) {
+        int m = r / NN, j = r % NN;
+        int32_t i = cn[NN * c + m];
         int64_t s = n2_ptr[i];
         int d = (int)(n2_ptr[i + 1] - s);
-        rank2[100 * c + r] = (uint16_t)lower_bound_i32(n2_col + s, d, cn[10 * c + j]);
+        rank2[R2 * c + r] = (uint16_t)lower_bound_i32(n2_col + s, d, cn[NN * c + j]);
     } else {
-        r -= 100;
-        int m = r / 4, w = r % 4;
-        int32_t i = cn[10 * c + m];
+        r -= R2;
+        int m = r / NV, w = r % NV;
+        int32_t i = cn[NN * c + m];
         int64_t s = n1_ptr[i];
         int d = (int)(n1_ptr[i + 1] - s);
-        rank1[40 * c + r] = (uint16_t)lower_bound_i32(n1_col + s, d, cells[4 * c + w]);
+        rank1[R1 * c + r] = (uint16_t)lower_bound_i32(n1_col + s, d, cells[NV * c + w]);
     }
 }
 
-__global__ void k_row_len(int64_t N, int64_t Nu, int64_t nv, int J, const int64_t* __restrict__ n2_ptr,
+__global__ void k_row_len(int64_t N, int64_t Nu, int64_t nv, int J, int dim, const int64_t* __restrict__ n2_ptr,
                           const int64_t* __restrict__ n1_ptr, int64_t* len) {
     int64_t r = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
     if (r > N) return;
@@ -226,11 +261,11 @@ __global__ void k_row_len(int64_t N, int64_t Nu, int64_t nv, int J, const int64_
         len[r] = 0;
         return;
     }
-    int64_t node = r < Nu ? r / 3 : (r - Nu) % nv;
-    len[r] = 3 * (n2_ptr[node + 1] - n2_ptr[node]) + (int64_t)J * (n1_ptr[node + 1] - n1_ptr[node]);
+    int64_t node = r < Nu ? r / dim : (r - Nu) % nv;
+    len[r] = dim * (n2_ptr[node + 1] - n2_ptr[node]) + (int64_t)J * (n1_ptr[node + 1] - n1_ptr[node]);
 }
 
-__global__ void k_fill_cols(int64_t N, int64_t Nu, int64_t nv, int J, const int64_t* __restrict__ row_ptr,
+__global__ void k_fill_cols(int64_t N, int64_t Nu, int64_t nv, int J, int dim, const int64_t* __restrict__ row_ptr,
                             const int64_t* __restrict__ n2_ptr, const int32_t* __restrict__ n2_col,
                             const int64_t* __restrict__ n1_ptr, const int32_t* __restrict__ n1_col,
                             int32_t* col) {
@@ -238,17 +273,17 @@ __global__ void k_fill_cols(int64_t N, int64_t Nu, int64_t nv, int J, const int6
     int64_t warp = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) >> 5;
     int64_t nwarps = ((int64_t)gridDim.x * blockDim.x) >> 5;
     for (int64_t r = warp; r < N; r += nwarps) {
-        int64_t node = r < Nu ? r / 3 : (r - Nu) % nv;
+        int64_t node = r < Nu ? r / dim : (r - Nu) % nv;
         int64_t s2 = n2_ptr[node], s1 = n1_ptr[node];
         int d2 = (int)(n2_ptr[node + 1] - s2), d1 = (int)(n1_ptr[node + 1] - s1);
-        int L = 3 * d2 + J * d1;
+        int L = dim * d2 + J * d1;
         int64_t base = row_ptr[r];
         for (int e = lane; e < L; e += 32) {
             int32_t cidx;
-            if (e < 3 * d2) {
-                cidx = 3 * n2_col[s2 + e / 3] + e % 3;
+            if (e < dim * d2) {
+                cidx = dim * n2_col[s2 + e / dim] + e % dim;
             } else {
-                int e2 = e - 3 * d2;
+                int e2 = e - dim * d2;
                 int a = e2 / d1;
                 cidx = (int32_t)(Nu + (int64_t)a * nv + n1_col[s1 + e2 % d1]);
             }
@@ -257,33 +292,36 @@ __global__ void k_fill_cols(int64_t N, int64_t Nu, int64_t nv, int J, const int6
     }
 }
 
+// a facet has D vertices and D(D-1)/2 edges (every vertex pair)
+template <int D>
 __global__ void k_bc_flags(const int32_t* __restrict__ bf, const int32_t* __restrict__ mk, int64_t nf, int J,
                            int64_t nv, const u64* __restrict__ ekey, int64_t ne, uint8_t* node_bc,
                            uint8_t* vert_bc) {
     int64_t f = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
     if (f >= nf) return;
-    int64_t v[3] = {bf[3 * f], bf[3 * f + 1], bf[3 * f + 2]};
+    int64_t v[D];
+    for (int k = 0; k < D; ++k) v[k] = bf[D * f + k];
     if (mk[f] == 0) {
-        for (int k = 0; k < 3; ++k) node_bc[v[k]] = 1;
-        const int pr[3][2] = {{0, 1}, {0, 2}, {1, 2}};
-        for (int k = 0; k < 3; ++k) {
-            int64_t a = v[pr[k][0]], b = v[pr[k][1]];
-            int64_t lo = a < b ? a : b, hi = a < b ? b : a;
-            int64_t pos = lower_bound_u64(ekey, ne, (u64)(lo * nv + hi));
-            if (pos < ne && ekey[pos] == (u64)(lo * nv + hi)) node_bc[nv + pos] = 1;
-        }
+        for (int k = 0; k < D; ++k) node_bc[v[k]] = 1;
+        for (int i = 0; i < D; ++i)
+            for (int j = i + 1; j < D; ++j) {
+                int64_t a = v[i], b = v[j];
+                int64_t lo = a < b ? a : b, hi = a < b ? b : a;
+                int64_t pos = lower_bound_u64(ekey, ne, (u64)(lo * nv + hi));
+                if (pos < ne && ekey[pos] == (u64)(lo * nv + hi)) node_bc[nv + pos] = 1;
+            }
     }
     for (int a = 0; a < J; ++a)
         if (mk[(int64_t)(1 + a) * nf + f] == 0)
-            for (int k = 0; k < 3; ++k) vert_bc[(int64_t)a * nv + v[k]] = 1;
+            for (int k = 0; k < D; ++k) vert_bc[(int64_t)a * nv + v[k]] = 1;
 }
 
-__global__ void k_bc_dofs_u(const int32_t* __restrict__ nodes, int64_t n, int32_t* dofs, uint8_t* dof_bc) {
+__global__ void k_bc_dofs_u(const int32_t* __restrict__ nodes, int64_t n, int dim, int32_t* dofs, uint8_t* dof_bc) {
     int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
     if (i >= n) return;
-    for (int k = 0; k < 3; ++k) {
-        int32_t d = 3 * nodes[i] + k;
-        dofs[3 * i + k] = d;
+    for (int k = 0; k < dim; ++k) {
+        int32_t d = dim * nodes[i] + k;
+        dofs[dim * i + k] = d;
         dof_bc[d] = 1;
     }
 }
@@ -299,35 +337,38 @@ __global__ void k_bc_dofs_p(const int32_t* __restrict__ verts, int64_t n, int64_
 
 // --- host drivers -------------------------------------------------------------------
 
-void build_topology(mpet_ctx* c) {
+template <int D>
+static void build_topology_d(mpet_ctx* c) {
+    constexpr int NE = Simplex<D>::NE, NN = Simplex<D>::NN, NV = Simplex<D>::NV;
     cudaStream_t s = c->stream;
     const int T = 256;
     int64_t nc = c->nc, nv = c->nv;
     // edges
     {
-        TmpBuf keys(sizeof(u64) * nc * 6);
-        k_edge_keys<<<grid_for(nc * 6, T), T, 0, s>>>(c->cells, nc, nv, keys.as<u64>());
+        TmpBuf keys(sizeof(u64) * nc * NE);
+        k_edge_keys<D><<<grid_for(nc * NE, T), T, 0, s>>>(c->cells, nc, nv, keys.as<u64>());
         MPET_CHECK_LAUNCH();
         u64* ek = nullptr;
-        c->ne = sort_unique(c, keys.as<u64>(), nc * 6, bits_for((u64)nv * (u64)nv), &ek);
+        c->ne = sort_unique(c, keys.as<u64>(), nc * NE, bits_for((u64)nv * (u64)nv), &ek);
         c->edge_key = (int64_t*)ek;
     }
     c->nnodes = nv + c->ne;
-    c->cell_nodes = c->pool.alloc<int32_t>(nc * 10);
-    k_cell_nodes<<<grid_for(nc * 10, T), T, 0, s>>>(c->cells, nc, nv, (const u64*)c->edge_key, c->ne,
+    c->cell_nodes = c->pool.alloc<int32_t>(nc * NN);
+    k_cell_nodes<D><<<grid_for(nc * NN, T), T, 0, s>>>(c->cells, nc, nv, (const u64*)c->edge_key, c->ne,
                                                      c->cell_nodes);
     MPET_CHECK_LAUNCH();
     c->geo = c->pool.alloc<double>(nc * 16);
-    k_geometry<<<grid_for(nc, T), T, 0, s>>>(c->x, c->cells, nc, c->geo);
+    if (D == 3) k_geometry<<<grid_for(nc, T), T, 0, s>>>(c->x, c->cells, nc, c->geo);
+    else k_geometry2<<<grid_for(nc, T), T, 0, s>>>(c->x, c->cells, nc, c->geo);
     MPET_CHECK_LAUNCH();
     int64_t nn = c->nnodes;
     // P2 node adjacency
     {
-        TmpBuf keys(sizeof(u64) * nc * 100);
-        k_pairs_n2<<<grid_for(nc * 100, T), T, 0, s>>>(c->cell_nodes, nc, nn, keys.as<u64>());
+        TmpBuf keys(sizeof(u64) * nc * NN * NN);
+        k_pairs_n2<D><<<grid_for(nc * NN * NN, T), T, 0, s>>>(c->cell_nodes, nc, nn, keys.as<u64>());
         MPET_CHECK_LAUNCH();
         u64* uk = nullptr;
-        c->n2_nnz = sort_unique(c, keys.as<u64>(), nc * 100, bits_for((u64)nn * (u64)nn), &uk);
+        c->n2_nnz = sort_unique(c, keys.as<u64>(), nc * NN * NN, bits_for((u64)nn * (u64)nn), &uk);
         c->n2_ptr = c->pool.alloc<int64_t>(nn + 1);
         c->n2_col = c->pool.alloc<int32_t>(c->n2_nnz);
         k_ptr_from_keys<<<grid_for(nn + 1, T), T, 0, s>>>(uk, c->n2_nnz, nn, (u64)nn, c->n2_ptr);
@@ -338,11 +379,11 @@ void build_topology(mpet_ctx* c) {
     }
     // vertices adjacent to each node
     {
-        TmpBuf keys(sizeof(u64) * nc * 40);
-        k_pairs_n1<<<grid_for(nc * 40, T), T, 0, s>>>(c->cell_nodes, c->cells, nc, nv, keys.as<u64>());
+        TmpBuf keys(sizeof(u64) * nc * NN * NV);
+        k_pairs_n1<D><<<grid_for(nc * NN * NV, T), T, 0, s>>>(c->cell_nodes, c->cells, nc, nv, keys.as<u64>());
         MPET_CHECK_LAUNCH();
         u64* uk = nullptr;
-        c->n1_nnz = sort_unique(c, keys.as<u64>(), nc * 40, bits_for((u64)nn * (u64)nv), &uk);
+        c->n1_nnz = sort_unique(c, keys.as<u64>(), nc * NN * NV, bits_for((u64)nn * (u64)nv), &uk);
         c->n1_ptr = c->pool.alloc<int64_t>(nn + 1);
         c->n1_col = c->pool.alloc<int32_t>(c->n1_nnz);
         k_ptr_from_keys<<<grid_for(nn + 1, T), T, 0, s>>>(uk, c->n1_nnz, nn, (u64)nv, c->n1_ptr);
@@ -354,12 +395,12 @@ void build_topology(mpet_ctx* c) {
     // node -> cell incidence (cells ascending within a node)
     {
         if (nc >= (1LL << 27)) fail(MPET_ERR_INVALID, "too many cells (limit 2^27: cell * 16 + local fits int32)");
-        TmpBuf keys(sizeof(u64) * nc * 10);
-        k_pairs_inc<<<grid_for(nc * 10, T), T, 0, s>>>(c->cell_nodes, nc, keys.as<u64>());
+        TmpBuf keys(sizeof(u64) * nc * NN);
+        k_pairs_inc<D><<<grid_for(nc * NN, T), T, 0, s>>>(c->cell_nodes, nc, keys.as<u64>());
         MPET_CHECK_LAUNCH();
         u64* uk = nullptr;
-        int64_t n = sort_unique(c, keys.as<u64>(), nc * 10, 32 + bits_for((u64)nn), &uk);
-        if (n != nc * 10) fail(MPET_ERR_INVALID, "degenerate cell (repeated vertex)");
+        int64_t n = sort_unique(c, keys.as<u64>(), nc * NN, 32 + bits_for((u64)nn), &uk);
+        if (n != nc * NN) fail(MPET_ERR_INVALID, "degenerate cell (repeated vertex)");
         c->inc_ptr = c->pool.alloc<int64_t>(nn + 1);
         c->inc = c->pool.alloc<int32_t>(n);
         k_ptr_from_keys<<<grid_for(nn + 1, T), T, 0, s>>>(uk, n, nn, 1ULL << 32, c->inc_ptr);
@@ -380,18 +421,23 @@ void build_topology(mpet_ctx* c) {
         MPET_CUDA(cudaStreamSynchronize(s));
         if (h[0] >= 65535) fail(MPET_ERR_INVALID, "node degree too large for 16-bit ranks");
     }
-    c->rank2 = c->pool.alloc<uint16_t>(nc * 100);
-    c->rank1 = c->pool.alloc<uint16_t>(nc * 40);
-    k_ranks<<<grid_for(nc * 140, T), T, 0, s>>>(c->cell_nodes, c->cells, nc, c->n2_ptr, c->n2_col, c->n1_ptr,
+    c->rank2 = c->pool.alloc<uint16_t>(nc * NN * NN);
+    c->rank1 = c->pool.alloc<uint16_t>(nc * NN * NV);
+    k_ranks<D><<<grid_for(nc * (NN * NN + NN * NV), T), T, 0, s>>>(c->cell_nodes, c->cells, nc, c->n2_ptr, c->n2_col, c->n1_ptr,
                                                  c->n1_col, c->rank2, c->rank1);
     MPET_CHECK_LAUNCH();
+}
+
+void build_topology(mpet_ctx* c) {
+    if (c->dim == 2) build_topology_d<2>(c);
+    else build_topology_d<3>(c);
 }
 
 void build_pattern(mpet_ctx* c) {
     cudaStream_t s = c->stream;
     const int T = 256;
     int J = c->J;
-    c->Nu = 3 * c->nnodes;
+    c->Nu = (int64_t)c->dim * c->nnodes;
     c->N = c->Nu + (int64_t)J * c->nv;
     if (c->N >= 2147483647LL) fail(MPET_ERR_INVALID, "too many DOFs for 32-bit column ids");
     int64_t N = c->N;
@@ -399,7 +445,8 @@ void build_pattern(mpet_ctx* c) {
     c->A.rp = c->pool.alloc<int64_t>(N + 1);
     {
         TmpBuf len(sizeof(int64_t) * (N + 1));
-        k_row_len<<<grid_for(N + 1, T), T, 0, s>>>(N, c->Nu, c->nv, J, c->n2_ptr, c->n1_ptr, len.as<int64_t>());
+        k_row_len<<<grid_for(N + 1, T), T, 0, s>>>(N, c->Nu, c->nv, J, c->dim, c->n2_ptr, c->n1_ptr,
+                                                   len.as<int64_t>());
         MPET_CHECK_LAUNCH();
         size_t tb = 0;
         MPET_CUDA(cub::DeviceScan::ExclusiveSum(nullptr, tb, len.as<int64_t>(), c->A.rp, (int)(N + 1), s));
@@ -410,8 +457,8 @@ void build_pattern(mpet_ctx* c) {
     MPET_CUDA(cudaStreamSynchronize(s));
     c->A.nnz = c->nnz;
     c->A.ci = c->pool.alloc<int32_t>(c->nnz);
-    k_fill_cols<<<152 * 16, 256, 0, s>>>(N, c->Nu, c->nv, J, c->A.rp, c->n2_ptr, c->n2_col, c->n1_ptr, c->n1_col,
-                                         c->A.ci);
+    k_fill_cols<<<152 * 16, 256, 0, s>>>(N, c->Nu, c->nv, J, c->dim, c->A.rp, c->n2_ptr, c->n2_col, c->n1_ptr,
+                                         c->n1_col, c->A.ci);
     MPET_CHECK_LAUNCH();
     c->A.lpr = choose_lpr(N, c->nnz);
     {
@@ -470,23 +517,27 @@ void build_bc(mpet_ctx* c) {
     MPET_CUDA(cudaMemsetAsync(c->vert_bc, 0, (size_t)J * c->nv, s));
     MPET_CUDA(cudaMemsetAsync(c->dof_bc, 0, c->N, s));
     if (c->nf > 0) {
-        k_bc_flags<<<grid_for(c->nf, T), T, 0, s>>>(c->bfacets, c->markers, c->nf, J, c->nv,
-                                                     (const u64*)c->edge_key, c->ne, c->node_bc, c->vert_bc);
+        if (c->dim == 2)
+            k_bc_flags<2><<<grid_for(c->nf, T), T, 0, s>>>(c->bfacets, c->markers, c->nf, J, c->nv,
+                                                            (const u64*)c->edge_key, c->ne, c->node_bc, c->vert_bc);
+        else
+            k_bc_flags<3><<<grid_for(c->nf, T), T, 0, s>>>(c->bfacets, c->markers, c->nf, J, c->nv,
+                                                            (const u64*)c->edge_key, c->ne, c->node_bc, c->vert_bc);
         MPET_CHECK_LAUNCH();
     }
     c->nbc_nodes[0] = compact_flags(c, c->node_bc, c->nnodes, &c->bc_nodes[0]);
     for (int a = 0; a < J; ++a)
         c->nbc_nodes[1 + a] = compact_flags(c, c->vert_bc + (int64_t)a * c->nv, c->nv, &c->bc_nodes[1 + a]);
     c->bc_off[0] = 0;
-    c->bc_off[1] = 3 * c->nbc_nodes[0];
+    c->bc_off[1] = (int64_t)c->dim * c->nbc_nodes[0];
     for (int a = 0; a < J; ++a) c->bc_off[2 + a] = c->bc_off[1 + a] + c->nbc_nodes[1 + a];
     c->nbc_dofs = c->bc_off[1 + J];
     c->bc_dofs = c->pool.alloc<int32_t>(c->nbc_dofs);
     c->bc_vals = c->pool.alloc<double>(c->nbc_dofs);
     MPET_CUDA(cudaMemsetAsync(c->bc_vals, 0, sizeof(double) * (c->nbc_dofs > 0 ? c->nbc_dofs : 1), s));
     if (c->nbc_nodes[0])
-        k_bc_dofs_u<<<grid_for(c->nbc_nodes[0], T), T, 0, s>>>(c->bc_nodes[0], c->nbc_nodes[0], c->bc_dofs,
-                                                                c->dof_bc);
+        k_bc_dofs_u<<<grid_for(c->nbc_nodes[0], T), T, 0, s>>>(c->bc_nodes[0], c->nbc_nodes[0], c->dim,
+                                                                c->bc_dofs, c->dof_bc);
     for (int a = 0; a < J; ++a)
         if (c->nbc_nodes[1 + a])
             k_bc_dofs_p<<<grid_for(c->nbc_nodes[1 + a], T), T, 0, s>>>(

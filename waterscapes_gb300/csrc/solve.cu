@@ -794,6 +794,7 @@ void fill_sell(mpet_ctx* c, Csr& A) {
 // vertex adjacency counts (host), values filled on the device.
 void build_node_blocks(mpet_ctx* c) {
     NodeBlocks& nb = c->A_nb;
+    if (c->dim != 3) return;  // 3-row displacement groups
     const int J = c->J;
     std::vector<int64_t> p2(c->nnodes + 1), p1(c->nnodes + 1);
     MPET_CUDA(cudaMemcpyAsync(p2.data(), c->n2_ptr, sizeof(int64_t) * p2.size(), cudaMemcpyDeviceToHost, c->stream));
@@ -1325,22 +1326,20 @@ static void vcycle(mpet_ctx* c, AmgHier& h, size_t k, const T* b, T* x) {
 // displacement components (3 per node) <-> the padded 4-wide layout of the
 // displacement hierarchy
 template <typename T>
-__global__ void k_pack34(int64_t nodes, const T* __restrict__ a, T* b4) {
+__global__ void k_pack34(int64_t nodes, int dim, const T* __restrict__ a, T* b4) {
     const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
     if (i >= nodes) return;
-    const T v[4] = {a[3 * i], a[3 * i + 1], a[3 * i + 2], T(0)};
+    const T v[4] = {a[dim * i], a[dim * i + 1], dim == 3 ? a[dim * i + 2] : T(0), T(0)};
     VecIO<T, 4>::store(b4, i, v);
 }
 
 template <typename T>
-__global__ void k_unpack43(int64_t nodes, const T* __restrict__ b4, T* a) {
+__global__ void k_unpack43(int64_t nodes, int dim, const T* __restrict__ b4, T* a) {
     const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
     if (i >= nodes) return;
     T v[4];
     VecIO<T, 4>::load(b4, i, v);
-    a[3 * i] = v[0];
-    a[3 * i + 1] = v[1];
-    a[3 * i + 2] = v[2];
+    for (int k = 0; k < dim; ++k) a[dim * i + k] = v[k];
 }
 
 // rt_k = sum_a Q_ak r_a (fwd) or z_a = sum_k Q_ak zt_k (back) at every vertex,
@@ -1391,9 +1390,9 @@ static void precond(mpet_ctx* c, const T* r, T* z) {
     const int64_t nodes = c->nnodes;
     T* bin = (T*)hu.pack_in;
     T* xout = (T*)hu.pack_out;
-    k_pack34<T><<<grid_for(nodes, 256), 256, 0, main>>>(nodes, r, bin);
+    k_pack34<T><<<grid_for(nodes, 256), 256, 0, main>>>(nodes, c->dim, r, bin);
     vcycle<T, 4>(c, hu, 0, bin, xout);
-    k_unpack43<T><<<grid_for(nodes, 256), 256, 0, main>>>(nodes, xout, z);
+    k_unpack43<T><<<grid_for(nodes, 256), 256, 0, main>>>(nodes, c->dim, xout, z);
     MPET_CHECK_LAUNCH();
     c->n_launch += 2;
     for (int a = 0; a < c->J; ++a) MPET_CUDA(cudaStreamWaitEvent(main, c->ev_join[a], 0));

@@ -49,7 +49,7 @@ class Function:
     def split(self, deepcopy=False):
         s = self._solver
         v = self._v.clone() if deepcopy else self._v
-        u = v[:s.Nu].view(s.nnodes, 3)
+        u = v[:s.Nu].view(s.nnodes, s.dim)
         ps = [v[s.Nu + a * s.nv: s.Nu + (a + 1) * s.nv] for a in range(s.J)]
         return tuple([u] + ps)
 
@@ -74,8 +74,9 @@ class MPETSolver:
             self.params.update(params)
         self.solver_monitor = {"niter": [], "relres": []}
         mesh = problem.mesh
-        if mesh.gdim != 3:
-            raise NotImplementedError("the GPU engine assembles tetrahedral (3D) meshes only")
+        if mesh.gdim not in (2, 3) or mesh.tdim != mesh.gdim:
+            raise NotImplementedError("the GPU engine assembles triangle (2D) and tetrahedral (3D) meshes")
+        self.dim = mesh.gdim
         if problem.u_has_nullspace or any(problem.p_has_nullspace):
             raise NotImplementedError("rigid-motion / constant nullspace multipliers are not built on the GPU")
         pp = problem.params
@@ -90,14 +91,15 @@ class MPETSolver:
         self._ctx = _lib.Context(dev)
         self._stream = torch.cuda.current_stream(self.device)
         self._ctx.call("mpet_set_stream", ctypes.c_void_p(self._stream.cuda_stream))
-        # mesh and markers
-        x = np.ascontiguousarray(mesh.coordinates(), dtype=np.float64)
+        # mesh and markers (coordinates as nv x 3, z = 0 in 2D)
+        x = np.zeros((mesh.num_vertices(), 3), dtype=np.float64)
+        x[:, :self.dim] = mesh.coordinates()
         cells = np.ascontiguousarray(mesh.cells(), dtype=np.int32)
         bf = np.ascontiguousarray(mesh.boundary_facets(), dtype=np.int32)
         markers = np.ascontiguousarray(np.stack(
             [problem.momentum_boundary_markers.as_int32()]
             + [problem.continuity_boundary_markers[a].as_int32() for a in range(self.J)], 0), dtype=np.int32)
-        self._ctx.call("mpet_mesh_upload", x.shape[0], _lib._ptr(x), cells.shape[0], _lib._ptr(cells),
+        self._ctx.call("mpet_mesh_upload_dim", self.dim, x.shape[0], _lib._ptr(x), cells.shape[0], _lib._ptr(cells),
                        bf.shape[0], _lib._ptr(bf), _lib._ptr(markers), self.J)
         self._prm = self._make_params()
         self._ctx.call("mpet_setup", ctypes.byref(self._prm))
@@ -113,7 +115,7 @@ class MPETSolver:
         self._ctx.call("mpet_get_sizes", ctypes.byref(N), ctypes.byref(nnz), ctypes.byref(nn), ctypes.byref(ne))
         self.N, self.nnz, self.nnodes, self.ne = N.value, nnz.value, nn.value, ne.value
         self.nv = mesh.num_vertices()
-        self.Nu = 3 * self.nnodes
+        self.Nu = self.dim * self.nnodes
         f64 = dict(dtype=torch.float64, device=self.device)
         self.up_ = Function(self, torch.zeros(self.N, **f64))
         self.up = Function(self, torch.zeros(self.N, **f64))
@@ -194,21 +196,24 @@ class MPETSolver:
         return bcs
 
     def _eval(self, expr, x, t, vector):
+        """Values of a data term at points x (n x 3 tensor; z = 0 in 2D): (n, dim)
+        for vector data, (n,) for scalar data."""
         torch = _torch()
         n = x.shape[0]
+        d = self.dim
         if expr is None:
-            v = torch.zeros((n, 3) if vector else (n,), dtype=torch.float64, device=self.device)
+            v = torch.zeros((n, d) if vector else (n,), dtype=torch.float64, device=self.device)
             return v
         if isinstance(expr, Constant) or isinstance(expr, (int, float, tuple, list)):
             val = expr.values() if isinstance(expr, Constant) else expr
             if vector:
-                val = tuple(float(a) for a in (val if isinstance(val, (tuple, list)) else (val,) * 3))
-                return torch.tensor(val, dtype=torch.float64, device=self.device).expand(n, 3).contiguous()
+                val = tuple(float(a) for a in (val if isinstance(val, (tuple, list)) else (val,) * d))
+                return torch.tensor(val, dtype=torch.float64, device=self.device).expand(n, d).contiguous()
             return torch.full((n,), float(val), dtype=torch.float64, device=self.device)
         v = expr(x, t)
         v = torch.as_tensor(v, dtype=torch.float64, device=self.device)
         if vector:
-            v = v.reshape(n, 3) if v.numel() == 3 * n else v.expand(n, 3)
+            v = v.reshape(n, d) if v.numel() == d * n else v.expand(n, d)
         else:
             v = v.reshape(n) if v.numel() == n else v.expand(n)
         return v.contiguous()
@@ -217,7 +222,7 @@ class MPETSolver:
         p = self.problem
         b0 = self._bcs[0]
         if b0["n"]:
-            xn = b0["coords"][0::3]
+            xn = b0["coords"][0::self.dim]
             vals = self._eval(p.u_bar, xn, t, True).reshape(-1).contiguous()
             self._bcv0 = vals
             self._ctx.call("mpet_set_bc_values", 0, _lib._ptr(vals))
@@ -234,7 +239,8 @@ class MPETSolver:
         if self._node_x is None:
             edges = np.empty((self.ne, 2), dtype=np.int64)
             self._ctx.call("mpet_get_edges", _lib._ptr(edges))
-            x = self.problem.mesh.coordinates()
+            x = np.zeros((self.nv, 3))
+            x[:, :self.dim] = self.problem.mesh.coordinates()                 # z = 0 in 2D
             nx = np.concatenate([x, 0.5 * (x[edges[:, 0]] + x[edges[:, 1]])], 0)
             self._node_x = torch.as_tensor(nx, dtype=torch.float64, device=self.device)
         return self._node_x
@@ -260,7 +266,8 @@ class MPETSolver:
             geo = torch.empty(max(nf, 1), 4, dtype=torch.float64, device=self.device)
             self._ctx.call("mpet_get_facet_data", _lib._ptr(fn), _lib._ptr(geo))
             self._fnodes, self._fgeo = fn[:nf], geo[:nf]
-            self._fx = self._node_coordinates()[self._fnodes.long()]          # (nf, 6, 3)
+            fn_count = 6 if self.dim == 3 else 3                                # P2 nodes of a facet
+            self._fx = self._node_coordinates()[self._fnodes[:, :fn_count].long()]  # (nf, FN, 3)
             p = self.problem
             mk = lambda m: torch.as_tensor(m, device=self.device)
             self._fmask_u = mk(p.momentum_boundary_markers.array() == NEUMANN_MARKER)
@@ -276,20 +283,22 @@ class MPETSolver:
             except TypeError:
                 v = expr.fn(x, t)
             v = torch.as_tensor(v, dtype=torch.float64, device=self.device)
-            return v.expand(x.shape[0], 3) if v.numel() != 3 * x.shape[0] else v.reshape(x.shape[0], 3)
+            d = self.dim
+            return v.expand(x.shape[0], d) if v.numel() != d * x.shape[0] else v.reshape(x.shape[0], d)
         return self._eval(expr, x, t, True)
 
     def _per_network_vertex_data(self, fields, t, mask_index):
         torch = _torch()
         fx, _ = self._facet_geometry()
-        xv = fx[:, :3, :].reshape(-1, 3)
+        fv = self.dim                                                      # vertices of a facet
+        xv = fx[:, :fv, :].reshape(-1, 3)
         nf = fx.shape[0]
-        out = torch.zeros(self.J, nf, 3, dtype=torch.float64, device=self.device)
+        out = torch.zeros(self.J, nf, fv, dtype=torch.float64, device=self.device)
         for a in range(self.J):
             mask = self._fmask_c[a][mask_index]
             if fields[a] is None or not bool(mask.any()):
                 continue
-            v = self._eval(fields[a], xv, t, False).reshape(nf, 3)
+            v = self._eval(fields[a], xv, t, False).reshape(nf, fv)
             out[a] = v * mask[:, None]
         return out.contiguous()
 
@@ -298,9 +307,9 @@ class MPETSolver:
         p = self.problem
         if self._traction_on:
             fx, geo = self._facet_geometry()
-            nf = fx.shape[0]
-            n = geo[:, 1:4].repeat_interleave(6, dim=0)
-            s = self._eval_traction(p.s, fx.reshape(-1, 3), t1, n).reshape(nf, 6, 3)
+            nf, fn = fx.shape[0], fx.shape[1]
+            n = geo[:, 1:1 + self.dim].repeat_interleave(fn, dim=0)
+            s = self._eval_traction(p.s, fx.reshape(-1, 3), t1, n).reshape(nf, fn, self.dim)
             self._f_s = (s * self._fmask_u[:, None, None]).contiguous()
             self._ctx.call("mpet_set_facet_data", 0, _lib._ptr(self._f_s))
         if self._flux_on:
