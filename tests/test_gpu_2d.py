@@ -112,7 +112,7 @@ def _rates_gpu(theta, ms, precision):
     hs = []
     for n, M in zip((8, 16, 32), ms):
         problem = _problem_2d(n, SYM_PARAMS, data)
-        s = _solver(problem, 1.0 / M, 1.0, theta, precision=precision, rtol=1e-12)
+        s = _solver(problem, 1.0 / M, 1.0, theta, precision=precision, rtol=1e-10)
         for up, t in s.solve():
             pass
         om = make_oracle(problem, theta)
