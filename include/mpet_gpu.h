@@ -78,6 +78,9 @@ typedef struct mpet_params {
                                           preconditioner; the reference form uses mu
                                           (mpetsolver.py:269), mu + lmbda balances the blocks;
                                           <= 0 means mu */
+    double prec_u_shift;               /* g in + g (u, v) added to that block (keeps it definite
+                                          when the displacement has no Dirichlet condition, e.g.
+                                          with rigid-motion modes); 0 for none */
 } mpet_params;
 
 typedef struct mpet_stats {
@@ -153,6 +156,20 @@ int mpet_set_sources(mpet_ctx* ctx, const double* f_nodes, const double* g_verti
  * -dt (K_a grad pm_a, grad q_a) (mpetsolver.py:200) and in the preconditioner
  * (:270); the matrix and preconditioner must be rebuilt afterwards. */
 int mpet_set_cell_permeability(mpet_ctx* ctx, const double* K_cells);
+
+/* Rigid-motion nullspace of the displacement (MPETProblem.u_has_nullspace,
+ * mpetsolver.py:115-124, 204-207, basis of rm_basis_L2.py:10-74): Z is a
+ * device array nz x Nu (nz = 3 in 2D, 6 in 3D) of the modes' nodal values in
+ * the displacement DOF layout, L2-orthonormal.  The reference adds one
+ * multiplier r_i per mode, r_i (Z_i, u) + z_i (Z_i, v); rigid motions are
+ * divergence-free, so they span the kernel of the coupled operator and each
+ * solve takes r_i = Z_i^T b_u, removes sum_i r_i M Z_i from the right-hand
+ * side, solves the consistent singular system and projects the displacement
+ * to (Z_i, u) = 0.  The displacement may have no Dirichlet DOFs (else
+ * MPET_ERR_INVALID).  mpet_get_rigid_multipliers returns the r_i of the last
+ * solve. */
+int mpet_set_rigid_modes(mpet_ctx* ctx, int32_t nz, const double* Z);
+int mpet_get_rigid_multipliers(mpet_ctx* ctx, double* r_host);
 
 /* Per-cell storage coefficients c_a (device array J x nc) and transfer
  * coefficients S_ab (J x J x nc, S_cells[(a J + b) nc + cell], symmetric in

@@ -48,6 +48,7 @@ class MpetParams(ctypes.Structure):
         ("amg_p2_to_p1", ctypes.c_int32),
         ("prec_network_modes", ctypes.c_int32),
         ("prec_u_weight", ctypes.c_double),
+        ("prec_u_shift", ctypes.c_double),
     ]
 
 
@@ -99,6 +100,8 @@ SIGNATURES = {
     "mpet_set_sources": [_P, _P, _P],
     "mpet_set_cell_permeability": [_P, _P],
     "mpet_set_cell_coefficients": [_P, _P, _P],
+    "mpet_set_rigid_modes": [_P, _I32, _P],
+    "mpet_get_rigid_multipliers": [_P, _P],
     "mpet_set_batch": [_P, _I32, _P],
     "mpet_get_batch_relres": [_P, _P],
     "mpet_get_facet_data": [_P, _P, _P],

@@ -330,6 +330,36 @@ int mpet_set_cell_permeability(mpet_ctx* c, const double* K_cells) {
     API_END(c)
 }
 
+int mpet_set_rigid_modes(mpet_ctx* c, int32_t nz, const double* Z) {
+    API_BEGIN(c)
+    require(c->setup_done, MPET_ERR_STATE, "mpet_setup must come first");
+    require(nz >= 0 && nz <= 6 && (nz == 0 || Z), MPET_ERR_INVALID, "nz must be in 0..6");
+    require(c->ninst == 0, MPET_ERR_INVALID, "rigid modes are not built for batches");
+    require(nz == 0 || c->bc_off[1] == c->bc_off[0], MPET_ERR_INVALID,
+            "rigid-motion modes need a displacement without Dirichlet DOFs");
+    if (nz > 0 && !c->rigid_Z) {
+        c->rigid_Z = c->pool.alloc<double>(6 * c->Nu);
+        c->rigid_MZ = c->pool.alloc<double>(6 * c->Nu);
+        c->rigid_b = c->pool.alloc<double>(c->N);
+    }
+    for (int i = 0; i < nz; ++i) {
+        MPET_CUDA(cudaMemcpyAsync(c->rigid_Z + (int64_t)i * c->Nu, Z + (int64_t)i * c->Nu, sizeof(double) * c->Nu,
+                                  cudaMemcpyDeviceToDevice, c->stream));
+        launch_mass_u(c, c->rigid_Z + (int64_t)i * c->Nu, c->rigid_MZ + (int64_t)i * c->Nu);
+    }
+    MPET_CUDA(cudaStreamSynchronize(c->stream));
+    c->nrigid = nz;
+    for (int i = 0; i < 6; ++i) c->rigid_r[i] = 0.0;
+    API_END(c)
+}
+
+int mpet_get_rigid_multipliers(mpet_ctx* c, double* r) {
+    API_BEGIN(c)
+    require(r, MPET_ERR_INVALID, "NULL argument");
+    for (int i = 0; i < c->nrigid; ++i) r[i] = c->rigid_r[i];
+    API_END(c)
+}
+
 int mpet_set_cell_coefficients(mpet_ctx* c, const double* c_cells, const double* S_cells) {
     API_BEGIN(c)
     require(c->setup_done, MPET_ERR_STATE, "mpet_setup must come first");
@@ -345,6 +375,7 @@ int mpet_set_batch(mpet_ctx* c, int32_t ninst, const int32_t* vertex_instance) {
     require(c->setup_done, MPET_ERR_STATE, "mpet_setup must come first");
     require(c->dim == 3, MPET_ERR_INVALID, "batches are built for tetrahedral meshes");
     require(c->ninst == 0, MPET_ERR_STATE, "the batch partition is already set");
+    require(c->nrigid == 0, MPET_ERR_STATE, "batches with rigid-motion modes are not built");
     require(ninst >= 1 && vertex_instance, MPET_ERR_INVALID, "need ninst >= 1 and an instance per vertex");
     setup_batch(c, ninst, vertex_instance);
     set_instances(c, ninst, vertex_instance);

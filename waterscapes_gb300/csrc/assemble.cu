@@ -49,6 +49,7 @@ struct MatCoef {
     const double* Sc;                                  // per-cell S (J x J x nc) or null
     int64_t nc;
     double prec_mu;                                    // weight of the displacement preconditioner block
+    double prec_shift;                                 // + prec_shift (u, v) in that block
     __device__ __forceinline__ double Kof(int a, int64_t cell) const { return Kc ? Kc[a * nc + cell] : K[a]; }
     __device__ __forceinline__ double cof(int a, int64_t cell) const { return cc ? cc[a * nc + cell] : c[a]; }
     __device__ __forceinline__ double Sof(int a, int b, int64_t cell) const {
@@ -335,7 +336,10 @@ __global__ void __launch_bounds__(256) k_assemble_prec(PrecArgs A, MatCoef P) {
                         for (int r = 0; r < NV; ++r) acc += gm[r][a] * gj[r][a];
                         tr += acc;
                     }
-                    A.lu[s2 + A.rank2[cell * (NN * NN) + m * NN + j]] += P.prec_mu * w20 * tr;
+                    double v = P.prec_mu * w20 * tr;
+                    if (P.prec_shift > 0.0)
+                        v += P.prec_shift * G.vol * (D == 3 ? c_m2[m][j] / 420.0 : c_m2t[m][j] / 180.0);
+                    A.lu[s2 + A.rank2[cell * (NN * NN) + m * NN + j]] += v;
                 } else {
                     const int w = t - NN;
                     const int32_t vw = A.cells[NV * cell + w];
@@ -534,6 +538,7 @@ static MatCoef make_coef(const mpet_ctx* c, double dt) {
     P.Sc = c->S_cells;
     P.nc = c->nc;
     P.prec_mu = c->prm.prec_u_weight > 0.0 ? c->prm.prec_u_weight : c->prm.mu;
+    P.prec_shift = c->prm.prec_u_shift > 0.0 ? c->prm.prec_u_shift : 0.0;
     return P;
 }
 
@@ -780,6 +785,15 @@ void launch_adjoint_rhs(mpet_ctx* c, double dt, const double* lam, double* out) 
     k_rhs_p<3, true><<<grid_for(c->nv, 128), 128, 0, c->stream>>>(A, P);
     MPET_CHECK_LAUNCH();
     launch_zero_bc_rows(c, out);
+}
+
+// out = M f on the displacement rows (P2 mass matrix of every component), f at P2 nodes
+void launch_mass_u(mpet_ctx* c, const double* f_nodes, double* out) {
+    RhsArgs A = rhs_args(c, 0.0, nullptr, out);
+    A.f = f_nodes;
+    if (c->dim == 2) k_rhs_u<2><<<grid_for(c->nnodes, 128), 128, 0, c->stream>>>(A);
+    else k_rhs_u<3><<<grid_for(c->nnodes, 128), 128, 0, c->stream>>>(A);
+    MPET_CHECK_LAUNCH();
 }
 
 void launch_zero_bc_rows(mpet_ctx* c, double* b) {

@@ -338,6 +338,15 @@ struct mpet_ctx {
     cudaGraphExec_t bmr_graph = nullptr;
     int64_t bmr_graph_launches = 0;
 
+    // rigid-motion modes of the displacement (nz x Nu, L2-orthonormal), their
+    // mass-weighted duals M Z, the multipliers of the last solve and a
+    // right-hand-side scratch vector
+    int nrigid = 0;
+    double* rigid_Z = nullptr;
+    double* rigid_MZ = nullptr;
+    double rigid_r[6] = {0, 0, 0, 0, 0, 0};
+    double* rigid_b = nullptr;
+
     // network eigenmodes of the pressure preconditioner (prec_network_modes):
     // per instance Q (J x J, column i = mode i) and lambda (J); vertex and
     // cell instance ids (batches); transformed residual / correction (J x nv)
@@ -419,6 +428,7 @@ void launch_set_bc_in_x(mpet_ctx* c, double* x);
 void launch_zero_bc_columns(mpet_ctx* c, double* b, const double* xbc);
 void launch_zero_bc_rows(mpet_ctx* c, double* b);
 void launch_adjoint_rhs(mpet_ctx* c, double dt, const double* lam, double* out);
+void launch_mass_u(mpet_ctx* c, const double* f_nodes, double* out);
 void launch_adjoint_grad(mpet_ctx* c, double dt, const double* lam, const double* up_prev, const double* up,
                          double* grad);
 void launch_misfit(mpet_ctx* c, const double* up, const double* target, double* dloss, double* loss_dev);

@@ -1517,12 +1517,53 @@ static int minres_run(mpet_ctx* c, double target, int max_iters, int* iters_done
     return status;
 }
 
+// ---- rigid-motion modes ---------------------------------------------------------------
+__global__ void k_axpy64(int64_t n, double* y, double a, const double* __restrict__ x) {
+    const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    if (i < n) y[i] += a * x[i];
+}
+
+__global__ void k_finish_dot(const double* __restrict__ partials, double* out) {
+    __shared__ double sh[8];
+    const double s = sum_partials(partials, sh);
+    if (threadIdx.x == 0) *out = s;
+}
+
+// a . b over n entries (fixed-order reduction), on the host
+static double dot_host(mpet_ctx* c, const double* a, const double* b, int64_t n) {
+    k_dot<double><<<NB_RED, 256, 0, c->stream>>>(n, a, b, c->partials);
+    k_finish_dot<<<1, 256, 0, c->stream>>>(c->partials, c->partials + 2 * NB_RED - 1);
+    MPET_CHECK_LAUNCH();
+    double v = 0.0;
+    MPET_CUDA(cudaMemcpyAsync(&v, c->partials + 2 * NB_RED - 1, sizeof(double), cudaMemcpyDeviceToHost,
+                              c->stream));
+    MPET_CUDA(cudaStreamSynchronize(c->stream));
+    return v;
+}
+
+// v_u -= sum_i (P_i . v_u) Q_i over the displacement rows (P, Q: the modes or their duals)
+static void rigid_project(mpet_ctx* c, double* v, const double* P, const double* Q, double* coef_out) {
+    const int64_t nu = c->Nu;
+    for (int i = 0; i < c->nrigid; ++i) {
+        const double t = dot_host(c, P + (int64_t)i * nu, v, nu);
+        if (coef_out) coef_out[i] = t;
+        k_axpy64<<<grid_for(nu, 256), 256, 0, c->stream>>>(nu, v, -t, Q + (int64_t)i * nu);
+        MPET_CHECK_LAUNCH();
+    }
+}
+
 template <typename T>
 static int solve_impl(mpet_ctx* c, const double* b, double* x, mpet_stats* st, bool homogeneous) {
     const int64_t n = c->N;
     const int G = grid_for(n, 256);
     if (homogeneous) launch_zero_bc_rows(c, x);
     else launch_set_bc_in_x(c, x);
+    if (c->nrigid > 0) {
+        // multipliers r_i = Z_i . b_u; solve with b - sum_i r_i M Z_i (consistent)
+        MPET_CUDA(cudaMemcpyAsync(c->rigid_b, b, sizeof(double) * n, cudaMemcpyDeviceToDevice, c->stream));
+        rigid_project(c, c->rigid_b, c->rigid_Z, c->rigid_MZ, c->rigid_r);
+        b = c->rigid_b;
+    }
     double eta0 = -1.0;
     int iters = 0, outer = 0;
     int status = MPET_OK;
@@ -1534,6 +1575,7 @@ static int solve_impl(mpet_ctx* c, const double* b, double* x, mpet_stats* st, b
         launch_spmv<double, 1>(c, c->A, c->A.v64, x, EpiResid64{c->orr, b, c->dinv});
         c->n_spmv++;
         k_outer_norms<<<1, 256, 0, c->stream>>>(c->sc, c->partials);
+        if (c->nrigid > 0) rigid_project(c, c->orr, c->rigid_Z, c->rigid_MZ, nullptr);  // rounding drift
         T* rhs = (T*)c->kr[0];
         k_scale_to<T><<<G, 256, 0, c->stream>>>(n, c->orr, rhs, c->sc);
         k_copy2<T><<<G, 256, 0, c->stream>>>(n, rhs, (T*)c->kr[1], (T*)c->kr[1]);
@@ -1585,6 +1627,8 @@ static int solve_impl(mpet_ctx* c, const double* b, double* x, mpet_stats* st, b
             break;
         }
     }
+    // (Z_i, u) = 0: remove the modes from the displacement (M-orthogonally)
+    if (c->nrigid > 0) rigid_project(c, x, c->rigid_MZ, c->rigid_Z, nullptr);
     if (outer >= max_outer && status == MPET_OK) status = MPET_ERR_MAXIT;
     int derr = 0;
     MPET_CUDA(cudaMemcpyAsync(&derr, c->dev_err, sizeof(int), cudaMemcpyDeviceToHost, c->stream));

@@ -317,3 +317,21 @@ def EllipsoidShellMesh(n_radial, semi_axes=(1.0, 0.8, 0.7), inner_ratio=0.3,
         x = x + d
         mesh = Mesh(x, cells)
     return mesh
+
+
+def AnnulusMesh(r_inner, r_outer, n_radial, n_angular, center=(0.0, 0.0)):
+    """Triangulated annulus (2D "donut"): a polar grid of n_radial layers from
+    r_inner to r_outer and n_angular sectors, every quadrilateral cut into two
+    triangles."""
+    nr, na = int(n_radial), int(n_angular)
+    r = np.linspace(r_inner, r_outer, nr + 1)
+    th = np.linspace(0.0, 2.0 * np.pi, na, endpoint=False)
+    R, T = np.meshgrid(r, th, indexing="ij")                 # (nr + 1, na)
+    coords = np.stack([center[0] + R * np.cos(T), center[1] + R * np.sin(T)], -1).reshape(-1, 2)
+    i, j = np.meshgrid(np.arange(nr), np.arange(na), indexing="ij")
+    v0 = i * na + j
+    v1 = i * na + (j + 1) % na
+    v2 = (i + 1) * na + j
+    v3 = (i + 1) * na + (j + 1) % na
+    tris = np.stack([np.stack([v0, v1, v3], -1), np.stack([v0, v3, v2], -1)], -2).reshape(-1, 3)
+    return Mesh(coords, tris)

@@ -51,7 +51,11 @@ class Function:
         v = self._v.clone() if deepcopy else self._v
         u = v[:s.Nu].view(s.nnodes, s.dim)
         ps = [v[s.Nu + a * s.nv: s.Nu + (a + 1) * s.nv] for a in range(s.J)]
-        return tuple([u] + ps)
+        extra = []
+        if getattr(s, "nrigid", 0):
+            # the rigid-motion multipliers r (the R-space part of the reference's mixed function)
+            extra = [s._rigid_r.clone() if deepcopy else s._rigid_r]
+        return tuple([u] + ps + extra)
 
     def assign(self, other):
         src = other.vector() if isinstance(other, Function) else other
@@ -77,8 +81,8 @@ class MPETSolver:
         if mesh.gdim not in (2, 3) or mesh.tdim != mesh.gdim:
             raise NotImplementedError("the GPU engine assembles triangle (2D) and tetrahedral (3D) meshes")
         self.dim = mesh.gdim
-        if problem.u_has_nullspace or any(problem.p_has_nullspace):
-            raise NotImplementedError("rigid-motion / constant nullspace multipliers are not built on the GPU")
+        if any(problem.p_has_nullspace):
+            raise NotImplementedError("constant-pressure nullspace multipliers are not built on the GPU")
         pp = problem.params
         self.J = int(pp["J"])
         S = np.asarray([[float(v) for v in row] for row in pp["S"]], dtype=np.float64).reshape(self.J, self.J)
@@ -122,6 +126,17 @@ class MPETSolver:
         self.dt = Constant(float(self.params["dt"]))
         self._bcs = self.create_dirichlet_bcs()
         self._node_x = None
+        # rigid-motion modes of a displacement without Dirichlet conditions
+        # (the R-space multipliers of mpetsolver.py:115-124, 204-207)
+        self.nrigid = 0
+        self._rigid_r = None
+        if problem.u_has_nullspace:
+            from .nullspace import rigid_motions
+            Z = rigid_motions(mesh, self._node_coordinates().cpu().numpy())
+            self.nrigid = Z.shape[0]
+            self._rigid_Z = torch.as_tensor(np.ascontiguousarray(Z.reshape(self.nrigid, -1)), device=self.device)
+            self._ctx.call("mpet_set_rigid_modes", self.nrigid, _lib._ptr(self._rigid_Z))
+            self._rigid_r = torch.zeros(self.nrigid, dtype=torch.float64, device=self.device)
         self._assembled_dt = None
         self._prec_dt = None
         self._f = None
@@ -167,6 +182,12 @@ class MPETSolver:
         w = self.params["prec_u_weight"]
         prm.prec_u_weight = (mu + lmbda) if w == "mu+lmbda" else (mu if w == "mu" else float(w))
         prm.prec_network_modes = 1 if self.params["prec_network_modes"] else 0
+        if self.problem.u_has_nullspace:
+            # mass shift of the displacement preconditioner block at the scale of the
+            # lowest elastic mode: (mu + lambda) / diam^2
+            xs = np.asarray(self.problem.mesh.coordinates())
+            diam = float(np.linalg.norm(xs.max(0) - xs.min(0)))
+            prm.prec_u_shift = (mu + lmbda) / diam ** 2
         return prm
 
     def _check_facet_data(self):
@@ -368,6 +389,10 @@ class MPETSolver:
         self.solver_monitor["niter"].append(st.iterations)
         self.solver_monitor["relres"].append(st.relres)
         self.last_stats = st.as_dict()
+        if self.nrigid:
+            r = np.zeros(self.nrigid)
+            self._ctx.call("mpet_get_rigid_multipliers", _lib._ptr(r))
+            self._rigid_r.copy_(_torch().as_tensor(r))
         return st
 
     def step(self, dt=None, up_=None):
