@@ -46,6 +46,17 @@ extern "C" {
 #define MPET_PRECISION_FP64 0  /* FP64 matrix, FP64 MINRES, FP64 AMG */
 #define MPET_PRECISION_MIXED 1 /* FP32 inner MINRES + AMG inside FP64 refinement */
 
+/* Block systems.  MPET_FORM_MPET: u and the J network pressures (MPETSolver,
+ * src/mpet/mpet/mpetsolver.py:196-261).  MPET_FORM_TOTAL_PRESSURE: u, the
+ * total pressure p0 = lmbda div u - sum_i alpha_i p_i and the networks
+ * (MPETTotalPressureSolver, src/mpet/mpet/mpettotalpressuresolver.py:262-305);
+ * pressure field 0 is p0 and fields 1..J-1 the networks, so num_networks,
+ * alpha, c, K, S and the continuity markers count p0 as field 0 (alpha[0] = 1
+ * weights p0 in the rank-one term, c[0] = K[0] = S[0][*] = S[*][0] = 0, and
+ * field 0 carries no boundary condition). */
+#define MPET_FORM_MPET 0
+#define MPET_FORM_TOTAL_PRESSURE 1
+
 typedef struct mpet_ctx mpet_ctx;
 
 /* Problem and solver parameters.  Material keys follow MPETProblem.params
@@ -81,6 +92,11 @@ typedef struct mpet_params {
     double prec_u_shift;               /* g in + g (u, v) added to that block (keeps it definite
                                           when the displacement has no Dirichlet condition, e.g.
                                           with rigid-motion modes); 0 for none */
+    int32_t formulation;               /* MPET_FORM_*: the block system assembled */
+    int32_t pad1;
+    double prec_p0_weight;             /* total-pressure form: w0 in the p0 block w0 (p0, w0) of
+                                          the preconditioner (the reference form uses 1,
+                                          mpettotalpressuresolver.py:281); <= 0 means 1 */
 } mpet_params;
 
 typedef struct mpet_stats {

@@ -49,6 +49,7 @@ def exact_solutions(params, dim=2):
     U = [lam(e) for e in u]
     dU = [[lam(sympy.diff(u[i], x[j])) for j in range(dim)] for i in range(dim)]
     P = [lam(e) for e in p[1:]]
+    P0 = lam(p[0])
     dP = [[lam(sympy.diff(p[i + 1], x[j])) for j in range(dim)] for i in range(J)]
     F = [lam(e) for e in f]
     G = [lam(e) for e in g]
@@ -71,6 +72,7 @@ def exact_solutions(params, dim=2):
         "du": lambda xx, tt: np.stack([np.stack([bcast(dU[i][j], xx, tt) for j in range(dim)], 1)
                                        for i in range(dim)], 1),
         "p": [(lambda i: (lambda xx, tt: bcast(P[i], xx, tt)))(i) for i in range(J)],
+        "p0": lambda xx, tt: bcast(P0, xx, tt),
         "dp": [(lambda i: (lambda xx, tt: np.stack([bcast(dP[i][j], xx, tt) for j in range(dim)], 1)))(i)
                for i in range(J)],
     }

@@ -2,7 +2,7 @@
 
 ``from waterscapes_gb300 import *`` mirrors ``from mpet import *``
 (src/mpet/mpet/__init__.py:10-17) for the hot path: MPETProblem,
-MPETSolver, the parameter conversions and the mesh/marker vocabulary.
+MPETSolver, MPETTotalPressureSolver, the parameter conversions and the mesh/marker vocabulary.
 """
 from .mesh import (INVALID_MARKER, CompiledSubDomain, EllipsoidShellMesh, Mesh, MeshFunction,
                    UnitCubeMesh, UnitSquareMesh, near)
@@ -17,9 +17,12 @@ def __getattr__(name):
     if name == "MPETBatchSolver":
         from . import batch
         return batch.MPETBatchSolver
+    if name == "MPETTotalPressureSolver":
+        from . import totalpressure
+        return totalpressure.MPETTotalPressureSolver
     raise AttributeError(name)
 
 
 __all__ = ["Mesh", "MeshFunction", "CompiledSubDomain", "UnitCubeMesh", "UnitSquareMesh",
            "EllipsoidShellMesh", "near", "INVALID_MARKER", "Constant", "Expression", "MPETProblem",
-           "MPETSolver", "MPETBatchSolver", "convert_to_E_nu", "convert_to_mu_lmbda"]
+           "MPETSolver", "MPETBatchSolver", "MPETTotalPressureSolver", "convert_to_E_nu", "convert_to_mu_lmbda"]

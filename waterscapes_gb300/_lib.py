@@ -23,6 +23,7 @@ ERRORS = {
     -7: "MPET_ERR_STATE",
 }
 PRECISION = {"fp64": 0, "mixed": 1}
+FORMULATION = {"mpet": 0, "total_pressure": 1}
 MAX_NETWORKS = 8
 
 
@@ -49,6 +50,9 @@ class MpetParams(ctypes.Structure):
         ("prec_network_modes", ctypes.c_int32),
         ("prec_u_weight", ctypes.c_double),
         ("prec_u_shift", ctypes.c_double),
+        ("formulation", ctypes.c_int32),
+        ("pad1", ctypes.c_int32),
+        ("prec_p0_weight", ctypes.c_double),
     ]
 
 

@@ -153,6 +153,16 @@ static void check_params(const mpet_ctx* c, const mpet_params* p) {
             "unknown precision");
     require(p->theta > 0.0 && p->theta <= 1.0, MPET_ERR_INVALID, "theta must be in (0, 1]");
     require(p->rtol > 0.0, MPET_ERR_INVALID, "rtol must be positive");
+    require(p->formulation == MPET_FORM_MPET || p->formulation == MPET_FORM_TOTAL_PRESSURE, MPET_ERR_INVALID,
+            "unknown formulation");
+    if (p->formulation == MPET_FORM_TOTAL_PRESSURE) {
+        require(c->J >= 2, MPET_ERR_INVALID, "the total-pressure form needs p0 and at least one network");
+        require(p->lmbda > 0.0, MPET_ERR_INVALID, "the total-pressure form needs lmbda > 0");
+        bool field0 = p->alpha[0] == 1.0 && p->c[0] == 0.0 && p->K[0] == 0.0;
+        for (int b = 0; b < c->J; ++b)
+            field0 = field0 && p->S[b] == 0.0 && p->S[b * MPET_MAX_NETWORKS] == 0.0;
+        require(field0, MPET_ERR_INVALID, "total-pressure field 0 needs alpha = 1, c = K = 0 and no transfer");
+    }
 }
 
 int mpet_setup(mpet_ctx* c, const mpet_params* p) {
@@ -323,6 +333,8 @@ int mpet_set_sources(mpet_ctx* c, const double* f, const double* g) {
 
 int mpet_set_cell_permeability(mpet_ctx* c, const double* K_cells) {
     API_BEGIN(c)
+    require(!c->setup_done || c->prm.formulation == MPET_FORM_MPET, MPET_ERR_INVALID,
+            "built for the MPET form only");
     require(c->setup_done, MPET_ERR_STATE, "mpet_setup must come first");
     c->K_cells = K_cells;
     c->assembled = false;
@@ -362,6 +374,8 @@ int mpet_get_rigid_multipliers(mpet_ctx* c, double* r) {
 
 int mpet_set_cell_coefficients(mpet_ctx* c, const double* c_cells, const double* S_cells) {
     API_BEGIN(c)
+    require(!c->setup_done || c->prm.formulation == MPET_FORM_MPET, MPET_ERR_INVALID,
+            "built for the MPET form only");
     require(c->setup_done, MPET_ERR_STATE, "mpet_setup must come first");
     c->c_cells = c_cells;
     c->S_cells = S_cells;
@@ -372,6 +386,8 @@ int mpet_set_cell_coefficients(mpet_ctx* c, const double* c_cells, const double*
 
 int mpet_set_batch(mpet_ctx* c, int32_t ninst, const int32_t* vertex_instance) {
     API_BEGIN(c)
+    require(!c->setup_done || c->prm.formulation == MPET_FORM_MPET, MPET_ERR_INVALID,
+            "built for the MPET form only");
     require(c->setup_done, MPET_ERR_STATE, "mpet_setup must come first");
     require(c->dim == 3, MPET_ERR_INVALID, "batches are built for tetrahedral meshes");
     require(c->ninst == 0, MPET_ERR_STATE, "the batch partition is already set");
@@ -655,6 +671,8 @@ int mpet_get_timing(mpet_ctx* c, double* inner_ms, int64_t* inner_iterations, do
 
 int mpet_pressure_misfit(mpet_ctx* c, const double* up, const double* p_target, double* loss, double* dloss) {
     API_BEGIN(c)
+    require(!c->setup_done || c->prm.formulation == MPET_FORM_MPET, MPET_ERR_INVALID,
+            "built for the MPET form only");
     require(c->setup_done, MPET_ERR_STATE, "mpet_setup must come first");
     require(c->dim == 3, MPET_ERR_INVALID, "the adjoint is built for tetrahedral meshes");
     require(up && p_target && loss, MPET_ERR_INVALID, "NULL argument");
@@ -673,6 +691,8 @@ static void require_adjoint_ok(mpet_ctx* c) {
 
 int mpet_adjoint_rhs(mpet_ctx* c, double dt, const double* lam, double* out) {
     API_BEGIN(c)
+    require(!c->setup_done || c->prm.formulation == MPET_FORM_MPET, MPET_ERR_INVALID,
+            "built for the MPET form only");
     require(c->setup_done, MPET_ERR_STATE, "mpet_setup must come first");
     require(lam && out && lam != out, MPET_ERR_INVALID, "lam and out must be distinct device arrays");
     require_adjoint_ok(c);
@@ -683,6 +703,8 @@ int mpet_adjoint_rhs(mpet_ctx* c, double dt, const double* lam, double* out) {
 int mpet_adjoint_step(mpet_ctx* c, double dt, const double* seed, const double* up_prev, const double* up,
                       double* lam, double* grad_K, mpet_stats* st) {
     API_BEGIN(c)
+    require(!c->setup_done || c->prm.formulation == MPET_FORM_MPET, MPET_ERR_INVALID,
+            "built for the MPET form only");
     require(c->assembled, MPET_ERR_STATE, "mpet_assemble must come first");
     require(c->precond_ready, MPET_ERR_STATE, "mpet_setup_preconditioner must come first");
     require(seed && lam && lam != seed, MPET_ERR_INVALID, "seed and lam must be distinct device arrays");

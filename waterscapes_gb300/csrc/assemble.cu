@@ -50,6 +50,13 @@ struct MatCoef {
     int64_t nc;
     double prec_mu;                                    // weight of the displacement preconditioner block
     double prec_shift;                                 // + prec_shift (u, v) in that block
+    // Form-dependent coefficients.  MPET: cpl_a = -alpha_a in (p_a, div v) and (div u, q_a),
+    // rhs_cu_a = -alpha_a on (div u^-, q_a), no rank-one term.  Total pressure: cpl = (1, 0, ..),
+    // rhs_cu = 0, and the rank-one mass term -(beta_a beta_b / lmbda) (p_b, w_a), beta = alpha
+    // with beta_0 = 1, whose previous-time part enters the network rows only (rank_rhs_0 = 0).
+    double cpl[MPET_MAX_NETWORKS], rhs_cu[MPET_MAX_NETWORKS];
+    double rank_b[MPET_MAX_NETWORKS], rank_rhs[MPET_MAX_NETWORKS], rank_inv;
+    double prec_extra[MPET_MAX_NETWORKS];              // + prec_extra_a (p_a, w_a) in pressure block a
     __device__ __forceinline__ double Kof(int a, int64_t cell) const { return Kc ? Kc[a * nc + cell] : K[a]; }
     __device__ __forceinline__ double cof(int a, int64_t cell) const { return cc ? cc[a * nc + cell] : c[a]; }
     __device__ __forceinline__ double Sof(int a, int b, int64_t cell) const {
@@ -220,13 +227,13 @@ __global__ void __launch_bounds__(256) k_assemble_matrix(AsmArgs A, MatCoef P) {
                     const int tt = t - T1, k = tt / NV, w = tt % NV;
                     const double C = w20 * (gm[w][k] + sm[k]);
                     const int64_t base = rp[k] + D * (int64_t)d2 + rk1[w];
-                    for (int a = 0; a < J; ++a) A.v64[base + (int64_t)a * d1] += -P.alpha[a] * C;
+                    for (int a = 0; a < J; ++a) A.v64[base + (int64_t)a * d1] += P.cpl[a] * C;
                 } else if (t < T3) {
                     const int tt = t - T2, j = tt / D, l = tt % D;
                     double g[3], s[3];
                     p2_grad_at<D>(G, j, m, g, s);
                     const double C = w20 * (g[l] + s[l]);
-                    for (int a = 0; a < J; ++a) A.v64[rp[D + a] + D * (int64_t)rk2[j] + l] += -P.alpha[a] * C;
+                    for (int a = 0; a < J; ++a) A.v64[rp[D + a] + D * (int64_t)rk2[j] + l] += P.cpl[a] * C;
                 } else {
                     const int w = t - T3;
                     const double M1 = w20 * (m == w ? 2.0 : 1.0);
@@ -234,7 +241,8 @@ __global__ void __launch_bounds__(256) k_assemble_matrix(AsmArgs A, MatCoef P) {
                     for (int a = 0; a < J; ++a) {
                         const int64_t base = rp[D + a] + D * (int64_t)d2 + rk1[w];
                         for (int b = 0; b < J; ++b) {
-                            double v = -P.dt_theta * ((a == b ? P.Ssumof(a, cell) : 0.0) - P.Sof(a, b, cell)) * M1;
+                            double v = -(P.dt_theta * ((a == b ? P.Ssumof(a, cell) : 0.0) - P.Sof(a, b, cell)) +
+                                         P.rank_inv * P.rank_b[a] * P.rank_b[b]) * M1;
                             if (a == b) v += -P.cof(a, cell) * M1 - P.dt_theta * P.Kof(a, cell) * L1;
                             A.v64[base + (int64_t)b * d1] += v;
                         }
@@ -360,7 +368,8 @@ __global__ void __launch_bounds__(256) k_assemble_prec(PrecArgs A, MatCoef P) {
                         for (int a = 0; a < J; ++a) {
                             if (A.vert_bc[(int64_t)a * A.nv + i] || A.vert_bc[(int64_t)a * A.nv + vw]) continue;
                             double sS = P.Ssumof(a, cell) - P.Sof(a, a, cell);
-                            A.pp[a][pos] += (P.cof(a, cell) + P.dt_theta * sS) * M1 + P.dt_theta * P.Kof(a, cell) * L1;
+                            A.pp[a][pos] += (P.cof(a, cell) + P.dt_theta * sS + P.prec_extra[a]) * M1 +
+                                            P.dt_theta * P.Kof(a, cell) * L1;
                         }
                     }
                 }
@@ -448,8 +457,11 @@ __global__ void __launch_bounds__(128) k_rhs_p(RhsArgs A, MatCoef P) {
             lp[a] = sl;
             acc[a] += A.dt * sg;
         }
+        double rank = 0.0;
+        if (P.rank_inv != 0.0)
+            for (int b = 0; b < J; ++b) rank += P.rank_b[b] * mp[b];
         for (int a = 0; a < J; ++a) {
-            double t = -P.alpha[a] * cp - P.cof(a, cell) * mp[a] + omt * P.Kof(a, cell) * lp[a];
+            double t = P.rhs_cu[a] * cp - P.cof(a, cell) * mp[a] + omt * P.Kof(a, cell) * lp[a] - P.rank_rhs[a] * rank;
             for (int b = 0; b < J; ++b) {
                 const double sab = P.Sof(a, b, cell);
                 if (ADJ) t += omt * (sab * mp[a] - P.Sof(b, a, cell) * mp[b]);
@@ -539,6 +551,18 @@ static MatCoef make_coef(const mpet_ctx* c, double dt) {
     P.nc = c->nc;
     P.prec_mu = c->prm.prec_u_weight > 0.0 ? c->prm.prec_u_weight : c->prm.mu;
     P.prec_shift = c->prm.prec_u_shift > 0.0 ? c->prm.prec_u_shift : 0.0;
+    const bool tp = c->prm.formulation == MPET_FORM_TOTAL_PRESSURE;
+    P.rank_inv = tp ? 1.0 / c->prm.lmbda : 0.0;
+    if (tp) P.lmbda = 0.0;  // 2 mu (eps u, eps v) only
+    for (int a = 0; a < c->J; ++a) {
+        P.cpl[a] = tp ? (a == 0 ? 1.0 : 0.0) : -c->prm.alpha[a];
+        P.rhs_cu[a] = tp ? 0.0 : -c->prm.alpha[a];
+        P.rank_b[a] = tp ? (a == 0 ? 1.0 : c->prm.alpha[a]) : 0.0;
+        P.rank_rhs[a] = (tp && a > 0) ? P.rank_b[a] * P.rank_inv : 0.0;
+        P.prec_extra[a] = !tp ? 0.0
+                        : a == 0 ? (c->prm.prec_p0_weight > 0.0 ? c->prm.prec_p0_weight : 1.0)
+                                 : c->prm.alpha[a] * c->prm.alpha[a] * P.rank_inv;
+    }
     return P;
 }
 
@@ -862,7 +886,7 @@ void set_instances(mpet_ctx* c, int ninst, const int32_t* vertex_inst_host) {
 void setup_network_modes(mpet_ctx* c, double dt) {
     const int J = c->J;
     c->net_modes = false;
-    if (!c->prm.prec_network_modes || J < 2) return;
+    if (!c->prm.prec_network_modes || J < 2 || c->prm.formulation != MPET_FORM_MPET) return;
     // the transform mixes the networks at a vertex: all networks need the same Dirichlet vertices
     std::vector<uint8_t> vb((size_t)J * c->nv);
     MPET_CUDA(cudaMemcpyAsync(vb.data(), c->vert_bc, vb.size(), cudaMemcpyDeviceToHost, c->stream));

@@ -180,7 +180,7 @@ class MPETSolver:
         prm.check_every = int(self.params["check_every"])
         prm.amg_p2_to_p1 = 1 if self.params["amg_p2_to_p1"] else 0
         w = self.params["prec_u_weight"]
-        prm.prec_u_weight = (mu + lmbda) if w == "mu+lmbda" else (mu if w == "mu" else float(w))
+        prm.prec_u_weight = {"mu+lmbda": mu + lmbda, "mu": mu, "2mu": 2.0 * mu}[w] if isinstance(w, str) else float(w)
         prm.prec_network_modes = 1 if self.params["prec_network_modes"] else 0
         if self.problem.u_has_nullspace:
             # mass shift of the displacement preconditioner block at the scale of the
