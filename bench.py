@@ -533,6 +533,8 @@ def main():
     ap.add_argument("--instances", type=int, default=256)
     ap.add_argument("--n-min", type=int, default=8)
     ap.add_argument("--n-max", type=int, default=32)
+    ap.add_argument("--formulation", default="mpet", choices=["mpet", "total-pressure"],
+                    help="total-pressure: MPETTotalPressureSolver (u, p0, networks) on the same workload")
     args = ap.parse_args()
     if args.batch:
         return batch_run(args)
@@ -541,8 +543,11 @@ def main():
     if args.adjoint:
         return adjoint_check(args)
     n, J = args.n, args.networks
-    N_full = 3 * (2 * n + 1) ** 3 + J * (n + 1) ** 3
+    tp = args.formulation == "total-pressure"
+    N_full = 3 * (2 * n + 1) ** 3 + (J + int(tp)) * (n + 1) ** 3
     workload_name = "Kuhn cube %d^3 x 6 tets, A=%d networks, P2/P1 (N=%d)" % (n, J, N_full)
+    if tp:
+        workload_name += ", total-pressure form (u, p0, p_1..p_A)"
     if args.workload == "ellipsoid":
         workload_name = ("jittered ellipsoidal shell (1, 0.8, 0.7; inner 0.3), %d radial layers, %d tets, A=%d, "
                          "log-normal per-cell K" % (n, 144 * n ** 3, J))
@@ -574,14 +579,15 @@ def main():
         import torch.distributed as dist
         dist.init_process_group("gloo")
     torch.cuda.set_device(local_rank)
-    from waterscapes_gb300 import MPETSolver, _lib
+    from waterscapes_gb300 import MPETSolver, MPETTotalPressureSolver, _lib
     lib = _lib
+    Solver = MPETTotalPressureSolver if tp else MPETSolver
     hbm, peak_kind = peaks()
 
     problem, dt = workload(n, J, args.workload)
     base = dict(dt=dt, T=1e9, theta=1.0, rtol=1e-10, device=local_rank)
     t0 = time.perf_counter()
-    sol = MPETSolver(problem, dict(base, precision="mixed"))
+    sol = Solver(problem, dict(base, precision="mixed"))
     t_setup = time.perf_counter() - t0
     torch.cuda.synchronize()
     t0 = time.perf_counter()
@@ -638,7 +644,7 @@ def main():
     res = {"mixed": {"ms_per_step": ms_mixed / args.steps, "iterations": its_mixed}}
     rel_err = None
     if not args.no_fp64:
-        sol64 = MPETSolver(problem, dict(base, precision="fp64"))
+        sol64 = Solver(problem, dict(base, precision="fp64"))
         sol64._assemble(dt)
         spmv64 = time_spmv(sol64, torch, lib)
         spmv["fp64_only_ctx"] = spmv64.get("fp64")
@@ -651,7 +657,7 @@ def main():
         del sol64
 
     cpu = None
-    if rank == 0 and not args.no_cpu:
+    if rank == 0 and not args.no_cpu and not tp:
         sec, Ns = cpu_baseline_sample(12, J, steps=1)
         cpu_val = 1.0 / (sec * N_full / Ns)
         cpu = {"value": cpu_val, "unit": "steps/s", "cores": 1, "kind": "port",
