@@ -322,6 +322,24 @@ int mpet_set_hierarchy_spmv_variant(mpet_ctx* ctx, int32_t variant);
 int mpet_get_timing(mpet_ctx* ctx, double* inner_ms, int64_t* inner_iterations,
                     double* solve_ms, int64_t* kernel_launches);
 
+/* ---- a posteriori error indicators (AdaptiveMPETSolver) --------------------
+ * DG0 indicators of src/mpet/mpet/adaptivempetsolver.py:82-155 for the step
+ * up_prev -> up (device vectors of length N) with time step dt:
+ * eta_p[K] (zeta_p_K), eta_u[K] (zeta_u_K), eta_u_dt[K] (zeta_u_dt_K), one
+ * device double per cell each, and the scalar R4p (:148-155) into *r4p_host.
+ * f_nodes / f_prev_nodes: body force at the current and previous time at the
+ * P2 nodes (nnodes x dim, NULL = 0); g_vert: sources at the vertices (J x nv,
+ * NULL = 0).  Interior facets, built once by the caller: ifacets (n_ifacets x 4
+ * int32: cell+, local vertex of cell+ opposite the facet, cell-, its local
+ * opposite vertex; local numbering of the ascending-sorted cell) and
+ * cell_facets (nc x (dim+1) int32: the interior facet opposite each local
+ * vertex, -1 on the boundary); both are range-checked on the device first.
+ * MPET form, scalar K, c, S and no batch only (MPET_ERR_INVALID otherwise). */
+int mpet_error_indicators(mpet_ctx* ctx, double dt, const double* up, const double* up_prev,
+                          const double* f_nodes, const double* f_prev_nodes, const double* g_vert,
+                          int64_t n_ifacets, const int32_t* ifacets, const int32_t* cell_facets,
+                          double* eta_p, double* eta_u, double* eta_u_dt, double* r4p_host);
+
 /* ---- discrete adjoint with respect to per-cell permeability ----------------
  * The reference has no adjoint; these entry points differentiate the
  * solve_direct time loop (mpetsolver.py:382-462) as this library discretises

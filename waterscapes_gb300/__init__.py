@@ -17,6 +17,9 @@ def __getattr__(name):
     if name == "MPETBatchSolver":
         from . import batch
         return batch.MPETBatchSolver
+    if name == "AdaptiveMPETSolver":
+        from . import adaptive
+        return adaptive.AdaptiveMPETSolver
     if name == "MPETTotalPressureSolver":
         from . import totalpressure
         return totalpressure.MPETTotalPressureSolver
@@ -25,4 +28,4 @@ def __getattr__(name):
 
 __all__ = ["Mesh", "MeshFunction", "CompiledSubDomain", "UnitCubeMesh", "UnitSquareMesh",
            "EllipsoidShellMesh", "near", "INVALID_MARKER", "Constant", "Expression", "MPETProblem",
-           "MPETSolver", "MPETBatchSolver", "MPETTotalPressureSolver", "convert_to_E_nu", "convert_to_mu_lmbda"]
+           "MPETSolver", "MPETBatchSolver", "MPETTotalPressureSolver", "AdaptiveMPETSolver", "convert_to_E_nu", "convert_to_mu_lmbda"]

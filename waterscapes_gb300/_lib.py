@@ -126,6 +126,7 @@ SIGNATURES = {
     "mpet_get_node_block_info": [_P, ctypes.POINTER(_I64), ctypes.POINTER(_I64)],
     "mpet_get_timing": [_P, ctypes.POINTER(_D), ctypes.POINTER(_I64), ctypes.POINTER(_D), ctypes.POINTER(_I64)],
     "mpet_pressure_misfit": [_P, _P, _P, ctypes.POINTER(_D), _P],
+    "mpet_error_indicators": [_P, _D, _P, _P, _P, _P, _P, _I64, _P, _P, _P, _P, _P, ctypes.POINTER(_D)],
     "mpet_adjoint_rhs": [_P, _D, _P, _P],
     "mpet_adjoint_step": [_P, _D, _P, _P, _P, _P, _P, ctypes.POINTER(MpetStats)],
 }

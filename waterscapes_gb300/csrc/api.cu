@@ -669,6 +669,25 @@ int mpet_get_timing(mpet_ctx* c, double* inner_ms, int64_t* inner_iterations, do
     API_END(c)
 }
 
+int mpet_error_indicators(mpet_ctx* c, double dt, const double* up, const double* up_prev, const double* f_nodes,
+                          const double* f_prev_nodes, const double* g_vert, int64_t n_ifacets,
+                          const int32_t* ifacets, const int32_t* cell_facets, double* eta_p, double* eta_u,
+                          double* eta_u_dt, double* r4p) {
+    API_BEGIN(c)
+    require(c->setup_done, MPET_ERR_STATE, "mpet_setup must come first");
+    require(c->prm.formulation == MPET_FORM_MPET, MPET_ERR_INVALID, "built for the MPET form only");
+    require(!c->K_cells && !c->c_cells && !c->S_cells && c->ninst == 0, MPET_ERR_INVALID,
+            "indicators take scalar K, c, S and a single instance");
+    require(dt > 0.0, MPET_ERR_INVALID, "dt must be positive");
+    require(up && up_prev && cell_facets && eta_p && eta_u && eta_u_dt && r4p && n_ifacets >= 0 &&
+                (n_ifacets == 0 || ifacets),
+            MPET_ERR_INVALID, "NULL argument");
+    require(launch_error_indicators(c, dt, up, up_prev, f_nodes, f_prev_nodes, g_vert, n_ifacets, ifacets,
+                                    cell_facets, eta_p, eta_u, eta_u_dt, r4p) == 0,
+            MPET_ERR_INVALID, "interior-facet tables do not match the mesh");
+    API_END(c)
+}
+
 int mpet_pressure_misfit(mpet_ctx* c, const double* up, const double* p_target, double* loss, double* dloss) {
     API_BEGIN(c)
     require(!c->setup_done || c->prm.formulation == MPET_FORM_MPET, MPET_ERR_INVALID,

@@ -971,4 +971,354 @@ void setup_network_modes(mpet_ctx* c, double dt) {
     c->net_modes = true;
 }
 
+// --- a posteriori error indicators (AdaptiveMPETSolver) ----------------------------
+//
+// DG0 indicators of adaptivempetsolver.py:82-155 for one step up_prev -> up:
+// cell residuals RK_u = f + div sigma(u) - sum_j alpha_j grad p_j (P2 per cell:
+// f is the P2 interpolant, div sigma(u) and grad p are constant) and
+// RK_p_j = -g_j - c_j (p_j - p_j^-)/dt - alpha_j div(u - u^-)/dt
+//          - sum_i S_ij (p_j - p_i)   (P1 per cell; div grad p = 0 for P1),
+// interior-facet residuals RE_u = -[sigma(u)] n (linear on the facet; the
+// pressure jump vanishes for continuous pressures) and RE_p_j = -K_j [grad p_j] n
+// (constant), all squared and integrated exactly with the simplex mass
+// matrices; h = cell diameter (largest vertex distance).  A thread per cell
+// writes the cell terms, a thread per interior facet its half-weighted facet
+// terms 0.5 avg(h) ||RE||_F^2, and a thread per cell adds the terms of its
+// interior facets in local order: no atomics, results reproducible.
+
+struct EstArgs {
+    int64_t nc, nv, Nu, nfi;
+    const double* geo;
+    const double* x;
+    const int32_t* cells;
+    const int32_t* cell_nodes;
+    const double* up;
+    const double* upp;
+    const double* f;
+    const double* fp;
+    const double* g;
+    const int32_t* ifacets;
+    const int32_t* cell_facets;
+    double dt;
+    double* eta_p;
+    double* eta_u;
+    double* eta_udt;
+    double* r4;
+    double* fval;
+    int32_t* bad;
+};
+
+template <int D>
+__device__ __forceinline__ double cell_diameter(const EstArgs& A, int64_t cell) {
+    constexpr int NV = Simplex<D>::NV;
+    double h2 = 0.0;
+    for (int r = 0; r < NV; ++r)
+        for (int s = r + 1; s < NV; ++s) {
+            const int64_t a = A.cells[NV * cell + r], b = A.cells[NV * cell + s];
+            double q = 0.0;
+            for (int k = 0; k < D; ++k) {
+                const double t = A.x[3 * a + k] - A.x[3 * b + k];
+                q += t * t;
+            }
+            h2 = fmax(h2, q);
+        }
+    return sqrt(h2);
+}
+
+// sigma(u) at local vertex r of a cell from the P2 displacement in v
+template <int D>
+__device__ __forceinline__ void sigma_at_vertex(const EstArgs& A, const Geo& G, const MatCoef& P, int64_t cell,
+                                                const double* v, int r, double sg[3][3]) {
+    constexpr int NN = Simplex<D>::NN;
+    double gu[3][3] = {{0, 0, 0}, {0, 0, 0}, {0, 0, 0}};
+    for (int j = 0; j < NN; ++j) {
+        double g[3], s[3];
+        p2_grad_at<D>(G, j, r, g, s);
+        const int64_t nj = A.cell_nodes[NN * cell + j];
+        for (int a = 0; a < D; ++a) {
+            const double ua = v[D * nj + a];
+            for (int b = 0; b < D; ++b) gu[a][b] += ua * g[b];
+        }
+    }
+    double tr = 0.0;
+    for (int a = 0; a < D; ++a) tr += gu[a][a];
+    for (int a = 0; a < D; ++a)
+        for (int b = 0; b < D; ++b) sg[a][b] = P.mu * (gu[a][b] + gu[b][a]) + (a == b ? P.lmbda * tr : 0.0);
+}
+
+template <int D>
+__global__ void __launch_bounds__(128) k_est_cell(EstArgs A, MatCoef P) {
+    constexpr int NV = Simplex<D>::NV, NN = Simplex<D>::NN;
+    const int64_t cell = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    if (cell >= A.nc) return;
+    Geo G;
+    load_geo(A.geo, cell, G);
+    const int J = P.J;
+    int64_t vt[4];
+    for (int r = 0; r < NV; ++r) vt[r] = A.cells[NV * cell + r];
+    double divs[2][3], tr[2][4];
+    for (int st = 0; st < 2; ++st) {
+        const double* v = st ? A.upp : A.up;
+        for (int a = 0; a < 3; ++a) divs[st][a] = 0.0;
+        for (int r = 0; r < NV; ++r) {
+            double sg[3][3];
+            sigma_at_vertex<D>(A, G, P, cell, v, r, sg);
+            double t = 0.0;
+            for (int a = 0; a < D; ++a) {
+                for (int b = 0; b < D; ++b) divs[st][a] += sg[a][b] * G.b[r][b];
+            }
+            // div u at vertex r
+            for (int j = 0; j < NN; ++j) {
+                double g[3], s[3];
+                p2_grad_at<D>(G, j, r, g, s);
+                const int64_t nj = A.cell_nodes[NN * cell + j];
+                for (int a = 0; a < D; ++a) t += v[D * nj + a] * g[a];
+            }
+            tr[st][r] = t;
+        }
+        for (int a = 0; a < J; ++a) {
+            const double* pa = v + A.Nu + (int64_t)a * A.nv;
+            for (int k = 0; k < D; ++k) {
+                double gk = 0.0;
+                for (int r = 0; r < NV; ++r) gk += pa[vt[r]] * G.b[r][k];
+                divs[st][k] -= P.alpha[a] * gk;
+            }
+        }
+    }
+    // momentum cell residuals: values at the P2 nodes, integrated with the P2 mass
+    const double w2 = G.vol / (D == 3 ? 420.0 : 180.0);
+    double iu = 0.0, iudt = 0.0;
+    for (int a = 0; a < D; ++a) {
+        double R[NN], Rd[NN];
+        for (int i = 0; i < NN; ++i) {
+            const int64_t ni = A.cell_nodes[NN * cell + i];
+            const double fi = A.f ? A.f[D * ni + a] : 0.0;
+            const double fpi = A.fp ? A.fp[D * ni + a] : 0.0;
+            R[i] = fi + divs[0][a];
+            Rd[i] = (R[i] - (fpi + divs[1][a])) / A.dt;
+        }
+        for (int i = 0; i < NN; ++i)
+            for (int j = 0; j < NN; ++j) {
+                const double m = D == 3 ? c_m2[i][j] : c_m2t[i][j];
+                iu += R[i] * m * R[j];
+                iudt += Rd[i] * m * Rd[j];
+            }
+    }
+    const double h = cell_diameter<D>(A, cell);
+    const double kv = kappa<D>() * G.vol;
+    // mass-equation cell residuals (P1) and the R4p density
+    double ip = 0.0, r4 = 0.0;
+    for (int j = 0; j < J; ++j) {
+        const double* pj = A.up + A.Nu + (int64_t)j * A.nv;
+        const double* pjp = A.upp + A.Nu + (int64_t)j * A.nv;
+        double R[4], sR = 0.0, qR = 0.0;
+        for (int r = 0; r < NV; ++r) {
+            double v = -(A.g ? A.g[(int64_t)j * A.nv + vt[r]] : 0.0) - P.c[j] * (pj[vt[r]] - pjp[vt[r]]) / A.dt -
+                       P.alpha[j] * (tr[0][r] - tr[1][r]) / A.dt;
+            for (int i = 0; i < J; ++i)
+                v -= P.S[i * MPET_MAX_NETWORKS + j] * (pj[vt[r]] - A.up[A.Nu + (int64_t)i * A.nv + vt[r]]);
+            R[r] = v;
+            sR += v;
+            qR += v * v;
+        }
+        ip += kv * (qR + sR * sR);
+        double gd[3] = {0.0, 0.0, 0.0};
+        for (int r = 0; r < NV; ++r)
+            for (int k = 0; k < D; ++k) gd[k] += (pj[vt[r]] - pjp[vt[r]]) * G.b[r][k];
+        r4 += P.K[j] * G.vol * (gd[0] * gd[0] + gd[1] * gd[1] + gd[2] * gd[2]);
+        for (int i = 0; i < J; ++i) {
+            const double sij = P.S[i * MPET_MAX_NETWORKS + j];
+            if (!(sij > 3.0e-16)) continue;
+            const double* pi = A.up + A.Nu + (int64_t)i * A.nv;
+            const double* pip = A.upp + A.Nu + (int64_t)i * A.nv;
+            double ab = 0.0, sa = 0.0, sb = 0.0;
+            for (int r = 0; r < NV; ++r) {
+                const double b = pj[vt[r]] - pjp[vt[r]];
+                const double a = b - (pi[vt[r]] - pip[vt[r]]);
+                ab += a * b;
+                sa += a;
+                sb += b;
+            }
+            r4 += sij * kv * (ab + sa * sb);
+        }
+    }
+    A.eta_u[cell] = h * h * w2 * iu;
+    A.eta_udt[cell] = h * h * w2 * iudt;
+    A.eta_p[cell] = h * h * ip;
+    A.r4[cell] = r4;
+}
+
+template <int D>
+__global__ void __launch_bounds__(128) k_est_facet(EstArgs A, MatCoef P) {
+    constexpr int NV = Simplex<D>::NV;
+    const int64_t f = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    if (f >= A.nfi) return;
+    const int64_t cp = A.ifacets[4 * f], cm = A.ifacets[4 * f + 2];
+    const int op = A.ifacets[4 * f + 1];
+    Geo Gp, Gm;
+    load_geo(A.geo, cp, Gp);
+    load_geo(A.geo, cm, Gm);
+    const double nb = sqrt(Gp.b[op][0] * Gp.b[op][0] + Gp.b[op][1] * Gp.b[op][1] + Gp.b[op][2] * Gp.b[op][2]);
+    double n[3];
+    for (int k = 0; k < 3; ++k) n[k] = -Gp.b[op][k] / nb;
+    const double area = D * Gp.vol * nb;
+    const int J = P.J;
+    double sq = 0.0, sqd = 0.0, sv[3] = {0, 0, 0}, svd[3] = {0, 0, 0};
+    for (int r = 0; r < NV; ++r) {
+        if (r == op) continue;
+        const int32_t vr = A.cells[NV * cp + r];
+        int rm = -1;
+        for (int q = 0; q < NV; ++q)
+            if (A.cells[NV * cm + q] == vr) rm = q;
+        if (rm < 0) {
+            *A.bad = 1;
+            return;
+        }
+        double e[3] = {0, 0, 0}, e0[3] = {0, 0, 0};
+        for (int st = 0; st < 2; ++st) {
+            const double* v = st ? A.upp : A.up;
+            double sp[3][3], sm[3][3];
+            sigma_at_vertex<D>(A, Gp, P, cp, v, r, sp);
+            sigma_at_vertex<D>(A, Gm, P, cm, v, rm, sm);
+            double* out = st ? e0 : e;
+            for (int a = 0; a < D; ++a) {
+                double t = 0.0;
+                for (int b = 0; b < D; ++b) t += (sp[a][b] - sm[a][b]) * n[b];
+                out[a] = -t;
+            }
+        }
+        for (int a = 0; a < D; ++a) {
+            const double ed = (e[a] - e0[a]) / A.dt;
+            sq += e[a] * e[a];
+            sqd += ed * ed;
+            sv[a] += e[a];
+            svd[a] += ed;
+        }
+    }
+    const double cF = area / (D * (D + 1));
+    const double iu = cF * (sq + sv[0] * sv[0] + sv[1] * sv[1] + sv[2] * sv[2]);
+    const double iudt = cF * (sqd + svd[0] * svd[0] + svd[1] * svd[1] + svd[2] * svd[2]);
+    double ip = 0.0;
+    for (int j = 0; j < J; ++j) {
+        const double* pj = A.up + A.Nu + (int64_t)j * A.nv;
+        double t = 0.0;
+        for (int r = 0; r < NV; ++r) {
+            const double a = pj[A.cells[NV * cp + r]], b = pj[A.cells[NV * cm + r]];
+            for (int k = 0; k < D; ++k) t += (a * Gp.b[r][k] - b * Gm.b[r][k]) * n[k];
+        }
+        const double re = -P.K[j] * t;
+        ip += area * re * re;
+    }
+    const double hav = 0.5 * (cell_diameter<D>(A, cp) + cell_diameter<D>(A, cm));
+    A.fval[3 * f] = 0.5 * hav * iu;
+    A.fval[3 * f + 1] = 0.5 * hav * iudt;
+    A.fval[3 * f + 2] = 0.5 * hav * ip;
+}
+
+template <int D>
+__global__ void k_est_gather(EstArgs A) {
+    constexpr int NV = Simplex<D>::NV;
+    const int64_t cell = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    if (cell >= A.nc) return;
+    double u = A.eta_u[cell], ud = A.eta_udt[cell], p = A.eta_p[cell];
+    for (int k = 0; k < NV; ++k) {
+        const int64_t fid = A.cell_facets[NV * cell + k];
+        if (fid < 0) continue;
+        u += A.fval[3 * fid];
+        ud += A.fval[3 * fid + 1];
+        p += A.fval[3 * fid + 2];
+    }
+    A.eta_u[cell] = u;
+    A.eta_udt[cell] = ud;
+    A.eta_p[cell] = p;
+}
+
+// index check of the caller's facet tables before any kernel reads through them
+__global__ void k_est_validate(int64_t nc, int nvc, int64_t nfi, const int32_t* __restrict__ ifacets,
+                               const int32_t* __restrict__ cell_facets, int32_t* bad) {
+    const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    if (i < nfi) {
+        const int32_t a = ifacets[4 * i], oa = ifacets[4 * i + 1], b = ifacets[4 * i + 2], ob = ifacets[4 * i + 3];
+        if (a < 0 || a >= nc || b < 0 || b >= nc || oa < 0 || oa >= nvc || ob < 0 || ob >= nvc) *bad = 1;
+    }
+    if (i < nc)
+        for (int k = 0; k < nvc; ++k) {
+            const int32_t fid = cell_facets[(int64_t)nvc * i + k];
+            if (fid < -1 || fid >= nfi) *bad = 1;
+        }
+}
+
+__global__ void __launch_bounds__(256) k_sum_array(int64_t n, const double* __restrict__ v, double* partials) {
+    __shared__ double sh[8];
+    double part = 0.0;
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
+        part += v[i];
+    part = block_sum256(part, sh);
+    if (threadIdx.x == 0) partials[blockIdx.x] = part;
+}
+
+int launch_error_indicators(mpet_ctx* c, double dt, const double* up, const double* up_prev, const double* f,
+                            const double* fp, const double* g, int64_t nfi, const int32_t* ifacets,
+                            const int32_t* cell_facets, double* eta_p, double* eta_u, double* eta_udt,
+                            double* r4_host) {
+    if (!c->est_bad) {
+        c->est_bad = c->pool.alloc<int32_t>(1);
+        c->est_r4 = c->pool.alloc<double>(c->nc);
+        c->est_sum = c->pool.alloc<double>(1);
+    }
+    if (nfi > c->est_fval_cap) {
+        c->est_fval = c->pool.alloc<double>(3 * (nfi > 0 ? nfi : 1));
+        c->est_fval_cap = nfi;
+    }
+    const int nvc = c->dim + 1;
+    MPET_CUDA(cudaMemsetAsync(c->est_bad, 0, sizeof(int32_t), c->stream));
+    const int64_t nmax = nfi > c->nc ? nfi : c->nc;
+    k_est_validate<<<grid_for(nmax, 256), 256, 0, c->stream>>>(c->nc, nvc, nfi, ifacets, cell_facets, c->est_bad);
+    MPET_CHECK_LAUNCH();
+    int32_t bad = 0;
+    MPET_CUDA(cudaMemcpyAsync(&bad, c->est_bad, sizeof(int32_t), cudaMemcpyDeviceToHost, c->stream));
+    MPET_CUDA(cudaStreamSynchronize(c->stream));
+    if (bad) return 1;
+    EstArgs A{};
+    A.nc = c->nc;
+    A.nv = c->nv;
+    A.Nu = c->Nu;
+    A.nfi = nfi;
+    A.geo = c->geo;
+    A.x = c->x;
+    A.cells = c->cells;
+    A.cell_nodes = c->cell_nodes;
+    A.up = up;
+    A.upp = up_prev;
+    A.f = f;
+    A.fp = fp;
+    A.g = g;
+    A.ifacets = ifacets;
+    A.cell_facets = cell_facets;
+    A.dt = dt;
+    A.eta_p = eta_p;
+    A.eta_u = eta_u;
+    A.eta_udt = eta_udt;
+    A.r4 = c->est_r4;
+    A.fval = c->est_fval;
+    A.bad = c->est_bad;
+    MatCoef P = make_coef(c, dt);
+    if (c->dim == 2) {
+        k_est_cell<2><<<grid_for(c->nc, 128), 128, 0, c->stream>>>(A, P);
+        if (nfi > 0) k_est_facet<2><<<grid_for(nfi, 128), 128, 0, c->stream>>>(A, P);
+        k_est_gather<2><<<grid_for(c->nc, 256), 256, 0, c->stream>>>(A);
+    } else {
+        k_est_cell<3><<<grid_for(c->nc, 128), 128, 0, c->stream>>>(A, P);
+        if (nfi > 0) k_est_facet<3><<<grid_for(nfi, 128), 128, 0, c->stream>>>(A, P);
+        k_est_gather<3><<<grid_for(c->nc, 256), 256, 0, c->stream>>>(A);
+    }
+    k_sum_array<<<NB_RED, 256, 0, c->stream>>>(c->nc, c->est_r4, c->partials);
+    k_finish_sum<<<1, 256, 0, c->stream>>>(c->partials, c->est_sum);
+    MPET_CHECK_LAUNCH();
+    MPET_CUDA(cudaMemcpyAsync(&bad, c->est_bad, sizeof(int32_t), cudaMemcpyDeviceToHost, c->stream));
+    MPET_CUDA(cudaMemcpyAsync(r4_host, c->est_sum, sizeof(double), cudaMemcpyDeviceToHost, c->stream));
+    MPET_CUDA(cudaStreamSynchronize(c->stream));
+    return bad ? 1 : 0;
+}
+
 }  // namespace mpet

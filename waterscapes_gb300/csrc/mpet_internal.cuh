@@ -300,6 +300,12 @@ struct mpet_ctx {
     unsigned char* l2_flush = nullptr;  // 256 MiB written between autotuner launches
     double* adj_b = nullptr;      // adjoint right-hand side (Dirichlet rows zeroed)
     double* adj_loss = nullptr;   // misfit value (1 double)
+    // error-indicator scratch: per-facet terms, per-cell R4p density, its sum, bad-index flag
+    double* est_fval = nullptr;
+    int64_t est_fval_cap = 0;
+    double* est_r4 = nullptr;
+    double* est_sum = nullptr;
+    int32_t* est_bad = nullptr;
     double* partials = nullptr;   // reduction partials
     mpet::MinresScalars* sc = nullptr;
     mpet::MinresScalars* sc_host = nullptr;  // pinned
@@ -432,6 +438,11 @@ void launch_mass_u(mpet_ctx* c, const double* f_nodes, double* out);
 void launch_adjoint_grad(mpet_ctx* c, double dt, const double* lam, const double* up_prev, const double* up,
                          double* grad);
 void launch_misfit(mpet_ctx* c, const double* up, const double* target, double* dloss, double* loss_dev);
+// returns nonzero when the facet tables are inconsistent with the mesh
+int launch_error_indicators(mpet_ctx* c, double dt, const double* up, const double* up_prev, const double* f,
+                            const double* fp, const double* g, int64_t nfi, const int32_t* ifacets,
+                            const int32_t* cell_facets, double* eta_p, double* eta_u, double* eta_udt,
+                            double* r4_host);
 
 // solve.cu
 template <typename T>
