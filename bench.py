@@ -331,6 +331,48 @@ def profile_case(args):
                       "nnz": sol.nnz, "step_s": time.perf_counter() - t0}))
 
 
+def estimator_run(args):
+    """Error indicators (AdaptiveMPETSolver) after one solve_direct step of the
+    --n cube: time per indicator evaluation (cell + interior-facet kernels, the
+    gather and the R4p sum) with CUDA events, against one step's time."""
+    import torch
+    from waterscapes_gb300 import AdaptiveMPETSolver, Constant, Expression
+    problem, dt = workload(args.n, args.networks)
+    problem.f = Expression(lambda x, t: torch.stack([torch.sin(x[:, 0] + t), x[:, 1] * t, x[:, 2]], 1))
+    params = AdaptiveMPETSolver.default_params()
+    params["MPETSolver"].update(dt=dt, T=1e9, theta=1.0, rtol=1e-10, precision="mixed")
+    f_ = Expression(problem.f.fn, t=Constant(0.0))
+    t0 = time.perf_counter()
+    ad = AdaptiveMPETSolver(problem, f_, params)
+    t_setup = time.perf_counter() - t0
+    s = ad.inner_solver
+    gen = s.solve_direct()
+    next(gen)
+    torch.cuda.synchronize()
+    stream = s._stream
+    e0 = torch.cuda.Event(enable_timing=True)
+    e1 = torch.cuda.Event(enable_timing=True)
+    for _ in range(2):
+        ad.indicators()
+    torch.cuda.synchronize()
+    reps = 5
+    e0.record(stream)
+    for _ in range(reps):
+        out = ad.indicators()
+    e1.record(stream)
+    torch.cuda.synchronize()
+    ms = e0.elapsed_time(e1) / reps
+    e0.record(stream)
+    next(gen)
+    e1.record(stream)
+    torch.cuda.synchronize()
+    step_ms = e0.elapsed_time(e1)
+    print(json.dumps({"estimators": "AdaptiveMPETSolver indicators", "workload": "Kuhn cube %d^3, A=%d" % (
+        args.n, args.networks), "cells": problem.mesh.num_cells(), "interior_facets": ad._nfi,
+        "indicators_ms": ms, "step_ms": step_ms, "facet_tables_plus_solver_setup_s": t_setup,
+        "eta_u_sum": float(out[1].sum()), "r4p": out[3]}))
+
+
 def adjoint_check(args):
     """Gradient of the final-pressure misfit w.r.t. per-cell K by the discrete
     adjoint: A=2 on the Kuhn n^3 cube (default 32^3), 20 steps of dt = 0.025,
@@ -533,6 +575,8 @@ def main():
     ap.add_argument("--instances", type=int, default=256)
     ap.add_argument("--n-min", type=int, default=8)
     ap.add_argument("--n-max", type=int, default=32)
+    ap.add_argument("--estimators", action="store_true",
+                    help="time the AdaptiveMPETSolver error indicators on the --n cube instead of the bench")
     ap.add_argument("--formulation", default="mpet", choices=["mpet", "total-pressure"],
                     help="total-pressure: MPETTotalPressureSolver (u, p0, networks) on the same workload")
     args = ap.parse_args()
@@ -542,6 +586,8 @@ def main():
         return profile_case(args)
     if args.adjoint:
         return adjoint_check(args)
+    if args.estimators:
+        return estimator_run(args)
     n, J = args.n, args.networks
     tp = args.formulation == "total-pressure"
     N_full = 3 * (2 * n + 1) ** 3 + (J + int(tp)) * (n + 1) ** 3
