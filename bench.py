@@ -575,6 +575,8 @@ def main():
     ap.add_argument("--instances", type=int, default=256)
     ap.add_argument("--n-min", type=int, default=8)
     ap.add_argument("--n-max", type=int, default=32)
+    ap.add_argument("--cheb-degree", type=int, default=None, help="override amg_cheb_degree")
+    ap.add_argument("--inner-rtol", type=float, default=None, help="override inner_rtol")
     ap.add_argument("--estimators", action="store_true",
                     help="time the AdaptiveMPETSolver error indicators on the --n cube instead of the bench")
     ap.add_argument("--formulation", default="mpet", choices=["mpet", "total-pressure"],
@@ -632,6 +634,10 @@ def main():
 
     problem, dt = workload(n, J, args.workload)
     base = dict(dt=dt, T=1e9, theta=1.0, rtol=1e-10, device=local_rank)
+    if args.cheb_degree is not None:
+        base["amg_cheb_degree"] = args.cheb_degree
+    if args.inner_rtol is not None:
+        base["inner_rtol"] = args.inner_rtol
     t0 = time.perf_counter()
     sol = Solver(problem, dict(base, precision="mixed"))
     t_setup = time.perf_counter() - t0
