@@ -15,6 +15,7 @@
 // the CSR positions given by the per-cell rank tables.  Every value is
 // written by exactly one warp in a fixed order, so the result is
 // deterministic and needs neither atomics nor a cell colouring.
+#include <memory>
 #include <string.h>
 
 #include <algorithm>
@@ -157,7 +158,50 @@ struct AsmArgs {
     float* v32;
     double* dinv;
     int apply_bc;
+    const double* Mst;  // per-cell displacement Gram blocks (k_elem_uu) or null
 };
+
+// Number of node pairs m <= j of a cell and the index of pair (m, j), m <= j.
+template <int D>
+__host__ __device__ constexpr int npairs() { return Simplex<D>::NN * (Simplex<D>::NN + 1) / 2; }
+template <int D>
+__device__ __forceinline__ int pair_index(int m, int j) {
+    return m * Simplex<D>::NN - m * (m - 1) / 2 + (j - m);
+}
+
+// The displacement-block Gram matrices of one cell, computed once per cell:
+// M_mj[a][b] = |T| kappa (s_m[a] s_j[b] + sum_r g_{m,r}[a] g_{j,r}[b]) = int dphi_m/dx_a dphi_j/dx_b
+// for the node pairs m <= j, stored cell-major (M_jm = M_mj^T).  The row-owner
+// assembly reads them instead of recomputing them for every (row node, cell),
+// which keeps the FP64 pipe (the bound of the assembly) to the unique work.
+template <int D>
+__global__ void __launch_bounds__(128) k_elem_uu(int64_t nc, const double* __restrict__ geo, double* Mst) {
+    constexpr int NN = Simplex<D>::NN, NV = Simplex<D>::NV, NP = npairs<D>(), DD = D * D;
+    const int64_t cell = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    if (cell >= nc) return;
+    Geo G;
+    load_geo(geo, cell, G);
+    const double w20 = G.vol * kappa<D>();
+    double* out = Mst + cell * (int64_t)(NP * DD);
+    for (int m = 0; m < NN; ++m) {
+        double gm[4][3], sm[3];
+        p2_grad_table<D>(G, m, gm, sm);
+        for (int j = m; j < NN; ++j) {
+            double gj[4][3], sj[3];
+            p2_grad_table<D>(G, j, gj, sj);
+            double* o = out + pair_index<D>(m, j) * DD;
+#pragma unroll
+            for (int a = 0; a < D; ++a)
+#pragma unroll
+                for (int b = 0; b < D; ++b) {
+                    double acc = sm[a] * sj[b];
+#pragma unroll
+                    for (int r = 0; r < NV; ++r) acc += gm[r][a] * gj[r][b];
+                    o[a * D + b] = w20 * acc;
+                }
+        }
+    }
+}
 
 // Task layout of one (node, cell) pair over the warp's lanes: NN*D
 // displacement-displacement entries (node j, component k), D*NV
@@ -193,7 +237,7 @@ __global__ void __launch_bounds__(256) k_assemble_matrix(AsmArgs A, MatCoef P) {
             Geo G;
             load_geo(A.geo, cell, G);
             double gm[4][3], sm[3];
-            p2_grad_table<D>(G, m, gm, sm);
+            if (!A.Mst) p2_grad_table<D>(G, m, gm, sm);
             const double w20 = G.vol * kappa<D>();
             const uint16_t* rk2 = A.rank2 + cell * (NN * NN) + m * NN;
             const uint16_t* rk1 = A.rank1 + cell * (NN * NV) + m * NV;
@@ -201,18 +245,36 @@ __global__ void __launch_bounds__(256) k_assemble_matrix(AsmArgs A, MatCoef P) {
             for (int t = lane; t < ntask; t += 32) {
                 if (t < T1) {
                     const int j = t / D, k = t % D;
-                    double gj[4][3], sj[3];
-                    p2_grad_table<D>(G, j, gj, sj);
                     double M[3][3];
+                    if (A.Mst) {
+                        constexpr int NP = npairs<D>(), DD = D * D;
+                        const double* src = A.Mst + cell * (int64_t)(NP * DD);
+                        if (m <= j) {
+                            src += pair_index<D>(m, j) * DD;
 #pragma unroll
-                    for (int a = 0; a < D; ++a)
+                            for (int a = 0; a < D; ++a)
 #pragma unroll
-                        for (int b = 0; b < D; ++b) {
-                            double acc = sm[a] * sj[b];
+                                for (int b = 0; b < D; ++b) M[a][b] = src[a * D + b];
+                        } else {
+                            src += pair_index<D>(j, m) * DD;
 #pragma unroll
-                            for (int r = 0; r < NV; ++r) acc += gm[r][a] * gj[r][b];
-                            M[a][b] = w20 * acc;
+                            for (int a = 0; a < D; ++a)
+#pragma unroll
+                                for (int b = 0; b < D; ++b) M[a][b] = src[b * D + a];
                         }
+                    } else {
+                        double gj[4][3], sj[3];
+                        p2_grad_table<D>(G, j, gj, sj);
+#pragma unroll
+                        for (int a = 0; a < D; ++a)
+#pragma unroll
+                            for (int b = 0; b < D; ++b) {
+                                double acc = sm[a] * sj[b];
+#pragma unroll
+                                for (int r = 0; r < NV; ++r) acc += gm[r][a] * gj[r][b];
+                                M[a][b] = w20 * acc;
+                            }
+                    }
                     double tr = 0.0;
 #pragma unroll
                     for (int a = 0; a < D; ++a) tr += M[a][a];
@@ -225,7 +287,14 @@ __global__ void __launch_bounds__(256) k_assemble_matrix(AsmArgs A, MatCoef P) {
                     }
                 } else if (t < T2) {
                     const int tt = t - T1, k = tt / NV, w = tt % NV;
-                    const double C = w20 * (gm[w][k] + sm[k]);
+                    double C;
+                    if (A.Mst) {
+                        double g[3], sg[3];
+                        p2_grad_at<D>(G, m, w, g, sg);
+                        C = w20 * (g[k] + sg[k]);
+                    } else {
+                        C = w20 * (gm[w][k] + sm[k]);
+                    }
                     const int64_t base = rp[k] + D * (int64_t)d2 + rk1[w];
                     for (int a = 0; a < J; ++a) A.v64[base + (int64_t)a * d1] += P.cpl[a] * C;
                 } else if (t < T3) {
@@ -596,9 +665,22 @@ void launch_assemble_matrix(mpet_ctx* c, double dt, bool apply_bc, bool write32)
     int64_t warps_needed = c->nnodes;
     int blocks = grid_for(warps_needed * 32, 256);
     if (blocks > 152 * 64) blocks = 152 * 64;
+    // per-cell Gram blocks when they fit beside everything else (a fifth of HBM stays free)
+    const size_t mst_bytes = (size_t)c->nc * (c->dim == 2 ? npairs<2>() * 4 : npairs<3>() * 9) * sizeof(double);
+    const bool staged = device_fits(c, mst_bytes);
+    std::unique_ptr<TmpBuf> mst;
+    if (staged) {
+        mst.reset(new TmpBuf(mst_bytes));
+        A.Mst = mst->as<double>();
+        if (c->dim == 2) k_elem_uu<2><<<grid_for(c->nc, 128), 128, 0, c->stream>>>(c->nc, c->geo, mst->as<double>());
+        else k_elem_uu<3><<<grid_for(c->nc, 128), 128, 0, c->stream>>>(c->nc, c->geo, mst->as<double>());
+        MPET_CHECK_LAUNCH();
+    }
     if (c->dim == 2) k_assemble_matrix<2><<<blocks, 256, 0, c->stream>>>(A, P);
     else k_assemble_matrix<3><<<blocks, 256, 0, c->stream>>>(A, P);
     MPET_CHECK_LAUNCH();
+    // the temporary blocks are released only after the assembly has read them
+    if (staged) MPET_CUDA(cudaStreamSynchronize(c->stream));
 }
 
 void launch_assemble_prec_blocks(mpet_ctx* c, double dt) {
