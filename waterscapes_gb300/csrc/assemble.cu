@@ -58,6 +58,10 @@ struct MatCoef {
     double cpl[MPET_MAX_NETWORKS], rhs_cu[MPET_MAX_NETWORKS];
     double rank_b[MPET_MAX_NETWORKS], rank_rhs[MPET_MAX_NETWORKS], rank_inv;
     double prec_extra[MPET_MAX_NETWORKS];              // + prec_extra_a (p_a, w_a) in pressure block a
+    // with scalar coefficients (no per-cell c, K, S): the pressure-pressure block of the
+    // system is Cm_ab (p_b, w_a) + [a == b] Kd_a (grad p_a, grad w_a)
+    int coef_const;
+    double Cm[MPET_MAX_NETWORKS * MPET_MAX_NETWORKS], Kd[MPET_MAX_NETWORKS];
     __device__ __forceinline__ double Kof(int a, int64_t cell) const { return Kc ? Kc[a * nc + cell] : K[a]; }
     __device__ __forceinline__ double cof(int a, int64_t cell) const { return cc ? cc[a * nc + cell] : c[a]; }
     __device__ __forceinline__ double Sof(int a, int b, int64_t cell) const {
@@ -211,7 +215,7 @@ __global__ void __launch_bounds__(128) k_elem_uu(int64_t nc, const double* __res
 template <int D>
 __global__ void __launch_bounds__(256) k_assemble_matrix(AsmArgs A, MatCoef P) {
     constexpr int NV = Simplex<D>::NV, NN = Simplex<D>::NN;
-    constexpr int T1 = NN * D, T2 = T1 + D * NV, T3 = T2 + NN * D, T4 = T3 + NV;
+    constexpr int X0 = (NN * D + 31) / 32 * 32;  // first coupling task
     const int lane = threadIdx.x & 31;
     const int64_t warp = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) >> 5;
     const int64_t nwarps = ((int64_t)gridDim.x * blockDim.x) >> 5;
@@ -236,14 +240,18 @@ __global__ void __launch_bounds__(256) k_assemble_matrix(AsmArgs A, MatCoef P) {
             const int m = packed & 15;
             Geo G;
             load_geo(A.geo, cell, G);
-            double gm[4][3], sm[3];
-            if (!A.Mst) p2_grad_table<D>(G, m, gm, sm);
             const double w20 = G.vol * kappa<D>();
             const uint16_t* rk2 = A.rank2 + cell * (NN * NN) + m * NN;
             const uint16_t* rk1 = A.rank1 + cell * (NN * NV) + m * NV;
-            const int ntask = isv ? T4 : T2;
+            // Lane tasks in class-aligned rounds of 32 (a round runs every branch any of its
+            // lanes takes): round 1 the NN*D displacement (node j, row k) tasks; then the
+            // u-p coupling tasks (u row k with vertex w, and for vertex rows the p rows with
+            // node j, component l); then for vertex rows the (network a, vertex w) pressure tasks.
+            const int nx = D * NV + (isv ? NN * D : 0);
+            const int ntask = X0 + nx + (isv ? J * NV : 0);
             for (int t = lane; t < ntask; t += 32) {
-                if (t < T1) {
+                if (t < X0) {
+                    if (t >= NN * D) continue;
                     const int j = t / D, k = t % D;
                     double M[3][3];
                     if (A.Mst) {
@@ -263,7 +271,8 @@ __global__ void __launch_bounds__(256) k_assemble_matrix(AsmArgs A, MatCoef P) {
                                 for (int b = 0; b < D; ++b) M[a][b] = src[b * D + a];
                         }
                     } else {
-                        double gj[4][3], sj[3];
+                        double gm[4][3], sm[3], gj[4][3], sj[3];
+                        p2_grad_table<D>(G, m, gm, sm);
                         p2_grad_table<D>(G, j, gj, sj);
 #pragma unroll
                         for (int a = 0; a < D; ++a)
@@ -285,30 +294,35 @@ __global__ void __launch_bounds__(256) k_assemble_matrix(AsmArgs A, MatCoef P) {
                         if (l == k) v += P.mu * tr;
                         A.v64[base + l] += v;
                     }
-                } else if (t < T2) {
-                    const int tt = t - T1, k = tt / NV, w = tt % NV;
-                    double C;
-                    if (A.Mst) {
-                        double g[3], sg[3];
-                        p2_grad_at<D>(G, m, w, g, sg);
-                        C = w20 * (g[k] + sg[k]);
-                    } else {
-                        C = w20 * (gm[w][k] + sm[k]);
+                } else if (t < X0 + nx) {
+                    // coupling value w20 (grad phi_node at vertex + s_node)[comp]: u row k with
+                    // vertex w (node m at vertex w), or p rows with node j (node j at vertex m)
+                    const int x = t - X0;
+                    const bool urow = x < D * NV;
+                    const int y = x - D * NV;
+                    const int gnode = urow ? m : y / D;
+                    const int gvert = urow ? x % NV : m;
+                    const int comp = urow ? x / NV : y % D;
+                    double g[3], sg[3];
+                    p2_grad_at<D>(G, gnode, gvert, g, sg);
+                    const double C = w20 * (g[comp] + sg[comp]);
+                    for (int a = 0; a < J; ++a) {
+                        const int64_t pos = urow ? rp[comp] + D * (int64_t)d2 + (int64_t)a * d1 + rk1[gvert]
+                                                 : rp[D + a] + D * (int64_t)rk2[gnode] + comp;
+                        A.v64[pos] += P.cpl[a] * C;
                     }
-                    const int64_t base = rp[k] + D * (int64_t)d2 + rk1[w];
-                    for (int a = 0; a < J; ++a) A.v64[base + (int64_t)a * d1] += P.cpl[a] * C;
-                } else if (t < T3) {
-                    const int tt = t - T2, j = tt / D, l = tt % D;
-                    double g[3], s[3];
-                    p2_grad_at<D>(G, j, m, g, s);
-                    const double C = w20 * (g[l] + s[l]);
-                    for (int a = 0; a < J; ++a) A.v64[rp[D + a] + D * (int64_t)rk2[j] + l] += P.cpl[a] * C;
                 } else {
-                    const int w = t - T3;
+                    const int q = t - X0 - nx, a = q / NV, w = q % NV;
                     const double M1 = w20 * (m == w ? 2.0 : 1.0);
                     const double L1 = G.vol * (G.b[m][0] * G.b[w][0] + G.b[m][1] * G.b[w][1] + G.b[m][2] * G.b[w][2]);
-                    for (int a = 0; a < J; ++a) {
-                        const int64_t base = rp[D + a] + D * (int64_t)d2 + rk1[w];
+                    const int64_t base = rp[D + a] + D * (int64_t)d2 + rk1[w];
+                    if (P.coef_const) {
+                        for (int b = 0; b < J; ++b) {
+                            double v = P.Cm[a * MPET_MAX_NETWORKS + b] * M1;
+                            if (a == b) v += P.Kd[a] * L1;
+                            A.v64[base + (int64_t)b * d1] += v;
+                        }
+                    } else {
                         for (int b = 0; b < J; ++b) {
                             double v = -(P.dt_theta * ((a == b ? P.Ssumof(a, cell) : 0.0) - P.Sof(a, b, cell)) +
                                          P.rank_inv * P.rank_b[a] * P.rank_b[b]) * M1;
@@ -631,6 +645,15 @@ static MatCoef make_coef(const mpet_ctx* c, double dt) {
         P.prec_extra[a] = !tp ? 0.0
                         : a == 0 ? (c->prm.prec_p0_weight > 0.0 ? c->prm.prec_p0_weight : 1.0)
                                  : c->prm.alpha[a] * c->prm.alpha[a] * P.rank_inv;
+    }
+    P.coef_const = (!P.Kc && !P.cc && !P.Sc) ? 1 : 0;
+    for (int a = 0; a < c->J; ++a) {
+        for (int b = 0; b < c->J; ++b)
+            P.Cm[a * MPET_MAX_NETWORKS + b] =
+                -(P.dt_theta * ((a == b ? P.Ssum[a] : 0.0) - P.S[a * MPET_MAX_NETWORKS + b]) +
+                  P.rank_inv * P.rank_b[a] * P.rank_b[b]) -
+                (a == b ? P.c[a] : 0.0);
+        P.Kd[a] = -P.dt_theta * P.K[a];
     }
     return P;
 }
