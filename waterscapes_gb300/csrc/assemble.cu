@@ -162,38 +162,55 @@ struct AsmArgs {
     float* v32;
     double* dinv;
     int apply_bc;
-    const double* Mst;  // per-cell displacement Gram blocks (k_elem_uu) or null
+    const double* Mst;  // per-cell displacement blocks (k_elem_uu) or null
 };
 
 // Number of node pairs m <= j of a cell and the index of pair (m, j), m <= j.
 template <int D>
 __host__ __device__ constexpr int npairs() { return Simplex<D>::NN * (Simplex<D>::NN + 1) / 2; }
+// doubles per cell of the staged element data: the displacement blocks, then the
+// coupling values C[g][r][k] = |T| kappa (g_{g,r}[k] + s_g[k])
+template <int D>
+__host__ __device__ constexpr int elem_record() {
+    return npairs<D>() * D * D + Simplex<D>::NN * Simplex<D>::NV * D;
+}
 template <int D>
 __device__ __forceinline__ int pair_index(int m, int j) {
     return m * Simplex<D>::NN - m * (m - 1) / 2 + (j - m);
 }
 
-// The displacement-block Gram matrices of one cell, computed once per cell:
-// M_mj[a][b] = |T| kappa (s_m[a] s_j[b] + sum_r g_{m,r}[a] g_{j,r}[b]) = int dphi_m/dx_a dphi_j/dx_b
-// for the node pairs m <= j, stored cell-major (M_jm = M_mj^T).  The row-owner
-// assembly reads them instead of recomputing them for every (row node, cell),
-// which keeps the FP64 pipe (the bound of the assembly) to the unique work.
+// The displacement blocks of one cell's element matrix, computed once per cell:
+// with the Gram matrix M_mj[a][b] = |T| kappa (s_m[a] s_j[b] + sum_r g_{m,r}[a] g_{j,r}[b])
+// = int dphi_m/dx_a dphi_j/dx_b, the block of rows (m, k) and columns (j, l) is
+// B_mj[k][l] = mu M_mj[l][k] + lmbda M_mj[k][l] + [k == l] mu tr M_mj, stored for the
+// node pairs m <= j, cell-major (B_jm = B_mj^T), followed by the u-p coupling values
+// C[g][r][k] (node g, vertex r, component k).  The row-owner assembly reads them
+// instead of recomputing them for every (row node, cell), which keeps the FP64 pipe
+// (the bound of the assembly) to the unique work.
 template <int D>
-__global__ void __launch_bounds__(128) k_elem_uu(int64_t nc, const double* __restrict__ geo, double* Mst) {
+__global__ void __launch_bounds__(128) k_elem_uu(int64_t nc, const double* __restrict__ geo, double mu,
+                                                 double lmbda, double* Mst) {
     constexpr int NN = Simplex<D>::NN, NV = Simplex<D>::NV, NP = npairs<D>(), DD = D * D;
     const int64_t cell = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
     if (cell >= nc) return;
     Geo G;
     load_geo(geo, cell, G);
     const double w20 = G.vol * kappa<D>();
-    double* out = Mst + cell * (int64_t)(NP * DD);
+    double* out = Mst + cell * (int64_t)elem_record<D>();
     for (int m = 0; m < NN; ++m) {
         double gm[4][3], sm[3];
         p2_grad_table<D>(G, m, gm, sm);
+        double* cpl = out + NP * DD + m * NV * D;
+#pragma unroll
+        for (int r = 0; r < NV; ++r)
+#pragma unroll
+            for (int k = 0; k < D; ++k) cpl[r * D + k] = w20 * (gm[r][k] + sm[k]);
         for (int j = m; j < NN; ++j) {
             double gj[4][3], sj[3];
             p2_grad_table<D>(G, j, gj, sj);
             double* o = out + pair_index<D>(m, j) * DD;
+            double M[3][3];
+            double tr = 0.0;
 #pragma unroll
             for (int a = 0; a < D; ++a)
 #pragma unroll
@@ -201,7 +218,17 @@ __global__ void __launch_bounds__(128) k_elem_uu(int64_t nc, const double* __res
                     double acc = sm[a] * sj[b];
 #pragma unroll
                     for (int r = 0; r < NV; ++r) acc += gm[r][a] * gj[r][b];
-                    o[a * D + b] = w20 * acc;
+                    M[a][b] = w20 * acc;
+                }
+#pragma unroll
+            for (int a = 0; a < D; ++a) tr += M[a][a];
+#pragma unroll
+            for (int k = 0; k < D; ++k)
+#pragma unroll
+                for (int l = 0; l < D; ++l) {
+                    double v = mu * M[l][k] + lmbda * M[k][l];
+                    if (l == k) v += mu * tr;
+                    o[k * D + l] = v;
                 }
         }
     }
@@ -253,24 +280,19 @@ __global__ void __launch_bounds__(256) k_assemble_matrix(AsmArgs A, MatCoef P) {
                 if (t < X0) {
                     if (t >= NN * D) continue;
                     const int j = t / D, k = t % D;
-                    double M[3][3];
+                    const int64_t base = rp[k] + D * (int64_t)rk2[j];
                     if (A.Mst) {
-                        constexpr int NP = npairs<D>(), DD = D * D;
-                        const double* src = A.Mst + cell * (int64_t)(NP * DD);
-                        if (m <= j) {
-                            src += pair_index<D>(m, j) * DD;
+                        // row k of B_mj (stored, or the transpose of the stored B_jm)
+                        constexpr int DD = D * D;
+                        const double* src = A.Mst + cell * (int64_t)elem_record<D>();
+                        const bool up = m <= j;
+                        src += pair_index<D>(up ? m : j, up ? j : m) * DD;
 #pragma unroll
-                            for (int a = 0; a < D; ++a)
-#pragma unroll
-                                for (int b = 0; b < D; ++b) M[a][b] = src[a * D + b];
-                        } else {
-                            src += pair_index<D>(j, m) * DD;
-#pragma unroll
-                            for (int a = 0; a < D; ++a)
-#pragma unroll
-                                for (int b = 0; b < D; ++b) M[a][b] = src[b * D + a];
-                        }
-                    } else {
+                        for (int l = 0; l < D; ++l) A.v64[base + l] += src[up ? k * D + l : l * D + k];
+                        continue;
+                    }
+                    double M[3][3];
+                    {
                         double gm[4][3], sm[3], gj[4][3], sj[3];
                         p2_grad_table<D>(G, m, gm, sm);
                         p2_grad_table<D>(G, j, gj, sj);
@@ -287,7 +309,6 @@ __global__ void __launch_bounds__(256) k_assemble_matrix(AsmArgs A, MatCoef P) {
                     double tr = 0.0;
 #pragma unroll
                     for (int a = 0; a < D; ++a) tr += M[a][a];
-                    const int64_t base = rp[k] + D * (int64_t)rk2[j];
 #pragma unroll
                     for (int l = 0; l < D; ++l) {
                         double v = P.mu * M[l][k] + P.lmbda * M[k][l];
@@ -303,9 +324,14 @@ __global__ void __launch_bounds__(256) k_assemble_matrix(AsmArgs A, MatCoef P) {
                     const int gnode = urow ? m : y / D;
                     const int gvert = urow ? x % NV : m;
                     const int comp = urow ? x / NV : y % D;
-                    double g[3], sg[3];
-                    p2_grad_at<D>(G, gnode, gvert, g, sg);
-                    const double C = w20 * (g[comp] + sg[comp]);
+                    double C;
+                    if (A.Mst) {
+                        C = A.Mst[cell * (int64_t)elem_record<D>() + npairs<D>() * D * D + (gnode * NV + gvert) * D + comp];
+                    } else {
+                        double g[3], sg[3];
+                        p2_grad_at<D>(G, gnode, gvert, g, sg);
+                        C = w20 * (g[comp] + sg[comp]);
+                    }
                     for (int a = 0; a < J; ++a) {
                         const int64_t pos = urow ? rp[comp] + D * (int64_t)d2 + (int64_t)a * d1 + rk1[gvert]
                                                  : rp[D + a] + D * (int64_t)rk2[gnode] + comp;
@@ -688,15 +714,17 @@ void launch_assemble_matrix(mpet_ctx* c, double dt, bool apply_bc, bool write32)
     int64_t warps_needed = c->nnodes;
     int blocks = grid_for(warps_needed * 32, 256);
     if (blocks > 152 * 64) blocks = 152 * 64;
-    // per-cell Gram blocks when they fit beside everything else (a fifth of HBM stays free)
-    const size_t mst_bytes = (size_t)c->nc * (c->dim == 2 ? npairs<2>() * 4 : npairs<3>() * 9) * sizeof(double);
+    // staged element data when it fits beside everything else (a fifth of HBM stays free)
+    const size_t mst_bytes = (size_t)c->nc * (c->dim == 2 ? elem_record<2>() : elem_record<3>()) * sizeof(double);
     const bool staged = device_fits(c, mst_bytes);
     std::unique_ptr<TmpBuf> mst;
     if (staged) {
         mst.reset(new TmpBuf(mst_bytes));
         A.Mst = mst->as<double>();
-        if (c->dim == 2) k_elem_uu<2><<<grid_for(c->nc, 128), 128, 0, c->stream>>>(c->nc, c->geo, mst->as<double>());
-        else k_elem_uu<3><<<grid_for(c->nc, 128), 128, 0, c->stream>>>(c->nc, c->geo, mst->as<double>());
+        if (c->dim == 2)
+            k_elem_uu<2><<<grid_for(c->nc, 128), 128, 0, c->stream>>>(c->nc, c->geo, P.mu, P.lmbda, mst->as<double>());
+        else
+            k_elem_uu<3><<<grid_for(c->nc, 128), 128, 0, c->stream>>>(c->nc, c->geo, P.mu, P.lmbda, mst->as<double>());
         MPET_CHECK_LAUNCH();
     }
     if (c->dim == 2) k_assemble_matrix<2><<<blocks, 256, 0, c->stream>>>(A, P);
