@@ -15,7 +15,6 @@
 // the CSR positions given by the per-cell rank tables.  Every value is
 // written by exactly one warp in a fixed order, so the result is
 // deterministic and needs neither atomics nor a cell colouring.
-#include <memory>
 #include <string.h>
 
 #include <algorithm>
@@ -716,22 +715,22 @@ void launch_assemble_matrix(mpet_ctx* c, double dt, bool apply_bc, bool write32)
     if (blocks > 152 * 64) blocks = 152 * 64;
     // staged element data when it fits beside everything else (a fifth of HBM stays free)
     const size_t mst_bytes = (size_t)c->nc * (c->dim == 2 ? elem_record<2>() : elem_record<3>()) * sizeof(double);
-    const bool staged = device_fits(c, mst_bytes);
-    std::unique_ptr<TmpBuf> mst;
-    if (staged) {
-        mst.reset(new TmpBuf(mst_bytes));
-        A.Mst = mst->as<double>();
+    // (kept for later assemblies; decided once per context)
+    if (!c->elem_tried) {
+        c->elem_tried = true;
+        if (device_fits(c, mst_bytes)) c->elem_buf = c->pool.alloc<double>((int64_t)(mst_bytes / sizeof(double)));
+    }
+    if (c->elem_buf) {
+        A.Mst = c->elem_buf;
         if (c->dim == 2)
-            k_elem_uu<2><<<grid_for(c->nc, 128), 128, 0, c->stream>>>(c->nc, c->geo, P.mu, P.lmbda, mst->as<double>());
+            k_elem_uu<2><<<grid_for(c->nc, 128), 128, 0, c->stream>>>(c->nc, c->geo, P.mu, P.lmbda, c->elem_buf);
         else
-            k_elem_uu<3><<<grid_for(c->nc, 128), 128, 0, c->stream>>>(c->nc, c->geo, P.mu, P.lmbda, mst->as<double>());
+            k_elem_uu<3><<<grid_for(c->nc, 128), 128, 0, c->stream>>>(c->nc, c->geo, P.mu, P.lmbda, c->elem_buf);
         MPET_CHECK_LAUNCH();
     }
     if (c->dim == 2) k_assemble_matrix<2><<<blocks, 256, 0, c->stream>>>(A, P);
     else k_assemble_matrix<3><<<blocks, 256, 0, c->stream>>>(A, P);
     MPET_CHECK_LAUNCH();
-    // the temporary blocks are released only after the assembly has read them
-    if (staged) MPET_CUDA(cudaStreamSynchronize(c->stream));
 }
 
 void launch_assemble_prec_blocks(mpet_ctx* c, double dt) {

@@ -300,6 +300,8 @@ struct mpet_ctx {
     unsigned char* l2_flush = nullptr;  // 256 MiB written between autotuner launches
     double* adj_b = nullptr;      // adjoint right-hand side (Dirichlet rows zeroed)
     double* adj_loss = nullptr;   // misfit value (1 double)
+    double* elem_buf = nullptr;   // staged per-cell element data of the assembly, or null
+    bool elem_tried = false;
     // error-indicator scratch: per-facet terms, per-cell R4p density, its sum, bad-index flag
     double* est_fval = nullptr;
     int64_t est_fval_cap = 0;
