@@ -238,6 +238,14 @@ def replica_rate(ms_local, steps):
     return world * steps / (ms / 1e3), ms
 
 
+def prec_form(solver):
+    """Displacement block the preconditioner runs (elasticity AMG or vector Laplacian)."""
+    import ctypes
+    v = ctypes.c_int32()
+    solver.ctx.call("mpet_get_prec_info", ctypes.byref(v))
+    return "elasticity AMG (rigid-body modes)" if v.value else "vector Laplacian AMG"
+
+
 def spmv_tuning(solver):
     import ctypes
     ms = np.zeros(7)
@@ -576,6 +584,8 @@ def main():
     ap.add_argument("--n-min", type=int, default=8)
     ap.add_argument("--n-max", type=int, default=32)
     ap.add_argument("--cheb-degree", type=int, default=None, help="override amg_cheb_degree")
+    ap.add_argument("--prec-u-form", default=None, choices=["elasticity", "laplacian"],
+                    help="override the displacement block of the preconditioner")
     ap.add_argument("--inner-rtol", type=float, default=None, help="override inner_rtol")
     ap.add_argument("--estimators", action="store_true",
                     help="time the AdaptiveMPETSolver error indicators on the --n cube instead of the bench")
@@ -638,6 +648,8 @@ def main():
         base["amg_cheb_degree"] = args.cheb_degree
     if args.inner_rtol is not None:
         base["inner_rtol"] = args.inner_rtol
+    if args.prec_u_form is not None:
+        base["prec_u_form"] = args.prec_u_form
     t0 = time.perf_counter()
     sol = Solver(problem, dict(base, precision="mixed"))
     t_setup = time.perf_counter() - t0
@@ -744,6 +756,7 @@ def main():
         "setup_s": {"mesh_dofmap_pattern": t_setup, "assemble_plus_amg": t_asm_amg},
         "spmv": spmv,
         "spmv_tuning": spmv_tuning(sol),
+        "preconditioner_u_block": prec_form(sol),
         "iteration_breakdown_ms": dict(split, spmv_fp32=(spmv.get("fp32") or spmv["fp64"])["ms"],
                                        preconditioner=precond_ms),
         "fp64_iteration_breakdown_ms": res.get("fp64", {}).get("iteration_breakdown_ms"),

@@ -93,7 +93,12 @@ typedef struct mpet_params {
                                           when the displacement has no Dirichlet condition, e.g.
                                           with rigid-motion modes); 0 for none */
     int32_t formulation;               /* MPET_FORM_*: the block system assembled */
-    int32_t pad1;
+    int32_t prec_u_form;               /* displacement block of the preconditioner: 0 = the
+                                          vector Laplacian w (grad u, grad v) (the reference's
+                                          form family, mpetsolver.py:269); 1 = the displacement
+                                          block of the system itself, smoothed-aggregation AMG
+                                          with rigid-body modes (3D with node blocks, Dirichlet
+                                          displacement, no batch; otherwise form 0 is used) */
     double prec_p0_weight;             /* total-pressure form: w0 in the p0 block w0 (p0, w0) of
                                           the preconditioner (the reference form uses 1,
                                           mpettotalpressuresolver.py:281); <= 0 means 1 */
@@ -236,6 +241,10 @@ int mpet_set_facet_data(mpet_ctx* ctx, int32_t kind, const double* values);
  * bc.apply(b) (mpetsolver.py:356-376).  up_prev and b are device arrays
  * of length N. */
 int mpet_rhs(mpet_ctx* ctx, double dt, const double* up_prev, double* b);
+
+/* Which displacement block the preconditioner runs: 1 = elasticity AMG
+ * (prec_u_form 1 and applicable), 0 = the vector Laplacian. */
+int mpet_get_prec_info(mpet_ctx* ctx, int32_t* u_elasticity);
 
 /* Block-diagonal preconditioner (mpetsolver.py:264-271): one smoothed-
  * aggregation AMG hierarchy per diagonal block, built for this dt. */

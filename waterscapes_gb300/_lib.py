@@ -51,7 +51,7 @@ class MpetParams(ctypes.Structure):
         ("prec_u_weight", ctypes.c_double),
         ("prec_u_shift", ctypes.c_double),
         ("formulation", ctypes.c_int32),
-        ("pad1", ctypes.c_int32),
+        ("prec_u_form", ctypes.c_int32),
         ("prec_p0_weight", ctypes.c_double),
     ]
 
@@ -114,6 +114,7 @@ SIGNATURES = {
     "mpet_setup_preconditioner": [_P, _D],
     "mpet_get_amg_info": [_P, _I32, ctypes.POINTER(_I32), _P, _P],
     "mpet_solve": [_P, _P, _P, ctypes.POINTER(MpetStats)],
+    "mpet_get_prec_info": [_P, ctypes.POINTER(_I32)],
     "mpet_step": [_P, _D, _P, _P, ctypes.POINTER(MpetStats)],
     "mpet_apply_preconditioner": [_P, _I32, _P, _P],
     "mpet_residual": [_P, _P, _P, _P, _P],

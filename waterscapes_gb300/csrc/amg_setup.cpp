@@ -151,6 +151,10 @@ static double tridiag_max_eig(const std::vector<double>& a, const std::vector<do
     return hi;
 }
 
+double tridiag_max_eig_host(const std::vector<double>& a, const std::vector<double>& b) {
+    return tridiag_max_eig(a, b);
+}
+
 // Spectral radius of D^-1 A: 30 Lanczos steps on D^-1/2 A D^-1/2 (same
 // spectrum, symmetric) from x_i = 0.5 + ((7919 i) mod 1009)/1009, then the
 // largest Ritz value.
@@ -455,6 +459,323 @@ void amg_setup_host(const HostCsr& A0, const HostCsr* P0, double theta, int coar
     out.ncoarse = nc;
     if (!cholesky_inverse(dense, nc, out.cinv))
         fail(MPET_ERR_INVALID, "AMG coarsest operator is not positive definite");
+}
+
+// ---- smoothed aggregation for the displacement block (vector elasticity) ----------
+//
+// The same recipe with a near-nullspace of rigid-body modes (Vanek, Mandel and
+// Brezina, Computing 56 (1996) 179-196): unknowns come in nodes (3 displacement
+// components at the first level, the coarse unknowns of an aggregate below);
+// strength and aggregation act on the node graph with Frobenius norms of the
+// node blocks; the tentative prolongator of an aggregate is the orthonormal
+// factor Q of its near-nullspace rows B_agg = Q R (Gram-Schmidt with rank
+// detection), and R gives the coarse near-nullspace; P = (I - 4/3 rho^-1 D^-1 A) T.
+
+static bool check_csr(const HostCsr& A) {
+    if ((int64_t)A.rp.size() != A.n + 1 || A.rp[0] != 0) return false;
+    for (int64_t i = 0; i < A.n; ++i)
+        if (A.rp[i + 1] < A.rp[i]) return false;
+    if (A.rp[A.n] != (int64_t)A.ci.size() || A.ci.size() != A.v.size()) return false;
+    for (int32_t j : A.ci)
+        if (j < 0 || j >= A.m) return false;
+    return true;
+}
+
+// C = T - w D^-1 (A T), rows of T and A T sorted
+static void smooth_prolongator(const HostCsr& A, const HostCsr& T, const std::vector<double>& dinv, double w,
+                               HostCsr& P) {
+    HostCsr AT;
+    spgemm(A, T, AT);
+    const int64_t n = T.n;
+    P = HostCsr();
+    P.n = n;
+    P.m = T.m;
+    P.rp.assign(n + 1, 0);
+    std::vector<std::vector<std::pair<int32_t, double>>> rows(n);
+#pragma omp parallel for schedule(dynamic, 1024)
+    for (int64_t i = 0; i < n; ++i) {
+        auto& r = rows[i];
+        int64_t a = T.rp[i], ae = T.rp[i + 1], b = AT.rp[i], be = AT.rp[i + 1];
+        const double f = -w * dinv[i];
+        while (a < ae || b < be) {
+            if (b >= be || (a < ae && T.ci[a] < AT.ci[b])) {
+                r.emplace_back(T.ci[a], T.v[a]);
+                ++a;
+            } else if (a >= ae || AT.ci[b] < T.ci[a]) {
+                r.emplace_back(AT.ci[b], f * AT.v[b]);
+                ++b;
+            } else {
+                r.emplace_back(T.ci[a], T.v[a] + f * AT.v[b]);
+                ++a;
+                ++b;
+            }
+        }
+    }
+    for (int64_t i = 0; i < n; ++i) P.rp[i + 1] = P.rp[i] + (int64_t)rows[i].size();
+    P.ci.resize(P.rp[n]);
+    P.v.resize(P.rp[n]);
+    for (int64_t i = 0; i < n; ++i) {
+        int64_t p = P.rp[i];
+        for (auto& e : rows[i]) {
+            P.ci[p] = e.first;
+            P.v[p] = e.second;
+            ++p;
+        }
+    }
+}
+
+// Node strength graph: nodes own the unknowns node_ptr[k]..node_ptr[k+1].
+static void node_strength(const HostCsr& A, const std::vector<int64_t>& node_ptr, double theta, HostCsr& S) {
+    const int64_t nn = (int64_t)node_ptr.size() - 1;
+    std::vector<int32_t> node_of(A.n);
+    for (int64_t k = 0; k < nn; ++k)
+        for (int64_t i = node_ptr[k]; i < node_ptr[k + 1]; ++i) node_of[i] = (int32_t)k;
+    std::vector<std::vector<std::pair<int32_t, double>>> nb(nn);
+    std::vector<double> dnorm(nn, 0.0);
+#pragma omp parallel
+    {
+        std::vector<double> acc(nn, 0.0);
+        std::vector<int32_t> cols;
+#pragma omp for schedule(dynamic, 256)
+        for (int64_t k = 0; k < nn; ++k) {
+            cols.clear();
+            for (int64_t i = node_ptr[k]; i < node_ptr[k + 1]; ++i)
+                for (int64_t e = A.rp[i]; e < A.rp[i + 1]; ++e) {
+                    const int32_t q = node_of[A.ci[e]];
+                    if (acc[q] == 0.0) cols.push_back(q);
+                    acc[q] += A.v[e] * A.v[e];
+                }
+            std::sort(cols.begin(), cols.end());
+            for (int32_t q : cols) {
+                if (q == k) dnorm[k] = sqrt(acc[q]);
+                else nb[k].emplace_back(q, sqrt(acc[q]));
+                acc[q] = 0.0;
+            }
+        }
+    }
+    S = HostCsr();
+    S.n = S.m = nn;
+    S.rp.assign(nn + 1, 0);
+    for (int64_t k = 0; k < nn; ++k) {
+        int64_t cnt = 0;
+        for (auto& e : nb[k])
+            if (e.second > 0.0 && e.second >= theta * sqrt(dnorm[k] * dnorm[e.first])) ++cnt;
+        S.rp[k + 1] = S.rp[k] + cnt;
+    }
+    S.ci.resize(S.rp[nn]);
+    S.v.assign(S.rp[nn], 1.0);
+    for (int64_t k = 0; k < nn; ++k) {
+        int64_t p = S.rp[k];
+        for (auto& e : nb[k])
+            if (e.second > 0.0 && e.second >= theta * sqrt(dnorm[k] * dnorm[e.first])) S.ci[p++] = e.first;
+    }
+}
+
+void amg_setup_block_host(const HostCsr& A1, const std::vector<double>& B1, int nb_cols, int bs, double theta,
+                          int coarse_size, int max_levels, HostAmg& out) {
+    out.lev.clear();
+    if (!check_csr(A1) || A1.n % bs != 0 || (int64_t)B1.size() != A1.n * nb_cols)
+        fail(MPET_ERR_INVALID, "block AMG input is inconsistent");
+    HostCsr A = A1;
+    std::vector<double> B = B1;  // A.n x nb_cols, row-major
+    std::vector<int64_t> node_ptr(A.n / bs + 1);
+    for (size_t k = 0; k < node_ptr.size(); ++k) node_ptr[k] = (int64_t)k * bs;
+    if (coarse_size < 1) coarse_size = 500;
+    if (max_levels < 1) max_levels = 12;
+#ifdef _OPENMP
+    omp_set_num_threads(host_threads());
+#endif
+    int sa_level = 0;
+    while (true) {
+        HostAmgLevel L;
+        const int64_t n = A.n;
+        L.dinv.resize(n);
+        for (int64_t i = 0; i < n; ++i) {
+            const double d = diag_of(A, i);
+            L.dinv[i] = d != 0.0 ? 1.0 / d : 0.0;
+        }
+        L.rho = lanczos_rho(A, L.dinv, 30);
+        L.A = A;
+        out.lev.push_back(L);
+        HostAmgLevel& cur = out.lev.back();
+        if (n <= coarse_size || (int)out.lev.size() >= max_levels) break;
+        const double th = theta * pow(0.5, (double)sa_level);
+        HostCsr S;
+        node_strength(A, node_ptr, th, S);
+        std::vector<int64_t> agg;
+        int64_t nagg = aggregate(S, agg);
+        if (nagg == 0 && th > 0.0) {
+            node_strength(A, node_ptr, 0.0, S);
+            nagg = aggregate(S, agg);
+        }
+        const int64_t nn = (int64_t)node_ptr.size() - 1;
+        if (nagg == 0 || nagg >= nn) break;
+        // tentative prolongator: per aggregate, Gram-Schmidt on its near-nullspace rows
+        std::vector<std::vector<int64_t>> members(nagg);
+        for (int64_t k = 0; k < nn; ++k)
+            if (agg[k] >= 0) members[agg[k]].push_back(k);
+        std::vector<int> kcols(nagg, 0);
+        std::vector<std::vector<double>> Qs(nagg), Rs(nagg);
+#pragma omp parallel for schedule(dynamic, 64)
+        for (int64_t g = 0; g < nagg; ++g) {
+            std::vector<int64_t> dofs;
+            for (int64_t k : members[g])
+                for (int64_t i = node_ptr[k]; i < node_ptr[k + 1]; ++i) dofs.push_back(i);
+            const int64_t m = (int64_t)dofs.size();
+            std::vector<double> Q(m * nb_cols), R(nb_cols * nb_cols, 0.0);
+            for (int64_t r = 0; r < m; ++r)
+                for (int q = 0; q < nb_cols; ++q) Q[r * nb_cols + q] = B[dofs[r] * nb_cols + q];
+            double scale = 0.0;
+            for (double v : Q) scale = fmax(scale, fabs(v));
+            int kept = 0;
+            std::vector<double> cols(m * nb_cols);  // kept orthonormal columns, column-major
+            for (int q = 0; q < nb_cols; ++q) {
+                std::vector<double> v(m);
+                for (int64_t r = 0; r < m; ++r) v[r] = Q[r * nb_cols + q];
+                double n0 = 0.0;
+                for (double t : v) n0 += t * t;
+                n0 = sqrt(n0);
+                for (int pass = 0; pass < 2; ++pass)
+                    for (int c2 = 0; c2 < kept; ++c2) {
+                        double d = 0.0;
+                        for (int64_t r = 0; r < m; ++r) d += cols[c2 * m + r] * v[r];
+                        R[c2 * nb_cols + q] += d;
+                        for (int64_t r = 0; r < m; ++r) v[r] -= d * cols[c2 * m + r];
+                    }
+                double nv2 = 0.0;
+                for (double t : v) nv2 += t * t;
+                nv2 = sqrt(nv2);
+                if (nv2 <= 1e-10 * fmax(n0, scale * sqrt((double)m)) || kept == m) continue;
+                for (int64_t r = 0; r < m; ++r) cols[kept * m + r] = v[r] / nv2;
+                R[kept * nb_cols + q] = nv2;
+                ++kept;
+            }
+            kcols[g] = kept;
+            Qs[g].assign(cols.begin(), cols.begin() + (size_t)kept * m);
+            Rs[g].assign(R.begin(), R.begin() + (size_t)kept * nb_cols);
+        }
+        std::vector<int64_t> cptr(nagg + 1, 0);
+        for (int64_t g = 0; g < nagg; ++g) cptr[g + 1] = cptr[g] + kcols[g];
+        const int64_t nc = cptr[nagg];
+        HostCsr T;
+        T.n = n;
+        T.m = nc;
+        T.rp.assign(n + 1, 0);
+        std::vector<int64_t> dof_agg(n, -1), dof_row(n, -1);
+        for (int64_t g = 0; g < nagg; ++g) {
+            int64_t r = 0;
+            for (int64_t k : members[g])
+                for (int64_t i = node_ptr[k]; i < node_ptr[k + 1]; ++i) {
+                    dof_agg[i] = g;
+                    dof_row[i] = r++;
+                }
+        }
+        for (int64_t i = 0; i < n; ++i) T.rp[i + 1] = T.rp[i] + (dof_agg[i] >= 0 ? kcols[dof_agg[i]] : 0);
+        T.ci.resize(T.rp[n]);
+        T.v.resize(T.rp[n]);
+        for (int64_t i = 0; i < n; ++i) {
+            const int64_t g = dof_agg[i];
+            if (g < 0) continue;
+            const int64_t m = (int64_t)Qs[g].size() / (kcols[g] > 0 ? kcols[g] : 1);
+            int64_t p = T.rp[i];
+            for (int q = 0; q < kcols[g]; ++q) {
+                T.ci[p] = (int32_t)(cptr[g] + q);
+                T.v[p] = Qs[g][q * m + dof_row[i]];
+                ++p;
+            }
+        }
+        std::vector<double> Bc(nc * nb_cols, 0.0);
+        for (int64_t g = 0; g < nagg; ++g)
+            for (int q = 0; q < kcols[g]; ++q)
+                for (int c2 = 0; c2 < nb_cols; ++c2) Bc[(cptr[g] + q) * nb_cols + c2] = Rs[g][q * nb_cols + c2];
+        HostCsr P;
+        smooth_prolongator(A, T, cur.dinv, 4.0 / 3.0 / cur.rho, P);
+        HostCsr R;
+        transpose(P, R);
+        HostCsr AP, Ac;
+        spgemm(A, P, AP);
+        spgemm(R, AP, Ac);
+        cur.P = std::move(P);
+        cur.R = std::move(R);
+        A = std::move(Ac);
+        B.swap(Bc);
+        node_ptr = cptr;
+        ++sa_level;
+    }
+    HostAmgLevel& last = out.lev.back();
+    const int64_t nc = last.A.n;
+    if (nc > 6000) fail(MPET_ERR_INVALID, "AMG coarsest level too large for a dense solve");
+    std::vector<double> dense(nc * nc, 0.0);
+    for (int64_t i = 0; i < nc; ++i)
+        for (int64_t e = last.A.rp[i]; e < last.A.rp[i + 1]; ++e) dense[i * nc + last.A.ci[e]] = last.A.v[e];
+    out.ncoarse = nc;
+    if (!cholesky_inverse(dense, nc, out.cinv))
+        fail(MPET_ERR_INVALID, "AMG coarsest operator is not positive definite");
+    for (auto& L : out.lev)
+        if (!check_csr(L.A) || (L.P.n > 0 && (!check_csr(L.P) || !check_csr(L.R))))
+            fail(MPET_ERR_INVALID, "block AMG produced an inconsistent level");
+}
+
+// P1 vector elasticity mu (grad u, grad v) + mu (grad u^T, grad v) + lmbda (div u, div v)
+// on the free vertices (3 unknowns each, interleaved): the Galerkin operator of the P2
+// displacement block under the P1-in-P2 embedding (the embedding is exact, so the
+// product P^T A P is the P1 stiffness).  Rows are owned per vertex, cells taken from the
+// vertex incidence in ascending order (deterministic); the pattern is the vertex
+// adjacency restricted to free vertices.
+void p1_elasticity_host(int64_t nv, const std::vector<int64_t>& vptr, const std::vector<int32_t>& vadj,
+                        const std::vector<int64_t>& inc_ptr, const std::vector<int32_t>& inc,
+                        const std::vector<double>& geo, const std::vector<int32_t>& cells,
+                        const std::vector<int64_t>& cidx, double mu, double lmbda, HostCsr& A) {
+    int64_t nf = 0;
+    for (int64_t v = 0; v < nv; ++v)
+        if (cidx[v] >= 0) nf = std::max(nf, cidx[v] + 1);
+    A = HostCsr();
+    A.n = A.m = 3 * nf;
+    A.rp.assign(A.n + 1, 0);
+    std::vector<int64_t> row_of(nf, -1);
+    for (int64_t v = 0; v < nv; ++v)
+        if (cidx[v] >= 0) row_of[cidx[v]] = v;
+    for (int64_t f = 0; f < nf; ++f) {
+        const int64_t v = row_of[f];
+        int64_t cnt = 0;
+        for (int64_t e = vptr[v]; e < vptr[v + 1]; ++e) cnt += cidx[vadj[e]] >= 0;
+        for (int a = 0; a < 3; ++a) A.rp[3 * f + a + 1] = 3 * cnt;
+    }
+    for (int64_t i = 0; i < A.n; ++i) A.rp[i + 1] += A.rp[i];
+    A.ci.resize(A.rp[A.n]);
+    A.v.assign(A.rp[A.n], 0.0);
+#ifdef _OPENMP
+    omp_set_num_threads(host_threads());
+#endif
+#pragma omp parallel for schedule(dynamic, 1024)
+    for (int64_t f = 0; f < nf; ++f) {
+        const int64_t v = row_of[f];
+        std::vector<int32_t> fcols;
+        for (int64_t e = vptr[v]; e < vptr[v + 1]; ++e)
+            if (cidx[vadj[e]] >= 0) fcols.push_back(vadj[e]);
+        const int64_t w = (int64_t)fcols.size();
+        for (int a = 0; a < 3; ++a)
+            for (int64_t q = 0; q < w; ++q)
+                for (int b = 0; b < 3; ++b) A.ci[A.rp[3 * f + a] + 3 * q + b] = (int32_t)(3 * cidx[fcols[q]] + b);
+        for (int64_t it = inc_ptr[v]; it < inc_ptr[v + 1]; ++it) {
+            const int64_t cell = inc[it] >> 4;
+            const int m = inc[it] & 15;
+            const double* g = &geo[16 * cell];
+            const double vol = g[12];
+            for (int s = 0; s < 4; ++s) {
+                const int32_t ws = cells[4 * cell + s];
+                if (cidx[ws] < 0) continue;
+                const int64_t q = std::lower_bound(fcols.begin(), fcols.end(), ws) - fcols.begin();
+                const double* bm = g + 3 * m;
+                const double* bs = g + 3 * s;
+                const double dot = bm[0] * bs[0] + bm[1] * bs[1] + bm[2] * bs[2];
+                for (int a = 0; a < 3; ++a)
+                    for (int b = 0; b < 3; ++b)
+                        A.v[A.rp[3 * f + a] + 3 * q + b] +=
+                            vol * ((a == b ? mu * dot : 0.0) + mu * bm[b] * bs[a] + lmbda * bm[a] * bs[b]);
+            }
+        }
+    }
 }
 
 // Symmetric eigendecomposition A = Q diag(lam) Q^T of a small n x n matrix

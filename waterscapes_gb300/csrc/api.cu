@@ -466,7 +466,19 @@ int mpet_setup_preconditioner(mpet_ctx* c, double dt) {
         if (h.rp[0] != 0) fail(MPET_ERR_STATE, "unexpected row pointer base");
     };
     const int cs = c->prm.amg_coarse_size > 0 ? c->prm.amg_coarse_size : 500;
-    {
+    bool elast = false;
+    if (c->prm.prec_u_form == 1) {
+        try {
+            elast = setup_u_elasticity(c, fp32);
+        } catch (const Error&) {
+            // e.g. a coarsest elasticity operator that is not definite: the Laplacian form stands in
+            cudaGetLastError();
+            elast = false;
+        }
+        c->u_elast = elast;
+    }
+    if (!elast) {
+        c->u_elast = false;
         HostCsr h;
         fetch(c->Lu, h);
         HostAmg ha;
@@ -529,6 +541,14 @@ int mpet_setup_preconditioner(mpet_ctx* c, double dt) {
     }
     c->precond_ready = true;
     c->prec_dt = dt;
+    API_END(c)
+}
+
+int mpet_get_prec_info(mpet_ctx* c, int32_t* u_elasticity) {
+    API_BEGIN(c)
+    require(c->precond_ready, MPET_ERR_STATE, "mpet_setup_preconditioner must come first");
+    require(u_elasticity, MPET_ERR_INVALID, "NULL argument");
+    *u_elasticity = c->u_elast ? 1 : 0;
     API_END(c)
 }
 

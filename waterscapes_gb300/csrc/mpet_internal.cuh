@@ -156,6 +156,7 @@ struct AmgLevel {
     double* dinv64 = nullptr;
     float* dinv32 = nullptr;
     double rho = 1.0;  // spectral radius estimate of D^-1 A
+    bool nb_uu = false;  // operator = displacement block of the system's node-block copy
     // work buffers, each n * nvec elements of double (reused for float)
     void* x = nullptr;
     void* b = nullptr;
@@ -208,6 +209,16 @@ struct HostAmg {
 void amg_setup_host(const HostCsr& A, const HostCsr* P0, double theta, int coarse_size, int max_levels,
                     HostAmg& out);
 void sym_eig(int n, const double* A, double* Q, double* lam);
+// block smoothed aggregation from a first level A1 with near-nullspace B1 (A1.n x nb_cols,
+// row-major) and bs unknowns per node
+void amg_setup_block_host(const HostCsr& A1, const std::vector<double>& B1, int nb_cols, int bs, double theta,
+                          int coarse_size, int max_levels, HostAmg& out);
+double tridiag_max_eig_host(const std::vector<double>& a, const std::vector<double>& b);
+bool setup_u_elasticity(mpet_ctx* c, bool fp32);
+void p1_elasticity_host(int64_t nv, const std::vector<int64_t>& vptr, const std::vector<int32_t>& vadj,
+                        const std::vector<int64_t>& inc_ptr, const std::vector<int32_t>& inc,
+                        const std::vector<double>& geo, const std::vector<int32_t>& cells,
+                        const std::vector<int64_t>& cidx, double mu, double lmbda, HostCsr& A);
 double network_kappa(int J, const double* C, const double* K, double g, const double* Q, const double* lam);
 
 }  // namespace mpet
@@ -301,6 +312,7 @@ struct mpet_ctx {
     double* adj_b = nullptr;      // adjoint right-hand side (Dirichlet rows zeroed)
     double* adj_loss = nullptr;   // misfit value (1 double)
     double* elem_buf = nullptr;   // staged per-cell element data of the assembly, or null
+    bool u_elast = false;         // displacement preconditioner block: elasticity AMG (else Laplacian)
     bool elem_tried = false;
     // error-indicator scratch: per-facet terms, per-cell R4p density, its sum, bad-index flag
     double* est_fval = nullptr;

@@ -379,7 +379,8 @@ __global__ void k_sell_fill(int64_t n, int64_t nslices, const int64_t* __restric
 // column id and the block's values (each a coalesced 128-byte line across the
 // warp), gathers the 3 displacement or J pressure entries of x and updates
 // its 3 or J accumulators.  JM is a compile-time bound on J (loops unrolled).
-template <typename T, int JM, class Epi>
+// UU: the displacement block only (u slices, node columns), x of length Nu.
+template <typename T, int JM, class Epi, bool UU = false>
 __global__ void __launch_bounds__(256) k_spmv_nb(int64_t nnodes, int64_t nv, int64_t Nu, int J, int64_t nsu,
                                                  int64_t ns, const NbSlice* __restrict__ sl,
                                                  const int32_t* __restrict__ perm, const int32_t* __restrict__ cols,
@@ -415,7 +416,7 @@ __global__ void __launch_bounds__(256) k_spmv_nb(int64_t nnodes, int64_t nv, int
             }
             const T* v1 = v2 + (int64_t)S.w2 * 9 * 32;
             const int B1 = 3 * J;
-            for (int m = 0; m < S.w1; ++m) {
+            for (int m = 0; m < (UU ? 0 : S.w1); ++m) {
                 const int64_t w = __ldcs(c1 + (int64_t)m * 32);
 #pragma unroll
                 for (int a = 0; a < JM; ++a) {
@@ -914,6 +915,17 @@ static void launch_nb(mpet_ctx* c, const NodeBlocks& nb, const T* x, const Epi& 
     c->n_launch++;
 }
 
+// displacement block of the node-block system copy: u slices only, no vertex columns
+template <typename T, class Epi>
+static void launch_nb_uu(mpet_ctx* c, const NodeBlocks& nb, const T* x, const Epi& epi) {
+    int blocks = Epi::kRed > 0 ? NB_RED : grid_for(nb.nsu * 32, 256);
+    if (Epi::kRed == 0 && blocks > 152 * 16) blocks = 152 * 16;
+    k_spmv_nb<T, 2, Epi, true><<<blocks, 256, 0, c->stream>>>(c->nnodes, c->nv, c->Nu, c->J, nb.nsu, nb.nsu, nb.sl,
+                                                             nb.perm, nb.cols, nb_vals<T>(nb), x, epi, c->partials);
+    MPET_CHECK_LAUNCH();
+    c->n_launch++;
+}
+
 template <typename T>
 static const T* sell_vals(const Csr& A);
 template <>
@@ -977,6 +989,18 @@ static void launch_spmv(mpet_ctx* c, const Csr& A, const T* va, const T* x, cons
     }
     MPET_CHECK_LAUNCH();
     c->n_launch++;
+}
+
+// operator of an AMG level: its CSR copy, or the displacement block of the system
+template <typename T, int NV, class Epi>
+static void level_spmv(mpet_ctx* c, const AmgLevel& L, const T* x, const Epi& epi) {
+    if constexpr (NV == 1) {
+        if (L.nb_uu) {
+            launch_nb_uu<T>(c, *c->A.nb, x, epi);
+            return;
+        }
+    }
+    launch_spmv<T, NV>(c, L.A, vals<T>(L.A), x, epi);
 }
 
 template <typename T>
@@ -1293,13 +1317,13 @@ static void cheb(mpet_ctx* c, AmgHier& h, AmgLevel& L, const T* b, const T* xin,
         c->n_launch++;
     } else {
         const EpiCheb<T, NV> e{b, xin, d, cur, dinv, T(0), (T)(1.0 / theta)};
-        launch_spmv<T, NV>(c, L.A, vals<T>(L.A), xin, e);
+        level_spmv<T, NV>(c, L, xin, e);
     }
     for (int j = 1; j < s; ++j) {
         const double rho_new = 1.0 / (2.0 * sigma - rho_old);
         const T c1 = (T)(rho_new * rho_old), c2 = (T)(2.0 * rho_new / delta);
         T* nxt = (j == s - 1) ? xout : (cur == t0 ? t1 : t0);
-        launch_spmv<T, NV>(c, L.A, vals<T>(L.A), cur, EpiCheb<T, NV>{b, cur, d, nxt, dinv, c1, c2});
+        level_spmv<T, NV>(c, L, cur, EpiCheb<T, NV>{b, cur, d, nxt, dinv, c1, c2});
         cur = nxt;
         rho_old = rho_new;
     }
@@ -1319,7 +1343,7 @@ static void vcycle(mpet_ctx* c, AmgHier& h, size_t k, const T* b, T* x) {
     T* xs = (T*)L.x;
     T* r = (T*)L.r;
     cheb<T, NV>(c, h, L, b, nullptr, xs);
-    launch_spmv<T, NV>(c, L.A, vals<T>(L.A), xs, EpiAxpby<T, NV>{r, b, T(-1), T(1)});
+    level_spmv<T, NV>(c, L, xs, EpiAxpby<T, NV>{r, b, T(-1), T(1)});
     launch_spmv<T, NV>(c, L.R, vals<T>(L.R), r, EpiStore<T, NV>{(T*)C.b});
     vcycle<T, NV>(c, h, k + 1, (const T*)C.b, (T*)C.x);
     launch_spmv<T, NV>(c, L.P, vals<T>(L.P), (const T*)C.x, EpiAxpby<T, NV>{xs, xs, T(1), T(1)});
@@ -1390,14 +1414,19 @@ static void precond(mpet_ctx* c, const T* r, T* z) {
     }
     c->stream = main;
     AmgHier& hu = c->amg_u;
-    const int64_t nodes = c->nnodes;
-    T* bin = (T*)hu.pack_in;
-    T* xout = (T*)hu.pack_out;
-    k_pack34<T><<<grid_for(nodes, 256), 256, 0, main>>>(nodes, c->dim, r, bin);
-    vcycle<T, 4>(c, hu, 0, bin, xout);
-    k_unpack43<T><<<grid_for(nodes, 256), 256, 0, main>>>(nodes, c->dim, xout, z);
-    MPET_CHECK_LAUNCH();
-    c->n_launch += 2;
+    if (c->u_elast) {
+        // elasticity hierarchy on the interleaved displacement unknowns
+        vcycle<T, 1>(c, hu, 0, r, z);
+    } else {
+        const int64_t nodes = c->nnodes;
+        T* bin = (T*)hu.pack_in;
+        T* xout = (T*)hu.pack_out;
+        k_pack34<T><<<grid_for(nodes, 256), 256, 0, main>>>(nodes, c->dim, r, bin);
+        vcycle<T, 4>(c, hu, 0, bin, xout);
+        k_unpack43<T><<<grid_for(nodes, 256), 256, 0, main>>>(nodes, c->dim, xout, z);
+        MPET_CHECK_LAUNCH();
+        c->n_launch += 2;
+    }
     for (int a = 0; a < c->J; ++a) MPET_CUDA(cudaStreamWaitEvent(main, c->ev_join[a], 0));
     if (c->net_modes) {
         k_modes<T, false><<<grid_for(c->nv, 256), 256, 0, main>>>(c->nv, c->J, c->vert_inst, c->mode_Q,
@@ -2247,6 +2276,241 @@ void upload_amg(mpet_ctx* c, AmgHier& h, const HostAmg& ha, int nvec, bool fp32)
     MPET_CUDA(cudaMemcpyAsync(h.cinv, ha.cinv.data(), sizeof(double) * ha.ncoarse * ha.ncoarse,
                               cudaMemcpyHostToDevice, c->stream));
     MPET_CUDA(cudaStreamSynchronize(c->stream));
+}
+
+// ---- displacement block as elasticity AMG ------------------------------------------------
+//
+// Level 0 is the displacement block of the system itself (its node-block copy,
+// Chebyshev on D^-1 A_uu); level 1 the P1 vector elasticity on the free vertices
+// reached by the P1-in-P2 embedding of each component; below it smoothed
+// aggregation with the six rigid-body modes (amg_setup_block_host).
+
+__global__ void k_lz_init(int64_t n, const double* __restrict__ dinv, const uint8_t* __restrict__ bc, double* s,
+                          double* v) {
+    const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    s[i] = dinv[i] > 0.0 ? sqrt(dinv[i]) : 0.0;
+    v[i] = bc[i] ? 0.0 : 0.5 + (double)((7919LL * i) % 1009LL) / 1009.0;
+}
+template <typename T>
+__global__ void k_lz_mul(int64_t n, const double* __restrict__ s, const double* __restrict__ v, T* w) {
+    const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    if (i < n) w[i] = (T)(s[i] * v[i]);
+}
+template <typename T>
+__global__ void k_lz_w(int64_t n, const double* __restrict__ s, const T* __restrict__ t, double beta,
+                       const double* __restrict__ vprev, double* w) {
+    const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    if (i < n) w[i] = s[i] * (double)t[i] - beta * vprev[i];
+}
+__global__ void k_lz_axpy(int64_t n, double* w, double a, const double* __restrict__ v) {
+    const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    if (i < n) w[i] += a * v[i];
+}
+__global__ void k_lz_next(int64_t n, const double* __restrict__ w, double ib, double* vprev, double* v) {
+    const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    vprev[i] = v[i];
+    v[i] = w[i] * ib;
+}
+
+// Spectral radius of D^-1 A_uu: 30 Lanczos steps on D^-1/2 A_uu D^-1/2 from the fixed
+// start vector of the host setup with the Dirichlet rows zeroed (the iterates stay
+// where the row-replaced block acts symmetrically).
+template <typename T>
+static double nb_uu_rho(mpet_ctx* c, const double* dinv) {
+    const int64_t n = c->Nu;
+    TmpBuf bs(sizeof(double) * n), bv(sizeof(double) * n), bp(sizeof(double) * n), bw(sizeof(double) * n),
+        bt(sizeof(double) * n);
+    double *s = bs.as<double>(), *v = bv.as<double>(), *vp = bp.as<double>(), *w = bw.as<double>();
+    T* t = bt.as<T>();
+    const int G = grid_for(n, 256);
+    k_lz_init<<<G, 256, 0, c->stream>>>(n, dinv, c->dof_bc, s, v);
+    MPET_CUDA(cudaMemsetAsync(vp, 0, sizeof(double) * n, c->stream));
+    MPET_CHECK_LAUNCH();
+    double nrm = sqrt(dot_host(c, v, v, n));
+    if (!(nrm > 0.0)) return 1.0;
+    k_lz_next<<<G, 256, 0, c->stream>>>(n, v, 1.0 / nrm, w, v);  // v /= |v| (w scratch)
+    MPET_CUDA(cudaMemsetAsync(vp, 0, sizeof(double) * n, c->stream));
+    std::vector<double> al, be(1, 0.0);
+    double beta = 0.0;
+    TmpBuf bx(sizeof(double) * n);
+    T* xin = bx.as<T>();
+    for (int k = 0; k < 30; ++k) {
+        k_lz_mul<T><<<G, 256, 0, c->stream>>>(n, s, v, xin);
+        launch_nb_uu<T>(c, *c->A.nb, xin, EpiStore<T, 1>{t});
+        k_lz_w<T><<<G, 256, 0, c->stream>>>(n, s, t, beta, vp, w);
+        MPET_CHECK_LAUNCH();
+        const double alpha = dot_host(c, w, v, n);
+        al.push_back(alpha);
+        k_lz_axpy<<<G, 256, 0, c->stream>>>(n, w, -alpha, v);
+        beta = sqrt(dot_host(c, w, w, n));
+        if (beta <= 1e-14 * fabs(alpha) || k + 1 == 30) break;
+        be.push_back(beta);
+        k_lz_next<<<G, 256, 0, c->stream>>>(n, w, 1.0 / beta, vp, v);
+    }
+    return tridiag_max_eig_host(al, be);
+}
+
+bool setup_u_elasticity(mpet_ctx* c, bool fp32) {
+    c->u_elast = false;
+    if (c->dim != 3 || !c->A.nb || c->ninst > 0 || c->nrigid > 0) return false;
+    if (fp32 ? !c->A.nb->v32 : !c->A.nb->v64) return false;
+    if (c->bc_off[1] == c->bc_off[0]) return false;  // no displacement Dirichlet rows: singular block
+    const int64_t nv = c->nv, nc = c->nc, Nu = c->Nu, nn = c->nnodes;
+    std::vector<uint8_t> bc(nn);
+    std::vector<int64_t> n1p(nn + 1), incp(nn + 1), ek(c->ne);
+    std::vector<double> geo((size_t)nc * 16), xyz((size_t)nv * 3);
+    std::vector<int32_t> cells((size_t)nc * 4);
+    auto d2h = [&](void* dst, const void* src, size_t bytes) {
+        MPET_CUDA(cudaMemcpyAsync(dst, src, bytes, cudaMemcpyDeviceToHost, c->stream));
+    };
+    d2h(bc.data(), c->node_bc, nn);
+    d2h(n1p.data(), c->n1_ptr, sizeof(int64_t) * (nn + 1));
+    d2h(incp.data(), c->inc_ptr, sizeof(int64_t) * (nn + 1));
+    d2h(ek.data(), c->edge_key, sizeof(int64_t) * c->ne);
+    d2h(geo.data(), c->geo, sizeof(double) * geo.size());
+    d2h(xyz.data(), c->x, sizeof(double) * xyz.size());
+    d2h(cells.data(), c->cells, sizeof(int32_t) * cells.size());
+    MPET_CUDA(cudaStreamSynchronize(c->stream));
+    std::vector<int32_t> n1c(n1p[nv]), inc(incp[nv]);
+    d2h(n1c.data(), c->n1_col, sizeof(int32_t) * n1c.size());
+    d2h(inc.data(), c->inc, sizeof(int32_t) * inc.size());
+    MPET_CUDA(cudaStreamSynchronize(c->stream));
+    std::vector<int64_t> vptr(n1p.begin(), n1p.begin() + nv + 1);
+    std::vector<int64_t> cidx(nv, -1);
+    int64_t nf = 0;
+    for (int64_t v = 0; v < nv; ++v)
+        if (!bc[v]) cidx[v] = nf++;
+    if (nf == 0) return false;
+    const double lm = c->prm.formulation == MPET_FORM_TOTAL_PRESSURE ? 0.0 : c->prm.lmbda;
+    HostCsr A1;
+    p1_elasticity_host(nv, vptr, n1c, std::vector<int64_t>(incp.begin(), incp.begin() + nv + 1), inc, geo, cells,
+                       cidx, c->prm.mu, lm, A1);
+    // rigid-body modes at the free vertices, about their centroid
+    double cx[3] = {0, 0, 0};
+    for (int64_t v = 0; v < nv; ++v)
+        if (cidx[v] >= 0)
+            for (int k = 0; k < 3; ++k) cx[k] += xyz[3 * v + k];
+    for (int k = 0; k < 3; ++k) cx[k] /= (double)nf;
+    std::vector<double> B1((size_t)3 * nf * 6, 0.0);
+    for (int64_t v = 0; v < nv; ++v) {
+        const int64_t f = cidx[v];
+        if (f < 0) continue;
+        const double X = xyz[3 * v] - cx[0], Y = xyz[3 * v + 1] - cx[1], Z = xyz[3 * v + 2] - cx[2];
+        double* b0 = &B1[(3 * f) * 6];
+        double* b1 = &B1[(3 * f + 1) * 6];
+        double* b2 = &B1[(3 * f + 2) * 6];
+        b0[0] = 1.0;
+        b1[1] = 1.0;
+        b2[2] = 1.0;
+        b1[3] = -Z; b2[3] = Y;   // e_x x r
+        b0[4] = Z;  b2[4] = -X;  // e_y x r
+        b0[5] = -Y; b1[5] = X;   // e_z x r
+    }
+    const int cs = c->prm.amg_coarse_size > 0 ? c->prm.amg_coarse_size : 500;
+    HostAmg ha;
+    amg_setup_block_host(A1, B1, 6, 3, 0.5 * (c->prm.amg_theta >= 0 ? c->prm.amg_theta : 0.1), cs, 12, ha);
+    AmgHier& h = c->amg_u;
+    upload_amg(c, h, ha, 1, fp32);
+    // level 0: the system's displacement block; P = P1-in-P2 embedding of each component
+    HostCsr P0;
+    P0.n = Nu;
+    P0.m = 3 * nf;
+    P0.rp.assign(Nu + 1, 0);
+    auto ends = [&](int64_t i, int64_t out[2]) -> int {
+        if (bc[i]) return 0;
+        if (i < nv) {
+            out[0] = i;
+            return 1;
+        }
+        int q = 0;
+        const int64_t lo = ek[i - nv] / nv, hi = ek[i - nv] % nv;
+        if (cidx[lo] >= 0) out[q++] = lo;
+        if (cidx[hi] >= 0) out[q++] = hi;
+        return q;
+    };
+    for (int64_t i = 0; i < nn; ++i) {
+        int64_t e2[2];
+        const int q = ends(i, e2);
+        for (int a = 0; a < 3; ++a) P0.rp[3 * i + a + 1] = q;
+    }
+    for (int64_t i = 0; i < Nu; ++i) P0.rp[i + 1] += P0.rp[i];
+    P0.ci.resize(P0.rp[Nu]);
+    P0.v.resize(P0.rp[Nu]);
+    for (int64_t i = 0; i < nn; ++i) {
+        int64_t e2[2];
+        const int q = ends(i, e2);
+        for (int a = 0; a < 3; ++a) {
+            int64_t p = P0.rp[3 * i + a];
+            for (int t = 0; t < q; ++t) {
+                P0.ci[p] = (int32_t)(3 * cidx[e2[t]] + a);
+                P0.v[p] = i < nv ? 1.0 : 0.5;
+                ++p;
+            }
+        }
+    }
+    // columns ascending within a row (lo < hi, cidx increasing with the vertex id); the
+    // tables index device arrays, so check them before the upload
+    for (int64_t i = 0; i < Nu; ++i)
+        if (P0.rp[i + 1] < P0.rp[i]) fail(MPET_ERR_INVALID, "embedding row pointers not monotone");
+    for (int32_t j : P0.ci)
+        if (j < 0 || j >= P0.m) fail(MPET_ERR_INVALID, "embedding column out of range");
+    if (h.lev.empty() || h.lev[0].A.n != P0.m) fail(MPET_ERR_INVALID, "elasticity hierarchy size mismatch");
+    AmgLevel L0;
+    L0.nb_uu = true;
+    L0.A.n = L0.A.m = Nu;
+    upload_csr(c, P0, L0.P, fp32);
+    HostCsr R0;
+    {
+        R0.n = P0.m;
+        R0.m = P0.n;
+        R0.rp.assign(R0.n + 1, 0);
+        for (int32_t j : P0.ci) R0.rp[j + 1]++;
+        for (int64_t i = 0; i < R0.n; ++i) R0.rp[i + 1] += R0.rp[i];
+        R0.ci.resize(P0.ci.size());
+        R0.v.resize(P0.ci.size());
+        std::vector<int64_t> pos(R0.rp.begin(), R0.rp.end() - 1);
+        for (int64_t i = 0; i < P0.n; ++i)
+            for (int64_t e = P0.rp[i]; e < P0.rp[i + 1]; ++e) {
+                const int64_t p = pos[P0.ci[e]]++;
+                R0.ci[p] = (int32_t)i;
+                R0.v[p] = P0.v[e];
+            }
+    }
+    upload_csr(c, R0, L0.R, fp32);
+    L0.dinv64 = c->pool.alloc<double>(Nu);
+    MPET_CUDA(cudaMemcpyAsync(L0.dinv64, c->dinv, sizeof(double) * Nu, cudaMemcpyDeviceToDevice, c->stream));
+    if (fp32) {
+        L0.dinv32 = c->pool.alloc<float>(Nu);
+        k_f64_to_f32<<<grid_for(Nu, 256), 256, 0, c->stream>>>(Nu, L0.dinv64, L0.dinv32);
+        MPET_CHECK_LAUNCH();
+    }
+    L0.rho = fp32 ? nb_uu_rho<float>(c, L0.dinv64) : nb_uu_rho<double>(c, L0.dinv64);
+    L0.x = c->pool.alloc<double>(Nu);
+    L0.b = c->pool.alloc<double>(Nu);
+    L0.r = c->pool.alloc<double>(Nu);
+    L0.d = c->pool.alloc<double>(Nu);
+    L0.t0 = c->pool.alloc<double>(Nu);
+    L0.t1 = c->pool.alloc<double>(Nu);
+    h.lev.insert(h.lev.begin(), L0);
+    {
+        AmgLevel& Z = h.lev[0];
+        AmgLevel& C = h.lev[1];
+        MPET_CUDA(cudaMemsetAsync(C.x, 0, sizeof(double) * C.A.n, c->stream));
+        MPET_CUDA(cudaMemsetAsync(Z.t0, 0, sizeof(double) * Nu, c->stream));
+        MPET_CUDA(cudaMemsetAsync(Z.r, 0, sizeof(double) * Nu, c->stream));
+        if (fp32) {
+            autotune_matrix<float, 1>(c, Z.P, (const float*)C.x, EpiAxpby<float, 1>{(float*)Z.t0, (const float*)Z.t0, 1.f, 1.f});
+            autotune_matrix<float, 1>(c, Z.R, (const float*)Z.r, EpiStore<float, 1>{(float*)C.b});
+        } else {
+            autotune_matrix<double, 1>(c, Z.P, (const double*)C.x, EpiAxpby<double, 1>{(double*)Z.t0, (const double*)Z.t0, 1.0, 1.0});
+            autotune_matrix<double, 1>(c, Z.R, (const double*)Z.r, EpiStore<double, 1>{(double*)C.b});
+        }
+    }
+    MPET_CUDA(cudaStreamSynchronize(c->stream));
+    c->u_elast = true;
+    return true;
 }
 
 // ---- public helpers used by the API ------------------------------------------------------
