@@ -151,7 +151,7 @@ class MPETSolver:
                 "precision": "mixed", "rtol": 1e-10, "inner_rtol": 1e-4, "maxit": 20000,
                 "max_outer": 40, "amg_theta": 0.1, "amg_cheb_degree": 4, "amg_coarse_size": 500,
                 "amg_p2_to_p1": True, "prec_u_weight": "mu+lmbda", "prec_network_modes": True,
-                "prec_u_form": "elasticity",
+                "prec_u_form": "laplacian",
                 "check_every": 4, "device": 0}
 
     def _make_params(self):
@@ -183,7 +183,7 @@ class MPETSolver:
         w = self.params["prec_u_weight"]
         prm.prec_u_weight = {"mu+lmbda": mu + lmbda, "mu": mu, "2mu": 2.0 * mu}[w] if isinstance(w, str) else float(w)
         prm.prec_network_modes = 1 if self.params["prec_network_modes"] else 0
-        prm.prec_u_form = {"laplacian": 0, "elasticity": 1}[self.params.get("prec_u_form", "elasticity")]
+        prm.prec_u_form = {"laplacian": 0, "elasticity": 1}[self.params.get("prec_u_form", "laplacian")]
         if self.problem.u_has_nullspace:
             # mass shift of the displacement preconditioner block at the scale of the
             # lowest elastic mode: (mu + lambda) / diam^2
