@@ -281,8 +281,12 @@ def loop_split(solver, before, steps):
             "outside_inner_ms_per_step": ((c1 - c0) - (a1 - a0)) / steps}
 
 
+CPU_SAMPLE_N = 16  # cube of the CPU sample (work per step scales with N: mesh-independent iterations)
+
+
 def cpu_baseline_sample(n_sample=12, J=4, steps=1):
-    """Oracle (numpy/scipy FP64, 1 thread) solve_direct steps on a small cube, scaled by N."""
+    """Oracle solve_direct steps on a small cube (the C restatement of MINRES + V-cycles on
+    every host thread when built, else numpy), for scaling by N."""
     sys.path.insert(0, os.path.join(ROOT, "tests"))
     from oracle import krylov
     from oracle.mpet import OracleMPET
@@ -301,6 +305,12 @@ def cpu_baseline_sample(n_sample=12, J=4, steps=1):
     hu = krylov.SAHierarchy(blocks[0], theta=0.1, cheb_degree=4, P0=P0)
     hp = [krylov.SAHierarchy(B, theta=0.1, cheb_degree=4) for B in blocks[1:]]
     M = krylov.block_preconditioner(hu, hp, 3, om.dm.Nu, om.dm.nv, Q=md[0])
+    try:
+        from oracle import cbaseline
+        cbaseline.load()
+        use_c = True
+    except Exception:
+        use_c = False
     up = np.zeros(om.dm.N)
     t = 0.0
     t0 = time.perf_counter()
@@ -311,11 +321,29 @@ def cpu_baseline_sample(n_sample=12, J=4, steps=1):
         x0 = up.copy()
         for d_, v_ in zip(dofs, vals):
             x0[d_] = v_
-        d, it, _ = krylov.minres(Abc, b - Abc @ x0, M, rtol=1e-10, maxiter=5000)
+        if use_c:
+            d, it, _ = cbaseline.minres(Abc, b - Abc @ x0, hu, hp, 3, om.dm.Nu, om.dm.nv, Q=md[0], rtol=1e-10,
+                                        maxiter=5000)
+        else:
+            d, it, _ = krylov.minres(Abc, b - Abc @ x0, M, rtol=1e-10, maxiter=5000)
         up = x0 + d
         t += dt
     sec = (time.perf_counter() - t0) / steps
-    return sec, om.dm.N
+    cores = host_cores() if use_c else 1
+    kind = ("oracle C restatement (OpenMP MINRES + SA V-cycles, %d threads; numpy right-hand side)" % cores
+            if use_c else "oracle (numpy/scipy FP64 MINRES + SA-AMG, 1 thread)")
+    return sec, om.dm.N, cores, kind
+
+
+def host_cores():
+    """Threads OpenMP will use: OMP_NUM_THREADS, else the CPU affinity set."""
+    v = os.environ.get("OMP_NUM_THREADS")
+    if v and v.isdigit():
+        return int(v)
+    try:
+        return len(os.sched_getaffinity(0))
+    except AttributeError:
+        return os.cpu_count() or 1
 
 
 def profile_case(args):
@@ -618,16 +646,16 @@ def main():
         if rank != 0:
             return
         steps = max(1, args.steps)
-        sec, Ns = cpu_baseline_sample(12, J, steps=min(steps, 3))
+        sec, Ns, cores, kind = cpu_baseline_sample(CPU_SAMPLE_N, J, steps=min(steps, 3))
         scaled = 1.0 / (sec * N_full / Ns)
         line = {"impl": "reference", "metric": METRIC, "value": scaled, "unit": "steps/s", "n_gpus": 0,
                 "steps": min(steps, 3), "warmup": 0, "ms_per_step": 1e3 / scaled, "higher_is_better": True,
                 "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
                 "config": {"workload": workload_name},
-                "cpu_baseline": {"value": scaled, "unit": "steps/s", "cores": 1, "kind": "port",
-                                 "sample": "oracle (numpy/scipy FP64 MINRES + SA-AMG, solve_direct step) on the 12^3 "
-                                           "A=4 cube (N=%d), per-step time scaled by N ratio %.1f; FEniCS/PETSc "
-                                           "(the reference's own path) is not installable here" % (Ns, N_full / Ns)},
+                "cpu_baseline": {"value": scaled, "unit": "steps/s", "cores": cores, "kind": "port",
+                                 "sample": "%s, solve_direct step on the %d^3 A=4 cube (N=%d), per-step time scaled "
+                                           "by N ratio %.1f; FEniCS/PETSc (the reference's own path) is not "
+                                           "installable here" % (kind, CPU_SAMPLE_N, Ns, N_full / Ns)},
                 "e2e": {"value": scaled, "unit": "steps/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
         print(json.dumps(line))
         return
@@ -722,11 +750,11 @@ def main():
 
     cpu = None
     if rank == 0 and not args.no_cpu and not tp:
-        sec, Ns = cpu_baseline_sample(12, J, steps=1)
+        sec, Ns, cores, kind = cpu_baseline_sample(CPU_SAMPLE_N, J, steps=1)
         cpu_val = 1.0 / (sec * N_full / Ns)
-        cpu = {"value": cpu_val, "unit": "steps/s", "cores": 1, "kind": "port",
-               "sample": "oracle (numpy/scipy FP64 MINRES + SA-AMG) one solve_direct step on the 12^3 A=4 cube "
-                         "(N=%d, %.1f s), scaled by the DOF ratio %.1f" % (Ns, sec, N_full / Ns)}
+        cpu = {"value": cpu_val, "unit": "steps/s", "cores": cores, "kind": "port",
+               "sample": "%s, one solve_direct step on the %d^3 A=4 cube (N=%d, %.1f s), scaled by the DOF "
+                         "ratio %.1f" % (kind, CPU_SAMPLE_N, Ns, sec, N_full / Ns)}
 
     if rank != 0:
         return
