@@ -281,7 +281,7 @@ def loop_split(solver, before, steps):
             "outside_inner_ms_per_step": ((c1 - c0) - (a1 - a0)) / steps}
 
 
-CPU_SAMPLE_N = 16  # cube of the CPU sample (work per step scales with N: mesh-independent iterations)
+CPU_SAMPLE_N = 20  # cube of the CPU sample (work per step scales with N: mesh-independent iterations)
 
 
 def cpu_baseline_sample(n_sample=12, J=4, steps=1):
