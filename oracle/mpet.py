@@ -377,8 +377,9 @@ class OracleMPET:
         """(Q, lambda) of the pressure blocks: per network (Q = I, lambda =
         diag C) or per eigenmode of the network mass coupling C = Q diag(lambda)
         Q^T, C = diag(c_a + dt theta sum_{b != a} S_ab) - dt theta S (off the
-        diagonal).  "auto" takes the form whose worst condition number of
-        P(t)^-1 (C + t dt theta diag(K)) over t in [1, 1e6] is smaller."""
+        diagonal).  "auto" takes the eigenmodes when their worst condition number of
+        P(t)^-1 (C + t dt theta diag(K)) over t in [1, 1e6] is below half that of the
+        per-network form."""
         J = self.J
         dth = dt * self.theta
         C = -dth * self.S.copy()
@@ -402,7 +403,7 @@ class OracleMPET:
                     np.linalg.cholesky(P), A).T).T)
                 worst = max(worst, ev.max() / ev.min())
             return worst
-        if np.all(lam > 0) and kappa(Q, lam) < kappa(*per_net):
+        if np.all(lam > 0) and 2.0 * kappa(Q, lam) < kappa(*per_net):
             return Q, lam
         return per_net
 

@@ -985,7 +985,8 @@ void launch_misfit(mpet_ctx* c, const double* up, const double* target, double* 
 // reference's block-diagonal form, mpetsolver.py:270, drops it and loses
 // robustness when dt S >> c) but averages the K_a of the modes (poor when
 // the K_a differ by orders of magnitude).  Each instance takes the form with
-// the smaller worst-case condition number of its J x J network operator.
+// the eigenmodes when their worst-case condition number of its J x J network operator
+// is below half that of the per-network form.
 
 __global__ void k_gather_coef(int ninst, const int64_t* __restrict__ rep, int J, int64_t nc,
                               const double* __restrict__ cc, const double* __restrict__ Sc,
@@ -1084,7 +1085,9 @@ void setup_network_modes(mpet_ctx* c, double dt) {
         for (int k = 0; k < J; ++k) modes_ok = modes_ok && lm[k] > 0.0;
         const double kd = network_kappa(J, C.data(), K.data(), dth, Qd.data(), ld.data());
         const double km = modes_ok ? network_kappa(J, C.data(), K.data(), dth, Qm.data(), lm.data()) : 1e300;
-        const bool use = km < kd;
+        // the eigenmodes must win clearly: the J x J analysis leaves out the displacement
+        // coupling, and at a ratio below 2 the per-network form often needs fewer iterations
+        const bool use = 2.0 * km < kd;
         used += use ? 1 : 0;
         std::copy((use ? Qm : Qd).begin(), (use ? Qm : Qd).end(), Q.begin() + (size_t)i * J * J);
         std::copy((use ? lm : ld).begin(), (use ? lm : ld).end(), lam.begin() + (size_t)i * J);
