@@ -824,7 +824,8 @@ void sym_eig(int n, const double* A_in, double* Q, double* lam) {
 // mass eigenvalues from the smoothest to the finest P1 mode), of the
 // preconditioned network operator P(t)^-1 (C + t g diag(K)) for
 // P(t) = Q (diag(lam) + t g diag(kt)) Q^T, kt_k = sum_a Q_ak^2 K_a.
-double network_kappa(int J, const double* C, const double* K, double g, const double* Q, const double* lam) {
+double network_kappa(int J, const double* C, const double* K, double g, const double* Q, const double* lam,
+                     int first_step) {
     double worst = 1.0;
     std::vector<double> A(J * J), P(J * J), L(J * J), W(J * J), T(J * J), V(J * J), ev(J);
     std::vector<double> kt(J);
@@ -832,7 +833,7 @@ double network_kappa(int J, const double* C, const double* K, double g, const do
         kt[k] = 0.0;
         for (int a = 0; a < J; ++a) kt[k] += Q[a * J + k] * Q[a * J + k] * K[a];
     }
-    for (int step = 0; step <= 60; ++step) {
+    for (int step = first_step; step <= 60; ++step) {
         const double t = pow(10.0, 0.1 * step);
         for (int a = 0; a < J; ++a)
             for (int b = 0; b < J; ++b) {

@@ -986,7 +986,7 @@ void launch_misfit(mpet_ctx* c, const double* up, const double* target, double* 
 // robustness when dt S >> c) but averages the K_a of the modes (poor when
 // the K_a differ by orders of magnitude).  Each instance takes the form with
 // the eigenmodes when their worst-case condition number of its J x J network operator
-// is below half that of the per-network form.
+// is below half that of the per-network form and at most twice it at large t.
 
 __global__ void k_gather_coef(int ninst, const int64_t* __restrict__ rep, int J, int64_t nc,
                               const double* __restrict__ cc, const double* __restrict__ Sc,
@@ -1085,9 +1085,12 @@ void setup_network_modes(mpet_ctx* c, double dt) {
         for (int k = 0; k < J; ++k) modes_ok = modes_ok && lm[k] > 0.0;
         const double kd = network_kappa(J, C.data(), K.data(), dth, Qd.data(), ld.data());
         const double km = modes_ok ? network_kappa(J, C.data(), K.data(), dth, Qm.data(), lm.data()) : 1e300;
-        // the eigenmodes must win clearly: the J x J analysis leaves out the displacement
-        // coupling, and at a ratio below 2 the per-network form often needs fewer iterations
-        const bool use = 2.0 * km < kd;
+        // The eigenmodes must win clearly over all t, and must not lose at large t (t >= 1e3),
+        // where most eigenvalues of the pressure blocks lie: there the modes average K over
+        // the networks, and a K spread costs far more iterations than a mass-regime outlier.
+        const double kdh = network_kappa(J, C.data(), K.data(), dth, Qd.data(), ld.data(), 30);
+        const double kmh = modes_ok ? network_kappa(J, C.data(), K.data(), dth, Qm.data(), lm.data(), 30) : 1e300;
+        const bool use = 2.0 * km < kd && kmh <= 2.0 * kdh;
         used += use ? 1 : 0;
         std::copy((use ? Qm : Qd).begin(), (use ? Qm : Qd).end(), Q.begin() + (size_t)i * J * J);
         std::copy((use ? lm : ld).begin(), (use ? lm : ld).end(), lam.begin() + (size_t)i * J);

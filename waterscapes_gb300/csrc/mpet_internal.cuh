@@ -219,7 +219,9 @@ void p1_elasticity_host(int64_t nv, const std::vector<int64_t>& vptr, const std:
                         const std::vector<int64_t>& inc_ptr, const std::vector<int32_t>& inc,
                         const std::vector<double>& geo, const std::vector<int32_t>& cells,
                         const std::vector<int64_t>& cidx, double mu, double lmbda, HostCsr& A);
-double network_kappa(int J, const double* C, const double* K, double g, const double* Q, const double* lam);
+// worst condition number of P(t)^-1 (C + t g diag(K)) over t = 10^(0.1 s), s = first_step..60
+double network_kappa(int J, const double* C, const double* K, double g, const double* Q, const double* lam,
+                     int first_step = 0);
 
 }  // namespace mpet
 
