@@ -377,10 +377,10 @@ class OracleMPET:
         """(Q, lambda) of the pressure blocks: per network (Q = I, lambda =
         diag C) or per eigenmode of the network mass coupling C = Q diag(lambda)
         Q^T, C = diag(c_a + dt theta sum_{b != a} S_ab) - dt theta S (off the
-        diagonal).  "auto" takes the eigenmodes when their worst condition number of
-        P(t)^-1 (C + t dt theta diag(K)) over t in [1, 1e6] is below half that of the
-        per-network form and, over t in [1e3, 1e6] (where most eigenvalues of the
-        pressure blocks lie), at most twice it."""
+        diagonal).  With kappa(form, T) the worst condition number of
+        P(t)^-1 (C + t dt theta diag(K)) over t in T, "auto" takes the eigenmodes when
+        kappa(modes, [1e3, 1e6])^2 < kappa(networks, [1, 1e6]): most eigenvalues of
+        the pressure blocks lie at large t, where the modes average K."""
         J = self.J
         dth = dt * self.theta
         C = -dth * self.S.copy()
@@ -404,8 +404,8 @@ class OracleMPET:
                     np.linalg.cholesky(P), A).T).T)
                 worst = max(worst, ev.max() / ev.min())
             return worst
-        if (np.all(lam > 0) and 2.0 * kappa(Q, lam) < kappa(*per_net)
-                and kappa(Q, lam, 30) <= 2.0 * kappa(*per_net, 30)):
+        kd = kappa(*per_net)
+        if np.all(lam > 0) and kappa(Q, lam) < kd and kappa(Q, lam, 30) ** 2 < kd:
             return Q, lam
         return per_net
 
