@@ -54,6 +54,15 @@ extern "C" {
  * alpha, c, K, S and the continuity markers count p0 as field 0 (alpha[0] = 1
  * weights p0 in the rank-one term, c[0] = K[0] = S[0][*] = S[*][0] = 0, and
  * field 0 carries no boundary condition). */
+/* Krylov methods.  AUTO: MINRES when the transfer matrix S is symmetric (the
+ * system is then symmetric), restarted GMRES with the same block-diagonal
+ * preconditioner (right-preconditioned) otherwise; the reference's direct
+ * solve has no such restriction (S = ((0, 2), (1, 0)) in
+ * src/mpet/test/test_convergence_mpetsolver.py:112-118). */
+#define MPET_KRYLOV_AUTO 0
+#define MPET_KRYLOV_MINRES 1
+#define MPET_KRYLOV_GMRES 2
+
 #define MPET_FORM_MPET 0
 #define MPET_FORM_TOTAL_PRESSURE 1
 
@@ -102,6 +111,8 @@ typedef struct mpet_params {
     double prec_p0_weight;             /* total-pressure form: w0 in the p0 block w0 (p0, w0) of
                                           the preconditioner (the reference form uses 1,
                                           mpettotalpressuresolver.py:281); <= 0 means 1 */
+    int32_t krylov;                    /* MPET_KRYLOV_*: the Krylov method of the solves */
+    int32_t gmres_restart;             /* GMRES restart length (<= 0: 30, at most 64) */
 } mpet_params;
 
 typedef struct mpet_stats {

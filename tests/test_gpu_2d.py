@@ -138,3 +138,53 @@ def test_reference_rate_thresholds_on_gpu(theta, ms, precision):
     assert r["p1L2"][-1] > 1.70
     assert r["p0H1"][-1] > 0.95
     assert r["p1H1"][-1] > 0.95
+
+
+@pytest.mark.parametrize("theta,ms,precision", [(1.0, (8, 32, 128), "fp64"), (0.5, (4, 8, 16), "fp64"),
+                                                (0.5, (4, 8, 16), "mixed")])
+def test_reference_rate_thresholds_nonsymmetric_S_gmres(theta, ms, precision):
+    """test_convergence_mpetsolver.py:234-239 with the reference's own transfer matrix
+    S = ((0, 2), (1, 0)) (:112-118): a non-symmetric system, solved by GMRES."""
+    data, exact = mms.exact_solutions(REF_PARAMS, 2)
+    errs = {k: [] for k in ("uL2", "uH1", "p0L2", "p1L2", "p0H1", "p1H1")}
+    hs = []
+    for n, M in zip((8, 16, 32), ms):
+        problem = _problem_2d(n, REF_PARAMS, data)
+        s = _solver(problem, 1.0 / M, 1.0, theta, precision=precision, rtol=1e-10)
+        for up, t in s.solve():
+            assert s.last_stats["status"] == 0
+        om = make_oracle(problem, theta)
+        e = mms.errornorms(om, up.vector().cpu().numpy(), t, exact)
+        errs["uL2"].append(e["uL2"])
+        errs["uH1"].append(e["uH1"])
+        for a in range(2):
+            errs["p%dL2" % a].append(e["pL2"][a])
+            errs["p%dH1" % a].append(e["pH1"][a])
+        hs.append(problem.mesh.hmin())
+    r = {k: mms.rates(v, hs) for k, v in errs.items()}
+    assert r["uH1"][-1] > 1.70
+    assert r["uL2"][-1] > 1.70
+    assert r["p0L2"][-1] > 1.70
+    assert r["p1L2"][-1] > 1.70
+    assert r["p0H1"][-1] > 0.95
+    assert r["p1H1"][-1] > 0.95
+
+
+@pytest.mark.parametrize("precision", ["fp64", "mixed"])
+def test_nonsymmetric_S_step_matches_oracle(precision):
+    """One step with S12 = 2, S21 = 1 (GMRES) against the oracle's SuperLU solve."""
+    data, exact = mms.exact_solutions(REF_PARAMS, 2)
+    problem = _problem_2d(6, REF_PARAMS, data)
+    dt = 0.05
+    s = _solver(problem, dt, 10 * dt, 1.0, precision=precision, rtol=1e-11)
+    om = make_oracle(problem, 1.0)
+    rng = np.random.default_rng(8)
+    up_prev = rng.standard_normal(om.dm.N) * 1e-2
+    t0 = 0.1
+    x_ref = om.step(up_prev, t0, dt, data)
+    s.up_.assign(torch.tensor(up_prev))
+    problem.time.assign(t0)
+    st = s.step(dt)
+    assert st.status == 0
+    x = s.up.vector().cpu().numpy()
+    assert np.linalg.norm(x - x_ref) <= 1e-8 * np.linalg.norm(x_ref)

@@ -24,6 +24,7 @@ ERRORS = {
 }
 PRECISION = {"fp64": 0, "mixed": 1}
 FORMULATION = {"mpet": 0, "total_pressure": 1}
+KRYLOV = {"auto": 0, "minres": 1, "gmres": 2}
 MAX_NETWORKS = 8
 
 
@@ -53,6 +54,8 @@ class MpetParams(ctypes.Structure):
         ("formulation", ctypes.c_int32),
         ("prec_u_form", ctypes.c_int32),
         ("prec_p0_weight", ctypes.c_double),
+        ("krylov", ctypes.c_int32),
+        ("gmres_restart", ctypes.c_int32),
     ]
 
 

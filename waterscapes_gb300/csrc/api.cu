@@ -146,6 +146,16 @@ int mpet_mesh_upload(mpet_ctx* c, int64_t nv, const double* xyz, int64_t nc, con
     return mpet_mesh_upload_dim(c, 3, nv, xyz, nc, tets, nf, bfacets, markers, J);
 }
 
+// GMRES when asked, or (AUTO) when the transfer matrix S is not symmetric
+static bool wants_gmres(const mpet_ctx* c, const mpet_params* p) {
+    if (p->krylov == MPET_KRYLOV_GMRES) return true;
+    if (p->krylov == MPET_KRYLOV_MINRES) return false;
+    for (int a = 0; a < c->J; ++a)
+        for (int b = 0; b < c->J; ++b)
+            if (p->S[a * MPET_MAX_NETWORKS + b] != p->S[b * MPET_MAX_NETWORKS + a]) return true;
+    return false;
+}
+
 static void check_params(const mpet_ctx* c, const mpet_params* p) {
     require(p != nullptr, MPET_ERR_INVALID, "params is NULL");
     require(p->num_networks == c->J, MPET_ERR_INVALID, "params.num_networks differs from the mesh upload");
@@ -155,6 +165,8 @@ static void check_params(const mpet_ctx* c, const mpet_params* p) {
     require(p->rtol > 0.0, MPET_ERR_INVALID, "rtol must be positive");
     require(p->formulation == MPET_FORM_MPET || p->formulation == MPET_FORM_TOTAL_PRESSURE, MPET_ERR_INVALID,
             "unknown formulation");
+    require(p->krylov >= MPET_KRYLOV_AUTO && p->krylov <= MPET_KRYLOV_GMRES && p->gmres_restart <= 64,
+            MPET_ERR_INVALID, "unknown Krylov method or restart above 64");
     if (p->formulation == MPET_FORM_TOTAL_PRESSURE) {
         require(c->J >= 2, MPET_ERR_INVALID, "the total-pressure form needs p0 and at least one network");
         require(p->lmbda > 0.0, MPET_ERR_INVALID, "the total-pressure form needs lmbda > 0");
@@ -171,6 +183,7 @@ int mpet_setup(mpet_ctx* c, const mpet_params* p) {
     require(!c->setup_done, MPET_ERR_STATE, "mpet_setup already done");
     check_params(c, p);
     c->prm = *p;
+    c->gmres = wants_gmres(c, p);
     if (c->prm.inner_rtol <= 0) c->prm.inner_rtol = 1e-4;
     if (c->prm.amg_theta < 0) c->prm.amg_theta = 0.1;
     build_topology(c);
@@ -206,6 +219,7 @@ int mpet_update_params(mpet_ctx* c, const mpet_params* p) {
     check_params(c, p);
     require(p->precision == c->prm.precision, MPET_ERR_INVALID, "precision is fixed at setup");
     c->prm = *p;
+    c->gmres = wants_gmres(c, p);
     if (c->prm.inner_rtol <= 0) c->prm.inner_rtol = 1e-4;
     c->assembled = false;
     c->precond_ready = false;
@@ -730,6 +744,7 @@ static void require_adjoint_ok(mpet_ctx* c) {
 
 int mpet_adjoint_rhs(mpet_ctx* c, double dt, const double* lam, double* out) {
     API_BEGIN(c)
+    require(!c->gmres, MPET_ERR_INVALID, "the adjoint needs a symmetric system (symmetric S)");
     require(!c->setup_done || c->prm.formulation == MPET_FORM_MPET, MPET_ERR_INVALID,
             "built for the MPET form only");
     require(c->setup_done, MPET_ERR_STATE, "mpet_setup must come first");
@@ -742,6 +757,7 @@ int mpet_adjoint_rhs(mpet_ctx* c, double dt, const double* lam, double* out) {
 int mpet_adjoint_step(mpet_ctx* c, double dt, const double* seed, const double* up_prev, const double* up,
                       double* lam, double* grad_K, mpet_stats* st) {
     API_BEGIN(c)
+    require(!c->gmres, MPET_ERR_INVALID, "the adjoint needs a symmetric system (symmetric S)");
     require(!c->setup_done || c->prm.formulation == MPET_FORM_MPET, MPET_ERR_INVALID,
             "built for the MPET form only");
     require(c->assembled, MPET_ERR_STATE, "mpet_assemble must come first");

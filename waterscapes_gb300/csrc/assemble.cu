@@ -1019,7 +1019,7 @@ void set_instances(mpet_ctx* c, int ninst, const int32_t* vertex_inst_host) {
 void setup_network_modes(mpet_ctx* c, double dt) {
     const int J = c->J;
     c->net_modes = false;
-    if (!c->prm.prec_network_modes || J < 2 || c->prm.formulation != MPET_FORM_MPET) return;
+    if (!c->prm.prec_network_modes || J < 2 || c->prm.formulation != MPET_FORM_MPET || c->gmres) return;
     // the transform mixes the networks at a vertex: all networks need the same Dirichlet vertices
     std::vector<uint8_t> vb((size_t)J * c->nv);
     MPET_CUDA(cudaMemcpyAsync(vb.data(), c->vert_bc, vb.size(), cudaMemcpyDeviceToHost, c->stream));

@@ -315,6 +315,15 @@ struct mpet_ctx {
     double* adj_loss = nullptr;   // misfit value (1 double)
     double* elem_buf = nullptr;   // staged per-cell element data of the assembly, or null
     bool u_elast = false;         // displacement preconditioner block: elasticity AMG (else Laplacian)
+    bool gmres = false;           // solves by restarted GMRES (non-symmetric system)
+    void* gm_V = nullptr;         // GMRES basis, (restart + 1) x N doubles
+    void* gm_z = nullptr;         // N doubles each
+    void* gm_w = nullptr;
+    void* gm_r = nullptr;
+    double* gm_part = nullptr;    // (restart + 1) * NB_RED reduction partials
+    double* gm_h = nullptr;       // restart + 1 device scalars
+    double* gm_h_host = nullptr;  // pinned
+    int gm_m = 0;                 // restart length the buffers hold
     bool elem_tried = false;
     // error-indicator scratch: per-facet terms, per-cell R4p density, its sum, bad-index flag
     double* est_fval = nullptr;

@@ -2172,11 +2172,273 @@ void batch_relres(mpet_ctx* c, double* out) {
     }
 }
 
+// ---- restarted GMRES (non-symmetric transfer matrix) ---------------------------------------
+//
+// Right-preconditioned GMRES(m) (Saad and Schultz, SIAM J. Sci. Stat. Comput. 7 (1986)
+// 856-869) with the block-diagonal preconditioner, inside the same FP64 refinement loop as
+// MINRES.  Arnoldi by classical Gram-Schmidt applied twice; the small Hessenberg system
+// and its Givens rotations live on the host.  Every reduction has a fixed order.
+
+// h[k] = V_k . w for k < m (V_k at V + k * ld); partials[k * NB_RED + block]
+template <typename T>
+__global__ void __launch_bounds__(256) k_mdot(int64_t n, int m, const T* __restrict__ V, int64_t ld,
+                                             const T* __restrict__ w, double* partials) {
+    __shared__ double sh[8];
+    for (int k = 0; k < m; ++k) {
+        double s = 0.0;
+        for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
+            s += (double)V[k * ld + i] * (double)w[i];
+        s = block_sum256(s, sh);
+        if (threadIdx.x == 0) partials[k * NB_RED + blockIdx.x] = s;
+    }
+}
+__global__ void k_mdot_finish(const double* __restrict__ partials, double* out) {
+    __shared__ double sh[8];
+    const double v = sum_partials(partials + blockIdx.x * NB_RED, sh);
+    if (threadIdx.x == 0) out[blockIdx.x] = v;
+}
+// w += sum_k coef[k] V_k (coef on the device, k < m)
+template <typename T>
+__global__ void k_mupdate(int64_t n, int m, const T* __restrict__ V, int64_t ld, const double* __restrict__ coef,
+                          double sign, T* w) {
+    const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    double s = 0.0;
+    for (int k = 0; k < m; ++k) s += coef[k] * (double)V[k * ld + i];
+    w[i] = (T)((double)w[i] + sign * s);
+}
+template <typename T>
+__global__ void k_gm_scale(int64_t n, const T* __restrict__ a, double f, T* out) {
+    const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    if (i < n) out[i] = (T)((double)a[i] * f);
+}
+template <typename T>
+__global__ void k_gm_sub(int64_t n, const T* __restrict__ a, const T* __restrict__ b, T* out) {
+    const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    if (i < n) out[i] = a[i] - b[i];
+}
+template <typename T>
+__global__ void k_gm_add(int64_t n, const T* __restrict__ a, T* out) {
+    const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    if (i < n) out[i] += a[i];
+}
+
+static void gm_alloc(mpet_ctx* c, int m) {
+    if (c->gm_V && c->gm_m >= m) return;
+    const int64_t n = c->N;
+    c->gm_V = c->pool.alloc<double>((int64_t)(m + 1) * n);
+    c->gm_z = c->pool.alloc<double>(n);
+    c->gm_w = c->pool.alloc<double>(n);
+    c->gm_r = c->pool.alloc<double>(n);
+    c->gm_part = c->pool.alloc<double>((int64_t)(m + 1) * NB_RED);
+    c->gm_h = c->pool.alloc<double>(m + 1);
+    if (c->gm_h_host) cudaFreeHost(c->gm_h_host);
+    MPET_CUDA(cudaMallocHost(&c->gm_h_host, sizeof(double) * (m + 1)));
+    c->gm_m = m;
+}
+
+// V_0..V_{k-1} . w into gm_h (device) and gm_h_host
+template <typename T>
+static void gm_dots(mpet_ctx* c, const T* V, int k, const T* w) {
+    const int64_t n = c->N;
+    k_mdot<T><<<NB_RED, 256, 0, c->stream>>>(n, k, V, n, w, c->gm_part);
+    k_mdot_finish<<<k, 256, 0, c->stream>>>(c->gm_part, c->gm_h);
+    MPET_CHECK_LAUNCH();
+    MPET_CUDA(cudaMemcpyAsync(c->gm_h_host, c->gm_h, sizeof(double) * k, cudaMemcpyDeviceToHost, c->stream));
+    MPET_CUDA(cudaStreamSynchronize(c->stream));
+}
+
+// d = GMRES(A, rhs) from d = 0 to ||rhs - A d||_2 <= target ||rhs||_2; returns the status
+template <typename T>
+static int gmres_run(mpet_ctx* c, const T* rhs, T* d, double target, int maxit, int* done) {
+    const int64_t n = c->N;
+    const int G = grid_for(n, 256);
+    int m = c->prm.gmres_restart > 0 ? c->prm.gmres_restart : 30;
+    if (m > 64) m = 64;
+    gm_alloc(c, m);
+    T* V = (T*)c->gm_V;
+    T* z = (T*)c->gm_z;
+    T* w = (T*)c->gm_w;
+    T* r = (T*)c->gm_r;
+    MPET_CUDA(cudaMemsetAsync(d, 0, sizeof(T) * n, c->stream));
+    MPET_CUDA(cudaMemcpyAsync(r, rhs, sizeof(T) * n, cudaMemcpyDeviceToDevice, c->stream));
+    gm_dots<T>(c, r, 1, r);
+    const double beta0 = sqrt(fmax(c->gm_h_host[0], 0.0));
+    double beta = beta0;
+    int total = 0;
+    *done = 0;
+    if (beta0 == 0.0) return MPET_OK;
+    std::vector<double> H((size_t)(m + 1) * m), cs(m), sn(m), g(m + 1), y(m);
+    while (true) {
+        k_gm_scale<T><<<G, 256, 0, c->stream>>>(n, r, 1.0 / beta, V);
+        MPET_CHECK_LAUNCH();
+        std::fill(g.begin(), g.end(), 0.0);
+        g[0] = beta;
+        int kk = 0;
+        bool conv = false;
+        for (int j = 0; j < m && total < maxit; ++j) {
+            T* vj = V + (int64_t)j * n;
+            precond<T>(c, vj, z);
+            launch_spmv<T, 1>(c, c->A, vals<T>(c->A), z, EpiStore<T, 1>{w});
+            c->n_spmv++;
+            double* h = &H[(size_t)j * (m + 1)];  // column j, rows 0..j+1
+            for (int i = 0; i <= j + 1; ++i) h[i] = 0.0;
+            for (int pass = 0; pass < 2; ++pass) {
+                gm_dots<T>(c, V, j + 1, w);
+                for (int i = 0; i <= j; ++i) h[i] += c->gm_h_host[i];
+                k_mupdate<T><<<G, 256, 0, c->stream>>>(n, j + 1, V, n, c->gm_h, -1.0, w);
+                MPET_CHECK_LAUNCH();
+            }
+            gm_dots<T>(c, w, 1, w);
+            const double hn = sqrt(fmax(c->gm_h_host[0], 0.0));
+            h[j + 1] = hn;
+            if (hn > 0.0) {
+                k_gm_scale<T><<<G, 256, 0, c->stream>>>(n, w, 1.0 / hn, V + (int64_t)(j + 1) * n);
+                MPET_CHECK_LAUNCH();
+            }
+            for (int i = 0; i < j; ++i) {  // earlier rotations
+                const double a = h[i], b = h[i + 1];
+                h[i] = cs[i] * a + sn[i] * b;
+                h[i + 1] = -sn[i] * a + cs[i] * b;
+            }
+            const double den = hypot(h[j], h[j + 1]);
+            cs[j] = den > 0.0 ? h[j] / den : 1.0;
+            sn[j] = den > 0.0 ? h[j + 1] / den : 0.0;
+            h[j] = den;
+            h[j + 1] = 0.0;
+            g[j + 1] = -sn[j] * g[j];
+            g[j] = cs[j] * g[j];
+            ++total;
+            kk = j + 1;
+            if (fabs(g[j + 1]) <= target * beta0 || hn == 0.0) {
+                conv = true;
+                break;
+            }
+        }
+        // y = R^-1 g, d += M^-1 (V y)
+        for (int i = kk - 1; i >= 0; --i) {
+            double t = g[i];
+            for (int q = i + 1; q < kk; ++q) t -= H[(size_t)q * (m + 1) + i] * y[q];
+            const double rii = H[(size_t)i * (m + 1) + i];
+            if (!(fabs(rii) > 0.0)) {
+                *done = total;
+                return MPET_ERR_BREAKDOWN;
+            }
+            y[i] = t / rii;
+        }
+        MPET_CUDA(cudaMemcpyAsync(c->gm_h, y.data(), sizeof(double) * kk, cudaMemcpyHostToDevice, c->stream));
+        MPET_CUDA(cudaMemsetAsync(w, 0, sizeof(T) * n, c->stream));
+        k_mupdate<T><<<G, 256, 0, c->stream>>>(n, kk, V, n, c->gm_h, 1.0, w);
+        MPET_CHECK_LAUNCH();
+        precond<T>(c, w, z);
+        k_gm_add<T><<<G, 256, 0, c->stream>>>(n, z, d);
+        MPET_CHECK_LAUNCH();
+        MPET_CUDA(cudaStreamSynchronize(c->stream));  // y is read from pageable host memory
+        if (conv || total >= maxit) {
+            *done = total;
+            return conv ? MPET_OK : MPET_ERR_MAXIT;
+        }
+        // restart from r = rhs - A d
+        launch_spmv<T, 1>(c, c->A, vals<T>(c->A), d, EpiStore<T, 1>{w});
+        c->n_spmv++;
+        k_gm_sub<T><<<G, 256, 0, c->stream>>>(n, rhs, w, r);
+        MPET_CHECK_LAUNCH();
+        gm_dots<T>(c, r, 1, r);
+        beta = sqrt(fmax(c->gm_h_host[0], 0.0));
+        if (beta <= target * beta0) {
+            *done = total;
+            return MPET_OK;
+        }
+    }
+}
+
+// FP64 refinement around GMRES in precision T (the MINRES loop of solve_impl with the
+// 2-norm of D^-1 r as the convergence measure)
+template <typename T>
+static int solve_gmres(mpet_ctx* c, const double* b, double* x, mpet_stats* st, bool homogeneous) {
+    const int64_t n = c->N;
+    const int G = grid_for(n, 256);
+    if (homogeneous) launch_zero_bc_rows(c, x);
+    else launch_set_bc_in_x(c, x);
+    double eta0 = -1.0, relres = 1.0, relres_true = 0.0;
+    int iters = 0, outer = 0, status = MPET_OK;
+    const bool fp64 = sizeof(T) == 8;
+    const int max_outer = c->prm.max_outer > 0 ? c->prm.max_outer : 20;
+    const int maxit = c->prm.maxit > 0 ? c->prm.maxit : 5000;
+    for (outer = 0; outer < max_outer; ++outer) {
+        launch_spmv<double, 1>(c, c->A, c->A.v64, x, EpiResid64{c->orr, b, c->dinv});
+        c->n_spmv++;
+        k_outer_norms<<<1, 256, 0, c->stream>>>(c->sc, c->partials);
+        MPET_CHECK_LAUNCH();
+        MPET_CUDA(cudaMemcpyAsync(c->sc_host, c->sc, sizeof(MinresScalars), cudaMemcpyDeviceToHost, c->stream));
+        MPET_CUDA(cudaStreamSynchronize(c->stream));
+        const MinresScalars h = *c->sc_host;
+        const double eta = sqrt(h.nr2 > 0 ? h.nr2 : 0.0);
+        relres_true = h.nb2 > 0 ? sqrt(h.nr2 / h.nb2) : 0.0;
+        if (eta0 < 0) eta0 = eta;
+        relres = eta0 > 0 ? eta / eta0 : 0.0;
+        if (!(eta == eta)) {
+            status = MPET_ERR_BREAKDOWN;
+            break;
+        }
+        if (eta == 0.0 || eta <= c->prm.rtol * eta0) break;
+        if (iters >= maxit) {
+            status = MPET_ERR_MAXIT;
+            break;
+        }
+        double target = c->prm.rtol * eta0 / eta;
+        if (fp64) {
+            if (target < 1e-15) target = 1e-15;
+        } else if (target < c->prm.inner_rtol) {
+            target = c->prm.inner_rtol;
+        }
+        T* rhs = (T*)c->kr[0];
+        k_scale_to<T><<<G, 256, 0, c->stream>>>(n, c->orr, rhs, c->sc);
+        MPET_CHECK_LAUNCH();
+        int done = 0;
+        MPET_CUDA(cudaEventRecord(c->ev_in0, c->stream));
+        const int s2 = gmres_run<T>(c, rhs, (T*)c->kd, target, maxit - iters, &done);
+        MPET_CUDA(cudaEventRecord(c->ev_in1, c->stream));
+        MPET_CUDA(cudaEventSynchronize(c->ev_in1));
+        float ims = 0.f;
+        MPET_CUDA(cudaEventElapsedTime(&ims, c->ev_in0, c->ev_in1));
+        c->t_inner_ms += ims;
+        c->n_inner_its += done;
+        iters += done;
+        k_add_scaled<T><<<G, 256, 0, c->stream>>>(n, x, (const T*)c->kd, c->sc);
+        MPET_CHECK_LAUNCH();
+        if (s2 == MPET_ERR_BREAKDOWN) {
+            status = s2;
+            break;
+        }
+    }
+    if (outer >= max_outer && status == MPET_OK) status = MPET_ERR_MAXIT;
+    int derr = 0;
+    MPET_CUDA(cudaMemcpyAsync(&derr, c->dev_err, sizeof(int), cudaMemcpyDeviceToHost, c->stream));
+    MPET_CUDA(cudaStreamSynchronize(c->stream));
+    if (derr) {
+        MPET_CUDA(cudaMemsetAsync(c->dev_err, 0, sizeof(int), c->stream));
+        status = MPET_ERR_TIMEOUT;
+    }
+    if (st) {
+        st->iterations = iters;
+        st->outer = outer + 1;
+        st->status = status;
+        st->relres = relres;
+        st->relres_true = relres_true;
+    }
+    return status;
+}
+
 int solve_system(mpet_ctx* c, const double* b, double* x, mpet_stats* st, bool homogeneous) {
     const bool mixed = c->prm.precision == MPET_PRECISION_MIXED;
     MPET_CUDA(cudaEventRecord(c->ev_sv0, c->stream));
     int s;
-    if (c->ninst > 0)
+    if (c->gmres && (c->ninst > 0 || c->nrigid > 0))
+        fail(MPET_ERR_INVALID, "GMRES (non-symmetric S) is built for single instances without rigid modes");
+    if (c->gmres)
+        s = mixed ? solve_gmres<float>(c, b, x, st, homogeneous) : solve_gmres<double>(c, b, x, st, homogeneous);
+    else if (c->ninst > 0)
         s = mixed ? solve_batch<float>(c, b, x, st, homogeneous) : solve_batch<double>(c, b, x, st, homogeneous);
     else
         s = mixed ? solve_impl<float>(c, b, x, st, homogeneous) : solve_impl<double>(c, b, x, st, homogeneous);

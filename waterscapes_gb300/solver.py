@@ -85,9 +85,6 @@ class MPETSolver:
             raise NotImplementedError("constant-pressure nullspace multipliers are not built on the GPU")
         pp = problem.params
         self.J = int(pp["J"])
-        S = np.asarray([[float(v) for v in row] for row in pp["S"]], dtype=np.float64).reshape(self.J, self.J)
-        if not np.allclose(S, S.T, rtol=0, atol=0):
-            raise NotImplementedError("non-symmetric transfer matrix S needs GMRES (not built); MINRES needs S = S^T")
         self._check_facet_data()
         dev = int(self.params["device"])
         self.device = torch.device("cuda", dev)
@@ -151,7 +148,7 @@ class MPETSolver:
                 "precision": "mixed", "rtol": 1e-10, "inner_rtol": 1e-4, "maxit": 20000,
                 "max_outer": 40, "amg_theta": 0.1, "amg_cheb_degree": 4, "amg_coarse_size": 500,
                 "amg_p2_to_p1": True, "prec_u_weight": "mu+lmbda", "prec_network_modes": True,
-                "prec_u_form": "laplacian",
+                "prec_u_form": "laplacian", "krylov": "auto", "gmres_restart": 30,
                 "check_every": 4, "device": 0}
 
     def _make_params(self):
@@ -184,6 +181,9 @@ class MPETSolver:
         prm.prec_u_weight = {"mu+lmbda": mu + lmbda, "mu": mu, "2mu": 2.0 * mu}[w] if isinstance(w, str) else float(w)
         prm.prec_network_modes = 1 if self.params["prec_network_modes"] else 0
         prm.prec_u_form = {"laplacian": 0, "elasticity": 1}[self.params.get("prec_u_form", "laplacian")]
+        # MINRES for a symmetric system; GMRES (auto: when S is not symmetric)
+        prm.krylov = _lib.KRYLOV[self.params.get("krylov", "auto")]
+        prm.gmres_restart = int(self.params.get("gmres_restart", 30))
         if self.problem.u_has_nullspace:
             # mass shift of the displacement preconditioner block at the scale of the
             # lowest elastic mode: (mu + lambda) / diam^2
