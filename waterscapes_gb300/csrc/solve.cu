@@ -2174,10 +2174,12 @@ void batch_relres(mpet_ctx* c, double* out) {
 
 // ---- restarted GMRES (non-symmetric transfer matrix) ---------------------------------------
 //
-// Right-preconditioned GMRES(m) (Saad and Schultz, SIAM J. Sci. Stat. Comput. 7 (1986)
-// 856-869) with the block-diagonal preconditioner, inside the same FP64 refinement loop as
-// MINRES.  Arnoldi by classical Gram-Schmidt applied twice; the small Hessenberg system
-// and its Givens rotations live on the host.  Every reduction has a fixed order.
+// Left-preconditioned GMRES(m) (Saad and Schultz, SIAM J. Sci. Stat. Comput. 7 (1986)
+// 856-869) with the block-diagonal preconditioner M, inside the same FP64 refinement loop
+// as MINRES: it minimises ||M^-1 (rhs - A d)||_2, a norm that weighs the displacement and
+// pressure rows alike (the plain 2-norm is dominated by the displacement rows).  Arnoldi
+// by classical Gram-Schmidt applied twice; the small Hessenberg system and its Givens
+// rotations live on the host.  Every reduction has a fixed order.
 
 // h[k] = V_k . w for k < m (V_k at V + k * ld); partials[k * NB_RED + block]
 template <typename T>
@@ -2248,7 +2250,7 @@ static void gm_dots(mpet_ctx* c, const T* V, int k, const T* w) {
     MPET_CUDA(cudaStreamSynchronize(c->stream));
 }
 
-// d = GMRES(A, rhs) from d = 0 to ||rhs - A d||_2 <= target ||rhs||_2; returns the status
+// d = GMRES(M^-1 A, M^-1 rhs) from d = 0 until ||M^-1 (rhs - A d)||_2 <= target ||M^-1 rhs||_2
 template <typename T>
 static int gmres_run(mpet_ctx* c, const T* rhs, T* d, double target, int maxit, int* done) {
     const int64_t n = c->N;
@@ -2261,7 +2263,7 @@ static int gmres_run(mpet_ctx* c, const T* rhs, T* d, double target, int maxit, 
     T* w = (T*)c->gm_w;
     T* r = (T*)c->gm_r;
     MPET_CUDA(cudaMemsetAsync(d, 0, sizeof(T) * n, c->stream));
-    MPET_CUDA(cudaMemcpyAsync(r, rhs, sizeof(T) * n, cudaMemcpyDeviceToDevice, c->stream));
+    precond<T>(c, rhs, r);
     gm_dots<T>(c, r, 1, r);
     const double beta0 = sqrt(fmax(c->gm_h_host[0], 0.0));
     double beta = beta0;
@@ -2278,9 +2280,9 @@ static int gmres_run(mpet_ctx* c, const T* rhs, T* d, double target, int maxit, 
         bool conv = false;
         for (int j = 0; j < m && total < maxit; ++j) {
             T* vj = V + (int64_t)j * n;
-            precond<T>(c, vj, z);
-            launch_spmv<T, 1>(c, c->A, vals<T>(c->A), z, EpiStore<T, 1>{w});
+            launch_spmv<T, 1>(c, c->A, vals<T>(c->A), vj, EpiStore<T, 1>{z});
             c->n_spmv++;
+            precond<T>(c, z, w);
             double* h = &H[(size_t)j * (m + 1)];  // column j, rows 0..j+1
             for (int i = 0; i <= j + 1; ++i) h[i] = 0.0;
             for (int pass = 0; pass < 2; ++pass) {
@@ -2315,7 +2317,7 @@ static int gmres_run(mpet_ctx* c, const T* rhs, T* d, double target, int maxit, 
                 break;
             }
         }
-        // y = R^-1 g, d += M^-1 (V y)
+        // y = R^-1 g, d += V y
         for (int i = kk - 1; i >= 0; --i) {
             double t = g[i];
             for (int q = i + 1; q < kk; ++q) t -= H[(size_t)q * (m + 1) + i] * y[q];
@@ -2327,22 +2329,19 @@ static int gmres_run(mpet_ctx* c, const T* rhs, T* d, double target, int maxit, 
             y[i] = t / rii;
         }
         MPET_CUDA(cudaMemcpyAsync(c->gm_h, y.data(), sizeof(double) * kk, cudaMemcpyHostToDevice, c->stream));
-        MPET_CUDA(cudaMemsetAsync(w, 0, sizeof(T) * n, c->stream));
-        k_mupdate<T><<<G, 256, 0, c->stream>>>(n, kk, V, n, c->gm_h, 1.0, w);
-        MPET_CHECK_LAUNCH();
-        precond<T>(c, w, z);
-        k_gm_add<T><<<G, 256, 0, c->stream>>>(n, z, d);
+        k_mupdate<T><<<G, 256, 0, c->stream>>>(n, kk, V, n, c->gm_h, 1.0, d);
         MPET_CHECK_LAUNCH();
         MPET_CUDA(cudaStreamSynchronize(c->stream));  // y is read from pageable host memory
         if (conv || total >= maxit) {
             *done = total;
             return conv ? MPET_OK : MPET_ERR_MAXIT;
         }
-        // restart from r = rhs - A d
+        // restart from r = M^-1 (rhs - A d)
         launch_spmv<T, 1>(c, c->A, vals<T>(c->A), d, EpiStore<T, 1>{w});
         c->n_spmv++;
-        k_gm_sub<T><<<G, 256, 0, c->stream>>>(n, rhs, w, r);
+        k_gm_sub<T><<<G, 256, 0, c->stream>>>(n, rhs, w, z);
         MPET_CHECK_LAUNCH();
+        precond<T>(c, z, r);
         gm_dots<T>(c, r, 1, r);
         beta = sqrt(fmax(c->gm_h_host[0], 0.0));
         if (beta <= target * beta0) {
@@ -2352,12 +2351,16 @@ static int gmres_run(mpet_ctx* c, const T* rhs, T* d, double target, int maxit, 
     }
 }
 
-// FP64 refinement around GMRES in precision T (the MINRES loop of solve_impl with the
-// 2-norm of D^-1 r as the convergence measure)
+// FP64 refinement around GMRES in precision T (the MINRES loop of solve_impl, with the
+// same preconditioned residual norm as the convergence measure)
 template <typename T>
 static int solve_gmres(mpet_ctx* c, const double* b, double* x, mpet_stats* st, bool homogeneous) {
     const int64_t n = c->N;
     const int G = grid_for(n, 256);
+    {
+        int m = c->prm.gmres_restart > 0 ? c->prm.gmres_restart : 30;
+        gm_alloc(c, m > 64 ? 64 : m);  // the reduction buffers are used before the first cycle
+    }
     if (homogeneous) launch_zero_bc_rows(c, x);
     else launch_set_bc_in_x(c, x);
     double eta0 = -1.0, relres = 1.0, relres_true = 0.0;
@@ -2373,8 +2376,15 @@ static int solve_gmres(mpet_ctx* c, const double* b, double* x, mpet_stats* st, 
         MPET_CUDA(cudaMemcpyAsync(c->sc_host, c->sc, sizeof(MinresScalars), cudaMemcpyDeviceToHost, c->stream));
         MPET_CUDA(cudaStreamSynchronize(c->stream));
         const MinresScalars h = *c->sc_host;
-        const double eta = sqrt(h.nr2 > 0 ? h.nr2 : 0.0);
+        const double nr = sqrt(h.nr2 > 0 ? h.nr2 : 0.0);
         relres_true = h.nb2 > 0 ? sqrt(h.nr2 / h.nb2) : 0.0;
+        // preconditioned norm (r^T M^-1 r)^1/2 of the residual, as MINRES measures it
+        T* rhs = (T*)c->kr[0];
+        k_scale_to<T><<<G, 256, 0, c->stream>>>(n, c->orr, rhs, c->sc);
+        MPET_CHECK_LAUNCH();
+        precond<T>(c, rhs, (T*)c->kr[2]);
+        gm_dots<T>(c, rhs, 1, (const T*)c->kr[2]);
+        const double eta = nr * sqrt(fmax(c->gm_h_host[0], 0.0));
         if (eta0 < 0) eta0 = eta;
         relres = eta0 > 0 ? eta / eta0 : 0.0;
         if (!(eta == eta)) {
@@ -2392,9 +2402,6 @@ static int solve_gmres(mpet_ctx* c, const double* b, double* x, mpet_stats* st, 
         } else if (target < c->prm.inner_rtol) {
             target = c->prm.inner_rtol;
         }
-        T* rhs = (T*)c->kr[0];
-        k_scale_to<T><<<G, 256, 0, c->stream>>>(n, c->orr, rhs, c->sc);
-        MPET_CHECK_LAUNCH();
         int done = 0;
         MPET_CUDA(cudaEventRecord(c->ev_in0, c->stream));
         const int s2 = gmres_run<T>(c, rhs, (T*)c->kd, target, maxit - iters, &done);
