@@ -203,6 +203,16 @@ int mpet_set_cell_permeability(mpet_ctx* ctx, const double* K_cells);
 int mpet_set_rigid_modes(mpet_ctx* ctx, int32_t nz, const double* Z);
 int mpet_get_rigid_multipliers(mpet_ctx* ctx, double* r_host);
 
+/* Constant-pressure constraints (the reference's p_has_nullspace,
+ * src/mpet/mpet/mpetsolver.py:120-124, 209-215): for each listed network
+ * (without Dirichlet DOFs) the constraint int p_a = 0 with a Lagrange
+ * multiplier p_null (an R-space unknown in the reference), solved by the
+ * Schur complement of the multipliers (nq extra solves after each assembly).
+ * The preconditioner block of such a network gets + dt theta K_a / diam^2 (p, w).
+ * mpet_get_pressure_multipliers writes the nq multipliers of the last solve. */
+int mpet_set_pressure_constraints(mpet_ctx* ctx, int32_t nq, const int32_t* networks);
+int mpet_get_pressure_multipliers(mpet_ctx* ctx, double* lambda_host);
+
 /* Per-cell storage coefficients c_a (device array J x nc) and transfer
  * coefficients S_ab (J x J x nc, S_cells[(a J + b) nc + cell], symmetric in
  * a, b per cell for MINRES); either may be NULL (= the constants of

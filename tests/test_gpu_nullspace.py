@@ -154,3 +154,64 @@ def test_bordered_system_against_oracle(dim, precision):
     assert np.allclose(r, r_ref, rtol=1e-7, atol=1e-9 * np.abs(r_ref).max())
     # displacement L2-orthogonal to the rigid motions
     assert np.abs(B[:, :om.dm.Nu] @ x[:om.dm.Nu]).max() <= 1e-10 * np.linalg.norm(x[:om.dm.Nu])
+
+
+@pytest.mark.parametrize("precision", ["fp64", "mixed"])
+def test_donut_with_pressure_nullspaces_against_oracle(precision):
+    """The second case of src/mpet/test/test_donut.py:73-131 (J = 2, c = 0, alpha = 1,
+    K = (1e-2, 1e-1), S = 0; traction t n everywhere, u_has_nullspace; both pressures
+    only determined up to constants, p_has_nullspace = (True, True); network 0 marked
+    Neumann, network 1 unmarked): one step equals the oracle's LU solve of the system
+    bordered by the rigid motions and the two constant-pressure constraints, the
+    pressures have zero mean, and the multipliers agree; then the reference's time loop
+    (dt = 0.1, T = 0.2) runs through."""
+    from waterscapes_gb300 import CompiledSubDomain, Constant, Expression, MPETProblem, MPETSolver
+    from waterscapes_gb300.mesh import AnnulusMesh
+    from waterscapes_gb300.nullspace import rigid_motions
+    mesh = AnnulusMesh(1.0, 2.0, 4, 24)
+    params = dict(J=2, c=(0.0, 0.0), alpha=(1.0, 1.0), K=(1e-2, 1e-1), S=((0.0, 0.0), (0.0, 0.0)), E=500.0,
+                  nu=0.35)
+    problem = MPETProblem(mesh, Constant(0.0), params=params)
+    problem.s = Expression(lambda x, t, n: float(t) * n[:, :2])
+    problem.u_has_nullspace = True
+    problem.p_has_nullspace = (True, True)
+    on_boundary = CompiledSubDomain.on_boundary()
+    on_boundary.mark(problem.momentum_boundary_markers, 1)
+    on_boundary.mark(problem.continuity_boundary_markers[0], 1)
+    dt, t0 = 0.1, 0.1
+    solver = MPETSolver(problem, dict(dt=dt, theta=1.0, T=0.2, precision=precision, rtol=1e-12))
+    assert solver.nq == 2 and solver.nrigid == 3
+    om = make_oracle(problem, 1.0)
+    data = {"s": lambda x, t, n: t * n}
+    rng = np.random.default_rng(9)
+    up_prev = rng.standard_normal(om.dm.N) * 1e-2
+    _, Abc, bbc, _, _ = om.step(up_prev, t0, dt, data, return_system=True)
+    Nu, nv, N = om.dm.Nu, om.dm.nv, om.dm.N
+    Z = rigid_motions(mesh, om.dm.node_x).reshape(-1, Nu)
+    Mu = _mass(om, "u")
+    Mp = _mass(om, "p")
+    load = np.asarray(Mp.sum(axis=1)).ravel()                 # int phi_v
+    B = np.zeros((Z.shape[0] + 2, N))
+    B[:Z.shape[0], :Nu] = (Mu @ Z.T).T
+    for a in range(2):
+        B[Z.shape[0] + a, Nu + a * nv: Nu + (a + 1) * nv] = load
+    K = sp.bmat([[Abc, sp.csr_matrix(B).T], [sp.csr_matrix(B), None]]).tocsc()
+    sol = spla.spsolve(K, np.concatenate([bbc, np.zeros(B.shape[0])]))
+    x_ref, lam_ref = sol[:N], sol[N:]
+    solver.up_.assign(torch.tensor(up_prev))
+    problem.time.assign(t0)
+    st = solver.step(dt)
+    assert st.status == 0
+    x = solver.up.vector().cpu().numpy()
+    assert np.linalg.norm(x - x_ref) <= 1e-8 * np.linalg.norm(x_ref)
+    assert np.abs(B[Z.shape[0]:] @ x).max() <= 1e-10 * np.abs(load).sum() * np.abs(x[Nu:]).max()
+    parts = solver.up.split()
+    assert len(parts) == 1 + 2 + 1 + 2
+    r, q0, q1 = (v.cpu().numpy() for v in parts[3:])
+    assert np.allclose(r, lam_ref[:3], rtol=1e-6, atol=1e-8 * np.abs(lam_ref).max())
+    assert np.allclose(np.concatenate([q0, q1]), lam_ref[3:], rtol=1e-6, atol=1e-8 * np.abs(lam_ref).max())
+    # the reference's loop: t = 0.1, 0.2
+    problem.time.assign(0.0)
+    solver.up_.vector().zero_()
+    ts = [t for _, t in solver.solve()]
+    assert len(ts) == 2 and abs(ts[-1] - 0.2) < 1e-12

@@ -109,6 +109,8 @@ SIGNATURES = {
     "mpet_set_cell_coefficients": [_P, _P, _P],
     "mpet_set_rigid_modes": [_P, _I32, _P],
     "mpet_get_rigid_multipliers": [_P, _P],
+    "mpet_set_pressure_constraints": [_P, _I32, _P],
+    "mpet_get_pressure_multipliers": [_P, _P],
     "mpet_set_batch": [_P, _I32, _P],
     "mpet_get_batch_relres": [_P, _P],
     "mpet_get_facet_data": [_P, _P, _P],

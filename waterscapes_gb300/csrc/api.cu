@@ -267,6 +267,7 @@ int mpet_assemble(mpet_ctx* c, double dt, int32_t apply_bc) {
     refresh_system_copies(c);
     MPET_CUDA(cudaStreamSynchronize(c->stream));
     c->assembled = true;
+    c->q_dirty = true;
     c->asm_dt = dt;
     API_END(c)
 }
@@ -383,6 +384,67 @@ int mpet_get_rigid_multipliers(mpet_ctx* c, double* r) {
     API_BEGIN(c)
     require(r, MPET_ERR_INVALID, "NULL argument");
     for (int i = 0; i < c->nrigid; ++i) r[i] = c->rigid_r[i];
+    API_END(c)
+}
+
+int mpet_set_pressure_constraints(mpet_ctx* c, int32_t nq, const int32_t* networks) {
+    API_BEGIN(c)
+    require(c->setup_done, MPET_ERR_STATE, "mpet_setup must come first");
+    require(c->ninst == 0 && !c->gmres, MPET_ERR_INVALID,
+            "pressure constraints are built for single instances solved by MINRES");
+    require(nq >= 0 && nq <= c->J && (nq == 0 || networks), MPET_ERR_INVALID, "nq must be in 0..J");
+    for (int k = 0; k < nq; ++k) {
+        const int a = networks[k];
+        require(a >= 0 && a < c->J, MPET_ERR_INVALID, "network index out of range");
+        for (int q = 0; q < k; ++q) require(networks[q] != a, MPET_ERR_INVALID, "network listed twice");
+        require(c->bc_off[2 + a] == c->bc_off[1 + a], MPET_ERR_INVALID,
+                "a constant-pressure constraint needs a network without Dirichlet DOFs");
+    }
+    // P1 load vector int phi_v = sum over the vertex's cells |T| / (dim + 1), and the diameter
+    const int nvc = c->dim + 1;
+    std::vector<double> geo((size_t)c->nc * 16), xyz((size_t)c->nv * 3);
+    std::vector<int32_t> cells((size_t)c->nc * nvc);
+    MPET_CUDA(cudaMemcpyAsync(geo.data(), c->geo, sizeof(double) * geo.size(), cudaMemcpyDeviceToHost, c->stream));
+    MPET_CUDA(cudaMemcpyAsync(xyz.data(), c->x, sizeof(double) * xyz.size(), cudaMemcpyDeviceToHost, c->stream));
+    MPET_CUDA(cudaMemcpyAsync(cells.data(), c->cells, sizeof(int32_t) * cells.size(), cudaMemcpyDeviceToHost,
+                              c->stream));
+    MPET_CUDA(cudaStreamSynchronize(c->stream));
+    std::vector<double> load(c->nv, 0.0);
+    for (int64_t e = 0; e < c->nc; ++e)
+        for (int r = 0; r < nvc; ++r) load[cells[(size_t)e * nvc + r]] += geo[16 * e + 12] / nvc;
+    double lo[3] = {1e300, 1e300, 1e300}, hi[3] = {-1e300, -1e300, -1e300};
+    for (int64_t v = 0; v < c->nv; ++v)
+        for (int k = 0; k < 3; ++k) {
+            lo[k] = std::min(lo[k], xyz[3 * v + k]);
+            hi[k] = std::max(hi[k], xyz[3 * v + k]);
+        }
+    double diam2 = 0.0;
+    for (int k = 0; k < 3; ++k) diam2 += (hi[k] - lo[k]) * (hi[k] - lo[k]);
+    if (!c->q_load) c->q_load = c->pool.alloc<double>(c->nv);
+    MPET_CUDA(cudaMemcpyAsync(c->q_load, load.data(), sizeof(double) * c->nv, cudaMemcpyHostToDevice, c->stream));
+    if (nq > 0 && (!c->q_W || nq > c->nq)) {
+        c->q_W = c->pool.alloc<double>((int64_t)nq * c->N);
+        c->q_N = c->pool.alloc<double>((int64_t)nq * c->N);
+    }
+    if (nq > 0 && !c->rigid_b) c->rigid_b = c->pool.alloc<double>(c->N);  // projected right-hand side
+    c->q_nk = 0;
+    for (int a = 0; a < MPET_MAX_NETWORKS; ++a) c->prec_p_shift[a] = 0.0;
+    for (int k = 0; k < nq; ++k) {
+        c->q_net[k] = networks[k];
+        c->prec_p_shift[networks[k]] = diam2 > 0.0 ? c->prm.K[networks[k]] / diam2 : 0.0;
+        c->q_lambda[k] = 0.0;
+    }
+    MPET_CUDA(cudaStreamSynchronize(c->stream));
+    c->nq = nq;
+    c->q_dirty = true;
+    c->precond_ready = false;
+    API_END(c)
+}
+
+int mpet_get_pressure_multipliers(mpet_ctx* c, double* lambda_host) {
+    API_BEGIN(c)
+    require(lambda_host, MPET_ERR_INVALID, "NULL argument");
+    for (int k = 0; k < c->nq; ++k) lambda_host[k] = c->q_lambda[k];
     API_END(c)
 }
 

@@ -670,6 +670,8 @@ static MatCoef make_coef(const mpet_ctx* c, double dt) {
         P.prec_extra[a] = !tp ? 0.0
                         : a == 0 ? (c->prm.prec_p0_weight > 0.0 ? c->prm.prec_p0_weight : 1.0)
                                  : c->prm.alpha[a] * c->prm.alpha[a] * P.rank_inv;
+        // networks with a constant-pressure constraint (no Dirichlet rows): + dt theta K / diam^2
+        P.prec_extra[a] += P.dt_theta * c->prec_p_shift[a];
     }
     P.coef_const = (!P.Kc && !P.cc && !P.Sc) ? 1 : 0;
     for (int a = 0; a < c->J; ++a) {

@@ -316,6 +316,18 @@ struct mpet_ctx {
     double* elem_buf = nullptr;   // staged per-cell element data of the assembly, or null
     bool u_elast = false;         // displacement preconditioner block: elasticity AMG (else Laplacian)
     bool gmres = false;           // solves by restarted GMRES (non-symmetric system)
+    // constant-pressure constraints (int p_k = 0, multiplier p_null_k): networks, the P1
+    // load vector (int phi_v), W_k = A^-1 B_k^T (nq x N), the inverse of B W, multipliers
+    int nq = 0;
+    int q_net[MPET_MAX_NETWORKS] = {0};
+    double* q_load = nullptr;
+    double* q_W = nullptr;
+    double q_Sinv[4 * MPET_MAX_NETWORKS * MPET_MAX_NETWORKS] = {0};  // inverse of the (nq + nk)^2 system
+    double* q_N = nullptr;        // nk Euclidean-orthonormal kernel vectors of A among the
+    int q_nk = 0;                 //   constant pressures of the constrained networks (N each)
+    double q_lambda[MPET_MAX_NETWORKS] = {0};
+    bool q_dirty = true;
+    double prec_p_shift[MPET_MAX_NETWORKS] = {0};  // + shift (p_a, w_a) in pressure block a
     void* gm_V = nullptr;         // GMRES basis, (restart + 1) x N doubles
     void* gm_z = nullptr;         // N doubles each
     void* gm_w = nullptr;

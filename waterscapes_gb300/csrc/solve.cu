@@ -1547,6 +1547,11 @@ static int minres_run(mpet_ctx* c, double target, int max_iters, int* iters_done
 }
 
 // ---- rigid-motion modes ---------------------------------------------------------------
+__global__ void k_fill64(int64_t n, double* y, double v) {
+    const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    if (i < n) y[i] = v;
+}
+
 __global__ void k_axpy64(int64_t n, double* y, double a, const double* __restrict__ x) {
     const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
     if (i < n) y[i] += a * x[i];
@@ -1570,6 +1575,17 @@ static double dot_host(mpet_ctx* c, const double* a, const double* b, int64_t n)
     return v;
 }
 
+// v -= sum_j (n_j . v) n_j over the pressure kernel vectors of the constrained networks
+static void kernel_project(mpet_ctx* c, double* v) {
+    const int64_t n = c->N;
+    for (int j = 0; j < c->q_nk; ++j) {
+        const double* nj = c->q_N + (int64_t)j * n;
+        const double t = dot_host(c, nj, v, n);
+        k_axpy64<<<grid_for(n, 256), 256, 0, c->stream>>>(n, v, -t, nj);
+    }
+    MPET_CHECK_LAUNCH();
+}
+
 // v_u -= sum_i (P_i . v_u) Q_i over the displacement rows (P, Q: the modes or their duals)
 static void rigid_project(mpet_ctx* c, double* v, const double* P, const double* Q, double* coef_out) {
     const int64_t nu = c->Nu;
@@ -1587,10 +1603,12 @@ static int solve_impl(mpet_ctx* c, const double* b, double* x, mpet_stats* st, b
     const int G = grid_for(n, 256);
     if (homogeneous) launch_zero_bc_rows(c, x);
     else launch_set_bc_in_x(c, x);
-    if (c->nrigid > 0) {
-        // multipliers r_i = Z_i . b_u; solve with b - sum_i r_i M Z_i (consistent)
+    if (c->nrigid > 0 || c->q_nk > 0) {
+        // multipliers r_i = Z_i . b_u; solve with b - sum_i r_i M Z_i (consistent), and without
+        // the components along the pressure kernel vectors
         MPET_CUDA(cudaMemcpyAsync(c->rigid_b, b, sizeof(double) * n, cudaMemcpyDeviceToDevice, c->stream));
-        rigid_project(c, c->rigid_b, c->rigid_Z, c->rigid_MZ, c->rigid_r);
+        if (c->nrigid > 0) rigid_project(c, c->rigid_b, c->rigid_Z, c->rigid_MZ, c->rigid_r);
+        if (c->q_nk > 0) kernel_project(c, c->rigid_b);
         b = c->rigid_b;
     }
     double eta0 = -1.0;
@@ -1605,6 +1623,7 @@ static int solve_impl(mpet_ctx* c, const double* b, double* x, mpet_stats* st, b
         c->n_spmv++;
         k_outer_norms<<<1, 256, 0, c->stream>>>(c->sc, c->partials);
         if (c->nrigid > 0) rigid_project(c, c->orr, c->rigid_Z, c->rigid_MZ, nullptr);  // rounding drift
+        if (c->q_nk > 0) kernel_project(c, c->orr);
         T* rhs = (T*)c->kr[0];
         k_scale_to<T><<<G, 256, 0, c->stream>>>(n, c->orr, rhs, c->sc);
         k_copy2<T><<<G, 256, 0, c->stream>>>(n, rhs, (T*)c->kr[1], (T*)c->kr[1]);
@@ -1656,8 +1675,10 @@ static int solve_impl(mpet_ctx* c, const double* b, double* x, mpet_stats* st, b
             break;
         }
     }
-    // (Z_i, u) = 0: remove the modes from the displacement (M-orthogonally)
+    // (Z_i, u) = 0: remove the modes from the displacement (M-orthogonally), and the kernel
+    // components (the constraints set them afterwards)
     if (c->nrigid > 0) rigid_project(c, x, c->rigid_MZ, c->rigid_Z, nullptr);
+    if (c->q_nk > 0) kernel_project(c, x);
     if (outer >= max_outer && status == MPET_OK) status = MPET_ERR_MAXIT;
     int derr = 0;
     MPET_CUDA(cudaMemcpyAsync(&derr, c->dev_err, sizeof(int), cudaMemcpyDeviceToHost, c->stream));
@@ -2437,18 +2458,158 @@ static int solve_gmres(mpet_ctx* c, const double* b, double* x, mpet_stats* st, 
     return status;
 }
 
+// ---- constant-pressure constraints ---------------------------------------------------------
+//
+// The reference borders the system with one R-space unknown per network whose pressure is
+// only determined up to a constant (mpetsolver.py:120-124, 209-215):
+//   A x + B^T lambda = b,  B x = 0,  B_k = (int phi_v) on the DOFs of network k.
+// Solved by the capacitance (Schur complement) method: W = A^-1 B^T (nq solves, redone
+// after each assembly), x0 = A^-1 b, lambda = (B W)^-1 B x0, x = x0 - W lambda.
+
+static int solve_plain(mpet_ctx* c, const double* b, double* x, mpet_stats* st, bool homogeneous) {
+    const bool mixed = c->prm.precision == MPET_PRECISION_MIXED;
+    if (c->gmres)
+        return mixed ? solve_gmres<float>(c, b, x, st, homogeneous) : solve_gmres<double>(c, b, x, st, homogeneous);
+    if (c->ninst > 0)
+        return mixed ? solve_batch<float>(c, b, x, st, homogeneous) : solve_batch<double>(c, b, x, st, homogeneous);
+    return mixed ? solve_impl<float>(c, b, x, st, homogeneous) : solve_impl<double>(c, b, x, st, homogeneous);
+}
+
+// B_k . x (the load vector against network k's pressures)
+static double q_dot(mpet_ctx* c, int k, const double* x) {
+    return dot_host(c, c->q_load, x + c->Nu + (int64_t)c->q_net[k] * c->nv, c->nv);
+}
+
+// Gauss-Jordan inverse of a small dense matrix (row-major m x m); false when singular
+static bool small_inverse(std::vector<double> S, int m, double* inv) {
+    std::vector<double> I((size_t)m * m, 0.0);
+    for (int k = 0; k < m; ++k) I[k * m + k] = 1.0;
+    for (int col = 0; col < m; ++col) {
+        int piv = col;
+        for (int r = col + 1; r < m; ++r)
+            if (fabs(S[r * m + col]) > fabs(S[piv * m + col])) piv = r;
+        if (!(fabs(S[piv * m + col]) > 0.0)) return false;
+        for (int q = 0; q < m; ++q) {
+            std::swap(S[col * m + q], S[piv * m + q]);
+            std::swap(I[col * m + q], I[piv * m + q]);
+        }
+        const double d = S[col * m + col];
+        for (int q = 0; q < m; ++q) {
+            S[col * m + q] /= d;
+            I[col * m + q] /= d;
+        }
+        for (int r = 0; r < m; ++r)
+            if (r != col) {
+                const double f = S[r * m + col];
+                for (int q = 0; q < m; ++q) {
+                    S[r * m + q] -= f * S[col * m + q];
+                    I[r * m + q] -= f * I[col * m + q];
+                }
+            }
+    }
+    for (int q = 0; q < m * m; ++q) inv[q] = I[q];
+    return true;
+}
+
+// With the kernel vectors n_j of A among the constrained constant pressures (A n_j = 0,
+// e.g. p_1 - p_2 for equal alpha, c = S = 0) and A^+ the solve on their complement:
+//   x = A^+ b - W lambda + N a,  W = A^+ B^T,
+//   N^T (b - B^T lambda) = 0  (consistency),  B x = 0  (constraints).
+static int solve_constrained(mpet_ctx* c, const double* b, double* x, mpet_stats* st, bool homogeneous) {
+    const int64_t n = c->N;
+    const int nq = c->nq;
+    int iters = 0;
+    if (c->q_dirty) {
+        // kernel of A among the constant pressures of the constrained networks
+        TmpBuf e(sizeof(double) * n), ae(sizeof(double) * n * (nq > 0 ? nq : 1));
+        for (int k = 0; k < nq; ++k) {
+            MPET_CUDA(cudaMemsetAsync(e.p, 0, sizeof(double) * n, c->stream));
+            k_fill64<<<grid_for(c->nv, 256), 256, 0, c->stream>>>(c->nv, e.as<double>() + c->Nu +
+                                                                   (int64_t)c->q_net[k] * c->nv, 1.0);
+            MPET_CHECK_LAUNCH();
+            launch_spmv<double, 1>(c, c->A, c->A.v64, e.as<double>(), EpiStore<double, 1>{ae.as<double>() + (int64_t)k * n});
+        }
+        std::vector<double> Gm((size_t)nq * nq), Q((size_t)nq * nq), lam(nq);
+        for (int k = 0; k < nq; ++k)
+            for (int l = 0; l <= k; ++l)
+                Gm[k * nq + l] = Gm[l * nq + k] =
+                    dot_host(c, ae.as<double>() + (int64_t)k * n, ae.as<double>() + (int64_t)l * n, n);
+        sym_eig(nq, Gm.data(), Q.data(), lam.data());
+        double gmax = 0.0;
+        for (int k = 0; k < nq; ++k) gmax = fmax(gmax, fabs(lam[k]));
+        c->q_nk = 0;
+        for (int j = 0; j < nq; ++j) {
+            if (!(fabs(lam[j]) <= 1e-12 * gmax)) continue;
+            double nrm = 0.0;
+            for (int k = 0; k < nq; ++k) nrm += Q[k * nq + j] * Q[k * nq + j];
+            nrm = sqrt(nrm * (double)c->nv);
+            double* nj = c->q_N + (int64_t)c->q_nk * n;
+            MPET_CUDA(cudaMemsetAsync(nj, 0, sizeof(double) * n, c->stream));
+            for (int k = 0; k < nq; ++k)
+                k_fill64<<<grid_for(c->nv, 256), 256, 0, c->stream>>>(c->nv, nj + c->Nu + (int64_t)c->q_net[k] * c->nv,
+                                                                       Q[k * nq + j] / nrm);
+            MPET_CHECK_LAUNCH();
+            ++c->q_nk;
+        }
+        MPET_CUDA(cudaStreamSynchronize(c->stream));
+        TmpBuf rhs(sizeof(double) * n);
+        for (int k = 0; k < nq; ++k) {
+            double* Wk = c->q_W + (int64_t)k * n;
+            MPET_CUDA(cudaMemsetAsync(rhs.p, 0, sizeof(double) * n, c->stream));
+            MPET_CUDA(cudaMemcpyAsync(rhs.as<double>() + c->Nu + (int64_t)c->q_net[k] * c->nv, c->q_load,
+                                      sizeof(double) * c->nv, cudaMemcpyDeviceToDevice, c->stream));
+            MPET_CUDA(cudaMemsetAsync(Wk, 0, sizeof(double) * n, c->stream));
+            mpet_stats s1{};
+            const int s = solve_plain(c, rhs.as<double>(), Wk, &s1, true);
+            iters += s1.iterations;
+            if (s != MPET_OK) {
+                if (st) *st = s1;
+                return s;
+            }
+        }
+        // [ -N^T B^T    0  ] [lambda]   [ -N^T b ]
+        // [ -B W      B N ] [  a   ] = [ -B x0  ]
+        const int nk = c->q_nk, m = nq + nk;
+        std::vector<double> Mt((size_t)m * m, 0.0);
+        for (int j = 0; j < nk; ++j)
+            for (int k = 0; k < nq; ++k) Mt[j * m + k] = -q_dot(c, k, c->q_N + (int64_t)j * n);
+        for (int k = 0; k < nq; ++k) {
+            for (int l = 0; l < nq; ++l) Mt[(nk + k) * m + l] = -q_dot(c, k, c->q_W + (int64_t)l * n);
+            for (int j = 0; j < nk; ++j) Mt[(nk + k) * m + nq + j] = q_dot(c, k, c->q_N + (int64_t)j * n);
+        }
+        if (!small_inverse(Mt, m, c->q_Sinv)) fail(MPET_ERR_BREAKDOWN, "singular pressure-constraint system");
+        c->q_dirty = false;
+    }
+    const int nk = c->q_nk, m = nq + nk;
+    std::vector<double> g(m);
+    for (int j = 0; j < nk; ++j) g[j] = -dot_host(c, c->q_N + (int64_t)j * n, b, n);
+    const int s = solve_plain(c, b, x, st, homogeneous);
+    if (st) st->iterations += iters;
+    if (s != MPET_OK) return s;
+    for (int k = 0; k < nq; ++k) g[nk + k] = -q_dot(c, k, x);
+    std::vector<double> z(m, 0.0);
+    for (int r = 0; r < m; ++r)
+        for (int q = 0; q < m; ++q) z[r] += c->q_Sinv[r * m + q] * g[q];
+    const int G = grid_for(n, 256);
+    for (int k = 0; k < nq; ++k) {
+        c->q_lambda[k] = z[k];
+        k_axpy64<<<G, 256, 0, c->stream>>>(n, x, -z[k], c->q_W + (int64_t)k * n);
+    }
+    for (int j = 0; j < nk; ++j) k_axpy64<<<G, 256, 0, c->stream>>>(n, x, z[nq + j], c->q_N + (int64_t)j * n);
+    MPET_CHECK_LAUNCH();
+    MPET_CUDA(cudaStreamSynchronize(c->stream));
+    return MPET_OK;
+}
+
 int solve_system(mpet_ctx* c, const double* b, double* x, mpet_stats* st, bool homogeneous) {
     const bool mixed = c->prm.precision == MPET_PRECISION_MIXED;
     MPET_CUDA(cudaEventRecord(c->ev_sv0, c->stream));
     int s;
     if (c->gmres && (c->ninst > 0 || c->nrigid > 0))
         fail(MPET_ERR_INVALID, "GMRES (non-symmetric S) is built for single instances without rigid modes");
-    if (c->gmres)
-        s = mixed ? solve_gmres<float>(c, b, x, st, homogeneous) : solve_gmres<double>(c, b, x, st, homogeneous);
-    else if (c->ninst > 0)
-        s = mixed ? solve_batch<float>(c, b, x, st, homogeneous) : solve_batch<double>(c, b, x, st, homogeneous);
-    else
-        s = mixed ? solve_impl<float>(c, b, x, st, homogeneous) : solve_impl<double>(c, b, x, st, homogeneous);
+    (void)mixed;
+    if (c->nq > 0) s = solve_constrained(c, b, x, st, homogeneous);
+    else s = solve_plain(c, b, x, st, homogeneous);
     MPET_CUDA(cudaEventRecord(c->ev_sv1, c->stream));
     MPET_CUDA(cudaEventSynchronize(c->ev_sv1));
     float ms = 0.f;

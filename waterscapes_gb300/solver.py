@@ -55,6 +55,10 @@ class Function:
         if getattr(s, "nrigid", 0):
             # the rigid-motion multipliers r (the R-space part of the reference's mixed function)
             extra = [s._rigid_r.clone() if deepcopy else s._rigid_r]
+        for k in range(getattr(s, "nq", 0)):
+            # one multiplier per constant-pressure constraint, in network order
+            q = s._p_null[k:k + 1]
+            extra.append(q.clone() if deepcopy else q)
         return tuple([u] + ps + extra)
 
     def assign(self, other):
@@ -81,8 +85,6 @@ class MPETSolver:
         if mesh.gdim not in (2, 3) or mesh.tdim != mesh.gdim:
             raise NotImplementedError("the GPU engine assembles triangle (2D) and tetrahedral (3D) meshes")
         self.dim = mesh.gdim
-        if any(problem.p_has_nullspace):
-            raise NotImplementedError("constant-pressure nullspace multipliers are not built on the GPU")
         pp = problem.params
         self.J = int(pp["J"])
         self._check_facet_data()
@@ -134,6 +136,14 @@ class MPETSolver:
             self._rigid_Z = torch.as_tensor(np.ascontiguousarray(Z.reshape(self.nrigid, -1)), device=self.device)
             self._ctx.call("mpet_set_rigid_modes", self.nrigid, _lib._ptr(self._rigid_Z))
             self._rigid_r = torch.zeros(self.nrigid, dtype=torch.float64, device=self.device)
+        # constant-pressure constraints with multipliers (mpetsolver.py:120-124, 209-215)
+        nets = [a for a, f in enumerate(problem.p_has_nullspace) if f]
+        self.nq = len(nets)
+        self._p_null = None
+        if nets:
+            arr = np.ascontiguousarray(nets, dtype=np.int32)
+            self._ctx.call("mpet_set_pressure_constraints", self.nq, _lib._ptr(arr))
+            self._p_null = torch.zeros(self.nq, dtype=torch.float64, device=self.device)
         self._assembled_dt = None
         self._prec_dt = None
         self._f = None
@@ -395,6 +405,10 @@ class MPETSolver:
             r = np.zeros(self.nrigid)
             self._ctx.call("mpet_get_rigid_multipliers", _lib._ptr(r))
             self._rigid_r.copy_(_torch().as_tensor(r))
+        if self.nq:
+            q = np.zeros(self.nq)
+            self._ctx.call("mpet_get_pressure_multipliers", _lib._ptr(q))
+            self._p_null.copy_(_torch().as_tensor(q))
         return st
 
     def step(self, dt=None, up_=None):
