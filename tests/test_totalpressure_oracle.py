@@ -68,3 +68,25 @@ def test_symmetric_and_same_sparsity_as_mpet_with_one_more_field():
     ref = OracleMPET(om.dm.x, om.dm.cells, om.bfacets, om.bfacet_cells, expand_params(TP_PARAMS), 0.5)
     B = ref.assemble_matrix(0.1).tocsr()
     assert np.array_equal(A.indptr, B.indptr) and np.array_equal(A.indices, B.indices)
+
+
+def test_engine_field_view_matches_oracle_expansion():
+    """The host side of MPETTotalPressureSolver presents p0 as pressure field 0 with the
+    same expanded parameters as the oracle, and reads through to the problem."""
+    from oracle.totalpressure import expand_params as oracle_expand
+    from waterscapes_gb300 import Constant, MPETProblem, UnitSquareMesh
+    from waterscapes_gb300.totalpressure import _FieldView, expand_params
+    params = dict(TP_PARAMS, S=((0.0, 0.7), (0.7, 0.0)))
+    a, b = expand_params(params), oracle_expand(params)
+    for key in ("J", "alpha", "c"):
+        assert tuple(np.atleast_1d(a[key])) == tuple(np.atleast_1d(b[key]))
+    assert np.array_equal(np.asarray(a["S"], dtype=float), np.asarray(b["S"], dtype=float))
+    assert np.array_equal(np.asarray(a["K"], dtype=float), np.asarray(b["K"], dtype=float))
+    problem = MPETProblem(UnitSquareMesh(2), Constant(0.0), params=params)
+    view = _FieldView(problem)
+    assert view.params["J"] == 3 and view.g[0] is None and len(view.continuity_boundary_markers) == 3
+    assert (view.continuity_boundary_markers[0].as_int32() == -1).all()
+    problem.p_bar = ["a", "b"]
+    assert view.p_bar == [None, "a", "b"]
+    view.u_has_nullspace = True
+    assert problem.u_has_nullspace is True

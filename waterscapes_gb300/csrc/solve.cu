@@ -2240,11 +2240,6 @@ __global__ void k_gm_sub(int64_t n, const T* __restrict__ a, const T* __restrict
     const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
     if (i < n) out[i] = a[i] - b[i];
 }
-template <typename T>
-__global__ void k_gm_add(int64_t n, const T* __restrict__ a, T* out) {
-    const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
-    if (i < n) out[i] += a[i];
-}
 
 static void gm_alloc(mpet_ctx* c, int m) {
     if (c->gm_V && c->gm_m >= m) return;
@@ -2602,12 +2597,10 @@ static int solve_constrained(mpet_ctx* c, const double* b, double* x, mpet_stats
 }
 
 int solve_system(mpet_ctx* c, const double* b, double* x, mpet_stats* st, bool homogeneous) {
-    const bool mixed = c->prm.precision == MPET_PRECISION_MIXED;
     MPET_CUDA(cudaEventRecord(c->ev_sv0, c->stream));
     int s;
     if (c->gmres && (c->ninst > 0 || c->nrigid > 0))
         fail(MPET_ERR_INVALID, "GMRES (non-symmetric S) is built for single instances without rigid modes");
-    (void)mixed;
     if (c->nq > 0) s = solve_constrained(c, b, x, st, homogeneous);
     else s = solve_plain(c, b, x, st, homogeneous);
     MPET_CUDA(cudaEventRecord(c->ev_sv1, c->stream));
