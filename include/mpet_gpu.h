@@ -300,14 +300,17 @@ int mpet_apply_preconditioner(mpet_ctx* ctx, int32_t precision, const void* r, v
 int mpet_residual(mpet_ctx* ctx, const double* b, const double* x, double* r, double* norms_host);
 
 /* Same result as mpet_residual for callers that cannot allocate device
- * memory (their allocator already holds the device, or they may not
- * allocate or synchronise after start-up).  No counterpart in the
- * reference: it exists only for such callers.  It allocates nothing: the
- * reduction scratch is a 256 KiB static device array that every GPU loading
- * the library keeps until exit, so the system may have at most 33,554,432
- * rows (larger systems get MPET_ERR_INVALID).  The first call on a device
- * looks up the array's device address and should come before any stream
- * capture; calls that overlap on the GPU share the array and race. */
+ * memory (their allocator already holds the device's free memory, or they
+ * may not allocate after start-up).  No counterpart in the reference: it
+ * exists only for such callers.  It allocates nothing: the reduction scratch
+ * is a 256 KiB static device array that every GPU on which a context was
+ * created keeps until exit, so the system may have at most 33,554,432 rows
+ * (larger systems get MPET_ERR_INVALID).  mpet_ctx_create looks up the
+ * array's device address (and so loads it onto the device); if that failed,
+ * the first call on the device retries and should come before any stream
+ * capture.  The call synchronises the context's stream, since it returns the
+ * norms to the host.  Calls that overlap on the GPU share the array and
+ * race. */
 int mpet_residual_noalloc(mpet_ctx* ctx, const double* b, const double* x, double* r, double* norms_host);
 
 /* y = A x with the assembled values; precision selects FP64 (x, y double)
@@ -338,6 +341,15 @@ int mpet_get_node_block_info(mpet_ctx* ctx, int64_t* blocks, int64_t* stored_val
  * computes the same product (summation order differs).  No reference
  * counterpart (tuning and test hook). */
 int mpet_set_spmv_variant(mpet_ctx* ctx, int32_t variant);
+
+/* Bound (in polls) of the bounded waits of the staged SpMV's tile copies
+ * (default 4,194,304).  A wait that gives up sets the context's device error
+ * flag; the call that launched it then returns MPET_ERR_TIMEOUT and the
+ * context stays usable.  0 makes every tile wait give up at once (the copies
+ * still land: the kernel then waits for them under the default bound before
+ * it exits), which is how the timeout path is tested without a fault.  No
+ * reference counterpart (test hook). */
+int mpet_set_wait_limit(mpet_ctx* ctx, int32_t polls);
 
 /* The same override for every matrix of the AMG hierarchies (operators,
  * prolongations, restrictions): each takes the variant where it can run and

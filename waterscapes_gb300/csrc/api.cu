@@ -32,6 +32,15 @@ static void require(bool cond, int code, const char* msg) {
 
 extern "C" {
 
+static const char* solve_status_message(int s) {
+    switch (s) {
+        case MPET_ERR_MAXIT: return "Krylov iteration limit reached";
+        case MPET_ERR_TIMEOUT: return "a staged SpMV copy did not complete within its wait limit";
+        case MPET_ERR_BREAKDOWN: return "Krylov breakdown (non-finite or indefinite preconditioned residual)";
+        default: return "solve failed";
+    }
+}
+
 int mpet_ctx_create(int device, mpet_ctx** out) {
     if (!out) return MPET_ERR_INVALID;
     *out = nullptr;
@@ -55,6 +64,7 @@ int mpet_ctx_create(int device, mpet_ctx** out) {
     cudaEventCreate(&c->ev_in1);
     cudaEventCreate(&c->ev_sv0);
     cudaEventCreate(&c->ev_sv1);
+    mpet::noalloc_prepare(device);
     *out = c;
     return MPET_OK;
 }
@@ -648,7 +658,7 @@ int mpet_solve(mpet_ctx* c, const double* b, double* x, mpet_stats* st) {
     require(b && x, MPET_ERR_INVALID, "NULL vector");
     int s = solve_system(c, b, x, st);
     if (s != MPET_OK) {
-        c->err = s == MPET_ERR_MAXIT ? "Krylov iteration limit reached" : "Krylov breakdown";
+        c->err = solve_status_message(s);
         return s;
     }
     API_END(c)
@@ -665,7 +675,7 @@ int mpet_step(mpet_ctx* c, double dt, const double* up_prev, double* up, mpet_st
         MPET_CUDA(cudaMemcpyAsync(up, up_prev, sizeof(double) * c->N, cudaMemcpyDeviceToDevice, c->stream));
     int s = solve_system(c, b, up, st);
     if (s != MPET_OK) {
-        c->err = s == MPET_ERR_MAXIT ? "Krylov iteration limit reached" : "Krylov breakdown";
+        c->err = solve_status_message(s);
         return s;
     }
     API_END(c)
@@ -756,6 +766,13 @@ int mpet_set_spmv_variant(mpet_ctx* c, int32_t variant) {
     API_END(c)
 }
 
+int mpet_set_wait_limit(mpet_ctx* c, int32_t polls) {
+    API_BEGIN(c)
+    require(polls >= 0, MPET_ERR_INVALID, "wait limit must be >= 0");
+    c->mbar_spin_limit = polls > 0 ? polls : 0;
+    API_END(c)
+}
+
 int mpet_get_timing(mpet_ctx* c, double* inner_ms, int64_t* inner_iterations, double* solve_ms, int64_t* launches) {
     API_BEGIN(c)
     if (inner_ms) *inner_ms = c->t_inner_ms;
@@ -837,7 +854,7 @@ int mpet_adjoint_step(mpet_ctx* c, double dt, const double* seed, const double* 
     MPET_CUDA(cudaMemsetAsync(lam, 0, sizeof(double) * c->N, c->stream));
     int s = solve_system(c, c->adj_b, lam, st, true);
     if (s != MPET_OK) {
-        c->err = s == MPET_ERR_MAXIT ? "Krylov iteration limit reached" : "Krylov breakdown";
+        c->err = solve_status_message(s);
         return s;
     }
     if (grad_K) launch_adjoint_grad(c, dt, lam, up_prev, up, grad_K);

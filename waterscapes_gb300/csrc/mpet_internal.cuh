@@ -403,6 +403,7 @@ struct mpet_ctx {
 
     // set by a kernel whose bounded wait gave up (read after each solve)
     int* dev_err = nullptr;
+    int mbar_spin_limit = 1 << 22;  // polls of a staged-SpMV tile wait (test hook lowers it)
     double spmv_variant_ms[7] = {0, 0, 0, 0, 0, 0, 0};  // variants 0..5 and 8 (node blocks)
 
     // timing
@@ -480,6 +481,10 @@ int launch_error_indicators(mpet_ctx* c, double dt, const double* up, const doub
                             const double* fp, const double* g, int64_t nfi, const int32_t* ifacets,
                             const int32_t* cell_facets, double* eta_p, double* eta_u, double* eta_udt,
                             double* r4_host);
+
+// noalloc.cu: device address of the static residual scratch, looked up at
+// context creation
+void noalloc_prepare(int device);
 
 // solve.cu
 template <typename T>

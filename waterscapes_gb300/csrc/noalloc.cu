@@ -14,13 +14,19 @@
 // which every GPU that loads this library holds until the process exits.
 //
 // Host code cannot use the array's name as a device address (on the host it
-// names a stand-in object), so the first call on a device, with that device
-// current, asks the runtime for the device address once with
-// cudaGetSymbolAddress and keeps it for later calls.  Make that first call
-// outside any stream capture.  Every call shares the one array; each call
-// overwrites every slot it reads, so nothing carries over from an earlier
-// call, but calls that overlap on the GPU (different streams or threads,
-// same device) race on it and must be serialised by the caller.
+// names a stand-in object), so the device address is asked for once per
+// device with cudaGetSymbolAddress, with that device current, and kept.
+// mpet_ctx_create does this eagerly: with lazy module loading (the CUDA
+// default) the lookup is also what loads this file's kernels and the array
+// onto the device, so it happens while the caller can still spare the
+// memory (256 KiB plus the code).  If that early lookup failed, the first
+// mpet_residual_noalloc call on the device retries it; make that call
+// outside any stream capture.  The call waits for its own stream (it
+// returns the norms to the host), so it synchronises the context's stream.
+// Every call shares the one array; each call overwrites every slot it reads,
+// so nothing carries over from an earlier call, but calls that overlap on
+// the GPU (different streams or threads, same device) race on it and must
+// be serialised by the caller.
 #include <math.h>
 
 #include <mutex>
@@ -41,6 +47,17 @@ static std::mutex g_noalloc_mutex;
 static double* g_noalloc_ptr[128] = {nullptr};
 
 // device address of the scratch array on the current device (looked up once)
+static double* noalloc_scratch(int device);
+
+// Eager lookup at context creation (the current device is `device`); a
+// failure here is left for the first call to report.
+void noalloc_prepare(int device) {
+    try {
+        noalloc_scratch(device);
+    } catch (const Error&) {
+    }
+}
+
 static double* noalloc_scratch(int device) {
     if (device < 0 || device >= 128) fail(MPET_ERR_INVALID, "device index out of range for the static scratch table");
     std::lock_guard<std::mutex> lock(g_noalloc_mutex);
@@ -135,6 +152,11 @@ static void residual_noalloc(mpet_ctx* c, const double* b, const double* x, doub
     if (n > NOALLOC_MAX_ROWS)
         fail(MPET_ERR_INVALID, "mpet_residual_noalloc handles at most 33,554,432 rows (static scratch of 16384 "
                                "blocks x 2048 rows); this system has " + std::to_string(n));
+    if (n == 0) {
+        norms[0] = 0.0;
+        norms[1] = 0.0;
+        return;
+    }
     double* part = noalloc_scratch(c->device);
     const int nblocks = (int)((n + NOALLOC_ROWS_PER_BLOCK - 1) / NOALLOC_ROWS_PER_BLOCK);
     const Csr& A = c->A;

@@ -541,7 +541,7 @@ __global__ void k_nb_fill(int64_t nnodes, int64_t nv, int64_t Nu, int J, int64_t
 // 64-byte tail of every pool allocation covers the read past the last entry.
 
 constexpr int SPMV_CAP = SPMV_TILE + 8;  // buffer entries (alignment slack)
-constexpr int MBAR_SPIN_LIMIT = 1 << 22;
+constexpr int MBAR_SPIN_LIMIT = 1 << 22;    // default bound of a tile wait (try_wait polls)
 
 __device__ __forceinline__ uint32_t smem_u32(const void* p) { return (uint32_t)__cvta_generic_to_shared(p); }
 
@@ -562,9 +562,10 @@ __device__ __forceinline__ void bulk_copy_g2s(void* dst, const void* src, uint32
                  : "memory");
 }
 
-// Bounded wait for the phase with the given parity; false if it never completed.
-__device__ __forceinline__ bool mbar_wait(uint64_t* bar, uint32_t parity) {
-    for (int it = 0; it < MBAR_SPIN_LIMIT; ++it) {
+// Bounded wait for the phase with the given parity; false if it never completed
+// within `limit` polls.
+__device__ __forceinline__ bool mbar_wait(uint64_t* bar, uint32_t parity, int limit = MBAR_SPIN_LIMIT) {
+    for (int it = 0; it < limit; ++it) {
         uint32_t ok;
         asm volatile(
             "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n selp.u32 %0, 1, 0, p;\n}\n"
@@ -585,7 +586,7 @@ template <typename T, int NV, int LPR, int U, class Epi>
 __global__ void __launch_bounds__(256) k_spmv_staged(const int64_t* __restrict__ rp, const int32_t* __restrict__ ci,
                                                      const T* __restrict__ va, const T* __restrict__ x, Epi epi,
                                                      double* partials, const int32_t* __restrict__ tiles, int ntiles,
-                                                     int* err) {
+                                                     int* err, int spin_limit) {
     extern __shared__ __align__(128) unsigned char smem[];
     uint64_t* bar = reinterpret_cast<uint64_t*>(smem);
     unsigned char* base = smem + 128;
@@ -624,8 +625,12 @@ __global__ void __launch_bounds__(256) k_spmv_staged(const int64_t* __restrict__
             issue(tn, b ^ 1);
             if (b) pending0 = true; else pending1 = true;
         }
-        const bool ok = mbar_wait(&bar[b], b ? ph1 : ph0);
-        if (b) { ph1 ^= 1u; pending1 = false; } else { ph0 ^= 1u; pending0 = false; }
+        const bool ok = mbar_wait(&bar[b], b ? ph1 : ph0, spin_limit);
+        // a buffer whose wait gave up stays pending at its parity, so the
+        // drain below waits for exactly that copy
+        if (ok) {
+            if (b) { ph1 ^= 1u; pending1 = false; } else { ph0 ^= 1u; pending0 = false; }
+        }
         if (__syncthreads_or(!ok)) {
             bad = true;
             break;
@@ -676,7 +681,8 @@ __global__ void __launch_bounds__(256) k_spmv_staged(const int64_t* __restrict__
         b ^= 1;
     }
     if (bad) {
-        // record the failure and let any copy still in flight land (bounded)
+        // record the failure and let any copy still in flight land (bounded by
+        // the default limit, whatever limit the tile waits had)
         if (threadIdx.x == 0) {
             atomicExch(err, 1);
             if (pending0) mbar_wait(&bar[0], ph0);
@@ -711,7 +717,8 @@ static void launch_staged(mpet_ctx* c, const Csr& A, const T* va, const T* x, co
         grid = nsm * (per_sm > 0 ? per_sm : 1);
         if (grid > NB_RED) grid = NB_RED;
     }
-    kern<<<grid, 256, sm, c->stream>>>(A.rp, A.ci, va, x, epi, c->partials, A.tiles, A.ntiles, c->dev_err);
+    kern<<<grid, 256, sm, c->stream>>>(A.rp, A.ci, va, x, epi, c->partials, A.tiles, A.ntiles, c->dev_err,
+                                       c->mbar_spin_limit);
     MPET_CHECK_LAUNCH();
     c->n_launch++;
 }
