@@ -124,10 +124,13 @@ def p1_in_p2_embedding(dm, bc_nodes):
 
 class SAHierarchy:
     """Smoothed-aggregation hierarchy; ``P0`` (optional) replaces aggregation on
-    the first level (the strength threshold then counts aggregation levels)."""
+    the first level (the strength threshold then counts aggregation levels);
+    ``aggregate_fn`` (optional) replaces ``aggregate`` by an equivalent (the C
+    restatement in cbaseline.aggregate)."""
 
-    def __init__(self, A, theta=0.0, coarse_size=500, max_levels=12, cheb_degree=2, P0=None):
+    def __init__(self, A, theta=0.0, coarse_size=500, max_levels=12, cheb_degree=2, P0=None, aggregate_fn=None):
         self.levels = []
+        agg_fn = aggregate if aggregate_fn is None else aggregate_fn
         self.cheb_degree = cheb_degree
         A = A.tocsr()
         while True:
@@ -146,9 +149,9 @@ class SAHierarchy:
             else:
                 th = theta * 0.5 ** (len(self.levels) - 1 - (1 if P0 is not None else 0))
                 S = strength(A, th)
-                agg, nagg = aggregate(S)
+                agg, nagg = agg_fn(S)
                 if nagg == 0 and th > 0.0:
-                    agg, nagg = aggregate(strength(A, 0.0))
+                    agg, nagg = agg_fn(strength(A, 0.0))
                 if nagg == 0 or nagg >= n:
                     break
                 rows = np.nonzero(agg >= 0)[0]

@@ -374,40 +374,9 @@ class OracleMPET:
 
     # --- preconditioner blocks (mpetsolver.py:264-271) ---------------------------------
     def network_modes(self, dt, form="auto"):
-        """(Q, lambda) of the pressure blocks: per network (Q = I, lambda =
-        diag C) or per eigenmode of the network mass coupling C = Q diag(lambda)
-        Q^T, C = diag(c_a + dt theta sum_{b != a} S_ab) - dt theta S (off the
-        diagonal).  With kappa(form, T) the worst condition number of
-        P(t)^-1 (C + t dt theta diag(K)) over t in T, "auto" takes the eigenmodes when
-        kappa(modes, [1e3, 1e6])^2 < kappa(networks, [1, 1e6]): most eigenvalues of
-        the pressure blocks lie at large t, where the modes average K."""
-        J = self.J
-        dth = dt * self.theta
-        C = -dth * self.S.copy()
-        for a in range(J):
-            C[a, a] = self.c[a] + dth * sum(self.S[a, b_] for b_ in range(J) if b_ != a)
-        lam, Q = np.linalg.eigh(C)
-        per_net = (np.eye(J), np.diag(C).copy())
-        if form == "networks":
-            return per_net
-        if form == "modes":
-            return Q, lam
-        K = np.array([float(np.mean(self.Kc[a])) for a in range(J)])
-
-        def kappa(Qx, lx, first=0):
-            kt = (Qx ** 2).T @ K
-            worst = 1.0
-            for t in 10.0 ** (0.1 * np.arange(first, 61)):
-                A = C + t * dth * np.diag(K)
-                P = Qx @ np.diag(lx + t * dth * kt) @ Qx.T
-                ev = np.linalg.eigvalsh(np.linalg.solve(np.linalg.cholesky(P), np.linalg.solve(
-                    np.linalg.cholesky(P), A).T).T)
-                worst = max(worst, ev.max() / ev.min())
-            return worst
-        kd = kappa(*per_net)
-        if np.all(lam > 0) and kappa(Q, lam) < kd and kappa(Q, lam, 30) ** 2 < kd:
-            return Q, lam
-        return per_net
+        """(Q, lambda) of the pressure blocks; see ``network_modes`` (module level)."""
+        K = np.array([float(np.mean(self.Kc[a])) for a in range(self.J)])
+        return network_modes(self.J, self.theta, self.S, self.c, K, dt, form)
 
     def preconditioner_blocks(self, dt, u_weight=None, modes=None):
         """Scalar SPD blocks: w (grad u, grad v) on P2 nodes (w = mu in the
@@ -482,14 +451,53 @@ class OracleMPET:
             up_ = up
 
 
+def network_modes(J, theta, S, c, K_mean, dt, form="auto"):
+    """(Q, lambda) of the pressure blocks: per network (Q = I, lambda =
+    diag C) or per eigenmode of the network mass coupling C = Q diag(lambda)
+    Q^T, C = diag(c_a + dt theta sum_{b != a} S_ab) - dt theta S (off the
+    diagonal).  With kappa(form, T) the worst condition number of
+    P(t)^-1 (C + t dt theta diag(K)) over t in T (K = the mean permeability of
+    each network), "auto" takes the eigenmodes when
+    kappa(modes, [1e3, 1e6])^2 < kappa(networks, [1, 1e6]): most eigenvalues of
+    the pressure blocks lie at large t, where the modes average K."""
+    S = np.asarray(S, dtype=np.float64).reshape(J, J)
+    c = np.asarray(c, dtype=np.float64)
+    dth = dt * theta
+    C = -dth * S.copy()
+    for a in range(J):
+        C[a, a] = c[a] + dth * sum(S[a, b_] for b_ in range(J) if b_ != a)
+    lam, Q = np.linalg.eigh(C)
+    per_net = (np.eye(J), np.diag(C).copy())
+    if form == "networks":
+        return per_net
+    if form == "modes":
+        return Q, lam
+    K = np.asarray(K_mean, dtype=np.float64)
+
+    def kappa(Qx, lx, first=0):
+        kt = (Qx ** 2).T @ K
+        worst = 1.0
+        for t in 10.0 ** (0.1 * np.arange(first, 61)):
+            A = C + t * dth * np.diag(K)
+            P = Qx @ np.diag(lx + t * dth * kt) @ Qx.T
+            ev = np.linalg.eigvalsh(np.linalg.solve(np.linalg.cholesky(P), np.linalg.solve(
+                np.linalg.cholesky(P), A).T).T)
+            worst = max(worst, ev.max() / ev.min())
+        return worst
+    kd = kappa(*per_net)
+    if np.all(lam > 0) and kappa(Q, lam) < kd and kappa(Q, lam, 30) ** 2 < kd:
+        return Q, lam
+    return per_net
+
+
 def _diag_positions(A):
     """Index into A.data of each diagonal entry (must exist)."""
     n = A.shape[0]
-    pos = np.empty(n, dtype=np.int64)
-    for i in range(n):
-        lo, hi = A.indptr[i], A.indptr[i + 1]
-        k = np.searchsorted(A.indices[lo:hi], i)
-        pos[i] = lo + k
+    rows = np.repeat(np.arange(n, dtype=np.int64), np.diff(A.indptr))
+    hit = np.nonzero(A.indices == rows)[0]
+    pos = np.full(n, -1, dtype=np.int64)
+    pos[rows[hit]] = hit
+    assert np.all(pos >= 0), "a diagonal entry is missing from the pattern"
     return pos
 
 
