@@ -139,13 +139,14 @@ class ClockSampler:
 
 
 def spmv_alg_bytes(solver, sv):
-    """Algorithmic bytes of one system SpMV with the chosen variant: every
-    stored nonzero value once, one column id per nonzero (CSR / SELL) or per
-    block (node-block copy), row pointers (CSR), x and y once each."""
+    """Algorithmic bytes of one system SpMV with the variant chosen for its
+    precision: every stored nonzero value once, one column id per nonzero
+    (CSR / SELL) or per block (node-block copy), row pointers (CSR), x and y
+    once each."""
     import ctypes
     N, nnz = solver.N, solver.nnz
     ch = ctypes.c_int32()
-    solver.ctx.call("mpet_get_spmv_tuning", None, ctypes.byref(ch))
+    solver.ctx.call("mpet_get_spmv_tuning" if sv == 4 else "mpet_get_spmv_tuning_fp64", None, ctypes.byref(ch))
     if ch.value == 8:
         nb = ctypes.c_int64()
         solver.ctx.call("mpet_get_node_block_info", ctypes.byref(nb), None)
@@ -246,11 +247,12 @@ def prec_form(solver):
     return "elasticity AMG (rigid-body modes)" if v.value else "vector Laplacian AMG"
 
 
-def spmv_tuning(solver):
+def spmv_tuning(solver, fp64=False):
     import ctypes
     ms = np.zeros(7)
     ch = ctypes.c_int32()
-    solver.ctx.call("mpet_get_spmv_tuning", ms.ctypes.data_as(ctypes.c_void_p), ctypes.byref(ch))
+    solver.ctx.call("mpet_get_spmv_tuning_fp64" if fp64 else "mpet_get_spmv_tuning",
+                    ms.ctypes.data_as(ctypes.c_void_p), ctypes.byref(ch))
     names = ["register/4", "register/8", "staged/4", "staged/8", "sell32/4", "sell32/8", "node-block"]
     return {"ms": {names[v]: round(float(ms[v]), 4) for v in range(7) if ms[v] > 0},
             "chosen": names[6 if ch.value == 8 else ch.value]}
@@ -583,6 +585,49 @@ def batch_run(args):
     print(json.dumps(out))
 
 
+def vcycle_profile(args):
+    """Per-level cost of the block preconditioner on the --n cube (mixed
+    precision): for every hierarchy (displacement, each pressure block) the
+    rows and nonzeros of each level, its own time (V-cycle from level k minus
+    V-cycle from level k+1, medians over L2-flushed launches), its algorithmic
+    bytes and their rate against the measured HBM peak; plus one whole
+    preconditioner application (the pressure V-cycles run concurrently with the
+    displacement V-cycle).  Prints one JSON line."""
+    import ctypes
+    import torch
+    from waterscapes_gb300 import MPETSolver, _lib
+    problem, dt = workload(args.n, args.networks, args.workload)
+    base = dict(dt=dt, T=1e9, theta=1.0, rtol=1e-10, precision="mixed")
+    if args.cheb_degree is not None:
+        base["amg_cheb_degree"] = args.cheb_degree
+    sol = MPETSolver(problem, base)
+    sol._assemble(dt)
+    torch.cuda.synchronize()
+    hbm, kind = peaks()
+    out = {"vcycle_profile": "Kuhn cube %d^3, A=%d" % (args.n, args.networks), "peak_gbs": hbm, "peak_kind": kind,
+           "blocks": []}
+    for blk in range(args.networks + 1):
+        sizes, nnz = sol.amg_info(blk)
+        nl = ctypes.c_int32()
+        ms = np.zeros(16)
+        by = np.zeros(16)
+        sol.ctx.call("mpet_profile_vcycle", blk, 7, ctypes.byref(nl), _lib._ptr(ms), _lib._ptr(by))
+        L = nl.value
+        levels = []
+        for k in range(L):
+            own = ms[k] - (ms[k + 1] if k + 1 < L else 0.0)
+            levels.append({"rows": sizes[k], "nnz": nnz[k], "own_ms": round(own, 5), "vcycle_from_here_ms":
+                           round(ms[k], 5), "alg_bytes": int(by[k]),
+                           "gbs": round(by[k] / own / 1e6, 1) if own > 0 else None,
+                           "frac": round(by[k] / own / 1e6 / hbm, 3) if own > 0 else None})
+        out["blocks"].append({"block": "displacement" if blk == 0 else "pressure %d" % blk, "levels": levels,
+                              "vcycle_ms": round(ms[0], 5), "alg_bytes": int(by[:L].sum())})
+    out["preconditioner_ms"] = time_precond(sol, torch, _lib)
+    out["preconditioner_alg_bytes"] = int(sum(b["alg_bytes"] for b in out["blocks"]))
+    out["preconditioner_gbs"] = out["preconditioner_alg_bytes"] / out["preconditioner_ms"] / 1e6
+    print(json.dumps(out))
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -610,6 +655,8 @@ def main():
     ap.add_argument("--prec-u-form", default=None, choices=["elasticity", "laplacian"],
                     help="override the displacement block of the preconditioner")
     ap.add_argument("--inner-rtol", type=float, default=None, help="override inner_rtol")
+    ap.add_argument("--vcycle-profile", action="store_true",
+                    help="per-level time and algorithmic bytes of the block preconditioner instead of the bench")
     ap.add_argument("--estimators", action="store_true",
                     help="time the AdaptiveMPETSolver error indicators on the --n cube instead of the bench")
     ap.add_argument("--formulation", default="mpet", choices=["mpet", "total-pressure"],
@@ -623,6 +670,8 @@ def main():
         return adjoint_check(args)
     if args.estimators:
         return estimator_run(args)
+    if args.vcycle_profile:
+        return vcycle_profile(args)
     n, J = args.n, args.networks
     tp = args.formulation == "total-pressure"
     N_full = 3 * (2 * n + 1) ** 3 + (J + int(tp)) * (n + 1) ** 3
@@ -791,6 +840,7 @@ def main():
         "setup_s": {"mesh_dofmap_pattern": t_setup, "assemble_plus_amg": t_asm_amg},
         "spmv": spmv,
         "spmv_tuning": spmv_tuning(sol),
+        "spmv_tuning_fp64_residual": spmv_tuning(sol, fp64=True),
         "preconditioner_u_block": prec_form(sol),
         "iteration_breakdown_ms": dict(split, spmv_fp32=(spmv.get("fp32") or spmv["fp64"])["ms"],
                                        preconditioner=precond_ms),

@@ -273,6 +273,17 @@ int mpet_setup_preconditioner(mpet_ctx* ctx, double dt);
 int mpet_get_amg_info(mpet_ctx* ctx, int32_t block, int32_t* levels, int64_t* sizes_host,
                       int64_t* nnz_host);
 
+/* Per-level cost of one hierarchy (block 0: displacement, a >= 1: pressure
+ * block a), in the context's precision: ms_host[k] = median time (ms) of a
+ * V-cycle started at level k over `reps` launches, each from a flushed L2;
+ * bytes_host[k] = the algorithmic bytes of level k's own work (every matrix
+ * entry and row pointer once per product, every vector once per read or
+ * write).  Level k's own time is ms_host[k] - ms_host[k+1].  Arrays hold 16
+ * entries.  No reference counterpart (measurement of the preconditioner
+ * that hypre applies inside PETSc, mpetsolver.py:507-556). */
+int mpet_profile_vcycle(mpet_ctx* ctx, int32_t block, int32_t reps, int32_t* nlev, double* ms_host,
+                        double* bytes_host);
+
 /* Solve A x = b with the assembled (BC-applied) matrix; x holds the
  * initial guess on entry (its Dirichlet entries are replaced by the BC
  * values).  Replaces LUSolver(A, "mumps").solve / PETScKrylovSolver
@@ -332,11 +343,18 @@ int mpet_apply_symmetric(mpet_ctx* ctx, double* b, const double* x_bc);
  * benchmarks). */
 int mpet_get_spmv_tuning(mpet_ctx* ctx, double* ms7_host, int32_t* chosen);
 
+/* The same for the FP64 products of the system matrix (the refinement
+ * residual).  In mixed precision they are tuned apart from the FP32 copy,
+ * with the residual epilogue they run with; otherwise this repeats
+ * mpet_get_spmv_tuning.  No reference counterpart (tuning report). */
+int mpet_get_spmv_tuning_fp64(mpet_ctx* ctx, double* ms7_host, int32_t* chosen);
+
 /* Size of the node-block copy: blocks of the matrix (one column id each) and
  * stored values including padding.  No reference counterpart. */
 int mpet_get_node_block_info(mpet_ctx* ctx, int64_t* blocks, int64_t* stored_values);
 
-/* Override the autotuned system-matrix SpMV variant (bits as above);
+/* Override the autotuned system-matrix SpMV variant (bits as above) for the
+ * products of both precisions;
  * MPET_ERR_INVALID if the variant cannot run on this matrix.  Every variant
  * computes the same product (summation order differs).  No reference
  * counterpart (tuning and test hook). */

@@ -118,6 +118,7 @@ SIGNATURES = {
     "mpet_rhs": [_P, _D, _P, _P],
     "mpet_setup_preconditioner": [_P, _D],
     "mpet_get_amg_info": [_P, _I32, ctypes.POINTER(_I32), _P, _P],
+    "mpet_profile_vcycle": [_P, _I32, _I32, ctypes.POINTER(_I32), _P, _P],
     "mpet_solve": [_P, _P, _P, ctypes.POINTER(MpetStats)],
     "mpet_get_prec_info": [_P, ctypes.POINTER(_I32)],
     "mpet_step": [_P, _D, _P, _P, ctypes.POINTER(MpetStats)],
@@ -127,6 +128,7 @@ SIGNATURES = {
     "mpet_spmv": [_P, _I32, _P, _P],
     "mpet_apply_symmetric": [_P, _P, _P],
     "mpet_get_spmv_tuning": [_P, _P, ctypes.POINTER(_I32)],
+    "mpet_get_spmv_tuning_fp64": [_P, _P, ctypes.POINTER(_I32)],
     "mpet_set_spmv_variant": [_P, _I32],
     "mpet_set_hierarchy_spmv_variant": [_P, _I32],
     "mpet_set_wait_limit": [_P, _I32],

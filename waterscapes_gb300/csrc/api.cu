@@ -651,6 +651,18 @@ int mpet_get_amg_info(mpet_ctx* c, int32_t block, int32_t* levels, int64_t* size
     API_END(c)
 }
 
+int mpet_profile_vcycle(mpet_ctx* c, int32_t block, int32_t reps, int32_t* nlev, double* ms, double* bytes) {
+    API_BEGIN(c)
+    require(c->precond_ready, MPET_ERR_STATE, "mpet_setup_preconditioner must come first");
+    require(block >= 0 && block <= c->J, MPET_ERR_INVALID, "bad block");
+    require(reps >= 1 && nlev && ms && bytes, MPET_ERR_INVALID, "reps >= 1 and non-NULL outputs");
+    destroy_minres_graph(c);
+    int n = 0;
+    profile_vcycle(c, block, reps, &n, ms, bytes);
+    *nlev = n;
+    API_END(c)
+}
+
 int mpet_solve(mpet_ctx* c, const double* b, double* x, mpet_stats* st) {
     API_BEGIN(c)
     require(c->assembled, MPET_ERR_STATE, "mpet_assemble must come first");
@@ -731,6 +743,16 @@ int mpet_get_spmv_tuning(mpet_ctx* c, double* ms7, int32_t* chosen) {
     API_END(c)
 }
 
+int mpet_get_spmv_tuning_fp64(mpet_ctx* c, double* ms7, int32_t* chosen) {
+    API_BEGIN(c)
+    require(c->setup_done, MPET_ERR_STATE, "mpet_setup must come first");
+    const bool own = c->A.variant64 >= 0;
+    if (ms7)
+        for (int v = 0; v < 7; ++v) ms7[v] = own ? c->spmv_variant_ms64[v] : c->spmv_variant_ms[v];
+    if (chosen) *chosen = own ? c->A.variant64 : c->A.variant;
+    API_END(c)
+}
+
 int mpet_set_hierarchy_spmv_variant(mpet_ctx* c, int32_t variant) {
     API_BEGIN(c)
     require(c->precond_ready, MPET_ERR_STATE, "mpet_setup_preconditioner must come first");
@@ -763,6 +785,7 @@ int mpet_set_spmv_variant(mpet_ctx* c, int32_t variant) {
     require(spmv_variant_available(c->A, variant), MPET_ERR_INVALID, "SpMV variant not available for this matrix");
     destroy_minres_graph(c);
     c->A.variant = variant;
+    c->A.variant64 = -1;  // the forced variant serves both precisions
     API_END(c)
 }
 

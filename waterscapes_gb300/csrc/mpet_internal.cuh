@@ -138,6 +138,10 @@ struct Csr {
     // 32 lanes per row, or with the SELL copy), bit 1 = shared-memory staged
     // (needs tiles), bit 2 = SELL-32 copy (needs s_off); 8 = node-block copy
     int variant = 0;
+    // mixed precision: variant and lanes per row of the FP64 products when they
+    // were tuned apart from the FP32 copy's (-1: none, use variant / lpr)
+    int variant64 = -1;
+    int lpr64 = 32;
     // SELL-32 copy: slices of 32 rows, column-major within a slice, padded
     // to the slice's longest row with zero values at the row's last column
     // (column 0 for empty rows); s_off[s] is the first entry of slice s
@@ -405,6 +409,7 @@ struct mpet_ctx {
     int* dev_err = nullptr;
     int mbar_spin_limit = 1 << 22;  // polls of a staged-SpMV tile wait (test hook lowers it)
     double spmv_variant_ms[7] = {0, 0, 0, 0, 0, 0, 0};  // variants 0..5 and 8 (node blocks)
+    double spmv_variant_ms64[7] = {0, 0, 0, 0, 0, 0, 0};  // FP64 residual products of the mixed path
 
     // timing
     cudaEvent_t ev0 = nullptr, ev1 = nullptr;
@@ -497,6 +502,7 @@ void alloc_krylov(mpet_ctx* c);
 void autotune_system(mpet_ctx* c);
 void residual_norms(mpet_ctx* c, const double* b, const double* x, double* r, double* norms);
 void apply_preconditioner(mpet_ctx* c, int precision, const void* r, void* z);
+void profile_vcycle(mpet_ctx* c, int block, int reps, int* nlev, double* ms, double* bytes);
 void setup_batch(mpet_ctx* c, int ninst, const int32_t* vertex_inst);
 void batch_relres(mpet_ctx* c, double* out);
 int choose_lpr(int64_t n, int64_t nnz);

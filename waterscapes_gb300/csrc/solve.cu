@@ -942,16 +942,20 @@ const float* sell_vals<float>(const Csr& A) { return A.s_v32; }
 
 template <typename T, int NV, class Epi>
 static void launch_spmv(mpet_ctx* c, const Csr& A, const T* va, const T* x, const Epi& epi) {
+    // FP64 products of a matrix tuned on its FP32 copy use their own tuning when they have one
+    const bool own64 = sizeof(T) == 8 && A.variant64 >= 0;
+    const int variant = own64 ? A.variant64 : A.variant;
+    const int lpr = own64 ? A.lpr64 : A.lpr;
     if constexpr (NV == 1 && Epi::kSystem) {
-        if (A.variant == 8 && A.nb && nb_vals<T>(*A.nb) && va == vals<T>(A)) {
+        if (variant == 8 && A.nb && nb_vals<T>(*A.nb) && va == vals<T>(A)) {
             launch_nb<T>(c, *A.nb, x, epi);
             return;
         }
     }
-    if ((A.variant & 4) && sell_vals<T>(A) && va == vals<T>(A)) {
+    if ((variant & 4) && sell_vals<T>(A) && va == vals<T>(A)) {
         int blocks = Epi::kRed > 0 ? NB_RED : grid_for(A.nslices * 32, 256);
         if (Epi::kRed == 0 && blocks > 152 * 16) blocks = 152 * 16;
-        if (A.variant & 1)
+        if (variant & 1)
             k_spmv_sell<T, NV, 8, Epi><<<blocks, 256, 0, c->stream>>>(A.n, A.nslices, A.s_off, A.s_ci,
                                                                       sell_vals<T>(A), x, epi, c->partials);
         else
@@ -961,9 +965,9 @@ static void launch_spmv(mpet_ctx* c, const Csr& A, const T* va, const T* x, cons
         c->n_launch++;
         return;
     }
-    const bool deep = A.lpr == 32 && (A.variant & 1);
-    if (A.ntiles > 0 && (A.variant & 2)) {
-        switch (A.lpr) {
+    const bool deep = lpr == 32 && (variant & 1);
+    if (A.ntiles > 0 && (variant & 2)) {
+        switch (lpr) {
             case 32:
                 if (deep) launch_staged<T, NV, 32, 8, Epi>(c, A, va, x, epi);
                 else launch_staged<T, NV, 32, 4, Epi>(c, A, va, x, epi);
@@ -978,13 +982,13 @@ static void launch_spmv(mpet_ctx* c, const Csr& A, const T* va, const T* x, cons
     if (Epi::kRed > 0) {
         blocks = NB_RED;
     } else {
-        int64_t rows_per_block = 256 / A.lpr;
+        int64_t rows_per_block = 256 / lpr;
         blocks = grid_for(A.n, (int)rows_per_block);
         if (blocks > 152 * 16) blocks = 152 * 16;
     }
     double* part = c->partials;
     cudaStream_t s = c->stream;
-    switch (A.lpr) {
+    switch (lpr) {
         case 32:
             if (deep) k_spmv<T, NV, 32, 8, Epi><<<blocks, 256, 0, s>>>(A.n, A.rp, A.ci, va, x, epi, part);
             else k_spmv<T, NV, 32, 4, Epi><<<blocks, 256, 0, s>>>(A.n, A.rp, A.ci, va, x, epi, part);
@@ -1088,12 +1092,26 @@ void autotune_system(mpet_ctx* c) {
         c->A.variant = 8;
         return;
     }
-    if (c->A.v32)
+    c->A.variant64 = -1;
+    if (c->A.v32) {
         autotune_matrix<float, 1>(c, c->A, (const float*)c->kv, EpiStore<float, 1>{(float*)c->kd},
                                   c->spmv_variant_ms);
-    else
+        if (c->A.v64) {
+            // the FP64 refinement residual of the mixed path is tuned on its own, with its epilogue
+            const int v32 = c->A.variant, l32 = c->A.lpr;
+            MPET_CUDA(cudaMemsetAsync(c->kd, 0, sizeof(double) * c->N, c->stream));
+            autotune_matrix<double, 1>(c, c->A, (const double*)c->kv, EpiResid64{c->orr, (const double*)c->kd,
+                                                                                  c->dinv},
+                                       c->spmv_variant_ms64);
+            c->A.variant64 = c->A.variant;
+            c->A.lpr64 = c->A.lpr;
+            c->A.variant = v32;
+            c->A.lpr = l32;
+        }
+    } else {
         autotune_matrix<double, 1>(c, c->A, (const double*)c->kv, EpiStore<double, 1>{(double*)c->kd},
                                    c->spmv_variant_ms);
+    }
 }
 
 template <typename T, int NV>
@@ -1355,6 +1373,68 @@ static void vcycle(mpet_ctx* c, AmgHier& h, size_t k, const T* b, T* x) {
     vcycle<T, NV>(c, h, k + 1, (const T*)C.b, (T*)C.x);
     launch_spmv<T, NV>(c, L.P, vals<T>(L.P), (const T*)C.x, EpiAxpby<T, NV>{xs, xs, T(1), T(1)});
     cheb<T, NV>(c, h, L, b, xs, x);
+}
+
+// Per-level profile of one hierarchy: ms[k] = median time of a V-cycle
+// started at level k (so level k's own share is ms[k] - ms[k+1]), each of
+// `reps` launches from a flushed L2 (in the solver every level is reached
+// after the system SpMV has streamed gigabytes through L2); bytes[k] = the
+// algorithmic bytes of level k's own work: every matrix entry (value + column
+// id) and row pointer once per product, every vector once per read or write
+// (2s products with A for Chebyshev degree s, the residual, R and P; the
+// dense inverse on the coarsest level).
+template <typename T, int NV>
+static void profile_levels(mpet_ctx* c, AmgHier& h, int reps, double* ms, double* bytes) {
+    constexpr size_t kFlush = 256u << 20;
+    if (!c->l2_flush) c->l2_flush = c->pool.alloc<unsigned char>(kFlush);
+    const int64_t l0 = c->n_launch;
+    const size_t nl = h.lev.size();
+    const double sv = sizeof(T);
+    const int s = h.cheb_degree;
+    for (size_t k = 0; k < nl; ++k) {
+        AmgLevel& L = h.lev[k];
+        MPET_CUDA(cudaMemsetAsync(L.b, 0, sizeof(double) * L.A.n * NV, c->stream));
+        std::vector<float> t;
+        for (int q = 0; q <= reps; ++q) {
+            MPET_CUDA(cudaMemsetAsync(c->l2_flush, q & 255, kFlush, c->stream));
+            MPET_CUDA(cudaEventRecord(c->ev0, c->stream));
+            vcycle<T, NV>(c, h, k, (const T*)L.b, (T*)L.x);
+            MPET_CUDA(cudaEventRecord(c->ev1, c->stream));
+            MPET_CUDA(cudaEventSynchronize(c->ev1));
+            float e = 0.f;
+            MPET_CUDA(cudaEventElapsedTime(&e, c->ev0, c->ev1));
+            if (q > 0) t.push_back(e);
+        }
+        std::sort(t.begin(), t.end());
+        ms[k] = t[t.size() / 2];
+        const double n = (double)L.A.n, vec = n * NV * sv, dv = n * sv;
+        if (k + 1 == nl) {
+            bytes[k] = (double)h.ncoarse * h.ncoarse * 8.0 + 2.0 * h.ncoarse * NV * sv;
+            continue;
+        }
+        const double nc = (double)h.lev[k + 1].A.n, vecc = nc * NV * sv;
+        const double mA = L.A.nnz * (sv + 4.0) + (n + 1) * 8.0;
+        double b = 3 * vec + dv;                              // first Chebyshev step (no product)
+        b += (2 * s - 1) * (mA + 5 * vec + dv);               // the other 2s - 1 smoothing products
+        b += mA + 3 * vec;                                    // residual
+        b += L.R.nnz * (sv + 4.0) + (nc + 1) * 8.0 + vec + vecc;  // restriction
+        b += L.P.nnz * (sv + 4.0) + (n + 1) * 8.0 + vecc + 2 * vec;  // prolongation + correction
+        bytes[k] = b;
+    }
+    c->n_launch = l0;
+}
+
+void profile_vcycle(mpet_ctx* c, int block, int reps, int* nlev, double* ms, double* bytes) {
+    const bool f32 = c->prm.precision == MPET_PRECISION_MIXED;
+    AmgHier& h = block == 0 ? c->amg_u : c->amg_p[block - 1];
+    *nlev = (int)h.lev.size();
+    if (block == 0 && !c->u_elast) {
+        if (f32) profile_levels<float, 4>(c, h, reps, ms, bytes);
+        else profile_levels<double, 4>(c, h, reps, ms, bytes);
+    } else {
+        if (f32) profile_levels<float, 1>(c, h, reps, ms, bytes);
+        else profile_levels<double, 1>(c, h, reps, ms, bytes);
+    }
 }
 
 // displacement components (3 per node) <-> the padded 4-wide layout of the
