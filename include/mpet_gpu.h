@@ -360,6 +360,14 @@ int mpet_get_node_block_info(mpet_ctx* ctx, int64_t* blocks, int64_t* stored_val
  * counterpart (tuning and test hook). */
 int mpet_set_spmv_variant(mpet_ctx* ctx, int32_t variant);
 
+/* Which kernel computes the displacement element blocks of tetrahedra (the
+ * 30 x 30 part of the element matrix, mpetsolver.py:196-201): 1 (default) the
+ * tensor cores (tcgen05 MMAs on exact 11-bit slices of the FP64 element
+ * features, combined in 64-bit integers), 0 the FP64 CUDA-core kernel.  Both
+ * give FP64 values; the next mpet_assemble uses the choice.  No reference
+ * counterpart (engine option and test hook). */
+int mpet_set_element_kernel(mpet_ctx* ctx, int32_t kind);
+
 /* Bound (in polls) of the bounded waits of the staged SpMV's tile copies
  * (default 4,194,304).  A wait that gives up sets the context's device error
  * flag; the call that launched it then returns MPET_ERR_TIMEOUT and the

@@ -16,7 +16,8 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 CSRC = os.path.join(HERE, "csrc")
 BUILD = os.path.join(HERE, "_build")
 LIB = os.path.join(HERE, "libmpetgpu.so")
-SOURCES = ["setup.cu", "assemble.cu", "facets.cu", "solve.cu", "api.cu", "noalloc.cu", "amg_setup.cpp"]
+SOURCES = ["setup.cu", "assemble.cu", "elem_tc.cu", "facets.cu", "solve.cu", "api.cu", "noalloc.cu",
+           "amg_setup.cpp"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 
 

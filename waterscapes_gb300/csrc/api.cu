@@ -789,6 +789,14 @@ int mpet_set_spmv_variant(mpet_ctx* c, int32_t variant) {
     API_END(c)
 }
 
+int mpet_set_element_kernel(mpet_ctx* c, int32_t kind) {
+    API_BEGIN(c)
+    require(kind == 0 || kind == 1, MPET_ERR_INVALID, "element kernel: 0 (FP64 CUDA cores) or 1 (tensor cores)");
+    c->elem_kernel = kind;
+    c->assembled = false;
+    API_END(c)
+}
+
 int mpet_set_wait_limit(mpet_ctx* c, int32_t polls) {
     API_BEGIN(c)
     require(polls >= 0, MPET_ERR_INVALID, "wait limit must be >= 0");

@@ -726,6 +726,8 @@ void launch_assemble_matrix(mpet_ctx* c, double dt, bool apply_bc, bool write32)
         A.Mst = c->elem_buf;
         if (c->dim == 2)
             k_elem_uu<2><<<grid_for(c->nc, 128), 128, 0, c->stream>>>(c->nc, c->geo, P.mu, P.lmbda, c->elem_buf);
+        else if (c->elem_kernel == 1)
+            launch_elem_uu_tc(c, P.mu, P.lmbda, c->elem_buf);
         else
             k_elem_uu<3><<<grid_for(c->nc, 128), 128, 0, c->stream>>>(c->nc, c->geo, P.mu, P.lmbda, c->elem_buf);
         MPET_CHECK_LAUNCH();

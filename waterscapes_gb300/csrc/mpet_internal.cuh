@@ -341,6 +341,7 @@ struct mpet_ctx {
     double* gm_h_host = nullptr;  // pinned
     int gm_m = 0;                 // restart length the buffers hold
     bool elem_tried = false;
+    int elem_kernel = 1;          // element blocks of tetrahedra: 1 tensor cores, 0 FP64 CUDA cores
     // error-indicator scratch: per-facet terms, per-cell R4p density, its sum, bad-index flag
     double* est_fval = nullptr;
     int64_t est_fval_cap = 0;
@@ -490,6 +491,10 @@ int launch_error_indicators(mpet_ctx* c, double dt, const double* up, const doub
 // noalloc.cu: device address of the static residual scratch, looked up at
 // context creation
 void noalloc_prepare(int device);
+
+// elem_tc.cu: the displacement element blocks of tetrahedra on the tensor cores
+// (same record as k_elem_uu<3>)
+void launch_elem_uu_tc(mpet_ctx* c, double mu, double lmbda, double* out);
 
 // solve.cu
 template <typename T>
