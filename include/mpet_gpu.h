@@ -360,6 +360,16 @@ int mpet_get_node_block_info(mpet_ctx* ctx, int64_t* blocks, int64_t* stored_val
  * counterpart (tuning and test hook). */
 int mpet_set_spmv_variant(mpet_ctx* ctx, int32_t variant);
 
+/* First level of the displacement preconditioner hierarchy (the block
+ * w (grad u, grad v) of mpetsolver.py:269 on P2 nodes): its products formed
+ * matrix-free from per-cell data (mode 1), from its CSR copy (0), or chosen
+ * per set-up by timing both (-1, default).  Takes effect at the next
+ * mpet_setup_preconditioner.  mpet_get_prec_matrix_free reports the choice
+ * and the two timed medians (ms; 0 when not timed).  No reference
+ * counterpart (engine option, tuning report and test hook). */
+int mpet_set_prec_matrix_free(mpet_ctx* ctx, int32_t mode);
+int mpet_get_prec_matrix_free(mpet_ctx* ctx, int32_t* used, float* ms2_host);
+
 /* Which kernel computes the displacement element blocks of tetrahedra (the
  * 30 x 30 part of the element matrix, mpetsolver.py:196-201): 1 (default) the
  * tensor cores (tcgen05 MMAs on exact 11-bit slices of the FP64 element

@@ -133,6 +133,8 @@ SIGNATURES = {
     "mpet_set_hierarchy_spmv_variant": [_P, _I32],
     "mpet_set_wait_limit": [_P, _I32],
     "mpet_set_element_kernel": [_P, _I32],
+    "mpet_set_prec_matrix_free": [_P, _I32],
+    "mpet_get_prec_matrix_free": [_P, ctypes.POINTER(_I32), _P],
     "mpet_get_node_block_info": [_P, ctypes.POINTER(_I64), ctypes.POINTER(_I64)],
     "mpet_get_timing": [_P, ctypes.POINTER(_D), ctypes.POINTER(_I64), ctypes.POINTER(_D), ctypes.POINTER(_I64)],
     "mpet_pressure_misfit": [_P, _P, _P, ctypes.POINTER(_D), _P],

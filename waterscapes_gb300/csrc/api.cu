@@ -537,6 +537,7 @@ int mpet_setup_preconditioner(mpet_ctx* c, double dt) {
     destroy_minres_graph(c);
     setup_network_modes(c, dt);
     launch_assemble_prec_blocks(c, dt);
+    if (c->prm.prec_u_form != 1) launch_mf_cells(c, dt);
     const bool fp32 = c->prm.precision == MPET_PRECISION_MIXED;
     auto fetch = [&](const Csr& d, HostCsr& h) {
         h.n = d.n;
@@ -786,6 +787,25 @@ int mpet_set_spmv_variant(mpet_ctx* c, int32_t variant) {
     destroy_minres_graph(c);
     c->A.variant = variant;
     c->A.variant64 = -1;  // the forced variant serves both precisions
+    API_END(c)
+}
+
+int mpet_set_prec_matrix_free(mpet_ctx* c, int32_t mode) {
+    API_BEGIN(c)
+    require(mode >= -1 && mode <= 1, MPET_ERR_INVALID, "mode: -1 (autotuned), 0 (CSR) or 1 (matrix-free)");
+    c->mf_mode = mode;
+    c->precond_ready = false;
+    API_END(c)
+}
+
+int mpet_get_prec_matrix_free(mpet_ctx* c, int32_t* used, float* ms2) {
+    API_BEGIN(c)
+    require(c->precond_ready, MPET_ERR_STATE, "mpet_setup_preconditioner must come first");
+    if (used) *used = (!c->u_elast && !c->amg_u.lev.empty() && c->amg_u.lev[0].mf) ? 1 : 0;
+    if (ms2) {
+        ms2[0] = c->mf_ms[0];
+        ms2[1] = c->mf_ms[1];
+    }
     API_END(c)
 }
 

@@ -767,6 +767,120 @@ void launch_assemble_prec_blocks(mpet_ctx* c, double dt) {
     MPET_CHECK_LAUNCH();
 }
 
+// ---- matrix-free displacement preconditioner level ------------------------------------
+//
+// The first level of the displacement hierarchy is the block w (grad u, grad v)
+// (+ shift (u, v)) on P2 nodes (k_assemble_prec above).  Its entries are, per
+// cell, K_mj = w |T| kappa sum_{p <= q} T6[mj][pq] (b_p . b_q) + shift |T| M2[m][j]
+// over the barycentric gradients b_1..b_D (b_0 = -(b_1 + ... + b_D) folded into
+// the integer table T6), so its product can be formed from D (D + 1) / 2 dot
+// products and |T| per cell instead of the 61e6-entry CSR matrix (64^3 cube).
+// Per cell: slots 0..NQ-1 = w |T| kappa (b_p . b_q) (p <= q), slot NQ = shift
+// |T|, slot 7 = bit mask of the cell's Dirichlet nodes (bit pattern).
+template <typename T, int D>
+__global__ void k_mf_cells(int64_t nc, const double* __restrict__ geo, const int32_t* __restrict__ cell_nodes,
+                           const uint8_t* __restrict__ node_bc, double w, double shift, T* out) {
+    constexpr int NN = Simplex<D>::NN;
+    const int64_t c = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    if (c >= nc) return;
+    Geo G;
+    load_geo(geo, c, G);
+    const double f = w * G.vol * kappa<D>();
+    T o[8];
+#pragma unroll
+    for (int q = 0; q < 8; ++q) o[q] = T(0);
+    int q = 0;
+#pragma unroll
+    for (int a = 1; a <= D; ++a)
+#pragma unroll
+        for (int b = a; b <= D; ++b) {
+            double dot = 0.0;
+#pragma unroll
+            for (int k = 0; k < D; ++k) dot += G.b[a][k] * G.b[b][k];
+            o[q++] = (T)(f * dot);
+        }
+    o[D * (D + 1) / 2] = (T)(shift * G.vol);
+    uint32_t mask = 0;
+    for (int j = 0; j < NN; ++j)
+        if (node_bc[cell_nodes[NN * c + j]]) mask |= 1u << j;
+    if constexpr (sizeof(T) == 4) o[7] = __uint_as_float(mask);
+    else o[7] = __longlong_as_double((long long)mask);
+#pragma unroll
+    for (int k = 0; k < 8; ++k) out[8 * c + k] = o[k];
+}
+
+// Host tables of the matrix-free level, as floats: T6 (node pairs m <= j x dot
+// products p <= q; integers sum_rs (1 + delta_rs) G[m][r][p] G[j][s][q] with b_0
+// folded, symmetrised) and the P2 mass matrix divided by |T| (M2):
+// tab = [T6 (NP x NQ), M2 (NN x NN)].
+template <int D>
+static std::vector<float> mf_table() {
+    constexpr int NN = Simplex<D>::NN, NV = Simplex<D>::NV;
+    double G[10][4][4] = {};
+    for (int i = 0; i < NV; ++i)
+        for (int r = 0; r < NV; ++r) G[i][r][i] = (r == i) ? 3.0 : -1.0;
+    for (int e = 0; e < Simplex<D>::NE; ++e) {
+        const int a = edge_end<D>(e, 0), b = edge_end<D>(e, 1);
+        G[NV + e][a][b] += 4.0;
+        G[NV + e][b][a] += 4.0;
+    }
+    std::vector<float> tab;
+    for (int m = 0; m < NN; ++m)
+        for (int j = m; j < NN; ++j) {
+            double Ct[4][4];
+            for (int p = 0; p < NV; ++p)
+                for (int q = 0; q < NV; ++q) {
+                    double s = 0.0;
+                    for (int r = 0; r < NV; ++r)
+                        for (int t = 0; t < NV; ++t) s += (r == t ? 2.0 : 1.0) * G[m][r][p] * G[j][t][q];
+                    Ct[p][q] = s;
+                }
+            auto cf = [&](int a, int b) { return Ct[a][b] - Ct[0][b] - Ct[a][0] + Ct[0][0]; };
+            for (int p = 1; p <= D; ++p)
+                for (int q = p; q <= D; ++q) tab.push_back((float)(p == q ? cf(p, p) : cf(p, q) + cf(q, p)));
+        }
+    // the P2 mass matrices of c_m2 / c_m2t above (host copies), divided by 420 / 180
+    static const double m3[10][10] = {
+        {6, 1, 1, 1, -6, -6, -6, -4, -4, -4},     {1, 6, 1, 1, -6, -4, -4, -6, -6, -4},
+        {1, 1, 6, 1, -4, -6, -4, -6, -4, -6},     {1, 1, 1, 6, -4, -4, -6, -4, -6, -6},
+        {-6, -6, -4, -4, 32, 16, 16, 16, 16, 8},  {-6, -4, -6, -4, 16, 32, 16, 16, 8, 16},
+        {-6, -4, -4, -6, 16, 16, 32, 8, 16, 16},  {-4, -6, -6, -4, 16, 16, 8, 32, 16, 16},
+        {-4, -6, -4, -6, 16, 8, 16, 16, 32, 16},  {-4, -4, -6, -6, 8, 16, 16, 16, 16, 32}};
+    static const double m2[6][6] = {{6, -1, -1, -4, 0, 0},  {-1, 6, -1, 0, -4, 0},  {-1, -1, 6, 0, 0, -4},
+                                    {-4, 0, 0, 32, 16, 16}, {0, -4, 0, 16, 32, 16}, {0, 0, -4, 16, 16, 32}};
+    for (int m = 0; m < NN; ++m)
+        for (int j = 0; j < NN; ++j) tab.push_back((float)(D == 3 ? m3[m][j] / 420.0 : m2[m][j] / 180.0));
+    return tab;
+}
+
+void launch_mf_cells(mpet_ctx* c, double dt) {
+    const MatCoef P = make_coef(c, dt);
+    const bool f32 = c->prm.precision == MPET_PRECISION_MIXED;
+    const size_t bytes = (size_t)c->nc * 8 * (f32 ? 4 : 8);
+    if (!c->mf_cell) {
+        if (!device_fits(c, bytes)) return;  // optional: the CSR level stands in
+        c->mf_cell = c->pool.alloc<unsigned char>((int64_t)bytes);
+        const std::vector<float> tab = c->dim == 2 ? mf_table<2>() : mf_table<3>();
+        c->mf_tab = c->pool.alloc<float>((int64_t)tab.size());
+        MPET_CUDA(cudaMemcpyAsync(c->mf_tab, tab.data(), sizeof(float) * tab.size(), cudaMemcpyHostToDevice,
+                                  c->stream));
+        MPET_CUDA(cudaStreamSynchronize(c->stream));
+    }
+    const int G = grid_for(c->nc, 256);
+    if (c->dim == 2) {
+        if (f32) k_mf_cells<float, 2><<<G, 256, 0, c->stream>>>(c->nc, c->geo, c->cell_nodes, c->node_bc, P.prec_mu,
+                                                                P.prec_shift, (float*)c->mf_cell);
+        else k_mf_cells<double, 2><<<G, 256, 0, c->stream>>>(c->nc, c->geo, c->cell_nodes, c->node_bc, P.prec_mu,
+                                                             P.prec_shift, (double*)c->mf_cell);
+    } else {
+        if (f32) k_mf_cells<float, 3><<<G, 256, 0, c->stream>>>(c->nc, c->geo, c->cell_nodes, c->node_bc, P.prec_mu,
+                                                                P.prec_shift, (float*)c->mf_cell);
+        else k_mf_cells<double, 3><<<G, 256, 0, c->stream>>>(c->nc, c->geo, c->cell_nodes, c->node_bc, P.prec_mu,
+                                                             P.prec_shift, (double*)c->mf_cell);
+    }
+    MPET_CHECK_LAUNCH();
+}
+
 void launch_rhs(mpet_ctx* c, double dt, const double* up_prev, double* b) {
     RhsArgs A{};
     A.nnodes = c->nnodes;

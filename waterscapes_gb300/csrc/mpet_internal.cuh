@@ -157,6 +157,7 @@ struct Csr {
 
 struct AmgLevel {
     Csr A, P, R;       // P: n x nc (prolongation), R = P^T
+    bool mf = false;   // products with A formed matrix-free from per-cell data (first displacement level)
     double* dinv64 = nullptr;
     float* dinv32 = nullptr;
     double rho = 1.0;  // spectral radius estimate of D^-1 A
@@ -319,6 +320,12 @@ struct mpet_ctx {
     double* adj_loss = nullptr;   // misfit value (1 double)
     double* elem_buf = nullptr;   // staged per-cell element data of the assembly, or null
     bool u_elast = false;         // displacement preconditioner block: elasticity AMG (else Laplacian)
+    // matrix-free first level of the displacement hierarchy: per-cell data (nc x 8
+    // floats or doubles), the float tables of its element operator, and the choice
+    void* mf_cell = nullptr;
+    float* mf_tab = nullptr;
+    int mf_mode = -1;             // -1 autotuned, 0 CSR, 1 matrix-free (test hook)
+    float mf_ms[2] = {0.f, 0.f};  // autotuner: Chebyshev product with the CSR level / matrix-free
     bool gmres = false;           // solves by restarted GMRES (non-symmetric system)
     // constant-pressure constraints (int p_k = 0, multiplier p_null_k): networks, the P1
     // load vector (int phi_v), W_k = A^-1 B_k^T (nq x N), the inverse of B W, multipliers
@@ -470,6 +477,9 @@ void launch_robin_matrix(mpet_ctx* c, double dt);
 // assemble.cu
 void launch_assemble_matrix(mpet_ctx* c, double dt, bool apply_bc, bool write32);
 void launch_assemble_prec_blocks(mpet_ctx* c, double dt);
+// per-cell data of the matrix-free first displacement level (c->mf_cell, c->mf_tab);
+// leaves c->mf_cell null when HBM is short
+void launch_mf_cells(mpet_ctx* c, double dt);
 void setup_network_modes(mpet_ctx* c, double dt);
 void set_instances(mpet_ctx* c, int ninst, const int32_t* vertex_inst_host);
 void launch_rhs(mpet_ctx* c, double dt, const double* up_prev, double* b);

@@ -1002,12 +1002,96 @@ static void launch_spmv(mpet_ctx* c, const Csr& A, const T* va, const T* x, cons
     c->n_launch++;
 }
 
-// operator of an AMG level: its CSR copy, or the displacement block of the system
+// Matrix-free product with the first displacement level w (grad u, grad v)
+// (+ shift (u, v)) on the 4-wide node layout: a thread owns a P2 node, walks its
+// incident cells (node -> cell incidence) and adds its row of each cell's element
+// operator, K_mj = sum_{p <= q} T6[mj][pq] a_pq + sh M2[m][j] with the cell's
+// a_pq = w |T| kappa (b_p . b_q) and sh = shift |T| (k_mf_cells).  Dirichlet rows
+// are the identity and Dirichlet columns are skipped (the cell's mask), as in the
+// CSR block.  Reads per product: the incidence, 8 values and NN node ids per
+// incident cell (mostly from L2) and the gathered x, against nnz (value + column)
+// of the CSR block.
+template <typename T, int D, class Epi>
+__global__ void __launch_bounds__(256) k_p2lap_mf(int64_t nnodes, const int64_t* __restrict__ inc_ptr,
+                                                  const int32_t* __restrict__ inc,
+                                                  const int32_t* __restrict__ cell_nodes, const T* __restrict__ cdat,
+                                                  const uint8_t* __restrict__ node_bc, const float* __restrict__ tab,
+                                                  const T* __restrict__ x, Epi epi) {
+    constexpr int NN = Simplex<D>::NN, NQ = D * (D + 1) / 2, NP = NN * (NN + 1) / 2;
+    __shared__ float s_t6[NP * NQ];
+    __shared__ float s_m2[NN * NN];
+    for (int e = threadIdx.x; e < NP * NQ + NN * NN; e += blockDim.x) {
+        if (e < NP * NQ) s_t6[e] = tab[e];
+        else s_m2[e - NP * NQ] = tab[e];
+    }
+    __syncthreads();
+    double r0 = 0.0, r1 = 0.0;
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < nnodes;
+         i += (int64_t)gridDim.x * blockDim.x) {
+        const typename Epi::Pre pre = epi.pre(i);
+        T acc[4] = {T(0), T(0), T(0), T(0)};
+        if (node_bc[i]) {
+            VecIO<T, 4>::load(x, i, acc);
+        } else {
+            const int64_t e1 = inc_ptr[i + 1];
+            for (int64_t it = inc_ptr[i]; it < e1; ++it) {
+                const int32_t packed = __ldg(inc + it);
+                const int64_t cell = packed >> 4;
+                const int m = packed & 15;
+                T a[8];
+#pragma unroll
+                for (int q = 0; q < 8; ++q) a[q] = __ldg(cdat + 8 * cell + q);
+                uint32_t mask;
+                if constexpr (sizeof(T) == 4) mask = __float_as_uint(a[7]);
+                else mask = (uint32_t)__double_as_longlong(a[7]);
+                const int32_t* cn = cell_nodes + NN * cell;
+#pragma unroll
+                for (int j = 0; j < NN; ++j) {
+                    if ((mask >> j) & 1u) continue;
+                    const int lo = m < j ? m : j, hi = m < j ? j : m;
+                    const int pr = lo * NN - lo * (lo - 1) / 2 + (hi - lo);
+                    T coef = a[NQ] * (T)s_m2[m * NN + j];
+#pragma unroll
+                    for (int q = 0; q < NQ; ++q) coef += (T)s_t6[pr * NQ + q] * a[q];
+                    T xv[4];
+                    VecIO<T, 4>::load(x, __ldg(cn + j), xv);
+#pragma unroll
+                    for (int k = 0; k < 4; ++k) acc[k] += coef * xv[k];
+                }
+            }
+        }
+        epi.apply(i, acc, pre, r0, r1);
+    }
+}
+
+template <typename T, class Epi>
+static void launch_p2lap_mf(mpet_ctx* c, const T* x, const Epi& epi) {
+    static_assert(Epi::kRed == 0, "no reductions in the matrix-free level");
+    int blocks = grid_for(c->nnodes, 256);
+    if (blocks > 152 * 16) blocks = 152 * 16;
+    if (c->dim == 2)
+        k_p2lap_mf<T, 2, Epi><<<blocks, 256, 0, c->stream>>>(c->nnodes, c->inc_ptr, c->inc, c->cell_nodes,
+                                                             (const T*)c->mf_cell, c->node_bc, c->mf_tab, x, epi);
+    else
+        k_p2lap_mf<T, 3, Epi><<<blocks, 256, 0, c->stream>>>(c->nnodes, c->inc_ptr, c->inc, c->cell_nodes,
+                                                             (const T*)c->mf_cell, c->node_bc, c->mf_tab, x, epi);
+    MPET_CHECK_LAUNCH();
+    c->n_launch++;
+}
+
+// operator of an AMG level: its CSR copy, the matrix-free first displacement
+// level, or the displacement block of the system
 template <typename T, int NV, class Epi>
 static void level_spmv(mpet_ctx* c, const AmgLevel& L, const T* x, const Epi& epi) {
     if constexpr (NV == 1) {
         if (L.nb_uu) {
             launch_nb_uu<T>(c, *c->A.nb, x, epi);
+            return;
+        }
+    }
+    if constexpr (NV == 4) {
+        if (L.mf) {
+            launch_p2lap_mf<T>(c, x, epi);
             return;
         }
     }
@@ -1413,7 +1497,12 @@ static void profile_levels(mpet_ctx* c, AmgHier& h, int reps, double* ms, double
             continue;
         }
         const double nc = (double)h.lev[k + 1].A.n, vecc = nc * NV * sv;
-        const double mA = L.A.nnz * (sv + 4.0) + (n + 1) * 8.0;
+        // a product with A: the CSR entries and row pointers, or (matrix-free) the
+        // incidence and per-cell node ids (NN each), the per-cell data, the row
+        // pointers of the incidence and the Dirichlet flags, once each
+        const double nn_cell = c->dim == 3 ? 10.0 : 6.0;
+        const double mA = L.mf ? (double)c->nc * (2.0 * nn_cell * 4.0 + 8.0 * sv) + n + (n + 1) * 8.0
+                               : L.A.nnz * (sv + 4.0) + (n + 1) * 8.0;
         double b = 3 * vec + dv;                              // first Chebyshev step (no product)
         b += (2 * s - 1) * (mA + 5 * vec + dv);               // the other 2s - 1 smoothing products
         b += mA + 3 * vec;                                    // residual
@@ -2743,6 +2832,45 @@ static void upload_csr(mpet_ctx* c, const HostCsr& h, Csr& d, bool fp32) {
     build_sell(c, d, fp32, false);
 }
 
+// First displacement level: matrix-free products when the per-cell data exist and
+// (autotuned) a Chebyshev product is faster that way than with the tuned CSR
+// layout (median of 5 launches from a flushed L2), or as forced by mf_mode.
+template <typename T>
+static void choose_mf(mpet_ctx* c, AmgHier& h) {
+    AmgLevel& L = h.lev[0];
+    L.mf = false;
+    c->mf_ms[0] = c->mf_ms[1] = 0.f;
+    if (!c->mf_cell || c->mf_mode == 0) return;
+    if (c->mf_mode == 1) {
+        L.mf = true;
+        return;
+    }
+    constexpr size_t kFlush = 256u << 20;
+    if (!c->l2_flush) c->l2_flush = c->pool.alloc<unsigned char>(kFlush);
+    const int64_t l0 = c->n_launch;
+    const EpiCheb<T, 4> e{(const T*)L.b, (const T*)L.x, (T*)L.d, (T*)L.t0, dinv_of<T>(L), T(0.5), T(0.5)};
+    float med[2];
+    for (int v = 0; v < 2; ++v) {
+        L.mf = v == 1;
+        level_spmv<T, 4>(c, L, (const T*)L.x, e);
+        float t[5];
+        for (int q = 0; q < 5; ++q) {
+            MPET_CUDA(cudaMemsetAsync(c->l2_flush, q, kFlush, c->stream));
+            MPET_CUDA(cudaEventRecord(c->ev0, c->stream));
+            level_spmv<T, 4>(c, L, (const T*)L.x, e);
+            MPET_CUDA(cudaEventRecord(c->ev1, c->stream));
+            MPET_CUDA(cudaEventSynchronize(c->ev1));
+            MPET_CUDA(cudaEventElapsedTime(&t[q], c->ev0, c->ev1));
+        }
+        std::sort(t, t + 5);
+        med[v] = t[2];
+    }
+    L.mf = med[1] < med[0];
+    c->mf_ms[0] = med[0];
+    c->mf_ms[1] = med[1];
+    c->n_launch = l0;
+}
+
 void upload_amg(mpet_ctx* c, AmgHier& h, const HostAmg& ha, int nvec, bool fp32) {
     h.nvec = nvec;
     h.cheb_degree = c->prm.amg_cheb_degree > 0 ? c->prm.amg_cheb_degree : 4;
@@ -2778,6 +2906,7 @@ void upload_amg(mpet_ctx* c, AmgHier& h, const HostAmg& ha, int nvec, bool fp32)
     }
     if (nvec == 4) {
         if (fp32) autotune_hier<float, 4>(c, h); else autotune_hier<double, 4>(c, h);
+        if (fp32) choose_mf<float>(c, h); else choose_mf<double>(c, h);
     } else {
         if (fp32) autotune_hier<float, 1>(c, h); else autotune_hier<double, 1>(c, h);
     }
