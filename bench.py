@@ -240,11 +240,18 @@ def replica_rate(ms_local, steps):
 
 
 def prec_form(solver):
-    """Displacement block the preconditioner runs (elasticity AMG or vector Laplacian)."""
+    """Displacement block the preconditioner runs (elasticity AMG or vector Laplacian,
+    with a matrix-free or CSR first level and the autotuner's timings of both)."""
     import ctypes
     v = ctypes.c_int32()
     solver.ctx.call("mpet_get_prec_info", ctypes.byref(v))
-    return "elasticity AMG (rigid-body modes)" if v.value else "vector Laplacian AMG"
+    if v.value:
+        return "elasticity AMG (rigid-body modes)"
+    used = ctypes.c_int32()
+    ms = (ctypes.c_float * 2)()
+    solver.ctx.call("mpet_get_prec_matrix_free", ctypes.byref(used), ms)
+    return "vector Laplacian AMG, %s first level (Chebyshev product: CSR %.4f ms, matrix-free %.4f ms)" % (
+        "matrix-free" if used.value else "CSR", ms[0], ms[1])
 
 
 def spmv_tuning(solver, fp64=False):
@@ -256,6 +263,16 @@ def spmv_tuning(solver, fp64=False):
     names = ["register/4", "register/8", "staged/4", "staged/8", "sell32/4", "sell32/8", "node-block"]
     return {"ms": {names[v]: round(float(ms[v]), 4) for v in range(7) if ms[v] > 0},
             "chosen": names[6 if ch.value == 8 else ch.value]}
+
+
+def prec_setup_ms(solver):
+    """Split of the last preconditioner set-up (ms): GPU block assembly, displacement
+    and pressure hierarchies (download + host set-up), uploads + autotuning."""
+    import ctypes
+    ms = np.zeros(4)
+    solver.ctx.call("mpet_get_setup_timing", ms.ctypes.data_as(ctypes.c_void_p))
+    return {"blocks_gpu": round(ms[0], 1), "u_hierarchy_host": round(ms[1], 1),
+            "p_hierarchies_host": round(ms[2], 1), "upload_autotune": round(ms[3], 1)}
 
 
 def launches(solver):
@@ -571,17 +588,45 @@ def batch_run(args):
         errs.append(float(torch.linalg.norm(finals[i] - ref) / torch.linalg.norm(ref)))
         del s
     sizes = [p.mesh.num_cells() // 6 for p in problems]
+    ninst, bN, bnnz, tuning = bs.ninst, bs.N, bs.nnz, spmv_tuning(bs)
+    del bs
+    torch.cuda.empty_cache()
+    seq = None
+    if args.sequential_steps > 0:
+        # the same instances solved one after another (each its own solver, matrix and AMG
+        # built before its timed steps), mixed path: one untimed step, then the timed ones
+        t_solve = 0.0
+        its_seq = []
+        for p in problems:
+            p.time.assign(0.0)
+            s = MPETSolver(p, dict(params, T=1e9))
+            g = s.solve_direct()
+            next(g)
+            torch.cuda.synchronize()
+            e0.record(s._stream)
+            for _ in range(args.sequential_steps):
+                next(g)
+            e1.record(s._stream)
+            torch.cuda.synchronize()
+            t_solve += e0.elapsed_time(e1) / 1e3
+            its_seq.append(s.solver_monitor["niter"][-1])
+            del g, s
+        seq = {"value": len(problems) * args.sequential_steps / t_solve, "unit": "instance-steps/s",
+               "steps_per_instance": args.sequential_steps, "after_untimed_steps": 1,
+               "iterations_last_step": {"min": int(min(its_seq)), "median": float(np.median(its_seq)),
+                                        "max": int(max(its_seq))}}
     out = {"metric": "batched MPET instance-steps/s (A=2 instances in one union mesh)",
-           "value": bs.ninst * args.steps / (ms / 1e3), "unit": "instance-steps/s",
+           "value": ninst * args.steps / (ms / 1e3), "unit": "instance-steps/s",
            "ms_per_step": ms / args.steps, "steps": args.steps, "warmup": args.warmup,
            "config": {"workload": "%d Kuhn cubes n^3 x 6 tets, n in [%d, %d] (seeded), A=2, dt=0.02"
-                      % (bs.ninst, args.n_min, args.n_max), "N": bs.N, "nnz": bs.nnz,
+                      % (ninst, args.n_min, args.n_max), "N": bN, "nnz": bnnz,
                       "cells": int(sum(p.mesh.num_cells() for p in problems)),
                       "n_mean": float(np.mean(sizes) ** (1 / 3.0))},
            "iterations_per_step": its, "worst_instance_relres": worst,
            "fp64_single_instance_check": {"instances": check, "rel_err": errs},
            "setup_s": {"meshes": t_mesh, "union_and_pattern": t_setup, "assemble_plus_amg": t_asm},
-           "spmv_tuning": spmv_tuning(bs)}
+           "sequential": seq,
+           "spmv_tuning": tuning}
     print(json.dumps(out))
 
 
@@ -651,7 +696,10 @@ def main():
     ap.add_argument("--instances", type=int, default=256)
     ap.add_argument("--n-min", type=int, default=8)
     ap.add_argument("--n-max", type=int, default=32)
+    ap.add_argument("--sequential-steps", type=int, default=3,
+                    help="batch mode: also time this many steps of every instance solved alone (0: skip)")
     ap.add_argument("--cheb-degree", type=int, default=None, help="override amg_cheb_degree")
+    ap.add_argument("--coarse-size", type=int, default=None, help="override amg_coarse_size")
     ap.add_argument("--prec-u-form", default=None, choices=["elasticity", "laplacian"],
                     help="override the displacement block of the preconditioner")
     ap.add_argument("--inner-rtol", type=float, default=None, help="override inner_rtol")
@@ -730,6 +778,8 @@ def main():
         base["amg_cheb_degree"] = args.cheb_degree
     if args.inner_rtol is not None:
         base["inner_rtol"] = args.inner_rtol
+    if args.coarse_size is not None:
+        base["amg_coarse_size"] = args.coarse_size
     if args.prec_u_form is not None:
         base["prec_u_form"] = args.prec_u_form
     t0 = time.perf_counter()
@@ -837,7 +887,8 @@ def main():
         "rel_err_mixed_vs_fp64": rel_err,
         "iterations_per_step": {"mixed": its_mixed, "fp64": res.get("fp64", {}).get("iterations")},
         "step_semantics": {"ms_per_step": step_ms, "assemble_ms": asm_ms},
-        "setup_s": {"mesh_dofmap_pattern": t_setup, "assemble_plus_amg": t_asm_amg},
+        "setup_s": {"mesh_dofmap_pattern": t_setup, "assemble_plus_amg": t_asm_amg,
+                    "preconditioner_ms": prec_setup_ms(sol)},
         "spmv": spmv,
         "spmv_tuning": spmv_tuning(sol),
         "spmv_tuning_fp64_residual": spmv_tuning(sol, fp64=True),

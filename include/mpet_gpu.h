@@ -267,6 +267,13 @@ int mpet_rhs(mpet_ctx* ctx, double dt, const double* up_prev, double* b);
  * (prec_u_form 1 and applicable), 0 = the vector Laplacian. */
 int mpet_get_prec_info(mpet_ctx* ctx, int32_t* u_elasticity);
 
+/* Where the last mpet_setup_preconditioner went (ms, wall clock): ms4_host[0]
+ * the preconditioner blocks assembled on the GPU, [1] the displacement
+ * hierarchy (download + host set-up), [2] the pressure hierarchies (download
+ * + host set-up), [3] uploads and SpMV autotuning.  No reference counterpart
+ * (measurement of what hypre's set-up does inside PETSc, mpetsolver.py:507). */
+int mpet_get_setup_timing(mpet_ctx* ctx, double* ms4_host);
+
 /* Block-diagonal preconditioner (mpetsolver.py:264-271): one smoothed-
  * aggregation AMG hierarchy per diagonal block, built for this dt. */
 int mpet_setup_preconditioner(mpet_ctx* ctx, double dt);

@@ -121,6 +121,7 @@ SIGNATURES = {
     "mpet_profile_vcycle": [_P, _I32, _I32, ctypes.POINTER(_I32), _P, _P],
     "mpet_solve": [_P, _P, _P, ctypes.POINTER(MpetStats)],
     "mpet_get_prec_info": [_P, ctypes.POINTER(_I32)],
+    "mpet_get_setup_timing": [_P, _P],
     "mpet_step": [_P, _D, _P, _P, ctypes.POINTER(MpetStats)],
     "mpet_apply_preconditioner": [_P, _I32, _P, _P],
     "mpet_residual": [_P, _P, _P, _P, _P],

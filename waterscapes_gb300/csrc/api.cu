@@ -82,6 +82,7 @@ int mpet_ctx_destroy(mpet_ctx* c) {
     if (c->ev_fork) cudaEventDestroy(c->ev_fork);
     c->pool.free_all();
     if (c->sc_host) cudaFreeHost(c->sc_host);
+    if (c->loop_ctl_host) cudaFreeHost(c->loop_ctl_host);
     if (c->inst_host) cudaFreeHost(c->inst_host);
     if (c->bsc_host) cudaFreeHost(c->bsc_host);
     if (c->bdone_host) cudaFreeHost(c->bdone_host);
@@ -535,9 +536,15 @@ int mpet_setup_preconditioner(mpet_ctx* c, double dt) {
     require(c->setup_done, MPET_ERR_STATE, "mpet_setup must come first");
     require(dt > 0.0, MPET_ERR_INVALID, "dt must be positive");
     destroy_minres_graph(c);
+    using clk = std::chrono::steady_clock;
+    auto since = [](clk::time_point t) { return std::chrono::duration<double, std::milli>(clk::now() - t).count(); };
+    auto t0 = clk::now();
     setup_network_modes(c, dt);
     launch_assemble_prec_blocks(c, dt);
     if (c->prm.prec_u_form != 1) launch_mf_cells(c, dt);
+    MPET_CUDA(cudaStreamSynchronize(c->stream));
+    c->setup_ms[0] = since(t0);  // block assembly on the GPU
+    t0 = clk::now();
     const bool fp32 = c->prm.precision == MPET_PRECISION_MIXED;
     auto fetch = [&](const Csr& d, HostCsr& h) {
         h.n = d.n;
@@ -617,17 +624,36 @@ int mpet_setup_preconditioner(mpet_ctx* c, double dt) {
         } else {
             amg_setup_host(h, nullptr, c->prm.amg_theta, cs, 12, ha);
         }
+        c->setup_ms[1] = since(t0);  // download + host hierarchy of the displacement block
+        t0 = clk::now();
         upload_amg(c, c->amg_u, ha, 4, fp32);
+        c->setup_ms[3] = since(t0);  // upload + autotuning
+    } else {
+        c->setup_ms[1] = since(t0);
+        c->setup_ms[3] = 0.0;
     }
+    t0 = clk::now();
+    double t_up = 0.0;
     for (int a = 0; a < c->J; ++a) {
         HostCsr h;
         fetch(c->Pp[a], h);
         HostAmg ha;
         amg_setup_host(h, nullptr, c->prm.amg_theta, cs, 12, ha);
+        const auto tu = clk::now();
         upload_amg(c, c->amg_p[a], ha, 1, fp32);
+        t_up += since(tu);
     }
+    c->setup_ms[2] = since(t0) - t_up;  // download + host hierarchies of the pressure blocks
+    c->setup_ms[3] += t_up;
     c->precond_ready = true;
     c->prec_dt = dt;
+    API_END(c)
+}
+
+int mpet_get_setup_timing(mpet_ctx* c, double* ms4) {
+    API_BEGIN(c)
+    require(ms4, MPET_ERR_INVALID, "NULL argument");
+    for (int k = 0; k < 4; ++k) ms4[k] = c->setup_ms[k];
     API_END(c)
 }
 

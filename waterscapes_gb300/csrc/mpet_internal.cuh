@@ -367,7 +367,9 @@ struct mpet_ctx {
 
     // MINRES iterations replayed from a CUDA graph (3 iterations per launch)
     cudaStream_t cap_stream = nullptr;
-    cudaGraphExec_t mr_graph = nullptr;
+    cudaGraphExec_t mr_graph = nullptr;  // whole inner solve: WHILE node over 3 iterations
+    void* loop_ctl = nullptr;            // device loop control (target, budget, iterations)
+    void* loop_ctl_host = nullptr;       // pinned copy
     int64_t mr_graph_launches = 0;  // kernels per graph launch
 
     // batch of independent instances in one mesh (ninst = 0: one instance):
@@ -422,6 +424,9 @@ struct mpet_ctx {
     // timing
     cudaEvent_t ev0 = nullptr, ev1 = nullptr;
     double t_inner_ms = 0.0, t_solve_ms = 0.0;  // MINRES graph replays / whole solves
+    // last preconditioner set-up (ms): block assembly (GPU), displacement hierarchy
+    // (download + host), pressure hierarchies (download + host), uploads + autotuning
+    double setup_ms[4] = {0, 0, 0, 0};
     int64_t n_inner_its = 0;
     cudaEvent_t ev_in0 = nullptr, ev_in1 = nullptr, ev_sv0 = nullptr, ev_sv1 = nullptr;
     int64_t n_spmv = 0, n_launch = 0;

@@ -380,8 +380,12 @@ __global__ void k_sell_fill(int64_t n, int64_t nslices, const int64_t* __restric
 // warp), gathers the 3 displacement or J pressure entries of x and updates
 // its 3 or J accumulators.  JM is a compile-time bound on J (loops unrolled).
 // UU: the displacement block only (u slices, node columns), x of length Nu.
+// FP64 instances are register-bound (each 3 x 3 block is 9 doubles): they load one
+// block per iteration, are held to 80 registers (3 resident 256-thread blocks per
+// SM) and run as one wave of resident blocks (the reduction partials past the grid
+// are written as zeros).
 template <typename T, int JM, class Epi, bool UU = false>
-__global__ void __launch_bounds__(256) k_spmv_nb(int64_t nnodes, int64_t nv, int64_t Nu, int J, int64_t nsu,
+__global__ void __launch_bounds__(256, sizeof(T) == 8 ? 3 : 1) k_spmv_nb(int64_t nnodes, int64_t nv, int64_t Nu, int J, int64_t nsu,
                                                  int64_t ns, const NbSlice* __restrict__ sl,
                                                  const int32_t* __restrict__ perm, const int32_t* __restrict__ cols,
                                                  const T* __restrict__ vals, const T* __restrict__ x, Epi epi,
@@ -404,7 +408,7 @@ __global__ void __launch_bounds__(256) k_spmv_nb(int64_t nnodes, int64_t nv, int
 #pragma unroll
                 for (int r = 0; r < 3; ++r) pre[r] = epi.pre(3 * node + r);
             T acc[3] = {T(0), T(0), T(0)};
-#pragma unroll 2
+#pragma unroll(sizeof(T) == 8 ? 1 : 2)
             for (int k = 0; k < S.w2; ++k) {
                 const int64_t j = __ldcs(c2 + (int64_t)k * 32);
                 T b[9];
@@ -440,7 +444,7 @@ __global__ void __launch_bounds__(256) k_spmv_nb(int64_t nnodes, int64_t nv, int
 #pragma unroll
             for (int a = 0; a < JM; ++a) acc[a] = T(0);
             const int B2 = 3 * J;
-#pragma unroll 2
+#pragma unroll(sizeof(T) == 8 ? 1 : 2)
             for (int k = 0; k < S.w2; ++k) {
                 const int64_t j = __ldcs(c2 + (int64_t)k * 32);
                 const T x0 = x[3 * j], x1 = x[3 * j + 1], x2 = x[3 * j + 2];
@@ -474,12 +478,13 @@ __global__ void __launch_bounds__(256) k_spmv_nb(int64_t nnodes, int64_t nv, int
     }
     if constexpr (Epi::kRed > 0) {
         __shared__ double sh[8];
-        double t0 = block_sum256(r0, sh);
-        if (threadIdx.x == 0) partials[blockIdx.x] = t0;
-        if constexpr (Epi::kRed > 1) {
-            double t1 = block_sum256(r1, sh);
-            if (threadIdx.x == 0) partials[NB_RED + blockIdx.x] = t1;
-        }
+        const double t0 = block_sum256(r0, sh);
+        const double t1 = Epi::kRed > 1 ? block_sum256(r1, sh) : 0.0;
+        if (threadIdx.x == 0)
+            for (int p = blockIdx.x; p < NB_RED; p += gridDim.x) {
+                partials[p] = p == (int)blockIdx.x ? t0 : 0.0;
+                if (Epi::kRed > 1) partials[NB_RED + p] = p == (int)blockIdx.x ? t1 : 0.0;
+            }
     }
 }
 
@@ -901,11 +906,27 @@ const double* nb_vals<double>(const NodeBlocks& nb) { return nb.v64; }
 template <>
 const float* nb_vals<float>(const NodeBlocks& nb) { return nb.v32; }
 
+// resident 256-thread blocks of a kernel on the current device (one wave), at most NB_RED
+template <class K>
+static int one_wave(K kern) {
+    int per_sm = 0, nsm = 0, dev = 0;
+    MPET_CUDA(cudaGetDevice(&dev));
+    MPET_CUDA(cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev));
+    MPET_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, 256, 0));
+    const int g = nsm * (per_sm > 0 ? per_sm : 1);
+    return g < NB_RED ? g : NB_RED;
+}
+
 template <typename T, class Epi>
 static void launch_nb(mpet_ctx* c, const NodeBlocks& nb, const T* x, const Epi& epi) {
     const int64_t ns = nb.nsu + nb.nsp;
     int blocks = Epi::kRed > 0 ? NB_RED : grid_for(ns * 32, 256);
     if (Epi::kRed == 0 && blocks > 152 * 16) blocks = 152 * 16;
+    if (sizeof(T) == 8 && Epi::kRed > 0) {
+        static int wave = 0;  // per instantiation (one device type per process)
+        if (wave == 0) wave = one_wave(k_spmv_nb<T, 4, Epi>);
+        blocks = wave;
+    }
     const int J = c->J;
     cudaStream_t st = c->stream;
     const T* v = nb_vals<T>(nb);
@@ -1688,9 +1709,102 @@ static void capture_graph(mpet_ctx* c, F body, cudaGraphExec_t* out, int64_t* la
     }
 }
 
+// Whole inner solves as one graph launch: a WHILE conditional node whose body
+// is three MINRES iterations followed by a one-thread kernel that counts the
+// iterations and keeps the loop going while no breakdown is flagged, the
+// target is not reached and the iteration budget lasts (the test the host
+// made after every three iterations before).  Target and budget live in
+// device memory (LoopCtl), written before each launch.
+struct LoopCtl {
+    double target;
+    int max_iters;
+    int iters;
+};
+
+__global__ void k_mr_continue(cudaGraphConditionalHandle h, const MinresScalars* sc, LoopCtl* ctl) {
+    const int it = ctl->iters + 3;
+    ctl->iters = it;
+    const bool go = sc->flag == 0.0 && !(sc->rel <= ctl->target) && it < ctl->max_iters;
+    cudaGraphSetConditional(h, go ? 1u : 0u);
+}
+
+// batches: continue while some instance is not done (done covers breakdowns)
+__global__ void k_bmr_continue(cudaGraphConditionalHandle h, int ni, const double* done, LoopCtl* ctl) {
+    __shared__ int open;
+    if (threadIdx.x == 0) open = 0;
+    __syncthreads();
+    for (int i = threadIdx.x; i < ni; i += blockDim.x)
+        if (done[i] == 0.0) open = 1;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        const int it = ctl->iters + 3;
+        ctl->iters = it;
+        cudaGraphSetConditional(h, (open && it < ctl->max_iters) ? 1u : 0u);
+    }
+}
+
+// Builds a graph of one WHILE node (default 1, reset every launch) whose body is
+// captured from body(c, handle) on the capture stream, and instantiates it.
+template <class F>
+static void build_while_graph(mpet_ctx* c, F body, cudaGraphExec_t* out, int64_t* launches, const char* what) {
+    if (!c->cap_stream) MPET_CUDA(cudaStreamCreateWithFlags(&c->cap_stream, cudaStreamNonBlocking));
+    cudaGraph_t g = nullptr;
+    MPET_CUDA(cudaGraphCreate(&g, 0));
+    cudaGraphConditionalHandle h;
+    cudaError_t e = cudaGraphConditionalHandleCreate(&h, g, 1, cudaGraphCondAssignDefault);
+    cudaGraphNode_t node;
+    cudaGraphNodeParams np{};
+    np.type = cudaGraphNodeTypeConditional;
+    np.conditional.handle = h;
+    np.conditional.type = cudaGraphCondTypeWhile;
+    np.conditional.size = 1;
+    if (e == cudaSuccess) e = cudaGraphAddNode(&node, g, nullptr, nullptr, 0, &np);
+    if (e != cudaSuccess) {
+        cudaGraphDestroy(g);
+        fail(MPET_ERR_CUDA, std::string(what) + " conditional node: " + cudaGetErrorString(e));
+    }
+    cudaGraph_t bodyg = np.conditional.phGraph_out[0];
+    cudaStream_t saved = c->stream;
+    const int64_t l0 = c->n_launch, s0 = c->n_spmv;
+    c->stream = c->cap_stream;
+    e = cudaStreamBeginCaptureToGraph(c->cap_stream, bodyg, nullptr, nullptr, 0, cudaStreamCaptureModeThreadLocal);
+    if (e == cudaSuccess) {
+        try {
+            body(c, h);
+        } catch (...) {
+            cudaGraph_t tmp = nullptr;
+            cudaStreamEndCapture(c->cap_stream, &tmp);
+            c->stream = saved;
+            cudaGraphDestroy(g);
+            throw;
+        }
+        cudaGraph_t tmp = nullptr;
+        e = cudaStreamEndCapture(c->cap_stream, &tmp);
+    }
+    c->stream = saved;
+    *launches = c->n_launch - l0;
+    c->n_launch = l0;
+    c->n_spmv = s0;
+    if (e == cudaSuccess) e = cudaGraphInstantiate(out, g, 0);
+    cudaGraphDestroy(g);
+    if (e != cudaSuccess) {
+        *out = nullptr;
+        fail(MPET_ERR_CUDA, std::string(what) + " while-graph: " + cudaGetErrorString(e));
+    }
+}
+
 template <typename T>
 static void capture_minres_graph(mpet_ctx* c) {
-    capture_graph(c, [](mpet_ctx* cc) { minres_three<T>(cc); }, &c->mr_graph, &c->mr_graph_launches, "MINRES");
+    if (!c->loop_ctl) c->loop_ctl = c->pool.alloc<unsigned char>(sizeof(LoopCtl));
+    build_while_graph(
+        c,
+        [](mpet_ctx* cc, cudaGraphConditionalHandle h) {
+            minres_three<T>(cc);
+            k_mr_continue<<<1, 1, 0, cc->stream>>>(h, cc->sc, (LoopCtl*)cc->loop_ctl);
+            MPET_CHECK_LAUNCH();
+            cc->n_launch++;
+        },
+        &c->mr_graph, &c->mr_graph_launches, "MINRES");
 }
 
 void destroy_minres_graph(mpet_ctx* c) {
@@ -1700,26 +1814,31 @@ void destroy_minres_graph(mpet_ctx* c) {
     c->bmr_graph = nullptr;
 }
 
+// Launches a whole-solve graph with the given target and budget; the loop
+// control comes back to its pinned host copy (read after the caller's sync).
+static void run_while_graph(mpet_ctx* c, cudaGraphExec_t g, double target, int max_iters) {
+    LoopCtl* hc = (LoopCtl*)c->loop_ctl_host;
+    hc->target = target;
+    hc->max_iters = max_iters;
+    hc->iters = 0;
+    MPET_CUDA(cudaMemcpyAsync(c->loop_ctl, hc, sizeof(LoopCtl), cudaMemcpyHostToDevice, c->stream));
+    MPET_CUDA(cudaGraphLaunch(g, c->stream));
+    MPET_CUDA(cudaMemcpyAsync(hc, c->loop_ctl, sizeof(LoopCtl), cudaMemcpyDeviceToHost, c->stream));
+}
+
 template <typename T>
 static int minres_run(mpet_ctx* c, double target, int max_iters, int* iters_done) {
+    *iters_done = 0;
+    if (max_iters <= 0) return MPET_OK;
     if (!c->mr_graph) capture_minres_graph<T>(c);
-    int it = 0;
-    int status = MPET_OK;
-    while (it < max_iters) {
-        MPET_CUDA(cudaGraphLaunch(c->mr_graph, c->stream));
-        it += 3;
-        c->n_launch += c->mr_graph_launches;
-        c->n_spmv += 3;
-        MPET_CUDA(cudaMemcpyAsync(c->sc_host, c->sc, sizeof(MinresScalars), cudaMemcpyDeviceToHost, c->stream));
-        MPET_CUDA(cudaStreamSynchronize(c->stream));
-        if (c->sc_host->flag != 0.0) {
-            status = MPET_ERR_BREAKDOWN;
-            break;
-        }
-        if (c->sc_host->rel <= target) break;
-    }
+    run_while_graph(c, c->mr_graph, target, max_iters);
+    MPET_CUDA(cudaMemcpyAsync(c->sc_host, c->sc, sizeof(MinresScalars), cudaMemcpyDeviceToHost, c->stream));
+    MPET_CUDA(cudaStreamSynchronize(c->stream));
+    const int it = ((LoopCtl*)c->loop_ctl_host)->iters;
+    c->n_launch += c->mr_graph_launches * (it / 3);
+    c->n_spmv += it;
     *iters_done = it;
-    return status;
+    return c->sc_host->flag != 0.0 ? MPET_ERR_BREAKDOWN : MPET_OK;
 }
 
 // ---- rigid-motion modes ---------------------------------------------------------------
@@ -2153,33 +2272,35 @@ static void bminres_three(mpet_ctx* c) {
     }
 }
 
-// Replays the 3-iteration batched graph until every instance is done.
+// The batched inner solve as one graph launch (a WHILE node over three batched
+// iterations) until every instance is done or the budget is spent.
 template <typename T>
 static int bminres_run(mpet_ctx* c, int max_iters, int* iters_done) {
+    *iters_done = 0;
+    if (max_iters <= 0) return MPET_OK;
+    if (!c->loop_ctl) c->loop_ctl = c->pool.alloc<unsigned char>(sizeof(LoopCtl));
     if (!c->bmr_graph)
-        capture_graph(c, [](mpet_ctx* cc) { bminres_three<T>(cc); }, &c->bmr_graph, &c->bmr_graph_launches,
-                      "batched MINRES");
+        build_while_graph(
+            c,
+            [](mpet_ctx* cc, cudaGraphConditionalHandle h) {
+                bminres_three<T>(cc);
+                k_bmr_continue<<<1, 256, 0, cc->stream>>>(h, cc->ninst, cc->bdone, (LoopCtl*)cc->loop_ctl);
+                MPET_CHECK_LAUNCH();
+                cc->n_launch++;
+            },
+            &c->bmr_graph, &c->bmr_graph_launches, "batched MINRES");
     const int ni = c->ninst;
-    int it = 0;
-    int status = MPET_OK;
-    while (it < max_iters) {
-        MPET_CUDA(cudaGraphLaunch(c->bmr_graph, c->stream));
-        it += 3;
-        c->n_launch += c->bmr_graph_launches;
-        c->n_spmv += 3;
-        MPET_CUDA(cudaMemcpyAsync(c->bdone_host, c->bdone, sizeof(double) * ni, cudaMemcpyDeviceToHost, c->stream));
-        MPET_CUDA(cudaMemcpyAsync(c->bsc_host, c->bsc, sizeof(MinresScalars) * ni, cudaMemcpyDeviceToHost,
-                                  c->stream));
-        MPET_CUDA(cudaStreamSynchronize(c->stream));
-        bool all = true;
-        for (int i = 0; i < ni; ++i) {
-            if (c->bsc_host[i].flag != 0.0) status = MPET_ERR_BREAKDOWN;
-            all = all && c->bdone_host[i] != 0.0;
-        }
-        if (status != MPET_OK || all) break;
-    }
+    run_while_graph(c, c->bmr_graph, 0.0, max_iters);
+    MPET_CUDA(cudaMemcpyAsync(c->bdone_host, c->bdone, sizeof(double) * ni, cudaMemcpyDeviceToHost, c->stream));
+    MPET_CUDA(cudaMemcpyAsync(c->bsc_host, c->bsc, sizeof(MinresScalars) * ni, cudaMemcpyDeviceToHost, c->stream));
+    MPET_CUDA(cudaStreamSynchronize(c->stream));
+    const int it = ((LoopCtl*)c->loop_ctl_host)->iters;
+    c->n_launch += c->bmr_graph_launches * (it / 3);
+    c->n_spmv += it;
     *iters_done = it;
-    return status;
+    for (int i = 0; i < ni; ++i)
+        if (c->bsc_host[i].flag != 0.0) return MPET_ERR_BREAKDOWN;
+    return MPET_OK;
 }
 
 template <typename T>
@@ -2806,6 +2927,7 @@ void alloc_krylov(mpet_ctx* c) {
     }
     c->sc = c->pool.alloc<MinresScalars>(1);
     if (!c->sc_host) MPET_CUDA(cudaMallocHost(&c->sc_host, sizeof(MinresScalars)));
+    if (!c->loop_ctl_host) MPET_CUDA(cudaMallocHost(&c->loop_ctl_host, 64));
 }
 
 // ---- AMG upload ---------------------------------------------------------------------------
