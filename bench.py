@@ -266,13 +266,13 @@ def spmv_tuning(solver, fp64=False):
 
 
 def prec_setup_ms(solver):
-    """Split of the last preconditioner set-up (ms): GPU block assembly, displacement
-    and pressure hierarchies (download + host set-up), uploads + autotuning."""
+    """Split of the last preconditioner set-up (ms): GPU block assembly, block
+    downloads, host set-up of the hierarchies (concurrent), uploads + autotuning."""
     import ctypes
     ms = np.zeros(4)
     solver.ctx.call("mpet_get_setup_timing", ms.ctypes.data_as(ctypes.c_void_p))
-    return {"blocks_gpu": round(ms[0], 1), "u_hierarchy_host": round(ms[1], 1),
-            "p_hierarchies_host": round(ms[2], 1), "upload_autotune": round(ms[3], 1)}
+    return {"blocks_gpu": round(ms[0], 1), "downloads": round(ms[1], 1),
+            "hierarchies_host": round(ms[2], 1), "upload_autotune": round(ms[3], 1)}
 
 
 def launches(solver):
@@ -685,6 +685,8 @@ def main():
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--no-fp64", action="store_true")
     ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--per-step-error", action="store_true",
+                    help="also run both precisions in lockstep and report the relative error after every step")
     ap.add_argument("--profile", action="store_true",
                     help="one step with at most --maxit MINRES iterations (small launch count for ncu)")
     ap.add_argument("--maxit", type=int, default=12)
@@ -700,6 +702,10 @@ def main():
                     help="batch mode: also time this many steps of every instance solved alone (0: skip)")
     ap.add_argument("--cheb-degree", type=int, default=None, help="override amg_cheb_degree")
     ap.add_argument("--coarse-size", type=int, default=None, help="override amg_coarse_size")
+    ap.add_argument("--cheb-degree-fine", type=int, default=None,
+                    help="override amg_cheb_degree_fine (the finest level of every hierarchy)")
+    ap.add_argument("--inner-loop", default=None, choices=["device", "host"],
+                    help="inner Krylov loop: one graph launch with a device-side loop, or host-checked replays")
     ap.add_argument("--prec-u-form", default=None, choices=["elasticity", "laplacian"],
                     help="override the displacement block of the preconditioner")
     ap.add_argument("--inner-rtol", type=float, default=None, help="override inner_rtol")
@@ -780,6 +786,10 @@ def main():
         base["inner_rtol"] = args.inner_rtol
     if args.coarse_size is not None:
         base["amg_coarse_size"] = args.coarse_size
+    if args.cheb_degree_fine is not None:
+        base["amg_cheb_degree_fine"] = args.cheb_degree_fine
+    if args.inner_loop is not None:
+        base["inner_loop"] = args.inner_loop
     if args.prec_u_form is not None:
         base["prec_u_form"] = args.prec_u_form
     t0 = time.perf_counter()
@@ -850,6 +860,23 @@ def main():
         res["fp64"] = {"ms_per_step": ms64 / args.steps, "iterations": its64,
                        "iteration_breakdown_ms": dict(split64, spmv_fp64=spmv64["fp64"]["ms"],
                                                       preconditioner=precond64_ms)}
+        if args.per_step_error:
+            # the two paths in lockstep from the zero state: relative error of the
+            # mixed-precision state against the FP64 one after every step
+            errs = []
+            problem.time.assign(0.0)
+            sol.up_.vector().zero_()
+            sol64.up_.vector().zero_()
+            g32, g64 = sol.solve_direct(), sol64.solve_direct()
+            for _ in range(args.warmup + args.steps):
+                t_now = float(problem.time)
+                up32, _ = next(g32)
+                problem.time.assign(t_now)
+                up64, _ = next(g64)
+                v64 = up64.vector()
+                errs.append(float(torch.linalg.norm(up32.vector() - v64) / torch.linalg.norm(v64)))
+            res["per_step_rel_err"] = errs
+            del g32, g64
         del sol64
 
     cpu = None
@@ -885,6 +912,7 @@ def main():
         "fp64_steps_per_s": (1e3 / res["fp64"]["ms_per_step"]) if "fp64" in res else None,
         "mixed_over_fp64": (res["fp64"]["ms_per_step"] / res["mixed"]["ms_per_step"]) if "fp64" in res else None,
         "rel_err_mixed_vs_fp64": rel_err,
+        "rel_err_mixed_vs_fp64_per_step": res.get("per_step_rel_err"),
         "iterations_per_step": {"mixed": its_mixed, "fp64": res.get("fp64", {}).get("iterations")},
         "step_semantics": {"ms_per_step": step_ms, "assemble_ms": asm_ms},
         "setup_s": {"mesh_dofmap_pattern": t_setup, "assemble_plus_amg": t_asm_amg,

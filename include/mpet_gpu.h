@@ -113,6 +113,11 @@ typedef struct mpet_params {
                                           mpettotalpressuresolver.py:281); <= 0 means 1 */
     int32_t krylov;                    /* MPET_KRYLOV_*: the Krylov method of the solves */
     int32_t gmres_restart;             /* GMRES restart length (<= 0: 30, at most 64) */
+    int32_t amg_cheb_degree_fine;      /* Chebyshev degree on the finest level of every
+                                          hierarchy (<= 0: amg_cheb_degree) */
+    int32_t inner_loop;                /* 0: each inner Krylov solve is one graph launch with a
+                                          device-side loop (default); 1: three-iteration graph
+                                          replays with a host check after each (test hook) */
 } mpet_params;
 
 typedef struct mpet_stats {
@@ -268,9 +273,9 @@ int mpet_rhs(mpet_ctx* ctx, double dt, const double* up_prev, double* b);
 int mpet_get_prec_info(mpet_ctx* ctx, int32_t* u_elasticity);
 
 /* Where the last mpet_setup_preconditioner went (ms, wall clock): ms4_host[0]
- * the preconditioner blocks assembled on the GPU, [1] the displacement
- * hierarchy (download + host set-up), [2] the pressure hierarchies (download
- * + host set-up), [3] uploads and SpMV autotuning.  No reference counterpart
+ * the preconditioner blocks assembled on the GPU, [1] their downloads, [2]
+ * the host set-up of every hierarchy (run concurrently), [3] uploads and
+ * SpMV autotuning.  No reference counterpart
  * (measurement of what hypre's set-up does inside PETSc, mpetsolver.py:507). */
 int mpet_get_setup_timing(mpet_ctx* ctx, double* ms4_host);
 

@@ -56,6 +56,8 @@ class MpetParams(ctypes.Structure):
         ("prec_p0_weight", ctypes.c_double),
         ("krylov", ctypes.c_int32),
         ("gmres_restart", ctypes.c_int32),
+        ("amg_cheb_degree_fine", ctypes.c_int32),
+        ("inner_loop", ctypes.c_int32),
     ]
 
 

@@ -297,7 +297,7 @@ static bool cholesky_inverse(std::vector<double>& a, int64_t n, std::vector<doub
 
 // Threads for the setup: the affinity set, capped by a cgroup CPU quota
 // (containers often expose every core but grant only a fraction).
-static int host_threads() {
+int host_threads() {
     int n = 1;
 #ifdef _OPENMP
     n = omp_get_num_procs();
@@ -407,13 +407,13 @@ static bool sa_prolongator(const HostCsr& A, const std::vector<double>& dinv, do
 }
 
 void amg_setup_host(const HostCsr& A0, const HostCsr* P0, double theta, int coarse_size, int max_levels,
-                    HostAmg& out) {
+                    HostAmg& out, int nthreads) {
     out.lev.clear();
     HostCsr A = A0;
     if (coarse_size < 1) coarse_size = 500;
     if (max_levels < 1) max_levels = 12;
 #ifdef _OPENMP
-    omp_set_num_threads(host_threads());
+    omp_set_num_threads(nthreads > 0 ? nthreads : host_threads());
 #endif
     while (true) {
         HostAmgLevel L;

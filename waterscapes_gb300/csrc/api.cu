@@ -5,6 +5,8 @@
 
 #include <algorithm>
 #include <chrono>
+#include <exception>
+#include <thread>
 
 #include "mpet_internal.cuh"
 
@@ -176,6 +178,8 @@ static void check_params(const mpet_ctx* c, const mpet_params* p) {
     require(p->rtol > 0.0, MPET_ERR_INVALID, "rtol must be positive");
     require(p->formulation == MPET_FORM_MPET || p->formulation == MPET_FORM_TOTAL_PRESSURE, MPET_ERR_INVALID,
             "unknown formulation");
+    require(p->inner_loop == 0 || p->inner_loop == 1, MPET_ERR_INVALID, "inner_loop must be 0 or 1");
+    require(p->amg_cheb_degree_fine <= 32, MPET_ERR_INVALID, "amg_cheb_degree_fine must be at most 32");
     require(p->krylov >= MPET_KRYLOV_AUTO && p->krylov <= MPET_KRYLOV_GMRES && p->gmres_restart <= 64,
             MPET_ERR_INVALID, "unknown Krylov method or restart above 64");
     if (p->formulation == MPET_FORM_TOTAL_PRESSURE) {
@@ -571,12 +575,15 @@ int mpet_setup_preconditioner(mpet_ctx* c, double dt) {
         }
         c->u_elast = elast;
     }
+    // downloads (and the P1-in-P2 embedding), then the host set-ups of all
+    // hierarchies concurrently (threads sharing the host cores), then uploads
+    HostCsr hu, P0;
+    bool use_p0 = false;
     if (!elast) {
         c->u_elast = false;
-        HostCsr h;
-        fetch(c->Lu, h);
-        HostAmg ha;
+        fetch(c->Lu, hu);
         if (c->prm.amg_p2_to_p1) {
+            use_p0 = true;
             // First level of the displacement hierarchy: the P1 functions that
             // vanish on the displacement Dirichlet boundary, embedded in P2
             // (vertex values copied, edge-midpoint values averaged).
@@ -590,7 +597,6 @@ int mpet_setup_preconditioner(mpet_ctx* c, double dt) {
             int64_t m = 0;
             for (int64_t v = 0; v < c->nv; ++v)
                 if (!bc[v]) cidx[v] = m++;
-            HostCsr P0;
             P0.n = c->nnodes;
             P0.m = m;
             P0.rp.assign(c->nnodes + 1, 0);
@@ -620,31 +626,45 @@ int mpet_setup_preconditioner(mpet_ctx* c, double dt) {
                         }
                 }
             }
-            amg_setup_host(h, &P0, c->prm.amg_theta, cs, 12, ha);
-        } else {
-            amg_setup_host(h, nullptr, c->prm.amg_theta, cs, 12, ha);
         }
-        c->setup_ms[1] = since(t0);  // download + host hierarchy of the displacement block
-        t0 = clk::now();
-        upload_amg(c, c->amg_u, ha, 4, fp32);
-        c->setup_ms[3] = since(t0);  // upload + autotuning
-    } else {
-        c->setup_ms[1] = since(t0);
-        c->setup_ms[3] = 0.0;
     }
+    std::vector<HostCsr> hp(c->J);
+    for (int a = 0; a < c->J; ++a) fetch(c->Pp[a], hp[a]);
+    c->setup_ms[1] = since(t0);  // downloads of the blocks
     t0 = clk::now();
-    double t_up = 0.0;
-    for (int a = 0; a < c->J; ++a) {
-        HostCsr h;
-        fetch(c->Pp[a], h);
-        HostAmg ha;
-        amg_setup_host(h, nullptr, c->prm.amg_theta, cs, 12, ha);
-        const auto tu = clk::now();
-        upload_amg(c, c->amg_p[a], ha, 1, fp32);
-        t_up += since(tu);
+    HostAmg hau;
+    std::vector<HostAmg> hap(c->J);
+    {
+        const int ntask = c->J + (elast ? 0 : 1);
+        const int nth = std::max(1, host_threads() / ntask);
+        std::vector<std::exception_ptr> errs(ntask);
+        std::vector<std::thread> th;
+        const double theta = c->prm.amg_theta;
+        for (int a = 0; a < c->J; ++a)
+            th.emplace_back([&, a] {
+                try {
+                    amg_setup_host(hp[a], nullptr, theta, cs, 12, hap[a], nth);
+                } catch (...) {
+                    errs[a] = std::current_exception();
+                }
+            });
+        if (!elast)
+            th.emplace_back([&] {
+                try {
+                    amg_setup_host(hu, use_p0 ? &P0 : nullptr, theta, cs, 12, hau, nth);
+                } catch (...) {
+                    errs[c->J] = std::current_exception();
+                }
+            });
+        for (auto& t : th) t.join();
+        for (auto& e : errs)
+            if (e) std::rethrow_exception(e);
     }
-    c->setup_ms[2] = since(t0) - t_up;  // download + host hierarchies of the pressure blocks
-    c->setup_ms[3] += t_up;
+    c->setup_ms[2] = since(t0);  // host hierarchies (concurrent)
+    t0 = clk::now();
+    if (!elast) upload_amg(c, c->amg_u, hau, 4, fp32);
+    for (int a = 0; a < c->J; ++a) upload_amg(c, c->amg_p[a], hap[a], 1, fp32);
+    c->setup_ms[3] = since(t0);  // uploads + autotuning
     c->precond_ready = true;
     c->prec_dt = dt;
     API_END(c)

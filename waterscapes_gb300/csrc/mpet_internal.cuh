@@ -174,6 +174,7 @@ struct AmgLevel {
 struct AmgHier {
     int nvec = 1;
     int cheb_degree = 3;
+    int cheb_degree0 = 3;  // on the finest level
     std::vector<AmgLevel> lev;
     int64_t ncoarse = 0;
     double* cinv = nullptr;  // dense inverse of the coarsest operator, FP64
@@ -211,8 +212,11 @@ struct HostAmg {
     std::vector<double> cinv;
 };
 // P0, if given, is the prolongator of the first level (otherwise smoothed aggregation).
+// (nthreads: OpenMP threads of this set-up; <= 0: every host thread)
 void amg_setup_host(const HostCsr& A, const HostCsr* P0, double theta, int coarse_size, int max_levels,
-                    HostAmg& out);
+                    HostAmg& out, int nthreads = 0);
+// threads for host set-ups: the affinity set, capped by a cgroup CPU quota
+int host_threads();
 void sym_eig(int n, const double* A, double* Q, double* lam);
 // block smoothed aggregation from a first level A1 with near-nullspace B1 (A1.n x nb_cols,
 // row-major) and bs unknowns per node
@@ -370,6 +374,8 @@ struct mpet_ctx {
     cudaGraphExec_t mr_graph = nullptr;  // whole inner solve: WHILE node over 3 iterations
     void* loop_ctl = nullptr;            // device loop control (target, budget, iterations)
     void* loop_ctl_host = nullptr;       // pinned copy
+    cudaGraphExec_t mr_graph3 = nullptr; // 3 iterations, host-checked replays (inner_loop = 1)
+    int64_t mr_graph3_launches = 0;
     int64_t mr_graph_launches = 0;  // kernels per graph launch
 
     // batch of independent instances in one mesh (ninst = 0: one instance):
@@ -424,8 +430,8 @@ struct mpet_ctx {
     // timing
     cudaEvent_t ev0 = nullptr, ev1 = nullptr;
     double t_inner_ms = 0.0, t_solve_ms = 0.0;  // MINRES graph replays / whole solves
-    // last preconditioner set-up (ms): block assembly (GPU), displacement hierarchy
-    // (download + host), pressure hierarchies (download + host), uploads + autotuning
+    // last preconditioner set-up (ms): block assembly (GPU), block downloads, host
+    // hierarchies (built concurrently), uploads + autotuning
     double setup_ms[4] = {0, 0, 0, 0};
     int64_t n_inner_its = 0;
     cudaEvent_t ev_in0 = nullptr, ev_in1 = nullptr, ev_sv0 = nullptr, ev_sv1 = nullptr;

@@ -16,10 +16,11 @@
 // Host code cannot use the array's name as a device address (on the host it
 // names a stand-in object), so the device address is asked for once per
 // device with cudaGetSymbolAddress, with that device current, and kept.
-// mpet_ctx_create does this eagerly: with lazy module loading (the CUDA
-// default) the lookup is also what loads this file's kernels and the array
-// onto the device, so it happens while the caller can still spare the
-// memory (256 KiB plus the code).  If that early lookup failed, the first
+// mpet_ctx_create does this eagerly, and also asks for the attributes of this
+// file's kernels: with lazy module loading (the CUDA default) that is what
+// loads the array and the kernels' code onto the device, so it happens while
+// the caller can still spare the memory (256 KiB plus the code), not at the
+// first call.  If that early lookup failed, the first
 // mpet_residual_noalloc call on the device retries it; make that call
 // outside any stream capture.  The call waits for its own stream (it
 // returns the norms to the host), so it synchronises the context's stream.
@@ -47,17 +48,6 @@ static std::mutex g_noalloc_mutex;
 static double* g_noalloc_ptr[128] = {nullptr};
 
 // device address of the scratch array on the current device (looked up once)
-static double* noalloc_scratch(int device);
-
-// Eager lookup at context creation (the current device is `device`); a
-// failure here is left for the first call to report.
-void noalloc_prepare(int device) {
-    try {
-        noalloc_scratch(device);
-    } catch (const Error&) {
-    }
-}
-
 static double* noalloc_scratch(int device) {
     if (device < 0 || device >= 128) fail(MPET_ERR_INVALID, "device index out of range for the static scratch table");
     std::lock_guard<std::mutex> lock(g_noalloc_mutex);
@@ -144,6 +134,24 @@ __global__ void __launch_bounds__(256) k_resid_finish(int nblocks, double* part)
     if (threadIdx.x == 0) {
         part[0] = a;
         part[NOALLOC_MAX_BLOCKS] = b;
+    }
+}
+
+// Eager set-up at context creation (the current device is `device`): the
+// scratch address, and the code of this file's kernels, which lazy module
+// loading would otherwise load (and allocate device memory for) at the first
+// call.  A failure here is left for the first call to report.
+void noalloc_prepare(int device) {
+    try {
+        noalloc_scratch(device);
+        cudaFuncAttributes fa;
+        cudaFuncGetAttributes(&fa, k_resid_blocks<32>);
+        cudaFuncGetAttributes(&fa, k_resid_blocks<16>);
+        cudaFuncGetAttributes(&fa, k_resid_blocks<8>);
+        cudaFuncGetAttributes(&fa, k_resid_blocks<4>);
+        cudaFuncGetAttributes(&fa, k_resid_finish);
+        cudaGetLastError();
+    } catch (const Error&) {
     }
 }
 

@@ -1435,7 +1435,7 @@ static void cheb(mpet_ctx* c, AmgHier& h, AmgLevel& L, const T* b, const T* xin,
     const double theta = 0.5 * (hi + lo), delta = 0.5 * (hi - lo);
     const double sigma = theta / delta;
     double rho_old = 1.0 / sigma;
-    const int s = h.cheb_degree;
+    const int s = (&L == &h.lev[0]) ? h.cheb_degree0 : h.cheb_degree;
     T* d = (T*)L.d;
     T* t0 = (T*)L.t0;
     T* t1 = (T*)L.t1;
@@ -1495,7 +1495,6 @@ static void profile_levels(mpet_ctx* c, AmgHier& h, int reps, double* ms, double
     const int64_t l0 = c->n_launch;
     const size_t nl = h.lev.size();
     const double sv = sizeof(T);
-    const int s = h.cheb_degree;
     for (size_t k = 0; k < nl; ++k) {
         AmgLevel& L = h.lev[k];
         MPET_CUDA(cudaMemsetAsync(L.b, 0, sizeof(double) * L.A.n * NV, c->stream));
@@ -1517,6 +1516,7 @@ static void profile_levels(mpet_ctx* c, AmgHier& h, int reps, double* ms, double
             bytes[k] = (double)h.ncoarse * h.ncoarse * 8.0 + 2.0 * h.ncoarse * NV * sv;
             continue;
         }
+        const int s = k == 0 ? h.cheb_degree0 : h.cheb_degree;
         const double nc = (double)h.lev[k + 1].A.n, vecc = nc * NV * sv;
         // a product with A: the CSR entries and row pointers, or (matrix-free) the
         // incidence and per-cell node ids (NN each), the per-cell data, the row
@@ -1810,6 +1810,8 @@ static void capture_minres_graph(mpet_ctx* c) {
 void destroy_minres_graph(mpet_ctx* c) {
     if (c->mr_graph) cudaGraphExecDestroy(c->mr_graph);
     c->mr_graph = nullptr;
+    if (c->mr_graph3) cudaGraphExecDestroy(c->mr_graph3);
+    c->mr_graph3 = nullptr;
     if (c->bmr_graph) cudaGraphExecDestroy(c->bmr_graph);
     c->bmr_graph = nullptr;
 }
@@ -1826,10 +1828,37 @@ static void run_while_graph(mpet_ctx* c, cudaGraphExec_t g, double target, int m
     MPET_CUDA(cudaMemcpyAsync(hc, c->loop_ctl, sizeof(LoopCtl), cudaMemcpyDeviceToHost, c->stream));
 }
 
+// The same three iterations replayed as a plain graph with a host check after
+// each replay (inner_loop = 1, a test hook to compare with the device loop).
+template <typename T>
+static int minres_run_host(mpet_ctx* c, double target, int max_iters, int* iters_done) {
+    if (!c->mr_graph3)
+        capture_graph(c, [](mpet_ctx* cc) { minres_three<T>(cc); }, &c->mr_graph3, &c->mr_graph3_launches,
+                      "MINRES");
+    int it = 0;
+    int status = MPET_OK;
+    while (it < max_iters) {
+        MPET_CUDA(cudaGraphLaunch(c->mr_graph3, c->stream));
+        it += 3;
+        c->n_launch += c->mr_graph3_launches;
+        c->n_spmv += 3;
+        MPET_CUDA(cudaMemcpyAsync(c->sc_host, c->sc, sizeof(MinresScalars), cudaMemcpyDeviceToHost, c->stream));
+        MPET_CUDA(cudaStreamSynchronize(c->stream));
+        if (c->sc_host->flag != 0.0) {
+            status = MPET_ERR_BREAKDOWN;
+            break;
+        }
+        if (c->sc_host->rel <= target) break;
+    }
+    *iters_done = it;
+    return status;
+}
+
 template <typename T>
 static int minres_run(mpet_ctx* c, double target, int max_iters, int* iters_done) {
     *iters_done = 0;
     if (max_iters <= 0) return MPET_OK;
+    if (c->prm.inner_loop == 1) return minres_run_host<T>(c, target, max_iters, iters_done);
     if (!c->mr_graph) capture_minres_graph<T>(c);
     run_while_graph(c, c->mr_graph, target, max_iters);
     MPET_CUDA(cudaMemcpyAsync(c->sc_host, c->sc, sizeof(MinresScalars), cudaMemcpyDeviceToHost, c->stream));
@@ -2996,6 +3025,7 @@ static void choose_mf(mpet_ctx* c, AmgHier& h) {
 void upload_amg(mpet_ctx* c, AmgHier& h, const HostAmg& ha, int nvec, bool fp32) {
     h.nvec = nvec;
     h.cheb_degree = c->prm.amg_cheb_degree > 0 ? c->prm.amg_cheb_degree : 4;
+    h.cheb_degree0 = c->prm.amg_cheb_degree_fine > 0 ? c->prm.amg_cheb_degree_fine : h.cheb_degree;
     h.lev.clear();
     h.lev.resize(ha.lev.size());
     for (size_t k = 0; k < ha.lev.size(); ++k) {
