@@ -2065,6 +2065,26 @@ __global__ void k_seg_dot(const int64_t* __restrict__ lo, const int32_t* __restr
     if (threadIdx.x == 0) part[ch] = s;
 }
 
+// k_seg_dot for the batched iterations: a converged instance's chunks contribute 0
+template <typename T>
+__global__ void k_seg_dot_open(const int64_t* __restrict__ lo, const int32_t* __restrict__ len,
+                               const int32_t* __restrict__ inst, const T* __restrict__ a, const T* __restrict__ b,
+                               double* part, const double* __restrict__ done) {
+    __shared__ double sh[8];
+    const int64_t ch = blockIdx.x;
+    if (done[inst[ch]] != 0.0) {
+        if (threadIdx.x == 0) part[ch] = 0.0;
+        return;
+    }
+    double s = 0.0;
+    for (int i = threadIdx.x; i < len[ch]; i += 256) {
+        const int64_t r = lo[ch] + i;
+        s += (double)a[r] * (double)b[r];
+    }
+    s = block_sum256(s, sh);
+    if (threadIdx.x == 0) part[ch] = s;
+}
+
 // (r D^-1)^2 and (b D^-1)^2 per chunk
 __global__ void k_seg_norms(const int64_t* __restrict__ lo, const int32_t* __restrict__ len, int64_t nch,
                             const double* __restrict__ r, const double* __restrict__ b,
@@ -2165,8 +2185,9 @@ __global__ void k_batch_status(int ninst, double* iv, double rtol, int first) {
 template <typename T>
 __global__ void k_bmr_v(const int64_t* __restrict__ lo, const int32_t* __restrict__ len,
                         const int32_t* __restrict__ inst, const T* __restrict__ y, T* v,
-                        const MinresScalars* __restrict__ sc) {
+                        const MinresScalars* __restrict__ sc, const double* __restrict__ done) {
     const int64_t ch = blockIdx.x;
+    if (done[inst[ch]] != 0.0) return;  // a converged instance's chunks are left as they are
     const T ib = (T)sc[inst[ch]].inv_beta;
     for (int i = threadIdx.x; i < len[ch]; i += 256) v[lo[ch] + i] = y[lo[ch] + i] * ib;
 }
@@ -2175,9 +2196,14 @@ __global__ void k_bmr_v(const int64_t* __restrict__ lo, const int32_t* __restric
 template <typename T>
 __global__ void k_bmr_axpy_dot(const int64_t* __restrict__ lo, const int32_t* __restrict__ len,
                                const int32_t* __restrict__ inst, T* y, const T* __restrict__ r1,
-                               const T* __restrict__ v, const MinresScalars* __restrict__ sc, double* part) {
+                               const T* __restrict__ v, const MinresScalars* __restrict__ sc, double* part,
+                               const double* __restrict__ done) {
     __shared__ double sh[8];
     const int64_t ch = blockIdx.x;
+    if (done[inst[ch]] != 0.0) {
+        if (threadIdx.x == 0) part[ch] = 0.0;
+        return;
+    }
     const T c1 = (T)sc[inst[ch]].c_r1;
     double s = 0.0;
     for (int i = threadIdx.x; i < len[ch]; i += 256) {
@@ -2193,8 +2219,9 @@ __global__ void k_bmr_axpy_dot(const int64_t* __restrict__ lo, const int32_t* __
 template <typename T>
 __global__ void k_bmr_axpy(const int64_t* __restrict__ lo, const int32_t* __restrict__ len,
                            const int32_t* __restrict__ inst, T* y, const T* __restrict__ r2,
-                           const MinresScalars* __restrict__ sc) {
+                           const MinresScalars* __restrict__ sc, const double* __restrict__ done) {
     const int64_t ch = blockIdx.x;
+    if (done[inst[ch]] != 0.0) return;
     const T c2 = (T)sc[inst[ch]].c_r2;
     for (int i = threadIdx.x; i < len[ch]; i += 256) y[lo[ch] + i] -= c2 * r2[lo[ch] + i];
 }
@@ -2202,8 +2229,10 @@ __global__ void k_bmr_axpy(const int64_t* __restrict__ lo, const int32_t* __rest
 template <typename T>
 __global__ void k_bmr_update(const int64_t* __restrict__ lo, const int32_t* __restrict__ len,
                              const int32_t* __restrict__ inst, const T* __restrict__ v, const T* __restrict__ w1,
-                             const T* __restrict__ w2, T* w, T* d, const MinresScalars* __restrict__ sc) {
+                             const T* __restrict__ w2, T* w, T* d, const MinresScalars* __restrict__ sc,
+                             const double* __restrict__ done) {
     const int64_t ch = blockIdx.x;
+    if (done[inst[ch]] == 1.0) return;  // 2: converged by this iteration's beta, its update still counts
     const MinresScalars& s = sc[inst[ch]];
     const T oe = (T)s.oldeps, de = (T)s.delta, ig = (T)s.inv_gamma, ph = (T)s.phi;
     for (int i = threadIdx.x; i < len[ch]; i += 256) {
@@ -2238,9 +2267,14 @@ __global__ void k_bmr_init(int ni, MinresScalars* sc, const double* q, const dou
     done[i] = on ? 0.0 : 1.0;
 }
 
-__global__ void k_bmr_freeze(int ni, MinresScalars* sc, const double* done) {
+// done: 0 open, 2 converged in the previous iteration (its last update was still
+// applied), 1 settled; settled instances' chunks are skipped by the vector kernels
+__global__ void k_bmr_freeze(int ni, MinresScalars* sc, double* done) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i < ni && done[i] != 0.0) mr_freeze(&sc[i]);
+    if (i < ni && done[i] != 0.0) {
+        mr_freeze(&sc[i]);
+        done[i] = 1.0;
+    }
 }
 
 __global__ void k_bmr_alfa(int ni, MinresScalars* sc, const double* t, const double* done) {
@@ -2252,7 +2286,7 @@ __global__ void k_bmr_beta(int ni, MinresScalars* sc, const double* t, const dou
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= ni || done[i] != 0.0) return;
     mr_beta_one(&sc[i], t[i]);
-    if (sc[i].rel <= target[i] || sc[i].flag != 0.0) done[i] = 1.0;
+    if (sc[i].rel <= target[i] || sc[i].flag != 0.0) done[i] = 2.0;  // the update of this iteration still runs
 }
 
 template <typename T>
@@ -2269,15 +2303,16 @@ static void bminres_three(mpet_ctx* c) {
         T* r2 = (T*)c->kr[ir2];
         T* y = (T*)c->kr[iy];
         k_bmr_freeze<<<gi, 128, 0, c->stream>>>(ni, c->bsc, c->bdone);
-        k_bmr_v<T><<<(unsigned)nch, 256, 0, c->stream>>>(c->ch_lo, c->ch_len, c->ch_inst, y, v, c->bsc);
+        k_bmr_v<T><<<(unsigned)nch, 256, 0, c->stream>>>(c->ch_lo, c->ch_len, c->ch_inst, y, v, c->bsc, c->bdone);
         MPET_CHECK_LAUNCH();
         launch_spmv<T, 1>(c, c->A, vals<T>(c->A), v, EpiStore<T, 1>{y});
         c->n_spmv++;
         k_bmr_axpy_dot<T><<<(unsigned)nch, 256, 0, c->stream>>>(c->ch_lo, c->ch_len, c->ch_inst, y, r1, v, c->bsc,
-                                                                 c->ch_part);
+                                                                 c->ch_part, c->bdone);
         k_seg_finish<<<gi, 128, 0, c->stream>>>(ni, c->inst_cptr, c->inst_chunks, c->ch_part, nch, 1, c->bval);
         k_bmr_alfa<<<gi, 128, 0, c->stream>>>(ni, c->bsc, c->bval, c->bdone);
-        k_bmr_axpy<T><<<(unsigned)nch, 256, 0, c->stream>>>(c->ch_lo, c->ch_len, c->ch_inst, y, r2, c->bsc);
+        k_bmr_axpy<T><<<(unsigned)nch, 256, 0, c->stream>>>(c->ch_lo, c->ch_len, c->ch_inst, y, r2, c->bsc,
+                                                             c->bdone);
         MPET_CHECK_LAUNCH();
         c->n_launch += 6;
         const int old1 = ir1;
@@ -2285,8 +2320,9 @@ static void bminres_three(mpet_ctx* c) {
         ir2 = iy;
         iy = old1;
         precond<T>(c, (const T*)c->kr[ir2], (T*)c->kr[iy]);
-        k_seg_dot<T><<<(unsigned)nch, 256, 0, c->stream>>>(c->ch_lo, c->ch_len, nch, (const T*)c->kr[ir2],
-                                                           (const T*)c->kr[iy], c->ch_part);
+        k_seg_dot_open<T><<<(unsigned)nch, 256, 0, c->stream>>>(c->ch_lo, c->ch_len, c->ch_inst,
+                                                                (const T*)c->kr[ir2], (const T*)c->kr[iy],
+                                                                c->ch_part, c->bdone);
         k_seg_finish<<<gi, 128, 0, c->stream>>>(ni, c->inst_cptr, c->inst_chunks, c->ch_part, nch, 1, c->bval);
         k_bmr_beta<<<gi, 128, 0, c->stream>>>(ni, c->bsc, c->bval, c->btarget, c->bdone);
         const int oldw1 = iw1;
@@ -2295,7 +2331,7 @@ static void bminres_three(mpet_ctx* c) {
         iw = oldw1;
         k_bmr_update<T><<<(unsigned)nch, 256, 0, c->stream>>>(c->ch_lo, c->ch_len, c->ch_inst, v,
                                                               (const T*)c->kw[iw1], (const T*)c->kw[iw2],
-                                                              (T*)c->kw[iw], d, c->bsc);
+                                                              (T*)c->kw[iw], d, c->bsc, c->bdone);
         MPET_CHECK_LAUNCH();
         c->n_launch += 4;
     }
