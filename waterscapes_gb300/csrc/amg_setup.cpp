@@ -406,10 +406,9 @@ static bool sa_prolongator(const HostCsr& A, const std::vector<double>& dinv, do
     return true;
 }
 
-void amg_setup_host(const HostCsr& A0, const HostCsr* P0, double theta, int coarse_size, int max_levels,
-                    HostAmg& out, int nthreads) {
+void amg_setup_host(HostCsr A, const HostCsr* P0, double theta, int coarse_size, int max_levels, HostAmg& out,
+                    int nthreads, bool rho0_device) {
     out.lev.clear();
-    HostCsr A = A0;
     if (coarse_size < 1) coarse_size = 500;
     if (max_levels < 1) max_levels = 12;
 #ifdef _OPENMP
@@ -423,11 +422,14 @@ void amg_setup_host(const HostCsr& A0, const HostCsr* P0, double theta, int coar
             const double d = diag_of(A, i);
             L.dinv[i] = d != 0.0 ? 1.0 / d : 0.0;
         }
-        L.rho = lanczos_rho(A, L.dinv, 30);
-        L.A = A;
-        out.lev.push_back(L);
+        // the first level's spectral radius is only needed by its smoother when P0
+        // is given: with rho0_device it is estimated on the GPU after the upload
+        // (rho < 0 marks that), the same Lanczos iteration on the same start vector
+        const bool given = P0 != nullptr && out.lev.empty();
+        L.rho = (given && rho0_device) ? -1.0 : lanczos_rho(A, L.dinv, 30);
+        L.A = std::move(A);
+        out.lev.push_back(std::move(L));
         HostAmgLevel& cur = out.lev.back();
-        const bool given = P0 != nullptr && out.lev.size() == 1;
         if (!given && (n <= coarse_size || (int)out.lev.size() >= max_levels)) break;
         HostCsr P;
         if (given) {
@@ -438,12 +440,12 @@ void amg_setup_host(const HostCsr& A0, const HostCsr* P0, double theta, int coar
             // strong connection is aggregated on its full graph (threshold 0)
             const int sa_level = (int)out.lev.size() - 1 - (P0 != nullptr ? 1 : 0);
             const double th = theta * pow(0.5, (double)sa_level);
-            if (!sa_prolongator(A, cur.dinv, cur.rho, th, P)) break;
+            if (!sa_prolongator(cur.A, cur.dinv, cur.rho, th, P)) break;
         }
         HostCsr R;
         transpose(P, R);
         HostCsr AP, Ac;
-        spgemm(A, P, AP);
+        spgemm(cur.A, P, AP);
         spgemm(R, AP, Ac);
         cur.P = std::move(P);
         cur.R = std::move(R);

@@ -643,7 +643,7 @@ int mpet_setup_preconditioner(mpet_ctx* c, double dt) {
         for (int a = 0; a < c->J; ++a)
             th.emplace_back([&, a] {
                 try {
-                    amg_setup_host(hp[a], nullptr, theta, cs, 12, hap[a], nth);
+                    amg_setup_host(std::move(hp[a]), nullptr, theta, cs, 12, hap[a], nth);
                 } catch (...) {
                     errs[a] = std::current_exception();
                 }
@@ -651,7 +651,7 @@ int mpet_setup_preconditioner(mpet_ctx* c, double dt) {
         if (!elast)
             th.emplace_back([&] {
                 try {
-                    amg_setup_host(hu, use_p0 ? &P0 : nullptr, theta, cs, 12, hau, nth);
+                    amg_setup_host(std::move(hu), use_p0 ? &P0 : nullptr, theta, cs, 12, hau, nth, true);
                 } catch (...) {
                     errs[c->J] = std::current_exception();
                 }

@@ -212,9 +212,10 @@ struct HostAmg {
     std::vector<double> cinv;
 };
 // P0, if given, is the prolongator of the first level (otherwise smoothed aggregation).
-// (nthreads: OpenMP threads of this set-up; <= 0: every host thread)
-void amg_setup_host(const HostCsr& A, const HostCsr* P0, double theta, int coarse_size, int max_levels,
-                    HostAmg& out, int nthreads = 0);
+// (nthreads: OpenMP threads of this set-up, <= 0: every host thread; rho0_device: with
+// P0 given, leave the first level's spectral radius to the GPU, marked rho < 0)
+void amg_setup_host(HostCsr A, const HostCsr* P0, double theta, int coarse_size, int max_levels, HostAmg& out,
+                    int nthreads = 0, bool rho0_device = false);
 // threads for host set-ups: the affinity set, capped by a cgroup CPU quota
 int host_threads();
 void sym_eig(int n, const double* A, double* Q, double* lam);

@@ -3058,6 +3058,8 @@ static void choose_mf(mpet_ctx* c, AmgHier& h) {
     c->n_launch = l0;
 }
 
+static double csr_rho(mpet_ctx* c, const Csr& A, const double* dinv);
+
 void upload_amg(mpet_ctx* c, AmgHier& h, const HostAmg& ha, int nvec, bool fp32) {
     h.nvec = nvec;
     h.cheb_degree = c->prm.amg_cheb_degree > 0 ? c->prm.amg_cheb_degree : 4;
@@ -3072,6 +3074,7 @@ void upload_amg(mpet_ctx* c, AmgHier& h, const HostAmg& ha, int nvec, bool fp32)
         const int64_t n = hl.A.n;
         L.dinv64 = c->pool.alloc<double>(n);
         MPET_CUDA(cudaMemcpyAsync(L.dinv64, hl.dinv.data(), sizeof(double) * n, cudaMemcpyHostToDevice, c->stream));
+        if (L.rho < 0.0) L.rho = csr_rho(c, L.A, L.dinv64);  // left to the GPU by the host set-up
         if (fp32) {
             L.dinv32 = c->pool.alloc<float>(n);
             k_f64_to_f32<<<grid_for(n, 256), 256, 0, c->stream>>>(n, L.dinv64, L.dinv32);
@@ -3117,7 +3120,7 @@ __global__ void k_lz_init(int64_t n, const double* __restrict__ dinv, const uint
     const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
     if (i >= n) return;
     s[i] = dinv[i] > 0.0 ? sqrt(dinv[i]) : 0.0;
-    v[i] = bc[i] ? 0.0 : 0.5 + (double)((7919LL * i) % 1009LL) / 1009.0;
+    v[i] = (bc && bc[i]) ? 0.0 : 0.5 + (double)((7919LL * i) % 1009LL) / 1009.0;
 }
 template <typename T>
 __global__ void k_lz_mul(int64_t n, const double* __restrict__ s, const double* __restrict__ v, T* w) {
@@ -3173,6 +3176,40 @@ static double nb_uu_rho(mpet_ctx* c, const double* dinv) {
         k_lz_axpy<<<G, 256, 0, c->stream>>>(n, w, -alpha, v);
         beta = sqrt(dot_host(c, w, w, n));
         if (beta <= 1e-14 * fabs(alpha) || k + 1 == 30) break;
+        be.push_back(beta);
+        k_lz_next<<<G, 256, 0, c->stream>>>(n, w, 1.0 / beta, vp, v);
+    }
+    return tridiag_max_eig_host(al, be);
+}
+
+// Spectral radius of D^-1 A for a CSR level on the device (FP64 values): the host
+// set-up's Lanczos iteration (lanczos_rho, amg_setup.cpp) with the same start vector,
+// 30 steps on D^-1/2 A D^-1/2, largest Ritz value.
+static double csr_rho(mpet_ctx* c, const Csr& A, const double* dinv) {
+    const int64_t n = A.n;
+    TmpBuf bs(sizeof(double) * n), bv(sizeof(double) * n), bp(sizeof(double) * n), bw(sizeof(double) * n),
+        bt(sizeof(double) * n), bx(sizeof(double) * n);
+    double *s = bs.as<double>(), *v = bv.as<double>(), *vp = bp.as<double>(), *w = bw.as<double>();
+    double *t = bt.as<double>(), *xin = bx.as<double>();
+    const int G = grid_for(n, 256);
+    k_lz_init<<<G, 256, 0, c->stream>>>(n, dinv, nullptr, s, v);
+    MPET_CHECK_LAUNCH();
+    double nrm = sqrt(dot_host(c, v, v, n));
+    if (!(nrm > 0.0)) return 1.0;
+    k_lz_next<<<G, 256, 0, c->stream>>>(n, v, 1.0 / nrm, w, v);  // v /= |v| (w scratch)
+    MPET_CUDA(cudaMemsetAsync(vp, 0, sizeof(double) * n, c->stream));
+    std::vector<double> al, be(1, 0.0);
+    double beta = 0.0;
+    for (int k = 0; k < 30 && k < n; ++k) {
+        k_lz_mul<double><<<G, 256, 0, c->stream>>>(n, s, v, xin);
+        launch_spmv<double, 1>(c, A, A.v64, xin, EpiStore<double, 1>{t});
+        k_lz_w<double><<<G, 256, 0, c->stream>>>(n, s, t, beta, vp, w);
+        MPET_CHECK_LAUNCH();
+        const double alpha = dot_host(c, w, v, n);
+        al.push_back(alpha);
+        k_lz_axpy<<<G, 256, 0, c->stream>>>(n, w, -alpha, v);
+        beta = sqrt(dot_host(c, w, w, n));
+        if (beta <= 1e-14 * fabs(alpha) || k + 1 == 30 || k + 1 == n) break;
         be.push_back(beta);
         k_lz_next<<<G, 256, 0, c->stream>>>(n, w, 1.0 / beta, vp, v);
     }
