@@ -1921,6 +1921,41 @@ static void rigid_project(mpet_ctx* c, double* v, const double* P, const double*
     }
 }
 
+// rhs_T = b / ||D^-1 b|| (the scale read on the device)
+template <typename T>
+__global__ void k_scale_b(int64_t n, const double* __restrict__ b, T* out, const MinresScalars* s) {
+    const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const double nb = sqrt(s->nb2);
+    out[i] = (T)(nb > 0.0 ? b[i] / nb : 0.0);
+}
+
+// Preconditioned norm (b^T M^-1 b)^1/2 of the right-hand side, in the working
+// precision, after the first refinement residual (which left ||D^-1 b||^2 in the
+// scalars).  The refinement stops at rtol times the larger of this norm and the
+// initial residual's, as PETSc's default convergence test measures against the
+// right-hand side (the reference's iterative solves, mpetsolver.py:507-556):
+// relative to a warm-started initial residual alone, a good initial guess would
+// push the target below what FP64 residuals resolve.  kr[0] and kr[2] are scratch.
+template <typename T>
+static double precond_norm_b(mpet_ctx* c, const double* b) {
+    const int64_t n = c->N;
+    T* rhs = (T*)c->kr[0];
+    T* y = (T*)c->kr[2];
+    k_scale_b<T><<<grid_for(n, 256), 256, 0, c->stream>>>(n, b, rhs, c->sc);
+    MPET_CHECK_LAUNCH();
+    precond<T>(c, rhs, y);
+    k_dot<T><<<NB_RED, 256, 0, c->stream>>>(n, rhs, y, c->partials);
+    k_finish_dot<<<1, 256, 0, c->stream>>>(c->partials, c->partials + 2 * NB_RED - 1);
+    MPET_CHECK_LAUNCH();
+    double q = 0.0;
+    MPET_CUDA(cudaMemcpyAsync(&q, c->partials + 2 * NB_RED - 1, sizeof(double), cudaMemcpyDeviceToHost,
+                              c->stream));
+    MPET_CUDA(cudaMemcpyAsync(c->sc_host, c->sc, sizeof(MinresScalars), cudaMemcpyDeviceToHost, c->stream));
+    MPET_CUDA(cudaStreamSynchronize(c->stream));
+    return sqrt(q > 0.0 ? q : 0.0) * sqrt(c->sc_host->nb2 > 0.0 ? c->sc_host->nb2 : 0.0);
+}
+
 template <typename T>
 static int solve_impl(mpet_ctx* c, const double* b, double* x, mpet_stats* st, bool homogeneous) {
     const int64_t n = c->N;
@@ -1942,10 +1977,12 @@ static int solve_impl(mpet_ctx* c, const double* b, double* x, mpet_stats* st, b
     const bool fp64 = sizeof(T) == 8;
     const int max_outer = c->prm.max_outer > 0 ? c->prm.max_outer : 20;
     const int maxit = c->prm.maxit > 0 ? c->prm.maxit : 5000;
+    double eta_b = 0.0;
     for (outer = 0; outer < max_outer; ++outer) {
         launch_spmv<double, 1>(c, c->A, c->A.v64, x, EpiResid64{c->orr, b, c->dinv});
         c->n_spmv++;
         k_outer_norms<<<1, 256, 0, c->stream>>>(c->sc, c->partials);
+        if (outer == 0) eta_b = precond_norm_b<T>(c, b);
         if (c->nrigid > 0) rigid_project(c, c->orr, c->rigid_Z, c->rigid_MZ, nullptr);  // rounding drift
         if (c->q_nk > 0) kernel_project(c, c->orr);
         T* rhs = (T*)c->kr[0];
@@ -1967,7 +2004,7 @@ static int solve_impl(mpet_ctx* c, const double* b, double* x, mpet_stats* st, b
             break;
         }
         const double eta = h.beta1 * nr;
-        if (eta0 < 0) eta0 = eta;
+        if (eta0 < 0) eta0 = eta > eta_b ? eta : eta_b;
         relres = eta0 > 0 ? eta / eta0 : 0.0;
         if (eta == 0.0 || eta <= c->prm.rtol * eta0) break;
         if (iters >= maxit) {
@@ -2148,7 +2185,14 @@ __global__ void k_seg_add(const int64_t* __restrict__ lo, const int32_t* __restr
 }
 
 // Per-instance scalars (BatchVals rows of ninst doubles).
-enum BatchVals { BV_NR2, BV_NB2, BV_Q, BV_RSCALE, BV_SIN, BV_SOUT, BV_ETA, BV_ETA0, BV_DONE, BV_COUNT };
+enum BatchVals { BV_NR2, BV_NB2, BV_Q, BV_RSCALE, BV_SIN, BV_SOUT, BV_ETA, BV_ETA0, BV_DONE, BV_QB, BV_COUNT };
+
+__global__ void k_batch_bscale(int ninst, double* iv) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= ninst) return;
+    const double nb = sqrt(iv[BV_NB2 * ninst + i]);
+    iv[BV_RSCALE * ninst + i] = nb > 0.0 ? 1.0 / nb : 0.0;
+}
 
 __global__ void k_batch_rscale(int ninst, double* iv) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
@@ -2165,7 +2209,12 @@ __global__ void k_batch_status(int ninst, double* iv, double rtol, int first) {
     const double q = iv[BV_Q * ninst + i];
     const double beta = q > 0.0 ? sqrt(q) : 0.0;
     const double eta = beta * nr;
-    if (first) iv[BV_ETA0 * ninst + i] = eta;
+    if (first) {
+        // the larger of the initial residual's and the right-hand side's preconditioned norms
+        const double qb = iv[BV_QB * ninst + i];
+        const double eta_b = (qb > 0.0 ? sqrt(qb) : 0.0) * sqrt(iv[BV_NB2 * ninst + i]);
+        iv[BV_ETA0 * ninst + i] = eta > eta_b ? eta : eta_b;
+    }
     const double eta0 = iv[BV_ETA0 * ninst + i];
     const bool done = !(eta > 0.0) || eta <= rtol * eta0;
     iv[BV_ETA * ninst + i] = eta;
@@ -2393,6 +2442,17 @@ static int solve_batch(mpet_ctx* c, const double* b, double* x, mpet_stats* st, 
         k_seg_norms<<<(unsigned)nch, 256, 0, c->stream>>>(c->ch_lo, c->ch_len, nch, c->orr, b, c->dinv, c->ch_part);
         k_seg_finish<<<gi, 128, 0, c->stream>>>(ni, c->inst_cptr, c->inst_chunks, c->ch_part, nch, 2,
                                                 iv + BV_NR2 * ni);
+        if (outer == 0) {
+            // right-hand sides scaled by 1 / ||D^-1 b_i||, their preconditioned squared norms (BV_QB)
+            k_batch_bscale<<<gi, 128, 0, c->stream>>>(ni, iv);
+            k_seg_scale_from64<T><<<(unsigned)nch, 256, 0, c->stream>>>(c->ch_lo, c->ch_len, c->ch_inst, b,
+                                                                        iv + BV_RSCALE * ni, rhs);
+            precond<T>(c, rhs, y);
+            k_seg_dot<T><<<(unsigned)nch, 256, 0, c->stream>>>(c->ch_lo, c->ch_len, nch, rhs, y, c->ch_part);
+            k_seg_finish<<<gi, 128, 0, c->stream>>>(ni, c->inst_cptr, c->inst_chunks, c->ch_part, nch, 1,
+                                                    iv + BV_QB * ni);
+            MPET_CHECK_LAUNCH();
+        }
         k_batch_rscale<<<gi, 128, 0, c->stream>>>(ni, iv);
         k_seg_scale_from64<T><<<(unsigned)nch, 256, 0, c->stream>>>(c->ch_lo, c->ch_len, c->ch_inst, c->orr,
                                                                     iv + BV_RSCALE * ni, rhs);
@@ -2746,11 +2806,13 @@ static int solve_gmres(mpet_ctx* c, const double* b, double* x, mpet_stats* st, 
     const bool fp64 = sizeof(T) == 8;
     const int max_outer = c->prm.max_outer > 0 ? c->prm.max_outer : 20;
     const int maxit = c->prm.maxit > 0 ? c->prm.maxit : 5000;
+    double eta_b = 0.0;
     for (outer = 0; outer < max_outer; ++outer) {
         launch_spmv<double, 1>(c, c->A, c->A.v64, x, EpiResid64{c->orr, b, c->dinv});
         c->n_spmv++;
         k_outer_norms<<<1, 256, 0, c->stream>>>(c->sc, c->partials);
         MPET_CHECK_LAUNCH();
+        if (outer == 0) eta_b = precond_norm_b<T>(c, b);
         MPET_CUDA(cudaMemcpyAsync(c->sc_host, c->sc, sizeof(MinresScalars), cudaMemcpyDeviceToHost, c->stream));
         MPET_CUDA(cudaStreamSynchronize(c->stream));
         const MinresScalars h = *c->sc_host;
@@ -2763,7 +2825,7 @@ static int solve_gmres(mpet_ctx* c, const double* b, double* x, mpet_stats* st, 
         precond<T>(c, rhs, (T*)c->kr[2]);
         gm_dots<T>(c, rhs, 1, (const T*)c->kr[2]);
         const double eta = nr * sqrt(fmax(c->gm_h_host[0], 0.0));
-        if (eta0 < 0) eta0 = eta;
+        if (eta0 < 0) eta0 = eta > eta_b ? eta : eta_b;
         relres = eta0 > 0 ? eta / eta0 : 0.0;
         if (!(eta == eta)) {
             status = MPET_ERR_BREAKDOWN;
