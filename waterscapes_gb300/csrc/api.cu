@@ -238,6 +238,7 @@ int mpet_update_params(mpet_ctx* c, const mpet_params* p) {
     if (c->prm.inner_rtol <= 0) c->prm.inner_rtol = 1e-4;
     c->assembled = false;
     c->precond_ready = false;
+    c->u_hier_valid = false;
     API_END(c)
 }
 
@@ -487,6 +488,7 @@ int mpet_set_batch(mpet_ctx* c, int32_t ninst, const int32_t* vertex_instance) {
     setup_batch(c, ninst, vertex_instance);
     set_instances(c, ninst, vertex_instance);
     c->precond_ready = false;
+    c->u_hier_valid = false;
     API_END(c)
 }
 
@@ -545,7 +547,10 @@ int mpet_setup_preconditioner(mpet_ctx* c, double dt) {
     auto t0 = clk::now();
     setup_network_modes(c, dt);
     launch_assemble_prec_blocks(c, dt);
-    if (c->prm.prec_u_form != 1) launch_mf_cells(c, dt);
+    // the displacement block w (grad u, grad v) depends on neither dt nor K, c, S: its
+    // hierarchy is kept from the last set-up unless the parameters changed
+    const bool reuse_u = c->u_hier_valid && c->prm.prec_u_form != 1;
+    if (c->prm.prec_u_form != 1 && !reuse_u) launch_mf_cells(c, dt);
     MPET_CUDA(cudaStreamSynchronize(c->stream));
     c->setup_ms[0] = since(t0);  // block assembly on the GPU
     t0 = clk::now();
@@ -579,7 +584,8 @@ int mpet_setup_preconditioner(mpet_ctx* c, double dt) {
     // hierarchies concurrently (threads sharing the host cores), then uploads
     HostCsr hu, P0;
     bool use_p0 = false;
-    if (!elast) {
+    const bool build_u = !elast && !reuse_u;
+    if (build_u) {
         c->u_elast = false;
         fetch(c->Lu, hu);
         if (c->prm.amg_p2_to_p1) {
@@ -635,7 +641,7 @@ int mpet_setup_preconditioner(mpet_ctx* c, double dt) {
     HostAmg hau;
     std::vector<HostAmg> hap(c->J);
     {
-        const int ntask = c->J + (elast ? 0 : 1);
+        const int ntask = c->J + (build_u ? 1 : 0);
         const int nth = std::max(1, host_threads() / ntask);
         std::vector<std::exception_ptr> errs(ntask);
         std::vector<std::thread> th;
@@ -648,7 +654,7 @@ int mpet_setup_preconditioner(mpet_ctx* c, double dt) {
                     errs[a] = std::current_exception();
                 }
             });
-        if (!elast)
+        if (build_u)
             th.emplace_back([&] {
                 try {
                     amg_setup_host(std::move(hu), use_p0 ? &P0 : nullptr, theta, cs, 12, hau, nth, true);
@@ -662,7 +668,10 @@ int mpet_setup_preconditioner(mpet_ctx* c, double dt) {
     }
     c->setup_ms[2] = since(t0);  // host hierarchies (concurrent)
     t0 = clk::now();
-    if (!elast) upload_amg(c, c->amg_u, hau, 4, fp32);
+    if (build_u) {
+        upload_amg(c, c->amg_u, hau, 4, fp32);
+        c->u_hier_valid = true;
+    }
     for (int a = 0; a < c->J; ++a) upload_amg(c, c->amg_p[a], hap[a], 1, fp32);
     c->setup_ms[3] = since(t0);  // uploads + autotuning
     c->precond_ready = true;
@@ -841,6 +850,7 @@ int mpet_set_prec_matrix_free(mpet_ctx* c, int32_t mode) {
     require(mode >= -1 && mode <= 1, MPET_ERR_INVALID, "mode: -1 (autotuned), 0 (CSR) or 1 (matrix-free)");
     c->mf_mode = mode;
     c->precond_ready = false;
+    c->u_hier_valid = false;
     API_END(c)
 }
 

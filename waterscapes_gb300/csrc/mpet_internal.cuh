@@ -325,6 +325,7 @@ struct mpet_ctx {
     double* adj_loss = nullptr;   // misfit value (1 double)
     double* elem_buf = nullptr;   // staged per-cell element data of the assembly, or null
     bool u_elast = false;         // displacement preconditioner block: elasticity AMG (else Laplacian)
+    bool u_hier_valid = false;    // the Laplacian displacement hierarchy can be kept by the next set-up
     // matrix-free first level of the displacement hierarchy: per-cell data (nc x 8
     // floats or doubles), the float tables of its element operator, and the choice
     void* mf_cell = nullptr;
