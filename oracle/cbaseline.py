@@ -62,11 +62,6 @@ def load():
         _lib.oracle_minres.restype = ctypes.c_int
         _lib.oracle_minres.argtypes = [ctypes.POINTER(OCsr), _P, _P, ctypes.POINTER(OPrec), _D, ctypes.c_int,
                                        ctypes.POINTER(_D)]
-        _lib.oracle_minres_ref.restype = ctypes.c_int
-        _lib.oracle_minres_ref.argtypes = [ctypes.POINTER(OCsr), _P, _P, ctypes.POINTER(OPrec), _D, ctypes.c_int, _D,
-                                           ctypes.POINTER(_D)]
-        _lib.oracle_prec_norm.restype = _D
-        _lib.oracle_prec_norm.argtypes = [ctypes.POINTER(OPrec), _P, _I64]
         _lib.oracle_hier_work.restype = _I64
         _lib.oracle_hier_work.argtypes = [ctypes.c_int, _P]
         _lib.oracle_node_adjacency.restype = ctypes.c_int
@@ -160,13 +155,10 @@ def aggregate(S):
     return agg[:n], int(nagg)
 
 
-def minres_raw(rp, ci, v, b, x, hu, hp, dim, Nu, nv, Q=None, rtol=1e-10, maxiter=5000, rhs_relative=False):
+def minres_raw(rp, ci, v, b, x, hu, hp, dim, Nu, nv, Q=None, rtol=1e-10, maxiter=5000):
     """x += MINRES(A, b - A x) in place, A given by CSR arrays (int64 rp, int32
     ci, float64 v; used without copies); preconditioned like
-    krylov.block_preconditioner.  Stops at rtol times the preconditioned norm of
-    the initial residual or, with rhs_relative, of the larger of that and the
-    right-hand side's (PETSc's default test for a warm-started solve, as the GPU
-    solver measures).  Returns (iterations, final relative residual)."""
+    krylov.block_preconditioner.  Returns (iterations, final phibar / beta1)."""
     lib = load()
     k = _Keep()
     n = rp.shape[0] - 1
@@ -183,10 +175,9 @@ def minres_raw(rp, ci, v, b, x, hu, hp, dim, Nu, nv, Q=None, rtol=1e-10, maxiter
     M = OPrec(Nu, nv, nnodes, dim, J, ctypes.pointer(hu_s), hp_s, q, scratch.ctypes.data)
     bb = k.arr(b, np.float64)
     rel = _D()
-    ref = lib.oracle_prec_norm(ctypes.byref(M), bb.ctypes.data, bb.shape[0]) if rhs_relative else 0.0
-    it = lib.oracle_minres_ref(ctypes.byref(Ac), bb.ctypes.data, x.ctypes.data, ctypes.byref(M), rtol, maxiter,
-                               ref, ctypes.byref(rel))
-    if it < 0 or ref < 0:
+    it = lib.oracle_minres(ctypes.byref(Ac), bb.ctypes.data, x.ctypes.data, ctypes.byref(M), rtol, maxiter,
+                           ctypes.byref(rel))
+    if it < 0:
         raise MemoryError("oracle MINRES could not allocate its vectors")
     return it, rel.value
 
@@ -320,17 +311,16 @@ class CSystem:
         self.hp = [krylov.SAHierarchy(B, theta=theta, cheb_degree=cheb_degree, aggregate_fn=aggregate)
                    for B in self.Pk]
 
-    def step(self, up_prev, bc_values, rtol=1e-10, maxiter=5000, rhs_relative=False):
+    def step(self, up_prev, bc_values, rtol=1e-10, maxiter=5000):
         """One solve_direct step: b = B up_ with the Dirichlet values
         ``bc_values`` (aligned with ``bc_dofs``) in its Dirichlet rows, solved
-        by MINRES from up_ with those values set (stopping rule: minres_raw).
-        Returns (up, iterations)."""
+        by MINRES from up_ with those values set.  Returns (up, iterations)."""
         b = self.rhs_prev(up_prev)
         b[self.bc_dofs] = bc_values
         x = np.array(up_prev, dtype=np.float64, copy=True)
         x[self.bc_dofs] = bc_values
         it, rel = minres_raw(self.rp, self.ci, self.A, b, x, self.hu, self.hp, self.d, self.Nu, self.nv, Q=self.Q,
-                             rtol=rtol, maxiter=maxiter, rhs_relative=rhs_relative)
+                             rtol=rtol, maxiter=maxiter)
         if not rel <= rtol:
             raise RuntimeError("oracle MINRES stopped at relative residual %.3e after %d iterations" % (rel, it))
         return x, it

@@ -185,35 +185,9 @@ static double dot(int64_t n, const double* a, const double* b) {
     return s;
 }
 
-/* Preconditioned norm (b^T M b)^1/2 of a vector (M: the block V-cycles). */
-double oracle_prec_norm(const oprec* M, const double* b, int64_t n) {
-    double* y = (double*)calloc((size_t)n, sizeof(double));
-    if (!y) return -1.0;
-    precond(M, b, y);
-    const double q = dot(n, b, y);
-    free(y);
-    return sqrt(fmax(q, 0.0));
-}
-
-static int minres_core(const ocsr* A, const double* b, double* x, const oprec* M, double rtol, int maxit,
-                       double ref, double* rel);
-
 /* x += MINRES(A, b - A x); returns iterations, writes phibar/beta1 to *rel. */
 int oracle_minres(const ocsr* A, const double* b, double* x, const oprec* M, double rtol, int maxit,
                   double* rel) {
-    return minres_core(A, b, x, M, rtol, maxit, 0.0, rel);
-}
-
-/* The same, stopping at phibar <= rtol * max(beta1, ref): with ref the preconditioned
- * norm of the right-hand side this is PETSc's default test (relative to the
- * right-hand side) for a warm-started solve. */
-int oracle_minres_ref(const ocsr* A, const double* b, double* x, const oprec* M, double rtol, int maxit,
-                      double ref, double* rel) {
-    return minres_core(A, b, x, M, rtol, maxit, ref, rel);
-}
-
-static int minres_core(const ocsr* A, const double* b, double* x, const oprec* M, double rtol, int maxit,
-                       double ref, double* rel) {
     const int64_t n = A->n;
     double* buf = (double*)calloc((size_t)n * 9, sizeof(double));
     if (!buf) return -1;
@@ -224,7 +198,6 @@ static int minres_core(const ocsr* A, const double* b, double* x, const oprec* M
     for (int64_t i = 0; i < n; ++i) r1[i] = b[i] - t[i];
     precond(M, r1, y);
     const double beta1 = sqrt(fmax(dot(n, r1, y), 0.0));
-    const double bref = ref > beta1 ? ref : beta1;
     *rel = 1.0;
     if (beta1 == 0.0) {
         free(buf);
@@ -274,8 +247,8 @@ static int minres_core(const ocsr* A, const double* b, double* x, const oprec* M
             w2[i] = wn;
             x[i] += phi * wn;
         }
-        *rel = phibar / bref;
-        if (phibar <= rtol * bref) break;
+        *rel = phibar / beta1;
+        if (phibar <= rtol * beta1) break;
     }
     free(buf);
     return it;

@@ -1932,11 +1932,12 @@ __global__ void k_scale_b(int64_t n, const double* __restrict__ b, T* out, const
 
 // Preconditioned norm (b^T M^-1 b)^1/2 of the right-hand side, in the working
 // precision, after the first refinement residual (which left ||D^-1 b||^2 in the
-// scalars).  The refinement stops at rtol times the larger of this norm and the
-// initial residual's, as PETSc's default convergence test measures against the
-// right-hand side (the reference's iterative solves, mpetsolver.py:507-556):
-// relative to a warm-started initial residual alone, a good initial guess would
-// push the target below what FP64 residuals resolve.  kr[0] and kr[2] are scratch.
+// scalars).  The refinement stops when the preconditioned residual is rtol times
+// the initial one; after a very good warm start that can lie below what FP64
+// residuals resolve, so it also stops when a sweep no longer halves the residual
+// and the residual is already below rtol times this norm (PETSc's default test,
+// the reference's iterative solves mpetsolver.py:507-556, measures against the
+// right-hand side).  kr[0] and kr[2] are scratch.
 template <typename T>
 static double precond_norm_b(mpet_ctx* c, const double* b) {
     const int64_t n = c->N;
@@ -1977,7 +1978,7 @@ static int solve_impl(mpet_ctx* c, const double* b, double* x, mpet_stats* st, b
     const bool fp64 = sizeof(T) == 8;
     const int max_outer = c->prm.max_outer > 0 ? c->prm.max_outer : 20;
     const int maxit = c->prm.maxit > 0 ? c->prm.maxit : 5000;
-    double eta_b = 0.0;
+    double eta_b = 0.0, eta_prev = 0.0;
     for (outer = 0; outer < max_outer; ++outer) {
         launch_spmv<double, 1>(c, c->A, c->A.v64, x, EpiResid64{c->orr, b, c->dinv});
         c->n_spmv++;
@@ -2004,9 +2005,11 @@ static int solve_impl(mpet_ctx* c, const double* b, double* x, mpet_stats* st, b
             break;
         }
         const double eta = h.beta1 * nr;
-        if (eta0 < 0) eta0 = eta > eta_b ? eta : eta_b;
+        if (eta0 < 0) eta0 = eta;
         relres = eta0 > 0 ? eta / eta0 : 0.0;
         if (eta == 0.0 || eta <= c->prm.rtol * eta0) break;
+        if (outer > 0 && eta > 0.5 * eta_prev && eta <= c->prm.rtol * eta_b) break;  // FP64 floor
+        eta_prev = eta;
         if (iters >= maxit) {
             status = MPET_ERR_MAXIT;
             break;
@@ -2185,7 +2188,8 @@ __global__ void k_seg_add(const int64_t* __restrict__ lo, const int32_t* __restr
 }
 
 // Per-instance scalars (BatchVals rows of ninst doubles).
-enum BatchVals { BV_NR2, BV_NB2, BV_Q, BV_RSCALE, BV_SIN, BV_SOUT, BV_ETA, BV_ETA0, BV_DONE, BV_QB, BV_COUNT };
+enum BatchVals { BV_NR2, BV_NB2, BV_Q, BV_RSCALE, BV_SIN, BV_SOUT, BV_ETA, BV_ETA0, BV_DONE, BV_QB, BV_ETAB,
+                 BV_COUNT };
 
 __global__ void k_batch_bscale(int ninst, double* iv) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
@@ -2210,13 +2214,15 @@ __global__ void k_batch_status(int ninst, double* iv, double rtol, int first) {
     const double beta = q > 0.0 ? sqrt(q) : 0.0;
     const double eta = beta * nr;
     if (first) {
-        // the larger of the initial residual's and the right-hand side's preconditioned norms
-        const double qb = iv[BV_QB * ninst + i];
-        const double eta_b = (qb > 0.0 ? sqrt(qb) : 0.0) * sqrt(iv[BV_NB2 * ninst + i]);
-        iv[BV_ETA0 * ninst + i] = eta > eta_b ? eta : eta_b;
+        iv[BV_ETA0 * ninst + i] = eta;
+        const double qb = iv[BV_QB * ninst + i];  // the right-hand side's preconditioned norm
+        iv[BV_ETAB * ninst + i] = (qb > 0.0 ? sqrt(qb) : 0.0) * sqrt(iv[BV_NB2 * ninst + i]);
     }
     const double eta0 = iv[BV_ETA0 * ninst + i];
-    const bool done = !(eta > 0.0) || eta <= rtol * eta0;
+    // done at rtol of the initial residual, or (FP64 floor) when a sweep no longer
+    // halves the residual and it is below rtol of the right-hand side's norm
+    const bool floor = !first && eta > 0.5 * iv[BV_ETA * ninst + i] && eta <= rtol * iv[BV_ETAB * ninst + i];
+    const bool done = !(eta > 0.0) || eta <= rtol * eta0 || floor;
     iv[BV_ETA * ninst + i] = eta;
     iv[BV_DONE * ninst + i] = done ? 1.0 : 0.0;
     iv[BV_SIN * ninst + i] = done ? 0.0 : 1.0 / beta;
@@ -2806,7 +2812,7 @@ static int solve_gmres(mpet_ctx* c, const double* b, double* x, mpet_stats* st, 
     const bool fp64 = sizeof(T) == 8;
     const int max_outer = c->prm.max_outer > 0 ? c->prm.max_outer : 20;
     const int maxit = c->prm.maxit > 0 ? c->prm.maxit : 5000;
-    double eta_b = 0.0;
+    double eta_b = 0.0, eta_prev = 0.0;
     for (outer = 0; outer < max_outer; ++outer) {
         launch_spmv<double, 1>(c, c->A, c->A.v64, x, EpiResid64{c->orr, b, c->dinv});
         c->n_spmv++;
@@ -2825,13 +2831,15 @@ static int solve_gmres(mpet_ctx* c, const double* b, double* x, mpet_stats* st, 
         precond<T>(c, rhs, (T*)c->kr[2]);
         gm_dots<T>(c, rhs, 1, (const T*)c->kr[2]);
         const double eta = nr * sqrt(fmax(c->gm_h_host[0], 0.0));
-        if (eta0 < 0) eta0 = eta > eta_b ? eta : eta_b;
+        if (eta0 < 0) eta0 = eta;
         relres = eta0 > 0 ? eta / eta0 : 0.0;
         if (!(eta == eta)) {
             status = MPET_ERR_BREAKDOWN;
             break;
         }
         if (eta == 0.0 || eta <= c->prm.rtol * eta0) break;
+        if (outer > 0 && eta > 0.5 * eta_prev && eta <= c->prm.rtol * eta_b) break;  // FP64 floor
+        eta_prev = eta;
         if (iters >= maxit) {
             status = MPET_ERR_MAXIT;
             break;
