@@ -399,6 +399,16 @@ int mpet_set_element_kernel(mpet_ctx* ctx, int32_t kind);
  * reference counterpart (test hook). */
 int mpet_set_wait_limit(mpet_ctx* ctx, int32_t polls);
 
+/* Batches: whether the system and preconditioner products of the batched
+ * inner iterations skip the rows of instances that have converged (1, the
+ * default) or run over every instance (0).  The results of the instances
+ * still iterating are the same either way; skipping makes an iteration cost
+ * what the unconverged instances need.  Takes effect at the next solve;
+ * set before mpet_setup_preconditioner, it also lets the set-up autotuner
+ * offer the staged CSR kernel again (which cannot skip).  No reference
+ * counterpart (engine option and test hook). */
+int mpet_set_batch_skip(mpet_ctx* ctx, int32_t on);
+
 /* The same override for every matrix of the AMG hierarchies (operators,
  * prolongations, restrictions): each takes the variant where it can run and
  * the CSR register kernel (0) elsewhere, until the next

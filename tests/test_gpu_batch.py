@@ -62,3 +62,28 @@ def test_batch_matches_single_instances(precision):
             b = batch_states[k][i]
             assert np.linalg.norm(b - single) <= 1e-8 * np.linalg.norm(single)
             assert np.linalg.norm(b - ref[k]) <= 1e-8 * np.linalg.norm(ref[k])
+
+
+@pytest.mark.parametrize("precision", ["fp64", "mixed"])
+def test_batch_skipping_converged_instances_keeps_results(precision):
+    """The batched products skip the rows of instances that have converged
+    (mpet_set_batch_skip, on by default); every instance's trajectory must be
+    the one it follows when every product runs over all instances (within
+    the 1e-8 bar: the two runs may tune different SpMV kernels)."""
+    from waterscapes_gb300 import MPETBatchSolver
+    dt, steps = 0.02, 2
+    params = dict(dt=dt, T=steps * dt, theta=1.0, precision=precision, rtol=1e-10)
+    runs = []
+    for skip in (1, 0):
+        bs = MPETBatchSolver(_batch_problems(), params)
+        bs._ctx.call("mpet_set_batch_skip", skip)
+        states = []
+        for up, t in bs.solve_direct():
+            assert np.all(bs.batch_relres() <= 1e-10)
+            states.append([bs.instance_vector(i).cpu().numpy() for i in range(bs.ninst)])
+        runs.append(states)
+        bs.ctx.close()
+    for k in range(steps):
+        for i in range(3):
+            a, b = runs[0][k][i], runs[1][k][i]
+            assert np.linalg.norm(a - b) <= 1e-8 * np.linalg.norm(b)

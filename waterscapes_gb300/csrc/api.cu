@@ -673,6 +673,7 @@ int mpet_setup_preconditioner(mpet_ctx* c, double dt) {
         c->u_hier_valid = true;
     }
     for (int a = 0; a < c->J; ++a) upload_amg(c, c->amg_p[a], hap[a], 1, fp32);
+    if (c->ninst > 0) build_skip_maps(c);
     c->setup_ms[3] = since(t0);  // uploads + autotuning
     c->precond_ready = true;
     c->prec_dt = dt;
@@ -877,6 +878,14 @@ int mpet_set_wait_limit(mpet_ctx* c, int32_t polls) {
     API_BEGIN(c)
     require(polls >= 0, MPET_ERR_INVALID, "wait limit must be >= 0");
     c->mbar_spin_limit = polls > 0 ? polls : 0;
+    API_END(c)
+}
+
+int mpet_set_batch_skip(mpet_ctx* c, int32_t on) {
+    API_BEGIN(c)
+    require(on == 0 || on == 1, MPET_ERR_INVALID, "batch skip: 0 or 1");
+    c->batch_skip = on == 1;
+    destroy_minres_graph(c);
     API_END(c)
 }
 

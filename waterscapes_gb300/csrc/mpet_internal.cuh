@@ -120,6 +120,7 @@ struct NodeBlocks {
     double* v64 = nullptr;
     int64_t ncols = 0, nvals = 0;  // stored (with padding)
     int64_t nblocks = 0;           // blocks of the matrix (without padding)
+    int32_t* skl = nullptr;        // batches: lowest and highest instance of each slice's lanes
 };
 
 struct Csr {
@@ -153,6 +154,10 @@ struct Csr {
     double* s_v64 = nullptr;
     // node-block copy (system matrix only; variant 8)
     NodeBlocks* nb = nullptr;
+    // batches: per 32-row slice the lowest and highest instance of its rows
+    // (lo > hi for a slice without rows); the products of the batched
+    // iterations skip a slice whose instances have all converged
+    int32_t* skl = nullptr;
 };
 
 struct AmgLevel {
@@ -169,6 +174,7 @@ struct AmgLevel {
     void* d = nullptr;
     void* t0 = nullptr;
     void* t1 = nullptr;
+    int32_t* inst = nullptr;  // batches: instance of each row
 };
 
 struct AmgHier {
@@ -402,6 +408,13 @@ struct mpet_ctx {
     double* bval = nullptr;                   // per-instance reduced sums
     cudaGraphExec_t bmr_graph = nullptr;
     int64_t bmr_graph_launches = 0;
+    // instance of each P2 node (vertices first), the skip maps of the matrices
+    // (Csr::skl) once built, and the done flags the products test (set only
+    // while the batched iterations are captured; null: no product skips)
+    int32_t* node_inst = nullptr;
+    bool skip_maps = false;
+    bool batch_skip = true;  // skip converged instances' slices (test hook: false)
+    const double* skip_done = nullptr;
 
     // rigid-motion modes of the displacement (nz x Nu, L2-orthonormal), their
     // mass-weighted duals M Z, the multipliers of the last solve and a
@@ -523,6 +536,8 @@ void launch_elem_uu_tc(mpet_ctx* c, double mu, double lmbda, double* out);
 template <typename T>
 void spmv(mpet_ctx* c, const Csr& A, int nvec, const T* x, T* y);
 void upload_amg(mpet_ctx* c, AmgHier& h, const HostAmg& ha, int nvec, bool fp32);
+// frees the device arrays of a hierarchy (before it is rebuilt)
+void release_hier(mpet_ctx* c, AmgHier& h);
 // homogeneous: the Dirichlet entries of x are zero (adjoint solves) instead
 // of the values set by mpet_set_bc_values
 int solve_system(mpet_ctx* c, const double* b, double* x, mpet_stats* st, bool homogeneous = false);
@@ -532,6 +547,9 @@ void residual_norms(mpet_ctx* c, const double* b, const double* x, double* r, do
 void apply_preconditioner(mpet_ctx* c, int precision, const void* r, void* z);
 void profile_vcycle(mpet_ctx* c, int block, int reps, int* nlev, double* ms, double* bytes);
 void setup_batch(mpet_ctx* c, int ninst, const int32_t* vertex_inst);
+// batches: per-slice instance ranges of the system matrix and of every level
+// of the Laplacian-form hierarchies (after each preconditioner set-up)
+void build_skip_maps(mpet_ctx* c);
 void batch_relres(mpet_ctx* c, double* out);
 int choose_lpr(int64_t n, int64_t nnz);
 void build_tiles(mpet_ctx* c, Csr& A, const int64_t* rp_host);

@@ -20,6 +20,7 @@
 //
 // All reductions are deterministic: a fixed grid of NB_RED blocks writes one
 // partial per block and a single block sums the partials in a fixed order.
+#include <limits.h>
 #include <math.h>
 
 #include <algorithm>
@@ -210,10 +211,24 @@ struct EpiResid64 {
     }
 };
 
+// Batches: slice s (32 rows, or 32 node-block lanes) belongs to instances
+// skl[2s]..skl[2s+1] (lo > hi: no rows); it is skipped, with no load and no
+// store, when every one of them has converged (done != 0).  The products of a
+// converged instance are never read again in the inner solve.
+__device__ __forceinline__ bool slice_frozen(const int32_t* __restrict__ skl, int64_t s,
+                                             const double* __restrict__ done) {
+    const int lo = skl[2 * s], hi = skl[2 * s + 1];
+    for (int i = lo; i <= hi; ++i)
+        if (done[i] == 0.0) return false;
+    return true;
+}
+
 template <typename T, int NV, int LPR, int U, class Epi>
 __global__ void __launch_bounds__(256) k_spmv(int64_t n, const int64_t* __restrict__ rp,
                                               const int32_t* __restrict__ ci, const T* __restrict__ va,
-                                              const T* __restrict__ x, Epi epi, double* partials) {
+                                              const T* __restrict__ x, Epi epi, double* partials,
+                                              const int32_t* __restrict__ skl = nullptr,
+                                              const double* __restrict__ skip = nullptr) {
     constexpr int RPW = 32 / LPR;  // rows per warp per pass
     const int lane = threadIdx.x & 31;
     const int sub = lane & (LPR - 1);
@@ -222,6 +237,8 @@ __global__ void __launch_bounds__(256) k_spmv(int64_t n, const int64_t* __restri
     const int64_t nwarps = ((int64_t)gridDim.x * blockDim.x) >> 5;
     double r0 = 0.0, r1 = 0.0;
     for (int64_t base = warp * RPW; base < n; base += nwarps * RPW) {
+        // the RPW rows of this pass lie in one 32-row slice (RPW divides 32)
+        if (skl && slice_frozen(skl, base >> 5, skip)) continue;
         const int64_t row = base + grp;
         T acc[NV];
 #pragma unroll
@@ -288,12 +305,15 @@ __global__ void __launch_bounds__(256) k_spmv(int64_t n, const int64_t* __restri
 template <typename T, int NV, int U, class Epi>
 __global__ void __launch_bounds__(256) k_spmv_sell(int64_t n, int64_t nslices, const int64_t* __restrict__ soff,
                                                    const int32_t* __restrict__ sci, const T* __restrict__ sva,
-                                                   const T* __restrict__ x, Epi epi, double* partials) {
+                                                   const T* __restrict__ x, Epi epi, double* partials,
+                                                   const int32_t* __restrict__ skl = nullptr,
+                                                   const double* __restrict__ skip = nullptr) {
     const int lane = threadIdx.x & 31;
     const int64_t warp = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) >> 5;
     const int64_t nwarps = ((int64_t)gridDim.x * blockDim.x) >> 5;
     double r0 = 0.0, r1 = 0.0;
     for (int64_t sl = warp; sl < nslices; sl += nwarps) {
+        if (skl && slice_frozen(skl, sl, skip)) continue;
         const int64_t row = sl * 32 + lane;
         const int64_t o1 = soff[sl + 1];
         typename Epi::Pre pre{};
@@ -389,12 +409,14 @@ __global__ void __launch_bounds__(256, sizeof(T) == 8 ? 3 : 1) k_spmv_nb(int64_t
                                                  int64_t ns, const NbSlice* __restrict__ sl,
                                                  const int32_t* __restrict__ perm, const int32_t* __restrict__ cols,
                                                  const T* __restrict__ vals, const T* __restrict__ x, Epi epi,
-                                                 double* partials) {
+                                                 double* partials, const int32_t* __restrict__ skl = nullptr,
+                                                 const double* __restrict__ skip = nullptr) {
     const int lane = threadIdx.x & 31;
     const int64_t warp = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) >> 5;
     const int64_t nwarps = ((int64_t)gridDim.x * blockDim.x) >> 5;
     double r0 = 0.0, r1 = 0.0;
     for (int64_t s = warp; s < ns; s += nwarps) {
+        if (skl && slice_frozen(skl, s, skip)) continue;
         const NbSlice S = sl[s];
         const int32_t* c2 = cols + S.coff + lane;
         const int32_t* c1 = c2 + (int64_t)S.w2 * 32;
@@ -930,15 +952,16 @@ static void launch_nb(mpet_ctx* c, const NodeBlocks& nb, const T* x, const Epi& 
     const int J = c->J;
     cudaStream_t st = c->stream;
     const T* v = nb_vals<T>(nb);
+    const int32_t* skl = c->skip_done ? nb.skl : nullptr;
     if (J <= 2)
         k_spmv_nb<T, 2, Epi><<<blocks, 256, 0, st>>>(c->nnodes, c->nv, c->Nu, J, nb.nsu, ns, nb.sl, nb.perm,
-                                                     nb.cols, v, x, epi, c->partials);
+                                                     nb.cols, v, x, epi, c->partials, skl, c->skip_done);
     else if (J <= 4)
         k_spmv_nb<T, 4, Epi><<<blocks, 256, 0, st>>>(c->nnodes, c->nv, c->Nu, J, nb.nsu, ns, nb.sl, nb.perm,
-                                                     nb.cols, v, x, epi, c->partials);
+                                                     nb.cols, v, x, epi, c->partials, skl, c->skip_done);
     else
         k_spmv_nb<T, 8, Epi><<<blocks, 256, 0, st>>>(c->nnodes, c->nv, c->Nu, J, nb.nsu, ns, nb.sl, nb.perm,
-                                                     nb.cols, v, x, epi, c->partials);
+                                                     nb.cols, v, x, epi, c->partials, skl, c->skip_done);
     MPET_CHECK_LAUNCH();
     c->n_launch++;
 }
@@ -973,15 +996,19 @@ static void launch_spmv(mpet_ctx* c, const Csr& A, const T* va, const T* x, cons
             return;
         }
     }
+    const int32_t* skl = c->skip_done ? A.skl : nullptr;
+    const double* skip = c->skip_done;
     if ((variant & 4) && sell_vals<T>(A) && va == vals<T>(A)) {
         int blocks = Epi::kRed > 0 ? NB_RED : grid_for(A.nslices * 32, 256);
         if (Epi::kRed == 0 && blocks > 152 * 16) blocks = 152 * 16;
         if (variant & 1)
             k_spmv_sell<T, NV, 8, Epi><<<blocks, 256, 0, c->stream>>>(A.n, A.nslices, A.s_off, A.s_ci,
-                                                                      sell_vals<T>(A), x, epi, c->partials);
+                                                                      sell_vals<T>(A), x, epi, c->partials, skl,
+                                                                      skip);
         else
             k_spmv_sell<T, NV, 4, Epi><<<blocks, 256, 0, c->stream>>>(A.n, A.nslices, A.s_off, A.s_ci,
-                                                                      sell_vals<T>(A), x, epi, c->partials);
+                                                                      sell_vals<T>(A), x, epi, c->partials, skl,
+                                                                      skip);
         MPET_CHECK_LAUNCH();
         c->n_launch++;
         return;
@@ -1011,13 +1038,15 @@ static void launch_spmv(mpet_ctx* c, const Csr& A, const T* va, const T* x, cons
     cudaStream_t s = c->stream;
     switch (lpr) {
         case 32:
-            if (deep) k_spmv<T, NV, 32, 8, Epi><<<blocks, 256, 0, s>>>(A.n, A.rp, A.ci, va, x, epi, part);
-            else k_spmv<T, NV, 32, 4, Epi><<<blocks, 256, 0, s>>>(A.n, A.rp, A.ci, va, x, epi, part);
+            if (deep) k_spmv<T, NV, 32, 8, Epi><<<blocks, 256, 0, s>>>(A.n, A.rp, A.ci, va, x, epi, part, skl, skip);
+            else k_spmv<T, NV, 32, 4, Epi><<<blocks, 256, 0, s>>>(A.n, A.rp, A.ci, va, x, epi, part, skl, skip);
             break;
-        case 16: k_spmv<T, NV, 16, 4, Epi><<<blocks, 256, 0, s>>>(A.n, A.rp, A.ci, va, x, epi, part); break;
-        case 8: k_spmv<T, NV, 8, 4, Epi><<<blocks, 256, 0, s>>>(A.n, A.rp, A.ci, va, x, epi, part); break;
-        case 4: k_spmv<T, NV, 4, 4, Epi><<<blocks, 256, 0, s>>>(A.n, A.rp, A.ci, va, x, epi, part); break;
-        default: k_spmv<T, NV, 1, 4, Epi><<<blocks, 256, 0, s>>>(A.n, A.rp, A.ci, va, x, epi, part); break;
+        case 16:
+            k_spmv<T, NV, 16, 4, Epi><<<blocks, 256, 0, s>>>(A.n, A.rp, A.ci, va, x, epi, part, skl, skip);
+            break;
+        case 8: k_spmv<T, NV, 8, 4, Epi><<<blocks, 256, 0, s>>>(A.n, A.rp, A.ci, va, x, epi, part, skl, skip); break;
+        case 4: k_spmv<T, NV, 4, 4, Epi><<<blocks, 256, 0, s>>>(A.n, A.rp, A.ci, va, x, epi, part, skl, skip); break;
+        default: k_spmv<T, NV, 1, 4, Epi><<<blocks, 256, 0, s>>>(A.n, A.rp, A.ci, va, x, epi, part, skl, skip); break;
     }
     MPET_CHECK_LAUNCH();
     c->n_launch++;
@@ -1160,6 +1189,8 @@ static void autotune_matrix(mpet_ctx* c, Csr& A, const T* x, const Epi& epi, dou
         for (int v : {0, 1, 2, 3, 4, 5, 8}) {
             if (!spmv_variant_available(A, v) || (v >= 4 && v < 8 && (!sell_vals<T>(A) || lpr != lpr0))) continue;
             if (v == 8 && (!Epi::kSystem || NV != 1 || !nb_vals<T>(*A.nb) || lpr != lpr0)) continue;
+            // batches: the staged kernel has no slice skipping
+            if (c->ninst > 0 && c->batch_skip && v < 4 && (v & 2)) continue;
             A.variant = v;
             launch_spmv<T, NV>(c, A, vals<T>(A), x, epi);
             float t[5];
@@ -1647,6 +1678,13 @@ static void minres_three(mpet_ctx* c) {
     T* d = (T*)c->kd;
     int ir1 = 0, ir2 = 1, iy = 2;
     int iw = 0, iw1 = 1, iw2 = 2;
+    // the products (system SpMV and preconditioner) skip the slices of
+    // instances that have converged
+    struct SkipScope {
+        mpet_ctx* c;
+        ~SkipScope() { c->skip_done = nullptr; }
+    } scope{c};
+    c->skip_done = (c->batch_skip && c->skip_maps) ? c->bdone : nullptr;
     for (int q = 0; q < 3; ++q) {
         T* r1 = (T*)c->kr[ir1];
         T* r2 = (T*)c->kr[ir2];
@@ -2608,8 +2646,128 @@ void setup_batch(mpet_ctx* c, int ninst, const int32_t* vertex_inst) {
     c->bval = c->pool.alloc<double>(ninst);
     MPET_CUDA(cudaMallocHost(&c->bsc_host, sizeof(MinresScalars) * ninst));
     MPET_CUDA(cudaMallocHost(&c->bdone_host, sizeof(double) * ninst));
+    c->node_inst = c->pool.alloc<int32_t>(c->nnodes);
+    MPET_CUDA(cudaMemcpyAsync(c->node_inst, node_inst.data(), sizeof(int32_t) * c->nnodes, cudaMemcpyHostToDevice,
+                              c->stream));
+    c->skip_maps = false;
     destroy_minres_graph(c);
     MPET_CUDA(cudaStreamSynchronize(c->stream));
+}
+
+// ---- skip maps of the batched products ------------------------------------------------
+
+// per 32-row slice: lowest and highest instance of its rows (0, -1 without rows)
+__global__ void k_skl_rows(int64_t n, int64_t nslices, const int32_t* __restrict__ ri, int ninst, int32_t* skl) {
+    const int64_t s = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    if (s >= nslices) return;
+    int lo = INT_MAX, hi = -1;
+    for (int64_t r = s * 32; r < s * 32 + 32 && r < n; ++r) {
+        const int i = ri[r];
+        if (i < 0 || i >= ninst) continue;
+        lo = i < lo ? i : lo;
+        hi = i > hi ? i : hi;
+    }
+    skl[2 * s] = hi >= 0 ? lo : 0;
+    skl[2 * s + 1] = hi;
+}
+
+// the system's DOF rows: displacement row r -> node r / dim, pressure row
+// Nu + a nv + v -> vertex v (vertices are the first P2 nodes)
+__global__ void k_skl_dofs(int64_t N, int64_t Nu, int64_t nv, int dim, int64_t nslices,
+                           const int32_t* __restrict__ node_inst, int32_t* skl) {
+    const int64_t s = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    if (s >= nslices) return;
+    int lo = INT_MAX, hi = -1;
+    for (int64_t r = s * 32; r < s * 32 + 32 && r < N; ++r) {
+        const int i = r < Nu ? node_inst[r / dim] : node_inst[(r - Nu) % nv];
+        lo = i < lo ? i : lo;
+        hi = i > hi ? i : hi;
+    }
+    skl[2 * s] = hi >= 0 ? lo : 0;
+    skl[2 * s + 1] = hi;
+}
+
+// node-block slices: the node (displacement slices) or vertex (pressure slices) of each lane
+__global__ void k_skl_nb(int64_t ns, const int32_t* __restrict__ perm, const int32_t* __restrict__ node_inst,
+                         int32_t* skl) {
+    const int64_t s = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    if (s >= ns) return;
+    int lo = INT_MAX, hi = -1;
+    for (int l = 0; l < 32; ++l) {
+        const int32_t g = perm[s * 32 + l];
+        if (g < 0) continue;
+        const int i = node_inst[g];
+        lo = i < lo ? i : lo;
+        hi = i > hi ? i : hi;
+    }
+    skl[2 * s] = hi >= 0 ? lo : 0;
+    skl[2 * s + 1] = hi;
+}
+
+// coarse rows take the instance of the fine rows that prolongate from them
+// (all of one instance: instance meshes share no entry)
+__global__ void k_coarse_inst(int64_t nf, const int64_t* __restrict__ rp, const int32_t* __restrict__ ci,
+                              const int32_t* __restrict__ fi, int32_t* co) {
+    const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    if (i >= nf) return;
+    for (int64_t e = rp[i]; e < rp[i + 1]; ++e) atomicMin(co + ci[e], fi[i]);
+}
+
+static int32_t* skl_of_rows(mpet_ctx* c, int64_t n, const int32_t* ri) {
+    const int64_t ns = (n + 31) / 32;
+    int32_t* skl = c->pool.alloc<int32_t>(2 * ns);
+    k_skl_rows<<<grid_for(ns, 256), 256, 0, c->stream>>>(n, ns, ri, c->ninst, skl);
+    MPET_CHECK_LAUNCH();
+    return skl;
+}
+
+// Instances of every level of a hierarchy whose first level's rows are given
+// (inst0: n0 instance ids), and the skip maps of each level's A, P and R.
+static void hier_skip_maps(mpet_ctx* c, AmgHier& h, const int32_t* inst0, int64_t n0) {
+    // (a kept hierarchy keeps its maps; a rebuilt one starts without)
+    if (h.lev.empty() || h.lev[0].A.n != n0 || h.lev[0].nb_uu || h.lev[0].inst) return;
+    for (size_t k = 0; k < h.lev.size(); ++k) {
+        AmgLevel& L = h.lev[k];
+        const int64_t n = L.A.n;
+        L.inst = c->pool.alloc<int32_t>(n);
+        if (k == 0) {
+            MPET_CUDA(cudaMemcpyAsync(L.inst, inst0, sizeof(int32_t) * n, cudaMemcpyDeviceToDevice, c->stream));
+        } else {
+            const AmgLevel& F = h.lev[k - 1];
+            if (F.P.n != F.A.n || F.P.m != n) fail(MPET_ERR_STATE, "prolongator shape does not match its levels");
+            MPET_CUDA(cudaMemsetAsync(L.inst, 0x7f, sizeof(int32_t) * n, c->stream));
+            k_coarse_inst<<<grid_for(F.A.n, 256), 256, 0, c->stream>>>(F.A.n, F.P.rp, F.P.ci, F.inst, L.inst);
+            MPET_CHECK_LAUNCH();
+        }
+        L.A.skl = skl_of_rows(c, n, L.inst);
+    }
+    for (size_t k = 0; k + 1 < h.lev.size(); ++k) {
+        AmgLevel& L = h.lev[k];
+        L.P.skl = skl_of_rows(c, L.P.n, L.inst);
+        L.R.skl = skl_of_rows(c, L.R.n, h.lev[k + 1].inst);
+    }
+}
+
+void build_skip_maps(mpet_ctx* c) {
+    if (c->ninst <= 0 || !c->node_inst) return;
+    if (!c->A.skl) {
+        const int64_t ns = (c->N + 31) / 32;
+        c->A.skl = c->pool.alloc<int32_t>(2 * ns);
+        k_skl_dofs<<<grid_for(ns, 256), 256, 0, c->stream>>>(c->N, c->Nu, c->nv, c->dim, ns, c->node_inst,
+                                                              c->A.skl);
+        MPET_CHECK_LAUNCH();
+    }
+    if (c->A.nb && !c->A.nb->skl) {
+        NodeBlocks& nb = *c->A.nb;
+        const int64_t ns = nb.nsu + nb.nsp;
+        nb.skl = c->pool.alloc<int32_t>(2 * ns);
+        k_skl_nb<<<grid_for(ns, 256), 256, 0, c->stream>>>(ns, nb.perm, c->node_inst, nb.skl);
+        MPET_CHECK_LAUNCH();
+    }
+    if (!c->u_elast) hier_skip_maps(c, c->amg_u, c->node_inst, c->nnodes);
+    for (int a = 0; a < c->J; ++a) hier_skip_maps(c, c->amg_p[a], c->node_inst, c->nv);
+    MPET_CUDA(cudaStreamSynchronize(c->stream));
+    c->skip_maps = true;
 }
 
 void batch_relres(mpet_ctx* c, double* out) {
@@ -3097,7 +3255,8 @@ static void choose_mf(mpet_ctx* c, AmgHier& h) {
     AmgLevel& L = h.lev[0];
     L.mf = false;
     c->mf_ms[0] = c->mf_ms[1] = 0.f;
-    if (!c->mf_cell || c->mf_mode == 0) return;
+    // batches keep the CSR level (its products skip converged instances)
+    if (!c->mf_cell || c->mf_mode == 0 || (c->ninst > 0 && c->batch_skip)) return;
     if (c->mf_mode == 1) {
         L.mf = true;
         return;
@@ -3130,11 +3289,33 @@ static void choose_mf(mpet_ctx* c, AmgHier& h) {
 
 static double csr_rho(mpet_ctx* c, const Csr& A, const double* dinv);
 
+static void release_csr(mpet_ctx* c, Csr& A) {
+    for (void* p : {(void*)A.rp, (void*)A.ci, (void*)A.v64, (void*)A.v32, (void*)A.tiles, (void*)A.s_off,
+                    (void*)A.s_ci, (void*)A.s_v32, (void*)A.s_v64, (void*)A.skl})
+        c->pool.release(p);
+    A = Csr();
+}
+
+void release_hier(mpet_ctx* c, AmgHier& h) {
+    for (AmgLevel& L : h.lev) {
+        release_csr(c, L.A);
+        release_csr(c, L.P);
+        release_csr(c, L.R);
+        for (void* p : {(void*)L.dinv64, (void*)L.dinv32, L.x, L.b, L.r, L.d, L.t0, L.t1, (void*)L.inst})
+            c->pool.release(p);
+    }
+    h.lev.clear();
+    for (void* p : {(void*)h.cinv, h.pack_in, h.pack_out}) c->pool.release(p);
+    h.cinv = nullptr;
+    h.pack_in = h.pack_out = nullptr;
+    h.ncoarse = 0;
+}
+
 void upload_amg(mpet_ctx* c, AmgHier& h, const HostAmg& ha, int nvec, bool fp32) {
+    release_hier(c, h);  // the arrays of an earlier set-up
     h.nvec = nvec;
     h.cheb_degree = c->prm.amg_cheb_degree > 0 ? c->prm.amg_cheb_degree : 4;
     h.cheb_degree0 = c->prm.amg_cheb_degree_fine > 0 ? c->prm.amg_cheb_degree_fine : h.cheb_degree;
-    h.lev.clear();
     h.lev.resize(ha.lev.size());
     for (size_t k = 0; k < ha.lev.size(); ++k) {
         const HostAmgLevel& hl = ha.lev[k];
