@@ -268,12 +268,13 @@ def spmv_tuning(solver, fp64=False):
 
 def prec_setup_ms(solver):
     """Split of the last preconditioner set-up (ms): GPU block assembly, block
-    downloads, host set-up of the hierarchies (concurrent), uploads + autotuning."""
+    downloads (host set-up only), the hierarchies (built on the GPU, or by
+    concurrent host threads), FP32 copies + SpMV layouts + uploads + autotuning."""
     import ctypes
     ms = np.zeros(4)
     solver.ctx.call("mpet_get_setup_timing", ms.ctypes.data_as(ctypes.c_void_p))
-    return {"blocks_gpu": round(ms[0], 1), "downloads": round(ms[1], 1),
-            "hierarchies_host": round(ms[2], 1), "upload_autotune": round(ms[3], 1)}
+    return {"where": solver.params.get("amg_setup", "device"), "blocks_gpu": round(ms[0], 1),
+            "downloads": round(ms[1], 1), "hierarchies": round(ms[2], 1), "layouts_autotune": round(ms[3], 1)}
 
 
 def launches(solver):
@@ -447,11 +448,13 @@ def adjoint_check(args):
     K_eval = np.stack([K0[a] * 10.0 ** rng.normal(0.0, 0.5, nc) for a in range(J)])
     dev = torch.device("cuda", 0)
     f64 = dict(dtype=torch.float64, device=dev)
-    solvers = {p: MPETSolver(problem, dict(dt=dt, T=1e9, theta=1.0, rtol=1e-12, precision=p))
+    where = args.amg_setup or "device"
+    solvers = {p: MPETSolver(problem, dict(dt=dt, T=1e9, theta=1.0, rtol=1e-12, precision=p, amg_setup=where))
                for p in ("mixed", "fp64")}
     # finite-difference solves start from the unperturbed state of their step
     # and reduce that O(h) residual by 1e-6 (far below h itself)
-    solvers["fd"] = MPETSolver(problem, dict(dt=dt, T=1e9, theta=1.0, rtol=1e-6, precision="mixed"))
+    solvers["fd"] = MPETSolver(problem, dict(dt=dt, T=1e9, theta=1.0, rtol=1e-6, precision="mixed",
+                                             amg_setup=where))
     zero = torch.zeros(solvers["mixed"].N, **f64)
 
     def driver(p, target):
@@ -506,6 +509,7 @@ def adjoint_check(args):
         errs.append(abs(fd - ad) / abs(ad))
     out["central_differences"] = {"directions": args.fd_dirs, "h": h, "max_rel_err": max(errs),
                                   "median_rel_err": statistics.median(errs), "seconds": time.perf_counter() - t0,
+                                  "amg_setup": where, "last_setup_ms": prec_setup_ms(solvers["fd"]),
                                   "path": "mixed precision with FP64 refinement; each perturbed solve starts "
                                           "from the unperturbed state (solved to 1e-12) and reduces the residual "
                                           "of the perturbation by 1e-6"}
@@ -715,6 +719,8 @@ def main():
     ap.add_argument("--coarse-size", type=int, default=None, help="override amg_coarse_size")
     ap.add_argument("--cheb-degree-fine", type=int, default=None,
                     help="override amg_cheb_degree_fine (the finest level of every hierarchy)")
+    ap.add_argument("--amg-setup", default=None, choices=["device", "host"],
+                    help="where the smoothed-aggregation hierarchies are built (default: device)")
     ap.add_argument("--inner-loop", default=None, choices=["device", "host"],
                     help="inner Krylov loop: one graph launch with a device-side loop, or host-checked replays")
     ap.add_argument("--prec-u-form", default=None, choices=["elasticity", "laplacian"],
@@ -801,6 +807,8 @@ def main():
         base["amg_cheb_degree_fine"] = args.cheb_degree_fine
     if args.inner_loop is not None:
         base["inner_loop"] = args.inner_loop
+    if args.amg_setup is not None:
+        base["amg_setup"] = args.amg_setup
     if args.prec_u_form is not None:
         base["prec_u_form"] = args.prec_u_form
     t0 = time.perf_counter()

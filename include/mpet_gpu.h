@@ -279,6 +279,26 @@ int mpet_get_prec_info(mpet_ctx* ctx, int32_t* u_elasticity);
  * (measurement of what hypre's set-up does inside PETSc, mpetsolver.py:507). */
 int mpet_get_setup_timing(mpet_ctx* ctx, double* ms4_host);
 
+/* Where mpet_setup_preconditioner builds the smoothed-aggregation
+ * hierarchies of the Laplacian-form blocks: 1 (default) on the GPU, from the
+ * blocks where they are assembled (strength, prolongator smoothing, Galerkin
+ * products and transposes in device kernels; the greedy aggregation pass and
+ * the coarsest dense inverse on the host); 0 on the host (blocks downloaded,
+ * hierarchies built by CPU threads, uploaded).  Both follow the same recipe
+ * and give the same hierarchies up to the rounding of their spectral-radius
+ * estimates.  Replaces the set-up half of the reference's hypre BoomerAMG
+ * (PETScKrylovSolver("minres", "hypre_amg"), src/mpet/mpet/mpetsolver.py:507;
+ * mpettotalpressuresolver.py:448).  The next set-up rebuilds everything. */
+int mpet_set_amg_setup(mpet_ctx* ctx, int32_t where);
+
+/* Copies out level `level` of hierarchy `block` (0 displacement, 1..J the
+ * networks): which = 0 its operator, 1 its prolongation (FP64 CSR, int64 row
+ * pointers).  Each output may be NULL; call once with rp, ci, v NULL for the
+ * sizes (n rows, m columns, nnz entries), then with arrays of n + 1, nnz and
+ * nnz elements.  No reference counterpart (inspection and test hook). */
+int mpet_get_amg_matrix(mpet_ctx* ctx, int32_t block, int32_t level, int32_t which, int64_t* n, int64_t* m,
+                        int64_t* nnz, int64_t* rp, int32_t* ci, double* v);
+
 /* Block-diagonal preconditioner (mpetsolver.py:264-271): one smoothed-
  * aggregation AMG hierarchy per diagonal block, built for this dt. */
 int mpet_setup_preconditioner(mpet_ctx* ctx, double dt);

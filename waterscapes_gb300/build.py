@@ -17,7 +17,7 @@ CSRC = os.path.join(HERE, "csrc")
 BUILD = os.path.join(HERE, "_build")
 LIB = os.path.join(HERE, "libmpetgpu.so")
 SOURCES = ["setup.cu", "assemble.cu", "elem_tc.cu", "facets.cu", "solve.cu", "api.cu", "noalloc.cu",
-           "amg_setup.cpp"]
+           "amg_device.cu", "amg_setup.cpp"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 
 
@@ -40,7 +40,9 @@ def _compile(src, extra=()):
     cmd = [nvcc(), "-std=c++17", "-O3", "-lineinfo", *ARCH, "-Xcompiler", "-fPIC,-fopenmp",
            "-c", path, "-o", out, *extra]
     if src.endswith(".cpp"):
-        cmd = [nvcc(), "-std=c++17", "-O3", "-x", "c++", "-Xcompiler", "-fPIC,-fopenmp",
+        # no fused multiply-add contraction on the host (aarch64 compilers contract by
+        # default): the host AMG set-up rounds like the device one
+        cmd = [nvcc(), "-std=c++17", "-O3", "-x", "c++", "-Xcompiler", "-fPIC,-fopenmp,-ffp-contract=off",
                "-c", path, "-o", out]
     r = subprocess.run(cmd, capture_output=True, text=True)
     if r.returncode != 0:

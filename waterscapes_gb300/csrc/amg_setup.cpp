@@ -227,7 +227,7 @@ static void strength(const HostCsr& A, double theta, HostCsr& S) {
     }
 }
 
-static int64_t aggregate(const HostCsr& S, std::vector<int64_t>& agg) {
+int64_t aggregate(const HostCsr& S, std::vector<int64_t>& agg) {
     const int64_t n = S.n;
     agg.assign(n, -1);
     int64_t nagg = 0;
@@ -264,7 +264,7 @@ static int64_t aggregate(const HostCsr& S, std::vector<int64_t>& agg) {
     return nagg;
 }
 
-static bool cholesky_inverse(std::vector<double>& a, int64_t n, std::vector<double>& inv) {
+bool cholesky_inverse(std::vector<double>& a, int64_t n, std::vector<double>& inv) {
     // in-place lower Cholesky of a (row-major n x n)
     for (int64_t j = 0; j < n; ++j) {
         double s = a[j * n + j];

@@ -580,11 +580,35 @@ int mpet_setup_preconditioner(mpet_ctx* c, double dt) {
         }
         c->u_elast = elast;
     }
+    const bool build_u = !elast && !reuse_u;
+    if (c->amg_device) {
+        // every hierarchy built where its block lies (amg_device.cu)
+        double ms[2], build = 0.0, finish = 0.0;
+        const double theta = c->prm.amg_theta;
+        if (build_u) {
+            c->u_elast = false;
+            amg_setup_device(c, c->amg_u, c->Lu, c->prm.amg_p2_to_p1 != 0, theta, cs, 12, 4, fp32, ms);
+            build += ms[0];
+            finish += ms[1];
+            c->u_hier_valid = true;
+        }
+        for (int a = 0; a < c->J; ++a) {
+            amg_setup_device(c, c->amg_p[a], c->Pp[a], false, theta, cs, 12, 1, fp32, ms);
+            build += ms[0];
+            finish += ms[1];
+        }
+        if (c->ninst > 0) build_skip_maps(c);
+        c->setup_ms[1] = 0.0;     // nothing downloaded
+        c->setup_ms[2] = build;   // hierarchies (device)
+        c->setup_ms[3] = finish;  // FP32 copies, layouts, autotuning
+        c->precond_ready = true;
+        c->prec_dt = dt;
+        return MPET_OK;
+    }
     // downloads (and the P1-in-P2 embedding), then the host set-ups of all
     // hierarchies concurrently (threads sharing the host cores), then uploads
     HostCsr hu, P0;
     bool use_p0 = false;
-    const bool build_u = !elast && !reuse_u;
     if (build_u) {
         c->u_elast = false;
         fetch(c->Lu, hu);
@@ -705,6 +729,36 @@ int mpet_get_amg_info(mpet_ctx* c, int32_t block, int32_t* levels, int64_t* size
         if (sizes) sizes[k] = h.lev[k].A.n;
         if (nnz) nnz[k] = h.lev[k].A.nnz;
     }
+    API_END(c)
+}
+
+int mpet_set_amg_setup(mpet_ctx* c, int32_t where) {
+    API_BEGIN(c)
+    require(where == 0 || where == 1, MPET_ERR_INVALID, "AMG set-up: 0 (host) or 1 (device)");
+    c->amg_device = where == 1;
+    c->u_hier_valid = false;
+    c->precond_ready = false;
+    API_END(c)
+}
+
+int mpet_get_amg_matrix(mpet_ctx* c, int32_t block, int32_t level, int32_t which, int64_t* n, int64_t* m,
+                        int64_t* nnz, int64_t* rp, int32_t* ci, double* v) {
+    API_BEGIN(c)
+    require(c->precond_ready, MPET_ERR_STATE, "mpet_setup_preconditioner must come first");
+    require(block >= 0 && block <= c->J, MPET_ERR_INVALID, "bad block");
+    require(which == 0 || which == 1, MPET_ERR_INVALID, "which: 0 (operator) or 1 (prolongation)");
+    const AmgHier& h = block == 0 ? c->amg_u : c->amg_p[block - 1];
+    require(level >= 0 && level < (int32_t)h.lev.size(), MPET_ERR_INVALID, "bad level");
+    require(!(which == 1 && level + 1 == (int32_t)h.lev.size()), MPET_ERR_INVALID, "the coarsest level has no P");
+    const Csr& d = which == 0 ? h.lev[level].A : h.lev[level].P;
+    require(d.rp != nullptr && d.v64 != nullptr, MPET_ERR_STATE, "this level has no stored matrix");
+    if (n) *n = d.n;
+    if (m) *m = d.m;
+    if (nnz) *nnz = d.nnz;
+    if (rp) MPET_CUDA(cudaMemcpyAsync(rp, d.rp, sizeof(int64_t) * (d.n + 1), cudaMemcpyDeviceToHost, c->stream));
+    if (ci && d.nnz) MPET_CUDA(cudaMemcpyAsync(ci, d.ci, sizeof(int32_t) * d.nnz, cudaMemcpyDeviceToHost, c->stream));
+    if (v && d.nnz) MPET_CUDA(cudaMemcpyAsync(v, d.v64, sizeof(double) * d.nnz, cudaMemcpyDeviceToHost, c->stream));
+    MPET_CUDA(cudaStreamSynchronize(c->stream));
     API_END(c)
 }
 

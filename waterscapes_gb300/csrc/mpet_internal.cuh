@@ -361,6 +361,7 @@ struct mpet_ctx {
     int gm_m = 0;                 // restart length the buffers hold
     bool elem_tried = false;
     int elem_kernel = 1;          // element blocks of tetrahedra: 1 tensor cores, 0 FP64 CUDA cores
+    bool amg_device = true;       // Laplacian-form hierarchies built on the GPU (false: host set-up)
     // error-indicator scratch: per-facet terms, per-cell R4p density, its sum, bad-index flag
     double* est_fval = nullptr;
     int64_t est_fval_cap = 0;
@@ -538,6 +539,20 @@ void spmv(mpet_ctx* c, const Csr& A, int nvec, const T* x, T* y);
 void upload_amg(mpet_ctx* c, AmgHier& h, const HostAmg& ha, int nvec, bool fp32);
 // frees the device arrays of a hierarchy (before it is rebuilt)
 void release_hier(mpet_ctx* c, AmgHier& h);
+// Smoothed-aggregation hierarchy built on the GPU from a device block (FP64
+// CSR) with the same recipe as amg_setup_host; with_p0: the first
+// prolongator is the P1-in-P2 embedding of the free vertices (the block is
+// the P2 displacement Laplacian).  ms[0] = hierarchy, ms[1] = layouts and
+// autotuning (amg_device.cu).
+void amg_setup_device(mpet_ctx* c, AmgHier& h, const Csr& A0, bool with_p0, double theta, int coarse_size,
+                      int max_levels, int nvec, bool fp32, double ms[2]);
+// FP32 copies, SpMV layouts, work buffers and autotuning of a hierarchy whose
+// FP64 levels (A, P, R, dinv64, rho) and coarsest inverse are on the device
+void finish_device_hier(mpet_ctx* c, AmgHier& h, int nvec, bool fp32);
+double device_rho(mpet_ctx* c, const Csr& A, const double* dinv);
+// greedy aggregation and dense SPD inverse of the host set-up (amg_setup.cpp)
+int64_t aggregate(const HostCsr& S, std::vector<int64_t>& agg);
+bool cholesky_inverse(std::vector<double>& a, int64_t n, std::vector<double>& inv);
 // homogeneous: the Dirichlet entries of x are zero (adjoint solves) instead
 // of the values set by mpet_set_bc_values
 int solve_system(mpet_ctx* c, const double* b, double* x, mpet_stats* st, bool homogeneous = false);

@@ -3359,6 +3359,60 @@ void upload_amg(mpet_ctx* c, AmgHier& h, const HostAmg& ha, int nvec, bool fp32)
     MPET_CUDA(cudaStreamSynchronize(c->stream));
 }
 
+// Levels built on the GPU (amg_device.cu) come with FP64 matrices, dinv64, rho
+// and the coarsest inverse; this adds what upload_amg adds to uploaded ones.
+static void finish_device_csr(mpet_ctx* c, Csr& d, bool fp32) {
+    if (fp32) {
+        d.v32 = c->pool.alloc<float>(d.nnz);
+        if (d.nnz) k_f64_to_f32<<<grid_for(d.nnz, 256), 256, 0, c->stream>>>(d.nnz, d.v64, d.v32);
+        MPET_CHECK_LAUNCH();
+    }
+    d.lpr = choose_lpr(d.n, d.nnz);
+    std::vector<int64_t> rp(d.n + 1);
+    MPET_CUDA(cudaMemcpyAsync(rp.data(), d.rp, sizeof(int64_t) * (d.n + 1), cudaMemcpyDeviceToHost, c->stream));
+    MPET_CUDA(cudaStreamSynchronize(c->stream));
+    build_tiles(c, d, rp.data());
+    build_sell(c, d, fp32, false);
+}
+
+void finish_device_hier(mpet_ctx* c, AmgHier& h, int nvec, bool fp32) {
+    h.nvec = nvec;
+    h.cheb_degree = c->prm.amg_cheb_degree > 0 ? c->prm.amg_cheb_degree : 4;
+    h.cheb_degree0 = c->prm.amg_cheb_degree_fine > 0 ? c->prm.amg_cheb_degree_fine : h.cheb_degree;
+    for (size_t k = 0; k < h.lev.size(); ++k) {
+        AmgLevel& L = h.lev[k];
+        finish_device_csr(c, L.A, fp32);
+        const int64_t n = L.A.n;
+        if (fp32) {
+            L.dinv32 = c->pool.alloc<float>(n);
+            k_f64_to_f32<<<grid_for(n, 256), 256, 0, c->stream>>>(n, L.dinv64, L.dinv32);
+            MPET_CHECK_LAUNCH();
+        }
+        if (k + 1 < h.lev.size()) {
+            finish_device_csr(c, L.P, fp32);
+            finish_device_csr(c, L.R, fp32);
+        }
+        const int64_t nn = n * nvec;
+        L.x = c->pool.alloc<double>(nn);
+        L.b = c->pool.alloc<double>(nn);
+        L.r = c->pool.alloc<double>(nn);
+        L.d = c->pool.alloc<double>(nn);
+        L.t0 = c->pool.alloc<double>(nn);
+        L.t1 = c->pool.alloc<double>(nn);
+    }
+    if (nvec == 4) {
+        h.pack_in = c->pool.alloc<double>(h.lev[0].A.n * 4);
+        h.pack_out = c->pool.alloc<double>(h.lev[0].A.n * 4);
+        if (fp32) autotune_hier<float, 4>(c, h); else autotune_hier<double, 4>(c, h);
+        if (fp32) choose_mf<float>(c, h); else choose_mf<double>(c, h);
+    } else {
+        if (fp32) autotune_hier<float, 1>(c, h); else autotune_hier<double, 1>(c, h);
+    }
+    MPET_CUDA(cudaStreamSynchronize(c->stream));
+}
+
+double device_rho(mpet_ctx* c, const Csr& A, const double* dinv) { return csr_rho(c, A, dinv); }
+
 // ---- displacement block as elasticity AMG ------------------------------------------------
 //
 // Level 0 is the displacement block of the system itself (its node-block copy,

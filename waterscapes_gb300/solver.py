@@ -106,6 +106,8 @@ class MPETSolver:
                        bf.shape[0], _lib._ptr(bf), _lib._ptr(markers), self.J)
         self._prm = self._make_params()
         self._ctx.call("mpet_setup", ctypes.byref(self._prm))
+        # smoothed-aggregation set-up on the GPU ("device") or on host threads ("host")
+        self._ctx.call("mpet_set_amg_setup", {"host": 0, "device": 1}[self.params.get("amg_setup", "device")])
         # per-cell permeability fields (K_a given as an array with one value per cell)
         Ks = [np.asarray(k, dtype=np.float64) for k in pp["K"]]
         self._K_cells = None
@@ -159,7 +161,7 @@ class MPETSolver:
                 "max_outer": 40, "amg_theta": 0.1, "amg_cheb_degree": 4, "amg_coarse_size": 500,
                 "amg_p2_to_p1": True, "prec_u_weight": "mu+lmbda", "prec_network_modes": True,
                 "prec_u_form": "laplacian", "krylov": "auto", "gmres_restart": 30,
-                "amg_cheb_degree_fine": 0, "inner_loop": "device",
+                "amg_cheb_degree_fine": 0, "inner_loop": "device", "amg_setup": "device",
                 "check_every": 4, "device": 0}
 
     def _make_params(self):
