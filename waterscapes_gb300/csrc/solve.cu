@@ -1678,13 +1678,6 @@ static void minres_three(mpet_ctx* c) {
     T* d = (T*)c->kd;
     int ir1 = 0, ir2 = 1, iy = 2;
     int iw = 0, iw1 = 1, iw2 = 2;
-    // the products (system SpMV and preconditioner) skip the slices of
-    // instances that have converged
-    struct SkipScope {
-        mpet_ctx* c;
-        ~SkipScope() { c->skip_done = nullptr; }
-    } scope{c};
-    c->skip_done = (c->batch_skip && c->skip_maps) ? c->bdone : nullptr;
     for (int q = 0; q < 3; ++q) {
         T* r1 = (T*)c->kr[ir1];
         T* r2 = (T*)c->kr[ir2];
@@ -2391,6 +2384,13 @@ static void bminres_three(mpet_ctx* c) {
     T* d = (T*)c->kd;
     int ir1 = 0, ir2 = 1, iy = 2;
     int iw = 0, iw1 = 1, iw2 = 2;
+    // the products (system SpMV and preconditioner) skip the slices of
+    // instances that have converged
+    struct SkipScope {
+        mpet_ctx* c;
+        ~SkipScope() { c->skip_done = nullptr; }
+    } scope{c};
+    c->skip_done = (c->batch_skip && c->skip_maps) ? c->bdone : nullptr;
     for (int q = 0; q < 3; ++q) {
         T* r1 = (T*)c->kr[ir1];
         T* r2 = (T*)c->kr[ir2];
