@@ -55,7 +55,8 @@ def _square(n):
 
 def _hierarchies(problem, dt, precision, where):
     from waterscapes_gb300 import MPETSolver
-    s = MPETSolver(problem, dict(dt=dt, T=dt, precision=precision, rtol=1e-11))
+    # a small coarsest size, so that these small meshes get several aggregation levels
+    s = MPETSolver(problem, dict(dt=dt, T=dt, precision=precision, rtol=1e-11, amg_coarse_size=40))
     s.ctx.call("mpet_set_amg_setup", where)
     s.ctx.call("mpet_assemble", dt, 1)
     s.ctx.call("mpet_setup_preconditioner", dt)
@@ -96,7 +97,7 @@ def test_device_setup_rebuilds_after_permeability_change():
     and still matches the host set-up of the new blocks."""
     from waterscapes_gb300 import MPETSolver
     problem, dt = make_problem(5, 2)
-    s = MPETSolver(problem, dict(dt=dt, T=dt, precision="fp64", rtol=1e-11))
+    s = MPETSolver(problem, dict(dt=dt, T=dt, precision="fp64", rtol=1e-11, amg_coarse_size=40))
     s.ctx.call("mpet_assemble", dt, 1)
     s.ctx.call("mpet_setup_preconditioner", dt)
     free0 = torch.cuda.mem_get_info()[0]
