@@ -137,7 +137,9 @@ struct Csr {
     int max_row = 0;  // longest row (entries)
     // SpMV variant: bit 0 = 8 entries per lane per batch (else 4, only with
     // 32 lanes per row, or with the SELL copy), bit 1 = shared-memory staged
-    // (needs tiles), bit 2 = SELL-32 copy (needs s_off); 8 = node-block copy
+    // (needs tiles; with bit 2: the SELL kernel with its epilogue loads after
+    // the accumulation, 6 and 7), bit 2 = SELL-32 copy (needs s_off);
+    // 8 = node-block copy
     int variant = 0;
     // mixed precision: variant and lanes per row of the FP64 products when they
     // were tuned apart from the FP32 copy's (-1: none, use variant / lpr)

@@ -302,12 +302,16 @@ __global__ void __launch_bounds__(256) k_spmv(int64_t n, const int64_t* __restri
 // line and a warp keeps 32 rows (U gathers each) in flight with no
 // cross-lane reduction.  Padding entries carry value 0 and a valid column
 // of the row.  The loop bound is the slice width, the same for every lane.
-template <typename T, int NV, int U, class Epi>
-__global__ void __launch_bounds__(256) k_spmv_sell(int64_t n, int64_t nslices, const int64_t* __restrict__ soff,
+// LATE: the epilogue's own loads come after the accumulation loop, which
+// frees their registers during it (more resident warps: the gathers are
+// latency-bound; k_spmv_sell_late); otherwise they are issued first and
+// overlap the loop (k_spmv_sell).
+template <typename T, int NV, int U, class Epi, bool LATE>
+__device__ __forceinline__ void spmv_sell_body(int64_t n, int64_t nslices, const int64_t* __restrict__ soff,
                                                    const int32_t* __restrict__ sci, const T* __restrict__ sva,
                                                    const T* __restrict__ x, Epi epi, double* partials,
-                                                   const int32_t* __restrict__ skl = nullptr,
-                                                   const double* __restrict__ skip = nullptr) {
+                                                   const int32_t* __restrict__ skl,
+                                                   const double* __restrict__ skip) {
     const int lane = threadIdx.x & 31;
     const int64_t warp = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) >> 5;
     const int64_t nwarps = ((int64_t)gridDim.x * blockDim.x) >> 5;
@@ -317,7 +321,7 @@ __global__ void __launch_bounds__(256) k_spmv_sell(int64_t n, int64_t nslices, c
         const int64_t row = sl * 32 + lane;
         const int64_t o1 = soff[sl + 1];
         typename Epi::Pre pre{};
-        if (row < n) pre = epi.pre(row);
+        if (!LATE && row < n) pre = epi.pre(row);
         T acc[NV];
 #pragma unroll
         for (int k = 0; k < NV; ++k) acc[k] = T(0);
@@ -343,6 +347,7 @@ __global__ void __launch_bounds__(256) k_spmv_sell(int64_t n, int64_t nslices, c
                 }
             }
         }
+        if (LATE && row < n) pre = epi.pre(row);
         if (row < n) epi.apply(row, acc, pre, r0, r1);
     }
     if constexpr (Epi::kRed > 0) {
@@ -354,6 +359,27 @@ __global__ void __launch_bounds__(256) k_spmv_sell(int64_t n, int64_t nslices, c
             if (threadIdx.x == 0) partials[NB_RED + blockIdx.x] = t1;
         }
     }
+}
+
+
+template <typename T, int NV, int U, class Epi>
+__global__ void __launch_bounds__(256) k_spmv_sell(int64_t n, int64_t nslices, const int64_t* __restrict__ soff,
+                                                   const int32_t* __restrict__ sci, const T* __restrict__ sva,
+                                                   const T* __restrict__ x, Epi epi, double* partials,
+                                                   const int32_t* __restrict__ skl = nullptr,
+                                                   const double* __restrict__ skip = nullptr) {
+    spmv_sell_body<T, NV, U, Epi, false>(n, nslices, soff, sci, sva, x, epi, partials, skl, skip);
+}
+
+template <typename T, int NV, int U, class Epi>
+__global__ void __launch_bounds__(256, 8) k_spmv_sell_late(int64_t n, int64_t nslices,
+                                                          const int64_t* __restrict__ soff,
+                                                          const int32_t* __restrict__ sci,
+                                                          const T* __restrict__ sva, const T* __restrict__ x,
+                                                          Epi epi, double* partials,
+                                                          const int32_t* __restrict__ skl = nullptr,
+                                                          const double* __restrict__ skip = nullptr) {
+    spmv_sell_body<T, NV, U, Epi, true>(n, nslices, soff, sci, sva, x, epi, partials, skl, skip);
 }
 
 __global__ void k_sell_width(int64_t n, int64_t nslices, const int64_t* __restrict__ rp, int64_t* w32) {
@@ -1001,14 +1027,25 @@ static void launch_spmv(mpet_ctx* c, const Csr& A, const T* va, const T* x, cons
     if ((variant & 4) && sell_vals<T>(A) && va == vals<T>(A)) {
         int blocks = Epi::kRed > 0 ? NB_RED : grid_for(A.nslices * 32, 256);
         if (Epi::kRed == 0 && blocks > 152 * 16) blocks = 152 * 16;
-        if (variant & 1)
-            k_spmv_sell<T, NV, 8, Epi><<<blocks, 256, 0, c->stream>>>(A.n, A.nslices, A.s_off, A.s_ci,
-                                                                      sell_vals<T>(A), x, epi, c->partials, skl,
-                                                                      skip);
-        else
-            k_spmv_sell<T, NV, 4, Epi><<<blocks, 256, 0, c->stream>>>(A.n, A.nslices, A.s_off, A.s_ci,
-                                                                      sell_vals<T>(A), x, epi, c->partials, skl,
-                                                                      skip);
+        const T* sv = sell_vals<T>(A);
+        switch (variant & 3) {
+            case 0:
+                k_spmv_sell<T, NV, 4, Epi><<<blocks, 256, 0, c->stream>>>(A.n, A.nslices, A.s_off, A.s_ci, sv, x, epi,
+                                                                          c->partials, skl, skip);
+                break;
+            case 1:
+                k_spmv_sell<T, NV, 8, Epi><<<blocks, 256, 0, c->stream>>>(A.n, A.nslices, A.s_off, A.s_ci, sv, x, epi,
+                                                                          c->partials, skl, skip);
+                break;
+            case 2:
+                k_spmv_sell_late<T, NV, 4, Epi><<<blocks, 256, 0, c->stream>>>(A.n, A.nslices, A.s_off, A.s_ci, sv,
+                                                                               x, epi, c->partials, skl, skip);
+                break;
+            default:
+                k_spmv_sell_late<T, NV, 8, Epi><<<blocks, 256, 0, c->stream>>>(A.n, A.nslices, A.s_off, A.s_ci, sv,
+                                                                               x, epi, c->partials, skl, skip);
+                break;
+        }
         MPET_CHECK_LAUNCH();
         c->n_launch++;
         return;
@@ -1161,7 +1198,7 @@ const float* dinv_of<float>(const AmgLevel& L) { return L.dinv32; }
 bool spmv_variant_available(const Csr& A, int v) {
     if (v == 8) return A.nb != nullptr;
     if (v < 0 || v > 5) return false;
-    if (v & 4) return A.s_off != nullptr && !(v & 2);
+    if (v & 4) return A.s_off != nullptr;  // 6, 7: SELL with late epilogue loads
     if ((v & 2) && A.ntiles == 0) return false;
     if ((v & 1) && A.lpr != 32) return false;
     return true;
@@ -1186,7 +1223,7 @@ static void autotune_matrix(mpet_ctx* c, Csr& A, const T* x, const Epi& epi, dou
     for (int lpr : {lpr0, lpr0 / 2, lpr0 * 2}) {
         if ((lpr < 4 || lpr > 32) && lpr != lpr0) continue;
         A.lpr = lpr;
-        for (int v : {0, 1, 2, 3, 4, 5, 8}) {
+        for (int v : {0, 1, 2, 3, 4, 5, 6, 7, 8}) {
             if (!spmv_variant_available(A, v) || (v >= 4 && v < 8 && (!sell_vals<T>(A) || lpr != lpr0))) continue;
             if (v == 8 && (!Epi::kSystem || NV != 1 || !nb_vals<T>(*A.nb) || lpr != lpr0)) continue;
             // batches: the staged kernel has no slice skipping
@@ -1207,7 +1244,7 @@ static void autotune_matrix(mpet_ctx* c, Csr& A, const T* x, const Epi& epi, dou
             // so near-ties do not flip from one set-up to the next
             const float med = t[2];
             const float ms = med * ((v == 0 && lpr == lpr0) ? 0.97f : 1.0f);
-            if (ms_out && lpr == lpr0) ms_out[v == 8 ? 6 : v] = med;
+            if (ms_out && lpr == lpr0 && (v <= 5 || v == 8)) ms_out[v == 8 ? 6 : v] = med;
             if (ms < best) {
                 best = ms;
                 best_v = v;
