@@ -719,6 +719,8 @@ def main():
     ap.add_argument("--coarse-size", type=int, default=None, help="override amg_coarse_size")
     ap.add_argument("--cheb-degree-fine", type=int, default=None,
                     help="override amg_cheb_degree_fine (the finest level of every hierarchy)")
+    ap.add_argument("--cheb-degree-coarse", type=int, default=None,
+                    help="override amg_cheb_degree_coarse (levels 2, 3, ... of every hierarchy)")
     ap.add_argument("--amg-setup", default=None, choices=["device", "host"],
                     help="where the smoothed-aggregation hierarchies are built (default: device)")
     ap.add_argument("--inner-loop", default=None, choices=["device", "host"],
@@ -805,6 +807,8 @@ def main():
         base["amg_coarse_size"] = args.coarse_size
     if args.cheb_degree_fine is not None:
         base["amg_cheb_degree_fine"] = args.cheb_degree_fine
+    if args.cheb_degree_coarse is not None:
+        base["amg_cheb_degree_coarse"] = args.cheb_degree_coarse
     if args.inner_loop is not None:
         base["inner_loop"] = args.inner_loop
     if args.amg_setup is not None:

@@ -118,6 +118,8 @@ typedef struct mpet_params {
     int32_t inner_loop;                /* 0: each inner Krylov solve is one graph launch with a
                                           device-side loop (default); 1: three-iteration graph
                                           replays with a host check after each (test hook) */
+    int32_t amg_cheb_degree_coarse;    /* Chebyshev degree on levels 2, 3, ... of every
+                                          hierarchy (<= 0: amg_cheb_degree) */
 } mpet_params;
 
 typedef struct mpet_stats {

@@ -58,6 +58,7 @@ class MpetParams(ctypes.Structure):
         ("gmres_restart", ctypes.c_int32),
         ("amg_cheb_degree_fine", ctypes.c_int32),
         ("inner_loop", ctypes.c_int32),
+        ("amg_cheb_degree_coarse", ctypes.c_int32),
     ]
 
 
