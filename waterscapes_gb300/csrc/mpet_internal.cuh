@@ -201,6 +201,11 @@ struct MinresScalars {
     double rel;      // phibar / beta1
     double flag;     // 1 = breakdown
     double nr2, nb2; // outer residual sums
+    double nr, inv_nr, inv_nb;  // sqrt(nr2), 1/sqrt(nr2), 1/sqrt(nb2) (0 for 0)
+    // FP32 copies of the scalars the FP32 vector kernels read, written with the
+    // FP64 values: those kernels then convert nothing per element on the
+    // narrow FP64 pipe
+    float f_inv_beta, f_c_r1, f_c_r2, f_oldeps, f_delta, f_inv_gamma, f_phi, f_pad;
 };
 
 // Host-side setup of one SA hierarchy from an FP64 CSR (amg_setup.cpp).

@@ -170,6 +170,14 @@ struct EpiCheb {
     }
 };
 
+// a scalar in the working precision: the FP64 value or its FP32 copy
+template <typename T>
+__device__ __forceinline__ T msc(double d, float f);
+template <>
+__device__ __forceinline__ double msc<double>(double d, float) { return d; }
+template <>
+__device__ __forceinline__ float msc<float>(double, float f) { return f; }
+
 // MINRES Lanczos step: y = A v - (beta/oldb) r1; partial v.y
 template <typename T>
 struct EpiMinres {
@@ -184,7 +192,7 @@ struct EpiMinres {
     };
     __device__ __forceinline__ Pre pre(int64_t row) const { return Pre{r1[row], v[row]}; }
     __device__ __forceinline__ void apply(int64_t row, const T* acc, const Pre& p, double& r0, double&) const {
-        const T c = (T)sc->c_r1;
+        const T c = msc<T>(sc->c_r1, sc->f_c_r1);
         const T yy = acc[0] - c * p.r;
         y[row] = yy;
         r0 += (double)p.v * (double)yy;
@@ -1341,10 +1349,12 @@ __global__ void k_dense_coarse(int64_t n, int nvec, const double* __restrict__ c
 template <typename T>
 __global__ void k_dot(int64_t n, const T* __restrict__ a, const T* __restrict__ b, double* partials) {
     __shared__ double sh[8];
-    double s = 0.0;
+    // a thread's products are summed in the working precision (a few dozen
+    // terms), then the thread sums in FP64: no per-element FP64 work
+    T acc = T(0);
     for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
-        s += (double)a[i] * (double)b[i];
-    s = block_sum256(s, sh);
+        acc += a[i] * b[i];
+    const double s = block_sum256((double)acc, sh);
     if (threadIdx.x == 0) partials[blockIdx.x] = s;
 }
 
@@ -1361,14 +1371,14 @@ template <typename T>
 __global__ void k_mr_v(int64_t n, const T* __restrict__ y, T* v, const MinresScalars* sc) {
     int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
     if (i >= n) return;
-    v[i] = y[i] * (T)sc->inv_beta;
+    v[i] = y[i] * msc<T>(sc->inv_beta, sc->f_inv_beta);
 }
 
 template <typename T>
 __global__ void k_mr_axpy(int64_t n, T* y, const T* __restrict__ r2, const MinresScalars* sc) {
     int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
     if (i >= n) return;
-    y[i] -= (T)sc->c_r2 * r2[i];
+    y[i] -= msc<T>(sc->c_r2, sc->f_c_r2) * r2[i];
 }
 
 // w = (v - oldeps w1 - delta w2) / gamma ; d += phi w  (w1, w2 already rotated)
@@ -1377,10 +1387,22 @@ __global__ void k_mr_update(int64_t n, const T* __restrict__ v, const T* __restr
                             T* w, T* d, const MinresScalars* sc) {
     int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
     if (i >= n) return;
-    const T oe = (T)sc->oldeps, de = (T)sc->delta, ig = (T)sc->inv_gamma, ph = (T)sc->phi;
+    const T oe = msc<T>(sc->oldeps, sc->f_oldeps), de = msc<T>(sc->delta, sc->f_delta);
+    const T ig = msc<T>(sc->inv_gamma, sc->f_inv_gamma), ph = msc<T>(sc->phi, sc->f_phi);
     const T wn = (v[i] - oe * w1[i] - de * w2[i]) * ig;
     w[i] = wn;
     d[i] += ph * wn;
+}
+
+// the FP32 copies of the scalars (after every update of the FP64 ones)
+__device__ __forceinline__ void mr_mirror(MinresScalars* s) {
+    s->f_inv_beta = (float)s->inv_beta;
+    s->f_c_r1 = (float)s->c_r1;
+    s->f_c_r2 = (float)s->c_r2;
+    s->f_oldeps = (float)s->oldeps;
+    s->f_delta = (float)s->delta;
+    s->f_inv_gamma = (float)s->inv_gamma;
+    s->f_phi = (float)s->phi;
 }
 
 // One MINRES scalar step (Paige-Saunders recurrences) on the reduced sums.
@@ -1400,11 +1422,14 @@ __device__ void mr_init_one(MinresScalars* s, double t) {
     s->inv_beta = b1 > 0.0 ? 1.0 / b1 : 0.0;
     s->rel = 1.0;
     s->flag = bad ? 1.0 : 0.0;
+    s->oldeps = s->delta = s->phi = s->inv_gamma = 0.0;
+    mr_mirror(s);
 }
 
 __device__ void mr_alfa_one(MinresScalars* s, double t) {
     s->alfa = t;
     s->c_r2 = t * s->inv_beta;
+    s->f_c_r2 = (float)s->c_r2;
 }
 
 __device__ void mr_beta_one(MinresScalars* s, double t) {
@@ -1441,6 +1466,7 @@ __device__ void mr_beta_one(MinresScalars* s, double t) {
     s->c_r1 = oldb > 0.0 ? beta / oldb : 0.0;
     s->rel = s->beta1 > 0.0 ? phibar / s->beta1 : 0.0;
     if (beta == 0.0 && phibar > 0.0) s->flag = 1.0;
+    mr_mirror(s);
 }
 
 __global__ void k_mr_init(MinresScalars* s, const double* partials) {
@@ -1468,6 +1494,9 @@ __global__ void k_outer_norms(MinresScalars* s, const double* partials) {
     if (threadIdx.x == 0) {
         s->nr2 = a;
         s->nb2 = b;
+        s->nr = a > 0.0 ? sqrt(a) : 0.0;
+        s->inv_nr = s->nr > 0.0 ? 1.0 / s->nr : 0.0;
+        s->inv_nb = b > 0.0 ? 1.0 / sqrt(b) : 0.0;
     }
 }
 
@@ -1476,16 +1505,14 @@ template <typename T>
 __global__ void k_scale_to(int64_t n, const double* __restrict__ r, T* out, const MinresScalars* s) {
     int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
     if (i >= n) return;
-    const double nr = sqrt(s->nr2);
-    const double sc = nr > 0.0 ? 1.0 / nr : 0.0;
-    out[i] = (T)(r[i] * sc);
+    out[i] = (T)(r[i] * s->inv_nr);
 }
 
 template <typename T>
 __global__ void k_add_scaled(int64_t n, double* x, const T* __restrict__ d, const MinresScalars* s) {
     int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
     if (i >= n) return;
-    x[i] += sqrt(s->nr2) * (double)d[i];
+    x[i] += s->nr * (double)d[i];
 }
 
 __global__ void k_f64_to_f32(int64_t n, const double* __restrict__ a, float* b) {
@@ -1995,8 +2022,7 @@ template <typename T>
 __global__ void k_scale_b(int64_t n, const double* __restrict__ b, T* out, const MinresScalars* s) {
     const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
     if (i >= n) return;
-    const double nb = sqrt(s->nb2);
-    out[i] = (T)(nb > 0.0 ? b[i] / nb : 0.0);
+    out[i] = (T)(b[i] * s->inv_nb);
 }
 
 // Preconditioned norm (b^T M^-1 b)^1/2 of the right-hand side, in the working
@@ -2185,12 +2211,12 @@ __global__ void k_seg_dot_open(const int64_t* __restrict__ lo, const int32_t* __
         if (threadIdx.x == 0) part[ch] = 0.0;
         return;
     }
-    double s = 0.0;
+    T acc = T(0);  // a thread's 16 products in the working precision, then FP64
     for (int i = threadIdx.x; i < len[ch]; i += 256) {
         const int64_t r = lo[ch] + i;
-        s += (double)a[r] * (double)b[r];
+        acc += a[r] * b[r];
     }
-    s = block_sum256(s, sh);
+    const double s = block_sum256((double)acc, sh);
     if (threadIdx.x == 0) part[ch] = s;
 }
 
@@ -2312,7 +2338,7 @@ __global__ void k_bmr_v(const int64_t* __restrict__ lo, const int32_t* __restric
                         const MinresScalars* __restrict__ sc, const double* __restrict__ done) {
     const int64_t ch = blockIdx.x;
     if (done[inst[ch]] != 0.0) return;  // a converged instance's chunks are left as they are
-    const T ib = (T)sc[inst[ch]].inv_beta;
+    const T ib = msc<T>(sc[inst[ch]].inv_beta, sc[inst[ch]].f_inv_beta);
     for (int i = threadIdx.x; i < len[ch]; i += 256) v[lo[ch] + i] = y[lo[ch] + i] * ib;
 }
 
@@ -2328,15 +2354,15 @@ __global__ void k_bmr_axpy_dot(const int64_t* __restrict__ lo, const int32_t* __
         if (threadIdx.x == 0) part[ch] = 0.0;
         return;
     }
-    const T c1 = (T)sc[inst[ch]].c_r1;
-    double s = 0.0;
+    const T c1 = msc<T>(sc[inst[ch]].c_r1, sc[inst[ch]].f_c_r1);
+    T acc = T(0);  // a thread's 16 products in the working precision, then FP64
     for (int i = threadIdx.x; i < len[ch]; i += 256) {
         const int64_t r = lo[ch] + i;
         const T yy = y[r] - c1 * r1[r];
         y[r] = yy;
-        s += (double)v[r] * (double)yy;
+        acc += v[r] * yy;
     }
-    s = block_sum256(s, sh);
+    const double s = block_sum256((double)acc, sh);
     if (threadIdx.x == 0) part[ch] = s;
 }
 
@@ -2346,7 +2372,7 @@ __global__ void k_bmr_axpy(const int64_t* __restrict__ lo, const int32_t* __rest
                            const MinresScalars* __restrict__ sc, const double* __restrict__ done) {
     const int64_t ch = blockIdx.x;
     if (done[inst[ch]] != 0.0) return;
-    const T c2 = (T)sc[inst[ch]].c_r2;
+    const T c2 = msc<T>(sc[inst[ch]].c_r2, sc[inst[ch]].f_c_r2);
     for (int i = threadIdx.x; i < len[ch]; i += 256) y[lo[ch] + i] -= c2 * r2[lo[ch] + i];
 }
 
@@ -2358,7 +2384,8 @@ __global__ void k_bmr_update(const int64_t* __restrict__ lo, const int32_t* __re
     const int64_t ch = blockIdx.x;
     if (done[inst[ch]] == 1.0) return;  // 2: converged by this iteration's beta, its update still counts
     const MinresScalars& s = sc[inst[ch]];
-    const T oe = (T)s.oldeps, de = (T)s.delta, ig = (T)s.inv_gamma, ph = (T)s.phi;
+    const T oe = msc<T>(s.oldeps, s.f_oldeps), de = msc<T>(s.delta, s.f_delta);
+    const T ig = msc<T>(s.inv_gamma, s.f_inv_gamma), ph = msc<T>(s.phi, s.f_phi);
     for (int i = threadIdx.x; i < len[ch]; i += 256) {
         const int64_t r = lo[ch] + i;
         const T wn = (v[r] - oe * w1[r] - de * w2[r]) * ig;
@@ -2376,6 +2403,7 @@ __device__ void mr_freeze(MinresScalars* s) {
     s->oldeps = 0.0;
     s->delta = 0.0;
     s->alfa = 0.0;
+    mr_mirror(s);
 }
 
 // start: q_i = rhs_i . M^-1 rhs_i; instances with active_i == 0 start frozen
