@@ -273,8 +273,15 @@ def prec_setup_ms(solver):
     import ctypes
     ms = np.zeros(4)
     solver.ctx.call("mpet_get_setup_timing", ms.ctypes.data_as(ctypes.c_void_p))
-    return {"where": solver.params.get("amg_setup", "device"), "blocks_gpu": round(ms[0], 1),
-            "downloads": round(ms[1], 1), "hierarchies": round(ms[2], 1), "layouts_autotune": round(ms[3], 1)}
+    out = {"where": solver.params.get("amg_setup", "device"), "blocks_gpu": round(ms[0], 1),
+           "downloads": round(ms[1], 1), "hierarchies": round(ms[2], 1), "layouts_autotune": round(ms[3], 1)}
+    if out["where"] == "device":
+        ph = np.zeros(8)
+        solver.ctx.call("mpet_get_amg_setup_phases", ph.ctypes.data_as(ctypes.c_void_p))
+        names = ["copy", "diag_rho", "strength_aggregate", "prolongator", "transpose", "galerkin", "coarsest",
+                 "layouts_autotune"]
+        out["device_phases"] = {k: round(float(v), 1) for k, v in zip(names, ph)}
+    return out
 
 
 def launches(solver):

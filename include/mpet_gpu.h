@@ -293,6 +293,14 @@ int mpet_get_setup_timing(mpet_ctx* ctx, double* ms4_host);
  * mpettotalpressuresolver.py:448).  The next set-up rebuilds everything. */
 int mpet_set_amg_setup(mpet_ctx* ctx, int32_t where);
 
+/* Where the last device set-up (mpet_set_amg_setup(ctx, 1)) spent its time,
+ * summed over its hierarchies (ms): ms8[0] block copies, [1] diagonals and
+ * spectral radii, [2] strength graphs and aggregation, [3] tentative and
+ * smoothed prolongators, [4] transposes, [5] Galerkin products, [6] coarsest
+ * inverses, [7] FP32 copies, SpMV layouts and autotuning.  No reference
+ * counterpart (set-up report). */
+int mpet_get_amg_setup_phases(mpet_ctx* ctx, double* ms8);
+
 /* Copies out level `level` of hierarchy `block` (0 displacement, 1..J the
  * networks): which = 0 its operator, 1 its prolongation (FP64 CSR, int64 row
  * pointers).  Each output may be NULL; call once with rp, ci, v NULL for the

@@ -521,8 +521,9 @@ DMat embedding_p0(mpet_ctx* c) {
 
 // Smoothed-aggregation prolongator of A at threshold th (false: A is not
 // coarsened: no aggregate, or as many aggregates as rows)
+template <class Tick>
 bool sa_prolongator_device(mpet_ctx* c, const DMat& A, const double* dg, const double* dinv, double rho, double th,
-                           DMat& P) {
+                           DMat& P, Tick& tick) {
     const int64_t n = A.n;
     TmpBuf bcnt(sizeof(int64_t) * (n + 1)), brp(sizeof(int64_t) * (n + 1));
     HostCsr S;
@@ -549,6 +550,7 @@ bool sa_prolongator_device(mpet_ctx* c, const DMat& A, const double* dg, const d
         strength(0.0);
         nagg = aggregate(S, agg);
     }
+    tick(2);
     if (nagg == 0 || nagg >= n) return false;
     std::vector<int64_t> size(nagg, 0);
     for (int64_t i = 0; i < n; ++i)
@@ -601,6 +603,14 @@ void amg_setup_device(mpet_ctx* c, AmgHier& h, const Csr& A0, bool with_p0, doub
                       int max_levels, int nvec, bool fp32, double ms[2]) {
     using clk = std::chrono::steady_clock;
     const auto t0 = clk::now();
+    auto tp = t0;
+    // phase k gets the time since the previous tick (after the stream drained)
+    auto tick = [&](int k) {
+        MPET_CUDA(cudaStreamSynchronize(c->stream));
+        const auto now = clk::now();
+        c->amg_phase_ms[k] += std::chrono::duration<double, std::milli>(now - tp).count();
+        tp = now;
+    };
     if (coarse_size < 1) coarse_size = 500;
     if (max_levels < 1) max_levels = 12;
     release_hier(c, h);
@@ -622,6 +632,7 @@ void amg_setup_device(mpet_ctx* c, AmgHier& h, const Csr& A0, bool with_p0, doub
         MPET_CUDA(cudaMemcpyAsync(A.ci, A0.ci, sizeof(int32_t) * A.nnz, cudaMemcpyDeviceToDevice, c->stream));
         MPET_CUDA(cudaMemcpyAsync(A.v, A0.v64, sizeof(double) * A.nnz, cudaMemcpyDeviceToDevice, c->stream));
     }
+    tick(0);
     while (true) {
         AmgLevel L;
         const int64_t n = A.n;
@@ -631,6 +642,7 @@ void amg_setup_device(mpet_ctx* c, AmgHier& h, const Csr& A0, bool with_p0, doub
         k_diag<<<grid_for(n, 256), 256, 0, c->stream>>>(n, A.rp, A.ci, A.v, bdg.as<double>(), L.dinv64);
         MPET_CHECK_LAUNCH();
         L.rho = device_rho(c, L.A, L.dinv64);
+        tick(1);
         const bool given = with_p0 && h.lev.empty();
         h.lev.push_back(L);
         if (!given && (n <= coarse_size || (int)h.lev.size() >= max_levels)) break;
@@ -641,13 +653,15 @@ void amg_setup_device(mpet_ctx* c, AmgHier& h, const Csr& A0, bool with_p0, doub
         } else {
             const int sa_level = (int)h.lev.size() - 1 - (with_p0 ? 1 : 0);
             const double th = theta * pow(0.5, (double)sa_level);
-            if (!sa_prolongator_device(c, A, bdg.as<double>(), L.dinv64, L.rho, th, P)) break;
+            if (!sa_prolongator_device(c, A, bdg.as<double>(), L.dinv64, L.rho, th, P, tick)) break;
         }
+        tick(3);
         DMat R = transpose(c, P);
+        tick(4);
         DMat AP = spgemm(c, A, P);
         DMat Ac = spgemm(c, R, AP);
-        MPET_CUDA(cudaStreamSynchronize(c->stream));
         dm_release(c, AP);
+        tick(5);
         AmgLevel& cur = h.lev.back();
         cur.P = as_csr(P);
         cur.R = as_csr(R);
@@ -672,9 +686,10 @@ void amg_setup_device(mpet_ctx* c, AmgHier& h, const Csr& A0, bool with_p0, doub
     h.ncoarse = nc;
     h.cinv = c->pool.alloc<double>(nc * nc);
     MPET_CUDA(cudaMemcpyAsync(h.cinv, inv.data(), sizeof(double) * nc * nc, cudaMemcpyHostToDevice, c->stream));
-    MPET_CUDA(cudaStreamSynchronize(c->stream));
+    tick(6);
     const auto t1 = clk::now();
     finish_device_hier(c, h, nvec, fp32);
+    tick(7);
     ms[0] = std::chrono::duration<double, std::milli>(t1 - t0).count();
     ms[1] = std::chrono::duration<double, std::milli>(clk::now() - t1).count();
 }

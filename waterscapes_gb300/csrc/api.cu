@@ -586,6 +586,7 @@ int mpet_setup_preconditioner(mpet_ctx* c, double dt) {
         // every hierarchy built where its block lies (amg_device.cu)
         double ms[2], build = 0.0, finish = 0.0;
         const double theta = c->prm.amg_theta;
+        for (double& x : c->amg_phase_ms) x = 0.0;
         if (build_u) {
             c->u_elast = false;
             amg_setup_device(c, c->amg_u, c->Lu, c->prm.amg_p2_to_p1 != 0, theta, cs, 12, 4, fp32, ms);
@@ -739,6 +740,13 @@ int mpet_set_amg_setup(mpet_ctx* c, int32_t where) {
     c->amg_device = where == 1;
     c->u_hier_valid = false;
     c->precond_ready = false;
+    API_END(c)
+}
+
+int mpet_get_amg_setup_phases(mpet_ctx* c, double* ms8) {
+    API_BEGIN(c)
+    require(ms8, MPET_ERR_INVALID, "NULL argument");
+    for (int k = 0; k < 8; ++k) ms8[k] = c->amg_phase_ms[k];
     API_END(c)
 }
 

@@ -370,6 +370,10 @@ struct mpet_ctx {
     bool elem_tried = false;
     int elem_kernel = 1;          // element blocks of tetrahedra: 1 tensor cores, 0 FP64 CUDA cores
     bool amg_device = true;       // Laplacian-form hierarchies built on the GPU (false: host set-up)
+    // last device set-up, summed over its hierarchies (ms): block copy, diagonal +
+    // spectral radius, strength + aggregation, tentative + smoothed prolongator,
+    // transposes, Galerkin products, coarsest inverse, layouts + autotuning
+    double amg_phase_ms[8] = {0, 0, 0, 0, 0, 0, 0, 0};
     // error-indicator scratch: per-facet terms, per-cell R4p density, its sum, bad-index flag
     double* est_fval = nullptr;
     int64_t est_fval_cap = 0;
