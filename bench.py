@@ -664,15 +664,17 @@ def vcycle_profile(args):
     import torch
     from waterscapes_gb300 import MPETSolver, _lib
     problem, dt = workload(args.n, args.networks, args.workload)
-    base = dict(dt=dt, T=1e9, theta=1.0, rtol=1e-10, precision="mixed")
+    base = dict(dt=dt, T=1e9, theta=1.0, rtol=1e-10, precision="mixed", amg_setup=args.amg_setup or "device")
     if args.cheb_degree is not None:
         base["amg_cheb_degree"] = args.cheb_degree
+    if args.cheb_degree_coarse is not None:
+        base["amg_cheb_degree_coarse"] = args.cheb_degree_coarse
     sol = MPETSolver(problem, base)
     sol._assemble(dt)
     torch.cuda.synchronize()
     hbm, kind = peaks()
     out = {"vcycle_profile": "Kuhn cube %d^3, A=%d" % (args.n, args.networks), "peak_gbs": hbm, "peak_kind": kind,
-           "blocks": []}
+           "setup_ms": prec_setup_ms(sol), "blocks": []}
     for blk in range(args.networks + 1):
         sizes, nnz = sol.amg_info(blk)
         nl = ctypes.c_int32()
