@@ -677,6 +677,8 @@ def vcycle_profile(args):
            "setup_ms": prec_setup_ms(sol), "blocks": []}
     for blk in range(args.networks + 1):
         sizes, nnz = sol.amg_info(blk)
+        va, vp, vr = (np.zeros(16, np.int32) for _ in range(3))
+        sol.ctx.call("mpet_get_amg_variants", blk, _lib._ptr(va), _lib._ptr(vp), _lib._ptr(vr))
         nl = ctypes.c_int32()
         ms = np.zeros(16)
         by = np.zeros(16)
@@ -685,7 +687,8 @@ def vcycle_profile(args):
         levels = []
         for k in range(L):
             own = ms[k] - (ms[k + 1] if k + 1 < L else 0.0)
-            levels.append({"rows": sizes[k], "nnz": nnz[k], "own_ms": round(own, 5), "vcycle_from_here_ms":
+            levels.append({"rows": sizes[k], "nnz": nnz[k], "variants_a_p_r": [int(va[k]), int(vp[k]), int(vr[k])],
+                           "own_ms": round(own, 5), "vcycle_from_here_ms":
                            round(ms[k], 5), "alg_bytes": int(by[k]),
                            "gbs": round(by[k] / own / 1e6, 1) if own > 0 else None,
                            "frac": round(by[k] / own / 1e6 / hbm, 3) if own > 0 else None})

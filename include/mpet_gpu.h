@@ -293,6 +293,13 @@ int mpet_get_setup_timing(mpet_ctx* ctx, double* ms4_host);
  * mpettotalpressuresolver.py:448).  The next set-up rebuilds everything. */
 int mpet_set_amg_setup(mpet_ctx* ctx, int32_t where);
 
+/* The SpMV variant the set-up autotuner chose for each level of hierarchy
+ * `block` (bits as for the system matrix; 8: the system's displacement block,
+ * 16: matrix-free first level): its operator, prolongation and restriction
+ * (-1 on the coarsest level).  Arrays of mpet_get_amg_info's level count; any
+ * may be NULL.  No reference counterpart (tuning report). */
+int mpet_get_amg_variants(mpet_ctx* ctx, int32_t block, int32_t* a_variant, int32_t* p_variant, int32_t* r_variant);
+
 /* Where the last device set-up (mpet_set_amg_setup(ctx, 1)) spent its time,
  * summed over its hierarchies (ms): ms8[0] block copies, [1] diagonals and
  * spectral radii, [2] strength graphs and aggregation, [3] tentative and

@@ -139,6 +139,7 @@ SIGNATURES = {
     "mpet_set_batch_skip": [_P, _I32],
     "mpet_set_amg_setup": [_P, _I32],
     "mpet_get_amg_setup_phases": [_P, _P],
+    "mpet_get_amg_variants": [_P, _I32, _P, _P, _P],
     "mpet_get_amg_matrix": [_P, _I32, _I32, _I32, _P, _P, _P, _P, _P, _P],
     "mpet_set_element_kernel": [_P, _I32],
     "mpet_set_prec_matrix_free": [_P, _I32],

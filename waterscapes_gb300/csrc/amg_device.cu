@@ -368,22 +368,67 @@ __global__ void k_tr_fill(int64_t n, const int64_t* __restrict__ rp, const int32
     }
 }
 
-// rows sorted by column (insertion sort; the scatter above left them in any order)
-__global__ void k_row_sort(int64_t n, const int64_t* __restrict__ rp, int32_t* ci, double* v) {
-    const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
-    if (i >= n) return;
-    const int64_t b = rp[i], e = rp[i + 1];
-    for (int64_t p = b + 1; p < e; ++p) {
-        const int32_t k = ci[p];
-        const double x = v[p];
-        int64_t q = p - 1;
-        while (q >= b && ci[q] > k) {
-            ci[q + 1] = ci[q];
-            v[q + 1] = v[q];
-            --q;
+// Rows put in column order (the scatter above left them in any order): a warp
+// per row marks the row's columns (distinct) in a shared-memory bitmap over
+// their window, in chunks of 16,384 columns, and each entry goes to the rank
+// of its column, found from the words' prefix counts.  Linear in the row
+// length plus the window, however long the row (the coarse levels' rows hold
+// thousands of entries).
+__global__ void __launch_bounds__(256) k_row_rank(int64_t n, const int64_t* __restrict__ rp,
+                                                  const int32_t* __restrict__ ci_in, const double* __restrict__ v_in,
+                                                  int32_t* ci, double* v) {
+    __shared__ uint32_t bm[SPG_WARPS][SPG_WORDS];
+    __shared__ int32_t pre[SPG_WARPS][SPG_WORDS];
+    const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const int64_t row = blockIdx.x * (int64_t)SPG_WARPS + w;
+    if (row >= n) return;  // whole warps; the kernel synchronises warps only
+    uint32_t* B = bm[w];
+    int32_t* X = pre[w];
+    const int64_t e0 = rp[row], e1 = rp[row + 1];
+    int l = INT_MAX, h = -1;
+    for (int64_t e = e0 + lane; e < e1; e += 32) {
+        l = min(l, ci_in[e]);
+        h = max(h, ci_in[e]);
+    }
+    l = warp_min(l);
+    h = warp_max(h);
+    constexpr int64_t CAP = (int64_t)SPG_WORDS * 32;
+    int64_t done = 0;  // entries of earlier chunks
+    for (int64_t base = l; base <= h; base += CAP) {
+        const int span = (int)min((int64_t)h - base + 1, CAP);
+        const int nw = (span + 31) >> 5;
+        for (int q = lane; q < nw; q += 32) B[q] = 0u;
+        __syncwarp();
+        for (int64_t e = e0 + lane; e < e1; e += 32) {
+            const int64_t col = (int64_t)ci_in[e] - base;
+            if (col >= 0 && col < span) atomicOr(&B[col >> 5], 1u << (col & 31));
         }
-        ci[q + 1] = k;
-        v[q + 1] = x;
+        __syncwarp();
+        int carry = 0;
+        for (int q0 = 0; q0 < nw; q0 += 32) {
+            const int q = q0 + lane;
+            const int pc = q < nw ? __popc(B[q]) : 0;
+            int incl = pc;
+#pragma unroll
+            for (int o = 1; o < 32; o <<= 1) {
+                const int t = __shfl_up_sync(0xffffffffu, incl, o);
+                if (lane >= o) incl += t;
+            }
+            if (q < nw) X[q] = carry + incl - pc;
+            carry += __shfl_sync(0xffffffffu, incl, 31);
+        }
+        __syncwarp();
+        for (int64_t e = e0 + lane; e < e1; e += 32) {
+            const int64_t col = (int64_t)ci_in[e] - base;
+            if (col >= 0 && col < span) {
+                const int wq = (int)(col >> 5), bit = (int)(col & 31);
+                const int64_t pos = e0 + done + X[wq] + __popc(B[wq] & ((1u << bit) - 1u));
+                ci[pos] = ci_in[e];
+                v[pos] = v_in[e];
+            }
+        }
+        done += carry;
+        __syncwarp();
     }
 }
 
@@ -402,11 +447,16 @@ DMat transpose(mpet_ctx* c, const DMat& P) {
     MPET_CHECK_LAUNCH();
     scan_counts(c, bc.as<int64_t>(), R.n, R.rp);
     MPET_CUDA(cudaMemsetAsync(bc.p, 0, sizeof(int64_t) * (R.n + 1), c->stream));
+    TmpBuf tci(sizeof(int32_t) * (R.nnz + 1)), tv(sizeof(double) * (R.nnz + 1));
     if (P.n > 0)
         k_tr_fill<<<grid_for(P.n, 256), 256, 0, c->stream>>>(P.n, P.rp, P.ci, P.v, R.rp,
-                                                             bc.as<unsigned long long>(), R.ci, R.v);
-    if (R.n > 0) k_row_sort<<<grid_for(R.n, 128), 128, 0, c->stream>>>(R.n, R.rp, R.ci, R.v);
+                                                             bc.as<unsigned long long>(), tci.as<int32_t>(),
+                                                             tv.as<double>());
+    if (R.n > 0)
+        k_row_rank<<<(unsigned)((R.n + SPG_WARPS - 1) / SPG_WARPS), 256, 0, c->stream>>>(
+            R.n, R.rp, tci.as<int32_t>(), tv.as<double>(), R.ci, R.v);
     MPET_CHECK_LAUNCH();
+    MPET_CUDA(cudaStreamSynchronize(c->stream));  // before the scratch goes
     return R;
 }
 

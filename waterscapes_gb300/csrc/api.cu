@@ -743,6 +743,20 @@ int mpet_set_amg_setup(mpet_ctx* c, int32_t where) {
     API_END(c)
 }
 
+int mpet_get_amg_variants(mpet_ctx* c, int32_t block, int32_t* a_variant, int32_t* p_variant, int32_t* r_variant) {
+    API_BEGIN(c)
+    require(c->precond_ready, MPET_ERR_STATE, "mpet_setup_preconditioner must come first");
+    require(block >= 0 && block <= c->J, MPET_ERR_INVALID, "bad block");
+    const AmgHier& h = block == 0 ? c->amg_u : c->amg_p[block - 1];
+    for (size_t k = 0; k < h.lev.size(); ++k) {
+        const AmgLevel& L = h.lev[k];
+        if (a_variant) a_variant[k] = L.mf ? 16 : (L.nb_uu ? 8 : L.A.variant);
+        if (p_variant) p_variant[k] = k + 1 < h.lev.size() ? L.P.variant : -1;
+        if (r_variant) r_variant[k] = k + 1 < h.lev.size() ? L.R.variant : -1;
+    }
+    API_END(c)
+}
+
 int mpet_get_amg_setup_phases(mpet_ctx* c, double* ms8) {
     API_BEGIN(c)
     require(ms8, MPET_ERR_INVALID, "NULL argument");
