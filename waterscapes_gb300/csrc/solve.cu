@@ -1214,9 +1214,12 @@ bool spmv_variant_available(const Csr& A, int v) {
 
 // Set-up autotuning: time every applicable SpMV variant on this matrix (CSR
 // with its lanes per row, half and double that; SELL-32; node blocks) with
-// the epilogue it runs in the solver (1 warm-up + median of 5 launches from a
-// flushed L2) and keep the fastest, the default CSR kernel winning ties
-// within 3%.  Times (ms per launch) go to ms_out if given.
+// the epilogue it runs in the solver (1 warm-up + median of 7 launches) and
+// keep the fastest, the default CSR kernel winning ties within 3%.  Times (ms
+// per launch) go to ms_out if given.  A matrix larger than a quarter of L2 is
+// timed from a flushed L2 (in the solver it streams from HBM every time); a
+// smaller one, a coarse AMG level read by several Chebyshev products in a
+// row, is timed warm, as it runs after its first product.
 template <typename T, int NV, class Epi>
 static void autotune_matrix(mpet_ctx* c, Csr& A, const T* x, const Epi& epi, double* ms_out = nullptr) {
     if (vals<T>(A) == nullptr || A.nnz == 0) return;
@@ -1224,8 +1227,8 @@ static void autotune_matrix(mpet_ctx* c, Csr& A, const T* x, const Epi& epi, dou
     float best = 1e30f;
     int best_v = 0, best_lpr = A.lpr;
     const int lpr0 = A.lpr;
-    // In the solver every matrix is read after the system SpMV has streamed
-    // gigabytes through L2, so each timed launch starts from a flushed L2.
+    const double mbytes = (double)A.nnz * (sizeof(T) + 4) + (double)(A.n + 1) * 8;
+    const bool flush = mbytes > 32.0 * 1024 * 1024;
     constexpr size_t kFlush = 256u << 20;
     if (!c->l2_flush) c->l2_flush = c->pool.alloc<unsigned char>(kFlush);
     for (int lpr : {lpr0, lpr0 / 2, lpr0 * 2}) {
@@ -1238,19 +1241,19 @@ static void autotune_matrix(mpet_ctx* c, Csr& A, const T* x, const Epi& epi, dou
             if (c->ninst > 0 && c->batch_skip && v < 4 && (v & 2)) continue;
             A.variant = v;
             launch_spmv<T, NV>(c, A, vals<T>(A), x, epi);
-            float t[5];
-            for (int q = 0; q < 5; ++q) {
-                MPET_CUDA(cudaMemsetAsync(c->l2_flush, q, kFlush, c->stream));
+            float t[7];
+            for (int q = 0; q < 7; ++q) {
+                if (flush) MPET_CUDA(cudaMemsetAsync(c->l2_flush, q, kFlush, c->stream));
                 MPET_CUDA(cudaEventRecord(c->ev0, c->stream));
                 launch_spmv<T, NV>(c, A, vals<T>(A), x, epi);
                 MPET_CUDA(cudaEventRecord(c->ev1, c->stream));
                 MPET_CUDA(cudaEventSynchronize(c->ev1));
                 MPET_CUDA(cudaEventElapsedTime(&t[q], c->ev0, c->ev1));
             }
-            std::sort(t, t + 5);
+            std::sort(t, t + 7);
             // median; a variant replaces the incumbent only when clearly faster,
             // so near-ties do not flip from one set-up to the next
-            const float med = t[2];
+            const float med = t[3];
             const float ms = med * ((v == 0 && lpr == lpr0) ? 0.97f : 1.0f);
             if (ms_out && lpr == lpr0 && (v <= 5 || v == 8)) ms_out[v == 8 ? 6 : v] = med;
             if (ms < best) {
