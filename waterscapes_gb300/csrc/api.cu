@@ -890,7 +890,7 @@ int mpet_get_spmv_tuning_fp64(mpet_ctx* c, double* ms7, int32_t* chosen) {
 int mpet_set_hierarchy_spmv_variant(mpet_ctx* c, int32_t variant) {
     API_BEGIN(c)
     require(c->precond_ready, MPET_ERR_STATE, "mpet_setup_preconditioner must come first");
-    require((variant >= 0 && variant <= 5) || variant == 8, MPET_ERR_INVALID, "variant out of range");
+    require((variant >= 0 && variant <= 8) || variant == 32, MPET_ERR_INVALID, "variant out of range");
     destroy_minres_graph(c);
     auto set = [&](mpet::Csr& M) { M.variant = spmv_variant_available(M, variant) ? variant : 0; };
     auto hier = [&](mpet::AmgHier& h) {

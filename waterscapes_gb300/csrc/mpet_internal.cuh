@@ -1,6 +1,7 @@
 // Internal declarations of libmpetgpu (not part of the C ABI).
 #pragma once
 
+#include <cuda_fp16.h>
 #include <cuda_runtime.h>
 #include <stdint.h>
 
@@ -139,7 +140,7 @@ struct Csr {
     // 32 lanes per row, or with the SELL copy), bit 1 = shared-memory staged
     // (needs tiles; with bit 2: the SELL kernel with its epilogue loads after
     // the accumulation, 6 and 7), bit 2 = SELL-32 copy (needs s_off);
-    // 8 = node-block copy
+    // 8 = node-block copy; 32 = SELL-32 with FP16 off-diagonals (needs s_v16)
     int variant = 0;
     // mixed precision: variant and lanes per row of the FP64 products when they
     // were tuned apart from the FP32 copy's (-1: none, use variant / lpr)
@@ -154,6 +155,14 @@ struct Csr {
     int32_t* s_ci = nullptr;
     float* s_v32 = nullptr;
     double* s_v64 = nullptr;
+    // half-precision SELL values (variant 32, FP32 products of a first AMG
+    // level): off-diagonal entries as FP16 times s_h_scale (a power of two),
+    // diagonal slots 0; the diagonal in FP32 (s_d32) is the exact row sum minus
+    // the rounded off-diagonals, so the rounded operator keeps the row sums
+    // (and the symmetry) of the original one
+    __half* s_v16 = nullptr;
+    float* s_d32 = nullptr;
+    float s_h_scale = 1.f;
     // node-block copy (system matrix only; variant 8)
     NodeBlocks* nb = nullptr;
     // batches: per 32-row slice the lowest and highest instance of its rows
@@ -581,6 +590,8 @@ void batch_relres(mpet_ctx* c, double* out);
 int choose_lpr(int64_t n, int64_t nnz);
 void build_tiles(mpet_ctx* c, Csr& A, const int64_t* rp_host);
 void build_sell(mpet_ctx* c, Csr& A, bool fp32, bool with64);
+// the FP16 SELL values of A (after build_sell; needs A.v64)
+void build_sell_half(mpet_ctx* c, Csr& A);
 void fill_sell(mpet_ctx* c, Csr& A);
 void build_node_blocks(mpet_ctx* c);
 bool device_fits(mpet_ctx* c, size_t bytes);

@@ -24,6 +24,8 @@
 #include <math.h>
 
 #include <algorithm>
+#include <cmath>
+#include <cstring>
 
 #include "mpet_internal.cuh"
 
@@ -388,6 +390,139 @@ __global__ void __launch_bounds__(256, 8) k_spmv_sell_late(int64_t n, int64_t ns
                                                           const int32_t* __restrict__ skl = nullptr,
                                                           const double* __restrict__ skip = nullptr) {
     spmv_sell_body<T, NV, U, Epi, true>(n, nslices, soff, sci, sva, x, epi, partials, skl, skip);
+}
+
+// SELL-32 with FP16 off-diagonal values (variant 32, FP32 vectors): the
+// stored values are a_ij / s (s a power of two), diagonal slots 0; the row's
+// result is s * sum + d_i x_i with the FP32 diagonal d_i that keeps the row
+// sums of the original matrix.  Six bytes per entry instead of eight.
+template <int NV, int U, class Epi>
+__global__ void __launch_bounds__(256) k_spmv_sell_h(int64_t n, int64_t nslices, const int64_t* __restrict__ soff,
+                                                     const int32_t* __restrict__ sci, const __half* __restrict__ sva,
+                                                     const float* __restrict__ dg, float hs,
+                                                     const float* __restrict__ x, Epi epi, double* partials,
+                                                     const int32_t* __restrict__ skl,
+                                                     const double* __restrict__ skip) {
+    const int lane = threadIdx.x & 31;
+    const int64_t warp = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) >> 5;
+    const int64_t nwarps = ((int64_t)gridDim.x * blockDim.x) >> 5;
+    double r0 = 0.0, r1 = 0.0;
+    for (int64_t sl = warp; sl < nslices; sl += nwarps) {
+        if (skl && slice_frozen(skl, sl, skip)) continue;
+        const int64_t row = sl * 32 + lane;
+        const int64_t o1 = soff[sl + 1];
+        typename Epi::Pre pre{};
+        if (row < n) pre = epi.pre(row);
+        float acc[NV];
+#pragma unroll
+        for (int k = 0; k < NV; ++k) acc[k] = 0.f;
+        for (int64_t e = soff[sl] + lane; e < o1; e += 32 * U) {
+            int32_t cc[U];
+            float aa[U];
+#pragma unroll
+            for (int u = 0; u < U; ++u) {
+                cc[u] = 0;
+                aa[u] = 0.f;
+                if (e + u * 32 < o1) {
+                    cc[u] = __ldcs(sci + e + u * 32);
+                    aa[u] = __half2float(__ldcs(sva + e + u * 32));
+                }
+            }
+#pragma unroll
+            for (int u = 0; u < U; ++u) {
+                if (e + u * 32 < o1) {
+                    float xv[NV];
+                    VecIO<float, NV>::load(x, cc[u], xv);
+#pragma unroll
+                    for (int k = 0; k < NV; ++k) acc[k] += aa[u] * xv[k];
+                }
+            }
+        }
+        if (row < n) {
+            float xr[NV];
+            VecIO<float, NV>::load(x, row, xr);
+            const float d = dg[row];
+#pragma unroll
+            for (int k = 0; k < NV; ++k) acc[k] = acc[k] * hs + d * xr[k];
+            epi.apply(row, acc, pre, r0, r1);
+        }
+    }
+    if constexpr (Epi::kRed > 0) {
+        __shared__ double sh[8];
+        double t0 = block_sum256(r0, sh);
+        if (threadIdx.x == 0) partials[blockIdx.x] = t0;
+        if constexpr (Epi::kRed > 1) {
+            double t1 = block_sum256(r1, sh);
+            if (threadIdx.x == 0) partials[NB_RED + blockIdx.x] = t1;
+        }
+    }
+}
+
+// largest |a_ij|, i != j, as the bits of a non-negative double (ordered like the values)
+__global__ void k_offdiag_absmax(int64_t n, const int64_t* __restrict__ rp, const int32_t* __restrict__ ci,
+                                 const double* __restrict__ v, unsigned long long* mx) {
+    const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    double m = 0.0;
+    for (int64_t e = rp[i]; e < rp[i + 1]; ++e)
+        if (ci[e] != i) m = fmax(m, fabs(v[e]));
+    if (m > 0.0) atomicMax(mx, (unsigned long long)__double_as_longlong(m));
+}
+
+// the FP16 SELL values (same slots as k_sell_fill) and the row-sum diagonal
+__global__ void k_sell_fill_half(int64_t n, int64_t nslices, const int64_t* __restrict__ rp,
+                                 const int32_t* __restrict__ ci, const double* __restrict__ v,
+                                 const int64_t* __restrict__ soff, double inv_scale, double scale, __half* sv,
+                                 float* dg) {
+    const int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    if (t >= nslices * 32) return;
+    const int64_t sl = t >> 5, lane = t & 31, row = t;
+    const int64_t w = (soff[sl + 1] - soff[sl]) >> 5;
+    const int64_t e0 = row < n ? rp[row] : 0, len = row < n ? rp[row + 1] - e0 : 0;
+    double rowsum = 0.0, kept = 0.0;
+    for (int64_t k = 0; k < w; ++k) {
+        __half h = __float2half_rn(0.f);
+        if (k < len) {
+            const double a = v[e0 + k];
+            rowsum += a;
+            if (ci[e0 + k] != row) {
+                h = __float2half_rn((float)(a * inv_scale));
+                kept += (double)__half2float(h) * scale;
+            }
+        }
+        sv[soff[sl] + k * 32 + lane] = h;
+    }
+    if (row < n) dg[row] = (float)(rowsum - kept);
+}
+
+void build_sell_half(mpet_ctx* c, Csr& A) {
+    if (!A.s_off || !A.v64 || A.n == 0 || A.nnz == 0) return;
+    const int64_t stored = 0;
+    (void)stored;
+    int64_t nst = 0;
+    MPET_CUDA(cudaMemcpyAsync(&nst, A.s_off + A.nslices, sizeof(int64_t), cudaMemcpyDeviceToHost, c->stream));
+    TmpBuf bm(sizeof(unsigned long long));
+    MPET_CUDA(cudaMemsetAsync(bm.p, 0, sizeof(unsigned long long), c->stream));
+    k_offdiag_absmax<<<grid_for(A.n, 256), 256, 0, c->stream>>>(A.n, A.rp, A.ci, A.v64, bm.as<unsigned long long>());
+    MPET_CHECK_LAUNCH();
+    unsigned long long bits = 0;
+    MPET_CUDA(cudaMemcpyAsync(&bits, bm.p, sizeof(bits), cudaMemcpyDeviceToHost, c->stream));
+    MPET_CUDA(cudaStreamSynchronize(c->stream));
+    double mx = 0.0;
+    memcpy(&mx, &bits, sizeof(mx));
+    if (!(mx > 0.0) || !std::isfinite(mx)) return;  // diagonal matrix: nothing to gain
+    // the largest off-diagonal maps to [2^13, 2^14): far from the FP16 maximum, with
+    // 2^-24 .. 2^14 (38 binades) of normal and subnormal range below it
+    const int e = (int)std::ceil(std::log2(mx)) - 14;
+    const double scale = std::ldexp(1.0, e);
+    if (!device_fits(c, (size_t)nst * 2 + (size_t)A.n * 4)) return;
+    A.s_v16 = c->pool.alloc<__half>(nst);
+    A.s_d32 = c->pool.alloc<float>(A.n);
+    A.s_h_scale = (float)scale;
+    k_sell_fill_half<<<grid_for(A.nslices * 32, 256), 256, 0, c->stream>>>(A.n, A.nslices, A.rp, A.ci, A.v64, A.s_off,
+                                                                          1.0 / scale, scale, A.s_v16, A.s_d32);
+    MPET_CHECK_LAUNCH();
+    MPET_CUDA(cudaStreamSynchronize(c->stream));
 }
 
 __global__ void k_sell_width(int64_t n, int64_t nslices, const int64_t* __restrict__ rp, int64_t* w32) {
@@ -1032,6 +1167,18 @@ static void launch_spmv(mpet_ctx* c, const Csr& A, const T* va, const T* x, cons
     }
     const int32_t* skl = c->skip_done ? A.skl : nullptr;
     const double* skip = c->skip_done;
+    if constexpr (sizeof(T) == 4) {
+        if (variant == 32 && A.s_v16 && va == vals<T>(A)) {
+            int blocks = Epi::kRed > 0 ? NB_RED : grid_for(A.nslices * 32, 256);
+            if (Epi::kRed == 0 && blocks > 152 * 16) blocks = 152 * 16;
+            k_spmv_sell_h<NV, 4, Epi><<<blocks, 256, 0, c->stream>>>(A.n, A.nslices, A.s_off, A.s_ci, A.s_v16, A.s_d32,
+                                                                     A.s_h_scale, (const float*)x, epi, c->partials,
+                                                                     skl, skip);
+            MPET_CHECK_LAUNCH();
+            c->n_launch++;
+            return;
+        }
+    }
     if ((variant & 4) && sell_vals<T>(A) && va == vals<T>(A)) {
         int blocks = Epi::kRed > 0 ? NB_RED : grid_for(A.nslices * 32, 256);
         if (Epi::kRed == 0 && blocks > 152 * 16) blocks = 152 * 16;
@@ -1204,6 +1351,7 @@ const float* dinv_of<float>(const AmgLevel& L) { return L.dinv32; }
 // per row: staged needs row tiles, SELL its copy, 8 entries per lane (CSR)
 // 32 lanes per row.
 bool spmv_variant_available(const Csr& A, int v) {
+    if (v == 32) return A.s_v16 != nullptr;
     if (v == 8) return A.nb != nullptr;
     if (v < 0 || v > 5) return false;
     if (v & 4) return A.s_off != nullptr;  // 6, 7: SELL with late epilogue loads
@@ -1234,7 +1382,8 @@ static void autotune_matrix(mpet_ctx* c, Csr& A, const T* x, const Epi& epi, dou
     for (int lpr : {lpr0, lpr0 / 2, lpr0 * 2}) {
         if ((lpr < 4 || lpr > 32) && lpr != lpr0) continue;
         A.lpr = lpr;
-        for (int v : {0, 1, 2, 3, 4, 5, 6, 7, 8}) {
+        for (int v : {0, 1, 2, 3, 4, 5, 6, 7, 8, 32}) {
+            if (v == 32 && (sizeof(T) != 4 || !A.s_v16 || lpr != lpr0)) continue;
             if (!spmv_variant_available(A, v) || (v >= 4 && v < 8 && (!sell_vals<T>(A) || lpr != lpr0))) continue;
             if (v == 8 && (!Epi::kSystem || NV != 1 || !nb_vals<T>(*A.nb) || lpr != lpr0)) continue;
             // batches: the staged kernel has no slice skipping
@@ -3360,7 +3509,8 @@ static double csr_rho(mpet_ctx* c, const Csr& A, const double* dinv);
 
 static void release_csr(mpet_ctx* c, Csr& A) {
     for (void* p : {(void*)A.rp, (void*)A.ci, (void*)A.v64, (void*)A.v32, (void*)A.tiles, (void*)A.s_off,
-                    (void*)A.s_ci, (void*)A.s_v32, (void*)A.s_v64, (void*)A.skl})
+                    (void*)A.s_ci, (void*)A.s_v32, (void*)A.s_v64, (void*)A.skl, (void*)A.s_v16,
+                    (void*)A.s_d32})
         c->pool.release(p);
     A = Csr();
 }
@@ -3391,6 +3541,7 @@ void upload_amg(mpet_ctx* c, AmgHier& h, const HostAmg& ha, int nvec, bool fp32)
         const HostAmgLevel& hl = ha.lev[k];
         AmgLevel& L = h.lev[k];
         upload_csr(c, hl.A, L.A, fp32);
+        if (fp32 && k == 0) build_sell_half(c, L.A);
         L.rho = hl.rho;
         const int64_t n = hl.A.n;
         L.dinv64 = c->pool.alloc<double>(n);
@@ -3453,6 +3604,7 @@ void finish_device_hier(mpet_ctx* c, AmgHier& h, int nvec, bool fp32) {
     for (size_t k = 0; k < h.lev.size(); ++k) {
         AmgLevel& L = h.lev[k];
         finish_device_csr(c, L.A, fp32);
+        if (fp32 && k == 0) build_sell_half(c, L.A);
         const int64_t n = L.A.n;
         if (fp32) {
             L.dinv32 = c->pool.alloc<float>(n);
