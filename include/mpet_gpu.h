@@ -120,6 +120,9 @@ typedef struct mpet_params {
                                           replays with a host check after each (test hook) */
     int32_t amg_cheb_degree_coarse;    /* Chebyshev degree on levels 2, 3, ... of every
                                           hierarchy (<= 0: amg_cheb_degree) */
+    int32_t prec_u_order;              /* rows of the first displacement level (device set-up):
+                                          0 the P2 node order, 1 (default) a spatial (Morton)
+                                          order of the nodes, for the locality of its products */
 } mpet_params;
 
 typedef struct mpet_stats {

@@ -647,6 +647,116 @@ bool sa_prolongator_device(mpet_ctx* c, const DMat& A, const double* dg, const d
     return true;
 }
 
+// ---- spatial order of the first displacement level ----------------------------------
+
+// new row k <- old row iperm[k]: row lengths
+__global__ void k_perm_len(int64_t n, const int64_t* __restrict__ rp, const int32_t* __restrict__ iperm, int64_t* cnt) {
+    const int64_t k = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    if (k < n) cnt[k] = rp[iperm[k] + 1] - rp[iperm[k]];
+}
+
+// copies old row iperm[k] to new row k, columns through perm (null: unchanged)
+__global__ void k_perm_fill(int64_t n, const int64_t* __restrict__ rp, const int32_t* __restrict__ ci,
+                            const double* __restrict__ v, const int32_t* __restrict__ iperm,
+                            const int32_t* __restrict__ perm, const int64_t* __restrict__ nrp, int32_t* oci,
+                            double* ov) {
+    const int64_t k = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    if (k >= n) return;
+    const int64_t i = iperm[k], e0 = rp[i], e1 = rp[i + 1], p0 = nrp[k];
+    for (int64_t e = e0; e < e1; ++e) {
+        oci[p0 + (e - e0)] = perm ? perm[ci[e]] : ci[e];
+        ov[p0 + (e - e0)] = v[e];
+    }
+}
+
+// Pi A Pi^T (cols = true) or Pi A (rows only), rows sorted
+DMat permuted(mpet_ctx* c, const DMat& A, const int32_t* perm, const int32_t* iperm, bool cols) {
+    DMat B;
+    B.n = A.n;
+    B.m = A.m;
+    B.rp = c->pool.alloc<int64_t>(A.n + 1);
+    TmpBuf bcnt(sizeof(int64_t) * (A.n + 1));
+    k_perm_len<<<grid_for(A.n, 256), 256, 0, c->stream>>>(A.n, A.rp, iperm, bcnt.as<int64_t>());
+    MPET_CHECK_LAUNCH();
+    B.nnz = scan_counts(c, bcnt.as<int64_t>(), A.n, B.rp);
+    if (B.nnz != A.nnz) fail(MPET_ERR_STATE, "permutation lost entries");
+    B.ci = c->pool.alloc<int32_t>(B.nnz);
+    B.v = c->pool.alloc<double>(B.nnz);
+    if (!cols) {
+        k_perm_fill<<<grid_for(A.n, 256), 256, 0, c->stream>>>(A.n, A.rp, A.ci, A.v, iperm, nullptr, B.rp, B.ci, B.v);
+        MPET_CHECK_LAUNCH();
+        return B;
+    }
+    TmpBuf tci(sizeof(int32_t) * (B.nnz + 1)), tv(sizeof(double) * (B.nnz + 1));
+    k_perm_fill<<<grid_for(A.n, 256), 256, 0, c->stream>>>(A.n, A.rp, A.ci, A.v, iperm, perm, B.rp,
+                                                           tci.as<int32_t>(), tv.as<double>());
+    k_row_rank<<<(unsigned)((B.n + SPG_WARPS - 1) / SPG_WARPS), 256, 0, c->stream>>>(
+        B.n, B.rp, tci.as<int32_t>(), tv.as<double>(), B.ci, B.v);
+    MPET_CHECK_LAUNCH();
+    MPET_CUDA(cudaStreamSynchronize(c->stream));
+    return B;
+}
+
+uint64_t spread3(uint64_t x) {  // the low 21 bits of x to every third bit
+    x &= 0x1fffffULL;
+    x = (x | x << 32) & 0x1f00000000ffffULL;
+    x = (x | x << 16) & 0x1f0000ff0000ffULL;
+    x = (x | x << 8) & 0x100f00f00f00f00fULL;
+    x = (x | x << 4) & 0x10c30c30c30c30c3ULL;
+    x = (x | x << 2) & 0x1249249249249249ULL;
+    return x;
+}
+
+// P2 nodes (vertices, then edge midpoints) sorted by the Morton code of their
+// position in the mesh's bounding box (21 bits per axis; ties by node id):
+// u_perm[node] = its row of the first displacement level, u_iperm the inverse.
+void build_u_perm(mpet_ctx* c) {
+    if (c->u_perm) return;
+    const int64_t nv = c->nv, ne = c->ne, nn = c->nnodes;
+    if (nn != nv + ne) fail(MPET_ERR_STATE, "P2 nodes are not vertices + edges");
+    std::vector<double> x((size_t)nv * 3);
+    std::vector<int64_t> ek(ne);
+    MPET_CUDA(cudaMemcpyAsync(x.data(), c->x, sizeof(double) * x.size(), cudaMemcpyDeviceToHost, c->stream));
+    if (ne) MPET_CUDA(cudaMemcpyAsync(ek.data(), c->edge_key, sizeof(int64_t) * ne, cudaMemcpyDeviceToHost, c->stream));
+    MPET_CUDA(cudaStreamSynchronize(c->stream));
+    double lo[3] = {x[0], x[1], x[2]}, hi[3] = {x[0], x[1], x[2]};
+    for (int64_t v = 0; v < nv; ++v)
+        for (int d = 0; d < 3; ++d) {
+            lo[d] = std::min(lo[d], x[3 * v + d]);
+            hi[d] = std::max(hi[d], x[3 * v + d]);
+        }
+    double sc[3];
+    for (int d = 0; d < 3; ++d) sc[d] = hi[d] > lo[d] ? 2097151.0 / (hi[d] - lo[d]) : 0.0;
+    std::vector<std::pair<uint64_t, int32_t>> key(nn);
+    auto code = [&](const double* p) {
+        uint64_t m = 0;
+        for (int d = 0; d < 3; ++d) {
+            double q = (p[d] - lo[d]) * sc[d];
+            q = q < 0.0 ? 0.0 : (q > 2097151.0 ? 2097151.0 : q);
+            m |= spread3((uint64_t)q) << d;
+        }
+        return m;
+    };
+    for (int64_t v = 0; v < nv; ++v) key[v] = {code(&x[3 * v]), (int32_t)v};
+    for (int64_t e = 0; e < ne; ++e) {
+        const int64_t a = ek[e] / nv, b = ek[e] % nv;
+        const double mid[3] = {0.5 * (x[3 * a] + x[3 * b]), 0.5 * (x[3 * a + 1] + x[3 * b + 1]),
+                               0.5 * (x[3 * a + 2] + x[3 * b + 2])};
+        key[nv + e] = {code(mid), (int32_t)(nv + e)};
+    }
+    std::sort(key.begin(), key.end());
+    std::vector<int32_t> perm(nn), iperm(nn);
+    for (int64_t k = 0; k < nn; ++k) {
+        iperm[k] = key[k].second;
+        perm[key[k].second] = (int32_t)k;
+    }
+    c->u_perm = c->pool.alloc<int32_t>(nn);
+    c->u_iperm = c->pool.alloc<int32_t>(nn);
+    MPET_CUDA(cudaMemcpyAsync(c->u_perm, perm.data(), sizeof(int32_t) * nn, cudaMemcpyHostToDevice, c->stream));
+    MPET_CUDA(cudaMemcpyAsync(c->u_iperm, iperm.data(), sizeof(int32_t) * nn, cudaMemcpyHostToDevice, c->stream));
+    MPET_CUDA(cudaStreamSynchronize(c->stream));
+}
+
 }  // namespace
 
 void amg_setup_device(mpet_ctx* c, AmgHier& h, const Csr& A0, bool with_p0, double theta, int coarse_size,
@@ -682,6 +792,17 @@ void amg_setup_device(mpet_ctx* c, AmgHier& h, const Csr& A0, bool with_p0, doub
         MPET_CUDA(cudaMemcpyAsync(A.ci, A0.ci, sizeof(int32_t) * A.nnz, cudaMemcpyDeviceToDevice, c->stream));
         MPET_CUDA(cudaMemcpyAsync(A.v, A0.v64, sizeof(double) * A.nnz, cudaMemcpyDeviceToDevice, c->stream));
     }
+    // the first displacement level in a spatial order (rows and columns), its
+    // embedding's rows with it: products over neighbouring rows then share columns
+    const bool spatial = with_p0 && c->prm.prec_u_order == 1 && A.n == c->nnodes;
+    if (spatial) {
+        build_u_perm(c);
+        DMat B = permuted(c, A, c->u_perm, c->u_iperm, true);
+        dm_release(c, A);
+        A = B;
+        h.perm = c->u_perm;
+        h.iperm = c->u_iperm;
+    }
     tick(0);
     while (true) {
         AmgLevel L;
@@ -700,6 +821,11 @@ void amg_setup_device(mpet_ctx* c, AmgHier& h, const Csr& A0, bool with_p0, doub
         if (given) {
             P = embedding_p0(c);
             if (P.n != n) fail(MPET_ERR_INVALID, "first-level prolongator has the wrong row count");
+            if (spatial) {
+                DMat Q = permuted(c, P, nullptr, c->u_iperm, false);
+                dm_release(c, P);
+                P = Q;
+            }
         } else {
             const int sa_level = (int)h.lev.size() - 1 - (with_p0 ? 1 : 0);
             const double th = theta * pow(0.5, (double)sa_level);

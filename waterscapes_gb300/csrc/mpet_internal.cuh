@@ -198,6 +198,10 @@ struct AmgHier {
     double* cinv = nullptr;  // dense inverse of the coarsest operator, FP64
     void* pack_in = nullptr;  // padded (nvec = 4) input/output of the first level
     void* pack_out = nullptr;
+    // first-level row of each P2 node and its inverse when the first level is in
+    // a spatial order (owned by the context; null: node order)
+    const int32_t* perm = nullptr;
+    const int32_t* iperm = nullptr;
 };
 
 // Device-resident MINRES scalars (all FP64).
@@ -379,6 +383,8 @@ struct mpet_ctx {
     bool elem_tried = false;
     int elem_kernel = 1;          // element blocks of tetrahedra: 1 tensor cores, 0 FP64 CUDA cores
     bool amg_device = true;       // Laplacian-form hierarchies built on the GPU (false: host set-up)
+    int32_t* u_perm = nullptr;    // P2 node -> row of the spatially ordered first displacement level
+    int32_t* u_iperm = nullptr;   // and back (built once per mesh)
     // last device set-up, summed over its hierarchies (ms): block copy, diagonal +
     // spectral radius, strength + aggregation, tentative + smoothed prolongator,
     // transposes, Galerkin products, coarsest inverse, layouts + autotuning

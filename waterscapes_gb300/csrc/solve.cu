@@ -1797,20 +1797,21 @@ void profile_vcycle(mpet_ctx* c, int block, int reps, int* nlev, double* ms, dou
 
 // displacement components (3 per node) <-> the padded 4-wide layout of the
 // displacement hierarchy
+// (perm: row of each node in a spatially ordered first level, or null)
 template <typename T>
-__global__ void k_pack34(int64_t nodes, int dim, const T* __restrict__ a, T* b4) {
+__global__ void k_pack34(int64_t nodes, int dim, const T* __restrict__ a, T* b4, const int32_t* __restrict__ perm) {
     const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
     if (i >= nodes) return;
     const T v[4] = {a[dim * i], a[dim * i + 1], dim == 3 ? a[dim * i + 2] : T(0), T(0)};
-    VecIO<T, 4>::store(b4, i, v);
+    VecIO<T, 4>::store(b4, perm ? perm[i] : i, v);
 }
 
 template <typename T>
-__global__ void k_unpack43(int64_t nodes, int dim, const T* __restrict__ b4, T* a) {
+__global__ void k_unpack43(int64_t nodes, int dim, const T* __restrict__ b4, T* a, const int32_t* __restrict__ perm) {
     const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
     if (i >= nodes) return;
     T v[4];
-    VecIO<T, 4>::load(b4, i, v);
+    VecIO<T, 4>::load(b4, perm ? perm[i] : i, v);
     for (int k = 0; k < dim; ++k) a[dim * i + k] = v[k];
 }
 
@@ -1866,9 +1867,9 @@ static void precond(mpet_ctx* c, const T* r, T* z) {
         const int64_t nodes = c->nnodes;
         T* bin = (T*)hu.pack_in;
         T* xout = (T*)hu.pack_out;
-        k_pack34<T><<<grid_for(nodes, 256), 256, 0, main>>>(nodes, c->dim, r, bin);
+        k_pack34<T><<<grid_for(nodes, 256), 256, 0, main>>>(nodes, c->dim, r, bin, hu.perm);
         vcycle<T, 4>(c, hu, 0, bin, xout);
-        k_unpack43<T><<<grid_for(nodes, 256), 256, 0, main>>>(nodes, c->dim, xout, z);
+        k_unpack43<T><<<grid_for(nodes, 256), 256, 0, main>>>(nodes, c->dim, xout, z, hu.perm);
         MPET_CHECK_LAUNCH();
         c->n_launch += 2;
     }
@@ -2931,6 +2932,11 @@ __global__ void k_coarse_inst(int64_t nf, const int64_t* __restrict__ rp, const 
     for (int64_t e = rp[i]; e < rp[i + 1]; ++e) atomicMin(co + ci[e], fi[i]);
 }
 
+__global__ void k_gather_i32(int64_t n, const int32_t* __restrict__ idx, const int32_t* __restrict__ a, int32_t* b) {
+    const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    if (i < n) b[i] = a[idx[i]];
+}
+
 static int32_t* skl_of_rows(mpet_ctx* c, int64_t n, const int32_t* ri) {
     const int64_t ns = (n + 31) / 32;
     int32_t* skl = c->pool.alloc<int32_t>(2 * ns);
@@ -2948,7 +2954,10 @@ static void hier_skip_maps(mpet_ctx* c, AmgHier& h, const int32_t* inst0, int64_
         AmgLevel& L = h.lev[k];
         const int64_t n = L.A.n;
         L.inst = c->pool.alloc<int32_t>(n);
-        if (k == 0) {
+        if (k == 0 && h.iperm) {
+            k_gather_i32<<<grid_for(n, 256), 256, 0, c->stream>>>(n, h.iperm, inst0, L.inst);
+            MPET_CHECK_LAUNCH();
+        } else if (k == 0) {
             MPET_CUDA(cudaMemcpyAsync(L.inst, inst0, sizeof(int32_t) * n, cudaMemcpyDeviceToDevice, c->stream));
         } else {
             const AmgLevel& F = h.lev[k - 1];
@@ -3473,8 +3482,9 @@ static void choose_mf(mpet_ctx* c, AmgHier& h) {
     AmgLevel& L = h.lev[0];
     L.mf = false;
     c->mf_ms[0] = c->mf_ms[1] = 0.f;
-    // batches keep the CSR level (its products skip converged instances)
-    if (!c->mf_cell || c->mf_mode == 0 || (c->ninst > 0 && c->batch_skip)) return;
+    // batches keep the CSR level (its products skip converged instances), and
+    // so does a first level in a spatial order (the per-cell data are in node order)
+    if (!c->mf_cell || c->mf_mode == 0 || (c->ninst > 0 && c->batch_skip) || h.perm) return;
     if (c->mf_mode == 1) {
         L.mf = true;
         return;
@@ -3528,6 +3538,7 @@ void release_hier(mpet_ctx* c, AmgHier& h) {
     h.cinv = nullptr;
     h.pack_in = h.pack_out = nullptr;
     h.ncoarse = 0;
+    h.perm = h.iperm = nullptr;  // the context owns the permutation
 }
 
 void upload_amg(mpet_ctx* c, AmgHier& h, const HostAmg& ha, int nvec, bool fp32) {
