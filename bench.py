@@ -377,7 +377,8 @@ def profile_case(args):
     # (--inner-loop host: the inner iterations replay a graph without conditional
     # nodes, whose kernels a profiler can list one by one)
     sol = MPETSolver(problem, dict(dt=dt, T=1e9, precision="mixed", maxit=args.maxit, rtol=1e-10,
-                                   inner_loop=args.inner_loop or "device"))
+                                   inner_loop=args.inner_loop or "device",
+                                   prec_u_order=args.prec_u_order or "spatial"))
     sol._assemble(dt)
     torch.cuda.synchronize()
     t0 = time.perf_counter()
@@ -664,7 +665,8 @@ def vcycle_profile(args):
     import torch
     from waterscapes_gb300 import MPETSolver, _lib
     problem, dt = workload(args.n, args.networks, args.workload)
-    base = dict(dt=dt, T=1e9, theta=1.0, rtol=1e-10, precision="mixed", amg_setup=args.amg_setup or "device")
+    base = dict(dt=dt, T=1e9, theta=1.0, rtol=1e-10, precision="mixed", amg_setup=args.amg_setup or "device",
+                prec_u_order=args.prec_u_order or "spatial")
     if args.cheb_degree is not None:
         base["amg_cheb_degree"] = args.cheb_degree
     if args.cheb_degree_coarse is not None:
@@ -733,6 +735,8 @@ def main():
                     help="override amg_cheb_degree_fine (the finest level of every hierarchy)")
     ap.add_argument("--cheb-degree-coarse", type=int, default=None,
                     help="override amg_cheb_degree_coarse (levels 2, 3, ... of every hierarchy)")
+    ap.add_argument("--prec-u-order", default=None, choices=["spatial", "natural"],
+                    help="row order of the first displacement level (default: spatial)")
     ap.add_argument("--amg-setup", default=None, choices=["device", "host"],
                     help="where the smoothed-aggregation hierarchies are built (default: device)")
     ap.add_argument("--inner-loop", default=None, choices=["device", "host"],
@@ -825,6 +829,8 @@ def main():
         base["inner_loop"] = args.inner_loop
     if args.amg_setup is not None:
         base["amg_setup"] = args.amg_setup
+    if args.prec_u_order is not None:
+        base["prec_u_order"] = args.prec_u_order
     if args.prec_u_form is not None:
         base["prec_u_form"] = args.prec_u_form
     t0 = time.perf_counter()
