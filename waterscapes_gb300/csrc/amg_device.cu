@@ -708,9 +708,13 @@ uint64_t spread3(uint64_t x) {  // the low 21 bits of x to every third bit
 }
 
 // P2 nodes (vertices, then edge midpoints) sorted by the Morton code of their
-// position in the mesh's bounding box (21 bits per axis; ties by node id):
+// position in the mesh's bounding box (21 bits per axis; ties by node id),
+// then, within each window of 256 positions (the rows one 256-thread block of
+// the SELL kernel takes at a time), by decreasing row length of the first
+// level (stable): the Morton order alone mixes vertex rows (about 65 entries)
+// and edge rows (10-27) in every 32-row slice, which doubles the SELL padding.
 // u_perm[node] = its row of the first displacement level, u_iperm the inverse.
-void build_u_perm(mpet_ctx* c) {
+void build_u_perm(mpet_ctx* c, const Csr& A0) {
     if (c->u_perm) return;
     const int64_t nv = c->nv, ne = c->ne, nn = c->nnodes;
     if (nn != nv + ne) fail(MPET_ERR_STATE, "P2 nodes are not vertices + edges");
@@ -745,11 +749,19 @@ void build_u_perm(mpet_ctx* c) {
         key[nv + e] = {code(mid), (int32_t)(nv + e)};
     }
     std::sort(key.begin(), key.end());
+    std::vector<int64_t> rp(nn + 1);
+    MPET_CUDA(cudaMemcpyAsync(rp.data(), A0.rp, sizeof(int64_t) * (nn + 1), cudaMemcpyDeviceToHost, c->stream));
+    MPET_CUDA(cudaStreamSynchronize(c->stream));
     std::vector<int32_t> perm(nn), iperm(nn);
-    for (int64_t k = 0; k < nn; ++k) {
-        iperm[k] = key[k].second;
-        perm[key[k].second] = (int32_t)k;
+    for (int64_t k = 0; k < nn; ++k) iperm[k] = key[k].second;
+    constexpr int64_t WIN = 256;
+    for (int64_t w0 = 0; w0 < nn; w0 += WIN) {
+        const int64_t w1 = std::min(w0 + WIN, nn);
+        std::stable_sort(iperm.begin() + w0, iperm.begin() + w1, [&](int32_t a, int32_t b) {
+            return rp[a + 1] - rp[a] > rp[b + 1] - rp[b];
+        });
     }
+    for (int64_t k = 0; k < nn; ++k) perm[iperm[k]] = (int32_t)k;
     c->u_perm = c->pool.alloc<int32_t>(nn);
     c->u_iperm = c->pool.alloc<int32_t>(nn);
     MPET_CUDA(cudaMemcpyAsync(c->u_perm, perm.data(), sizeof(int32_t) * nn, cudaMemcpyHostToDevice, c->stream));
@@ -796,7 +808,7 @@ void amg_setup_device(mpet_ctx* c, AmgHier& h, const Csr& A0, bool with_p0, doub
     // embedding's rows with it: products over neighbouring rows then share columns
     const bool spatial = with_p0 && c->prm.prec_u_order == 1 && A.n == c->nnodes;
     if (spatial) {
-        build_u_perm(c);
+        build_u_perm(c, A0);
         DMat B = permuted(c, A, c->u_perm, c->u_iperm, true);
         dm_release(c, A);
         A = B;

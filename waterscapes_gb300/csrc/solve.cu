@@ -314,7 +314,8 @@ __global__ void __launch_bounds__(256) k_spmv(int64_t n, const int64_t* __restri
 // of the row.  The loop bound is the slice width, the same for every lane.
 // LATE: the epilogue's own loads come after the accumulation loop, which
 // frees their registers during it (more resident warps: the gathers are
-// latency-bound; k_spmv_sell_late); otherwise they are issued first and
+// latency-bound), and the slice's entries two chunks ahead are prefetched into
+// L2 (k_spmv_sell_late); otherwise the epilogue loads are issued first and
 // overlap the loop (k_spmv_sell).
 template <typename T, int NV, int U, class Epi, bool LATE>
 __device__ __forceinline__ void spmv_sell_body(int64_t n, int64_t nslices, const int64_t* __restrict__ soff,
@@ -336,6 +337,16 @@ __device__ __forceinline__ void spmv_sell_body(int64_t n, int64_t nslices, const
 #pragma unroll
         for (int k = 0; k < NV; ++k) acc[k] = T(0);
         for (int64_t e = soff[sl] + lane; e < o1; e += 32 * U) {
+            if (LATE && lane < U) {
+                // late variants also pull the slice's entries two chunks ahead into
+                // L2 (one 128-byte line per array and chunk row): the dependent
+                // loads of the next chunks then wait on L2, not on HBM
+                const int64_t pf = e - lane + (int64_t)(2 * U + lane) * 32;
+                if (pf < o1) {
+                    asm volatile("prefetch.global.L2 [%0];" ::"l"(sci + pf));
+                    asm volatile("prefetch.global.L2 [%0];" ::"l"(sva + pf));
+                }
+            }
             int32_t cc[U];
             T aa[U];
 #pragma unroll
