@@ -378,7 +378,7 @@ def profile_case(args):
     # nodes, whose kernels a profiler can list one by one)
     sol = MPETSolver(problem, dict(dt=dt, T=1e9, precision="mixed", maxit=args.maxit, rtol=1e-10,
                                    inner_loop=args.inner_loop or "device",
-                                   prec_u_order=args.prec_u_order or "spatial"))
+                                   prec_u_order=args.prec_u_order or "natural"))
     sol._assemble(dt)
     torch.cuda.synchronize()
     t0 = time.perf_counter()
@@ -666,7 +666,7 @@ def vcycle_profile(args):
     from waterscapes_gb300 import MPETSolver, _lib
     problem, dt = workload(args.n, args.networks, args.workload)
     base = dict(dt=dt, T=1e9, theta=1.0, rtol=1e-10, precision="mixed", amg_setup=args.amg_setup or "device",
-                prec_u_order=args.prec_u_order or "spatial")
+                prec_u_order=args.prec_u_order or "natural")
     if args.cheb_degree is not None:
         base["amg_cheb_degree"] = args.cheb_degree
     if args.cheb_degree_coarse is not None:
@@ -736,7 +736,7 @@ def main():
     ap.add_argument("--cheb-degree-coarse", type=int, default=None,
                     help="override amg_cheb_degree_coarse (levels 2, 3, ... of every hierarchy)")
     ap.add_argument("--prec-u-order", default=None, choices=["spatial", "natural"],
-                    help="row order of the first displacement level (default: spatial)")
+                    help="row order of the first displacement level (default: natural)")
     ap.add_argument("--amg-setup", default=None, choices=["device", "host"],
                     help="where the smoothed-aggregation hierarchies are built (default: device)")
     ap.add_argument("--inner-loop", default=None, choices=["device", "host"],

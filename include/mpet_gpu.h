@@ -121,8 +121,10 @@ typedef struct mpet_params {
     int32_t amg_cheb_degree_coarse;    /* Chebyshev degree on levels 2, 3, ... of every
                                           hierarchy (<= 0: amg_cheb_degree) */
     int32_t prec_u_order;              /* rows of the first displacement level (device set-up):
-                                          0 the P2 node order, 1 (default) a spatial (Morton)
-                                          order of the nodes, for the locality of its products */
+                                          0 (default) the P2 node order, 1 a spatial (Morton)
+                                          order of the nodes, each 256-row window sorted by row
+                                          length (slower at 64^3: 2.04 ms for the level against
+                                          1.33; kept as an option) */
 } mpet_params;
 
 typedef struct mpet_stats {
