@@ -2196,12 +2196,12 @@ __global__ void k_scale_b(int64_t n, const double* __restrict__ b, T* out, const
 // residuals resolve, so it also stops when a sweep no longer halves the residual
 // and the residual is already below rtol times this norm (PETSc's default test,
 // the reference's iterative solves mpetsolver.py:507-556, measures against the
-// right-hand side).  kr[0] and kr[2] are scratch.
+// right-hand side).  rhs and y are scratch vectors (default kr[0], kr[2]).
 template <typename T>
-static double precond_norm_b(mpet_ctx* c, const double* b) {
+static double precond_norm_b(mpet_ctx* c, const double* b, T* rhs = nullptr, T* y = nullptr) {
     const int64_t n = c->N;
-    T* rhs = (T*)c->kr[0];
-    T* y = (T*)c->kr[2];
+    if (!rhs) rhs = (T*)c->kr[0];
+    if (!y) y = (T*)c->kr[2];
     k_scale_b<T><<<grid_for(n, 256), 256, 0, c->stream>>>(n, b, rhs, c->sc);
     MPET_CHECK_LAUNCH();
     precond<T>(c, rhs, y);
@@ -2242,7 +2242,6 @@ static int solve_impl(mpet_ctx* c, const double* b, double* x, mpet_stats* st, b
         launch_spmv<double, 1>(c, c->A, c->A.v64, x, EpiResid64{c->orr, b, c->dinv});
         c->n_spmv++;
         k_outer_norms<<<1, 256, 0, c->stream>>>(c->sc, c->partials);
-        if (outer == 0) eta_b = precond_norm_b<T>(c, b);
         if (c->nrigid > 0) rigid_project(c, c->orr, c->rigid_Z, c->rigid_MZ, nullptr);  // rounding drift
         if (c->q_nk > 0) kernel_project(c, c->orr);
         T* rhs = (T*)c->kr[0];
@@ -2267,7 +2266,13 @@ static int solve_impl(mpet_ctx* c, const double* b, double* x, mpet_stats* st, b
         if (eta0 < 0) eta0 = eta;
         relres = eta0 > 0 ? eta / eta0 : 0.0;
         if (eta == 0.0 || eta <= c->prm.rtol * eta0) break;
-        if (outer > 0 && eta > 0.5 * eta_prev && eta <= c->prm.rtol * eta_b) break;  // FP64 floor
+        if (outer > 0 && eta > 0.5 * eta_prev) {
+            // a sweep that no longer halves the residual: the FP64 floor test, with the
+            // right-hand side's norm computed once, when first needed (kw[0], kw[1] are
+            // free until their reset below)
+            if (eta_b == 0.0) eta_b = precond_norm_b<T>(c, b, (T*)c->kw[0], (T*)c->kw[1]);
+            if (eta <= c->prm.rtol * eta_b) break;
+        }
         eta_prev = eta;
         if (iters >= maxit) {
             status = MPET_ERR_MAXIT;
