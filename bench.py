@@ -266,6 +266,20 @@ def spmv_tuning(solver, fp64=False):
             "chosen": names[6 if ch.value == 8 else ch.value]}
 
 
+def level_variants(solver):
+    """SpMV variant the set-up autotuner chose for each level's operator, per
+    hierarchy (displacement, then each network): 4/5 SELL-32, 6/7 SELL late,
+    0-3 CSR register/staged, 8 node blocks, 16 matrix-free, 32 SELL FP16."""
+    from waterscapes_gb300 import _lib
+    out = {}
+    for blk in range(solver.J + 1):
+        sizes, _ = solver.amg_info(blk)
+        va = np.zeros(max(len(sizes), 1), np.int32)
+        solver.ctx.call("mpet_get_amg_variants", blk, _lib._ptr(va), None, None)
+        out["displacement" if blk == 0 else "pressure %d" % blk] = [int(v) for v in va[:len(sizes)]]
+    return out
+
+
 def prec_setup_ms(solver):
     """Split of the last preconditioner set-up (ms): GPU block assembly, block
     downloads (host set-up only), the hierarchies (built on the GPU, or by
@@ -963,6 +977,7 @@ def main():
         "spmv_tuning": spmv_tuning(sol),
         "spmv_tuning_fp64_residual": spmv_tuning(sol, fp64=True),
         "preconditioner_u_block": prec_form(sol),
+        "preconditioner_level_variants": level_variants(sol),
         "iteration_breakdown_ms": dict(split, spmv_fp32=(spmv.get("fp32") or spmv["fp64"])["ms"],
                                        preconditioner=precond_ms),
         "fp64_iteration_breakdown_ms": res.get("fp64", {}).get("iteration_breakdown_ms"),

@@ -82,7 +82,7 @@ typedef struct mpet_params {
     double S[MPET_MAX_NETWORKS * MPET_MAX_NETWORKS]; /* transfer, row-major J x J (stride 8) */
     double theta;                      /* theta-scheme weight */
     double rtol;                       /* relative preconditioned residual, e.g. 1e-10 */
-    double inner_rtol;                 /* mixed: reduction per inner FP32 MINRES solve */
+    double inner_rtol;                 /* mixed: reduction per inner FP32 MINRES solve (<= 0: 3e-4) */
     int32_t maxit;                     /* Krylov iterations per solve (all inner solves) */
     int32_t max_outer;                 /* refinement sweeps per solve */
     double amg_theta;                  /* strength threshold, e.g. 0.1 */
@@ -119,7 +119,8 @@ typedef struct mpet_params {
                                           device-side loop (default); 1: three-iteration graph
                                           replays with a host check after each (test hook) */
     int32_t amg_cheb_degree_coarse;    /* Chebyshev degree on levels 2, 3, ... of every
-                                          hierarchy (<= 0: amg_cheb_degree) */
+                                          hierarchy (<= 0: amg_cheb_degree; the Python
+                                          solver's default is 3) */
     int32_t prec_u_order;              /* rows of the first displacement level (device set-up):
                                           0 (default) the P2 node order, 1 a spatial (Morton)
                                           order of the nodes, each 256-row window sorted by row

@@ -201,7 +201,7 @@ int mpet_setup(mpet_ctx* c, const mpet_params* p) {
     check_params(c, p);
     c->prm = *p;
     c->gmres = wants_gmres(c, p);
-    if (c->prm.inner_rtol <= 0) c->prm.inner_rtol = 1e-4;
+    if (c->prm.inner_rtol <= 0) c->prm.inner_rtol = 3e-4;
     if (c->prm.amg_theta < 0) c->prm.amg_theta = 0.1;
     build_topology(c);
     build_pattern(c);
@@ -237,7 +237,7 @@ int mpet_update_params(mpet_ctx* c, const mpet_params* p) {
     require(p->precision == c->prm.precision, MPET_ERR_INVALID, "precision is fixed at setup");
     c->prm = *p;
     c->gmres = wants_gmres(c, p);
-    if (c->prm.inner_rtol <= 0) c->prm.inner_rtol = 1e-4;
+    if (c->prm.inner_rtol <= 0) c->prm.inner_rtol = 3e-4;
     c->assembled = false;
     c->precond_ready = false;
     c->u_hier_valid = false;

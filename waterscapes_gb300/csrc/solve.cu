@@ -1416,7 +1416,9 @@ static void autotune_matrix(mpet_ctx* c, Csr& A, const T* x, const Epi& epi, dou
             const float med = t[3];
             const float ms = med * ((v == 0 && lpr == lpr0) ? 0.97f : 1.0f);
             if (ms_out && lpr == lpr0 && (v <= 5 || v == 8)) ms_out[v == 8 ? 6 : v] = med;
-            if (ms < best) {
+            // a later candidate must beat the incumbent by 2%: near-ties keep the
+            // earlier (simpler) variant instead of following the timing noise
+            if (ms < 0.98f * best || best >= 1e30f) {
                 best = ms;
                 best_v = v;
                 best_lpr = lpr;

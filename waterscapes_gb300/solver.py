@@ -157,11 +157,11 @@ class MPETSolver:
         """mpetsolver.py:86-98 plus engine keys (ignored by the reference)."""
         return {"dt": 0.1, "t": 0.0, "T": 1.0, "theta": 1.0, "u_degree": 2, "p_degree": 1,
                 "direct_solver": True,
-                "precision": "mixed", "rtol": 1e-10, "inner_rtol": 1e-4, "maxit": 20000,
+                "precision": "mixed", "rtol": 1e-10, "inner_rtol": 3e-4, "maxit": 20000,
                 "max_outer": 40, "amg_theta": 0.1, "amg_cheb_degree": 4, "amg_coarse_size": 500,
                 "amg_p2_to_p1": True, "prec_u_weight": "mu+lmbda", "prec_network_modes": True,
                 "prec_u_form": "laplacian", "krylov": "auto", "gmres_restart": 30,
-                "amg_cheb_degree_fine": 0, "amg_cheb_degree_coarse": 0, "inner_loop": "device",
+                "amg_cheb_degree_fine": 0, "amg_cheb_degree_coarse": 3, "inner_loop": "device",
                 "amg_setup": "device", "prec_u_order": "natural",
                 "check_every": 4, "device": 0}
 
@@ -199,7 +199,7 @@ class MPETSolver:
         prm.krylov = _lib.KRYLOV[self.params.get("krylov", "auto")]
         prm.gmres_restart = int(self.params.get("gmres_restart", 30))
         prm.amg_cheb_degree_fine = int(self.params.get("amg_cheb_degree_fine", 0))
-        prm.amg_cheb_degree_coarse = int(self.params.get("amg_cheb_degree_coarse", 0))
+        prm.amg_cheb_degree_coarse = int(self.params.get("amg_cheb_degree_coarse", 3))
         prm.prec_u_order = {"natural": 0, "spatial": 1}[self.params.get("prec_u_order", "natural")]
         prm.inner_loop = {"device": 0, "host": 1}[self.params.get("inner_loop", "device")]
         if self.problem.u_has_nullspace:
