@@ -148,7 +148,7 @@ def spmv_alg_bytes(solver, sv):
     N, nnz = solver.N, solver.nnz
     ch = ctypes.c_int32()
     solver.ctx.call("mpet_get_spmv_tuning" if sv == 4 else "mpet_get_spmv_tuning_fp64", None, ctypes.byref(ch))
-    if ch.value == 8:
+    if ch.value in (8, 9):
         nb = ctypes.c_int64()
         solver.ctx.call("mpet_get_node_block_info", ctypes.byref(nb), None)
         return nnz * sv + nb.value * 4 + 2 * N * sv, "node-block"
@@ -261,9 +261,12 @@ def spmv_tuning(solver, fp64=False):
     ch = ctypes.c_int32()
     solver.ctx.call("mpet_get_spmv_tuning_fp64" if fp64 else "mpet_get_spmv_tuning",
                     ms.ctypes.data_as(ctypes.c_void_p), ctypes.byref(ch))
-    names = ["register/4", "register/8", "staged/4", "staged/8", "sell32/4", "sell32/8", "node-block"]
-    return {"ms": {names[v]: round(float(ms[v]), 4) for v in range(7) if ms[v] > 0},
-            "chosen": names[6 if ch.value == 8 else ch.value]}
+    slots = ["register/4", "register/8", "staged/4", "staged/8", "sell32/4", "sell32/8", "node-block"]
+    variants = {0: "register/4", 1: "register/8", 2: "staged/4", 3: "staged/8", 4: "sell32/4", 5: "sell32/8",
+                6: "sell32-late/4", 7: "sell32-late/8", 8: "node-block", 9: "node-block/64 registers",
+                32: "sell32-fp16"}
+    return {"ms": {slots[v]: round(float(ms[v]), 4) for v in range(7) if ms[v] > 0},
+            "chosen": variants.get(ch.value, str(ch.value))}
 
 
 def level_variants(solver):

@@ -140,7 +140,8 @@ struct Csr {
     // 32 lanes per row, or with the SELL copy), bit 1 = shared-memory staged
     // (needs tiles; with bit 2: the SELL kernel with its epilogue loads after
     // the accumulation, 6 and 7), bit 2 = SELL-32 copy (needs s_off);
-    // 8 = node-block copy; 32 = SELL-32 with FP16 off-diagonals (needs s_v16)
+    // 8 = node-block copy (9: its FP32 kernel held to 64 registers, 4 blocks per
+    // SM); 32 = SELL-32 with FP16 off-diagonals (needs s_v16)
     int variant = 0;
     // mixed precision: variant and lanes per row of the FP64 products when they
     // were tuned apart from the FP32 copy's (-1: none, use variant / lpr)

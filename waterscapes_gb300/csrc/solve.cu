@@ -584,8 +584,9 @@ __global__ void k_sell_fill(int64_t n, int64_t nslices, const int64_t* __restric
 // block per iteration, are held to 80 registers (3 resident 256-thread blocks per
 // SM) and run as one wave of resident blocks (the reduction partials past the grid
 // are written as zeros).
-template <typename T, int JM, class Epi, bool UU = false>
-__global__ void __launch_bounds__(256, sizeof(T) == 8 ? 3 : 1) k_spmv_nb(int64_t nnodes, int64_t nv, int64_t Nu, int J, int64_t nsu,
+// OCC (FP32 only): held to 64 registers, 4 resident blocks per SM (variant 9).
+template <typename T, int JM, class Epi, bool UU = false, bool OCC = false>
+__global__ void __launch_bounds__(256, sizeof(T) == 8 ? 3 : (OCC ? 4 : 1)) k_spmv_nb(int64_t nnodes, int64_t nv, int64_t Nu, int J, int64_t nsu,
                                                  int64_t ns, const NbSlice* __restrict__ sl,
                                                  const int32_t* __restrict__ perm, const int32_t* __restrict__ cols,
                                                  const T* __restrict__ vals, const T* __restrict__ x, Epi epi,
@@ -1120,7 +1121,7 @@ static int one_wave(K kern) {
 }
 
 template <typename T, class Epi>
-static void launch_nb(mpet_ctx* c, const NodeBlocks& nb, const T* x, const Epi& epi) {
+static void launch_nb(mpet_ctx* c, const NodeBlocks& nb, const T* x, const Epi& epi, bool occ = false) {
     const int64_t ns = nb.nsu + nb.nsp;
     int blocks = Epi::kRed > 0 ? NB_RED : grid_for(ns * 32, 256);
     if (Epi::kRed == 0 && blocks > 152 * 16) blocks = 152 * 16;
@@ -1133,7 +1134,20 @@ static void launch_nb(mpet_ctx* c, const NodeBlocks& nb, const T* x, const Epi& 
     cudaStream_t st = c->stream;
     const T* v = nb_vals<T>(nb);
     const int32_t* skl = c->skip_done ? nb.skl : nullptr;
-    if (J <= 2)
+    if (occ && sizeof(T) == 4) {
+        if (J <= 2)
+            k_spmv_nb<T, 2, Epi, false, true><<<blocks, 256, 0, st>>>(c->nnodes, c->nv, c->Nu, J, nb.nsu, ns, nb.sl,
+                                                                      nb.perm, nb.cols, v, x, epi, c->partials, skl,
+                                                                      c->skip_done);
+        else if (J <= 4)
+            k_spmv_nb<T, 4, Epi, false, true><<<blocks, 256, 0, st>>>(c->nnodes, c->nv, c->Nu, J, nb.nsu, ns, nb.sl,
+                                                                      nb.perm, nb.cols, v, x, epi, c->partials, skl,
+                                                                      c->skip_done);
+        else
+            k_spmv_nb<T, 8, Epi, false, true><<<blocks, 256, 0, st>>>(c->nnodes, c->nv, c->Nu, J, nb.nsu, ns, nb.sl,
+                                                                      nb.perm, nb.cols, v, x, epi, c->partials, skl,
+                                                                      c->skip_done);
+    } else if (J <= 2)
         k_spmv_nb<T, 2, Epi><<<blocks, 256, 0, st>>>(c->nnodes, c->nv, c->Nu, J, nb.nsu, ns, nb.sl, nb.perm,
                                                      nb.cols, v, x, epi, c->partials, skl, c->skip_done);
     else if (J <= 4)
@@ -1171,8 +1185,8 @@ static void launch_spmv(mpet_ctx* c, const Csr& A, const T* va, const T* x, cons
     const int variant = own64 ? A.variant64 : A.variant;
     const int lpr = own64 ? A.lpr64 : A.lpr;
     if constexpr (NV == 1 && Epi::kSystem) {
-        if (variant == 8 && A.nb && nb_vals<T>(*A.nb) && va == vals<T>(A)) {
-            launch_nb<T>(c, *A.nb, x, epi);
+        if ((variant == 8 || variant == 9) && A.nb && nb_vals<T>(*A.nb) && va == vals<T>(A)) {
+            launch_nb<T>(c, *A.nb, x, epi, variant == 9);
             return;
         }
     }
@@ -1364,6 +1378,7 @@ const float* dinv_of<float>(const AmgLevel& L) { return L.dinv32; }
 bool spmv_variant_available(const Csr& A, int v) {
     if (v == 32) return A.s_v16 != nullptr;
     if (v == 8) return A.nb != nullptr;
+    if (v == 9) return A.nb != nullptr && A.v32 != nullptr;  // FP32 node blocks at 4 blocks per SM
     if (v < 0 || v > 5) return false;
     if (v & 4) return A.s_off != nullptr;  // 6, 7: SELL with late epilogue loads
     if ((v & 2) && A.ntiles == 0) return false;
@@ -1393,10 +1408,11 @@ static void autotune_matrix(mpet_ctx* c, Csr& A, const T* x, const Epi& epi, dou
     for (int lpr : {lpr0, lpr0 / 2, lpr0 * 2}) {
         if ((lpr < 4 || lpr > 32) && lpr != lpr0) continue;
         A.lpr = lpr;
-        for (int v : {0, 1, 2, 3, 4, 5, 6, 7, 8, 32}) {
+        for (int v : {0, 1, 2, 3, 4, 5, 6, 7, 8, 9, 32}) {
             if (v == 32 && (sizeof(T) != 4 || !A.s_v16 || lpr != lpr0)) continue;
+            if (v == 9 && sizeof(T) != 4) continue;
             if (!spmv_variant_available(A, v) || (v >= 4 && v < 8 && (!sell_vals<T>(A) || lpr != lpr0))) continue;
-            if (v == 8 && (!Epi::kSystem || NV != 1 || !nb_vals<T>(*A.nb) || lpr != lpr0)) continue;
+            if ((v == 8 || v == 9) && (!Epi::kSystem || NV != 1 || !nb_vals<T>(*A.nb) || lpr != lpr0)) continue;
             // batches: the staged kernel has no slice skipping
             if (c->ninst > 0 && c->batch_skip && v < 4 && (v & 2)) continue;
             A.variant = v;
@@ -1415,7 +1431,9 @@ static void autotune_matrix(mpet_ctx* c, Csr& A, const T* x, const Epi& epi, dou
             // so near-ties do not flip from one set-up to the next
             const float med = t[3];
             const float ms = med * ((v == 0 && lpr == lpr0) ? 0.97f : 1.0f);
+            // (slot 6: the faster node-block kernel)
             if (ms_out && lpr == lpr0 && (v <= 5 || v == 8)) ms_out[v == 8 ? 6 : v] = med;
+            if (ms_out && lpr == lpr0 && v == 9 && (ms_out[6] <= 0.0 || med < ms_out[6])) ms_out[6] = med;
             // a later candidate must beat the incumbent by 2%: near-ties keep the
             // earlier (simpler) variant instead of following the timing noise
             if (ms < 0.98f * best || best >= 1e30f) {
