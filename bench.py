@@ -688,6 +688,8 @@ def vcycle_profile(args):
         base["amg_cheb_degree"] = args.cheb_degree
     if args.cheb_degree_coarse is not None:
         base["amg_cheb_degree_coarse"] = args.cheb_degree_coarse
+    if args.cheb_coarse_level is not None:
+        base["amg_cheb_coarse_level"] = args.cheb_coarse_level
     sol = MPETSolver(problem, base)
     sol._assemble(dt)
     torch.cuda.synchronize()
@@ -752,6 +754,8 @@ def main():
                     help="override amg_cheb_degree_fine (the finest level of every hierarchy)")
     ap.add_argument("--cheb-degree-coarse", type=int, default=None,
                     help="override amg_cheb_degree_coarse (levels 2, 3, ... of every hierarchy)")
+    ap.add_argument("--cheb-coarse-level", type=int, default=None,
+                    help="override amg_cheb_coarse_level (first level with the coarse degree)")
     ap.add_argument("--prec-u-order", default=None, choices=["spatial", "natural"],
                     help="row order of the first displacement level (default: natural)")
     ap.add_argument("--amg-setup", default=None, choices=["device", "host"],

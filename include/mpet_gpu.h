@@ -118,9 +118,12 @@ typedef struct mpet_params {
     int32_t inner_loop;                /* 0: each inner Krylov solve is one graph launch with a
                                           device-side loop (default); 1: three-iteration graph
                                           replays with a host check after each (test hook) */
-    int32_t amg_cheb_degree_coarse;    /* Chebyshev degree on levels 2, 3, ... of every
-                                          hierarchy (<= 0: amg_cheb_degree; the Python
-                                          solver's default is 3) */
+    int32_t amg_cheb_degree_coarse;    /* Chebyshev degree on the levels from
+                                          amg_cheb_coarse_level on, in every hierarchy
+                                          (<= 0: amg_cheb_degree; the Python solver's
+                                          default is 3) */
+    int32_t amg_cheb_coarse_level;     /* first level that takes amg_cheb_degree_coarse
+                                          (<= 0: 2) */
     int32_t prec_u_order;              /* rows of the first displacement level (device set-up):
                                           0 (default) the P2 node order, 1 a spatial (Morton)
                                           order of the nodes, each 256-row window sorted by row

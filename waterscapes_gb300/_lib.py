@@ -59,6 +59,7 @@ class MpetParams(ctypes.Structure):
         ("amg_cheb_degree_fine", ctypes.c_int32),
         ("inner_loop", ctypes.c_int32),
         ("amg_cheb_degree_coarse", ctypes.c_int32),
+        ("amg_cheb_coarse_level", ctypes.c_int32),
         ("prec_u_order", ctypes.c_int32),
     ]
 

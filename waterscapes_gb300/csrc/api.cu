@@ -182,6 +182,7 @@ static void check_params(const mpet_ctx* c, const mpet_params* p) {
     require(p->amg_cheb_degree_fine <= 32, MPET_ERR_INVALID, "amg_cheb_degree_fine must be at most 32");
     require(p->amg_cheb_degree_coarse <= 32, MPET_ERR_INVALID, "amg_cheb_degree_coarse must be at most 32");
     require(p->prec_u_order == 0 || p->prec_u_order == 1, MPET_ERR_INVALID, "prec_u_order must be 0 or 1");
+    require(p->amg_cheb_coarse_level <= 16, MPET_ERR_INVALID, "amg_cheb_coarse_level must be at most 16");
     require(p->krylov >= MPET_KRYLOV_AUTO && p->krylov <= MPET_KRYLOV_GMRES && p->gmres_restart <= 64,
             MPET_ERR_INVALID, "unknown Krylov method or restart above 64");
     if (p->formulation == MPET_FORM_TOTAL_PRESSURE) {

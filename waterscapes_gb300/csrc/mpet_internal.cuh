@@ -193,7 +193,8 @@ struct AmgHier {
     int nvec = 1;
     int cheb_degree = 3;
     int cheb_degree0 = 3;  // on the finest level
-    int cheb_degree_c = 3;  // on levels 2, 3, ...
+    int cheb_degree_c = 3;  // on levels cheb_level_c, ...
+    int cheb_level_c = 2;
     std::vector<AmgLevel> lev;
     int64_t ncoarse = 0;
     double* cinv = nullptr;  // dense inverse of the coarsest operator, FP64

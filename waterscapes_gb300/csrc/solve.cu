@@ -1714,7 +1714,7 @@ static void cheb(mpet_ctx* c, AmgHier& h, AmgLevel& L, const T* b, const T* xin,
     const double sigma = theta / delta;
     double rho_old = 1.0 / sigma;
     const int64_t lk = &L - &h.lev[0];
-    const int s = lk == 0 ? h.cheb_degree0 : (lk >= 2 ? h.cheb_degree_c : h.cheb_degree);
+    const int s = lk == 0 ? h.cheb_degree0 : (lk >= h.cheb_level_c ? h.cheb_degree_c : h.cheb_degree);
     T* d = (T*)L.d;
     T* t0 = (T*)L.t0;
     T* t1 = (T*)L.t1;
@@ -1795,7 +1795,7 @@ static void profile_levels(mpet_ctx* c, AmgHier& h, int reps, double* ms, double
             bytes[k] = (double)h.ncoarse * h.ncoarse * 8.0 + 2.0 * h.ncoarse * NV * sv;
             continue;
         }
-        const int s = k == 0 ? h.cheb_degree0 : (k >= 2 ? h.cheb_degree_c : h.cheb_degree);
+        const int s = k == 0 ? h.cheb_degree0 : ((int)k >= h.cheb_level_c ? h.cheb_degree_c : h.cheb_degree);
         const double nc = (double)h.lev[k + 1].A.n, vecc = nc * NV * sv;
         // a product with A: the CSR entries and row pointers, or (matrix-free) the
         // incidence and per-cell node ids (NN each), the per-cell data, the row
@@ -3583,6 +3583,7 @@ void upload_amg(mpet_ctx* c, AmgHier& h, const HostAmg& ha, int nvec, bool fp32)
     h.cheb_degree = c->prm.amg_cheb_degree > 0 ? c->prm.amg_cheb_degree : 4;
     h.cheb_degree0 = c->prm.amg_cheb_degree_fine > 0 ? c->prm.amg_cheb_degree_fine : h.cheb_degree;
     h.cheb_degree_c = c->prm.amg_cheb_degree_coarse > 0 ? c->prm.amg_cheb_degree_coarse : h.cheb_degree;
+    h.cheb_level_c = c->prm.amg_cheb_coarse_level > 0 ? c->prm.amg_cheb_coarse_level : 2;
     h.lev.resize(ha.lev.size());
     for (size_t k = 0; k < ha.lev.size(); ++k) {
         const HostAmgLevel& hl = ha.lev[k];
@@ -3648,6 +3649,7 @@ void finish_device_hier(mpet_ctx* c, AmgHier& h, int nvec, bool fp32) {
     h.cheb_degree = c->prm.amg_cheb_degree > 0 ? c->prm.amg_cheb_degree : 4;
     h.cheb_degree0 = c->prm.amg_cheb_degree_fine > 0 ? c->prm.amg_cheb_degree_fine : h.cheb_degree;
     h.cheb_degree_c = c->prm.amg_cheb_degree_coarse > 0 ? c->prm.amg_cheb_degree_coarse : h.cheb_degree;
+    h.cheb_level_c = c->prm.amg_cheb_coarse_level > 0 ? c->prm.amg_cheb_coarse_level : 2;
     for (size_t k = 0; k < h.lev.size(); ++k) {
         AmgLevel& L = h.lev[k];
         finish_device_csr(c, L.A, fp32);

@@ -161,7 +161,8 @@ class MPETSolver:
                 "max_outer": 40, "amg_theta": 0.1, "amg_cheb_degree": 4, "amg_coarse_size": 500,
                 "amg_p2_to_p1": True, "prec_u_weight": "mu+lmbda", "prec_network_modes": True,
                 "prec_u_form": "laplacian", "krylov": "auto", "gmres_restart": 30,
-                "amg_cheb_degree_fine": 0, "amg_cheb_degree_coarse": 3, "inner_loop": "device",
+                "amg_cheb_degree_fine": 0, "amg_cheb_degree_coarse": 3, "amg_cheb_coarse_level": 2,
+                "inner_loop": "device",
                 "amg_setup": "device", "prec_u_order": "natural",
                 "check_every": 4, "device": 0}
 
@@ -200,6 +201,7 @@ class MPETSolver:
         prm.gmres_restart = int(self.params.get("gmres_restart", 30))
         prm.amg_cheb_degree_fine = int(self.params.get("amg_cheb_degree_fine", 0))
         prm.amg_cheb_degree_coarse = int(self.params.get("amg_cheb_degree_coarse", 3))
+        prm.amg_cheb_coarse_level = int(self.params.get("amg_cheb_coarse_level", 2))
         prm.prec_u_order = {"natural": 0, "spatial": 1}[self.params.get("prec_u_order", "natural")]
         prm.inner_loop = {"device": 0, "host": 1}[self.params.get("inner_loop", "device")]
         if self.problem.u_has_nullspace:
