@@ -955,6 +955,7 @@ def main():
         return
     sp32 = spmv.get("fp32") or spmv.get("fp64")
     headline = args.workload == "cube" and n == 64 and J == 4 and not tp
+    tuning = spmv_tuning(sol)
     line = {
         "metric": METRIC if headline else "MPET steps/s, mixed vs FP64 GPU at 1e-8 rel err; SpMV HBM GB/s",
         "value": value,
@@ -981,14 +982,15 @@ def main():
         "setup_s": {"mesh_dofmap_pattern": t_setup, "assemble_plus_amg": t_asm_amg,
                     "preconditioner_ms": prec_setup_ms(sol)},
         "spmv": spmv,
-        "spmv_tuning": spmv_tuning(sol),
+        "spmv_tuning": tuning,
         "spmv_tuning_fp64_residual": spmv_tuning(sol, fp64=True),
         "preconditioner_u_block": prec_form(sol),
         "preconditioner_level_variants": level_variants(sol),
         "iteration_breakdown_ms": dict(split, spmv_fp32=(spmv.get("fp32") or spmv["fp64"])["ms"],
                                        preconditioner=precond_ms),
         "fp64_iteration_breakdown_ms": res.get("fp64", {}).get("iteration_breakdown_ms"),
-        "roofline": {"kernel": ROOFLINE_KERNEL[sp32["layout"]] + (" FP32" if "fp32" in spmv else " FP64"),
+        "roofline": {"kernel": ROOFLINE_KERNEL[sp32["layout"]] + (" FP32" if "fp32" in spmv else " FP64")
+                     + (", 64-register kernel" if tuning.get("chosen") == "node-block/64 registers" else ""),
                      "bound": "hbm", "achieved": sp32["gbs"], "peak": hbm, "unit": "GB/s",
                      "frac": sp32["gbs"] / hbm, "peak_kind": peak_kind,
                      "alg_bytes_per_launch": sp32["alg_bytes"],
