@@ -508,9 +508,7 @@ __global__ void k_sell_fill_half(int64_t n, int64_t nslices, const int64_t* __re
 
 void build_sell_half(mpet_ctx* c, Csr& A) {
     if (!A.s_off || !A.v64 || A.n == 0 || A.nnz == 0) return;
-    const int64_t stored = 0;
-    (void)stored;
-    int64_t nst = 0;
+    int64_t nst = 0;  // stored SELL entries (with padding)
     MPET_CUDA(cudaMemcpyAsync(&nst, A.s_off + A.nslices, sizeof(int64_t), cudaMemcpyDeviceToHost, c->stream));
     TmpBuf bm(sizeof(unsigned long long));
     MPET_CUDA(cudaMemsetAsync(bm.p, 0, sizeof(unsigned long long), c->stream));
