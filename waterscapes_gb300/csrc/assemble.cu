@@ -270,7 +270,7 @@ __global__ void __launch_bounds__(256) k_assemble_matrix(AsmArgs A, MatCoef P) {
             const uint16_t* rk2 = A.rank2 + cell * (NN * NN) + m * NN;
             const uint16_t* rk1 = A.rank1 + cell * (NN * NV) + m * NV;
             // Lane tasks in class-aligned rounds of 32 (a round runs every branch any of its
-            // lanes takes): round 1 the NN*D displacement (node j, row k) tasks; then the
+            // lanes takes): first the NN*D displacement (node j, row k) tasks; then the
             // u-p coupling tasks (u row k with vertex w, and for vertex rows the p rows with
             // node j, component l); then for vertex rows the (network a, vertex w) pressure tasks.
             const int nx = D * NV + (isv ? NN * D : 0);
