@@ -96,6 +96,13 @@ def test_rhs_parity(theta):
     s.ctx.call("mpet_rhs", dt, _lib()._ptr(up), _lib()._ptr(bg))
     torch.cuda.synchronize()
     assert np.allclose(_np(bg), b, rtol=1e-12, atol=1e-13 * np.abs(b).max())
+    # once the matrix is assembled, the pressure rows' -alpha (div u^n, q) term comes from
+    # the system's pressure-row, displacement-column block (an FP64 node-block product)
+    s.ctx.call("mpet_assemble", dt, 1)
+    bm = torch.empty(s.N, dtype=torch.float64, device=s.device)
+    s.ctx.call("mpet_rhs", dt, _lib()._ptr(up), _lib()._ptr(bm))
+    torch.cuda.synchronize()
+    assert np.allclose(_np(bm), b, rtol=1e-12, atol=1e-13 * np.abs(b).max())
 
 
 @pytest.mark.parametrize("precision", ["fp64", "mixed"])

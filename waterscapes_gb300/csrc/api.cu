@@ -286,6 +286,7 @@ int mpet_assemble(mpet_ctx* c, double dt, int32_t apply_bc) {
     refresh_system_copies(c);
     MPET_CUDA(cudaStreamSynchronize(c->stream));
     c->assembled = true;
+    c->bc_cols_zeroed = false;
     c->q_dirty = true;
     c->asm_dt = dt;
     API_END(c)
@@ -864,6 +865,7 @@ int mpet_apply_symmetric(mpet_ctx* c, double* b, const double* xbc) {
     API_BEGIN(c)
     require(c->assembled, MPET_ERR_STATE, "mpet_assemble must come first");
     launch_zero_bc_columns(c, b, xbc);
+    c->bc_cols_zeroed = true;
     convert_values_to_f32(c);
     refresh_system_copies(c);
     MPET_CUDA(cudaStreamSynchronize(c->stream));

@@ -517,7 +517,8 @@ struct RhsArgs {
 //   + dt (1-theta) [K_a (grad p_a^n, grad q) + sum_b S_ab (p_a^n - p_b^n, q)] + dt (g_a, q).
 // ADJ: the pressure rows of B^T lam for the old-state operator B of those
 // rows (no displacement or source term, S transposed).
-template <int D, bool ADJ>
+// DIV = false: without the divergence term (added by rhs_div_from_matrix).
+template <int D, bool ADJ, bool DIV = true>
 __global__ void __launch_bounds__(128) k_rhs_p(RhsArgs A, MatCoef P) {
     constexpr int NV = Simplex<D>::NV, NN = Simplex<D>::NN;
     const int64_t v = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
@@ -534,7 +535,7 @@ __global__ void __launch_bounds__(128) k_rhs_p(RhsArgs A, MatCoef P) {
         load_geo(A.geo, cell, G);
         const double w20 = G.vol * kappa<D>();
         double cp = 0.0;
-        for (int j = 0; j < (ADJ ? 0 : NN); ++j) {
+        for (int j = 0; j < ((ADJ || !DIV) ? 0 : NN); ++j) {
             double g[3], s[3];
             p2_grad_at<D>(G, j, m, g, s);
             const int64_t nj = A.cell_nodes[NN * cell + j];
@@ -898,14 +899,23 @@ void launch_rhs(mpet_ctx* c, double dt, const double* up_prev, double* b) {
     A.dt = dt;
     A.theta = c->prm.theta;
     MatCoef P = make_coef(c, dt);
+    // The MPET form's -alpha_a (div u^n, q_a) equals the system's pressure-row,
+    // displacement-column block applied to u^n (the same coefficient, the same
+    // exact integrals): once the matrix is assembled (and its Dirichlet columns
+    // are intact) it comes from one FP64 node-block product over the pressure
+    // rows instead of every vertex re-deriving its cells' P2 gradients.
+    const bool div_by_matrix = c->dim == 3 && c->prm.formulation == MPET_FORM_MPET && c->assembled &&
+                               !c->bc_cols_zeroed && c->A.nb && c->A.nb->v64 && c->rhs_div_matrix;
     if (c->dim == 2) {
         k_rhs_u<2><<<grid_for(c->nnodes, 128), 128, 0, c->stream>>>(A);
         k_rhs_p<2, false><<<grid_for(c->nv, 128), 128, 0, c->stream>>>(A, P);
     } else {
         k_rhs_u<3><<<grid_for(c->nnodes, 128), 128, 0, c->stream>>>(A);
-        k_rhs_p<3, false><<<grid_for(c->nv, 128), 128, 0, c->stream>>>(A, P);
+        if (div_by_matrix) k_rhs_p<3, false, false><<<grid_for(c->nv, 128), 128, 0, c->stream>>>(A, P);
+        else k_rhs_p<3, false><<<grid_for(c->nv, 128), 128, 0, c->stream>>>(A, P);
     }
     MPET_CHECK_LAUNCH();
+    if (div_by_matrix && !rhs_div_from_matrix(c, up_prev, b)) fail(MPET_ERR_STATE, "divergence term not added");
     launch_facet_rhs(c, dt, up_prev, b);
     launch_bc_vector(c, b);
 }

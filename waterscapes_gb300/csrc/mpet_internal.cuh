@@ -385,6 +385,8 @@ struct mpet_ctx {
     bool elem_tried = false;
     int elem_kernel = 1;          // element blocks of tetrahedra: 1 tensor cores, 0 FP64 CUDA cores
     bool amg_device = true;       // Laplacian-form hierarchies built on the GPU (false: host set-up)
+    bool bc_cols_zeroed = false;  // mpet_apply_symmetric zeroed the Dirichlet columns of A (until the next assembly)
+    bool rhs_div_matrix = true;   // pressure rows' divergence term from the node-block product (test hook: false)
     int32_t* u_perm = nullptr;    // P2 node -> row of the spatially ordered first displacement level
     int32_t* u_iperm = nullptr;   // and back (built once per mesh)
     // last device set-up, summed over its hierarchies (ms): block copy, diagonal +
@@ -539,6 +541,10 @@ void launch_mf_cells(mpet_ctx* c, double dt);
 void setup_network_modes(mpet_ctx* c, double dt);
 void set_instances(mpet_ctx* c, int ninst, const int32_t* vertex_inst_host);
 void launch_rhs(mpet_ctx* c, double dt, const double* up_prev, double* b);
+// b_p += (pressure rows, displacement columns of the assembled system) u: the
+// -alpha_a (div u^n, q_a) term of the right-hand side from the FP64 node-block
+// copy; false when that copy cannot serve (none, or its columns were changed)
+bool rhs_div_from_matrix(mpet_ctx* c, const double* up_prev, double* b);
 void launch_bc_vector(mpet_ctx* c, double* b);
 void launch_set_bc_in_x(mpet_ctx* c, double* x);
 void launch_zero_bc_columns(mpet_ctx* c, double* b, const double* xbc);

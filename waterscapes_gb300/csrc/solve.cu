@@ -583,7 +583,8 @@ __global__ void k_sell_fill(int64_t n, int64_t nslices, const int64_t* __restric
 // SM) and run as one wave of resident blocks (the reduction partials past the grid
 // are written as zeros).
 // OCC (FP32 only): held to 64 registers, 4 resident blocks per SM (variant 9).
-template <typename T, int JM, class Epi, bool UU = false, bool OCC = false>
+// PU: the pressure slices only, their displacement (node) columns only.
+template <typename T, int JM, class Epi, bool UU = false, bool OCC = false, bool PU = false>
 __global__ void __launch_bounds__(256, sizeof(T) == 8 ? 3 : (OCC ? 4 : 1)) k_spmv_nb(int64_t nnodes, int64_t nv, int64_t Nu, int J, int64_t nsu,
                                                  int64_t ns, const NbSlice* __restrict__ sl,
                                                  const int32_t* __restrict__ perm, const int32_t* __restrict__ cols,
@@ -594,7 +595,7 @@ __global__ void __launch_bounds__(256, sizeof(T) == 8 ? 3 : (OCC ? 4 : 1)) k_spm
     const int64_t warp = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) >> 5;
     const int64_t nwarps = ((int64_t)gridDim.x * blockDim.x) >> 5;
     double r0 = 0.0, r1 = 0.0;
-    for (int64_t s = warp; s < ns; s += nwarps) {
+    for (int64_t s = (PU ? nsu : 0) + warp; s < ns; s += nwarps) {
         if (skl && slice_frozen(skl, s, skip)) continue;
         const NbSlice S = sl[s];
         const int32_t* c2 = cols + S.coff + lane;
@@ -659,7 +660,7 @@ __global__ void __launch_bounds__(256, sizeof(T) == 8 ? 3 : (OCC ? 4 : 1)) k_spm
             }
             const T* v1 = v2 + (int64_t)S.w2 * B2 * 32;
             const int B1 = J * J;
-            for (int m = 0; m < S.w1; ++m) {
+            for (int m = 0; m < (PU ? 0 : S.w1); ++m) {
                 const int64_t w = __ldcs(c1 + (int64_t)m * 32);
 #pragma unroll
                 for (int b = 0; b < JM; ++b) {
@@ -1156,6 +1157,42 @@ static void launch_nb(mpet_ctx* c, const NodeBlocks& nb, const T* x, const Epi& 
                                                      nb.cols, v, x, epi, c->partials, skl, c->skip_done);
     MPET_CHECK_LAUNCH();
     c->n_launch++;
+}
+
+// b += the pressure rows' displacement-column products (FP64 right-hand side term)
+struct EpiAddRhs {
+    double* b;
+    static constexpr int kRed = 0;
+    static constexpr bool kSystem = true;
+    struct Pre {};
+    __device__ __forceinline__ Pre pre(int64_t) const { return Pre{}; }
+    __device__ __forceinline__ void apply(int64_t row, const double* acc, const Pre&, double&, double&) const {
+        b[row] += acc[0];
+    }
+};
+
+bool rhs_div_from_matrix(mpet_ctx* c, const double* up_prev, double* b) {
+    if (!c->A.nb || !c->A.nb->v64 || c->dim != 3) return false;
+    const NodeBlocks& nb = *c->A.nb;
+    const int64_t ns = nb.nsu + nb.nsp;
+    int blocks = grid_for(nb.nsp * 32, 256);
+    if (blocks > 152 * 16) blocks = 152 * 16;
+    const int J = c->J;
+    cudaStream_t st = c->stream;
+    if (J <= 2)
+        k_spmv_nb<double, 2, EpiAddRhs, false, false, true><<<blocks, 256, 0, st>>>(
+            c->nnodes, c->nv, c->Nu, J, nb.nsu, ns, nb.sl, nb.perm, nb.cols, nb.v64, up_prev, EpiAddRhs{b},
+            c->partials, nullptr, nullptr);
+    else if (J <= 4)
+        k_spmv_nb<double, 4, EpiAddRhs, false, false, true><<<blocks, 256, 0, st>>>(
+            c->nnodes, c->nv, c->Nu, J, nb.nsu, ns, nb.sl, nb.perm, nb.cols, nb.v64, up_prev, EpiAddRhs{b},
+            c->partials, nullptr, nullptr);
+    else
+        k_spmv_nb<double, 8, EpiAddRhs, false, false, true><<<blocks, 256, 0, st>>>(
+            c->nnodes, c->nv, c->Nu, J, nb.nsu, ns, nb.sl, nb.perm, nb.cols, nb.v64, up_prev, EpiAddRhs{b},
+            c->partials, nullptr, nullptr);
+    MPET_CHECK_LAUNCH();
+    return true;
 }
 
 // displacement block of the node-block system copy: u slices only, no vertex columns
